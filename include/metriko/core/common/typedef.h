@@ -1,0 +1,234 @@
+//
+// metriko-gb300: minimal dense/sparse containers behind the reference's type names.
+//
+// The reference spells its host API with Eigen types (include/metriko/core/common/typedef.h:13-40
+// in metriko): complex, Row3d, VecXi/VecXd/VecXc, MatXi/MatXd/MatXc, SprsD/SprsC, TripD/TripC.
+// Eigen is not part of this build, so the same names are provided here with only the
+// operations the field + integration + IGM path needs.  Dense matrices are row-major.
+//
+#ifndef METRIKO_TYPEDEF_H
+#define METRIKO_TYPEDEF_H
+#include <algorithm>
+#include <cassert>
+#include <cmath>
+#include <complex>
+#include <cstdint>
+#include <numeric>
+#include <stdexcept>
+#include <vector>
+
+namespace metriko {
+    constexpr double PI = 3.14159265358979323846;
+    constexpr double TwoPI = 2 * PI;
+    constexpr double EPS = 1e-9;
+    using complex = std::complex<double>;
+
+    // ------------------------------------------------------------------ fixed-size rows
+    struct Row3d {
+        double v[3] = {0, 0, 0};
+        Row3d() = default;
+        Row3d(double a, double b, double c) : v{a, b, c} {}
+        double x() const { return v[0]; }
+        double y() const { return v[1]; }
+        double z() const { return v[2]; }
+        double& operator[](int i) { return v[i]; }
+        double operator[](int i) const { return v[i]; }
+        Row3d operator+(const Row3d& o) const { return {v[0] + o.v[0], v[1] + o.v[1], v[2] + o.v[2]}; }
+        Row3d operator-(const Row3d& o) const { return {v[0] - o.v[0], v[1] - o.v[1], v[2] - o.v[2]}; }
+        Row3d operator-() const { return {-v[0], -v[1], -v[2]}; }
+        Row3d operator*(double s) const { return {v[0] * s, v[1] * s, v[2] * s}; }
+        Row3d operator/(double s) const { return {v[0] / s, v[1] / s, v[2] / s}; }
+        Row3d& operator+=(const Row3d& o) { v[0] += o.v[0]; v[1] += o.v[1]; v[2] += o.v[2]; return *this; }
+        double dot(const Row3d& o) const { return v[0] * o.v[0] + v[1] * o.v[1] + v[2] * o.v[2]; }
+        Row3d cross(const Row3d& o) const {
+            return {v[1] * o.v[2] - v[2] * o.v[1], v[2] * o.v[0] - v[0] * o.v[2], v[0] * o.v[1] - v[1] * o.v[0]};
+        }
+        double squaredNorm() const { return v[0] * v[0] + v[1] * v[1] + v[2] * v[2]; }
+        double norm() const { return std::sqrt(squaredNorm()); }
+        Row3d normalized() const { double n = squaredNorm(); return n > 0 ? *this / std::sqrt(n) : *this; }
+    };
+    inline Row3d operator*(double s, const Row3d& r) { return r * s; }
+    using Vec3d = Row3d;
+
+    // ------------------------------------------------------------------ dense vector
+    template <typename T>
+    struct VecX {
+        std::vector<T> d;
+        VecX() = default;
+        explicit VecX(size_t n, T val = T()) : d(n, val) {}
+        VecX(std::vector<T> v) : d(std::move(v)) {}
+        static VecX Zero(size_t n) { return VecX(n, T(0)); }
+        static VecX Constant(size_t n, T c) { return VecX(n, c); }
+        int size() const { return static_cast<int>(d.size()); }
+        int rows() const { return size(); }
+        void resize(size_t n) { d.resize(n); }
+        void setConstant(T c) { std::fill(d.begin(), d.end(), c); }
+        void setZero() { setConstant(T(0)); }
+        T& operator[](size_t i) { return d[i]; }
+        const T& operator[](size_t i) const { return d[i]; }
+        T& operator()(size_t i) { return d[i]; }
+        const T& operator()(size_t i) const { return d[i]; }
+        T* data() { return d.data(); }
+        const T* data() const { return d.data(); }
+        auto begin() { return d.begin(); }
+        auto end() { return d.end(); }
+        auto begin() const { return d.begin(); }
+        auto end() const { return d.end(); }
+    };
+    using VecXi = VecX<int>;
+    using VecXd = VecX<double>;
+    using VecXc = VecX<complex>;
+    using VecXb = VecX<bool>;
+
+    // ------------------------------------------------------------------ dense matrix (row-major)
+    template <typename T>
+    struct MatX {
+        int r = 0, c = 0;
+        std::vector<T> d;
+        MatX() = default;
+        MatX(int rows, int cols, T val = T()) : r(rows), c(cols), d(size_t(rows) * cols, val) {}
+        static MatX Zero(int rows, int cols) { return MatX(rows, cols, T(0)); }
+        static MatX Constant(int rows, int cols, T v) { return MatX(rows, cols, v); }
+        static MatX Identity(int n, int m) { MatX a(n, m, T(0)); for (int i = 0; i < std::min(n, m); i++) a(i, i) = T(1); return a; }
+        int rows() const { return r; }
+        int cols() const { return c; }
+        void resize(int rows, int cols) { r = rows; c = cols; d.assign(size_t(rows) * cols, T()); }
+        T& operator()(int i, int j) { return d[size_t(i) * c + j]; }
+        const T& operator()(int i, int j) const { return d[size_t(i) * c + j]; }
+        T* row(int i) { return d.data() + size_t(i) * c; }
+        const T* row(int i) const { return d.data() + size_t(i) * c; }
+        T* data() { return d.data(); }
+        const T* data() const { return d.data(); }
+        MatX operator*(const MatX& o) const {
+            MatX out(r, o.c, T(0));
+            for (int i = 0; i < r; i++)
+                for (int k = 0; k < c; k++) {
+                    T a = (*this)(i, k);
+                    if (a == T(0)) continue;
+                    for (int j = 0; j < o.c; j++) out(i, j) += a * o(k, j);
+                }
+            return out;
+        }
+        MatX operator-() const { MatX o(*this); for (auto& x : o.d) x = -x; return o; }
+        MatX& operator+=(const MatX& o) { for (size_t i = 0; i < d.size(); i++) d[i] += o.d[i]; return *this; }
+        MatX& operator-=(const MatX& o) { for (size_t i = 0; i < d.size(); i++) d[i] -= o.d[i]; return *this; }
+        bool isZero() const { for (auto& x : d) if (x != T(0)) return false; return true; }
+    };
+    using MatXi = MatX<int>;
+    using MatXd = MatX<double>;
+    using MatXc = MatX<complex>;
+
+    inline Row3d row3(const MatXd& m, int i) { return {m(i, 0), m(i, 1), m(i, 2)}; }
+    inline void set_row3(MatXd& m, int i, const Row3d& v) { m(i, 0) = v[0]; m(i, 1) = v[1]; m(i, 2) = v[2]; }
+
+    // ------------------------------------------------------------------ sparse (CSR)
+    template <typename T>
+    struct Triplet {
+        int r, c;
+        T v;
+        Triplet(int r_, int c_, T v_) : r(r_), c(c_), v(v_) {}
+        int row() const { return r; }
+        int col() const { return c; }
+        T value() const { return v; }
+    };
+    using TripI = Triplet<int>;
+    using TripD = Triplet<double>;
+    using TripC = Triplet<complex>;
+
+    // Compressed sparse rows with sorted, unique column indices.
+    template <typename T>
+    struct Sprs {
+        int nr = 0, nc = 0;
+        std::vector<int> ptr{0}, idx;
+        std::vector<T> val;
+        Sprs() = default;
+        Sprs(int rows, int cols) : nr(rows), nc(cols), ptr(rows + 1, 0) {}
+        int rows() const { return nr; }
+        int cols() const { return nc; }
+        int nonZeros() const { return static_cast<int>(idx.size()); }
+        void resize(int rows, int cols) { nr = rows; nc = cols; ptr.assign(rows + 1, 0); idx.clear(); val.clear(); }
+
+        // Duplicates are summed (Eigen setFromTriplets semantics).
+        template <typename It>
+        void setFromTriplets(It b, It e) {
+            ptr.assign(nr + 1, 0);
+            size_t n = 0;
+            for (It it = b; it != e; ++it) { ptr[it->r + 1]++; n++; }
+            for (int i = 0; i < nr; i++) ptr[i + 1] += ptr[i];
+            std::vector<int> ci(n);
+            std::vector<T> cv(n);
+            std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+            for (It it = b; it != e; ++it) { int p = fill[it->r]++; ci[p] = it->c; cv[p] = it->v; }
+            idx.clear(); val.clear();
+            std::vector<int> nptr(nr + 1, 0);
+            std::vector<std::pair<int, T>> rowbuf;
+            for (int i = 0; i < nr; i++) {
+                rowbuf.clear();
+                for (int p = ptr[i]; p < ptr[i + 1]; p++) rowbuf.emplace_back(ci[p], cv[p]);
+                std::stable_sort(rowbuf.begin(), rowbuf.end(), [](auto& a, auto& b2) { return a.first < b2.first; });
+                for (size_t k = 0; k < rowbuf.size(); k++) {
+                    if (!idx.empty() && int(idx.size()) > nptr[i] && idx.back() == rowbuf[k].first) val.back() += rowbuf[k].second;
+                    else { idx.push_back(rowbuf[k].first); val.push_back(rowbuf[k].second); }
+                }
+                nptr[i + 1] = static_cast<int>(idx.size());
+            }
+            ptr = std::move(nptr);
+        }
+        // Removes entries with |v| <= |reference| * epsilon (Eigen prune semantics).
+        void prune(double reference, double epsilon = 1e-12) {
+            std::vector<int> np(nr + 1, 0), ni;
+            std::vector<T> nv;
+            for (int i = 0; i < nr; i++) {
+                for (int p = ptr[i]; p < ptr[i + 1]; p++)
+                    if (std::abs(val[p]) > std::abs(reference) * epsilon) { ni.push_back(idx[p]); nv.push_back(val[p]); }
+                np[i + 1] = static_cast<int>(ni.size());
+            }
+            ptr = std::move(np); idx = std::move(ni); val = std::move(nv);
+        }
+        std::vector<T> operator*(const std::vector<T>& x) const {
+            std::vector<T> y(nr, T(0));
+            for (int i = 0; i < nr; i++) {
+                T s(0);
+                for (int p = ptr[i]; p < ptr[i + 1]; p++) s += val[p] * x[idx[p]];
+                y[i] = s;
+            }
+            return y;
+        }
+        VecX<T> operator*(const VecX<T>& x) const { return VecX<T>((*this) * x.d); }
+        Sprs transpose() const {
+            std::vector<Triplet<T>> t;
+            t.reserve(idx.size());
+            for (int i = 0; i < nr; i++) for (int p = ptr[i]; p < ptr[i + 1]; p++) t.emplace_back(idx[p], i, val[p]);
+            Sprs o(nc, nr);
+            o.setFromTriplets(t.begin(), t.end());
+            return o;
+        }
+        Sprs operator*(const Sprs& B) const {
+            if (nc != B.nr) throw std::invalid_argument("sparse product: size mismatch");
+            Sprs C(nr, B.nc);
+            std::vector<T> acc(B.nc, T(0));
+            std::vector<char> used(B.nc, 0);
+            std::vector<int> cols;
+            for (int i = 0; i < nr; i++) {
+                cols.clear();
+                for (int p = ptr[i]; p < ptr[i + 1]; p++) {
+                    int k = idx[p];
+                    for (int q = B.ptr[k]; q < B.ptr[k + 1]; q++) {
+                        int j = B.idx[q];
+                        if (!used[j]) { used[j] = 1; cols.push_back(j); acc[j] = T(0); }
+                        acc[j] += val[p] * B.val[q];
+                    }
+                }
+                std::sort(cols.begin(), cols.end());
+                for (int j : cols) { C.idx.push_back(j); C.val.push_back(acc[j]); used[j] = 0; }
+                C.ptr[i + 1] = static_cast<int>(C.idx.size());
+            }
+            return C;
+        }
+    };
+    using SprsI = Sprs<int>;
+    using SprsD = Sprs<double>;
+    using SprsC = Sprs<complex>;
+}
+
+#endif

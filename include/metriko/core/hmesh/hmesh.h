@@ -1,0 +1,294 @@
+//
+// metriko-gb300: halfedge mesh (DCEL) with the reference's numbering.
+//
+// Replaces metriko include/metriko/core/hmesh/hmesh.h:24-611 (struct Hmesh, handles, dcel()).
+// Only closed, consistently oriented, edge-manifold triangle meshes are accepted (the
+// workloads of this path); anything else throws std::invalid_argument.
+//
+// Numbering follows the reference exactly, because every later integer decision depends on it:
+//  * edges: libigl v2.5.0 edge_topology -- entries (min v, max v, face, corner) sorted
+//    lexicographically, one edge per distinct (min, max); edge2face(e,0) is the face in which
+//    the edge runs min->max (restated from libigl's documented behaviour);
+//  * halfedge 2e starts at edge2vert(e,0) inside edge2face(e,0), 2e+1 is its twin;
+//  * vert2half[v] is the last halfedge written for v in edge order (hmesh.h:313-323);
+//  * face2half[f] runs F(f,0)->F(f,1) (hmesh.h:421).
+//
+#ifndef METRIKO_HMESH_H
+#define METRIKO_HMESH_H
+#include "metriko/core/common/typedef.h"
+
+namespace metriko {
+    struct Hmesh;
+    struct Half; struct Vert; struct Edge; struct Face;
+
+    struct Elem {
+        int id;
+        const Hmesh* m;
+        bool operator==(const Elem& rhs) const { return id == rhs.id; }
+    };
+
+    template <typename N> struct AdjIter;
+    struct AdjVH; struct AdjFH;
+
+    struct Face : Elem {
+        Half half() const;
+        Row3d basisX() const;
+        Row3d basisY() const;
+        Row3d normal() const;
+        Row3d center() const;
+        double area() const;
+        AdjIter<AdjFH> adjHalfs(bool ccw = true) const;
+    };
+    struct Edge : Elem {
+        Half half() const;
+        Vert vert0() const;
+        Vert vert1() const;
+        Face face0() const;
+        Face face1() const;
+        bool isBoundary() const { return false; }
+    };
+    struct Vert : Elem {
+        Half half() const;
+        Row3d pos() const;
+        bool isBoundary() const { return false; }
+        bool isInterior() const { return true; }
+        AdjIter<AdjVH> adjHalfs(bool ccw = true) const;
+        AdjIter<AdjVH> adjHalfs(Half h, bool ccw = true) const;
+    };
+    struct Half : Elem {
+        Half next() const;
+        Half prev() const;
+        Half twin() const;
+        Vert tail() const;
+        Vert head() const;
+        Edge edge() const;
+        Face face() const;
+        double farg() const;
+        double len() const { return vec().norm(); }
+        bool isBoundary() const { return false; }
+        bool isCanonical() const;
+        Row3d vec() const;
+    };
+
+    struct Hmesh {
+        int nV = 0, nF = 0, nE = 0, nH = 0, nL = 0, nC = 0, nEularChars = 0;
+        std::vector<int> vert2half, edge2half, face2half, crnr2half;
+        std::vector<int> next, prev, twin, tail, head, edge, face, crnr;
+        std::vector<Half> halfs;
+        std::vector<Vert> verts;
+        std::vector<Edge> edges;
+        std::vector<Face> faces;
+        MatXd pos;
+        MatXi idx;
+        MatXi edge2vert;   // nE x 2
+        MatXi edge2face;   // nE x 2
+        MatXi face2edge;   // nF x 3, edge of (F(f,j), F(f,j+1))
+        MatXi face2half3;  // nF x 3, halfedge of face f on face2edge(f,j)
+        MatXd faceBasisX, faceBasisY, faceNormal, baryCenter;
+        VecXd faceArea, angleDefect, heArgOnFace;
+
+        Hmesh(const MatXd& V, const MatXi& F);
+        Hmesh(const Hmesh&) = delete;
+        Hmesh& operator=(const Hmesh&) = delete;
+    };
+
+    struct AdjBase {
+        Half h;
+        bool bgn;
+        bool ccw;
+        AdjBase(Half h_, bool c) : h(h_), bgn(false), ccw(c) {}
+        Half operator*() const { return h; }
+        bool operator!=(const AdjBase& a) const { return !bgn || h.id != a.h.id; }
+    };
+    struct AdjVH : AdjBase {
+        AdjVH(const Hmesh* m, int hid, bool c) : AdjBase(Half{{hid, m}}, c) {}
+        AdjVH& operator++() { h = ccw ? h.prev().twin() : h.twin().next(); bgn = true; return *this; }
+    };
+    struct AdjFH : AdjBase {
+        AdjFH(const Hmesh* m, int hid, bool c) : AdjBase(Half{{hid, m}}, c) {}
+        AdjFH& operator++() { h = ccw ? h.next() : h.prev(); bgn = true; return *this; }
+    };
+    template <typename N>
+    struct AdjIter {
+        AdjIter(const Hmesh* m, int iX, bool ccw) : bgnNav(N(m, iX, ccw)), endNav(N(m, iX, ccw)) {}
+        N begin() { return bgnNav; }
+        N end() { return endNav; }
+        N bgnNav, endNav;
+    };
+
+    inline Half Half::next() const { return {{m->next[id], m}}; }
+    inline Half Half::prev() const { return {{m->prev[id], m}}; }
+    inline Half Half::twin() const { return {{m->twin[id], m}}; }
+    inline Vert Half::tail() const { return {{m->tail[id], m}}; }
+    inline Vert Half::head() const { return {{m->head[id], m}}; }
+    inline Edge Half::edge() const { return {{m->edge[id], m}}; }
+    inline Face Half::face() const { return {{m->face[id], m}}; }
+    inline double Half::farg() const { return m->heArgOnFace[id]; }
+    inline bool Half::isCanonical() const { return m->edge2half[m->edge[id]] == id; }
+    inline Row3d Half::vec() const { return row3(m->pos, m->head[id]) - row3(m->pos, m->tail[id]); }
+    inline Half Vert::half() const { return {{m->vert2half[id], m}}; }
+    inline Row3d Vert::pos() const { return row3(m->pos, id); }
+    inline Half Edge::half() const { return {{m->edge2half[id], m}}; }
+    inline Vert Edge::vert0() const { return {{m->edge2vert(id, 0), m}}; }
+    inline Vert Edge::vert1() const { return {{m->edge2vert(id, 1), m}}; }
+    inline Face Edge::face0() const { return {{m->edge2face(id, 0), m}}; }
+    inline Face Edge::face1() const { return {{m->edge2face(id, 1), m}}; }
+    inline Half Face::half() const { return {{m->face2half[id], m}}; }
+    inline Row3d Face::basisX() const { return row3(m->faceBasisX, id); }
+    inline Row3d Face::basisY() const { return row3(m->faceBasisY, id); }
+    inline Row3d Face::normal() const { return row3(m->faceNormal, id); }
+    inline Row3d Face::center() const { return row3(m->baryCenter, id); }
+    inline double Face::area() const { return m->faceArea[id]; }
+    inline AdjIter<AdjFH> Face::adjHalfs(bool ccw) const { return {m, m->face2half[id], ccw}; }
+    inline AdjIter<AdjVH> Vert::adjHalfs(bool ccw) const { return {m, m->vert2half[id], ccw}; }
+    inline AdjIter<AdjVH> Vert::adjHalfs(Half h, bool ccw) const { return {m, h.id, ccw}; }
+
+    // libigl v2.5.0 edge_topology semantics (see file header).  EV: nE x 2, FE: nF x 3, EF: nE x 2.
+    inline void edge_topology(const MatXi& F, int nV, MatXi& EV, MatXi& FE, MatXi& EF) {
+        const int nF = F.rows();
+        struct Ent { int hi, f, i, a; };
+        std::vector<int> cnt(nV + 1, 0);
+        for (int f = 0; f < nF; f++)
+            for (int i = 0; i < 3; i++) {
+                int a = F(f, i), b = F(f, (i + 1) % 3);
+                if (a < 0 || a >= nV || b < 0 || b >= nV || a == b) throw std::invalid_argument("bad face index");
+                cnt[std::min(a, b) + 1]++;
+            }
+        for (int v = 0; v < nV; v++) cnt[v + 1] += cnt[v];
+        std::vector<Ent> ent(size_t(3) * nF);
+        std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+        for (int f = 0; f < nF; f++)
+            for (int i = 0; i < 3; i++) {
+                int a = F(f, i), b = F(f, (i + 1) % 3);
+                ent[fill[std::min(a, b)]++] = {std::max(a, b), f, i, a};
+            }
+        for (int v = 0; v < nV; v++)
+            std::sort(ent.begin() + cnt[v], ent.begin() + cnt[v + 1], [](const Ent& x, const Ent& y) {
+                if (x.hi != y.hi) return x.hi < y.hi;
+                if (x.f != y.f) return x.f < y.f;
+                return x.i < y.i;
+            });
+        int nE = 0;
+        std::vector<int> lo_of(ent.size());
+        for (int v = 0; v < nV; v++) for (int p = cnt[v]; p < cnt[v + 1]; p++) lo_of[p] = v;
+        for (size_t p = 0; p < ent.size(); p++)
+            if (p == 0 || lo_of[p] != lo_of[p - 1] || ent[p].hi != ent[p - 1].hi) nE++;
+        EV = MatXi(nE, 2, -1);
+        EF = MatXi(nE, 2, -1);
+        FE = MatXi(nF, 3, -1);
+        int e = -1;
+        std::vector<int> dir0(nE, 0), count(nE, 0);
+        for (size_t p = 0; p < ent.size(); p++) {
+            bool fresh = p == 0 || lo_of[p] != lo_of[p - 1] || ent[p].hi != ent[p - 1].hi;
+            if (fresh) {
+                e++;
+                EV(e, 0) = lo_of[p];
+                EV(e, 1) = ent[p].hi;
+                EF(e, 0) = ent[p].f;
+                dir0[e] = ent[p].a == lo_of[p];
+            } else {
+                if (count[e] >= 2) throw std::invalid_argument("mesh is not edge-manifold");
+                EF(e, 1) = ent[p].f;
+            }
+            count[e]++;
+            FE(ent[p].f, ent[p].i) = e;
+        }
+        for (int k = 0; k < nE; k++) {
+            if (count[k] != 2) throw std::invalid_argument(count[k] > 2 ? "mesh is not edge-manifold" : "mesh has boundary edges (closed meshes only)");
+            if (!dir0[k]) std::swap(EF(k, 0), EF(k, 1));
+            if (EF(k, 0) == EF(k, 1)) throw std::invalid_argument("degenerate edge");
+        }
+    }
+
+    inline Hmesh::Hmesh(const MatXd& V, const MatXi& F) {
+        if (V.cols() != 3 || F.cols() != 3) throw std::invalid_argument("V and F must have 3 columns");
+        pos = V;
+        idx = F;
+        nV = V.rows();
+        nF = F.rows();
+        edge_topology(F, nV, edge2vert, face2edge, edge2face);
+        nE = edge2vert.rows();
+        nH = 2 * nE;
+        nC = 3 * nF;
+        nEularChars = nV - nE + nF;
+        vert2half.assign(nV, -1);
+        edge2half.resize(nE);
+        face2half.resize(nF);
+        crnr2half.assign(nC, -1);
+        next.assign(nH, -1); prev.assign(nH, -1); twin.resize(nH); tail.resize(nH);
+        head.resize(nH); edge.resize(nH); face.resize(nH); crnr.assign(nH, -1);
+        for (int e = 0; e < nE; e++) {
+            tail[2 * e] = edge2vert(e, 0);
+            tail[2 * e + 1] = edge2vert(e, 1);
+            face[2 * e] = edge2face(e, 0);
+            face[2 * e + 1] = edge2face(e, 1);
+            twin[2 * e] = 2 * e + 1;
+            twin[2 * e + 1] = 2 * e;
+            edge[2 * e] = edge[2 * e + 1] = e;
+            edge2half[e] = 2 * e;
+            vert2half[edge2vert(e, 0)] = 2 * e;       // last write wins (dcel, hmesh.h:314-323)
+            vert2half[edge2vert(e, 1)] = 2 * e + 1;
+        }
+        for (int v = 0; v < nV; v++) if (vert2half[v] < 0) throw std::invalid_argument("isolated vertex");
+        face2half3 = MatXi(nF, 3);
+        for (int f = 0; f < nF; f++)
+            for (int j = 0; j < 3; j++) {
+                int e = face2edge(f, j);
+                face2half3(f, j) = 2 * e + (edge2face(e, 0) == f ? 0 : 1);
+            }
+        for (int f = 0; f < nF; f++) {
+            for (int j = 0; j < 3; j++) {
+                next[face2half3(f, j)] = face2half3(f, (j + 1) % 3);
+                prev[face2half3(f, (j + 1) % 3)] = face2half3(f, j);
+            }
+            face2half[f] = face2half3(f, 0);
+            // corner 3f+it is the halfedge opposite F(f,it) (hmesh.h:471-484)
+            for (int it = 0; it < 3; it++) {
+                int h = face2half3(f, (it + 1) % 3);
+                crnr2half[3 * f + it] = h;
+                crnr[h] = 3 * f + it;
+            }
+        }
+        for (int h = 0; h < nH; h++) head[h] = tail[next[h]];
+        for (int i = 0; i < nF; i++) faces.push_back(Face{{i, this}});
+        for (int i = 0; i < nV; i++) verts.push_back(Vert{{i, this}});
+        for (int i = 0; i < nE; i++) edges.push_back(Edge{{i, this}});
+        for (int i = 0; i < nH; i++) halfs.push_back(Half{{i, this}});
+
+        faceBasisX = MatXd(nF, 3); faceBasisY = MatXd(nF, 3); faceNormal = MatXd(nF, 3); baryCenter = MatXd(nF, 3);
+        faceArea = VecXd(nF); heArgOnFace = VecXd(nH); angleDefect = VecXd(nV);
+        for (int f = 0; f < nF; f++) {
+            Row3d p0 = row3(pos, F(f, 0)), p1 = row3(pos, F(f, 1)), p2 = row3(pos, F(f, 2));
+            Row3d x = p1 - p0;
+            Row3d t = (p0 - p2) * -1;
+            Row3d n = x.cross(t);
+            set_row3(faceBasisX, f, x.normalized());
+            set_row3(faceBasisY, f, (-x.cross(n)).normalized());
+            set_row3(faceNormal, f, n.normalized());
+            set_row3(baryCenter, f, (p0 + p1 + p2) / 3.0);
+            faceArea[f] = n.norm() * 0.5;
+        }
+        for (int f = 0; f < nF; f++) {     // hmesh.h:522-531
+            double sum = 0;
+            Row3d bx = row3(faceBasisX, f);
+            for (int j = 0; j < 3; j++) {
+                Half h{{face2half3(f, j), this}};
+                Row3d v1 = h.vec().normalized();
+                Row3d v2 = h.prev().vec().normalized();
+                if ((v1 - bx).norm() > 1e-10) sum += std::acos(v1.dot(v2));
+                heArgOnFace[h.id] = sum;
+            }
+        }
+        for (int v = 0; v < nV; v++) {     // hmesh.h:599-610
+            double sum = 0;
+            for (Half h : verts[v].adjHalfs()) {
+                Row3d v1 = h.vec().normalized();
+                Row3d v2 = h.prev().twin().vec().normalized();
+                sum += std::acos(v1.dot(v2));
+            }
+            angleDefect[v] = TwoPI - sum;
+        }
+    }
+}
+
+#endif

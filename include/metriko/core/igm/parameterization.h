@@ -1,0 +1,397 @@
+//
+// metriko-gb300: seamless parameterization front-end (RosyParameterization).
+//
+// Replaces metriko include/metriko/core/igm/parameterization.h:11-152,
+// parameterization_setup.ipp:3-170 and parameterization_integ.ipp:3-120.
+//  * setup() is host code with the reference's control flow: transition ids along the seam,
+//    per-halfedge matchings, the vertex+transition -> cut-vertex map (vtrans2cut), the
+//    constraints of non-trivial permutation cycles, uncompress (sign symmetry), fixed,
+//    integer and singular index sets.
+//  * integ() reduces the constraints (matrix_ops.h), builds UFull's kernel block, the target
+//    field and the grid length, and runs naive integration + seamless LM + greedy rounding on
+//    the GPU (mtk_iterative_rounding), then forms nfn and cfn.
+// The cut mesh is a lightweight CutMesh (positions + faces): integ() only uses its indices and
+// per-face geometry, which equals the raw mesh's.
+//
+#ifndef METRIKO_PARAMETERIZATION_H
+#define METRIKO_PARAMETERIZATION_H
+#include <map>
+#include <memory>
+#include <set>
+
+#include "metriko/core/hmesh/hmesh.h"
+#include "metriko/core/igm/iterative_rounding/iter_rounding.h"
+#include "metriko/core/solver/matrix_ops.h"
+
+namespace metriko {
+    struct CutMesh {
+        int nV = 0, nF = 0;
+        MatXd pos;
+        MatXi idx;
+    };
+
+    // parameterization.h:126-152: duplicate every vertex once per seam sector.
+    inline std::unique_ptr<CutMesh> compute_cut_mesh(const Hmesh& m, const std::vector<bool>& seam) {
+        auto cm = std::make_unique<CutMesh>();
+        cm->nF = m.nF;
+        cm->idx = MatXi(m.nF, 3, -1);
+        std::vector<int> cut2raw;
+        for (int v = 0; v < m.nV; v++) {
+            int bgn = m.vert2half[v];
+            {   // first seam halfedge in cw order from v.half()
+                int h0 = bgn, h = h0;
+                do {
+                    if (seam[m.edge[h]]) { bgn = h; break; }
+                    h = m.next[m.twin[h]];
+                } while (h != h0);
+            }
+            int h = bgn;
+            do {
+                if (seam[m.edge[h]] || h == bgn) cut2raw.push_back(v);
+                int f = m.face[h];
+                for (int j = 0; j < 3; j++) if (m.idx(f, j) == v) cm->idx(f, j) = int(cut2raw.size()) - 1;
+                h = m.twin[m.prev[h]];
+            } while (h != bgn);
+        }
+        cm->nV = int(cut2raw.size());
+        cm->pos = MatXd(cm->nV, 3);
+        for (int i = 0; i < cm->nV; i++) for (int k = 0; k < 3; k++) cm->pos(i, k) = m.pos(cut2raw[i], k);
+        return cm;
+    }
+
+    // Host products of integ() handed to the device (mtk_igm_desc points into these buffers).
+    struct IntegSystem {
+        SprsD fullx2Nfunc;
+        std::vector<int> uniqueJ, full2y, w_ptr, w_idx;
+        std::vector<double> F2, w_val, cutV;
+        MatXd USmall;
+        double length = 0;
+        mtk_igm_desc desc{};
+    };
+
+    class RosyParameterization {
+        const Hmesh& raw;
+        const CutMesh& cut;
+        const MatXd& ext;
+        const VecXi& singlars;
+        const VecXi& matching;
+        const std::vector<bool>& seam;
+        double gridscale;
+        int nT = 0;     // transitions
+        int nR = 0;     // raw vertices + transitions
+        int nS = 0;     // inner singular vertices
+    public:
+        int N = 4;
+        int n = 2;
+        SprsD vtrans2cut;
+        SprsD constraint;
+        SprsD uncompress;
+        VecXi he2matching;
+        VecXi he2transidx;
+        VecXi integerIdcs;
+        VecXi singularIdcs;
+        VecXi fixedIdcs;
+        VecXd fixedVals;
+        MatXi lreductor;
+        VecXd fullx;
+        VecXd naivex;        // naive Poisson solution (ni.x0), for diagnostics
+        MatXd nfn;
+        MatXd cfn;
+        std::vector<int> fixOrder, fixVals;   // greedy rounding order (diagnostics)
+        bool verbose = false;
+        bool seamless = false;
+        bool roundSeams = true;
+        bool localInjectivity = false;
+        int nJ = 0, nZ = 0;  // constrained block / kernel dimension (diagnostics)
+
+        RosyParameterization(const Hmesh& raw_, const CutMesh& cut_, const MatXd& ext_, const VecXi& sing_,
+                             const VecXi& matching_, const std::vector<bool>& seam_, const int degree,
+                             const double ratio = 0.02)
+            : raw(raw_), cut(cut_), ext(ext_), singlars(sing_), matching(matching_), seam(seam_), gridscale(ratio) {
+            N = degree;
+            if (N % 2 != 0) throw std::invalid_argument("odd N is not part of this build");
+            n = N / 2;
+            lreductor = MatXi(N, n, 0);
+            for (int i = 0; i < n; i++) { lreductor(i, i) = 1; lreductor(n + i, i) = -1; }
+            fixedVals = VecXd::Zero(n);
+            compute_he2transidx();
+            compute_he2matching();
+            nR = raw.nV + nT;
+            nS = 0;
+            for (int v = 0; v < raw.nV; v++) nS += is_inside_singular(v);
+        }
+
+        int numTransitions() const { return nT; }
+        int numSingular() const { return nS; }
+
+        void setup();
+        void build_system(IntegSystem& sys);   // host part of integ()
+        bool integ();
+
+    private:
+        bool is_inside_singular(int v) const { return singlars[v] != 0; }
+        int first_seam_he(int v) const {
+            int h0 = raw.vert2half[v], h = h0;
+            do {
+                if (seam[raw.edge[h]]) return h;
+                h = raw.next[raw.twin[h]];
+            } while (h != h0);
+            return h0;
+        }
+
+        // parameterization_setup.ipp:3-8
+        void compute_he2matching() {
+            he2matching = VecXi(raw.nH);
+            for (int h = 0; h < raw.nH; h++) {
+                int m = (raw.edge2half[raw.edge[h]] == h ? -1 : 1) * matching[raw.edge[h]];
+                he2matching[h] = m < 0 ? (N + m % N) % N : m % N;
+            }
+        }
+
+        // parameterization_setup.ipp:10-49
+        void compute_he2transidx() {
+            he2transidx = VecXi(raw.nH, 32767);
+            std::vector<int> valence(raw.nV, 0);
+            std::vector<char> claimed(raw.nE, 0);
+            for (int e = 0; e < raw.nE; e++)
+                if (seam[e]) { valence[raw.edge2vert(e, 0)]++; valence[raw.edge2vert(e, 1)]++; }
+            int tid = 1;
+            for (int v = 0; v < raw.nV; v++) {
+                if ((valence[v] == 2 && !is_inside_singular(v)) || valence[v] == 0) continue;
+                int h0 = raw.vert2half[v], cH = h0;
+                do {
+                    int cE = raw.edge[cH];
+                    if (seam[cE] && !claimed[cE]) {
+                        he2transidx[cH] = tid;
+                        he2transidx[raw.twin[cH]] = -tid;
+                        claimed[cE] = 1;
+                        int jv = raw.head[cH];
+                        while (valence[jv] == 2 && !is_inside_singular(jv)) {
+                            int nh = -1, g0 = raw.vert2half[jv], g = g0;
+                            do {
+                                if (seam[raw.edge[g]] && !claimed[raw.edge[g]]) { nh = g; break; }
+                                g = raw.twin[raw.prev[g]];
+                            } while (g != g0);
+                            if (nh < 0) throw std::runtime_error("seam tracing failed");
+                            he2transidx[nh] = tid;
+                            he2transidx[raw.twin[nh]] = -tid;
+                            claimed[raw.edge[nh]] = 1;
+                            jv = raw.head[nh];
+                        }
+                        tid++;
+                    }
+                    cH = raw.twin[raw.prev[cH]];
+                } while (cH != h0);
+            }
+            nT = tid - 1;
+        }
+    };
+
+    inline void RosyParameterization::setup() {
+        // cyclic permutation group (setup.ipp:55-61)
+        std::vector<MatXi> perms(N);
+        MatXi unit = MatXi::Zero(N, N);
+        for (int i = 0; i < N; i++) unit((i + 1) % N, i) = 1;
+        perms[0] = MatXi::Identity(N, N);
+        for (int i = 1; i < N; i++) perms[i] = unit * perms[i - 1];
+        const MatXi I = MatXi::Identity(N, N);
+        std::vector<TripD> vT, cT;
+        auto block = [&](std::vector<TripD>& T, const MatXi& mat, int r0, int c0) {
+            for (int i = 0; i < mat.rows(); i++)
+                for (int j = 0; j < mat.cols(); j++)
+                    if (mat(i, j) != 0) T.emplace_back(r0 + i, c0 + j, double(mat(i, j)));
+        };
+        int currConstraint = 0;
+        for (int v = 0; v < raw.nV; v++) {       // setup.ipp:66-124
+            std::vector<MatXi> pm{I};
+            std::vector<int> pidx{v};
+            int iVcut = -1;
+            const int h0 = first_seam_he(v);
+            int h = h0;
+            do {
+                int f = raw.face[h];
+                int jVcut = -1;
+                for (int j = 0; j < 3; j++) if (raw.idx(f, j) == v) jVcut = cut.idx(f, j);
+                if (jVcut != iVcut) {
+                    iVcut = jVcut;
+                    for (size_t i = 0; i < pidx.size(); i++) block(vT, pm[i], N * iVcut, N * pidx[i]);
+                }
+                int hn = raw.twin[raw.prev[h]];
+                if (seam[raw.edge[hn]]) {
+                    const MatXi& p = perms[he2matching[hn]];
+                    int t = he2transidx[hn];
+                    if (t > 0) {
+                        for (auto& mm : pm) mm = p * mm;
+                        pm.push_back(I);
+                        pidx.push_back(raw.nV + t - 1);
+                    } else {
+                        pm.push_back(-I);
+                        pidx.push_back(raw.nV - t - 1);
+                        for (auto& mm : pm) mm = p * mm;
+                    }
+                }
+                h = hn;
+            } while (h != h0);
+            std::set<int> uniq(pidx.begin(), pidx.end());
+            std::vector<int> idcs(uniq.begin(), uniq.end());
+            std::vector<MatXi> mats(idcs.size());
+            bool any = false;
+            for (size_t j = 0; j < idcs.size(); j++) {
+                mats[j] = MatXi::Zero(N, N);
+                for (size_t k = 0; k < pidx.size(); k++) if (idcs[j] == pidx[k]) mats[j] += pm[k];
+                if (idcs[j] == v) mats[j] -= I;
+                if (!mats[j].isZero()) any = true;
+            }
+            if (any) {
+                for (size_t j = 0; j < mats.size(); j++) block(cT, mats[j], N * currConstraint, N * idcs[j]);
+                currConstraint++;
+            }
+        }
+        vtrans2cut = SprsD(N * cut.nV, N * nR);
+        vtrans2cut.setFromTriplets(vT.begin(), vT.end());
+        vtrans2cut.prune(1e-3);
+        constraint = SprsD(N * currConstraint, N * nR);
+        constraint.setFromTriplets(cT.begin(), cT.end());
+        constraint.prune(1e-3);
+        std::vector<TripD> buff;
+        for (int i = 0; i < N * nR; i += N)
+            for (int a = 0; a < N; a++)
+                for (int b = 0; b < n; b++)
+                    if (lreductor(a, b) != 0) buff.emplace_back(i + a, i * n / N + b, double(lreductor(a, b)));
+        uncompress = SprsD(N * nR, n * nR);
+        uncompress.setFromTriplets(buff.begin(), buff.end());
+
+        fixedIdcs = VecXi(n);
+        if (nS == 0) {
+            for (int j = 0; j < n; j++) fixedIdcs[j] = j;
+        } else {
+            int iV = 0;
+            for (iV = 0; iV < raw.nV; iV++) if (is_inside_singular(iV)) break;
+            for (int j = 0; j < n; j++) fixedIdcs[j] = n * iV + j;
+        }
+        integerIdcs = VecXi(nT * n);
+        for (int i = 0; i < nT; i++) for (int j = 0; j < n; j++) integerIdcs[n * i + j] = n * (raw.nV + i) + j;
+        singularIdcs = VecXi(n * nS);
+        int c = 0;
+        for (int v = 0; v < raw.nV; v++)
+            if (is_inside_singular(v)) for (int j = 0; j < n; j++) singularIdcs[c++] = n * v + j;
+    }
+
+    inline void RosyParameterization::build_system(IntegSystem& sys) {
+        SprsD& fullx2Nfunc = sys.fullx2Nfunc;
+        fullx2Nfunc = vtrans2cut * uncompress;
+        SprsD Cfull = constraint * uncompress;     // structural zeros kept (Eigen product semantics)
+        reduce_to_linearly_independent(Cfull);
+        const int nFull = n * nR;
+
+        // ---- UFull = permutation * blockdiag(I, kernel(CSmall))  (iter_rounding_init.h:195-251)
+        std::vector<int>& uniqueJ = sys.uniqueJ;
+        uniqueJ.clear();
+        {
+            std::vector<char> used(nFull, 0);
+            for (int p = 0; p < Cfull.nonZeros(); p++) used[Cfull.idx[p]] = 1;
+            for (int i = 0; i < nFull; i++) if (used[i]) uniqueJ.push_back(i);
+        }
+        std::vector<int>& full2y = sys.full2y;
+        full2y.assign(nFull, -1);
+        MatXd& USmall = sys.USmall;
+        USmall = MatXd();
+        if (Cfull.rows() == 0) {
+            uniqueJ.clear();
+            for (int i = 0; i < nFull; i++) full2y[i] = i;
+        } else {
+            std::vector<int> slot(nFull, -1);
+            for (size_t s = 0; s < uniqueJ.size(); s++) slot[uniqueJ[s]] = int(s);
+            MatXd CSmall(Cfull.rows(), int(uniqueJ.size()), 0.0);
+            for (int i = 0; i < Cfull.rows(); i++)
+                for (int p = Cfull.ptr[i]; p < Cfull.ptr[i + 1]; p++) CSmall(i, slot[Cfull.idx[p]]) = Cfull.val[p];
+            USmall = fullpiv_kernel(CSmall);
+            int y = 0;
+            for (int i = 0; i < nFull; i++) if (slot[i] < 0) full2y[i] = y++;
+        }
+        nJ = int(uniqueJ.size());
+        nZ = USmall.cols();
+
+        // ---- target field (integ.ipp:30-43) and grid length (:70)
+        double norm = 0;
+        for (int f = 0; f < cut.nF; f++)
+            for (int j = 0; j < N; j++) {
+                double s = 0;
+                for (int k = 0; k < 3; k++) s += ext(f, 3 * j + k) * ext(f, 3 * j + k);
+                norm += std::sqrt(s);
+            }
+        norm /= double(N) * cut.nF;
+        std::vector<double>& F2 = sys.F2;
+        F2.assign(2 * size_t(N) * cut.nF, 0.0);
+        for (int f = 0; f < cut.nF; f++)
+            for (int i = 0; i < N; i++) {
+                double sx = 0, sy = 0;
+                for (int k = 0; k < 3; k++) {
+                    sx += ext(f, 3 * i + k) * raw.faceBasisX(f, k);
+                    sy += ext(f, 3 * i + k) * raw.faceBasisY(f, k);
+                }
+                F2[2 * N * f + 2 * i] = sx;
+                F2[2 * N * f + 2 * i + 1] = sy;
+            }
+        double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
+        for (int i = 0; i < cut.nV; i++)
+            for (int k = 0; k < 3; k++) { mn[k] = std::min(mn[k], cut.pos(i, k)); mx[k] = std::max(mx[k], cut.pos(i, k)); }
+        double bb = std::sqrt((mx[0] - mn[0]) * (mx[0] - mn[0]) + (mx[1] - mn[1]) * (mx[1] - mn[1]) + (mx[2] - mn[2]) * (mx[2] - mn[2]));
+        const double length = bb * gridscale / norm;
+        sys.length = length;
+
+        // ---- W = rows k < n of fullx2Nfunc (rows k >= n are their negatives)
+        std::vector<int>& w_ptr = sys.w_ptr;
+        std::vector<int>& w_idx = sys.w_idx;
+        std::vector<double>& w_val = sys.w_val;
+        w_ptr.assign(n * size_t(cut.nV) + 1, 0);
+        w_idx.clear();
+        w_val.clear();
+        for (int c = 0; c < cut.nV; c++)
+            for (int k = 0; k < n; k++) {
+                int r = N * c + k;
+                for (int p = fullx2Nfunc.ptr[r]; p < fullx2Nfunc.ptr[r + 1]; p++) {
+                    if (fullx2Nfunc.val[p] == 0) continue;
+                    w_idx.push_back(fullx2Nfunc.idx[p]);
+                    w_val.push_back(fullx2Nfunc.val[p]);
+                }
+                w_ptr[n * c + k + 1] = int(w_idx.size());
+            }
+        std::vector<double>& cutV = sys.cutV;
+        cutV.assign(3 * size_t(cut.nV), 0.0);
+        for (int i = 0; i < cut.nV; i++) for (int k = 0; k < 3; k++) cutV[3 * i + k] = cut.pos(i, k);
+
+        mtk_igm_desc& d = sys.desc;
+        d = mtk_igm_desc{};
+        d.nF = cut.nF; d.nCut = cut.nV; d.N = N; d.n = n;
+        d.cutF = cut.idx.data(); d.cutV = cutV.data();
+        d.w_ptr = w_ptr.data(); d.w_idx = w_idx.data(); d.w_val = w_val.data();
+        d.nFull = nFull; d.full2y = full2y.data();
+        d.nJ = nJ; d.nZ = nZ; d.uniqueJ = uniqueJ.data(); d.USmall = USmall.data();
+        d.F2 = F2.data(); d.length = length;
+        d.nFixed = fixedIdcs.size(); d.fixedIdcs = fixedIdcs.data(); d.fixedVals = fixedVals.data();
+        d.nSingular = singularIdcs.size(); d.singularIdcs = singularIdcs.data();
+        d.nInteger = integerIdcs.size(); d.integerIdcs = integerIdcs.data();
+        d.seamless = seamless; d.roundSeams = roundSeams;
+        if (localInjectivity) throw std::invalid_argument("localInjectivity is not part of this build");
+    }
+
+    inline bool RosyParameterization::integ() {
+        IntegSystem sys;
+        build_system(sys);
+        const SprsD& fullx2Nfunc = sys.fullx2Nfunc;
+        bool success = iterative_rounding(sys.desc, fullx, naivex, fixOrder, fixVals);
+
+        // ---- nfn (cut vertex x N) and cfn (face x 3N)  (integ.ipp:88-98)
+        std::vector<double> NF = fullx2Nfunc * fullx.d;
+        nfn = MatXd(cut.nV, N);
+        for (int i = 0; i < cut.nV; i++) for (int k = 0; k < N; k++) nfn(i, k) = NF[N * size_t(i) + k];
+        cfn = MatXd(raw.nF, 3 * N);
+        for (int f = 0; f < raw.nF; f++)
+            for (int j = 0; j < 3; j++)
+                for (int k = 0; k < N; k++) cfn(f, N * j + k) = nfn(cut.idx(f, j), k);
+        return success;
+    }
+}
+
+#endif

@@ -1,0 +1,398 @@
+//
+// metriko-gb300: face-based N-RoSy field, matching, singularities, seams, combing.
+//
+// Replaces metriko include/metriko/core/vectorfield/face_rosy_field.h:16-386.
+//  * The smoothest field (connectionLaplacian + galerkinMassMatrix + solveSmallestEig, :43-110)
+//    is computed on the GPU by mtk_field_smoothest (assembly, PCG inverse iteration).
+//  * Matching, singularities, seams, combing and the extrinsic field are host algorithms with
+//    integer outputs; they follow the reference's control flow and tie-breaking exactly.
+//  * The seam builder restates libigl v2.5.0 cut_mesh_from_singularities (flood fill from
+//    face 0, then leaf retraction scanning faces in order, at most 10001 passes) and
+//    dijkstra (unit weights, pops ordered by (distance, vertex id)).
+//  * The power iteration starts from mtk_seeded_init(nF, options().seed) instead of
+//    VecXc::Random.
+//
+#ifndef METRIKO_FACE_ROSY_FIELD_H
+#define METRIKO_FACE_ROSY_FIELD_H
+#include <deque>
+#include <functional>
+#include <memory>
+#include <queue>
+#include <set>
+
+#include "base_field.h"
+#include "metriko/gpu/device.h"
+
+namespace metriko {
+    class FaceRosyField : public BaseVectorField {
+    public:
+        FaceRosyField(const Hmesh& m, const int nRosy) : BaseVectorField(m, nRosy) {}
+        FaceRosyField(const Hmesh& m, const int nRosy, FieldType type, const VecXc* start = nullptr)
+            : BaseVectorField(m, nRosy) {
+            switch (type) {
+                case FieldType::Smoothest: compressed = solveSmoothest(start); break;
+                case FieldType::CurvatureAligned:
+                    throw std::invalid_argument("FieldType::CurvatureAligned is not part of this build");
+                default: break;
+            }
+            if (compressed.size() == m.nF) set_field_from_compressed();
+        }
+
+        // face_rosy_field.h:63-69: field(f,i) = pow(polar(1, arg c_f), 1/N) * pow(r, i)
+        void set_field_from_compressed() {
+            const complex r = std::polar(1., TwoPI / rosyN);
+            field = MatXc(mesh.nF, rosyN);
+            for (int f = 0; f < mesh.nF; f++) {
+                complex root = std::exp(std::log(std::polar(1., std::arg(compressed[f]))) * (1. / rosyN));
+                for (int i = 0; i < rosyN; i++) field(f, i) = root * (i ? std::exp(double(i) * std::log(r)) : complex(1, 0));
+            }
+        }
+
+        // Inputs of the device assembly: neighbour across each face halfedge and
+        // theta = farg(h) - farg(twin h); L(f, nbr) = -(-e^{i theta})^N (face_rosy_field.h:78-96).
+        void assembly_inputs(std::vector<int>& nbr, std::vector<double>& theta) const {
+            nbr.resize(3 * size_t(mesh.nF));
+            theta.resize(3 * size_t(mesh.nF));
+            for (int f = 0; f < mesh.nF; f++)
+                for (int j = 0; j < 3; j++) {
+                    int h = mesh.face2half3(f, j), t = mesh.twin[h];
+                    nbr[3 * f + j] = mesh.face[t];
+                    theta[3 * f + j] = mesh.heArgOnFace[h] - mesh.heArgOnFace[t];
+                }
+        }
+
+        VecXc solveSmoothest(const VecXc* start, int nIter = -1) {
+            if (nIter < 0) nIter = gpu::options().n_iter;
+            std::vector<int> nbr;
+            std::vector<double> theta;
+            assembly_inputs(nbr, theta);
+            std::vector<double> x0(2 * size_t(mesh.nF));
+            if (start) {
+                if (start->size() != mesh.nF) throw std::invalid_argument("start vector size");
+                for (int f = 0; f < mesh.nF; f++) { x0[2 * f] = (*start)[f].real(); x0[2 * f + 1] = (*start)[f].imag(); }
+            } else {
+                mtk_seeded_init(mesh.nF, gpu::options().seed, x0.data());
+            }
+            std::vector<double> out(2 * size_t(mesh.nF));
+            gpu::check(mtk_field_smoothest(gpu::context(), mesh.nF, rosyN, nbr.data(), theta.data(), mesh.faceArea.data(),
+                                           x0.data(), nIter, &gpu::options().solve, out.data(), &gpu::stats()),
+                       "mtk_field_smoothest");
+            VecXc c(mesh.nF);
+            for (int f = 0; f < mesh.nF; f++) c[f] = complex(out[2 * f], out[2 * f + 1]);
+            return c;
+        }
+
+        void computeConnection() {      // face_rosy_field.h:135-143
+            connection = VecXc(mesh.nE, complex(0, 0));
+            for (int e = 0; e < mesh.nE; e++) {
+                Row3d v = Half{{mesh.edge2half[e], &mesh}}.vec().normalized();
+                int f0 = mesh.edge2face(e, 0), f1 = mesh.edge2face(e, 1);
+                complex ef(v.dot(row3(mesh.faceBasisX, f0)), v.dot(row3(mesh.faceBasisY, f0)));
+                complex eg(v.dot(row3(mesh.faceBasisX, f1)), v.dot(row3(mesh.faceBasisY, f1)));
+                connection[e] = eg / ef;
+            }
+        }
+
+        void computeSingular(const VecXd& effort) {   // face_rosy_field.h:126-133
+            singular = VecXi(mesh.nV, 1);
+            for (int v = 0; v < mesh.nV; v++) {
+                double sum = mesh.angleDefect[v] * rosyN;
+                int h0 = mesh.vert2half[v], h = h0;
+                do {
+                    sum += (mesh.edge2half[mesh.edge[h]] == h ? -1 : 1) * effort[mesh.edge[h]];
+                    h = mesh.twin[mesh.prev[h]];
+                } while (h != h0);
+                singular[v] = static_cast<int>(std::round(sum / TwoPI));
+            }
+        }
+
+        void computeMatching(const MatchingType type) {   // face_rosy_field.h:145-161
+            computeConnection();
+            matching = VecXi(mesh.nE, -1);
+            VecXd effort = VecXd::Zero(mesh.nE);
+            if (type == MatchingType::Principal) pMatching(effort);
+            else cMatching(effort);
+            computeSingular(effort);
+        }
+
+    private:
+        void pMatching(VecXd& effort) {    // face_rosy_field.h:164-193
+            for (int e = 0; e < mesh.nE; e++) {
+                int f0 = mesh.edge2face(e, 0), f1 = mesh.edge2face(e, 1);
+                complex conn = connection[e];
+                double minRot = 1000.;
+                int offset = 0;
+                complex coef(1, 0);
+                complex transport0 = conn * field(f0, 0);
+                for (int i = 0; i < rosyN; i++) {
+                    complex jf = field(f0, i), jg = field(f1, i);
+                    coef *= jg / (conn * jf);
+                    double r = std::arg(jg / transport0);
+                    if (std::abs(r) < std::abs(minRot)) { offset = i; minRot = r; }
+                }
+                effort[e] = std::arg(coef);
+                double residuals = 0;
+                for (int i = 0; i < rosyN; i++) residuals += std::arg(field(f1, (i + offset) % rosyN) / (conn * field(f0, i)));
+                matching[e] = offset - static_cast<int>(std::round((residuals - effort[e]) / TwoPI));
+            }
+        }
+
+        void cMatching(VecXd& effort) {    // face_rosy_field.h:195-228
+            for (int e = 0; e < mesh.nE; e++) {
+                int iM = 0;
+                double mn = 32767000.;
+                Row3d v = Half{{mesh.edge2half[e], &mesh}}.vec().normalized();
+                int f0 = mesh.edge2face(e, 0), f1 = mesh.edge2face(e, 1);
+                Row3d bx0 = row3(mesh.faceBasisX, f0), by0 = row3(mesh.faceBasisY, f0);
+                Row3d bx1 = row3(mesh.faceBasisX, f1), by1 = row3(mesh.faceBasisY, f1);
+                for (int i = 0; i < rosyN; i++) {
+                    double curl = 0;
+                    for (int j = 0; j < rosyN; j++) {
+                        complex c0 = field(f0, j), c1 = field(f1, (i + j) % rosyN);
+                        Row3d v0 = bx0 * c0.real() + by0 * c0.imag();
+                        Row3d v1 = bx1 * c1.real() + by1 * c1.imag();
+                        double d = v.dot(v1 - v0);
+                        curl += d * d;
+                    }
+                    if (curl < mn) { iM = i; mn = curl; }
+                }
+                matching[e] = iM;
+                complex coef(1, 0);
+                for (int i = 0; i < rosyN; i++) coef *= field(f1, (i + iM) % rosyN) / (field(f0, i) * connection[e]);
+                effort[e] = std::arg(coef);
+            }
+        }
+    };
+
+    // face_rosy_field.h:233-275
+    inline std::unique_ptr<FaceRosyField> compute_combbed_field(const FaceRosyField& fld, const std::vector<bool>& seam) {
+        const Hmesh& m = fld.mesh;
+        const int N = fld.rosyN;
+        auto F = std::make_unique<FaceRosyField>(m, N);
+        F->field = MatXc(m.nF, N, complex(0, 0));
+        F->connection = fld.connection;
+        F->compressed = fld.compressed;
+        F->singular = fld.singular;
+        std::vector<int> turns(m.nF, 0);
+        std::vector<char> visit(m.nF, 0);
+        std::deque<std::pair<int, int>> q;
+        q.emplace_back(0, 0);
+        while (!q.empty()) {
+            auto [i, mm] = q.front();
+            q.pop_front();
+            if (visit[i]) continue;
+            visit[i] = 1;
+            turns[i] = mm;
+            for (int k = 0; k < N; k++) F->field(i, k) = fld.field(i, (k + mm) % N);
+            for (int j = 0; j < 3; j++) {
+                int e = m.edge[m.face2half3(i, j)];
+                bool b = m.edge2face(e, 0) == i;
+                int fn = b ? m.edge2face(e, 1) : m.edge2face(e, 0);
+                int n = (b ? 1 : -1) * fld.matching[e];
+                n = (n + mm + 1000 * N) % N;
+                if (!visit[fn] && !seam[e]) q.emplace_back(fn, n);
+            }
+        }
+        F->matching = VecXi(m.nE, -1);
+        for (int e = 0; e < m.nE; e++)
+            F->matching[e] = (turns[m.edge2face(e, 0)] - turns[m.edge2face(e, 1)] + fld.matching[e] + 1000 * N) % N;
+        return F;
+    }
+
+    // face_rosy_field.h:277-290 (N = 4)
+    inline MatXd compute_extrinsic_field(const Hmesh& mesh, const FaceRosyField& fld, int rosyN) {
+        MatXd ext(mesh.nF, 3 * rosyN);
+        for (int f = 0; f < mesh.nF; f++) {
+            Row3d bx = row3(mesh.faceBasisX, f), by = row3(mesh.faceBasisY, f);
+            for (int i = 0; i < rosyN; i++) {
+                complex c = fld.field(f, i);
+                Row3d v = (bx * c.real() + by * c.imag()).normalized();
+                for (int k = 0; k < 3; k++) ext(f, 3 * i + k) = v[k];
+            }
+        }
+        return ext;
+    }
+
+    namespace detail {
+        // TT(f,s): face across edge s = (F(f,s), F(f,s+1)); TTi(f,s): that edge's slot in TT(f,s).
+        inline void triangle_adjacency(const Hmesh& m, MatXi& TT, MatXi& TTi) {
+            TT = MatXi(m.nF, 3);
+            TTi = MatXi(m.nF, 3);
+            for (int f = 0; f < m.nF; f++)
+                for (int s = 0; s < 3; s++) {
+                    int t = m.twin[m.face2half3(f, s)];
+                    int g = m.face[t];
+                    TT(f, s) = g;
+                    TTi(f, s) = m.face2half3(g, 0) == t ? 0 : (m.face2half3(g, 1) == t ? 1 : 2);
+                }
+        }
+
+        // libigl cut_mesh_from_singularities with an all-zero matching (see file header).
+        inline MatXi spanning_cut(const Hmesh& m, const MatXi& TT, const MatXi& TTi) {
+            const MatXi& F = m.idx;
+            const int nF = m.nF;
+            MatXi seams(nF, 3, 1);
+            std::vector<char> visited(nF, 0);
+            std::deque<int> dq;
+            for (int f0 = 0; f0 < nF; f0++) {
+                if (visited[f0]) continue;
+                visited[f0] = 1;
+                dq.push_back(f0);
+                while (!dq.empty()) {
+                    int f = dq.front();
+                    dq.pop_front();
+                    for (int s = 0; s < 3; s++) {
+                        int g = TT(f, s), j = TTi(f, s);
+                        if (!visited[g]) {
+                            visited[g] = 1;
+                            seams(f, s) = 0;
+                            seams(g, j) = 0;
+                            dq.push_back(g);
+                        }
+                    }
+                }
+            }
+            // Retract: exact pass-by-pass semantics, event driven.
+            std::vector<int> e(m.nV, 0);
+            for (int f = 0; f < nF; f++)
+                for (int s = 0; s < 3; s++)
+                    if (seams(f, s) && TT(f, s) <= f) { e[F(f, s)]++; e[F(f, (s + 1) % 3)]++; }
+            std::vector<int> vptr(m.nV + 1, 0);
+            for (int f = 0; f < nF; f++)
+                for (int s = 0; s < 3; s++)
+                    if (seams(f, s)) { vptr[F(f, s) + 1]++; vptr[F(f, (s + 1) % 3) + 1]++; }
+            for (int v = 0; v < m.nV; v++) vptr[v + 1] += vptr[v];
+            std::vector<int> vpos(vptr[m.nV]);
+            {
+                std::vector<int> fill(vptr.begin(), vptr.end() - 1);
+                for (int f = 0; f < nF; f++)
+                    for (int s = 0; s < 3; s++)
+                        if (seams(f, s)) { vpos[fill[F(f, s)]++] = 3 * f + s; vpos[fill[F(f, (s + 1) % 3)]++] = 3 * f + s; }
+            }
+            auto leaf_edge = [&](int p) { int f = p / 3, s = p % 3; return e[F(f, s)] == 1 || e[F(f, (s + 1) % 3)] == 1; };
+            std::priority_queue<int, std::vector<int>, std::greater<int>> cur;
+            for (int f = 0; f < nF; f++)
+                for (int s = 0; s < 3; s++)
+                    if (seams(f, s) && leaf_edge(3 * f + s)) cur.push(3 * f + s);
+            std::vector<int> nxt;
+            int guard = 0;
+            while (true) {
+                bool removed = false;
+                int cursor = -1;
+                while (!cur.empty()) {
+                    int p = cur.top();
+                    cur.pop();
+                    if (p <= cursor) continue;
+                    cursor = p;
+                    int f = p / 3, s = p % 3;
+                    if (!seams(f, s)) continue;
+                    int a = F(f, s), b = F(f, (s + 1) % 3);
+                    if (e[a] == 1 || e[b] == 1) {
+                        seams(f, s) = 0;
+                        seams(TT(f, s), TTi(f, s)) = 0;
+                        e[a]--;
+                        e[b]--;
+                        removed = true;
+                        for (int v : {a, b}) {
+                            if (e[v] != 1) continue;
+                            for (int k = vptr[v]; k < vptr[v + 1]; k++) {
+                                int qp = vpos[k];
+                                if (!seams(qp / 3, qp % 3)) continue;
+                                if (qp > p) cur.push(qp);
+                                else nxt.push_back(qp);
+                            }
+                        }
+                    }
+                }
+                guard++;
+                if (!removed || guard > 10000) break;
+                std::sort(nxt.begin(), nxt.end());
+                nxt.erase(std::unique(nxt.begin(), nxt.end()), nxt.end());
+                for (int p : nxt) cur.push(p);
+                nxt.clear();
+            }
+            return seams;
+        }
+    }
+
+    // face_rosy_field.h:294-369 (cut_mesh_with_singularities)
+    inline void cut_mesh_with_singularities(const Hmesh& m, const VecXi& singularities, MatXi& cuts) {
+        const MatXi& F = m.idx;
+        MatXi TT, TTi;
+        detail::triangle_adjacency(m, TT, TTi);
+        cuts = detail::spanning_cut(m, TT, TTi);
+        // vertex -> faces (ascending) and vertex -> vertices (sorted, unique)
+        std::vector<int> fptr(m.nV + 1, 0);
+        for (int f = 0; f < m.nF; f++) for (int j = 0; j < 3; j++) fptr[F(f, j) + 1]++;
+        for (int v = 0; v < m.nV; v++) fptr[v + 1] += fptr[v];
+        std::vector<int> vf(fptr[m.nV]);
+        {
+            std::vector<int> fill(fptr.begin(), fptr.end() - 1);
+            for (int f = 0; f < m.nF; f++) for (int j = 0; j < 3; j++) vf[fill[F(f, j)]++] = f;
+        }
+        std::vector<int> in_cut(m.nV, 0);
+        for (int f = 0; f < m.nF; f++) for (int j = 0; j < 3; j++) if (cuts(f, j)) in_cut[F(f, j)] = 1;
+        std::vector<int> dist(m.nV, -1), prev(m.nV, -1), touched;
+        for (int i = 0; i < singularities.size(); i++) {
+            const int src = singularities[i];
+            // unit-weight Dijkstra; pops ordered by (distance, id)
+            for (int v : touched) { dist[v] = -1; prev[v] = -1; }
+            touched.clear();
+            std::priority_queue<std::pair<int, int>, std::vector<std::pair<int, int>>, std::greater<>> pq;
+            dist[src] = 0;
+            touched.push_back(src);
+            pq.emplace(0, src);
+            int found = -1;
+            while (!pq.empty()) {
+                auto [d, u] = pq.top();
+                pq.pop();
+                if (d > dist[u]) continue;
+                if (in_cut[u]) { found = u; break; }
+                // neighbours of u: the other corners of its faces (order is irrelevant)
+                for (int k = fptr[u]; k < fptr[u + 1]; k++) {
+                    int f = vf[k];
+                    for (int j = 0; j < 3; j++) {
+                        int w = F(f, j);
+                        if (w == u) continue;
+                        if (dist[w] < 0 || d + 1 < dist[w]) {
+                            if (dist[w] < 0) touched.push_back(w);
+                            dist[w] = d + 1;
+                            prev[w] = u;
+                            pq.emplace(d + 1, w);
+                        }
+                    }
+                }
+            }
+            std::vector<int> path;
+            if (found == -1) path.push_back(src);
+            else for (int v = found; v != -1; v = prev[v]) path.push_back(v);
+            for (int v : path) in_cut[v] = 1;
+            for (size_t ii = 0; ii + 1 < path.size(); ii++) {
+                int v0 = path[ii], v1 = path[ii + 1];
+                int fi = -1;
+                for (int k = fptr[v0]; k < fptr[v0 + 1] && fi < 0; k++)
+                    for (int k2 = fptr[v1]; k2 < fptr[v1 + 1]; k2++)
+                        if (vf[k] == vf[k2]) { fi = vf[k]; break; }
+                int j = -1;
+                for (int z = 0; z < 3; z++)
+                    if ((F(fi, z) == v0 && F(fi, (z + 1) % 3) == v1) || (F(fi, z) == v1 && F(fi, (z + 1) % 3) == v0)) j = z;
+                cuts(fi, j) = 1;
+                cuts(TT(fi, j), TTi(fi, j)) = 1;
+            }
+        }
+    }
+
+    // face_rosy_field.h:371-386
+    inline std::vector<bool> compute_seam(const FaceRosyField& f) {
+        std::vector<bool> seam(f.mesh.nE, false);
+        std::vector<int> sv;
+        for (int v = 0; v < f.mesh.nV; v++) if (f.singular[v] != 0) sv.push_back(v);
+        MatXi cuts;
+        cut_mesh_with_singularities(f.mesh, VecXi(sv), cuts);
+        for (int iF = 0; iF < f.mesh.nF; iF++)
+            for (int j = 0; j < 3; j++) if (cuts(iF, j)) seam[f.mesh.face2edge(iF, j)] = true;
+        return seam;
+    }
+}
+
+#endif

@@ -1,0 +1,197 @@
+/*
+ * metriko-gb300 C ABI: the drop-in boundary between the header-only C++ host code
+ * (include/metriko/...) and the sm_103a CUDA kernels in libmetriko_cuda.so.
+ *
+ * Every function returns an int status (MTK_OK on success).  Pointers are plain host
+ * pointers unless a parameter says otherwise; no C++ or torch types cross this boundary.
+ * Each context owns one CUDA device and one stream; calls on one context are not re-entrant.
+ *
+ * Reference interfaces replaced (paths inside the metriko project):
+ *   mtk_field_smoothest   <- FaceRosyField(const Hmesh&, int, FieldType::Smoothest)
+ *                            (include/metriko/core/vectorfield/face_rosy_field.h:43-49) with
+ *                            connectionLaplacian (:72-102), galerkinMassMatrix (:104-110) and
+ *                            solveSmallestEig(SprsC&, SprsC&, int nIter = 50)
+ *                            (include/metriko/core/solver/sparse_linear_solver.h:452-477)
+ *   mtk_iterative_rounding <- iterative_rounding(fixedIdcs, fixedVals, singularIdcs,
+ *                            integerIdcs, length, Cfull, G2, N, n, nF, seamless, roundSeams,
+ *                            localInjectivity, verbose, intrinsicField, iter_cb, fullx)
+ *                            (include/metriko/core/igm/iterative_rounding/iter_rounding.h:33-113)
+ *                            including NaiveIntegration (iter_rounding_init.h:16-233),
+ *                            SeamlessIntegration (iter_rounding_loop.h:10-125) and the
+ *                            LMSolver/CholeskyWrapper linear-solver seam
+ *                            (include/metriko/core/solver/levenberg_marquardt.h:140-231,
+ *                            iter_rounding.h:14-31)
+ *   mtk_topology_from_field <- the host stages of the same sequence for a given field
+ *                            (face_rosy_field.h:126-386, parameterization.h:43-152,
+ *                            parameterization_setup.ipp:3-170, parameterization_integ.ipp:3-70)
+ *   mtk_pipeline_run      <- the example_igm.cpp:13-31 call sequence (Hmesh -> field ->
+ *                            matching -> seam -> cut -> combing -> RosyParameterization
+ *                            setup()/integ()) as one call with host buffers
+ */
+#ifndef METRIKO_CUDA_H
+#define METRIKO_CUDA_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum mtk_status {
+    MTK_OK = 0,
+    MTK_ERR_BAD_INPUT = 1,      /* invalid sizes / indices / non-manifold mesh          */
+    MTK_ERR_CUDA = 2,           /* a CUDA runtime call failed (see mtk_last_error)      */
+    MTK_ERR_NOT_CONVERGED = 3,  /* an iterative solve hit its iteration cap             */
+    MTK_ERR_BREAKDOWN = 4,      /* PCG breakdown: p^H A p <= 0 or a NaN                 */
+    MTK_ERR_TIMEOUT = 5,        /* a bounded device-side wait gave up                   */
+    MTK_ERR_NO_DEVICE = 6,      /* no CUDA device is visible                            */
+    MTK_ERR_ROUNDING = 7        /* post-rounding integrality check failed               */
+};
+
+enum mtk_precision {
+    MTK_PREC_FP64 = 0,          /* FP64 SpMV, dots and PCG throughout                   */
+    MTK_PREC_MIXED = 1          /* FP32 PCG inside FP64 iterative refinement            */
+};
+
+typedef struct mtk_ctx mtk_ctx;
+
+typedef struct {
+    int32_t precision;          /* mtk_precision                                        */
+    double tol;                 /* relative residual ||b - A x|| / ||b|| per solve       */
+    int32_t max_iter;           /* PCG iteration cap per inner solve                     */
+    int32_t max_refine;         /* outer FP64 refinement steps (MIXED)                   */
+    double inner_tol;           /* relative tolerance of each inner FP32 solve (MIXED)   */
+} mtk_solve_opts;
+
+typedef struct {
+    int64_t pcg_iters;          /* PCG iterations summed over all solves                 */
+    int64_t solves;             /* linear solves                                         */
+    int64_t refinements;        /* FP64 residual evaluations                             */
+    int64_t spmv_calls;         /* operator applications                                 */
+    int64_t kernel_launches;    /* kernels launched by the library                       */
+    double max_rel_residual;    /* worst final relative residual of any solve            */
+    double ms_field;            /* device time, field stage                              */
+    double ms_integrate;        /* device time, naive + LM integration                   */
+    double ms_rounding;         /* device time, greedy rounding loop                     */
+    double ms_host;             /* host-side topology time (pipeline only)               */
+    double ms_total;            /* wall time of the call                                 */
+    int64_t resolves;           /* IGM re-solves (rounded variables that needed a solve) */
+    int64_t lm_iterations;      /* LM iterations over all LM solves                      */
+    double min_order_margin;    /* smallest gap between best and second-best rounding    */
+} mtk_stats;
+
+const char* mtk_status_string(int status);
+const char* mtk_last_error(void);
+void mtk_default_opts(mtk_solve_opts* opts);
+
+int mtk_ctx_create(int device, mtk_ctx** out);
+int mtk_ctx_destroy(mtk_ctx* ctx);
+/* Number of library kernels launched on this context so far (instrumentation). */
+int64_t mtk_ctx_kernel_count(const mtk_ctx* ctx);
+
+/*
+ * Smoothest N-RoSy field: assemble the connection Laplacian L (face graph, 3 neighbours per
+ * face) and the lumped mass M = diag(area) on the device, then run n_iter steps of inverse
+ * power iteration  x = L^-1 M u,  x /= sqrt|x^H M x|,  u = x.
+ *   nbr[3*f+j]   face across the j-th halfedge of face f (halfedge F(f,j) -> F(f,j+1))
+ *   theta[3*f+j] heArgOnFace(h) - heArgOnFace(twin(h)) for that halfedge; the off-diagonal
+ *                entry is  L(f, nbr) = -(-exp(i theta))^nRosy,  the diagonal #nbr + 1e-9
+ *   area[f]      face area;  x0[2*f], x0[2*f+1]  start vector (re, im)
+ *   out[2*f], out[2*f+1]  the compressed field (re, im), unit M-norm
+ */
+int mtk_field_smoothest(mtk_ctx* ctx, int32_t nF, int32_t nRosy, const int32_t* nbr,
+                        const double* theta, const double* area, const double* x0,
+                        int32_t n_iter, const mtk_solve_opts* opts, double* out,
+                        mtk_stats* stats);
+
+/*
+ * Integer-grid-map rounding system, in the reference's reduced coordinates
+ * xs = [y ; z]: y = free full variables (identity rows of UFull), z = kernel coordinates of
+ * the constrained block (UFull rows = USmall).  Full variables are n per raw vertex followed
+ * by n per seam transition (n = N/2 under sign symmetry).
+ */
+typedef struct {
+    int32_t nF, nCut, N, n;
+    const int32_t* cutF;        /* nF*3 cut-mesh vertex of each corner                     */
+    const double* cutV;         /* nCut*3 cut-mesh vertex positions                        */
+    /* W: cut vertex c, function k < n  ->  sum_e w_val[e] * X[w_idx[e]], rows r = n*c + k */
+    const int32_t* w_ptr;       /* n*nCut + 1                                              */
+    const int32_t* w_idx;       /* full-variable indices                                   */
+    const double* w_val;
+    int32_t nFull;              /* n * (nV + nT)                                           */
+    const int32_t* full2y;      /* nFull: y index of a free variable, else -1              */
+    int32_t nJ, nZ;             /* constrained variables / kernel dimension                */
+    const int32_t* uniqueJ;     /* nJ full indices of the constrained block (ascending)   */
+    const double* USmall;       /* nJ x nZ row-major kernel basis                          */
+    const double* F2;           /* 2*N*nF target field, face frame (rawF2Vec)              */
+    double length;              /* grid edge length (bbox diagonal * ratio / norm)         */
+    int32_t nFixed;             /* anchor of the naive solve (fixedIdcs / fixedVals)      */
+    const int32_t* fixedIdcs;
+    const double* fixedVals;
+    int32_t nSingular;          /* singularIdcs (rounded first unless roundSeams)          */
+    const int32_t* singularIdcs;
+    int32_t nInteger;           /* integerIdcs (transition variables)                      */
+    const int32_t* integerIdcs;
+    int32_t seamless;           /* RosyParameterization::seamless                          */
+    int32_t roundSeams;         /* RosyParameterization::roundSeams                        */
+} mtk_igm_desc;
+
+/*
+ * Naive (Poisson) integration, the seamless LM solve and the greedy rounding loop.
+ *   fullx[nFull]      result (reference iter_rounding.h:111)
+ *   fix_order/fix_vals (capacity nSingular + nInteger) the rounded full indices and their
+ *                      integer values in fixing order; *n_fixed receives the count
+ *   x_naive[nFull]    optional (may be NULL): the naive Poisson solution ni.x0
+ * Returns MTK_ERR_ROUNDING when the post-rounding integrality check fails (fullx is still
+ * written, as the reference does).
+ */
+int mtk_iterative_rounding(mtk_ctx* ctx, const mtk_igm_desc* desc, const mtk_solve_opts* opts,
+                           double* fullx, int32_t* fix_order, int32_t* fix_vals,
+                           int32_t* n_fixed, double* x_naive, mtk_stats* stats);
+
+/*
+ * Whole path of example_igm.cpp with host buffers: V (nV*3), F (nF*3), N = 4, Smoothest
+ * field, Curl matching, seamless = 1, localInjectivity = 0.  Outputs (caller-allocated,
+ * may be NULL unless noted):
+ *   singular[nV], matching[nE] (combed), seam[nE] (0/1), compressed[2*nF]
+ *   cfn[nF*3*N]       corner parameterisation (row f: corner j, function k at N*j + k)
+ *   fullx / x_naive   capacity given by fullx_cap; *n_full receives the length
+ *   fix_order / fix_vals capacity fix_cap; *n_fixed receives the count
+ *   counts[8]         nV, nE, nCut, nT, nS, nJ, nZ, nFull
+ */
+typedef struct {
+    int32_t seed;               /* start vector seed (splitmix64, see mtk_seeded_init)   */
+    int32_t n_iter;             /* power iterations (reference: 50)                       */
+    double ratio;               /* RosyParameterization ratio (grid scale)                */
+    int32_t round_seams;        /* RosyParameterization::roundSeams                       */
+    int32_t seamless;           /* RosyParameterization::seamless                         */
+    int32_t stop_after;         /* 0 = full path, 1 = after field+matching, 2 = after setup */
+} mtk_pipeline_opts;
+
+int mtk_pipeline_run(mtk_ctx* ctx, int32_t nV, int32_t nF, const double* V, const int32_t* F,
+                     const mtk_pipeline_opts* popts, const mtk_solve_opts* sopts,
+                     int32_t* singular, int32_t* matching, uint8_t* seam, double* compressed,
+                     double* cfn, double* fullx, double* x_naive, int32_t fullx_cap,
+                     int32_t* n_full, int32_t* fix_order, int32_t* fix_vals, int32_t fix_cap,
+                     int32_t* n_fixed, int32_t* counts, mtk_stats* stats);
+
+/*
+ * Host-only topology stages for a caller-supplied field (no device work): Hmesh, Curl
+ * matching and singularities, seams, cut mesh, combing, RosyParameterization::setup() and the
+ * host part of integ() (constraint reduction, UFull kernel block, target field, grid length).
+ * Replaces the face_rosy_field.h:126-386 and parameterization*.{h,ipp} host code.
+ *   compressed[2*nF]  field eigenvector (re, im) -- e.g. the output of mtk_field_smoothest
+ *   singular[nV], matching[nE] (combed), seam[nE], cutF[nF*3]
+ *   counts[8]         nV, nE, nCut, nT, nS, nJ, nZ, nFull;   *length: grid edge length
+ */
+int mtk_topology_from_field(int32_t nV, int32_t nF, const double* V, const int32_t* F,
+                            const double* compressed, double ratio, int32_t round_seams,
+                            int32_t* singular, int32_t* matching, uint8_t* seam, int32_t* cutF,
+                            int32_t* counts, double* length);
+
+/* The deterministic start vector used by the pipeline: re/im of face f from splitmix64. */
+void mtk_seeded_init(int32_t n, int32_t seed, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

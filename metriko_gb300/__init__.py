@@ -1,0 +1,9 @@
+"""metriko_gb300: GB300-native smoothest 4-RoSy field, seamless integration and Integer-Grid-Map
+rounding (the numerical core of komietty/metriko), as hand-written sm_103a CUDA behind a C ABI
+(include/metriko_cuda.h) and header-only C++ host code (include/metriko/...).
+
+Python here is plumbing for tests and benchmarks: `Context`, `pipeline`, `field_smoothest`.
+"""
+from ._lib import (Context, MetrikoError, PREC_FP64, PREC_MIXED, field_smoothest, lib,  # noqa: F401
+                   pipeline, seeded_init, solve_opts, topology_from_field)
+from . import meshgen  # noqa: F401

@@ -1,0 +1,216 @@
+"""ctypes binding of libmetriko_cuda.so (C ABI declared in include/metriko_cuda.h).
+
+The library is the product: there is no CPU fallback.  Loading fails loudly when the shared
+library is missing, and every call raises MetrikoError on a non-zero status.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "libmetriko_cuda.so"
+
+OK, BAD_INPUT, CUDA, NOT_CONVERGED, BREAKDOWN, TIMEOUT, NO_DEVICE, ROUNDING = range(8)
+PREC_FP64, PREC_MIXED = 0, 1
+
+# every symbol include/metriko_cuda.h declares
+EXPORTS = [
+    "mtk_status_string", "mtk_last_error", "mtk_default_opts", "mtk_ctx_create", "mtk_ctx_destroy",
+    "mtk_ctx_kernel_count", "mtk_field_smoothest", "mtk_iterative_rounding", "mtk_pipeline_run",
+    "mtk_seeded_init", "mtk_topology_from_field",
+]
+
+
+class MetrikoError(RuntimeError):
+    def __init__(self, status, what, detail=""):
+        super().__init__(f"{what}: status {status} ({detail})")
+        self.status = status
+
+
+class SolveOpts(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("tol", C.c_double), ("max_iter", C.c_int32),
+                ("max_refine", C.c_int32), ("inner_tol", C.c_double)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("pcg_iters", C.c_int64), ("solves", C.c_int64), ("refinements", C.c_int64),
+                ("spmv_calls", C.c_int64), ("kernel_launches", C.c_int64),
+                ("max_rel_residual", C.c_double), ("ms_field", C.c_double),
+                ("ms_integrate", C.c_double), ("ms_rounding", C.c_double), ("ms_host", C.c_double),
+                ("ms_total", C.c_double), ("resolves", C.c_int64), ("lm_iterations", C.c_int64),
+                ("min_order_margin", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class PipelineOpts(C.Structure):
+    _fields_ = [("seed", C.c_int32), ("n_iter", C.c_int32), ("ratio", C.c_double),
+                ("round_seams", C.c_int32), ("seamless", C.c_int32), ("stop_after", C.c_int32)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise ImportError(f"{LIB_PATH} is missing: run __graft_entry__.build() (nvcc, sm_103a)")
+        L = C.CDLL(str(LIB_PATH))
+        L.mtk_status_string.restype = C.c_char_p
+        L.mtk_status_string.argtypes = [C.c_int]
+        L.mtk_last_error.restype = C.c_char_p
+        L.mtk_default_opts.argtypes = [C.POINTER(SolveOpts)]
+        L.mtk_ctx_create.argtypes = [C.c_int, C.POINTER(C.c_void_p)]
+        L.mtk_ctx_destroy.argtypes = [C.c_void_p]
+        L.mtk_ctx_kernel_count.argtypes = [C.c_void_p]
+        L.mtk_ctx_kernel_count.restype = C.c_int64
+        L.mtk_seeded_init.argtypes = [C.c_int32, C.c_int32, C.c_void_p]
+        L.mtk_field_smoothest.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.c_void_p, C.c_int32, C.POINTER(SolveOpts), C.c_void_p,
+                                          C.POINTER(Stats)]
+        L.mtk_pipeline_run.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
+                                       C.POINTER(PipelineOpts), C.POINTER(SolveOpts)] + [C.c_void_p] * 7 + \
+                                      [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
+                                       C.c_void_p, C.POINTER(Stats)]
+        L.mtk_topology_from_field.argtypes = [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
+                                              C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                              C.c_void_p, C.c_void_p]
+        _lib = L
+    return _lib
+
+
+def _check(status, what):
+    if status != OK:
+        L = lib()
+        raise MetrikoError(status, what, f"{L.mtk_status_string(status).decode()}: {L.mtk_last_error().decode()}")
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def solve_opts(precision="mixed", tol=1e-8, max_iter=50000, max_refine=12, inner_tol=1e-4):
+    o = SolveOpts()
+    lib().mtk_default_opts(C.byref(o))
+    o.precision = PREC_MIXED if precision == "mixed" else PREC_FP64
+    o.tol, o.max_iter, o.max_refine, o.inner_tol = tol, max_iter, max_refine, inner_tol
+    return o
+
+
+class Context:
+    """One CUDA device + stream (mtk_ctx)."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        _check(lib().mtk_ctx_create(device, C.byref(h)), "mtk_ctx_create")
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            lib().mtk_ctx_destroy(self.handle)
+            self.handle = None
+
+    def kernel_count(self):
+        return int(lib().mtk_ctx_kernel_count(self.handle))
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def seeded_init(n: int, seed: int = 0) -> np.ndarray:
+    out = np.empty(2 * n, np.float64)
+    lib().mtk_seeded_init(n, seed, _ptr(out))
+    return out[0::2] + 1j * out[1::2]
+
+
+def field_smoothest(ctx: Context, nbr, theta, area, x0, n_rosy=4, n_iter=50, opts=None):
+    """mtk_field_smoothest on face-graph inputs; returns (compressed field, stats dict)."""
+    nbr = np.ascontiguousarray(nbr, np.int32).reshape(-1)
+    theta = np.ascontiguousarray(theta, np.float64).reshape(-1)
+    area = np.ascontiguousarray(area, np.float64)
+    nF = len(area)
+    x = np.empty(2 * nF)
+    x[0::2], x[1::2] = np.real(x0), np.imag(x0)
+    out = np.empty(2 * nF)
+    st = Stats()
+    o = opts or solve_opts()
+    _check(lib().mtk_field_smoothest(ctx.handle, nF, n_rosy, _ptr(nbr), _ptr(theta), _ptr(area), _ptr(x), n_iter,
+                                     C.byref(o), _ptr(out), C.byref(st)), "mtk_field_smoothest")
+    return out[0::2] + 1j * out[1::2], st.as_dict()
+
+
+def pipeline(ctx: Context, V, F, ratio=0.02, seed=0, round_seams=False, seamless=True, n_iter=50,
+             opts=None, stop_after=0, check=True):
+    """mtk_pipeline_run: Hmesh -> smoothest field -> Curl matching -> seams -> cut mesh ->
+    combing -> RosyParameterization setup()/integ() (example_igm.cpp:13-31)."""
+    V = np.ascontiguousarray(V, np.float64)
+    F = np.ascontiguousarray(F, np.int32)
+    nV, nF = len(V), len(F)
+    nE = 3 * nF // 2
+    singular = np.zeros(nV, np.int32)
+    matching = np.zeros(nE, np.int32)
+    seam = np.zeros(nE, np.uint8)
+    compressed = np.zeros(2 * nF)
+    cfn = np.zeros(nF * 12)
+    cap = 2 * (nV + 4 * nE) + 16
+    fullx = np.zeros(cap)
+    xnaive = np.zeros(cap)
+    fix_cap = 2 * (nV + nE) + 16
+    fix_order = np.zeros(fix_cap, np.int32)
+    fix_vals = np.zeros(fix_cap, np.int32)
+    counts = np.zeros(8, np.int32)
+    n_full = C.c_int32(0)
+    n_fixed = C.c_int32(0)
+    p = PipelineOpts(seed, n_iter, ratio, int(round_seams), int(seamless), stop_after)
+    o = opts or solve_opts()
+    st = Stats()
+    status = lib().mtk_pipeline_run(ctx.handle, nV, nF, _ptr(V), _ptr(F), C.byref(p), C.byref(o),
+                                    _ptr(singular), _ptr(matching), _ptr(seam), _ptr(compressed), _ptr(cfn),
+                                    _ptr(fullx), _ptr(xnaive), cap, C.byref(n_full), _ptr(fix_order),
+                                    _ptr(fix_vals), fix_cap, C.byref(n_fixed), _ptr(counts), C.byref(st))
+    if check and status not in (OK, ROUNDING):
+        _check(status, "mtk_pipeline_run")
+    nfull, nfix = n_full.value, n_fixed.value
+    return dict(status=status, singular=singular, matching=matching, seam=seam.astype(bool),
+                compressed=compressed[0::2] + 1j * compressed[1::2], cfn=cfn.reshape(nF, 12),
+                fullx=fullx[:nfull].copy(), x_naive=xnaive[:nfull].copy(),
+                fix_order=fix_order[:nfix].copy(), fix_vals=fix_vals[:nfix].copy(),
+                counts=dict(zip(["nV", "nE", "nCut", "nT", "nS", "nJ", "nZ", "nFull"], counts.tolist())),
+                stats=st.as_dict())
+
+
+def topology_from_field(V, F, compressed, ratio=0.02, round_seams=False):
+    """Host-only stages (no GPU): matching, singularities, seam, cut mesh, combing, setup and
+    the host part of integ() for a given field eigenvector."""
+    V = np.ascontiguousarray(V, np.float64)
+    F = np.ascontiguousarray(F, np.int32)
+    nV, nF = len(V), len(F)
+    nE = 3 * nF // 2
+    c = np.empty(2 * nF)
+    c[0::2], c[1::2] = np.real(compressed), np.imag(compressed)
+    singular = np.zeros(nV, np.int32)
+    matching = np.zeros(nE, np.int32)
+    seam = np.zeros(nE, np.uint8)
+    cutF = np.zeros(3 * nF, np.int32)
+    counts = np.zeros(8, np.int32)
+    length = C.c_double(0)
+    _check(lib().mtk_topology_from_field(nV, nF, _ptr(V), _ptr(F), _ptr(c), ratio, int(round_seams),
+                                         _ptr(singular), _ptr(matching), _ptr(seam), _ptr(cutF), _ptr(counts),
+                                         C.byref(length)), "mtk_topology_from_field")
+    return dict(singular=singular, matching=matching, seam=seam.astype(bool), cutF=cutF.reshape(nF, 3),
+                counts=dict(zip(["nV", "nE", "nCut", "nT", "nS", "nJ", "nZ", "nFull"], counts.tolist())),
+                length=length.value)

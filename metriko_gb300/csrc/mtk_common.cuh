@@ -1,0 +1,143 @@
+// Shared device helpers for the metriko GB300 kernels.
+//
+// * status codes returned through the C ABI (include/metriko_cuda.h);
+// * a bounded software grid barrier for cooperative persistent kernels: every spin has an
+//   iteration cap after which the kernel records MTK_ERR_TIMEOUT in a device flag and all
+//   blocks leave the solve loop (no trap, no unbounded wait);
+// * deterministic reductions: every block writes one partial per slot, and after the grid
+//   barrier every block re-reduces all partials in the same fixed order, so each block holds
+//   bit-identical scalars without a second barrier.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+
+#include "metriko_cuda.h"
+
+#define MTK_CUDA_TRY(expr)                                                           \
+    do {                                                                             \
+        cudaError_t _e = (expr);                                                     \
+        if (_e != cudaSuccess) {                                                     \
+            mtk_set_last_error(cudaGetErrorString(_e), __FILE__, __LINE__);          \
+            return MTK_ERR_CUDA;                                                     \
+        }                                                                            \
+    } while (0)
+
+#define MTK_TRY(expr)                          \
+    do {                                       \
+        int _s = (expr);                       \
+        if (_s != MTK_OK) return _s;           \
+    } while (0)
+
+void mtk_set_last_error(const char* msg, const char* file, int line);
+
+namespace mtk {
+
+constexpr int kBlock = 256;               // threads per CTA of the persistent solvers
+constexpr int kWarps = kBlock / 32;
+constexpr long long kSpinLimit = 1LL << 25;   // ~ seconds with nanosleep backoff
+
+struct GridBarrier {
+    unsigned int* count;       // arrivals in the current generation
+    unsigned int* gen;         // generation counter
+    int* err;                  // sticky error flag (MTK_ERR_TIMEOUT)
+};
+
+__device__ __forceinline__ unsigned int ld_acquire(const unsigned int* p) {
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(unsigned int* p, unsigned int v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ int ld_volatile(const int* p) {
+    return *reinterpret_cast<const volatile int*>(p);
+}
+
+// Returns false (in every thread of the block) if the barrier timed out or an error was
+// already recorded; callers then leave their loop.
+__device__ __forceinline__ bool grid_sync(const GridBarrier& b) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = ld_volatile(b.err) == 0;
+        if (ok) {
+            unsigned int g = ld_acquire(b.gen);
+            __threadfence();
+            unsigned int arrived = atomicAdd(b.count, 1u);
+            if (arrived == gridDim.x - 1) {
+                atomicExch(b.count, 0u);
+                __threadfence();
+                st_release(b.gen, g + 1);
+            } else {
+                long long spins = 0;
+                while (ld_acquire(b.gen) == g) {
+                    if (++spins > kSpinLimit) { atomicExch(b.err, (int)MTK_ERR_TIMEOUT); ok = 0; break; }
+                    if (ld_volatile(b.err) != 0) { ok = 0; break; }
+                    __nanosleep(64);
+                }
+            }
+            __threadfence();
+        }
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// Fixed-order block reduction of K values per thread; result valid in all threads.
+template <typename T, int K>
+__device__ __forceinline__ void block_sum(T (&v)[K]) {
+    __shared__ T s_red[K][kWarps];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        T x = v[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if (lane == 0) s_red[k][warp] = x;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        T x = T(0);
+        for (int w = 0; w < kWarps; w++) x += s_red[k][w];
+        v[k] = x;
+    }
+    __syncthreads();
+}
+
+// Writes the block partials (K values) to partials[k * gridDim.x + blockIdx.x].
+template <typename T, int K>
+__device__ __forceinline__ void publish_partials(T (&v)[K], T* partials) {
+    block_sum<T, K>(v);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; k++) partials[k * gridDim.x + blockIdx.x] = v[k];
+    }
+}
+
+// After a grid barrier: every block reduces all partials in the same order.
+template <typename T, int K>
+__device__ __forceinline__ void gather_partials(const T* partials, T (&out)[K]) {
+    T v[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        T x = T(0);
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) x += __ldcg(partials + k * gridDim.x + b);
+        v[k] = x;
+    }
+    block_sum<T, K>(v);
+#pragma unroll
+    for (int k = 0; k < K; k++) out[k] = v[k];
+}
+
+// ----------------------------------------------------------------- small complex helpers
+template <typename T> struct cplx { T re, im; };
+template <typename T> __device__ __forceinline__ cplx<T> cmul(cplx<T> a, cplx<T> b) {
+    return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+template <typename T> __device__ __forceinline__ cplx<T> cadd(cplx<T> a, cplx<T> b) { return {a.re + b.re, a.im + b.im}; }
+
+}  // namespace mtk

@@ -1,0 +1,85 @@
+// Context object behind the opaque mtk_ctx handle, plus small device-buffer helpers.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "mtk_common.cuh"
+
+struct mtk_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_a = nullptr, ev_b = nullptr;
+    // bounded grid barrier state (3 words) + error flag, and reduction scratch
+    unsigned int* bar = nullptr;   // [0] count, [1] generation
+    int* dev_err = nullptr;
+    double* partials = nullptr;    // reduction partials (>= 8 slots per block)
+    double* scalars = nullptr;     // finalized scalars (64 doubles)
+    double* h_scalars = nullptr;   // pinned host mirror of scalars
+    int* h_int = nullptr;          // pinned host ints
+    int* dev_int = nullptr;        // device ints (iteration counts, status)
+    int partial_blocks = 0;        // capacity in blocks
+    long long kernels = 0;
+};
+
+namespace mtk {
+
+// RAII device buffer (allocation happens once per solve set-up, never inside the loops).
+template <typename T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    ~DBuf() { if (p) cudaFree(p); }
+    int alloc(size_t count) {
+        if (p) { cudaFree(p); p = nullptr; }
+        n = count;
+        if (count == 0) return MTK_OK;
+        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        if (e != cudaSuccess) { mtk_set_last_error(cudaGetErrorString(e), __FILE__, __LINE__); p = nullptr; return MTK_ERR_CUDA; }
+        return MTK_OK;
+    }
+    int upload(const T* h, size_t count, cudaStream_t s) {
+        MTK_TRY(alloc(count));
+        if (count) MTK_CUDA_TRY(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+        return MTK_OK;
+    }
+    int zero(cudaStream_t s) {
+        if (n) MTK_CUDA_TRY(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+        return MTK_OK;
+    }
+};
+
+inline GridBarrier barrier_of(mtk_ctx* c) { return GridBarrier{c->bar, c->bar + 1, c->dev_err}; }
+
+// Resets the barrier words and the error flag before a cooperative launch.
+inline int reset_barrier(mtk_ctx* c) {
+    MTK_CUDA_TRY(cudaMemsetAsync(c->bar, 0, 2 * sizeof(unsigned int), c->stream));
+    MTK_CUDA_TRY(cudaMemsetAsync(c->dev_err, 0, sizeof(int), c->stream));
+    return MTK_OK;
+}
+
+// Cooperative launch of a persistent kernel sized to fill every SM.
+template <typename K, typename... Args>
+int launch_persistent(mtk_ctx* c, K kernel, int* grid_out, Args... args) {
+    int per_sm = 0;
+    MTK_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0));
+    if (per_sm < 1) { mtk_set_last_error("persistent kernel does not fit on an SM", __FILE__, __LINE__); return MTK_ERR_CUDA; }
+    per_sm = per_sm > 4 ? 4 : per_sm;
+    int grid = c->num_sms * per_sm;
+    if (grid > c->partial_blocks) grid = c->partial_blocks;
+    if (grid_out) *grid_out = grid;
+    void* params[] = {reinterpret_cast<void*>(&args)...};
+    MTK_TRY(reset_barrier(c));
+    MTK_CUDA_TRY(cudaLaunchCooperativeKernel(reinterpret_cast<void*>(kernel), dim3(grid), dim3(kBlock), params, 0, c->stream));
+    c->kernels++;
+    return MTK_OK;
+}
+
+inline int stream_grid(mtk_ctx* c) { return c->num_sms * 4; }
+
+}  // namespace mtk

@@ -1,0 +1,1200 @@
+// Integer-grid-map integration and greedy rounding on the device.
+//
+// Replaces (metriko) iterative_rounding (iter_rounding.h:33-113), NaiveIntegration
+// (iter_rounding_init.h:16-233), SeamlessIntegration (iter_rounding_loop.h:10-125) and the
+// per-iteration SimplicialLLT factorisations of LMSolver (levenberg_marquardt.h:140-231).
+//
+// Structure used instead of assembling X2F^T X2F on the host:
+//   X2F = G2 * fullx2Nfunc * UFull, and under sign symmetry (functions k+n = -functions k)
+//   X2F^T X2F = UFull^T (2 W^T S W) UFull,
+// with S the per-face gradient Gram matrix of the cut mesh (S_ab = sum_f g_a . g_b, a scalar
+// stiffness shared by u and v), W the cut-vertex <- full-variable map (rows k < n of
+// fullx2Nfunc: +-1 permutations plus seam translations) and UFull = [I ; USmall] in the
+// reference's reduced coordinates xs = [y ; z].  The operator is applied matrix-free:
+//   B: U = W [y ; USmall z]   (u,v of every cut vertex: two right-hand sides in one pass)
+//   C: Q = S U                (SELL-free padded CSR, one thread per cut vertex)
+//   D: y' = 2 W_y^T Q,  XJ' = 2 W_J^T Q
+//   E: z' = USmall^T XJ'      (replicated per block: nZ is small)
+// The kernel coordinates z (and the constraint projector on them) are replicated in every
+// block's shared memory, so the constrained block costs no extra grid barrier.
+//
+// Constraints (the reference's 1e8 / 1e10 penalty rows) are imposed exactly by projection:
+// fixed free variables are Dirichlet entries, fixed constrained variables are rows of USmall
+// on z, kept orthonormal (Q) so that P_z = I - Q^T Q.  The difference from the penalty
+// solution is O(1 / penalty).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <vector>
+
+#include "mtk_ctx.cuh"
+
+namespace mtk {
+
+constexpr int kMaxFaceDeg = 30;   // faces around one cut vertex (stiffness row capacity)
+
+template <typename T>
+struct IgmOp {
+    int nCut, nY, nZ, nJ;
+    const int* w_ptr;   // 2*nCut + 1
+    const int* w_tag;   // >= 0: y index, < 0: -1 - J slot
+    const T* w_val;
+    const int* s_ptr;   // nCut + 1 (padded rows)
+    const int* s_col;
+    const T* s_val;
+    const int* yt_ptr;  // nY + 1: rows r (= 2c + k) referencing y_j
+    const int* yt_row;
+    const T* yt_val;
+    const int* jt_ptr;  // nJ + 1
+    const int* jt_row;
+    const T* jt_val;
+    const T* Us;        // nJ x nZ
+    T scale, shift;
+    T* U;               // 2*nCut gather buffer
+    T* Qc;              // 2*nCut stiffness product
+    T* XoJ;             // nJ
+};
+
+// Shared-memory layout of the replicated z state.
+template <typename T>
+struct ZSmem {
+    T *xz, *rz, *zz, *pz, *qz, *XJ, *tmpJ, *tz;
+    __device__ void bind(T* base, int nZ, int nJ) {
+        xz = base; rz = xz + nZ; zz = rz + nZ; pz = zz + nZ; qz = pz + nZ; tz = qz + nZ;
+        XJ = tz + nZ; tmpJ = XJ + nJ;
+    }
+};
+
+template <typename T>
+struct ZProj {
+    int kq;             // orthonormal constraint rows on z
+    const T* Q;         // kq x nZ
+    const T* Minv;      // nZ x nZ (dense inverse of the z block) or nullptr
+};
+
+// v <- v - Q^T (Q v) on a replicated smem vector (block-wide).  tmp: >= kq scratch.
+template <typename T>
+__device__ void project_z(const ZProj<T>& P, int nZ, T* v, T* tmp) {
+    if (P.kq == 0) return;
+    for (int a = threadIdx.x; a < P.kq; a += blockDim.x) {
+        T s = T(0);
+        for (int j = 0; j < nZ; j++) s += P.Q[(size_t)a * nZ + j] * v[j];
+        tmp[a] = s;
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < nZ; j += blockDim.x) {
+        T s = v[j];
+        for (int a = 0; a < P.kq; a++) s -= P.Q[(size_t)a * nZ + j] * tmp[a];
+        v[j] = s;
+    }
+    __syncthreads();
+}
+
+// out = Minv * in (dense) or copy; replicated.
+template <typename T>
+__device__ void precond_z(const ZProj<T>& P, int nZ, const T* in, T* out) {
+    for (int j = threadIdx.x; j < nZ; j += blockDim.x) {
+        T s = T(0);
+        if (P.Minv) {
+            for (int k = 0; k < nZ; k++) s += P.Minv[(size_t)j * nZ + k] * in[k];
+        } else {
+            s = in[j];
+        }
+        out[j] = s;
+    }
+    __syncthreads();
+}
+
+// Fixed-order block dot of two replicated smem vectors (same value in every block).
+template <typename T>
+__device__ T smem_dot(const T* a, const T* b, int n) {
+    T v[1] = {T(0)};
+    for (int j = threadIdx.x; j < n; j += blockDim.x) v[0] += a[j] * b[j];
+    block_sum<T, 1>(v);
+    return v[0];
+}
+
+// Operator K p, with p = [py (global) ; pz (smem)].  Result: qy (global, masked, projected)
+// and qz (smem, projected).  Returns partial <py, qy> of this block in *pq_part and false on
+// a barrier failure.  Three grid barriers.
+template <typename T>
+__device__ bool igm_apply(const IgmOp<T>& A, const ZProj<T>& P, const unsigned char* __restrict__ fixy,
+                          const T* py, const T* pz, T* qy, T* qz, ZSmem<T>& zs, const GridBarrier& bar, T& pq_part) {
+    const int stride = gridDim.x * blockDim.x;
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    // A (replicated): XJ = USmall pz
+    for (int s = threadIdx.x; s < A.nJ; s += blockDim.x) {
+        T acc = T(0);
+        const T* row = A.Us + (size_t)s * A.nZ;
+        for (int j = 0; j < A.nZ; j++) acc += row[j] * pz[j];
+        zs.XJ[s] = acc;
+    }
+    __syncthreads();
+    // B: U = W [py ; XJ]
+    for (int r = t0; r < 2 * A.nCut; r += stride) {
+        T acc = T(0);
+        for (int e = A.w_ptr[r]; e < A.w_ptr[r + 1]; e++) {
+            int tag = A.w_tag[e];
+            T xv = tag >= 0 ? __ldcg(py + tag) : zs.XJ[-1 - tag];
+            acc += A.w_val[e] * xv;
+        }
+        A.U[r] = acc;
+    }
+    if (!grid_sync(bar)) return false;
+    // C: Qc = S U  (two right-hand sides per row)
+    for (int c = t0; c < A.nCut; c += stride) {
+        T a0 = T(0), a1 = T(0);
+        for (int e = A.s_ptr[c]; e < A.s_ptr[c + 1]; e++) {
+            int b = A.s_col[e];
+            T s = A.s_val[e];
+            a0 += s * __ldcg(A.U + 2 * b);
+            a1 += s * __ldcg(A.U + 2 * b + 1);
+        }
+        A.Qc[2 * c] = a0;
+        A.Qc[2 * c + 1] = a1;
+    }
+    if (!grid_sync(bar)) return false;
+    // D: qy = scale * 2 W_y^T Qc + shift * py (masked);  XoJ = 2 W_J^T Qc
+    const T two_scale = T(2) * A.scale;
+    T part = T(0);
+    for (int j = t0; j < A.nY; j += stride) {
+        T acc = T(0);
+        for (int e = A.yt_ptr[j]; e < A.yt_ptr[j + 1]; e++) acc += A.yt_val[e] * __ldcg(A.Qc + A.yt_row[e]);
+        T pj = py[j];
+        T qv = fixy[j] ? T(0) : two_scale * acc + A.shift * pj;
+        qy[j] = qv;
+        part += pj * qv;
+    }
+    for (int s = t0; s < A.nJ; s += stride) {
+        T acc = T(0);
+        for (int e = A.jt_ptr[s]; e < A.jt_ptr[s + 1]; e++) acc += A.jt_val[e] * __ldcg(A.Qc + A.jt_row[e]);
+        A.XoJ[s] = T(2) * acc;
+    }
+    pq_part = part;
+    return true;
+    // (E is done by the caller after the next barrier: igm_apply_z)
+}
+
+// E (replicated, after a barrier): qz = P_z (scale USmall^T XoJ + shift pz)
+template <typename T>
+__device__ void igm_apply_z(const IgmOp<T>& A, const ZProj<T>& P, const T* pz, T* qz, ZSmem<T>& zs) {
+    for (int s = threadIdx.x; s < A.nJ; s += blockDim.x) zs.tmpJ[s] = __ldcg(A.XoJ + s);
+    __syncthreads();
+    for (int j = threadIdx.x; j < A.nZ; j += blockDim.x) {
+        T acc = T(0);
+        for (int s = 0; s < A.nJ; s++) acc += A.Us[(size_t)s * A.nZ + j] * zs.tmpJ[s];
+        qz[j] = A.scale * acc + A.shift * pz[j];
+    }
+    __syncthreads();
+    project_z(P, A.nZ, qz, zs.tz);
+}
+
+// Persistent projected PCG.  mode 0: solve K x = b from a feasible x (x, b: [y ; z] global).
+// mode 1: residual only, r = P(b - K x) written to r, |r|^2 in out.
+// out[0] status, out[1] iterations, (double*)(out+4): final |r|^2.
+template <typename T>
+__global__ void __launch_bounds__(kBlock) igm_pcg(IgmOp<T> A, ZProj<T> P, const unsigned char* __restrict__ fixy,
+                                                 const T* __restrict__ minvy, const T* __restrict__ b, T* x, T* r, T* z,
+                                                 T* p, T* q, T* partials, GridBarrier bar, double tol2, int maxit,
+                                                 int mode, int* out) {
+    extern __shared__ unsigned char smem_raw[];
+    ZSmem<T> zs;
+    zs.bind(reinterpret_cast<T*>(smem_raw), A.nZ, A.nJ);
+    const int nY = A.nY, nZ = A.nZ;
+    const int stride = gridDim.x * blockDim.x;
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    int status = 3, it = 0;
+    T rr = T(0);
+    T part[2];
+    T pq1[1];
+    // replicated z state
+    for (int j = threadIdx.x; j < nZ; j += blockDim.x) {
+        zs.xz[j] = x[nY + j];
+        zs.pz[j] = x[nY + j];
+    }
+    __syncthreads();
+    // r = P(b - K x): apply K to x (py = x_y)
+    T pqp = T(0);
+    if (!igm_apply(A, P, fixy, x, zs.pz, q, zs.qz, zs, bar, pqp)) { status = 5; goto done; }
+    if (!grid_sync(bar)) { status = 5; goto done; }
+    igm_apply_z(A, P, zs.pz, zs.qz, zs);
+    part[0] = T(0);
+    part[1] = T(0);
+    for (int j = t0; j < nY; j += stride) {
+        T rj = fixy[j] ? T(0) : b[j] - q[j];
+        r[j] = rj;
+        T zj = minvy[j] * rj;
+        part[1] += rj * rj;
+        if (mode == 0) {
+            z[j] = zj;
+            p[j] = zj;
+            part[0] += rj * zj;
+        }
+    }
+    for (int j = threadIdx.x; j < nZ; j += blockDim.x) zs.rz[j] = __ldg(b + nY + j) - zs.qz[j];
+    __syncthreads();
+    project_z(P, nZ, zs.rz, zs.tz);
+    if (mode == 0) {
+        precond_z(P, nZ, zs.rz, zs.zz);
+        project_z(P, nZ, zs.zz, zs.tz);
+        for (int j = threadIdx.x; j < nZ; j += blockDim.x) zs.pz[j] = zs.zz[j];
+        __syncthreads();
+    }
+    publish_partials<T, 2>(part, partials);
+    if (!grid_sync(bar)) { status = 5; goto done; }
+    gather_partials<T, 2>(partials, part);
+    {
+        T rz = part[0] + (mode == 0 ? smem_dot(zs.rz, zs.zz, nZ) : T(0));
+        rr = part[1] + smem_dot(zs.rz, zs.rz, nZ);
+        if (mode == 1) {
+            if (blockIdx.x == 0)
+                for (int j = threadIdx.x; j < nZ; j += blockDim.x) r[nY + j] = zs.rz[j];
+            status = 0;
+            goto done;
+        }
+        for (;;) {
+            if ((double)rr <= tol2) { status = 0; break; }
+            if (it >= maxit) { status = 3; break; }
+            // q = K p
+            T pq_part = T(0);
+            if (!igm_apply(A, P, fixy, p, zs.pz, q, zs.qz, zs, bar, pq_part)) { status = 5; break; }
+            pq1[0] = pq_part;
+            publish_partials<T, 1>(pq1, partials + 2 * gridDim.x);
+            if (!grid_sync(bar)) { status = 5; break; }
+            gather_partials<T, 1>(partials + 2 * gridDim.x, pq1);
+            igm_apply_z(A, P, zs.pz, zs.qz, zs);
+            T pq = pq1[0] + smem_dot(zs.pz, zs.qz, nZ);
+            if (!(pq > T(0))) { status = 4; break; }
+            T alpha = rz / pq;
+            part[0] = T(0);
+            part[1] = T(0);
+            for (int j = t0; j < nY; j += stride) {
+                T rj = r[j] - alpha * q[j];
+                x[j] += alpha * p[j];
+                r[j] = rj;
+                T zj = minvy[j] * rj;
+                z[j] = zj;
+                part[0] += rj * zj;
+                part[1] += rj * rj;
+            }
+            for (int j = threadIdx.x; j < nZ; j += blockDim.x) {
+                zs.xz[j] += alpha * zs.pz[j];
+                zs.rz[j] -= alpha * zs.qz[j];
+            }
+            __syncthreads();
+            precond_z(P, nZ, zs.rz, zs.zz);
+            project_z(P, nZ, zs.zz, zs.tz);
+            publish_partials<T, 2>(part, partials + 3 * gridDim.x);
+            if (!grid_sync(bar)) { status = 5; break; }
+            gather_partials<T, 2>(partials + 3 * gridDim.x, part);
+            T rz_new = part[0] + smem_dot(zs.rz, zs.zz, nZ);
+            rr = part[1] + smem_dot(zs.rz, zs.rz, nZ);
+            if (rr != rr) { status = 4; break; }
+            T beta = rz_new / rz;
+            rz = rz_new;
+            for (int j = t0; j < nY; j += stride) p[j] = z[j] + beta * p[j];
+            for (int j = threadIdx.x; j < nZ; j += blockDim.x) zs.pz[j] = zs.zz[j] + beta * zs.pz[j];
+            __syncthreads();
+            it++;
+            if (!grid_sync(bar)) { status = 5; break; }
+        }
+        if (blockIdx.x == 0)
+            for (int j = threadIdx.x; j < nZ; j += blockDim.x) x[nY + j] = zs.xz[j];
+    }
+done:
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        out[0] = status;
+        out[1] = it;
+        reinterpret_cast<double*>(out + 4)[0] = (double)rr;
+    }
+}
+
+// ------------------------------------------------------------------------ set-up kernels
+// Per-face hat-function gradients in the face frame (parameterization_integ.ipp:11-24):
+// g_j = n x (P_{j+2} - P_{j+1}) / (2A); grad[6f + 2j] = g_j . bX, grad[6f + 2j + 1] = g_j . bY.
+__global__ void face_gradients(int nF, const int* __restrict__ cutF, const double* __restrict__ V, double* grad) {
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nF; f += gridDim.x * blockDim.x) {
+        double P[3][3];
+        for (int j = 0; j < 3; j++)
+            for (int k = 0; k < 3; k++) P[j][k] = V[3 * cutF[3 * f + j] + k];
+        double x[3], t[3], n[3];
+        for (int k = 0; k < 3; k++) { x[k] = P[1][k] - P[0][k]; t[k] = -(P[0][k] - P[2][k]); }
+        n[0] = x[1] * t[2] - x[2] * t[1];
+        n[1] = x[2] * t[0] - x[0] * t[2];
+        n[2] = x[0] * t[1] - x[1] * t[0];
+        double nn = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        double xn = sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+        double area = nn * 0.5;
+        double un[3] = {n[0] / nn, n[1] / nn, n[2] / nn};
+        double bx[3] = {x[0] / xn, x[1] / xn, x[2] / xn};
+        double c[3];   // -(x cross n)
+        c[0] = -(x[1] * n[2] - x[2] * n[1]);
+        c[1] = -(x[2] * n[0] - x[0] * n[2]);
+        c[2] = -(x[0] * n[1] - x[1] * n[0]);
+        double cn = sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+        double by[3] = {c[0] / cn, c[1] / cn, c[2] / cn};
+        for (int j = 0; j < 3; j++) {
+            double e[3];
+            for (int k = 0; k < 3; k++) e[k] = P[(j + 2) % 3][k] - P[(j + 1) % 3][k];
+            double g[3];
+            g[0] = (un[1] * e[2] - un[2] * e[1]) / (area * 2);
+            g[1] = (un[2] * e[0] - un[0] * e[2]) / (area * 2);
+            g[2] = (un[0] * e[1] - un[1] * e[0]) / (area * 2);
+            grad[6 * f + 2 * j] = g[0] * bx[0] + g[1] * bx[1] + g[2] * bx[2];
+            grad[6 * f + 2 * j + 1] = g[0] * by[0] + g[1] * by[1] + g[2] * by[2];
+        }
+    }
+}
+
+// Stiffness row of cut vertex c gathered from its faces (ascending face ids), entries sorted
+// by column and written into the padded CSR row; padding entries are (c, 0).  Deterministic.
+__global__ void assemble_stiffness(int nCut, const int* __restrict__ vf_ptr, const int* __restrict__ vf_face,
+                                   const int* __restrict__ cutF, const double* __restrict__ grad,
+                                   const int* __restrict__ s_ptr, int* s_col, double* s_val, float* s_val32,
+                                   double* s_diag) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nCut; c += gridDim.x * blockDim.x) {
+        int cols[kMaxFaceDeg + 2];
+        double vals[kMaxFaceDeg + 2];
+        int cnt = 0;
+        for (int k = vf_ptr[c]; k < vf_ptr[c + 1]; k++) {
+            int f = vf_face[k];
+            int a = cutF[3 * f] == c ? 0 : (cutF[3 * f + 1] == c ? 1 : 2);
+            double ga0 = grad[6 * f + 2 * a], ga1 = grad[6 * f + 2 * a + 1];
+            for (int j = 0; j < 3; j++) {
+                int bcol = cutF[3 * f + j];
+                double v = ga0 * grad[6 * f + 2 * j] + ga1 * grad[6 * f + 2 * j + 1];
+                int pos = -1;
+                for (int q = 0; q < cnt; q++) if (cols[q] == bcol) { pos = q; break; }
+                if (pos < 0) {
+                    if (cnt < kMaxFaceDeg + 2) { cols[cnt] = bcol; vals[cnt] = v; cnt++; }
+                } else {
+                    vals[pos] += v;
+                }
+            }
+        }
+        for (int i = 1; i < cnt; i++) {   // insertion sort by column
+            int kc = cols[i];
+            double kv = vals[i];
+            int j = i - 1;
+            while (j >= 0 && cols[j] > kc) { cols[j + 1] = cols[j]; vals[j + 1] = vals[j]; j--; }
+            cols[j + 1] = kc;
+            vals[j + 1] = kv;
+        }
+        int base = s_ptr[c], cap = s_ptr[c + 1] - base;
+        double dg = 0;
+        for (int i = 0; i < cap; i++) {
+            int col = i < cnt ? cols[i] : c;
+            double v = i < cnt ? vals[i] : 0.0;
+            s_col[base + i] = col;
+            s_val[base + i] = v;
+            s_val32[base + i] = (float)v;
+            if (i < cnt && col == c) dg = v;
+        }
+        s_diag[c] = dg;
+    }
+}
+
+// Per cut vertex: hb[2c + k] = sum_f g_c . (F[f,k] - F[f,k+n]) for k < n (N = 4, n = 2).
+__global__ void cut_loads(int nCut, const int* __restrict__ vf_ptr, const int* __restrict__ vf_face,
+                          const int* __restrict__ cutF, const double* __restrict__ grad, const double* __restrict__ Ff,
+                          double* hb) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nCut; c += gridDim.x * blockDim.x) {
+        double h[4] = {0, 0, 0, 0};
+        for (int k = vf_ptr[c]; k < vf_ptr[c + 1]; k++) {
+            int f = vf_face[k];
+            int a = cutF[3 * f] == c ? 0 : (cutF[3 * f + 1] == c ? 1 : 2);
+            double gx = grad[6 * f + 2 * a], gy = grad[6 * f + 2 * a + 1];
+            for (int fn = 0; fn < 4; fn++) h[fn] += gx * Ff[8 * f + 2 * fn] + gy * Ff[8 * f + 2 * fn + 1];
+        }
+        hb[2 * c] = h[0] - h[2];
+        hb[2 * c + 1] = h[1] - h[3];
+    }
+}
+
+// Reduced right-hand side, free part: b_y = scale * W_y^T hb + shift * prev_y ; J part -> XbJ.
+__global__ void rhs_reduce(int nY, int nJ, const int* __restrict__ yt_ptr, const int* __restrict__ yt_row,
+                           const double* __restrict__ yt_val, const int* __restrict__ jt_ptr, const int* __restrict__ jt_row,
+                           const double* __restrict__ jt_val, const double* __restrict__ hb, double scale, double shift,
+                           const double* __restrict__ prev, const unsigned char* __restrict__ fixy, double* b, double* XbJ) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nY; j += gridDim.x * blockDim.x) {
+        double acc = 0;
+        for (int e = yt_ptr[j]; e < yt_ptr[j + 1]; e++) acc += yt_val[e] * hb[yt_row[e]];
+        b[j] = fixy && fixy[j] ? 0.0 : scale * acc + (prev ? shift * prev[j] : 0.0);
+    }
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nJ; s += gridDim.x * blockDim.x) {
+        double acc = 0;
+        for (int e = jt_ptr[s]; e < jt_ptr[s + 1]; e++) acc += jt_val[e] * hb[jt_row[e]];
+        XbJ[s] = acc;
+    }
+}
+
+// z part of the right-hand side (one block): b_z = scale * USmall^T XbJ + shift * prev_z
+__global__ void rhs_reduce_z(int nY, int nZ, int nJ, const double* __restrict__ Us, const double* __restrict__ XbJ,
+                             double scale, double shift, const double* __restrict__ prev, double* b) {
+    for (int j = threadIdx.x; j < nZ; j += blockDim.x) {
+        double acc = 0;
+        for (int s = 0; s < nJ; s++) acc += Us[(size_t)s * nZ + j] * XbJ[s];
+        b[nY + j] = scale * acc + (prev ? shift * prev[nY + j] : 0.0);
+    }
+}
+
+// Jacobi diagonal of the free block: 2 scale sum val^2 S_cc + shift.
+__global__ void jacobi_y(int nY, const int* __restrict__ yt_ptr, const int* __restrict__ yt_row,
+                         const double* __restrict__ yt_val, const double* __restrict__ s_diag, double scale, double shift,
+                         double* minv64, float* minv32) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nY; j += gridDim.x * blockDim.x) {
+        double acc = 0;
+        for (int e = yt_ptr[j]; e < yt_ptr[j + 1]; e++) acc += yt_val[e] * yt_val[e] * s_diag[yt_row[e] >> 1];
+        double d = 2 * scale * acc + shift;
+        double m = d > 0 ? 1.0 / d : 1.0;
+        minv64[j] = m;
+        minv32[j] = (float)m;
+    }
+}
+
+// X (full variables) from xs: free -> y, constrained -> USmall z.  Full layout for fullx.
+__global__ void expand_full(int nFull, const int* __restrict__ full2y, const int* __restrict__ full2j, int nY, int nZ,
+                            const double* __restrict__ Us, const double* __restrict__ xs, double* X) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nFull; i += gridDim.x * blockDim.x) {
+        int y = full2y[i];
+        double v;
+        if (y >= 0) {
+            v = xs[y];
+        } else {
+            int s = full2j[i];
+            v = 0;
+            for (int j = 0; j < nZ; j++) v += Us[(size_t)s * nZ + j] * xs[nY + j];
+        }
+        X[i] = v;
+    }
+}
+
+// Greedy rounding choice (iter_rounding_loop.h:29-43), one block: d_i = |X - round X| over the
+// left indices; d < 1e-9 counts as 0 (round-off ties); first minimum wins.
+__global__ void round_argmin(int nLeft, const int* __restrict__ left, const int* __restrict__ full2y,
+                             const int* __restrict__ full2j, int nY, int nZ, const double* __restrict__ Us,
+                             const double* __restrict__ xs, double* out /* [pos, d, X, second d] */) {
+    __shared__ double sd[kBlock];
+    __shared__ int si[kBlock];
+    __shared__ double sX[kBlock];
+    __shared__ double s2[kBlock];
+    double bd = 1e300, b2 = 1e300, bX = 0;
+    int bi = 0x7fffffff;
+    for (int t = threadIdx.x; t < nLeft; t += blockDim.x) {
+        int i = left[t];
+        int y = full2y[i];
+        double X;
+        if (y >= 0) X = xs[y];
+        else {
+            int s = full2j[i];
+            X = 0;
+            for (int j = 0; j < nZ; j++) X += Us[(size_t)s * nZ + j] * xs[nY + j];
+        }
+        double d = fabs(X - round(X));
+        if (d < 1e-9) d = 0.0;
+        if (d < bd || (d == bd && t < bi)) { b2 = bd; bd = d; bi = t; bX = X; }
+        else if (d < b2) b2 = d;
+    }
+    sd[threadIdx.x] = bd; si[threadIdx.x] = bi; sX[threadIdx.x] = bX; s2[threadIdx.x] = b2;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            double d1 = sd[threadIdx.x], d2 = sd[threadIdx.x + w];
+            int i1 = si[threadIdx.x], i2 = si[threadIdx.x + w];
+            double sec = fmin(s2[threadIdx.x], s2[threadIdx.x + w]);
+            if (d2 < d1 || (d2 == d1 && i2 < i1)) {
+                sec = fmin(sec, d1);
+                sd[threadIdx.x] = d2; si[threadIdx.x] = i2; sX[threadIdx.x] = sX[threadIdx.x + w];
+            } else {
+                sec = fmin(sec, d2);
+            }
+            s2[threadIdx.x] = sec;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) { out[0] = (double)si[0]; out[1] = sd[0]; out[2] = sX[0]; out[3] = s2[0]; }
+}
+
+// NI-LM field block (Gauss-Newton with the diagonal field block eliminated exactly):
+// f* = (wI^2 length grad(x) + wC^2 F2) / (wI^2 + wC^2), grad over the N functions.
+__global__ void lm_field_target(int nF, const int* __restrict__ cutF, const double* __restrict__ grad,
+                                const double* __restrict__ U /* 2*nCut */, const double* __restrict__ F2, double length,
+                                double wI2, double wC2, double* Fout) {
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nF; f += gridDim.x * blockDim.x) {
+        double g[2][2] = {{0, 0}, {0, 0}};
+        for (int a = 0; a < 3; a++) {
+            int c = cutF[3 * f + a];
+            double gx = grad[6 * f + 2 * a], gy = grad[6 * f + 2 * a + 1];
+            for (int k = 0; k < 2; k++) { g[k][0] += gx * U[2 * c + k]; g[k][1] += gy * U[2 * c + k]; }
+        }
+        for (int k = 0; k < 4; k++) {
+            double sgn = k < 2 ? 1.0 : -1.0;
+            for (int comp = 0; comp < 2; comp++) {
+                double gg = sgn * g[k & 1][comp];
+                Fout[8 * f + 2 * k + comp] = (wI2 * length * gg + wC2 * F2[8 * f + 2 * k + comp]) / (wI2 + wC2);
+            }
+        }
+    }
+}
+
+// U = W X for FP64 xs (used by lm_field_target).
+__global__ void gather_U(int nCut, const int* __restrict__ w_ptr, const int* __restrict__ w_tag,
+                         const double* __restrict__ w_val, const double* __restrict__ xs, const double* __restrict__ XJ,
+                         double* U) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < 2 * nCut; r += gridDim.x * blockDim.x) {
+        double acc = 0;
+        for (int e = w_ptr[r]; e < w_ptr[r + 1]; e++) {
+            int tag = w_tag[e];
+            acc += w_val[e] * (tag >= 0 ? xs[tag] : XJ[-1 - tag]);
+        }
+        U[r] = acc;
+    }
+}
+
+__global__ void xj_from_z(int nJ, int nY, int nZ, const double* __restrict__ Us, const double* __restrict__ xs, double* XJ) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nJ; s += gridDim.x * blockDim.x) {
+        double v = 0;
+        for (int j = 0; j < nZ; j++) v += Us[(size_t)s * nZ + j] * xs[nY + j];
+        XJ[s] = v;
+    }
+}
+
+__global__ void to_f32(int n, const double* __restrict__ a, float* b) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = (float)a[i];
+}
+__global__ void add_f32(int n, const float* __restrict__ e, double* x) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] += (double)e[i];
+}
+__global__ void dot_partial(int n, const double* __restrict__ a, const double* __restrict__ b, double* partials) {
+    double v[1] = {0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[0] += a[i] * b[i];
+    publish_partials<double, 1>(v, partials);
+}
+__global__ void finalize1(const double* partials, int nb, double* out) {
+    double v[1] = {0};
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) v[0] += partials[i];
+    block_sum<double, 1>(v);
+    if (threadIdx.x == 0) out[0] = v[0];
+}
+
+}  // namespace mtk
+
+using namespace mtk;
+
+namespace {
+
+struct Igm {
+    mtk_ctx* c = nullptr;
+    cudaStream_t st = nullptr;
+    int nF = 0, nCut = 0, nY = 0, nZ = 0, nJ = 0, nFull = 0, nRed = 0;
+    double length = 0;
+    // host copies needed by the loop
+    std::vector<int> full2y, full2j;
+    std::vector<double> USmall;      // nJ x nZ
+    // device topology / operators
+    DBuf<int> cutF, vf_ptr, vf_face, s_ptr, s_col, w_ptr, w_tag, yt_ptr, yt_row, jt_ptr, jt_row, d_full2y, d_full2j, left;
+    DBuf<double> cutV, grad, s_val, s_diag, w_val, yt_val, jt_val, Us, F2, Fsi, hb, XbJ, U, Qc, XoJ, minvy, Mz, Qz;
+    DBuf<float> s_val32, w_val32, yt_val32, jt_val32, Us32, minvy32, Mz32, Qz32, U32, Qc32, XoJ32;
+    DBuf<double> xs, bsys, r64, z64, p64, q64, prev, Xfull, XJ64, scratch;
+    DBuf<float> r32, e32, z32, p32, q32;
+    DBuf<unsigned char> fixy;
+    std::vector<unsigned char> h_fixy;
+    int kq = 0;
+    size_t smem64 = 0, smem32 = 0;
+
+    IgmOp<double> op64(double scale, double shift) {
+        return {nCut, nY, nZ, nJ, w_ptr.p, w_tag.p, w_val.p, s_ptr.p, s_col.p, s_val.p, yt_ptr.p, yt_row.p, yt_val.p,
+                jt_ptr.p, jt_row.p, jt_val.p, Us.p, scale, shift, U.p, Qc.p, XoJ.p};
+    }
+    IgmOp<float> op32(double scale, double shift) {
+        return {nCut, nY, nZ, nJ, w_ptr.p, w_tag.p, w_val32.p, s_ptr.p, s_col.p, s_val32.p, yt_ptr.p, yt_row.p, yt_val32.p,
+                jt_ptr.p, jt_row.p, jt_val32.p, Us32.p, (float)scale, (float)shift, U32.p, Qc32.p, XoJ32.p};
+    }
+
+    template <typename T>
+    int run_pcg(IgmOp<T> A, ZProj<T> P, const T* minv, const T* b, T* x, T* r, T* z, T* p, T* q, double tol2, int maxit,
+                int mode, size_t smem, long long* iters, double* rr_out) {
+        auto kern = igm_pcg<T>;
+        MTK_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int per_sm = 0;
+        MTK_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, smem));
+        if (per_sm < 1) { mtk_set_last_error("IGM solver does not fit on an SM", __FILE__, __LINE__); return MTK_ERR_CUDA; }
+        per_sm = std::min(per_sm, 4);
+        int grid = std::min(c->num_sms * per_sm, c->partial_blocks);
+        const unsigned char* fx = fixy.p;
+        T* partials = reinterpret_cast<T*>(c->partials);
+        GridBarrier bar = barrier_of(c);
+        int* out = c->dev_int;
+        void* params[] = {&A, &P, (void*)&fx, (void*)&minv, (void*)&b, (void*)&x, (void*)&r, (void*)&z, (void*)&p,
+                          (void*)&q, (void*)&partials, &bar, &tol2, &maxit, &mode, (void*)&out};
+        MTK_TRY(reset_barrier(c));
+        MTK_CUDA_TRY(cudaLaunchCooperativeKernel(reinterpret_cast<void*>(kern), dim3(grid), dim3(kBlock), params, smem, st));
+        c->kernels++;
+        MTK_CUDA_TRY(cudaMemcpyAsync(c->h_int, c->dev_int, 8 * sizeof(int), cudaMemcpyDeviceToHost, st));
+        MTK_CUDA_TRY(cudaStreamSynchronize(st));
+        if (iters) *iters += c->h_int[1];
+        if (rr_out) *rr_out = reinterpret_cast<double*>(c->h_int + 4)[0];
+        int s = c->h_int[0];
+        if (s == 5) return MTK_ERR_TIMEOUT;
+        if (s == 4) return MTK_ERR_BREAKDOWN;
+        if (s == 3) return MTK_ERR_NOT_CONVERGED;
+        return MTK_OK;
+    }
+
+    int grid() const { return stream_grid(c); }
+
+    // b = scale * UFull^T W^T hb(F) + shift * prev   (prev may be null)
+    int build_rhs(const double* Fface, double scale, double shift, const double* prevx, double* b) {
+        cut_loads<<<grid(), kBlock, 0, st>>>(nCut, vf_ptr.p, vf_face.p, cutF.p, grad.p, Fface, hb.p);
+        rhs_reduce<<<grid(), kBlock, 0, st>>>(nY, nJ, yt_ptr.p, yt_row.p, yt_val.p, jt_ptr.p, jt_row.p, jt_val.p, hb.p, scale,
+                                              shift, prevx, fixy.p, b, XbJ.p);
+        rhs_reduce_z<<<1, kBlock, 0, st>>>(nY, nZ, nJ, Us.p, XbJ.p, scale, shift, prevx, b);
+        c->kernels += 3;
+        MTK_CUDA_TRY(cudaGetLastError());
+        return MTK_OK;
+    }
+
+    int dot(const double* a, const double* b, int n, double* out) {
+        int G = grid();
+        dot_partial<<<G, kBlock, 0, st>>>(n, a, b, c->partials);
+        finalize1<<<1, kBlock, 0, st>>>(c->partials, G, c->scalars);
+        c->kernels += 2;
+        MTK_CUDA_TRY(cudaMemcpyAsync(c->h_scalars, c->scalars, sizeof(double), cudaMemcpyDeviceToHost, st));
+        MTK_CUDA_TRY(cudaStreamSynchronize(st));
+        *out = c->h_scalars[0];
+        return MTK_OK;
+    }
+
+    // Solve K x = b (projected, x feasible on entry) to ||P(b - K x)|| <= tol ||P b||.
+    int solve(double scale, double shift, const double* b, double* x, const mtk_solve_opts& o, mtk_stats* stats,
+              double* rel_out) {
+        long long iters = 0, refines = 0;
+        double rr = 0, bb = 0;
+        // ||P b||^2: residual mode with x = 0 gives P(b)
+        MTK_CUDA_TRY(cudaMemsetAsync(scratch.p, 0, sizeof(double) * nRed, st));
+        MTK_TRY(run_pcg<double>(op64(scale, shift), ZProj<double>{kq, Qz.p, Mz.p}, minvy.p, b, scratch.p, r64.p, z64.p,
+                                p64.p, q64.p, 0.0, 0, 1, smem64, nullptr, &bb));
+        const double goal2 = o.tol * o.tol * bb;
+        if (o.precision == MTK_PREC_FP64) {
+            int s = run_pcg<double>(op64(scale, shift), ZProj<double>{kq, Qz.p, Mz.p}, minvy.p, b, x, r64.p, z64.p, p64.p,
+                                    q64.p, goal2, o.max_iter, 0, smem64, &iters, &rr);
+            if (s != MTK_OK) return s;
+            MTK_TRY(run_pcg<double>(op64(scale, shift), ZProj<double>{kq, Qz.p, Mz.p}, minvy.p, b, x, r64.p, z64.p, p64.p,
+                                    q64.p, 0.0, 0, 1, smem64, nullptr, &rr));
+            refines++;
+        } else {
+            MTK_TRY(run_pcg<double>(op64(scale, shift), ZProj<double>{kq, Qz.p, Mz.p}, minvy.p, b, x, r64.p, z64.p, p64.p,
+                                    q64.p, 0.0, 0, 1, smem64, nullptr, &rr));
+            refines++;
+            int outer = 0;
+            while (rr > goal2) {
+                if (outer >= o.max_refine) return MTK_ERR_NOT_CONVERGED;
+                outer++;
+                double itol = o.inner_tol;
+                double need = std::sqrt(goal2 / rr) * 0.5;
+                if (need > itol) itol = need;
+                to_f32<<<grid(), kBlock, 0, st>>>(nRed, r64.p, r32.p);
+                MTK_CUDA_TRY(cudaMemsetAsync(e32.p, 0, sizeof(float) * nRed, st));
+                c->kernels++;
+                int s = run_pcg<float>(op32(scale, shift), ZProj<float>{kq, Qz32.p, Mz32.p}, minvy32.p, r32.p, e32.p,
+                                       z32.p /*r*/, p32.p /*z*/, q32.p /*p*/, reinterpret_cast<float*>(Xfull.p) /*q*/,
+                                       itol * itol * rr, o.max_iter, 0, smem32, &iters, nullptr);
+                if (s == MTK_ERR_TIMEOUT || s == MTK_ERR_BREAKDOWN) return s;
+                add_f32<<<grid(), kBlock, 0, st>>>(nRed, e32.p, x);
+                c->kernels++;
+                MTK_TRY(run_pcg<double>(op64(scale, shift), ZProj<double>{kq, Qz.p, Mz.p}, minvy.p, b, x, r64.p, z64.p,
+                                        p64.p, q64.p, 0.0, 0, 1, smem64, nullptr, &rr));
+                refines++;
+            }
+        }
+        double rel = bb > 0 ? std::sqrt(rr / bb) : 0.0;
+        if (rel_out) *rel_out = rel;
+        if (stats) {
+            stats->pcg_iters += iters;
+            stats->solves += 1;
+            stats->refinements += refines;
+            stats->spmv_calls += iters + refines + 1;
+            if (rel > stats->max_rel_residual) stats->max_rel_residual = rel;
+        }
+        return MTK_OK;
+    }
+};
+
+// Orthonormal rows (two-pass Gram-Schmidt); returns false if `row` is dependent.
+bool add_orthonormal(std::vector<std::vector<double>>& Q, std::vector<double> row) {
+    double n0 = 0;
+    for (double v : row) n0 += v * v;
+    n0 = std::sqrt(n0);
+    if (n0 == 0) return false;
+    for (int pass = 0; pass < 2; pass++)
+        for (auto& q : Q) {
+            double d = 0;
+            for (size_t j = 0; j < row.size(); j++) d += q[j] * row[j];
+            for (size_t j = 0; j < row.size(); j++) row[j] -= d * q[j];
+        }
+    double n = 0;
+    for (double v : row) n += v * v;
+    n = std::sqrt(n);
+    if (n <= 1e-10 * n0) return false;
+    for (double& v : row) v /= n;
+    Q.push_back(std::move(row));
+    return true;
+}
+
+// Dense Cholesky inverse of an SPD matrix (n x n, row-major); returns false if not SPD.
+bool spd_inverse(std::vector<double>& A, int n) {
+    std::vector<double> L(A);
+    for (int j = 0; j < n; j++) {
+        double d = L[(size_t)j * n + j];
+        for (int k = 0; k < j; k++) d -= L[(size_t)j * n + k] * L[(size_t)j * n + k];
+        if (!(d > 0)) return false;
+        d = std::sqrt(d);
+        L[(size_t)j * n + j] = d;
+        for (int i = j + 1; i < n; i++) {
+            double s = L[(size_t)i * n + j];
+            for (int k = 0; k < j; k++) s -= L[(size_t)i * n + k] * L[(size_t)j * n + k];
+            L[(size_t)i * n + j] = s / d;
+        }
+    }
+    // inverse via solving L L^T X = I column by column
+    std::vector<double> inv((size_t)n * n, 0.0), y(n);
+    for (int col = 0; col < n; col++) {
+        for (int i = 0; i < n; i++) {
+            double s = i == col ? 1.0 : 0.0;
+            for (int k = 0; k < i; k++) s -= L[(size_t)i * n + k] * y[k];
+            y[i] = s / L[(size_t)i * n + i];
+        }
+        for (int i = n - 1; i >= 0; i--) {
+            double s = y[i];
+            for (int k = i + 1; k < n; k++) s -= L[(size_t)k * n + i] * inv[(size_t)k * n + col];
+            inv[(size_t)i * n + col] = s / L[(size_t)i * n + i];
+        }
+    }
+    A.swap(inv);
+    return true;
+}
+
+}  // namespace
+
+extern "C" int mtk_iterative_rounding(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts_in, double* fullx,
+                                      int32_t* fix_order, int32_t* fix_vals, int32_t* n_fixed, double* x_naive,
+                                      mtk_stats* stats) {
+    if (!c || !d || !fullx) return MTK_ERR_BAD_INPUT;
+    if (d->N != 4 || d->n != 2) { mtk_set_last_error("only N = 4 (n = 2) is supported", __FILE__, __LINE__); return MTK_ERR_BAD_INPUT; }
+    if (d->nF <= 0 || d->nCut <= 0 || d->nFull <= 0 || !d->cutF || !d->cutV || !d->w_ptr || !d->full2y || !d->F2)
+        return MTK_ERR_BAD_INPUT;
+    mtk_solve_opts o;
+    mtk_default_opts(&o);
+    if (opts_in) o = *opts_in;
+    MTK_CUDA_TRY(cudaSetDevice(c->device));
+    auto t_start = std::chrono::steady_clock::now();
+    Igm S;
+    S.c = c;
+    S.st = c->stream;
+    cudaStream_t st = c->stream;
+    const int nF = d->nF, nCut = d->nCut, nFull = d->nFull, nJ = d->nJ, nZ = d->nZ;
+    S.nF = nF; S.nCut = nCut; S.nFull = nFull; S.nJ = nJ; S.nZ = nZ; S.length = d->length;
+    // ---- index maps
+    S.full2y.assign(d->full2y, d->full2y + nFull);
+    S.full2j.assign(nFull, -1);
+    int nY = 0;
+    for (int i = 0; i < nFull; i++) if (S.full2y[i] >= 0) nY = std::max(nY, S.full2y[i] + 1);
+    for (int s = 0; s < nJ; s++) {
+        int i = d->uniqueJ[s];
+        if (i < 0 || i >= nFull || S.full2y[i] >= 0) return MTK_ERR_BAD_INPUT;
+        S.full2j[i] = s;
+    }
+    std::vector<int> y2full(nY, -1);
+    for (int i = 0; i < nFull; i++) if (S.full2y[i] >= 0) y2full[S.full2y[i]] = i;
+    for (int j = 0; j < nY; j++) if (y2full[j] < 0) return MTK_ERR_BAD_INPUT;
+    S.nY = nY;
+    S.nRed = nY + nZ;
+    S.USmall.assign(d->USmall, d->USmall + (size_t)nJ * nZ);
+    for (int i = 0; i < 3 * nF; i++) if (d->cutF[i] < 0 || d->cutF[i] >= nCut) return MTK_ERR_BAD_INPUT;
+    // ---- W with tags, and its transpose split into y / J parts
+    const int nW = 2 * nCut;
+    const int nnzW = d->w_ptr[nW];
+    std::vector<int> tag(nnzW);
+    for (int e = 0; e < nnzW; e++) {
+        int i = d->w_idx[e];
+        if (i < 0 || i >= nFull) return MTK_ERR_BAD_INPUT;
+        tag[e] = S.full2y[i] >= 0 ? S.full2y[i] : -1 - S.full2j[i];
+    }
+    std::vector<int> yptr(nY + 1, 0), jptr(nJ + 1, 0);
+    for (int e = 0; e < nnzW; e++) { if (tag[e] >= 0) yptr[tag[e] + 1]++; else jptr[-tag[e]]++; }
+    for (int j = 0; j < nY; j++) yptr[j + 1] += yptr[j];
+    for (int s = 0; s < nJ; s++) jptr[s + 1] += jptr[s];
+    std::vector<int> yrow(yptr[nY]), jrow(jptr[nJ]);
+    std::vector<double> yval(yptr[nY]), jval(jptr[nJ]);
+    {
+        std::vector<int> fy(yptr.begin(), yptr.end() - 1), fj(jptr.begin(), jptr.end() - 1);
+        for (int r = 0; r < nW; r++)
+            for (int e = d->w_ptr[r]; e < d->w_ptr[r + 1]; e++) {
+                if (tag[e] >= 0) { int p = fy[tag[e]]++; yrow[p] = r; yval[p] = d->w_val[e]; }
+                else { int s = -1 - tag[e]; int p = fj[s]++; jrow[p] = r; jval[p] = d->w_val[e]; }
+            }
+    }
+    // ---- cut vertex -> faces and padded stiffness rows
+    std::vector<int> vptr(nCut + 1, 0);
+    for (int i = 0; i < 3 * nF; i++) vptr[d->cutF[i] + 1]++;
+    int maxdeg = 0;
+    for (int v = 0; v < nCut; v++) maxdeg = std::max(maxdeg, vptr[v + 1]);
+    if (maxdeg > kMaxFaceDeg) { mtk_set_last_error("vertex with more than 30 faces", __FILE__, __LINE__); return MTK_ERR_BAD_INPUT; }
+    std::vector<int> sptr(nCut + 1, 0);
+    for (int v = 0; v < nCut; v++) sptr[v + 1] = sptr[v] + vptr[v + 1] + 2;
+    for (int v = 0; v < nCut; v++) vptr[v + 1] += vptr[v];
+    std::vector<int> vface(vptr[nCut]);
+    {
+        std::vector<int> fill(vptr.begin(), vptr.end() - 1);
+        for (int f = 0; f < nF; f++) for (int j = 0; j < 3; j++) vface[fill[d->cutF[3 * f + j]]++] = f;
+    }
+    // ---- uploads
+    MTK_TRY(S.cutF.upload(d->cutF, 3 * (size_t)nF, st));
+    MTK_TRY(S.cutV.upload(d->cutV, 3 * (size_t)nCut, st));
+    MTK_TRY(S.vf_ptr.upload(vptr.data(), vptr.size(), st));
+    MTK_TRY(S.vf_face.upload(vface.data(), vface.size(), st));
+    MTK_TRY(S.s_ptr.upload(sptr.data(), sptr.size(), st));
+    MTK_TRY(S.s_col.alloc(sptr[nCut])); MTK_TRY(S.s_val.alloc(sptr[nCut])); MTK_TRY(S.s_val32.alloc(sptr[nCut]));
+    MTK_TRY(S.s_diag.alloc(nCut));
+    MTK_TRY(S.w_ptr.upload(d->w_ptr, nW + 1, st));
+    MTK_TRY(S.w_tag.upload(tag.data(), nnzW, st));
+    MTK_TRY(S.w_val.upload(d->w_val, nnzW, st));
+    std::vector<float> wv32(d->w_val, d->w_val + nnzW), yv32(yval.begin(), yval.end()), jv32(jval.begin(), jval.end());
+    MTK_TRY(S.w_val32.upload(wv32.data(), nnzW, st));
+    MTK_TRY(S.yt_ptr.upload(yptr.data(), yptr.size(), st));
+    MTK_TRY(S.yt_row.upload(yrow.data(), yrow.size(), st));
+    MTK_TRY(S.yt_val.upload(yval.data(), yval.size(), st));
+    MTK_TRY(S.yt_val32.upload(yv32.data(), yv32.size(), st));
+    MTK_TRY(S.jt_ptr.upload(jptr.data(), jptr.size(), st));
+    MTK_TRY(S.jt_row.upload(jrow.data(), jrow.size(), st));
+    MTK_TRY(S.jt_val.upload(jval.data(), jval.size(), st));
+    MTK_TRY(S.jt_val32.upload(jv32.data(), jv32.size(), st));
+    MTK_TRY(S.Us.upload(S.USmall.data(), S.USmall.size(), st));
+    std::vector<float> us32(S.USmall.begin(), S.USmall.end());
+    MTK_TRY(S.Us32.upload(us32.data(), us32.size(), st));
+    MTK_TRY(S.d_full2y.upload(S.full2y.data(), nFull, st));
+    MTK_TRY(S.d_full2j.upload(S.full2j.data(), nFull, st));
+    MTK_TRY(S.F2.upload(d->F2, 8 * (size_t)nF, st));
+    MTK_TRY(S.Fsi.alloc(8 * (size_t)nF));
+    MTK_TRY(S.grad.alloc(6 * (size_t)nF));
+    MTK_TRY(S.hb.alloc(2 * (size_t)nCut)); MTK_TRY(S.XbJ.alloc(std::max(nJ, 1)));
+    MTK_TRY(S.U.alloc(2 * (size_t)nCut)); MTK_TRY(S.Qc.alloc(2 * (size_t)nCut)); MTK_TRY(S.XoJ.alloc(std::max(nJ, 1)));
+    MTK_TRY(S.U32.alloc(2 * (size_t)nCut)); MTK_TRY(S.Qc32.alloc(2 * (size_t)nCut)); MTK_TRY(S.XoJ32.alloc(std::max(nJ, 1)));
+    MTK_TRY(S.minvy.alloc(std::max(nY, 1))); MTK_TRY(S.minvy32.alloc(std::max(nY, 1)));
+    const int nRed = S.nRed;
+    MTK_TRY(S.xs.alloc(nRed)); MTK_TRY(S.bsys.alloc(nRed)); MTK_TRY(S.r64.alloc(nRed)); MTK_TRY(S.z64.alloc(nRed));
+    MTK_TRY(S.p64.alloc(nRed)); MTK_TRY(S.q64.alloc(nRed)); MTK_TRY(S.prev.alloc(nRed)); MTK_TRY(S.scratch.alloc(nRed));
+    MTK_TRY(S.Xfull.alloc(std::max(nFull, nRed)));
+    MTK_TRY(S.XJ64.alloc(std::max(nJ, 1)));
+    MTK_TRY(S.r32.alloc(nRed)); MTK_TRY(S.e32.alloc(nRed)); MTK_TRY(S.z32.alloc(nRed)); MTK_TRY(S.p32.alloc(nRed));
+    MTK_TRY(S.q32.alloc(nRed));
+    S.h_fixy.assign(std::max(nY, 1), 0);
+    MTK_TRY(S.fixy.upload(S.h_fixy.data(), S.h_fixy.size(), st));
+    const int nLeftCap = std::max(1, d->nSingular + d->nInteger);
+    MTK_TRY(S.left.alloc(nLeftCap));
+    // shared memory for the replicated z state: 6 nZ + 2 nJ values
+    S.smem64 = sizeof(double) * (6 * (size_t)nZ + 2 * (size_t)nJ + 8);
+    S.smem32 = sizeof(float) * (6 * (size_t)nZ + 2 * (size_t)nJ + 8);
+    if (S.smem64 > 200 * 1024) { mtk_set_last_error("constrained block too large for shared memory", __FILE__, __LINE__); return MTK_ERR_BAD_INPUT; }
+
+    const int G = S.grid();
+    MTK_CUDA_TRY(cudaEventRecord(c->ev_a, st));
+    face_gradients<<<G, kBlock, 0, st>>>(nF, S.cutF.p, S.cutV.p, S.grad.p);
+    assemble_stiffness<<<G, kBlock, 0, st>>>(nCut, S.vf_ptr.p, S.vf_face.p, S.cutF.p, S.grad.p, S.s_ptr.p, S.s_col.p,
+                                             S.s_val.p, S.s_val32.p, S.s_diag.p);
+    c->kernels += 2;
+    MTK_CUDA_TRY(cudaGetLastError());
+
+    // ---- dense z block of the normal matrix (host, FP64) for the block-Jacobi preconditioner:
+    //      K_zz = scale * USmall^T (2 W_J^T S W_J) USmall + shift I.  Only faces touching J matter.
+    std::vector<double> h_grad(6 * (size_t)nF);
+    std::vector<double> BJJ((size_t)nJ * nJ, 0.0);
+    if (nJ > 0) {
+        MTK_CUDA_TRY(cudaMemcpyAsync(h_grad.data(), S.grad.p, sizeof(double) * h_grad.size(), cudaMemcpyDeviceToHost, st));
+        MTK_CUDA_TRY(cudaStreamSynchronize(st));
+        std::vector<char> touchJ(nCut, 0);
+        for (int r = 0; r < nW; r++)
+            for (int e = d->w_ptr[r]; e < d->w_ptr[r + 1]; e++) if (tag[e] < 0) touchJ[r >> 1] = 1;
+        for (int f = 0; f < nF; f++) {
+            int cv[3] = {d->cutF[3 * f], d->cutF[3 * f + 1], d->cutF[3 * f + 2]};
+            if (!touchJ[cv[0]] && !touchJ[cv[1]] && !touchJ[cv[2]]) continue;
+            for (int a = 0; a < 3; a++)
+                for (int b = 0; b < 3; b++) {
+                    double sab = h_grad[6 * f + 2 * a] * h_grad[6 * f + 2 * b] + h_grad[6 * f + 2 * a + 1] * h_grad[6 * f + 2 * b + 1];
+                    for (int k = 0; k < 2; k++) {
+                        int ra = 2 * cv[a] + k, rb = 2 * cv[b] + k;
+                        for (int e1 = d->w_ptr[ra]; e1 < d->w_ptr[ra + 1]; e1++) {
+                            if (tag[e1] >= 0) continue;
+                            for (int e2 = d->w_ptr[rb]; e2 < d->w_ptr[rb + 1]; e2++) {
+                                if (tag[e2] >= 0) continue;
+                                BJJ[(size_t)(-1 - tag[e1]) * nJ + (-1 - tag[e2])] += 2.0 * d->w_val[e1] * sab * d->w_val[e2];
+                            }
+                        }
+                    }
+                }
+        }
+    }
+    auto build_zblock = [&](double scale, double shift, std::vector<double>& Kzz) {
+        Kzz.assign((size_t)nZ * nZ, 0.0);
+        std::vector<double> tmp((size_t)nJ * nZ, 0.0);   // BJJ * USmall
+        for (int a = 0; a < nJ; a++)
+            for (int b = 0; b < nJ; b++) {
+                double v = BJJ[(size_t)a * nJ + b];
+                if (v == 0) continue;
+                for (int j = 0; j < nZ; j++) tmp[(size_t)a * nZ + j] += v * S.USmall[(size_t)b * nZ + j];
+            }
+        for (int i = 0; i < nZ; i++)
+            for (int j = 0; j < nZ; j++) {
+                double s = 0;
+                for (int a = 0; a < nJ; a++) s += S.USmall[(size_t)a * nZ + i] * tmp[(size_t)a * nZ + j];
+                Kzz[(size_t)i * nZ + j] = scale * s + (i == j ? shift : 0.0);
+            }
+    };
+    // constraint state
+    std::vector<std::vector<double>> Qrows;          // orthonormal rows on z
+    std::vector<std::vector<double>> Arows;          // raw constraint rows on z
+    std::vector<double> Avals;
+    auto upload_constraints = [&](double scale, double shift) -> int {
+        // projector rows
+        S.kq = (int)Qrows.size();
+        std::vector<double> q((size_t)std::max(S.kq, 1) * std::max(nZ, 1), 0.0);
+        for (int a = 0; a < S.kq; a++) for (int j = 0; j < nZ; j++) q[(size_t)a * nZ + j] = Qrows[a][j];
+        MTK_TRY(S.Qz.upload(q.data(), q.size(), st));
+        std::vector<float> q32(q.begin(), q.end());
+        MTK_TRY(S.Qz32.upload(q32.data(), q32.size(), st));
+        // z-block preconditioner: inverse of (P K_zz P + Q^T Q) restricted, i.e. of K_zz on the
+        // complement plus identity on the constrained directions
+        if (nZ > 0) {
+            std::vector<double> Kzz;
+            build_zblock(scale, shift, Kzz);
+            std::vector<double> PK((size_t)nZ * nZ);
+            // P K P + Q^T Q (SPD when K is SPD on range(P))
+            std::vector<double> Pm((size_t)nZ * nZ, 0.0);
+            for (int i = 0; i < nZ; i++) Pm[(size_t)i * nZ + i] = 1.0;
+            for (auto& qr : Qrows)
+                for (int i = 0; i < nZ; i++) for (int j = 0; j < nZ; j++) Pm[(size_t)i * nZ + j] -= qr[i] * qr[j];
+            std::vector<double> t1((size_t)nZ * nZ, 0.0);
+            for (int i = 0; i < nZ; i++) for (int k = 0; k < nZ; k++) {
+                double a = Pm[(size_t)i * nZ + k];
+                if (a == 0) continue;
+                for (int j = 0; j < nZ; j++) t1[(size_t)i * nZ + j] += a * Kzz[(size_t)k * nZ + j];
+            }
+            for (int i = 0; i < nZ; i++) for (int j = 0; j < nZ; j++) {
+                double s = 0;
+                for (int k = 0; k < nZ; k++) s += t1[(size_t)i * nZ + k] * Pm[(size_t)k * nZ + j];
+                PK[(size_t)i * nZ + j] = s;
+            }
+            double dmax = 0;
+            for (int i = 0; i < nZ; i++) dmax = std::max(dmax, PK[(size_t)i * nZ + i]);
+            if (dmax <= 0) dmax = 1;
+            for (auto& qr : Qrows) for (int i = 0; i < nZ; i++) for (int j = 0; j < nZ; j++) PK[(size_t)i * nZ + j] += dmax * qr[i] * qr[j];
+            std::vector<double> inv = PK;
+            if (!spd_inverse(inv, nZ)) {   // fall back to the diagonal
+                inv.assign((size_t)nZ * nZ, 0.0);
+                for (int i = 0; i < nZ; i++) { double v = PK[(size_t)i * nZ + i]; inv[(size_t)i * nZ + i] = v > 0 ? 1.0 / v : 1.0; }
+            }
+            MTK_TRY(S.Mz.upload(inv.data(), inv.size(), st));
+            std::vector<float> inv32(inv.begin(), inv.end());
+            MTK_TRY(S.Mz32.upload(inv32.data(), inv32.size(), st));
+        } else {
+            double one = 1.0;
+            float onef = 1.f;
+            MTK_TRY(S.Mz.upload(&one, 1, st));
+            MTK_TRY(S.Mz32.upload(&onef, 1, st));
+        }
+        jacobi_y<<<G, kBlock, 0, st>>>(nY, S.yt_ptr.p, S.yt_row.p, S.yt_val.p, S.s_diag.p, scale, shift, S.minvy.p, S.minvy32.p);
+        c->kernels++;
+        MTK_TRY(S.fixy.upload(S.h_fixy.data(), S.h_fixy.size(), st));
+        MTK_CUDA_TRY(cudaGetLastError());
+        return MTK_OK;
+    };
+    // Adds the constraint X[full] = val; moves xs (device) to the nearest feasible point.
+    auto add_constraint = [&](int full, double val) -> int {
+        int y = S.full2y[full];
+        if (y >= 0) {
+            S.h_fixy[y] = 1;
+            MTK_CUDA_TRY(cudaMemcpyAsync(S.xs.p + y, &val, sizeof(double), cudaMemcpyHostToDevice, st));
+            MTK_CUDA_TRY(cudaStreamSynchronize(st));
+            return MTK_OK;
+        }
+        int s = S.full2j[full];
+        std::vector<double> row(S.USmall.begin() + (size_t)s * nZ, S.USmall.begin() + (size_t)(s + 1) * nZ);
+        Arows.push_back(row);
+        Avals.push_back(val);
+        add_orthonormal(Qrows, row);
+        // feasible correction of z: z += A^T (A A^T)^+ (g - A z), via the orthonormal basis:
+        // solve in the row space with least squares (Q spans the rows of A).
+        std::vector<double> z(nZ);
+        MTK_CUDA_TRY(cudaMemcpyAsync(z.data(), S.xs.p + S.nY, sizeof(double) * nZ, cudaMemcpyDeviceToHost, st));
+        MTK_CUDA_TRY(cudaStreamSynchronize(st));
+        // Gauss-Newton on the small system: minimise |dz| s.t. A (z + dz) = g (a few refinement passes)
+        const int m = (int)Arows.size();
+        for (int pass = 0; pass < 3; pass++) {
+            std::vector<double> res(m);
+            double worst = 0;
+            for (int a = 0; a < m; a++) {
+                double t = Avals[a];
+                for (int j = 0; j < nZ; j++) t -= Arows[a][j] * z[j];
+                res[a] = t;
+                worst = std::max(worst, std::fabs(t));
+            }
+            if (worst < 1e-13) break;
+            // normal equations (A A^T) w = res, dz = A^T w (m small; Cholesky with tiny ridge)
+            std::vector<double> AAt((size_t)m * m);
+            for (int a = 0; a < m; a++)
+                for (int b2 = 0; b2 < m; b2++) {
+                    double t = 0;
+                    for (int j = 0; j < nZ; j++) t += Arows[a][j] * Arows[b2][j];
+                    AAt[(size_t)a * m + b2] = t + (a == b2 ? 1e-14 : 0.0);
+                }
+            if (!spd_inverse(AAt, m)) break;
+            std::vector<double> w(m, 0.0);
+            for (int a = 0; a < m; a++) for (int b2 = 0; b2 < m; b2++) w[a] += AAt[(size_t)a * m + b2] * res[b2];
+            for (int j = 0; j < nZ; j++) {
+                double t = 0;
+                for (int a = 0; a < m; a++) t += Arows[a][j] * w[a];
+                z[j] += t;
+            }
+        }
+        MTK_CUDA_TRY(cudaMemcpyAsync(S.xs.p + S.nY, z.data(), sizeof(double) * nZ, cudaMemcpyHostToDevice, st));
+        MTK_CUDA_TRY(cudaStreamSynchronize(st));
+        return MTK_OK;
+    };
+    auto read_full = [&](int full) -> double {
+        int y = S.full2y[full];
+        std::vector<double> v(std::max(nZ, 1));
+        if (y >= 0) {
+            cudaMemcpyAsync(v.data(), S.xs.p + y, sizeof(double), cudaMemcpyDeviceToHost, st);
+            cudaStreamSynchronize(st);
+            return v[0];
+        }
+        cudaMemcpyAsync(v.data(), S.xs.p + S.nY, sizeof(double) * nZ, cudaMemcpyDeviceToHost, st);
+        cudaStreamSynchronize(st);
+        int s = S.full2j[full];
+        double t = 0;
+        for (int j = 0; j < nZ; j++) t += S.USmall[(size_t)s * nZ + j] * v[j];
+        return t;
+    };
+
+    mtk_stats local{};
+    mtk_stats* stt = stats ? stats : &local;
+    // ================= naive integration (iter_rounding_init.h:171-212) =================
+    // length X2F^T X2F x = X2F^T F2 with the anchor rows UFull[fixedIdcs] x = fixedVals.
+    const double length = d->length;
+    MTK_CUDA_TRY(cudaMemsetAsync(S.xs.p, 0, sizeof(double) * nRed, st));
+    for (int k = 0; k < d->nFixed; k++) MTK_TRY(add_constraint(d->fixedIdcs[k], d->fixedVals[k]));
+    MTK_TRY(upload_constraints(length, 0.0));
+    MTK_TRY(S.build_rhs(S.F2.p, 1.0, 0.0, nullptr, S.bsys.p));
+    double rel = 0;
+    MTK_TRY(S.solve(length, 0.0, S.bsys.p, S.xs.p, o, stt, &rel));
+    if (x_naive) {
+        expand_full<<<G, kBlock, 0, st>>>(nFull, S.d_full2y.p, S.d_full2j.p, nY, nZ, S.Us.p, S.xs.p, S.Xfull.p);
+        c->kernels++;
+        MTK_CUDA_TRY(cudaMemcpyAsync(x_naive, S.Xfull.p, sizeof(double) * nFull, cudaMemcpyDeviceToHost, st));
+    }
+    // x0 of the naive solution, kept for the "nothing rounded" exit (iter_rounding.h:111)
+    DBuf<double> x0red;
+    MTK_TRY(x0red.alloc(nRed));
+    MTK_CUDA_TRY(cudaMemcpyAsync(x0red.p, S.xs.p, sizeof(double) * nRed, cudaMemcpyDeviceToDevice, st));
+    MTK_CUDA_TRY(cudaEventRecord(c->ev_b, st));
+    MTK_CUDA_TRY(cudaStreamSynchronize(st));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->ev_a, c->ev_b);
+    stt->ms_integrate += ms;
+    int status = MTK_OK;
+    int nfix = 0;
+    auto finish = [&](const double* xsrc) -> int {
+        expand_full<<<G, kBlock, 0, st>>>(nFull, S.d_full2y.p, S.d_full2j.p, nY, nZ, S.Us.p, xsrc, S.Xfull.p);
+        c->kernels++;
+        MTK_CUDA_TRY(cudaMemcpyAsync(fullx, S.Xfull.p, sizeof(double) * nFull, cudaMemcpyDeviceToHost, st));
+        MTK_CUDA_TRY(cudaStreamSynchronize(st));
+        if (n_fixed) *n_fixed = nfix;
+        stt->kernel_launches = c->kernels;
+        stt->ms_total += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+        return status;
+    };
+    if (!d->seamless) return finish(S.xs.p);
+
+    // ================= NI Levenberg-Marquardt (lambda = 0), levenberg_marquardt.h:140-231 =======
+    // Variables (xs, f); the f block of J^T J is diagonal and is eliminated exactly.  From the
+    // naive solution the reduced Gauss-Newton step for xs is zero (same normal equations), so
+    // one step gives f* = (wI^2 length grad(x) + wC^2 F2) / (wI^2 + wC^2); the second
+    // iteration's direction is zero and the solve stops (direction norm < tolerance).
+    MTK_CUDA_TRY(cudaEventRecord(c->ev_a, st));
+    {
+        const double wI = 10e3, wC = 1.0;
+        xj_from_z<<<G, kBlock, 0, st>>>(nJ, nY, nZ, S.Us.p, S.xs.p, S.XJ64.p);
+        gather_U<<<G, kBlock, 0, st>>>(nCut, S.w_ptr.p, S.w_tag.p, S.w_val.p, S.xs.p, S.XJ64.p, S.U.p);
+        lm_field_target<<<G, kBlock, 0, st>>>(nF, S.cutF.p, S.grad.p, S.U.p, S.F2.p, length, wI * wI, wC * wC, S.Fsi.p);
+        c->kernels += 3;
+        MTK_CUDA_TRY(cudaGetLastError());
+        stt->lm_iterations += 2;
+    }
+    // ================= seamless rounding loop (iter_rounding.h:99-109) ==========================
+    // SI: wInteg = 1, wClose = 0.01, wConst = 1e5; X2F_si = length * G2 * fullx2N * UFull.
+    const double scale_si = length * length, shift_si = 0.01 * 0.01;
+    // SI constraints start empty (the NI anchor is not an SI constraint)
+    Qrows.clear(); Arows.clear(); Avals.clear();
+    std::fill(S.h_fixy.begin(), S.h_fixy.end(), 0);
+    S.kq = 0;
+    std::vector<int> leftv;
+    const bool roundSeams = d->roundSeams != 0;
+    bool roundedSingulars = false;
+    if (roundSeams) leftv.assign(d->integerIdcs, d->integerIdcs + d->nInteger);
+    else leftv.assign(d->singularIdcs, d->singularIdcs + d->nSingular);
+    bool rounded = false;
+    double min_margin = 1e300;
+    std::vector<double> h_arg(4);
+    bool constraints_dirty = true;
+    while (!leftv.empty()) {
+        // ---- initFixedIndices: argmin |X - round X| over leftIdcs (FP64 on the device)
+        MTK_CUDA_TRY(cudaMemcpyAsync(S.left.p, leftv.data(), sizeof(int) * leftv.size(), cudaMemcpyHostToDevice, st));
+        round_argmin<<<1, kBlock, 0, st>>>((int)leftv.size(), S.left.p, S.d_full2y.p, S.d_full2j.p, nY, nZ, S.Us.p, S.xs.p,
+                                           c->scalars);
+        c->kernels++;
+        MTK_CUDA_TRY(cudaMemcpyAsync(h_arg.data(), c->scalars, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        MTK_CUDA_TRY(cudaStreamSynchronize(st));
+        const int k = (int)h_arg[0];
+        const double mind = h_arg[1];
+        if (leftv.size() > 1) min_margin = std::min(min_margin, h_arg[3] - mind);
+        const int idx = leftv[k];
+        const int ival = (int)std::round(h_arg[2]);
+        if (fix_order && nfix < nLeftCap) { fix_order[nfix] = idx; if (fix_vals) fix_vals[nfix] = ival; }
+        nfix++;
+        leftv.erase(leftv.begin() + k);
+        if (leftv.empty() && !roundSeams && !roundedSingulars) {
+            leftv.assign(d->integerIdcs, d->integerIdcs + d->nInteger);
+            roundedSingulars = true;
+        }
+        // prev = xs (xPrev = xCurr) before the constraint moves xs
+        MTK_CUDA_TRY(cudaMemcpyAsync(S.prev.p, S.xs.p, sizeof(double) * nRed, cudaMemcpyDeviceToDevice, st));
+        MTK_TRY(add_constraint(idx, (double)ival));
+        constraints_dirty = true;
+        if (!(mind > 10e-7)) continue;    // already integral: no re-solve
+        rounded = true;
+        // ---- LM solve of the SI objective: one exact constrained Gauss-Newton step
+        MTK_CUDA_TRY(cudaEventRecord(c->ev_a, st));
+        if (constraints_dirty) { MTK_TRY(upload_constraints(scale_si, shift_si)); constraints_dirty = false; }
+        // b = length UFull^T W^T hb(F_si) + shift * xPrev
+        MTK_TRY(S.build_rhs(S.Fsi.p, length, shift_si, S.prev.p, S.bsys.p));
+        int s = S.solve(scale_si, shift_si, S.bsys.p, S.xs.p, o, stt, &rel);
+        if (s != MTK_OK) { status = s; break; }
+        stt->resolves++;
+        stt->lm_iterations += 2;
+        MTK_CUDA_TRY(cudaEventRecord(c->ev_b, st));
+        MTK_CUDA_TRY(cudaStreamSynchronize(st));
+        cudaEventElapsedTime(&ms, c->ev_a, c->ev_b);
+        stt->ms_rounding += ms;
+        // ---- post_checking: every fixed value within 1e-6 of an integer
+        double worst = 0;
+        for (int q = 0; q < std::min(nfix, nLeftCap); q++) {
+            if (!fix_order) break;
+            double v = read_full(fix_order[q]);
+            worst = std::max(worst, std::fabs(v - std::round(v)));
+        }
+        if (worst > 10e-7) { status = MTK_ERR_ROUNDING; break; }
+    }
+    stt->min_order_margin = std::min(stt->min_order_margin == 0 ? 1e300 : stt->min_order_margin, min_margin);
+    if (!rounded) return finish(x0red.p);
+    return finish(S.xs.p);
+}

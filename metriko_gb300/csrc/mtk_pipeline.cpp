@@ -1,0 +1,150 @@
+// mtk_pipeline_run: the example_igm.cpp:13-31 call sequence through the header-only host API
+// (include/metriko/...), with host buffers in and out.  Topology stages run on the host, the
+// field and the integration / rounding solves on the GPU.
+#include <chrono>
+#include <cstring>
+
+#include "metriko/core/igm/parameterization.h"
+#include "metriko/core/vectorfield/face_rosy_field.h"
+
+void mtk_set_last_error(const char* msg, const char* file, int line);
+
+using namespace metriko;
+
+extern "C" int mtk_pipeline_run(mtk_ctx* ctx, int32_t nV, int32_t nF, const double* Vb, const int32_t* Fb,
+                                const mtk_pipeline_opts* popts, const mtk_solve_opts* sopts, int32_t* singular,
+                                int32_t* matching, uint8_t* seam_out, double* compressed, double* cfn_out,
+                                double* fullx_out, double* x_naive, int32_t fullx_cap, int32_t* n_full,
+                                int32_t* fix_order, int32_t* fix_vals, int32_t fix_cap, int32_t* n_fixed,
+                                int32_t* counts, mtk_stats* stats) {
+    if (!ctx || nV <= 0 || nF <= 0 || !Vb || !Fb || !popts) return MTK_ERR_BAD_INPUT;
+    using clk = std::chrono::steady_clock;
+    auto t0 = clk::now();
+    double host_ms = 0;
+    auto lap = [&](clk::time_point& a) {
+        auto b = clk::now();
+        host_ms += std::chrono::duration<double, std::milli>(b - a).count();
+        a = b;
+    };
+    gpu::bound_context() = ctx;
+    struct Unbind { ~Unbind() { gpu::bound_context() = nullptr; } } unbind;
+    gpu::stats() = mtk_stats{};
+    if (sopts) gpu::options().solve = *sopts;
+    else mtk_default_opts(&gpu::options().solve);
+    gpu::options().seed = popts->seed;
+    gpu::options().n_iter = popts->n_iter > 0 ? popts->n_iter : 50;
+    try {
+        auto ts = clk::now();
+        MatXd V(nV, 3);
+        MatXi F(nF, 3);
+        std::memcpy(V.data(), Vb, sizeof(double) * 3 * size_t(nV));
+        std::memcpy(F.data(), Fb, sizeof(int32_t) * 3 * size_t(nF));
+        auto mesh = std::make_unique<Hmesh>(V, F);
+        lap(ts);
+        FaceRosyField rawf(*mesh, 4, FieldType::Smoothest);
+        ts = clk::now();
+        rawf.computeMatching(MatchingType::Curl);
+        if (compressed)
+            for (int f = 0; f < nF; f++) { compressed[2 * f] = rawf.compressed[f].real(); compressed[2 * f + 1] = rawf.compressed[f].imag(); }
+        if (singular) std::memcpy(singular, rawf.singular.data(), sizeof(int32_t) * nV);
+        if (counts) { counts[0] = mesh->nV; counts[1] = mesh->nE; }
+        if (popts->stop_after == 1) {
+            if (matching) std::memcpy(matching, rawf.matching.data(), sizeof(int32_t) * mesh->nE);
+            lap(ts);
+            if (stats) { *stats = gpu::stats(); stats->ms_host = host_ms; stats->ms_total = std::chrono::duration<double, std::milli>(clk::now() - t0).count(); }
+            return MTK_OK;
+        }
+        auto seam = compute_seam(rawf);
+        auto cutm = compute_cut_mesh(*mesh, seam);
+        auto cmbf = compute_combbed_field(rawf, seam);
+        MatXd extf = compute_extrinsic_field(*mesh, *cmbf, 4);
+        RosyParameterization rp(*mesh, *cutm, extf, cmbf->singular, cmbf->matching, seam, 4, popts->ratio);
+        rp.seamless = popts->seamless != 0;
+        rp.localInjectivity = false;
+        rp.roundSeams = popts->round_seams != 0;
+        rp.verbose = false;
+        rp.setup();
+        lap(ts);
+        if (matching) std::memcpy(matching, cmbf->matching.data(), sizeof(int32_t) * mesh->nE);
+        if (seam_out) for (int e = 0; e < mesh->nE; e++) seam_out[e] = seam[e] ? 1 : 0;
+        if (counts) {
+            counts[2] = cutm->nV;
+            counts[3] = rp.numTransitions();
+            counts[4] = rp.numSingular();
+        }
+        if (popts->stop_after == 2) {
+            if (stats) { *stats = gpu::stats(); stats->ms_host = host_ms; stats->ms_total = std::chrono::duration<double, std::milli>(clk::now() - t0).count(); }
+            return MTK_OK;
+        }
+        bool ok = rp.integ();
+        const int nFull = rp.fullx.size();
+        if (counts) { counts[5] = rp.nJ; counts[6] = rp.nZ; counts[7] = nFull; }
+        if (n_full) *n_full = nFull;
+        if (fullx_out && fullx_cap >= nFull) std::memcpy(fullx_out, rp.fullx.data(), sizeof(double) * nFull);
+        if (x_naive && fullx_cap >= nFull) std::memcpy(x_naive, rp.naivex.data(), sizeof(double) * nFull);
+        const int nfix = int(rp.fixOrder.size());
+        if (n_fixed) *n_fixed = nfix;
+        for (int i = 0; i < nfix && i < fix_cap; i++) {
+            if (fix_order) fix_order[i] = rp.fixOrder[i];
+            if (fix_vals) fix_vals[i] = rp.fixVals[i];
+        }
+        if (cfn_out) std::memcpy(cfn_out, rp.cfn.data(), sizeof(double) * size_t(nF) * 12);
+        if (stats) {
+            *stats = gpu::stats();
+            stats->ms_total = std::chrono::duration<double, std::milli>(clk::now() - t0).count();
+            stats->ms_host = stats->ms_total - stats->ms_field - stats->ms_integrate - stats->ms_rounding;
+        }
+        return ok ? MTK_OK : MTK_ERR_ROUNDING;
+    } catch (const std::invalid_argument& e) {
+        mtk_set_last_error(e.what(), __FILE__, __LINE__);
+        return MTK_ERR_BAD_INPUT;
+    } catch (const std::exception& e) {
+        mtk_set_last_error(e.what(), __FILE__, __LINE__);
+        return MTK_ERR_CUDA;
+    }
+}
+
+extern "C" int mtk_topology_from_field(int32_t nV, int32_t nF, const double* Vb, const int32_t* Fb,
+                                       const double* compressed, double ratio, int32_t round_seams,
+                                       int32_t* singular, int32_t* matching, uint8_t* seam_out, int32_t* cutF,
+                                       int32_t* counts, double* length) {
+    if (nV <= 0 || nF <= 0 || !Vb || !Fb || !compressed) return MTK_ERR_BAD_INPUT;
+    try {
+        MatXd V(nV, 3);
+        MatXi F(nF, 3);
+        std::memcpy(V.data(), Vb, sizeof(double) * 3 * size_t(nV));
+        std::memcpy(F.data(), Fb, sizeof(int32_t) * 3 * size_t(nF));
+        auto mesh = std::make_unique<Hmesh>(V, F);
+        FaceRosyField rawf(*mesh, 4);
+        rawf.compressed = VecXc(nF);
+        for (int f = 0; f < nF; f++) rawf.compressed[f] = complex(compressed[2 * f], compressed[2 * f + 1]);
+        rawf.set_field_from_compressed();
+        rawf.computeMatching(MatchingType::Curl);
+        if (singular) std::memcpy(singular, rawf.singular.data(), sizeof(int32_t) * nV);
+        auto seam = compute_seam(rawf);
+        auto cutm = compute_cut_mesh(*mesh, seam);
+        auto cmbf = compute_combbed_field(rawf, seam);
+        MatXd extf = compute_extrinsic_field(*mesh, *cmbf, 4);
+        RosyParameterization rp(*mesh, *cutm, extf, cmbf->singular, cmbf->matching, seam, 4, ratio);
+        rp.seamless = true;
+        rp.roundSeams = round_seams != 0;
+        rp.setup();
+        IntegSystem sys;
+        rp.build_system(sys);
+        if (matching) std::memcpy(matching, cmbf->matching.data(), sizeof(int32_t) * mesh->nE);
+        if (seam_out) for (int e = 0; e < mesh->nE; e++) seam_out[e] = seam[e] ? 1 : 0;
+        if (cutF) std::memcpy(cutF, cutm->idx.data(), sizeof(int32_t) * 3 * size_t(nF));
+        if (counts) {
+            counts[0] = mesh->nV; counts[1] = mesh->nE; counts[2] = cutm->nV; counts[3] = rp.numTransitions();
+            counts[4] = rp.numSingular(); counts[5] = rp.nJ; counts[6] = rp.nZ; counts[7] = sys.desc.nFull;
+        }
+        if (length) *length = sys.length;
+        return MTK_OK;
+    } catch (const std::invalid_argument& e) {
+        mtk_set_last_error(e.what(), __FILE__, __LINE__);
+        return MTK_ERR_BAD_INPUT;
+    } catch (const std::exception& e) {
+        mtk_set_last_error(e.what(), __FILE__, __LINE__);
+        return MTK_ERR_BAD_INPUT;
+    }
+}

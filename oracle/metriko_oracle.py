@@ -1,0 +1,1122 @@
+"""FP64 CPU ORACLE for metriko's field + seamless-integration + IGM path.
+
+TEST INFRASTRUCTURE ONLY.  This module is the checker for the CUDA path and the timed CPU
+baseline.  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference arm
+may import it.  Nothing in the product (metriko_gb300/, include/) imports it.
+
+What it restates (reference paths are relative to the metriko project root):
+
+  a1  Hmesh construction              include/metriko/core/hmesh/hmesh.h:282-611
+      (libigl v2.5.0 edge_topology restated from its documented behaviour)
+  a2  connectionLaplacian             include/metriko/core/vectorfield/face_rosy_field.h:72-102
+  a3  galerkinMassMatrix              face_rosy_field.h:104-110
+  a4  solveSmallestEig (50 iters)     include/metriko/core/solver/sparse_linear_solver.h:452-477
+      direct sparse LU (scipy SuperLU), the reference's non-SuiteSparse branch
+  a5  N-th root field                 face_rosy_field.h:63-69
+  a6  computeConnection / cMatching / computeSingular   face_rosy_field.h:126-143,195-228
+  a7  compute_seam / cut_mesh_with_singularities        face_rosy_field.h:294-386
+      (libigl v2.5.0 cut_mesh_from_singularities, dijkstra, adjacency_list,
+       vertex_triangle_adjacency, triangle_triangle_adjacency restated)
+  a8  compute_combbed_field / compute_extrinsic_field   face_rosy_field.h:233-290
+  a9  compute_cut_mesh                include/metriko/core/igm/parameterization.h:126-152
+  a10 compute_he2transidx / he2matching   include/metriko/core/igm/parameterization_setup.ipp:3-49
+  a11 setup                           parameterization_setup.ipp:51-170
+  a12 integ                           include/metriko/core/igm/parameterization_integ.ipp:3-120
+  a13 reduce_to_linearly_independent  include/metriko/core/solver/matrix_ops.h:12-28
+  a14 NaiveIntegration                include/metriko/core/igm/iterative_rounding/iter_rounding_init.h:16-233
+  a17 LMSolver + DiagonalDamping      include/metriko/core/solver/levenberg_marquardt.h:13-231
+  a19 iterative_rounding              include/metriko/core/igm/iterative_rounding/iter_rounding.h:33-113
+  a20 SeamlessIntegration             include/metriko/core/igm/iterative_rounding/iter_rounding_loop.h:10-125
+
+Deliberate, documented choices (identical in the product path):
+  * the power iteration starts from a caller-supplied seeded vector instead of
+    Eigen's std::rand-based VecXc::Random (sparse_linear_solver.h:455);
+  * reduce_to_linearly_independent keeps the greedy (first-in-row-order) maximal independent
+    row set instead of Eigen SparseQR<COLAMD>'s column-pivot order; the constraint null space
+    is the same;
+  * the constraint kernel basis restates Eigen's FullPivLU::kernel (complete pivoting, first
+    maximum in column-major order, identity on the free columns);
+  * near-integer ties in the greedy rounding order (|x - round(x)| < 1e-9, decided by
+    round-off in the reference) are resolved by position.
+Closed, consistently oriented, edge-manifold triangle meshes only.
+
+Parity status: the reference cannot be compiled here (Eigen, libigl, SuiteSparse absent) and
+holds no tests or golden vectors, so this restatement is pinned only by the reference's own
+invariants (sum of singular indices = N * Euler characteristic, post-rounding integrality,
+Hermitian positive-definite L) -- parity unpinned against reference binaries.
+"""
+from __future__ import annotations
+
+import heapq
+import math
+from collections import deque
+
+import numpy as np
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+TWO_PI = 2.0 * math.pi
+
+
+def cround(x):
+    """C/C++ std::round: half away from zero."""
+    return np.sign(x) * np.floor(np.abs(x) + 0.5)
+
+
+def _norm3(a):
+    return np.sqrt(a[..., 0] * a[..., 0] + a[..., 1] * a[..., 1] + a[..., 2] * a[..., 2])
+
+
+def _dot3(a, b):
+    return a[..., 0] * b[..., 0] + a[..., 1] * b[..., 1] + a[..., 2] * b[..., 2]
+
+
+def _normalized(a):
+    return a / _norm3(a)[..., None]
+
+
+# --------------------------------------------------------------------------------------------
+# a1  mesh
+# --------------------------------------------------------------------------------------------
+def edge_topology(F):
+    """libigl v2.5.0 edge_topology: edges sorted by (min v, max v, face, corner);
+    EF[e,0] is the face in which the edge runs min->max."""
+    F = np.asarray(F, np.int64)
+    nF = len(F)
+    a = F.ravel()
+    b = F[:, [1, 2, 0]].ravel()
+    lo, hi = np.minimum(a, b), np.maximum(a, b)
+    fid = np.repeat(np.arange(nF), 3)
+    loc = np.tile(np.arange(3), nF)
+    order = np.lexsort((loc, fid, hi, lo))
+    lo_s, hi_s, f_s, l_s, a_s = lo[order], hi[order], fid[order], loc[order], a[order]
+    new = np.ones(len(order), bool)
+    new[1:] = (lo_s[1:] != lo_s[:-1]) | (hi_s[1:] != hi_s[:-1])
+    eid = np.cumsum(new) - 1
+    nE = int(eid[-1]) + 1
+    cnt = np.bincount(eid, minlength=nE)
+    if cnt.max() > 2:
+        raise ValueError("mesh is not edge-manifold")
+    if cnt.min() < 2:
+        raise ValueError("mesh has boundary edges (closed meshes only)")
+    first = np.flatnonzero(new)
+    FE = np.empty((nF, 3), np.int64)
+    FE[f_s, l_s] = eid
+    EV = np.stack([lo_s[first], hi_s[first]], 1)
+    EF = np.stack([f_s[first], f_s[first + 1]], 1)
+    # flip so that EF[e,0] holds the directed edge lo->hi
+    dir0 = a_s[first] == lo_s[first]
+    flip = ~dir0
+    EF[flip] = EF[flip][:, ::-1]
+    return EV, FE, EF
+
+
+class Hmesh:
+    """Halfedge mesh with the reference's numbering (hmesh.h:282-611) for closed meshes."""
+
+    def __init__(self, V, F):
+        V = np.asarray(V, np.float64)
+        F = np.asarray(F, np.int64)
+        EV, FE, EF = edge_topology(F)
+        self.pos, self.idx = V, F
+        nV, nF, nE = len(V), len(F), len(EV)
+        self.nV, self.nF, self.nE, self.nH = nV, nF, nE, 2 * nE
+        self.edge2vert, self.face2edge, self.edge2face = EV, FE, EF
+        ar = np.arange(nE)
+        # halfedge 2e: tail EV[e,0], face EF[e,0]; 2e+1: tail EV[e,1], face EF[e,1]
+        tail = np.empty(2 * nE, np.int64)
+        tail[0::2], tail[1::2] = EV[:, 0], EV[:, 1]
+        face = np.empty(2 * nE, np.int64)
+        face[0::2], face[1::2] = EF[:, 0], EF[:, 1]
+        twin = np.empty(2 * nE, np.int64)
+        twin[0::2], twin[1::2] = 2 * ar + 1, 2 * ar
+        edge = np.repeat(ar, 2)
+        # FH[f,j]: the halfedge of face f on edge FE[f,j]
+        FH = 2 * FE + (EF[FE, 0] != np.arange(nF)[:, None])
+        nxt = np.empty(2 * nE, np.int64)
+        prv = np.empty(2 * nE, np.int64)
+        for j in range(3):
+            nxt[FH[:, j]] = FH[:, (j + 1) % 3]
+            prv[FH[:, (j + 1) % 3]] = FH[:, j]
+        # vert2half: dcel() writes in edge order, last write wins
+        emax = np.full(nV, -1, np.int64)
+        np.maximum.at(emax, EV[:, 0], ar)
+        np.maximum.at(emax, EV[:, 1], ar)
+        if (emax < 0).any():
+            raise ValueError("isolated vertex")
+        vert2half = 2 * emax + (EV[emax, 1] == np.arange(nV))
+        self.tail, self.face, self.twin, self.edge = tail, face, twin, edge
+        self.next, self.prev = nxt, prv
+        self.head = tail[nxt]
+        self.FH = FH
+        self.face2half = FH[:, 0]
+        self.edge2half = 2 * ar
+        self.vert2half = vert2half
+        # face frames (hmesh.h:503-520)
+        P0, P1, P2 = V[F[:, 0]], V[F[:, 1]], V[F[:, 2]]
+        x = P1 - P0
+        t = -(P0 - P2)
+        n = np.cross(x, t)
+        self.faceBasisX = _normalized(x)
+        self.faceBasisY = _normalized(-np.cross(x, n))
+        self.faceNormal = _normalized(n)
+        self.faceArea = _norm3(n) * 0.5
+        # heArgOnFace (hmesh.h:522-531)
+        vec = V[self.head] - V[self.tail]
+        self.hvec = vec
+        farg = np.zeros(2 * nE)
+        s = np.zeros(nF)
+        for j in range(3):
+            h = FH[:, j]
+            v1 = _normalized(vec[h])
+            v2 = _normalized(vec[prv[h]])
+            far = _norm3(v1 - self.faceBasisX) > 1e-10
+            s = s + np.where(far, np.arccos(_dot3(v1, v2)), 0.0)
+            farg[h] = s
+        self.farg = farg
+        # angleDefect (hmesh.h:599-610): interior angle at tail(h) inside face(h)
+        h = np.arange(2 * nE)
+        ang = np.arccos(_dot3(_normalized(vec[h]), _normalized(vec[twin[prv[h]]])))
+        ssum = np.zeros(nV)
+        for v in range(nV):  # ccw order from vert2half, as the reference sums
+            h0 = vert2half[v]
+            hh = h0
+            acc = 0.0
+            while True:
+                acc += ang[hh]
+                hh = twin[prv[hh]]
+                if hh == h0:
+                    break
+            ssum[v] = acc
+        self.angleDefect = TWO_PI - ssum
+
+    def is_canonical(self, h):
+        return self.edge2half[self.edge[h]] == h
+
+    def ccw(self, h0):
+        """Outgoing halfedges around tail(h0), ccw (AdjVH with ccw=true)."""
+        out, h = [], h0
+        while True:
+            out.append(h)
+            h = self.twin[self.prev[h]]
+            if h == h0:
+                return out
+
+    def cw(self, h0):
+        out, h = [], h0
+        while True:
+            out.append(h)
+            h = self.next[self.twin[h]]
+            if h == h0:
+                return out
+
+
+# --------------------------------------------------------------------------------------------
+# a2-a5  smoothest N-RoSy field
+# --------------------------------------------------------------------------------------------
+def connection_laplacian(m: Hmesh, N: int):
+    """face_rosy_field.h:72-102: L_ff = #interior neighbours + 1e-9, L_fg = -r_twin^N."""
+    h1 = m.edge2half
+    h2 = m.twin[h1]
+    v1 = np.exp(1j * m.farg[h1])
+    v2 = np.exp(1j * m.farg[h2])
+    r = -v2 / v1
+    transport = np.empty(m.nH, np.complex128)
+    transport[h1] = r
+    transport[h2] = 1.0 / r
+    rows, cols, vals = [], [], []
+    for j in range(3):
+        h = m.FH[:, j]
+        t = m.twin[h]
+        rr = transport[t]
+        rows += [np.arange(m.nF), np.arange(m.nF)]
+        cols += [np.arange(m.nF), m.face[t]]
+        vals += [np.ones(m.nF, np.complex128), -np.exp(N * np.log(rr))]
+    L = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                      shape=(m.nF, m.nF))
+    L = L + 1e-9 * sp.identity(m.nF, dtype=np.complex128, format="csr")
+    return L.tocsr()
+
+
+def mass_matrix(m: Hmesh):
+    return sp.diags(m.faceArea.astype(np.complex128)).tocsr()
+
+
+def seeded_init(n: int, seed: int):
+    """Deterministic complex start vector, re/im in [-1, 1): splitmix64 of (seed, 2i / 2i+1).
+
+    The product library generates the same vector from the same seed."""
+    idx = np.arange(2 * n, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        z = (np.uint64(seed) * np.uint64(0x9E3779B97F4A7C15)
+             + (idx + np.uint64(1)) * np.uint64(0x9E3779B97F4A7C15))
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    u = (z >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+    u = 2.0 * u - 1.0
+    return u[0::2] + 1j * u[1::2]
+
+
+def smallest_eig(L, M, x0, n_iter=50):
+    """sparse_linear_solver.h:452-477: x = L^-1 M u; x /= sqrt|x^H M x|; u = x (n_iter times)."""
+    lu = spla.splu(L.tocsc())
+    u = x0.copy()
+    x = u
+    for _ in range(n_iter):
+        x = lu.solve(M @ u)
+        s = math.sqrt(abs(np.vdot(x, M @ x)))
+        x = x / s
+        u = x
+    return x
+
+
+def rosy_from_compressed(c, N):
+    """face_rosy_field.h:63-69: field(f,i) = pow(polar(1, arg c_f), 1/N) * pow(r, i)."""
+    z = np.exp(1j * np.angle(c))
+    root = np.exp(np.log(z) * (1.0 / N))
+    r = np.exp(1j * TWO_PI / N)
+    pw = np.array([np.exp(i * np.log(r)) if i else 1.0 + 0j for i in range(N)])
+    return root[:, None] * pw[None, :]
+
+
+# --------------------------------------------------------------------------------------------
+# a6  matching and singularities
+# --------------------------------------------------------------------------------------------
+def compute_connection(m: Hmesh):
+    h = m.edge2half
+    v = _normalized(m.hvec[h])
+    f0, f1 = m.edge2face[:, 0], m.edge2face[:, 1]
+    ef = _dot3(v, m.faceBasisX[f0]) + 1j * _dot3(v, m.faceBasisY[f0])
+    eg = _dot3(v, m.faceBasisX[f1]) + 1j * _dot3(v, m.faceBasisY[f1])
+    return eg / ef
+
+
+def c_matching(m: Hmesh, field, conn, N):
+    """face_rosy_field.h:195-228 (MatchingType::Curl)."""
+    h = m.edge2half
+    v = _normalized(m.hvec[h])
+    f0, f1 = m.edge2face[:, 0], m.edge2face[:, 1]
+    bx0, by0, bx1, by1 = m.faceBasisX[f0], m.faceBasisY[f0], m.faceBasisX[f1], m.faceBasisY[f1]
+    best = np.full(m.nE, 32767000.0)
+    iM = np.zeros(m.nE, np.int64)
+    for i in range(N):
+        curl = np.zeros(m.nE)
+        for j in range(N):
+            c0 = field[f0, j]
+            c1 = field[f1, (i + j) % N]
+            v0 = c0.real[:, None] * bx0 + c0.imag[:, None] * by0
+            v1 = c1.real[:, None] * bx1 + c1.imag[:, None] * by1
+            d = _dot3(v, v1 - v0)
+            curl = curl + d * d
+        better = curl < best
+        iM[better] = i
+        best[better] = curl[better]
+    coef = np.ones(m.nE, np.complex128)
+    for i in range(N):
+        a0 = field[f0, i]
+        a1 = field[f1, (i + iM) % N]
+        coef = coef * (a1 / (a0 * conn))
+    effort = np.angle(coef)
+    return iM, effort
+
+
+def compute_singular(m: Hmesh, effort, N):
+    """face_rosy_field.h:126-133."""
+    h = np.arange(m.nH)
+    sgn = np.where(m.is_canonical(h), -1.0, 1.0)
+    contrib = sgn * effort[m.edge[h]]
+    s = m.angleDefect * N
+    acc = np.zeros(m.nV)
+    for v in range(m.nV):
+        t = s[v]
+        for hh in m.ccw(m.vert2half[v]):
+            t += contrib[hh]
+        acc[v] = t
+    return cround(acc / TWO_PI).astype(np.int64)
+
+
+# --------------------------------------------------------------------------------------------
+# a7  seams: libigl cut_mesh_from_singularities + dijkstra, then singularity paths
+# --------------------------------------------------------------------------------------------
+def triangle_triangle_adjacency(m: Hmesh):
+    F = m.idx
+    TT = np.empty((m.nF, 3), np.int64)
+    TTi = np.empty((m.nF, 3), np.int64)
+    for j in range(3):
+        h = m.FH[:, j]
+        t = m.twin[h]
+        g = m.face[t]
+        TT[:, j] = g
+        # local index of twin halfedge inside g
+        loc = np.argmax(m.FH[g] == t[:, None], axis=1)
+        TTi[:, j] = loc
+    return TT, TTi
+
+
+def cut_mesh_from_singularities_zero(m: Hmesh, TT, TTi):
+    """libigl MeshCutter with an all-zero matching: BFS flood fill from face 0 marks the dual
+    spanning tree; Retract() dissolves seam edges with a degree-1 endpoint, scanning faces in
+    order, pass after pass, at most 10001 passes (guard > 10000)."""
+    F = m.idx
+    nF = m.nF
+    seams = np.ones((nF, 3), bool)
+    visited = np.zeros(nF, bool)
+    for f0 in range(nF):
+        if visited[f0]:
+            continue
+        visited[f0] = True
+        dq = deque([f0])
+        while dq:
+            f = dq.popleft()
+            for s in range(3):
+                g, j = TT[f, s], TTi[f, s]
+                if j == -1:
+                    seams[f, s] = True
+                    continue
+                if not visited[g]:
+                    visited[g] = True
+                    seams[f, s] = False
+                    seams[g, j] = False
+                    dq.append(g)
+    # Retract
+    e = np.zeros(m.nV, np.int64)
+    fs, ss = np.nonzero(seams & (TT <= np.arange(nF)[:, None]))
+    np.add.at(e, F[fs, ss], 1)
+    np.add.at(e, F[fs, (ss + 1) % 3], 1)
+    vpos = [[] for _ in range(m.nV)]   # seam face-sides incident to each vertex
+    fs, ss = np.nonzero(seams)
+    for f, s in zip(fs.tolist(), ss.tolist()):
+        p = 3 * f + s
+        vpos[F[f, s]].append(p)
+        vpos[F[f, (s + 1) % 3]].append(p)
+    cur = sorted(p for p in (3 * fs + ss).tolist()
+                 if e[F[p // 3, p % 3]] == 1 or e[F[p // 3, (p % 3 + 1) % 3]] == 1)
+    heapq.heapify(cur)
+    nxt = set()
+    guard = 0
+    while True:
+        removed = False
+        cursor = -1
+        while cur:
+            p = heapq.heappop(cur)
+            if p <= cursor:
+                continue
+            cursor = p
+            f, s = divmod(p, 3)
+            if not seams[f, s]:
+                continue
+            a, b = F[f, s], F[f, (s + 1) % 3]
+            if e[a] == 1 or e[b] == 1:
+                seams[f, s] = False
+                if TTi[f, s] != -1:
+                    seams[TT[f, s], TTi[f, s]] = False
+                e[a] -= 1
+                e[b] -= 1
+                removed = True
+                for v in (a, b):
+                    if e[v] == 1:
+                        for q in vpos[v]:
+                            if seams[q // 3, q % 3]:
+                                if q > p:
+                                    heapq.heappush(cur, q)
+                                else:
+                                    nxt.add(q)
+        guard += 1
+        if not removed or guard > 10000:
+            break
+        cur = sorted(nxt)
+        nxt = set()
+    return seams
+
+
+def dijkstra_unit(source, targets, VV):
+    """libigl dijkstra with unit weights: pops (distance, vertex) in lexicographic order,
+    returns the first target popped (or -1) and the predecessor array."""
+    nV = len(VV)
+    dist = np.full(nV, np.inf)
+    prev = np.full(nV, -1, np.int64)
+    dist[source] = 0.0
+    heap = [(0.0, source)]
+    while heap:
+        d, u = heapq.heappop(heap)
+        if d > dist[u]:
+            continue
+        if u in targets:
+            return u, prev
+        for w in VV[u]:
+            nd = d + 1.0
+            if nd < dist[w]:
+                dist[w] = nd
+                prev[w] = u
+                heapq.heappush(heap, (nd, w))
+    return -1, prev
+
+
+def compute_seam(m: Hmesh, singular):
+    """face_rosy_field.h:294-386."""
+    F = m.idx
+    TT, TTi = triangle_triangle_adjacency(m)
+    cuts = cut_mesh_from_singularities_zero(m, TT, TTi)
+    VF = [[] for _ in range(m.nV)]
+    for f in range(m.nF):
+        for j in range(3):
+            VF[F[f, j]].append(f)
+    VV = [set() for _ in range(m.nV)]
+    for f in range(m.nF):
+        for j in range(3):
+            s, d = F[f, j], F[f, (j + 1) % 3]
+            VV[s].add(d)
+            VV[d].add(s)
+    VV = [sorted(x) for x in VV]
+    in_cut = set(F[cuts].tolist())
+    for s in np.flatnonzero(singular != 0).tolist():
+        found, prev = dijkstra_unit(s, in_cut, VV)
+        if found == -1:
+            path = [s]
+        else:
+            path = []
+            v = found
+            while v != -1:
+                path.append(v)
+                v = prev[v]
+        in_cut.update(path)
+        for v0, v1 in zip(path[:-1], path[1:]):
+            common = sorted(set(VF[v0]) & set(VF[v1]))
+            fi = common[0]
+            jj = -1
+            for z in range(3):
+                a, b = F[fi, z], F[fi, (z + 1) % 3]
+                if (a == v0 and b == v1) or (a == v1 and b == v0):
+                    jj = z
+            cuts[fi, jj] = True
+            cuts[TT[fi, jj], TTi[fi, jj]] = True
+    seam = np.zeros(m.nE, bool)
+    fs, js = np.nonzero(cuts)
+    seam[m.face2edge[fs, js]] = True
+    return seam
+
+
+# --------------------------------------------------------------------------------------------
+# a8  combing and extrinsic field
+# --------------------------------------------------------------------------------------------
+def combed_field(m: Hmesh, field, matching, seam, N):
+    """face_rosy_field.h:233-275."""
+    nF = m.nF
+    out = np.zeros_like(field)
+    turns = np.zeros(nF, np.int64)
+    visit = np.zeros(nF, bool)
+    q = deque([(0, 0)])
+    while q:
+        i, mm = q.popleft()
+        r = N - mm
+        if visit[i]:
+            continue
+        visit[i] = True
+        turns[i] = mm
+        out[i, :r] = field[i, mm:]
+        out[i, r:] = field[i, :mm]
+        for j in range(3):
+            h = m.FH[i, j]
+            e = m.edge[h]
+            b = m.edge2face[e, 0] == i
+            fn = m.edge2face[e, 1] if b else m.edge2face[e, 0]
+            n = (1 if b else -1) * matching[e]
+            n = (n + mm + 1000 * N) % N
+            if not visit[fn] and not seam[e]:
+                q.append((fn, n))
+    newm = (turns[m.edge2face[:, 0]] - turns[m.edge2face[:, 1]] + matching + 1000 * N) % N
+    return out, newm
+
+
+def extrinsic_field(m: Hmesh, field):
+    """face_rosy_field.h:277-290 (N = 4)."""
+    ext = np.empty((m.nF, 12))
+    for i in range(4):
+        c = field[:, i]
+        ext[:, 3 * i:3 * i + 3] = _normalized(c.real[:, None] * m.faceBasisX
+                                              + c.imag[:, None] * m.faceBasisY)
+    return ext
+
+
+# --------------------------------------------------------------------------------------------
+# a9  cut mesh
+# --------------------------------------------------------------------------------------------
+def first_seam_he(m: Hmesh, seam, v):
+    for h in m.cw(m.vert2half[v]):
+        if seam[m.edge[h]]:
+            return h
+    return m.vert2half[v]
+
+
+def cut_mesh(m: Hmesh, seam):
+    """parameterization.h:126-152; returns (cutV, cutF)."""
+    F = m.idx
+    cutF = np.empty_like(F)
+    cut2pos = []
+    for v in range(m.nV):
+        bgn = first_seam_he(m, seam, v)
+        for h in m.ccw(bgn):
+            if seam[m.edge[h]] or h == bgn:
+                cut2pos.append(v)
+            f = m.face[h]
+            for j in range(3):
+                if F[f, j] == v:
+                    cutF[f, j] = len(cut2pos) - 1
+    return m.pos[np.asarray(cut2pos)], cutF
+
+
+# --------------------------------------------------------------------------------------------
+# a10-a11  transitions, matchings, setup
+# --------------------------------------------------------------------------------------------
+def he2transidx(m: Hmesh, seam, singular):
+    """parameterization_setup.ipp:10-49 (closed meshes)."""
+    valence = np.zeros(m.nV, np.int64)
+    np.add.at(valence, m.edge2vert[seam, 0], 1)
+    np.add.at(valence, m.edge2vert[seam, 1], 1)
+    inside_sing = singular != 0
+    hti = np.full(m.nH, 32767, np.int64)
+    claimed = np.zeros(m.nE, bool)
+    tid = 1
+    for v in range(m.nV):
+        if (valence[v] == 2 and not inside_sing[v]) or valence[v] == 0:
+            continue
+        for cH in m.ccw(m.vert2half[v]):
+            cE = m.edge[cH]
+            if not seam[cE] or claimed[cE]:
+                continue
+            hti[cH] = tid
+            hti[m.twin[cH]] = -tid
+            claimed[cE] = True
+            jv = m.head[cH]
+            while valence[jv] == 2 and not inside_sing[jv]:
+                nh = None
+                for h in m.ccw(m.vert2half[jv]):
+                    if seam[m.edge[h]] and not claimed[m.edge[h]]:
+                        nh = h
+                        break
+                hti[nh] = tid
+                hti[m.twin[nh]] = -tid
+                claimed[m.edge[nh]] = True
+                jv = m.head[nh]
+            tid += 1
+    return hti, tid - 1
+
+
+def he2matching(m: Hmesh, matching, N):
+    h = np.arange(m.nH)
+    mm = np.where(m.is_canonical(h), -1, 1) * matching[m.edge[h]]
+    return mm % N   # == (N + m % N) % N for C truncating %
+
+
+def setup(m: Hmesh, cutF, n_cut, seam, singular, matching, N=4):
+    """parameterization_setup.ipp:51-170.  Returns a dict of the setup products."""
+    n = N // 2
+    lred = np.vstack([np.eye(n), -np.eye(n)])
+    hti, nT = he2transidx(m, seam, singular)
+    hem = he2matching(m, matching, N)
+    nV = m.nV
+    nR = nV + nT
+    inside_sing = singular != 0
+    nS = int(inside_sing.sum())
+    unit = np.zeros((N, N), np.int64)
+    for i in range(N):
+        unit[(i + 1) % N, i] = 1
+    perms = [np.eye(N, dtype=np.int64)]
+    for i in range(1, N):
+        perms.append(unit @ perms[-1])
+    I = np.eye(N, dtype=np.int64)
+    vr, vc, vv = [], [], []
+    cr, cc, cv = [], [], []
+    cur_c = 0
+    F = m.idx
+
+    def block(rr, cc_, vv_, mat, r0, c0):
+        ii, jj = np.nonzero(mat)
+        rr.extend((r0 + ii).tolist())
+        cc_.extend((c0 + jj).tolist())
+        vv_.extend(mat[ii, jj].tolist())
+
+    for v in range(nV):
+        pm = [I.copy()]
+        pidx = [v]
+        iv = -1
+        for h in m.ccw(first_seam_he(m, seam, v)):
+            f = m.face[h]
+            jv = -1
+            for j in range(3):
+                if F[f, j] == v:
+                    jv = cutF[f, j]
+            if jv != iv:
+                iv = jv
+                for k in range(len(pidx)):
+                    block(vr, vc, vv, pm[k], N * iv, N * pidx[k])
+            hn = m.twin[m.prev[h]]
+            if seam[m.edge[hn]]:
+                p = perms[hem[hn]]
+                t = hti[hn]
+                if t > 0:
+                    pm = [p @ x for x in pm]
+                    pm.append(I.copy())
+                    pidx.append(nV + t - 1)
+                else:
+                    pm.append(-I)
+                    pidx.append(nV - t - 1)
+                    pm = [p @ x for x in pm]
+        idcs = sorted(set(pidx))
+        mats = []
+        for j in idcs:
+            mt = np.zeros((N, N), np.int64)
+            for k in range(len(pidx)):
+                if pidx[k] == j:
+                    mt += pm[k]
+            if j == v:
+                mt -= I
+            mats.append(mt)
+        if any(np.abs(mt).max() != 0 for mt in mats):
+            for j, mt in zip(idcs, mats):
+                block(cr, cc, cv, mt, N * cur_c, N * j)
+            cur_c += 1
+    vtrans2cut = sp.csr_matrix((np.asarray(vv, float), (vr, vc)), shape=(N * n_cut, N * nR))
+    vtrans2cut.sum_duplicates()
+    vtrans2cut.eliminate_zeros()
+    constraint = sp.csr_matrix((np.asarray(cv, float), (cr, cc)), shape=(N * cur_c, N * nR))
+    constraint.sum_duplicates()
+    constraint.eliminate_zeros()
+    uncompress = sp.kron(sp.identity(nR), sp.csr_matrix(lred)).tocsr()
+    if nS == 0:
+        fixed = np.arange(n)
+    else:
+        iv0 = int(np.flatnonzero(inside_sing)[0])
+        fixed = n * iv0 + np.arange(n)
+    integer = (n * (nV + np.arange(nT))[:, None] + np.arange(n)[None, :]).ravel()
+    singular_idx = (n * np.flatnonzero(inside_sing)[:, None] + np.arange(n)[None, :]).ravel()
+    return dict(hti=hti, hem=hem, nT=nT, nR=nR, nS=nS, N=N, n=n,
+                vtrans2cut=vtrans2cut, constraint=constraint, uncompress=uncompress,
+                fixedIdcs=fixed, fixedVals=np.zeros(n), integerIdcs=integer,
+                singularIdcs=singular_idx)
+
+
+# --------------------------------------------------------------------------------------------
+# a13  independent rows, a14 kernel basis
+# --------------------------------------------------------------------------------------------
+def structural_product(A, B):
+    """A @ B keeping entries that cancel to zero (Eigen's sparse product keeps its structural
+    pattern; scipy's drops exact zeros)."""
+    P = (abs(sp.csr_matrix(A)) @ abs(sp.csr_matrix(B))).tocsr()
+    P.sort_indices()
+    V = (sp.csr_matrix(A) @ sp.csr_matrix(B)).tocsr()
+    V.sort_indices()
+    ncol = P.shape[1]
+    pr = np.repeat(np.arange(P.shape[0]), np.diff(P.indptr)).astype(np.int64)
+    vr = np.repeat(np.arange(V.shape[0]), np.diff(V.indptr)).astype(np.int64)
+    pk = pr * ncol + P.indices
+    vk = vr * ncol + V.indices
+    data = np.zeros(P.nnz)
+    data[np.searchsorted(pk, vk)] = V.data
+    return sp.csr_matrix((data, P.indices.copy(), P.indptr.copy()), shape=P.shape)
+
+
+def independent_rows(C, tol=1e-9):
+    """Greedy maximal independent row subset, in row order (two-pass Gram-Schmidt), computed on
+    the structurally non-zero columns."""
+    if sp.issparse(C):
+        C = sp.csr_matrix(C)
+        cols = np.unique(C.indices)
+        C = C[:, cols].toarray()
+    else:
+        C = np.asarray(C)
+    basis = []
+    keep = []
+    for i in range(C.shape[0]):
+        r = C[i].astype(np.float64).copy()
+        nr0 = np.linalg.norm(r)
+        if nr0 == 0:
+            continue
+        for _ in range(2):
+            for q in basis:
+                r -= (q @ r) * q
+        nr = np.linalg.norm(r)
+        if nr > tol * nr0:
+            basis.append(r / nr)
+            keep.append(i)
+    return np.asarray(keep, np.int64)
+
+
+def fullpiv_kernel(A):
+    """Null-space basis of a dense matrix by LU with complete pivoting (Eigen FullPivLU::kernel
+    semantics: pivot = first maximum |a_ij| of the trailing block in column-major order;
+    rank threshold = eps * min(rows, cols) * max pivot; basis is the identity on the free
+    columns and -U11^-1 U12 on the pivot columns)."""
+    A = np.array(A, np.float64, copy=True)
+    rows, cols = A.shape
+    size = min(rows, cols)
+    rowp = np.arange(rows)
+    colq = np.arange(cols)
+    maxpivot = 0.0
+    nzp = size
+    for k in range(size):
+        sub = np.abs(A[k:, k:])
+        flat = sub.T.ravel()          # column-major scan
+        pos = int(np.argmax(flat))    # first maximum
+        best = flat[pos]
+        if best == 0.0:
+            nzp = k
+            break
+        pc, pr = divmod(pos, rows - k)
+        pr += k
+        pc += k
+        maxpivot = max(maxpivot, best)
+        if pr != k:
+            A[[k, pr]] = A[[pr, k]]
+            rowp[[k, pr]] = rowp[[pr, k]]
+        if pc != k:
+            A[:, [k, pc]] = A[:, [pc, k]]
+            colq[[k, pc]] = colq[[pc, k]]
+        if k < rows - 1:
+            A[k + 1:, k] /= A[k, k]
+        if k < size - 1:
+            A[k + 1:, k + 1:] -= np.outer(A[k + 1:, k], A[k, k + 1:])
+    thr = np.finfo(np.float64).eps * size * maxpivot
+    piv = [i for i in range(nzp) if abs(A[i, i]) > thr]
+    rank = len(piv)
+    dimker = cols - rank
+    K = np.zeros((cols, dimker))
+    if dimker == 0:
+        return K
+    U = np.zeros((rank, cols))
+    for i, p in enumerate(piv):
+        U[i, i:] = A[p, i:]
+    # bring the pivot columns to the front (no-op when the pivots are 0..rank-1)
+    for i, p in enumerate(piv):
+        U[:, [i, p]] = U[:, [p, i]]
+    X = U[:, rank:].copy()
+    for i in range(rank - 1, -1, -1):   # back substitution U11 X = U12 (sequential sums)
+        s = X[i].copy()
+        for k in range(i + 1, rank):
+            s = s - U[i, k] * X[k]
+        X[i] = s / U[i, i]
+    Mfull = np.hstack([U[:, :rank], X])
+    for i in range(rank - 1, -1, -1):
+        p = piv[i]
+        Mfull[:, [i, p]] = Mfull[:, [p, i]]
+    for i in range(rank):
+        K[colq[i]] = -Mfull[i, rank:]
+    for k in range(dimker):
+        K[colq[rank + k], k] = 1.0
+    return K
+
+
+def build_ufull(Cfull):
+    """iter_rounding_init.h:195-251: UFull = permutation * blockdiag(I, kernel(CSmall))."""
+    Cfull = sp.csr_matrix(Cfull)
+    ncols = Cfull.shape[1]
+    uniqueJ = np.unique(Cfull.indices) if Cfull.nnz else np.zeros(0, np.int64)
+    if Cfull.shape[0] == 0:
+        return sp.identity(ncols, format="csr"), np.arange(ncols), np.zeros(0, np.int64), \
+            np.zeros((0, 0))
+    CSmall = Cfull[:, uniqueJ].toarray()
+    USmall = fullpiv_kernel(CSmall)
+    nonpart = np.setdiff1d(np.arange(ncols), uniqueJ)
+    npart = len(nonpart)
+    r = list(nonpart)
+    c = list(range(npart))
+    v = [1.0] * npart
+    ii, jj = np.nonzero(np.ones_like(USmall, bool))
+    r += uniqueJ[ii].tolist()
+    c += (npart + jj).tolist()
+    v += USmall[ii, jj].tolist()
+    UFull = sp.csr_matrix((v, (r, c)), shape=(ncols, npart + USmall.shape[1]))
+    return UFull, nonpart, uniqueJ, USmall
+
+
+# --------------------------------------------------------------------------------------------
+# a12  integ: G2 operator, target field, length
+# --------------------------------------------------------------------------------------------
+def gradient_operator(m: Hmesh, cutF, n_cut, N):
+    """parameterization_integ.ipp:8-28 (G2 only): rows 2N*f + 2k + {0,1}, cols N*cutv + k."""
+    V, F = m.pos, m.idx
+    rows, cols, vals = [], [], []
+    for j in range(3):
+        nxt = V[F[:, (j + 2) % 3]] - V[F[:, (j + 1) % 3]]
+        g = np.cross(m.faceNormal, nxt) / (m.faceArea * 2)[:, None]
+        gx = _dot3(g, m.faceBasisX)
+        gy = _dot3(g, m.faceBasisY)
+        for k in range(N):
+            c = N * cutF[:, j] + k
+            ir = 2 * N * np.arange(m.nF) + 2 * k
+            rows += [ir, ir + 1]
+            cols += [c, c]
+            vals += [gx, gy]
+    G2 = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                       shape=(2 * N * m.nF, N * n_cut))
+    return G2
+
+
+def target_field(m: Hmesh, ext, N):
+    norm = 0.0
+    blocks = np.stack([_norm3(ext[:, 3 * j:3 * j + 3]) for j in range(N)], 1)
+    norm = blocks.sum() / (N * m.nF)
+    F2 = np.empty((m.nF, 2 * N))
+    for i in range(N):
+        e = ext[:, 3 * i:3 * i + 3]
+        F2[:, 2 * i] = _dot3(e, m.faceBasisX)
+        F2[:, 2 * i + 1] = _dot3(e, m.faceBasisY)
+    return F2.ravel(), norm
+
+
+# --------------------------------------------------------------------------------------------
+# a14-a21  iterative rounding
+# --------------------------------------------------------------------------------------------
+class _LLT:
+    """CholeskyWrapper stand-in (iter_rounding.h:14-31): direct factorisation per call."""
+
+    def factorize(self, A):
+        self.lu = spla.splu(sp.csc_matrix(A))
+        return True
+
+    def solve(self, rhs):
+        return self.lu.solve(rhs)
+
+
+def lm_solve(st, max_iter=100, func_tol=1e-9, foo_tol=1e-9, stats=None):
+    """levenberg_marquardt.h:140-231 with DiagonalDamping(lambda = 0), verbose = false."""
+    ls = _LLT()
+    prevx = st.initial_solution().copy()
+    E, J = st.objective_jacobian(prevx, True)
+    x = prevx.copy()
+    it = 0
+    while True:
+        rhs = -(J.T @ E)
+        foo = np.abs(rhs).max() if rhs.size else 0.0
+        if foo < foo_tol:
+            x = prevx.copy()
+        ls.factorize((J.T @ J).tocsc())
+        if stats is not None:
+            stats["factorizations"] = stats.get("factorizations", 0) + 1
+        d = ls.solve(rhs)
+        if np.linalg.norm(d) < func_tol:
+            return True, prevx.copy()
+        e_prev = float(st.objective_jacobian(prevx, False)[0] @ st.objective_jacobian(prevx, False)[0])
+        Enew = st.objective_jacobian(prevx + d, False)[0]
+        e_new = float(Enew @ Enew)
+        if e_prev > e_new:
+            x = prevx + d
+            if abs(e_prev - e_new) < func_tol:
+                return False, x
+        else:
+            x = prevx.copy()
+        E, J = st.objective_jacobian(x, True)
+        if st.post_iteration(x):
+            return True, x
+        it += 1
+        prevx = x.copy()
+        if it > max_iter:
+            return False, x
+
+
+class NaiveIntegration:
+    """iter_rounding_init.h:16-233 (localInjectivity = false)."""
+    wInteg, wConst, wClose = 10e3, 10e3, 1.0
+
+    def __init__(self, G2, Cfull, F2, fixedIdcs, fixedVals, length, nF, N, n):
+        self.G2, self.F2, self.length = G2, F2, length
+        self.fixedIdcs, self.fixedVals = np.asarray(fixedIdcs), np.asarray(fixedVals, float)
+        self.UFull, self.nonpart, self.uniqueJ, self.USmall = build_ufull(Cfull)
+        UFull = self.UFull
+        X2F = (G2 @ UFull).tocsr()
+        X2F.eliminate_zeros()
+        self.X2F = X2F
+        E = (X2F.T @ X2F) * length
+        f = X2F.T @ F2
+        constMat = UFull[self.fixedIdcs, :]
+        nd = E.shape[0]
+        big = sp.bmat([[E, constMat.T], [constMat, None]]).tocsc()
+        sol = spla.splu(big).solve(np.concatenate([f, self.fixedVals]))
+        XSmall = sol[:nd]
+        self.XSmall = XSmall
+        self.x0 = UFull @ XSmall
+        self.nfull = UFull.shape[0]
+        l1 = len(F2)
+        self.UExt = sp.block_diag([UFull, sp.identity(l1)]).tocsr()
+        self.XF_Small = np.concatenate([XSmall, F2])
+        nx = UFull.shape[0]
+        gI = sp.hstack([-length * G2, sp.identity(l1)]).tocsr()
+        gC = sp.hstack([sp.csr_matrix((l1, nx)), sp.identity(l1)]).tocsr()
+        S = sp.csr_matrix((np.ones(len(self.fixedIdcs)),
+                           (np.arange(len(self.fixedIdcs)), self.fixedIdcs)),
+                          shape=(len(self.fixedIdcs), nx + l1))
+        self.J = sp.vstack([gI @ self.UExt * self.wInteg, gC @ self.UExt * self.wClose,
+                            S @ self.UExt * self.wConst]).tocsr()
+
+    def initial_solution(self):
+        return self.XF_Small
+
+    def post_iteration(self, x):
+        return False
+
+    def objective_jacobian(self, xf_, updateJ):
+        xf = self.UExt @ xf_
+        x = xf[:self.nfull]
+        f = xf[self.nfull:]
+        fI = f - self.length * (self.G2 @ x)
+        fC = f - self.F2
+        fK = x[self.fixedIdcs] - self.fixedVals
+        E = np.concatenate([fI * self.wInteg, fC * self.wClose, fK * self.wConst])
+        return E, self.J
+
+
+class SeamlessIntegration:
+    """iter_rounding_loop.h:10-125 (frac = 1, localInjectivity = false)."""
+    wInteg, wConst, wClose = 1.0, 10e4, 0.01
+
+    def __init__(self, ni: NaiveIntegration, xInit, F2, integerIdcs, singularIdcs, roundSeams):
+        self.UFull = ni.UFull
+        self.F2 = F2
+        self.X2F = (ni.G2 @ ni.UFull * ni.length).tocsr()
+        self.X2F.eliminate_zeros()
+        self.xInit = xInit.copy()
+        self.xCurr = xInit.copy()
+        self.xPrev = xInit.copy()
+        self.integerIdcs = list(np.asarray(integerIdcs).tolist())
+        self.singularIdcs = list(np.asarray(singularIdcs).tolist())
+        self.roundSeams = roundSeams
+        self.roundedSingulars = False
+        self.leftIdcs = list(self.integerIdcs if roundSeams else self.singularIdcs)
+        self.fixedIdcs, self.fixedVals = [], []
+        self.order_margin = []
+
+    def init_fixed_indices(self):
+        self.xPrev = self.xCurr.copy()
+        X = self.UFull @ self.xCurr
+        vals = X[self.leftIdcs]
+        d = np.abs(vals - cround(vals))
+        d = np.where(d < 1e-9, 0.0, d)            # near-integer ties resolved by position
+        k = int(np.argmin(d))                     # first minimum (strict < in the reference)
+        mind = d[k]
+        if len(d) > 1:
+            self.order_margin.append(float(np.partition(d, 1)[1] - mind))
+        idx = self.leftIdcs[k]
+        self.fixedIdcs.append(idx)
+        self.fixedVals.append(int(cround(X[idx])))
+        del self.leftIdcs[k]
+        if not self.leftIdcs and not self.roundSeams and not self.roundedSingulars:
+            self.leftIdcs = list(self.integerIdcs)
+            self.roundedSingulars = True
+        nx = self.UFull.shape[1]
+        S = sp.csr_matrix((np.ones(len(self.fixedIdcs)),
+                           (np.arange(len(self.fixedIdcs)), self.fixedIdcs)),
+                          shape=(len(self.fixedIdcs), self.UFull.shape[0]))
+        self.J = sp.vstack([self.X2F * self.wInteg, sp.identity(nx) * self.wClose,
+                            S @ self.UFull * self.wConst]).tocsr()
+        return mind > 10e-7
+
+    def initial_solution(self):
+        return self.xInit
+
+    def post_iteration(self, x):
+        return False
+
+    def objective_jacobian(self, xs, updateJ):
+        X = self.UFull @ xs
+        field = self.X2F @ xs
+        fI = field - self.F2
+        fC = xs - self.xPrev
+        fK = X[self.fixedIdcs] - np.asarray(self.fixedVals, float)
+        return np.concatenate([fI * self.wInteg, fC * self.wClose, fK * self.wConst]), self.J
+
+    def post_checking(self, x):
+        X = self.UFull @ x
+        v = X[self.fixedIdcs]
+        mx = np.abs(v - cround(v)).max() if len(v) else -1.0
+        self.xCurr = x.copy()
+        self.xInit = x.copy()
+        self.xPrev = x.copy()
+        return mx <= 10e-7
+
+
+def iterative_rounding(fixedIdcs, fixedVals, singularIdcs, integerIdcs, length, Cfull, G2,
+                       N, n, nF, seamless, roundSeams, F2, stats=None):
+    """iter_rounding.h:33-113 (localInjectivity = false).  Returns (success, fullx, info)."""
+    stats = {} if stats is None else stats
+    ni = NaiveIntegration(G2, Cfull, F2, fixedIdcs, fixedVals, length, nF, N, n)
+    info = dict(ni=ni, x0=ni.x0.copy())
+    if not seamless:
+        return True, ni.x0.copy(), info
+    _, xlm = lm_solve(ni, stats=stats)
+    fullx = (ni.UExt @ xlm)[:ni.nfull]
+    X_ = xlm[:ni.UFull.shape[1]]
+    F2_ = (ni.UExt @ xlm)[ni.nfull:]
+    info["x_ni_lm"] = fullx.copy()
+    si = SeamlessIntegration(ni, X_, F2_, integerIdcs, singularIdcs, roundSeams)
+    success, rounded = True, False
+    resolves = 0
+    xs = None
+    while si.leftIdcs:
+        if not si.init_fixed_indices():
+            continue
+        rounded = True
+        _, xs = lm_solve(si, max_iter=100, func_tol=1e-7, foo_tol=1e-7, stats=stats)
+        resolves += 1
+        if not si.post_checking(xs):
+            success = False
+            break
+    fullx = (ni.UFull @ xs) if rounded else ni.x0.copy()
+    info.update(si=si, fix_order=list(si.fixedIdcs), fix_vals=list(si.fixedVals),
+                resolves=resolves, margins=si.order_margin)
+    return success, fullx, info
+
+
+# --------------------------------------------------------------------------------------------
+# whole path (example_igm.cpp:13-31)
+# --------------------------------------------------------------------------------------------
+def run_field(V, F, N=4, seed=0, n_iter=50, x0=None):
+    m = Hmesh(V, F)
+    L = connection_laplacian(m, N)
+    M = mass_matrix(m)
+    if x0 is None:
+        x0 = seeded_init(m.nF, seed)
+    c = smallest_eig(L, M, x0, n_iter)
+    field = rosy_from_compressed(c, N)
+    return m, L, M, c, field
+
+
+def pipeline(V, F, ratio=0.02, N=4, seed=0, seamless=True, round_seams=False, n_iter=50,
+             x0=None, stop_after=None):
+    out = {}
+    m, L, M, c, field = run_field(V, F, N, seed, n_iter, x0)
+    out.update(mesh=m, L=L, M=M, compressed=c, field=field)
+    conn = compute_connection(m)
+    matching, effort = c_matching(m, field, conn, N)
+    singular = compute_singular(m, effort, N)
+    out.update(connection=conn, matching=matching, effort=effort, singular=singular)
+    if stop_after == "field":
+        return out
+    seam = compute_seam(m, singular)
+    cutV, cutF = cut_mesh(m, seam)
+    cfield, cmatch = combed_field(m, field, matching, seam, N)
+    ext = extrinsic_field(m, cfield)
+    out.update(seam=seam, cutV=cutV, cutF=cutF, combed=cfield, combed_matching=cmatch, ext=ext)
+    st = setup(m, cutF, len(cutV), seam, singular, cmatch, N)
+    out["setup"] = st
+    if stop_after == "setup":
+        return out
+    n = st["n"]
+    fullx2N = (st["vtrans2cut"] @ st["uncompress"]).tocsr()
+    Cfull = structural_product(st["constraint"], st["uncompress"])
+    keep = independent_rows(Cfull)
+    Cfull = Cfull[keep]
+    G2 = gradient_operator(m, cutF, len(cutV), N)
+    F2, norm = target_field(m, ext, N)
+    bbox = np.linalg.norm(cutV.max(0) - cutV.min(0))
+    length = bbox * ratio / norm
+    stats = {}
+    ok, fullx, info = iterative_rounding(st["fixedIdcs"], st["fixedVals"], st["singularIdcs"],
+                                         st["integerIdcs"], length, Cfull, (G2 @ fullx2N).tocsr(),
+                                         N, n, m.nF, seamless, round_seams, F2, stats)
+    NF = fullx2N @ fullx
+    nfn = NF.reshape(-1, N)
+    cfn = np.concatenate([nfn[cutF[:, j]] for j in range(3)], axis=1)
+    out.update(Cfull=Cfull, G2=G2, F2=F2, length=length, success=ok, fullx=fullx, nfn=nfn,
+               cfn=cfn, info=info, stats=stats, fullx2N=fullx2N)
+    return out

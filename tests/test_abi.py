@@ -1,0 +1,76 @@
+"""C ABI: the library loads, exports every symbol include/*.h declares, and its host-only
+entry points behave without a GPU."""
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import metriko_gb300 as M
+from metriko_gb300 import _lib
+from oracle import metriko_oracle as O
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_functions():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        text = h.read_text()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names.update(re.findall(r"\b(mtk_[a-z0-9_]+)\s*\(", text))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    L = M.lib()
+    names = declared_functions()
+    assert "mtk_field_smoothest" in names and "mtk_iterative_rounding" in names
+    for n in names:
+        assert hasattr(L, n), n
+    assert set(_lib.EXPORTS) == names
+
+
+def test_status_strings():
+    L = M.lib()
+    assert L.mtk_status_string(0).decode() == "ok"
+    assert "converged" in L.mtk_status_string(3).decode()
+    assert L.mtk_status_string(99).decode() == "unknown status"
+
+
+def test_default_opts():
+    o = M.solve_opts()
+    assert o.precision == M.PREC_MIXED and o.tol == 1e-8 and o.max_iter > 0
+
+
+@pytest.mark.parametrize("seed", [0, 1, 12345])
+def test_seeded_init_matches_oracle(seed):
+    a = M.seeded_init(1000, seed)
+    b = O.seeded_init(1000, seed)
+    assert np.array_equal(a, b)
+    assert np.abs(a.real).max() <= 1 and np.abs(a.imag).max() <= 1
+
+
+def test_topology_rejects_open_mesh():
+    V = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], float)
+    F = np.array([[0, 1, 2]], np.int32)
+    with pytest.raises(M.MetrikoError) as e:
+        M.topology_from_field(V, F, np.ones(1, complex))
+    assert e.value.status == _lib.BAD_INPUT
+
+
+def test_topology_rejects_bad_index():
+    V, F = M.meshgen.icosphere(1)
+    F = F.copy()
+    F[3, 1] = 10_000
+    with pytest.raises(M.MetrikoError):
+        M.topology_from_field(V, F, np.ones(len(F), complex))
+
+
+def test_ctx_create_without_gpu():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(M.MetrikoError) as e:
+        M.Context(0)
+    assert e.value.status == _lib.NO_DEVICE

@@ -1,0 +1,46 @@
+"""Host C++ topology stages (through the C ABI, no GPU) against the oracle: matching,
+singularities, seams, combing and the cut mesh are integer outputs and must be bit-exact."""
+import numpy as np
+import pytest
+
+import metriko_gb300 as M
+from metriko_gb300 import meshgen
+from oracle import metriko_oracle as O
+
+
+@pytest.mark.parametrize("name", ["ico2_noise", "ico3_noise", "ico4_noise", "torus_32x16", "torus_64x32"])
+def test_topology_matches_oracle(name):
+    V, F, ratio, rs = meshgen.workload(name)
+    ref = O.pipeline(V, F, ratio=ratio, round_seams=rs, stop_after="setup")
+    res = M.topology_from_field(V, F, ref["compressed"], ratio, rs)
+    assert np.array_equal(res["singular"], ref["singular"])
+    assert np.array_equal(res["seam"], ref["seam"])
+    assert np.array_equal(res["matching"], ref["combed_matching"])
+    assert np.array_equal(res["cutF"], ref["cutF"])
+    c = res["counts"]
+    st = ref["setup"]
+    assert c["nCut"] == len(ref["cutV"]) and c["nT"] == st["nT"] and c["nS"] == st["nS"]
+    assert c["nFull"] == st["n"] * st["nR"]
+
+
+def test_topology_length_and_ufull_sizes():
+    name = "ico3_noise"
+    V, F, ratio, rs = meshgen.workload(name)
+    ref = O.pipeline(V, F, ratio=ratio, round_seams=rs)
+    res = M.topology_from_field(V, F, ref["compressed"], ratio, rs)
+    assert abs(res["length"] - ref["length"]) <= 1e-12 * ref["length"]
+    ni = ref["info"]["ni"]
+    assert res["counts"]["nJ"] == len(ni.uniqueJ)
+    assert res["counts"]["nZ"] == ni.USmall.shape[1]
+
+
+def test_seam_is_tree_through_singularities():
+    """On a sphere the seam is a tree touching every singular vertex."""
+    V, F, ratio, rs = meshgen.workload("ico3_noise")
+    ref = O.pipeline(V, F, ratio=ratio, stop_after="field")
+    res = M.topology_from_field(V, F, ref["compressed"], ratio, rs)
+    m = O.Hmesh(V, F)
+    E = m.edge2vert[res["seam"]]
+    verts = np.unique(E)
+    assert len(E) == len(verts) - 1          # a tree
+    assert set(np.flatnonzero(res["singular"])) <= set(verts.tolist())
