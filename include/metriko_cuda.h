@@ -77,6 +77,14 @@ typedef struct {
     int64_t resolves;           /* IGM re-solves (rounded variables that needed a solve) */
     int64_t lm_iterations;      /* LM iterations over all LM solves                      */
     double min_order_margin;    /* smallest gap between best and second-best rounding    */
+    /* persistent PCG kernels: launches, device ms (CUDA events around each launch) and
+       algorithmic bytes (per-iteration formula evaluated on the actual sizes / nnz)       */
+    int64_t field_pcg_launches;
+    double field_pcg_ms;
+    double field_pcg_bytes;
+    int64_t igm_pcg_launches;
+    double igm_pcg_ms;
+    double igm_pcg_bytes;
 } mtk_stats;
 
 const char* mtk_status_string(int status);

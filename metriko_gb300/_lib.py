@@ -41,7 +41,9 @@ class Stats(C.Structure):
                 ("max_rel_residual", C.c_double), ("ms_field", C.c_double),
                 ("ms_integrate", C.c_double), ("ms_rounding", C.c_double), ("ms_host", C.c_double),
                 ("ms_total", C.c_double), ("resolves", C.c_int64), ("lm_iterations", C.c_int64),
-                ("min_order_margin", C.c_double)]
+                ("min_order_margin", C.c_double), ("field_pcg_launches", C.c_int64),
+                ("field_pcg_ms", C.c_double), ("field_pcg_bytes", C.c_double), ("igm_pcg_launches", C.c_int64),
+                ("igm_pcg_ms", C.c_double), ("igm_pcg_bytes", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -33,9 +33,10 @@ void mtk_set_last_error(const char* msg, const char* file, int line);
 
 namespace mtk {
 
-constexpr int kBlock = 256;               // threads per CTA of the persistent solvers
-constexpr int kWarps = kBlock / 32;
-constexpr long long kSpinLimit = 1LL << 25;   // ~ seconds with nanosleep backoff
+constexpr int kBlock = 1024;              // threads per CTA (persistent solvers: one CTA per SM)
+constexpr int kWarps = kBlock / 32;      // upper bound on warps per CTA
+constexpr int kStream = 256;              // threads per CTA of the streaming (non-persistent) kernels
+constexpr long long kSpinLimit = 1LL << 24;   // bounded spin (about a second with backoff)
 
 struct GridBarrier {
     unsigned int* count;       // arrivals in the current generation
@@ -55,8 +56,21 @@ __device__ __forceinline__ int ld_volatile(const int* p) {
     return *reinterpret_cast<const volatile int*>(p);
 }
 
-// Returns false (in every thread of the block) if the barrier timed out or an error was
-// already recorded; callers then leave their loop.
+__device__ __forceinline__ unsigned int atom_add_acq_rel(unsigned int* p, unsigned int v) {
+    unsigned int old;
+    asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+__device__ __forceinline__ void st_relaxed(unsigned int* p, unsigned int v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Grid-wide barrier for a cooperative launch (one CTA per SM).  Thread 0 of every CTA
+// arrives with an acq_rel atomic; the last arrival resets the counter and publishes the next
+// generation with a release store; the others poll it with acquire loads (tight spin first,
+// then nanosleep backoff) for at most kSpinLimit polls, after which MTK_ERR_TIMEOUT is
+// recorded and every CTA leaves.  Returns false (in every thread) on timeout or a recorded
+// error; callers then leave their loop.
 __device__ __forceinline__ bool grid_sync(const GridBarrier& b) {
     __shared__ int s_ok;
     __syncthreads();
@@ -64,21 +78,18 @@ __device__ __forceinline__ bool grid_sync(const GridBarrier& b) {
         int ok = ld_volatile(b.err) == 0;
         if (ok) {
             unsigned int g = ld_acquire(b.gen);
-            __threadfence();
-            unsigned int arrived = atomicAdd(b.count, 1u);
+            unsigned int arrived = atom_add_acq_rel(b.count, 1u);
             if (arrived == gridDim.x - 1) {
-                atomicExch(b.count, 0u);
-                __threadfence();
+                st_relaxed(b.count, 0u);
                 st_release(b.gen, g + 1);
             } else {
                 long long spins = 0;
                 while (ld_acquire(b.gen) == g) {
                     if (++spins > kSpinLimit) { atomicExch(b.err, (int)MTK_ERR_TIMEOUT); ok = 0; break; }
-                    if (ld_volatile(b.err) != 0) { ok = 0; break; }
-                    __nanosleep(64);
+                    if ((spins & 255) == 0 && ld_volatile(b.err) != 0) { ok = 0; break; }
+                    if (spins > 2048) __nanosleep(100);
                 }
             }
-            __threadfence();
         }
         s_ok = ok;
     }
@@ -99,10 +110,11 @@ __device__ __forceinline__ void block_sum(T (&v)[K]) {
         if (lane == 0) s_red[k][warp] = x;
     }
     __syncthreads();
+    const int nw = (int)(blockDim.x >> 5);
 #pragma unroll
     for (int k = 0; k < K; k++) {
         T x = T(0);
-        for (int w = 0; w < kWarps; w++) x += s_red[k][w];
+        for (int w = 0; w < nw; w++) x += s_red[k][w];
         v[k] = x;
     }
     __syncthreads();

@@ -55,6 +55,8 @@ extern "C" int mtk_ctx_create(int device, mtk_ctx** out) {
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev_a);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev_b);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev_k0);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev_k1);
     if (e == cudaSuccess) e = cudaMalloc(&c->bar, 4 * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMalloc(&c->dev_err, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&c->partials, sizeof(double) * 16 * c->partial_blocks);
@@ -86,6 +88,8 @@ extern "C" int mtk_ctx_destroy(mtk_ctx* c) {
     if (c->h_int) cudaFreeHost(c->h_int);
     if (c->ev_a) cudaEventDestroy(c->ev_a);
     if (c->ev_b) cudaEventDestroy(c->ev_b);
+    if (c->ev_k0) cudaEventDestroy(c->ev_k0);
+    if (c->ev_k1) cudaEventDestroy(c->ev_k1);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return MTK_OK;

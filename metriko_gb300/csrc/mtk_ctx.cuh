@@ -12,6 +12,7 @@ struct mtk_ctx {
     int num_sms = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev_a = nullptr, ev_b = nullptr;
+    cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr;   // around each persistent-kernel launch
     // bounded grid barrier state (3 words) + error flag, and reduction scratch
     unsigned int* bar = nullptr;   // [0] count, [1] generation
     int* dev_err = nullptr;
@@ -69,7 +70,7 @@ int launch_persistent(mtk_ctx* c, K kernel, int* grid_out, Args... args) {
     int per_sm = 0;
     MTK_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0));
     if (per_sm < 1) { mtk_set_last_error("persistent kernel does not fit on an SM", __FILE__, __LINE__); return MTK_ERR_CUDA; }
-    per_sm = per_sm > 4 ? 4 : per_sm;
+    per_sm = 1;   // one CTA per SM: fewest barrier arrivals
     int grid = c->num_sms * per_sm;
     if (grid > c->partial_blocks) grid = c->partial_blocks;
     if (grid_out) *grid_out = grid;
@@ -80,6 +81,6 @@ int launch_persistent(mtk_ctx* c, K kernel, int* grid_out, Args... args) {
     return MTK_OK;
 }
 
-inline int stream_grid(mtk_ctx* c) { return c->num_sms * 4; }
+inline int stream_grid(mtk_ctx* c) { return c->num_sms * 2; }
 
 }  // namespace mtk

@@ -304,12 +304,14 @@ struct FieldSolver {
     DBuf<double2> v64, u, b, Lu, x, r, z64, p64, q64;
     DBuf<float2> v32, r32, e32, z32, p32, q32;
     int grid = 0;
+    double pcg_ms = 0, pcg_bytes = 0;
+    long long pcg_launches = 0;
 
     ComplexEll<double> A64() const { return {n, nbr.p, v64.p, d64.p}; }
     ComplexEll<float> A32() const { return {n, nbr.p, v32.p, d32.p}; }
 
     int finalize(int nb, int K) {
-        finalize_partials<<<1, kBlock, 0, c->stream>>>(c->partials, nb, K, c->scalars);
+        finalize_partials<<<1, kStream, 0, c->stream>>>(c->partials, nb, K, c->scalars);
         c->kernels++;
         MTK_CUDA_TRY(cudaGetLastError());
         return MTK_OK;
@@ -324,10 +326,21 @@ struct FieldSolver {
     int pcg(ComplexEll<T> A, const T* minv, const V2* bb, V2* xx, V2* rr, V2* zz, V2* pp, V2* qq, double tol2,
             int maxit, long long* iters, double* final_rr) {
         int g = 0;
+        MTK_TRY(reset_barrier(c));
+        MTK_CUDA_TRY(cudaEventRecord(c->ev_k0, c->stream));
         MTK_TRY(launch_persistent(c, pcg_complex<T>, &g, A, minv, bb, xx, rr, zz, pp, qq,
                                   reinterpret_cast<T*>(c->partials), barrier_of(c), tol2, maxit, c->dev_int));
+        MTK_CUDA_TRY(cudaEventRecord(c->ev_k1, c->stream));
         MTK_CUDA_TRY(cudaMemcpyAsync(c->h_int, c->dev_int, 8 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
         MTK_CUDA_TRY(cudaStreamSynchronize(c->stream));
+        float kms = 0;
+        cudaEventElapsedTime(&kms, c->ev_k0, c->ev_k1);
+        pcg_ms += kms;
+        pcg_launches++;
+        // algorithmic bytes per iteration and row: SpMV 3*(2T+4) + T + 2*2T, x/r/p updates
+        // 3 * 3*2T, z = M^-1 r: T + 2T (the r read is shared with the r update)
+        const double per_row = 3.0 * (2 * sizeof(T) + 4) + sizeof(T) + 4.0 * sizeof(T) + 18.0 * sizeof(T) + 3.0 * sizeof(T);
+        pcg_bytes += per_row * (double)n * (double)(c->h_int[1] + 1);
         *iters += c->h_int[1];
         if (final_rr) *final_rr = reinterpret_cast<double*>(c->h_int + 4)[0];
         int st = c->h_int[0];
@@ -373,7 +386,7 @@ extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const 
         MTK_TRY(S.z64.alloc(n)); MTK_TRY(S.p64.alloc(n)); MTK_TRY(S.q64.alloc(n));
     }
     const int G = stream_grid(c);
-    field_assemble<<<G, kBlock, 0, st>>>(n, nRosy, S.nbr_in.p, S.theta.p, S.area.p, S.nbr.p, S.v64.p, S.v32.p, S.d64.p,
+    field_assemble<<<G, kStream, 0, st>>>(n, nRosy, S.nbr_in.p, S.theta.p, S.area.p, S.nbr.p, S.v64.p, S.v32.p, S.d64.p,
                                          S.d32.p, S.inv64.p, S.inv32.p, S.area32.p);
     c->kernels++;
     MTK_CUDA_TRY(cudaGetLastError());
@@ -383,10 +396,10 @@ extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const 
     const double tol = opts.tol;
     for (int k = 0; k < n_iter; k++) {
         // b = M u, Galerkin start x = u (u^H M u)/(u^H L u), r = b - L x
-        power_prepare<<<G, kBlock, 0, st>>>(S.A64(), S.area.p, S.u.p, S.b.p, S.Lu.p, c->partials);
+        power_prepare<<<G, kStream, 0, st>>>(S.A64(), S.area.p, S.u.p, S.b.p, S.Lu.p, c->partials);
         c->kernels++;
         MTK_TRY(S.finalize(G, 3));
-        power_start<<<G, kBlock, 0, st>>>(n, c->scalars, S.u.p, S.b.p, S.Lu.p, S.x.p, S.r.p, mixed ? S.r32.p : nullptr,
+        power_start<<<G, kStream, 0, st>>>(n, c->scalars, S.u.p, S.b.p, S.Lu.p, S.x.p, S.r.p, mixed ? S.r32.p : nullptr,
                                           c->partials);
         c->kernels++;
         MTK_CUDA_TRY(cudaMemcpyAsync(c->h_scalars, c->scalars, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -404,7 +417,7 @@ extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const 
                                            opts.max_iter, &iters, &frr);
             if (s != MTK_OK) return s;
             // true FP64 residual of the result
-            residual64<<<G, kBlock, 0, st>>>(S.A64(), S.b.p, S.x.p, S.r.p, nullptr, c->partials);
+            residual64<<<G, kStream, 0, st>>>(S.A64(), S.b.p, S.x.p, S.r.p, nullptr, c->partials);
             c->kernels++;
             MTK_TRY(S.finalize(G, 1));
             MTK_TRY(S.read_scalars(1));
@@ -419,14 +432,14 @@ extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const 
                 double itol = opts.inner_tol;
                 double need = std::sqrt(goal2 / rr) * 0.5;
                 if (need > itol) itol = need;
-                zero_f2<<<G, kBlock, 0, st>>>(n, S.e32.p);
+                zero_f2<<<G, kStream, 0, st>>>(n, S.e32.p);
                 c->kernels++;
                 int s = S.pcg<float, float2>(S.A32(), S.inv32.p, S.r32.p, S.e32.p, S.z32.p /*r*/, S.p32.p /*z*/,
                                              S.q32.p /*p*/, reinterpret_cast<float2*>(S.Lu.p) /*q*/, itol * itol * rr,
                                              opts.max_iter, &iters, nullptr);
                 if (s == MTK_ERR_TIMEOUT || s == MTK_ERR_BREAKDOWN) return s;
-                add_correction<<<G, kBlock, 0, st>>>(n, S.e32.p, S.x.p);
-                residual64<<<G, kBlock, 0, st>>>(S.A64(), S.b.p, S.x.p, S.r.p, S.r32.p, c->partials);
+                add_correction<<<G, kStream, 0, st>>>(n, S.e32.p, S.x.p);
+                residual64<<<G, kStream, 0, st>>>(S.A64(), S.b.p, S.x.p, S.r.p, S.r32.p, c->partials);
                 c->kernels += 2;
                 MTK_TRY(S.finalize(G, 1));
                 MTK_TRY(S.read_scalars(1));
@@ -437,10 +450,10 @@ extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const 
         double rel = bnorm2 > 0 ? std::sqrt(rr / bnorm2) : 0.0;
         if (rel > worst) worst = rel;
         // x /= sqrt|x^H M x|; u = x
-        mnorm_partial<<<G, kBlock, 0, st>>>(n, S.area.p, S.x.p, c->partials);
+        mnorm_partial<<<G, kStream, 0, st>>>(n, S.area.p, S.x.p, c->partials);
         c->kernels++;
         MTK_TRY(S.finalize(G, 1));
-        normalize_to<<<G, kBlock, 0, st>>>(n, c->scalars, S.x.p, S.u.p);
+        normalize_to<<<G, kStream, 0, st>>>(n, c->scalars, S.x.p, S.u.p);
         c->kernels++;
         MTK_CUDA_TRY(cudaGetLastError());
     }
@@ -456,6 +469,9 @@ extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const 
         stats->spmv_calls += iters + refines + n_iter;
         if (worst > stats->max_rel_residual) stats->max_rel_residual = worst;
         stats->ms_field += ms;
+        stats->field_pcg_launches += S.pcg_launches;
+        stats->field_pcg_ms += S.pcg_ms;
+        stats->field_pcg_bytes += S.pcg_bytes;
         stats->kernel_launches = c->kernels;
     }
     return MTK_OK;

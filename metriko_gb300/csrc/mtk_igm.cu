@@ -24,6 +24,8 @@
 // solution is O(1 / penalty).
 #include <algorithm>
 #include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <cmath>
 #include <vector>
 
@@ -264,7 +266,15 @@ __global__ void __launch_bounds__(kBlock) igm_pcg(IgmOp<T> A, ZProj<T> P, const 
             gather_partials<T, 1>(partials + 2 * gridDim.x, pq1);
             igm_apply_z(A, P, zs.pz, zs.qz, zs);
             T pq = pq1[0] + smem_dot(zs.pz, zs.qz, nZ);
-            if (!(pq > T(0))) { status = 4; break; }
+            if (!(pq > T(0))) {
+                status = 4;
+                if (blockIdx.x == 0 && threadIdx.x == 0) {
+                    reinterpret_cast<double*>(out + 6)[0] = (double)pq;
+                    reinterpret_cast<double*>(out + 8)[0] = (double)rz;
+                    reinterpret_cast<double*>(out + 10)[0] = (double)pq1[0];
+                }
+                break;
+            }
             T alpha = rz / pq;
             part[0] = T(0);
             part[1] = T(0);
@@ -470,49 +480,67 @@ __global__ void expand_full(int nFull, const int* __restrict__ full2y, const int
 }
 
 // Greedy rounding choice (iter_rounding_loop.h:29-43), one block: d_i = |X - round X| over the
-// left indices; d < 1e-9 counts as 0 (round-off ties); first minimum wins.
+// left indices (d <= 1e-6 counts as 0, the reference's integrality threshold); the pick is the
+// first position whose d is within 1e-6 of the minimum -- the reference's strict '<' among
+// values that close is decided by round-off (constraint-linked variables share their
+// fractional part).  out = [position, d, X, smallest d outside the tie group].
+__device__ __forceinline__ double left_value(int i, const int* __restrict__ full2y, const int* __restrict__ full2j,
+                                             int nY, int nZ, const double* __restrict__ Us, const double* __restrict__ xs) {
+    int y = full2y[i];
+    if (y >= 0) return xs[y];
+    int s = full2j[i];
+    double X = 0;
+    for (int j = 0; j < nZ; j++) X += Us[(size_t)s * nZ + j] * xs[nY + j];
+    return X;
+}
+
 __global__ void round_argmin(int nLeft, const int* __restrict__ left, const int* __restrict__ full2y,
                              const int* __restrict__ full2j, int nY, int nZ, const double* __restrict__ Us,
-                             const double* __restrict__ xs, double* out /* [pos, d, X, second d] */) {
-    __shared__ double sd[kBlock];
-    __shared__ int si[kBlock];
-    __shared__ double sX[kBlock];
-    __shared__ double s2[kBlock];
-    double bd = 1e300, b2 = 1e300, bX = 0;
-    int bi = 0x7fffffff;
+                             const double* __restrict__ xs, double* out) {
+    __shared__ double sd[kStream];
+    __shared__ int si[kStream];
+    // pass 1: minimum distance
+    double bd = 1e300;
     for (int t = threadIdx.x; t < nLeft; t += blockDim.x) {
-        int i = left[t];
-        int y = full2y[i];
-        double X;
-        if (y >= 0) X = xs[y];
-        else {
-            int s = full2j[i];
-            X = 0;
-            for (int j = 0; j < nZ; j++) X += Us[(size_t)s * nZ + j] * xs[nY + j];
-        }
+        double X = left_value(left[t], full2y, full2j, nY, nZ, Us, xs);
         double d = fabs(X - round(X));
-        if (d < 1e-9) d = 0.0;
-        if (d < bd || (d == bd && t < bi)) { b2 = bd; bd = d; bi = t; bX = X; }
-        else if (d < b2) b2 = d;
+        if (d <= 10e-7) d = 0.0;
+        bd = fmin(bd, d);
     }
-    sd[threadIdx.x] = bd; si[threadIdx.x] = bi; sX[threadIdx.x] = bX; s2[threadIdx.x] = b2;
+    sd[threadIdx.x] = bd;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sd[threadIdx.x] = fmin(sd[threadIdx.x], sd[threadIdx.x + w]);
+        __syncthreads();
+    }
+    const double dmin = sd[0];
+    __syncthreads();
+    // pass 2: first position inside the tie group, and the best distance outside it
+    int bi = 0x7fffffff;
+    double bX = 0, bdist = 0, other = 1e300;
+    for (int t = threadIdx.x; t < nLeft; t += blockDim.x) {
+        double X = left_value(left[t], full2y, full2j, nY, nZ, Us, xs);
+        double d = fabs(X - round(X));
+        if (d <= 10e-7) d = 0.0;
+        if (d <= dmin + 10e-7) {
+            if (t < bi) { bi = t; bX = X; bdist = d; }
+        } else {
+            other = fmin(other, d);
+        }
+    }
+    __shared__ double sX[kStream], sdd[kStream], so[kStream];
+    si[threadIdx.x] = bi; sX[threadIdx.x] = bX; sdd[threadIdx.x] = bdist; so[threadIdx.x] = other;
     __syncthreads();
     for (int w = blockDim.x / 2; w > 0; w >>= 1) {
         if (threadIdx.x < w) {
-            double d1 = sd[threadIdx.x], d2 = sd[threadIdx.x + w];
-            int i1 = si[threadIdx.x], i2 = si[threadIdx.x + w];
-            double sec = fmin(s2[threadIdx.x], s2[threadIdx.x + w]);
-            if (d2 < d1 || (d2 == d1 && i2 < i1)) {
-                sec = fmin(sec, d1);
-                sd[threadIdx.x] = d2; si[threadIdx.x] = i2; sX[threadIdx.x] = sX[threadIdx.x + w];
-            } else {
-                sec = fmin(sec, d2);
+            if (si[threadIdx.x + w] < si[threadIdx.x]) {
+                si[threadIdx.x] = si[threadIdx.x + w]; sX[threadIdx.x] = sX[threadIdx.x + w]; sdd[threadIdx.x] = sdd[threadIdx.x + w];
             }
-            s2[threadIdx.x] = sec;
+            so[threadIdx.x] = fmin(so[threadIdx.x], so[threadIdx.x + w]);
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0) { out[0] = (double)si[0]; out[1] = sd[0]; out[2] = sX[0]; out[3] = s2[0]; }
+    if (threadIdx.x == 0) { out[0] = (double)si[0]; out[1] = sdd[0]; out[2] = sX[0]; out[3] = so[0]; }
 }
 
 // NI-LM field block (Gauss-Newton with the diagonal field block eliminated exactly):
@@ -565,6 +593,29 @@ __global__ void to_f32(int n, const double* __restrict__ a, float* b) {
 __global__ void add_f32(int n, const float* __restrict__ e, double* x) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] += (double)e[i];
 }
+
+// x_z += P_z e_z with the FP64 projector (one block).  The FP32 solve's own projector leaves
+// O(1e-7) components along the constraint rows; the FP64 residual cannot see components in
+// the null space of K, so they are removed here before the correction is accumulated.
+__global__ void add_z_projected(int nY, int nZ, int kq, const double* __restrict__ Q, const float* __restrict__ e,
+                                double* x) {
+    extern __shared__ double sz[];
+    double* ez = sz;
+    double* t = sz + nZ;
+    for (int j = threadIdx.x; j < nZ; j += blockDim.x) ez[j] = (double)e[nY + j];
+    __syncthreads();
+    for (int a = threadIdx.x; a < kq; a += blockDim.x) {
+        double v = 0;
+        for (int j = 0; j < nZ; j++) v += Q[(size_t)a * nZ + j] * ez[j];
+        t[a] = v;
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < nZ; j += blockDim.x) {
+        double v = ez[j];
+        for (int a = 0; a < kq; a++) v -= Q[(size_t)a * nZ + j] * t[a];
+        x[nY + j] += v;
+    }
+}
 __global__ void dot_partial(int n, const double* __restrict__ a, const double* __restrict__ b, double* partials) {
     double v[1] = {0};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[0] += a[i] * b[i];
@@ -601,6 +652,19 @@ struct Igm {
     std::vector<unsigned char> h_fixy;
     int kq = 0;
     size_t smem64 = 0, smem32 = 0;
+    double pcg_ms = 0, pcg_bytes = 0;
+    long long pcg_launches = 0;
+    long long nnzW = 0, nnzS = 0, nnzYT = 0;
+
+    // Algorithmic bytes of one projected-PCG iteration (operator chain + vector updates):
+    //   W gather   nnzW (tag 4 + val T + x T) + 2 nCut (ptr 4 + U write T)
+    //   S product  nnzS (col 4 + val T) + nCut ptr 4 + U read 2T + Qc write 2T
+    //   W^T gather nnzYT (row 4 + val T + Qc T) + nY (ptr 4 + p T + q write T)
+    //   vectors    nY * 11 T  (x, r, p read+write; z = M^-1 r: minv read + z write)
+    double iter_bytes(size_t T) const {
+        return (double)nnzW * (4 + 2 * T) + 2.0 * nCut * (4 + T) + (double)nnzS * (4 + T) + nCut * (4.0 + 4 * T) +
+               (double)nnzYT * (4 + 2 * T) + (double)nY * (4 + 2 * T) + (double)nY * 11 * T;
+    }
 
     IgmOp<double> op64(double scale, double shift) {
         return {nCut, nY, nZ, nJ, w_ptr.p, w_tag.p, w_val.p, s_ptr.p, s_col.p, s_val.p, yt_ptr.p, yt_row.p, yt_val.p,
@@ -619,7 +683,7 @@ struct Igm {
         int per_sm = 0;
         MTK_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, smem));
         if (per_sm < 1) { mtk_set_last_error("IGM solver does not fit on an SM", __FILE__, __LINE__); return MTK_ERR_CUDA; }
-        per_sm = std::min(per_sm, 4);
+        per_sm = 1;   // one CTA per SM
         int grid = std::min(c->num_sms * per_sm, c->partial_blocks);
         const unsigned char* fx = fixy.p;
         T* partials = reinterpret_cast<T*>(c->partials);
@@ -628,27 +692,47 @@ struct Igm {
         void* params[] = {&A, &P, (void*)&fx, (void*)&minv, (void*)&b, (void*)&x, (void*)&r, (void*)&z, (void*)&p,
                           (void*)&q, (void*)&partials, &bar, &tol2, &maxit, &mode, (void*)&out};
         MTK_TRY(reset_barrier(c));
+        MTK_CUDA_TRY(cudaEventRecord(c->ev_k0, st));
         MTK_CUDA_TRY(cudaLaunchCooperativeKernel(reinterpret_cast<void*>(kern), dim3(grid), dim3(kBlock), params, smem, st));
+        MTK_CUDA_TRY(cudaEventRecord(c->ev_k1, st));
         c->kernels++;
         MTK_CUDA_TRY(cudaMemcpyAsync(c->h_int, c->dev_int, 8 * sizeof(int), cudaMemcpyDeviceToHost, st));
         MTK_CUDA_TRY(cudaStreamSynchronize(st));
+        float kms = 0;
+        cudaEventElapsedTime(&kms, c->ev_k0, c->ev_k1);
+        pcg_ms += kms;
+        pcg_launches++;
+        pcg_bytes += iter_bytes(sizeof(T)) * (double)(c->h_int[1] + 1);
         if (iters) *iters += c->h_int[1];
         if (rr_out) *rr_out = reinterpret_cast<double*>(c->h_int + 4)[0];
         int s = c->h_int[0];
+        if (debug())
+            fprintf(stderr, "[igm_pcg T=%zu mode=%d] status=%d iters=%d rr=%.3e tol2=%.3e kq=%d%s\n", sizeof(T), mode, s,
+                    c->h_int[1], reinterpret_cast<double*>(c->h_int + 4)[0], tol2, kq,
+                    s == 4 ? " (breakdown)" : "");
+        if (s == 4 && debug())
+            fprintf(stderr, "   pq=%.3e rz=%.3e pq_y=%.3e\n", reinterpret_cast<double*>(c->h_int + 6)[0],
+                    reinterpret_cast<double*>(c->h_int + 8)[0], reinterpret_cast<double*>(c->h_int + 10)[0]);
         if (s == 5) return MTK_ERR_TIMEOUT;
         if (s == 4) return MTK_ERR_BREAKDOWN;
         if (s == 3) return MTK_ERR_NOT_CONVERGED;
         return MTK_OK;
     }
 
+    static bool debug() {
+        static int d = -1;
+        if (d < 0) { const char* e = getenv("MTK_DEBUG"); d = (e && *e == '1') ? 1 : 0; }
+        return d == 1;
+    }
+
     int grid() const { return stream_grid(c); }
 
     // b = scale * UFull^T W^T hb(F) + shift * prev   (prev may be null)
     int build_rhs(const double* Fface, double scale, double shift, const double* prevx, double* b) {
-        cut_loads<<<grid(), kBlock, 0, st>>>(nCut, vf_ptr.p, vf_face.p, cutF.p, grad.p, Fface, hb.p);
-        rhs_reduce<<<grid(), kBlock, 0, st>>>(nY, nJ, yt_ptr.p, yt_row.p, yt_val.p, jt_ptr.p, jt_row.p, jt_val.p, hb.p, scale,
+        cut_loads<<<grid(), kStream, 0, st>>>(nCut, vf_ptr.p, vf_face.p, cutF.p, grad.p, Fface, hb.p);
+        rhs_reduce<<<grid(), kStream, 0, st>>>(nY, nJ, yt_ptr.p, yt_row.p, yt_val.p, jt_ptr.p, jt_row.p, jt_val.p, hb.p, scale,
                                               shift, prevx, fixy.p, b, XbJ.p);
-        rhs_reduce_z<<<1, kBlock, 0, st>>>(nY, nZ, nJ, Us.p, XbJ.p, scale, shift, prevx, b);
+        rhs_reduce_z<<<1, kStream, 0, st>>>(nY, nZ, nJ, Us.p, XbJ.p, scale, shift, prevx, b);
         c->kernels += 3;
         MTK_CUDA_TRY(cudaGetLastError());
         return MTK_OK;
@@ -656,8 +740,8 @@ struct Igm {
 
     int dot(const double* a, const double* b, int n, double* out) {
         int G = grid();
-        dot_partial<<<G, kBlock, 0, st>>>(n, a, b, c->partials);
-        finalize1<<<1, kBlock, 0, st>>>(c->partials, G, c->scalars);
+        dot_partial<<<G, kStream, 0, st>>>(n, a, b, c->partials);
+        finalize1<<<1, kStream, 0, st>>>(c->partials, G, c->scalars);
         c->kernels += 2;
         MTK_CUDA_TRY(cudaMemcpyAsync(c->h_scalars, c->scalars, sizeof(double), cudaMemcpyDeviceToHost, st));
         MTK_CUDA_TRY(cudaStreamSynchronize(st));
@@ -693,15 +777,17 @@ struct Igm {
                 double itol = o.inner_tol;
                 double need = std::sqrt(goal2 / rr) * 0.5;
                 if (need > itol) itol = need;
-                to_f32<<<grid(), kBlock, 0, st>>>(nRed, r64.p, r32.p);
+                to_f32<<<grid(), kStream, 0, st>>>(nRed, r64.p, r32.p);
                 MTK_CUDA_TRY(cudaMemsetAsync(e32.p, 0, sizeof(float) * nRed, st));
                 c->kernels++;
                 int s = run_pcg<float>(op32(scale, shift), ZProj<float>{kq, Qz32.p, Mz32.p}, minvy32.p, r32.p, e32.p,
                                        z32.p /*r*/, p32.p /*z*/, q32.p /*p*/, reinterpret_cast<float*>(Xfull.p) /*q*/,
                                        itol * itol * rr, o.max_iter, 0, smem32, &iters, nullptr);
                 if (s == MTK_ERR_TIMEOUT || s == MTK_ERR_BREAKDOWN) return s;
-                add_f32<<<grid(), kBlock, 0, st>>>(nRed, e32.p, x);
-                c->kernels++;
+                add_f32<<<grid(), kStream, 0, st>>>(nY, e32.p, x);
+                if (nZ > 0)
+                    add_z_projected<<<1, kStream, sizeof(double) * 2 * (size_t)nZ, st>>>(nY, nZ, kq, Qz.p, e32.p, x);
+                c->kernels += 2;
                 MTK_TRY(run_pcg<double>(op64(scale, shift), ZProj<double>{kq, Qz.p, Mz.p}, minvy.p, b, x, r64.p, z64.p,
                                         p64.p, q64.p, 0.0, 0, 1, smem64, nullptr, &rr));
                 refines++;
@@ -814,6 +900,7 @@ extern "C" int mtk_iterative_rounding(mtk_ctx* c, const mtk_igm_desc* d, const m
     // ---- W with tags, and its transpose split into y / J parts
     const int nW = 2 * nCut;
     const int nnzW = d->w_ptr[nW];
+    S.nnzW = nnzW;
     std::vector<int> tag(nnzW);
     for (int e = 0; e < nnzW; e++) {
         int i = d->w_idx[e];
@@ -825,6 +912,7 @@ extern "C" int mtk_iterative_rounding(mtk_ctx* c, const mtk_igm_desc* d, const m
     for (int j = 0; j < nY; j++) yptr[j + 1] += yptr[j];
     for (int s = 0; s < nJ; s++) jptr[s + 1] += jptr[s];
     std::vector<int> yrow(yptr[nY]), jrow(jptr[nJ]);
+    S.nnzYT = yptr[nY];
     std::vector<double> yval(yptr[nY]), jval(jptr[nJ]);
     {
         std::vector<int> fy(yptr.begin(), yptr.end() - 1), fj(jptr.begin(), jptr.end() - 1);
@@ -842,6 +930,7 @@ extern "C" int mtk_iterative_rounding(mtk_ctx* c, const mtk_igm_desc* d, const m
     if (maxdeg > kMaxFaceDeg) { mtk_set_last_error("vertex with more than 30 faces", __FILE__, __LINE__); return MTK_ERR_BAD_INPUT; }
     std::vector<int> sptr(nCut + 1, 0);
     for (int v = 0; v < nCut; v++) sptr[v + 1] = sptr[v] + vptr[v + 1] + 2;
+    S.nnzS = sptr[nCut];
     for (int v = 0; v < nCut; v++) vptr[v + 1] += vptr[v];
     std::vector<int> vface(vptr[nCut]);
     {
@@ -899,8 +988,8 @@ extern "C" int mtk_iterative_rounding(mtk_ctx* c, const mtk_igm_desc* d, const m
 
     const int G = S.grid();
     MTK_CUDA_TRY(cudaEventRecord(c->ev_a, st));
-    face_gradients<<<G, kBlock, 0, st>>>(nF, S.cutF.p, S.cutV.p, S.grad.p);
-    assemble_stiffness<<<G, kBlock, 0, st>>>(nCut, S.vf_ptr.p, S.vf_face.p, S.cutF.p, S.grad.p, S.s_ptr.p, S.s_col.p,
+    face_gradients<<<G, kStream, 0, st>>>(nF, S.cutF.p, S.cutV.p, S.grad.p);
+    assemble_stiffness<<<G, kStream, 0, st>>>(nCut, S.vf_ptr.p, S.vf_face.p, S.cutF.p, S.grad.p, S.s_ptr.p, S.s_col.p,
                                              S.s_val.p, S.s_val32.p, S.s_diag.p);
     c->kernels += 2;
     MTK_CUDA_TRY(cudaGetLastError());
@@ -984,9 +1073,11 @@ extern "C" int mtk_iterative_rounding(mtk_ctx* c, const mtk_igm_desc* d, const m
                 for (int k = 0; k < nZ; k++) s += t1[(size_t)i * nZ + k] * Pm[(size_t)k * nZ + j];
                 PK[(size_t)i * nZ + j] = s;
             }
+            // ridge on the constrained directions, scaled from the unprojected block (the
+            // projected block is pure round-off once the constraints pin every z direction)
             double dmax = 0;
-            for (int i = 0; i < nZ; i++) dmax = std::max(dmax, PK[(size_t)i * nZ + i]);
-            if (dmax <= 0) dmax = 1;
+            for (int i = 0; i < nZ; i++) dmax = std::max(dmax, Kzz[(size_t)i * nZ + i]);
+            if (!(dmax > 0)) dmax = 1;
             for (auto& qr : Qrows) for (int i = 0; i < nZ; i++) for (int j = 0; j < nZ; j++) PK[(size_t)i * nZ + j] += dmax * qr[i] * qr[j];
             std::vector<double> inv = PK;
             if (!spd_inverse(inv, nZ)) {   // fall back to the diagonal
@@ -1002,7 +1093,7 @@ extern "C" int mtk_iterative_rounding(mtk_ctx* c, const mtk_igm_desc* d, const m
             MTK_TRY(S.Mz.upload(&one, 1, st));
             MTK_TRY(S.Mz32.upload(&onef, 1, st));
         }
-        jacobi_y<<<G, kBlock, 0, st>>>(nY, S.yt_ptr.p, S.yt_row.p, S.yt_val.p, S.s_diag.p, scale, shift, S.minvy.p, S.minvy32.p);
+        jacobi_y<<<G, kStream, 0, st>>>(nY, S.yt_ptr.p, S.yt_row.p, S.yt_val.p, S.s_diag.p, scale, shift, S.minvy.p, S.minvy32.p);
         c->kernels++;
         MTK_TRY(S.fixy.upload(S.h_fixy.data(), S.h_fixy.size(), st));
         MTK_CUDA_TRY(cudaGetLastError());
@@ -1019,9 +1110,11 @@ extern "C" int mtk_iterative_rounding(mtk_ctx* c, const mtk_igm_desc* d, const m
         }
         int s = S.full2j[full];
         std::vector<double> row(S.USmall.begin() + (size_t)s * nZ, S.USmall.begin() + (size_t)(s + 1) * nZ);
+        // A row in the span of the earlier rows adds no constraint (its value is implied by
+        // them; the greedy order only fixes such a variable when it is already integral).
+        if (!add_orthonormal(Qrows, row)) return MTK_OK;
         Arows.push_back(row);
         Avals.push_back(val);
-        add_orthonormal(Qrows, row);
         // feasible correction of z: z += A^T (A A^T)^+ (g - A z), via the orthonormal basis:
         // solve in the row space with least squares (Q spans the rows of A).
         std::vector<double> z(nZ);
@@ -1088,7 +1181,7 @@ extern "C" int mtk_iterative_rounding(mtk_ctx* c, const mtk_igm_desc* d, const m
     double rel = 0;
     MTK_TRY(S.solve(length, 0.0, S.bsys.p, S.xs.p, o, stt, &rel));
     if (x_naive) {
-        expand_full<<<G, kBlock, 0, st>>>(nFull, S.d_full2y.p, S.d_full2j.p, nY, nZ, S.Us.p, S.xs.p, S.Xfull.p);
+        expand_full<<<G, kStream, 0, st>>>(nFull, S.d_full2y.p, S.d_full2j.p, nY, nZ, S.Us.p, S.xs.p, S.Xfull.p);
         c->kernels++;
         MTK_CUDA_TRY(cudaMemcpyAsync(x_naive, S.Xfull.p, sizeof(double) * nFull, cudaMemcpyDeviceToHost, st));
     }
@@ -1104,7 +1197,10 @@ extern "C" int mtk_iterative_rounding(mtk_ctx* c, const mtk_igm_desc* d, const m
     int status = MTK_OK;
     int nfix = 0;
     auto finish = [&](const double* xsrc) -> int {
-        expand_full<<<G, kBlock, 0, st>>>(nFull, S.d_full2y.p, S.d_full2j.p, nY, nZ, S.Us.p, xsrc, S.Xfull.p);
+        stt->igm_pcg_launches += S.pcg_launches;
+        stt->igm_pcg_ms += S.pcg_ms;
+        stt->igm_pcg_bytes += S.pcg_bytes;
+        expand_full<<<G, kStream, 0, st>>>(nFull, S.d_full2y.p, S.d_full2j.p, nY, nZ, S.Us.p, xsrc, S.Xfull.p);
         c->kernels++;
         MTK_CUDA_TRY(cudaMemcpyAsync(fullx, S.Xfull.p, sizeof(double) * nFull, cudaMemcpyDeviceToHost, st));
         MTK_CUDA_TRY(cudaStreamSynchronize(st));
@@ -1123,9 +1219,9 @@ extern "C" int mtk_iterative_rounding(mtk_ctx* c, const mtk_igm_desc* d, const m
     MTK_CUDA_TRY(cudaEventRecord(c->ev_a, st));
     {
         const double wI = 10e3, wC = 1.0;
-        xj_from_z<<<G, kBlock, 0, st>>>(nJ, nY, nZ, S.Us.p, S.xs.p, S.XJ64.p);
-        gather_U<<<G, kBlock, 0, st>>>(nCut, S.w_ptr.p, S.w_tag.p, S.w_val.p, S.xs.p, S.XJ64.p, S.U.p);
-        lm_field_target<<<G, kBlock, 0, st>>>(nF, S.cutF.p, S.grad.p, S.U.p, S.F2.p, length, wI * wI, wC * wC, S.Fsi.p);
+        xj_from_z<<<G, kStream, 0, st>>>(nJ, nY, nZ, S.Us.p, S.xs.p, S.XJ64.p);
+        gather_U<<<G, kStream, 0, st>>>(nCut, S.w_ptr.p, S.w_tag.p, S.w_val.p, S.xs.p, S.XJ64.p, S.U.p);
+        lm_field_target<<<G, kStream, 0, st>>>(nF, S.cutF.p, S.grad.p, S.U.p, S.F2.p, length, wI * wI, wC * wC, S.Fsi.p);
         c->kernels += 3;
         MTK_CUDA_TRY(cudaGetLastError());
         stt->lm_iterations += 2;
@@ -1149,14 +1245,15 @@ extern "C" int mtk_iterative_rounding(mtk_ctx* c, const mtk_igm_desc* d, const m
     while (!leftv.empty()) {
         // ---- initFixedIndices: argmin |X - round X| over leftIdcs (FP64 on the device)
         MTK_CUDA_TRY(cudaMemcpyAsync(S.left.p, leftv.data(), sizeof(int) * leftv.size(), cudaMemcpyHostToDevice, st));
-        round_argmin<<<1, kBlock, 0, st>>>((int)leftv.size(), S.left.p, S.d_full2y.p, S.d_full2j.p, nY, nZ, S.Us.p, S.xs.p,
+        round_argmin<<<1, kStream, 0, st>>>((int)leftv.size(), S.left.p, S.d_full2y.p, S.d_full2j.p, nY, nZ, S.Us.p, S.xs.p,
                                            c->scalars);
         c->kernels++;
         MTK_CUDA_TRY(cudaMemcpyAsync(h_arg.data(), c->scalars, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
         MTK_CUDA_TRY(cudaStreamSynchronize(st));
         const int k = (int)h_arg[0];
         const double mind = h_arg[1];
-        if (leftv.size() > 1) min_margin = std::min(min_margin, h_arg[3] - mind);
+        if (Igm::debug()) fprintf(stderr, "[round] left=%zu pick=%d full=%d X=%.9f d=%.3e second=%.3e\n", leftv.size(), k, leftv[k], h_arg[2], mind, h_arg[3]);
+        if (h_arg[3] < 1e299) min_margin = std::min(min_margin, h_arg[3] - mind);
         const int idx = leftv[k];
         const int ival = (int)std::round(h_arg[2]);
         if (fix_order && nfix < nLeftCap) { fix_order[nfix] = idx; if (fix_vals) fix_vals[nfix] = ival; }

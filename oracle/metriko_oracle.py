@@ -36,8 +36,10 @@ Deliberate, documented choices (identical in the product path):
     is the same;
   * the constraint kernel basis restates Eigen's FullPivLU::kernel (complete pivoting, first
     maximum in column-major order, identity on the free columns);
-  * near-integer ties in the greedy rounding order (|x - round(x)| < 1e-9, decided by
-    round-off in the reference) are resolved by position.
+  * greedy rounding (iter_rounding_loop.h:34-38) picks the first position among candidates
+    whose distance to an integer is within 1e-6 of the minimum (distances <= 1e-6 count as 0,
+    the reference's own integrality threshold): the reference's strict '<' there is decided
+    by round-off (structural ties between constraint-linked variables, already-integral values).
 Closed, consistently oriented, edge-manifold triangle meshes only.
 
 Parity status: the reference cannot be compiled here (Eigen, libigl, SuiteSparse absent) and
@@ -991,11 +993,17 @@ class SeamlessIntegration:
         X = self.UFull @ self.xCurr
         vals = X[self.leftIdcs]
         d = np.abs(vals - cround(vals))
-        d = np.where(d < 1e-9, 0.0, d)            # near-integer ties resolved by position
-        k = int(np.argmin(d))                     # first minimum (strict < in the reference)
+        d = np.where(d <= 10e-7, 0.0, d)          # integral values (order = round-off): by position
+        # argmin with ties within 1e-6 resolved by position (the reference's strict '<' keeps
+        # the first minimum; values this close differ only by round-off, e.g. two variables
+        # tied by a constraint)
+        dmin = d.min()
+        tied = d <= dmin + 10e-7
+        k = int(np.flatnonzero(tied)[0])
         mind = d[k]
-        if len(d) > 1:
-            self.order_margin.append(float(np.partition(d, 1)[1] - mind))
+        rest = d[~tied]
+        if len(rest):
+            self.order_margin.append(float(rest.min() - dmin))
         idx = self.leftIdcs[k]
         self.fixedIdcs.append(idx)
         self.fixedVals.append(int(cround(X[idx])))

@@ -1,0 +1,77 @@
+"""Whole path on the GPU (mtk_pipeline_run through the C ABI) against the oracle and the golden
+fixtures: singularities, seams, combed matching, the greedy fixing order and the rounded values
+are integer outputs and must be identical; uv (fullx) within 1e-6 of the uv bounding-box
+diagonal; FP64 and mixed precision both."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import metriko_gb300 as M
+from metriko_gb300 import meshgen
+from oracle import metriko_oracle as O
+
+from conftest import oracle_run
+
+pytestmark = pytest.mark.gpu
+GOLDEN = Path(__file__).parent / "golden"
+TOL = 1e-10
+
+
+def _uv_diag(x):
+    return max(np.ptp(x), 1.0) * np.sqrt(2.0)
+
+
+@pytest.mark.parametrize("name", ["ico2_noise", "ico3_noise", "torus_32x16"])
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+def test_pipeline_matches_golden(gpu_ctx, name, prec):
+    g = np.load(GOLDEN / f"{name}.npz")
+    r = M.pipeline(gpu_ctx, g["V"], g["F"], ratio=float(g["ratio"]), round_seams=bool(g["round_seams"]),
+                   opts=M.solve_opts(prec, tol=TOL))
+    assert r["status"] == 0
+    assert np.array_equal(r["singular"], g["singular"])
+    assert np.array_equal(r["seam"], np.unpackbits(g["seam"])[: int(g["n_edges"])].astype(bool))
+    assert np.array_equal(r["matching"], g["combed_matching"])
+    assert list(r["fix_order"]) == list(g["fix_order"])
+    assert list(r["fix_vals"]) == list(g["fix_vals"])
+    assert np.abs(r["fullx"] - g["fullx"]).max() <= 1e-6 * _uv_diag(g["fullx"])
+    assert np.abs(r["x_naive"] - g["x_naive"]).max() <= 1e-6 * _uv_diag(g["x_naive"])
+    assert np.abs(np.angle(r["compressed"] / g["compressed"])).max() / 4 < 1e-5
+
+
+@pytest.mark.parametrize("name", ["ico4_noise", "torus_64x32"])
+def test_pipeline_matches_oracle(gpu_ctx, name):
+    V, F, ratio, rs, ref = oracle_run(name)
+    r = M.pipeline(gpu_ctx, V, F, ratio=ratio, round_seams=rs, opts=M.solve_opts("mixed", tol=TOL))
+    assert r["status"] == 0
+    assert np.array_equal(r["singular"], ref["singular"])
+    assert np.array_equal(r["seam"], ref["seam"])
+    assert list(r["fix_order"]) == list(ref["info"]["fix_order"])
+    assert list(r["fix_vals"]) == list(ref["info"]["fix_vals"])
+    assert np.abs(r["fullx"] - ref["fullx"]).max() <= 1e-6 * _uv_diag(ref["fullx"])
+    cfn = r["cfn"]
+    assert np.abs(cfn - ref["cfn"]).max() <= 1e-6 * _uv_diag(ref["fullx"])
+
+
+def test_pipeline_deterministic(gpu_ctx):
+    V, F, ratio, rs = meshgen.workload("ico4_noise")
+    a = M.pipeline(gpu_ctx, V, F, ratio=ratio)
+    b = M.pipeline(gpu_ctx, V, F, ratio=ratio)
+    assert np.array_equal(a["fullx"], b["fullx"])
+    assert list(a["fix_order"]) == list(b["fix_order"])
+
+
+@pytest.mark.parametrize("name", ["ico6_sh8"])
+def test_pipeline_size_independent_properties(gpu_ctx, name):
+    """At sizes beyond the oracle: sum of indices = 8 on a sphere, every rounded value within
+    1e-6 of an integer and equal to the reported value, all solves at the requested residual."""
+    V, F, ratio, rs = meshgen.workload(name)
+    r = M.pipeline(gpu_ctx, V, F, ratio=ratio, round_seams=rs, opts=M.solve_opts("mixed", tol=1e-8))
+    assert r["status"] == 0
+    assert r["singular"].sum() == 8
+    X = r["fullx"]
+    fo = r["fix_order"]
+    assert len(fo) == 2 * (r["counts"]["nS"] + r["counts"]["nT"])
+    assert np.abs(X[fo] - np.round(X[fo])).max() <= 1e-6
+    assert np.array_equal(np.round(X[fo]).astype(int), r["fix_vals"])
+    assert r["stats"]["max_rel_residual"] <= 1e-8 * 1.0001
