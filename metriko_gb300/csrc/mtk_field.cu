@@ -14,6 +14,7 @@
 //   v64[j*n + f]  double2 off-diagonal value L(f, nbr)       v32: float2 copy
 //   d64[f], d32[f]        diagonal (#neighbours + 1e-9)     inv32/inv64: Jacobi inverse
 // Algorithmic bytes per SpMV row: FP32 3*(8+4) + 4 + 2*8 = 56 B, FP64 3*(16+4) + 8 + 2*16 = 100 B.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -222,18 +223,51 @@ __global__ void finalize_partials(const double* partials, int nb, int K, double*
     }
 }
 
-// K2: x = g u, r = b - g Lu (exact algebra of the Galerkin start), partial |r|^2, r32 = r
-// g = scal[1] / scal[0] read on the device (no host round trip).
-__global__ void power_start(int n, const double* __restrict__ scal, const double2* __restrict__ u,
-                            const double2* __restrict__ b, const double2* __restrict__ Lu, double2* x, double2* r,
-                            float2* r32, double* partials) {
-    const double g = scal[0] > 0 ? scal[1] / scal[0] : 0.0;
+// Subspace warm start.  The inverse iterates on a sphere stay inside a nearly degenerate
+// cluster of eigenvectors, so the previous m iterates span the solution well: the start of
+// each solve is the Galerkin solution of L x = b on V = [u_k, ..., u_{k-m+1}] (L V is kept
+// from power_prepare, so no extra operator applications).
+constexpr int kRing = 12;
+
+// partials for j < cnt: [Re, Im] of u^H (L V_j) and of V_j^H b
+struct RingPtrs { const double2* V[kRing]; const double2* LV[kRing]; int cnt; };
+
+__global__ void gram_row(int n, RingPtrs R, const double2* __restrict__ u, const double2* __restrict__ b,
+                         double* partials) {
+    for (int j = 0; j < R.cnt; j++) {
+        double red[4] = {0, 0, 0, 0};
+        const double2* Vj = R.V[j];
+        const double2* Lj = R.LV[j];
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+            double2 ui = u[i], li = Lj[i], vi = Vj[i], bi = b[i];
+            red[0] += ui.x * li.x + ui.y * li.y;   // conj(u) * Lv
+            red[1] += ui.x * li.y - ui.y * li.x;
+            red[2] += vi.x * bi.x + vi.y * bi.y;   // conj(v) * b
+            red[3] += vi.x * bi.y - vi.y * bi.x;
+        }
+        double* pj = partials + 4 * j * gridDim.x;
+        publish_partials<double, 4>(red, pj);
+    }
+}
+
+struct StartCoef { double re[kRing], im[kRing]; const double2* V[kRing]; const double2* LV[kRing]; int cnt; };
+
+// x = V y, r = b - (L V) y, r32 = r, partial |r|^2
+__global__ void combine_start(int n, StartCoef c, const double2* __restrict__ b, double2* x, double2* r, float2* r32,
+                              double* partials) {
     double red[1] = {0};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        double2 ui = u[i], bi = b[i], li = Lu[i];
-        double2 xi = make_double2(g * ui.x, g * ui.y);
-        double2 ri = make_double2(bi.x - g * li.x, bi.y - g * li.y);
-        x[i] = xi;
+        double xr = 0, xi = 0, lr = 0, li = 0;
+        for (int j = 0; j < c.cnt; j++) {
+            double2 v = c.V[j][i], l = c.LV[j][i];
+            xr += c.re[j] * v.x - c.im[j] * v.y;
+            xi += c.re[j] * v.y + c.im[j] * v.x;
+            lr += c.re[j] * l.x - c.im[j] * l.y;
+            li += c.re[j] * l.y + c.im[j] * l.x;
+        }
+        double2 bi = b[i];
+        double2 ri = make_double2(bi.x - lr, bi.y - li);
+        x[i] = make_double2(xr, xi);
         r[i] = ri;
         if (r32) r32[i] = make_float2((float)ri.x, (float)ri.y);
         red[0] += ri.x * ri.x + ri.y * ri.y;
@@ -295,6 +329,67 @@ using namespace mtk;
 
 namespace {
 
+// y = G^+ h for a small Hermitian G (cnt x cnt), through the real symmetric embedding
+// [[Re G, -Im G], [Im G, Re G]] and cyclic Jacobi rotations; eigenvalues below
+// 1e-12 * max are dropped (the warm-start basis becomes nearly dependent as the iterates settle).
+void hermitian_pinv_solve(const std::vector<double>& Gr, const std::vector<double>& Gi, const std::vector<double>& hr,
+                          const std::vector<double>& hi, int cnt, std::vector<double>& yr, std::vector<double>& yi) {
+    const int m = 2 * cnt;
+    std::vector<double> A((size_t)m * m), Vm((size_t)m * m, 0.0), rhs(m);
+    for (int i = 0; i < cnt; i++)
+        for (int j = 0; j < cnt; j++) {
+            double a = Gr[i * kRing + j], b = Gi[i * kRing + j];
+            A[(size_t)i * m + j] = a;
+            A[(size_t)(i + cnt) * m + (j + cnt)] = a;
+            A[(size_t)i * m + (j + cnt)] = -b;
+            A[(size_t)(i + cnt) * m + j] = b;
+        }
+    for (int i = 0; i < cnt; i++) { rhs[i] = hr[i]; rhs[i + cnt] = hi[i]; }
+    for (int i = 0; i < m; i++) Vm[(size_t)i * m + i] = 1.0;
+    for (int sweep = 0; sweep < 60; sweep++) {
+        double off = 0;
+        for (int p = 0; p < m; p++) for (int q = p + 1; q < m; q++) off += A[(size_t)p * m + q] * A[(size_t)p * m + q];
+        if (off < 1e-30) break;
+        for (int p = 0; p < m; p++)
+            for (int q = p + 1; q < m; q++) {
+                double apq = A[(size_t)p * m + q];
+                if (std::fabs(apq) < 1e-300) continue;
+                double app = A[(size_t)p * m + p], aqq = A[(size_t)q * m + q];
+                double theta = (aqq - app) / (2 * apq);
+                double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1));
+                double c = 1 / std::sqrt(t * t + 1), sn = t * c;
+                for (int k = 0; k < m; k++) {
+                    double akp = A[(size_t)k * m + p], akq = A[(size_t)k * m + q];
+                    A[(size_t)k * m + p] = c * akp - sn * akq;
+                    A[(size_t)k * m + q] = sn * akp + c * akq;
+                }
+                for (int k = 0; k < m; k++) {
+                    double apk = A[(size_t)p * m + k], aqk = A[(size_t)q * m + k];
+                    A[(size_t)p * m + k] = c * apk - sn * aqk;
+                    A[(size_t)q * m + k] = sn * apk + c * aqk;
+                }
+                for (int k = 0; k < m; k++) {
+                    double vkp = Vm[(size_t)k * m + p], vkq = Vm[(size_t)k * m + q];
+                    Vm[(size_t)k * m + p] = c * vkp - sn * vkq;
+                    Vm[(size_t)k * m + q] = sn * vkp + c * vkq;
+                }
+            }
+    }
+    double lmax = 0;
+    for (int k = 0; k < m; k++) lmax = std::max(lmax, std::fabs(A[(size_t)k * m + k]));
+    std::vector<double> y(m, 0.0);
+    for (int k = 0; k < m; k++) {
+        double lam = A[(size_t)k * m + k];
+        if (!(lam > 1e-12 * lmax)) continue;
+        double d = 0;
+        for (int i = 0; i < m; i++) d += Vm[(size_t)i * m + k] * rhs[i];
+        d /= lam;
+        for (int i = 0; i < m; i++) y[i] += d * Vm[(size_t)i * m + k];
+    }
+    yr.assign(y.begin(), y.begin() + cnt);
+    yi.assign(y.begin() + cnt, y.end());
+}
+
 struct FieldSolver {
     mtk_ctx* c;
     int n;
@@ -302,6 +397,7 @@ struct FieldSolver {
     DBuf<double> theta, area, d64, inv64;
     DBuf<float> d32, inv32, area32;
     DBuf<double2> v64, u, b, Lu, x, r, z64, p64, q64;
+    DBuf<double2> ringU[kRing], ringL[kRing];
     DBuf<float2> v32, r32, e32, z32, p32, q32;
     int grid = 0;
     double pcg_ms = 0, pcg_bytes = 0;
@@ -372,7 +468,9 @@ extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const 
     MTK_TRY(S.nbr_in.upload(nbr_h, 3 * (size_t)n, st));
     MTK_TRY(S.theta.upload(theta_h, 3 * (size_t)n, st));
     MTK_TRY(S.area.upload(area_h, n, st));
-    MTK_TRY(S.u.upload(reinterpret_cast<const double2*>(x0), n, st));
+    const int ring = std::min(kRing, std::max(n_iter, 1));
+    for (int j = 0; j < ring; j++) { MTK_TRY(S.ringU[j].alloc(n)); MTK_TRY(S.ringL[j].alloc(n)); }
+    MTK_CUDA_TRY(cudaMemcpyAsync(S.ringU[0].p, x0, sizeof(double2) * n, cudaMemcpyHostToDevice, st));
     MTK_TRY(S.nbr.alloc(3 * (size_t)n));
     MTK_TRY(S.v64.alloc(3 * (size_t)n));
     MTK_TRY(S.v32.alloc(3 * (size_t)n));
@@ -393,16 +491,56 @@ extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const 
 
     long long iters = 0, solves = 0, refines = 0;
     double worst = 0.0;
+    std::vector<double> Gr(kRing * kRing, 0.0), Gi(kRing * kRing, 0.0);
     const double tol = opts.tol;
     for (int k = 0; k < n_iter; k++) {
-        // b = M u, Galerkin start x = u (u^H M u)/(u^H L u), r = b - L x
-        power_prepare<<<G, kStream, 0, st>>>(S.A64(), S.area.p, S.u.p, S.b.p, S.Lu.p, c->partials);
+        // b = M u_k, L u_k kept in the ring; Galerkin start on the last `ring` iterates
+        const int slot = k % ring;
+        const int cnt = std::min(k + 1, ring);
+        double2* uk = S.ringU[slot].p;
+        power_prepare<<<G, kStream, 0, st>>>(S.A64(), S.area.p, uk, S.b.p, S.ringL[slot].p, c->partials);
         c->kernels++;
         MTK_TRY(S.finalize(G, 3));
-        power_start<<<G, kStream, 0, st>>>(n, c->scalars, S.u.p, S.b.p, S.Lu.p, S.x.p, S.r.p, mixed ? S.r32.p : nullptr,
-                                          c->partials);
-        c->kernels++;
         MTK_CUDA_TRY(cudaMemcpyAsync(c->h_scalars, c->scalars, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        RingPtrs R{};
+        std::vector<int> slots(cnt);
+        for (int j = 0; j < cnt; j++) {
+            int sj = (slot - j + ring) % ring;
+            slots[j] = sj;
+            R.V[j] = S.ringU[sj].p;
+            R.LV[j] = S.ringL[sj].p;
+        }
+        R.cnt = cnt;
+        gram_row<<<G, kStream, 0, st>>>(n, R, uk, S.b.p, c->partials);
+        c->kernels++;
+        MTK_TRY(S.finalize(G, 4 * cnt));
+        MTK_CUDA_TRY(cudaMemcpyAsync(c->h_scalars + 8, c->scalars, 4 * cnt * sizeof(double), cudaMemcpyDeviceToHost, st));
+        MTK_CUDA_TRY(cudaStreamSynchronize(st));
+        // row / column of the new iterate; older entries stay valid (their vectors are unchanged)
+        for (int j = 0; j < cnt; j++) {
+            int sj = slots[j];
+            double gr = c->h_scalars[8 + 4 * j], gi = c->h_scalars[8 + 4 * j + 1];
+            Gr[slot * kRing + sj] = gr;
+            Gi[slot * kRing + sj] = gi;
+            Gr[sj * kRing + slot] = gr;
+            Gi[sj * kRing + slot] = -gi;
+            if (sj == slot) Gi[slot * kRing + slot] = 0.0;
+        }
+        std::vector<double> gr_sub(kRing * kRing), gi_sub(kRing * kRing), hr(cnt), hi(cnt), yr, yi;
+        for (int a = 0; a < cnt; a++) {
+            for (int b2 = 0; b2 < cnt; b2++) {
+                gr_sub[a * kRing + b2] = Gr[slots[a] * kRing + slots[b2]];
+                gi_sub[a * kRing + b2] = Gi[slots[a] * kRing + slots[b2]];
+            }
+            hr[a] = c->h_scalars[8 + 4 * a + 2];
+            hi[a] = c->h_scalars[8 + 4 * a + 3];
+        }
+        hermitian_pinv_solve(gr_sub, gi_sub, hr, hi, cnt, yr, yi);
+        StartCoef sc{};
+        for (int j = 0; j < cnt; j++) { sc.re[j] = yr[j]; sc.im[j] = yi[j]; sc.V[j] = R.V[j]; sc.LV[j] = R.LV[j]; }
+        sc.cnt = cnt;
+        combine_start<<<G, kStream, 0, st>>>(n, sc, S.b.p, S.x.p, S.r.p, mixed ? S.r32.p : nullptr, c->partials);
+        c->kernels++;
         MTK_TRY(S.finalize(G, 1));
         MTK_CUDA_TRY(cudaMemcpyAsync(c->h_scalars + 3, c->scalars, sizeof(double), cudaMemcpyDeviceToHost, st));
         MTK_CUDA_TRY(cudaStreamSynchronize(st));
@@ -453,11 +591,11 @@ extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const 
         mnorm_partial<<<G, kStream, 0, st>>>(n, S.area.p, S.x.p, c->partials);
         c->kernels++;
         MTK_TRY(S.finalize(G, 1));
-        normalize_to<<<G, kStream, 0, st>>>(n, c->scalars, S.x.p, S.u.p);
+        normalize_to<<<G, kStream, 0, st>>>(n, c->scalars, S.x.p, S.ringU[(k + 1) % ring].p);
         c->kernels++;
         MTK_CUDA_TRY(cudaGetLastError());
     }
-    MTK_CUDA_TRY(cudaMemcpyAsync(out, S.u.p, sizeof(double2) * n, cudaMemcpyDeviceToHost, st));
+    MTK_CUDA_TRY(cudaMemcpyAsync(out, S.ringU[n_iter % ring].p, sizeof(double2) * n, cudaMemcpyDeviceToHost, st));
     MTK_CUDA_TRY(cudaEventRecord(c->ev_b, st));
     MTK_CUDA_TRY(cudaStreamSynchronize(st));
     float ms = 0;

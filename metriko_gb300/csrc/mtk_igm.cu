@@ -167,10 +167,19 @@ __device__ bool igm_apply(const IgmOp<T>& A, const ZProj<T>& P, const unsigned c
         qy[j] = qv;
         part += pj * qv;
     }
-    for (int s = t0; s < A.nJ; s += stride) {
-        T acc = T(0);
-        for (int e = A.jt_ptr[s]; e < A.jt_ptr[s + 1]; e++) acc += A.jt_val[e] * __ldcg(A.Qc + A.jt_row[e]);
-        A.XoJ[s] = T(2) * acc;
+    // constrained variables: seam translations are referenced by every cut copy along their
+    // seam segment (long lists), so one warp reduces each list (fixed lane order)
+    {
+        const int lane = threadIdx.x & 31;
+        const int nwarps = stride >> 5;
+        const int gw = nwarps - 1 - (t0 >> 5);   // last warps of the grid
+        for (int s = gw; s < A.nJ; s += nwarps) {
+            T acc = T(0);
+            for (int e = A.jt_ptr[s] + lane; e < A.jt_ptr[s + 1]; e += 32) acc += A.jt_val[e] * __ldcg(A.Qc + A.jt_row[e]);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) A.XoJ[s] = T(2) * acc;
+        }
     }
     pq_part = part;
     return true;
@@ -431,10 +440,15 @@ __global__ void rhs_reduce(int nY, int nJ, const int* __restrict__ yt_ptr, const
         for (int e = yt_ptr[j]; e < yt_ptr[j + 1]; e++) acc += yt_val[e] * hb[yt_row[e]];
         b[j] = fixy && fixy[j] ? 0.0 : scale * acc + (prev ? shift * prev[j] : 0.0);
     }
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nJ; s += gridDim.x * blockDim.x) {
-        double acc = 0;
-        for (int e = jt_ptr[s]; e < jt_ptr[s + 1]; e++) acc += jt_val[e] * hb[jt_row[e]];
-        XbJ[s] = acc;
+    {   // one warp per constrained variable (long seam lists)
+        const int lane = threadIdx.x & 31;
+        const int nwarps = (gridDim.x * blockDim.x) >> 5;
+        for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nJ; s += nwarps) {
+            double acc = 0;
+            for (int e = jt_ptr[s] + lane; e < jt_ptr[s + 1]; e += 32) acc += jt_val[e] * hb[jt_row[e]];
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) XbJ[s] = acc;
+        }
     }
 }
 
