@@ -196,6 +196,23 @@ int mtk_topology_from_field(int32_t nV, int32_t nF, const double* V, const int32
                             int32_t* singular, int32_t* matching, uint8_t* seam, int32_t* cutF,
                             int32_t* counts, double* length);
 
+/*
+ * Allocation-free variant of mtk_field_smoothest (FP64 path) for callers that cannot call
+ * cudaMalloc -- code inside a host framework that owns all device memory through its own
+ * allocator, or code that must not allocate after start-up.  No counterpart in the reference
+ * (which has no GPU code); it allocates nothing and needs no mtk_ctx.
+ *   All pointers are DEVICE pointers owned by the caller: nbr[3*nF], theta[3*nF], area[nF],
+ *   x0[2*nF] (re, im), out[2*nF].  stream: a cudaStream_t (NULL = default stream).
+ *   Working memory is a 64 MiB static device array inside the library (held by every GPU that
+ *   loads the library until exit), which limits nF to 409600; larger nF -> MTK_ERR_BAD_INPUT.
+ *   The first call on a device looks the array up (cudaGetSymbolAddress): make that first
+ *   call before any stream capture.  All calls share the array: calls that overlap on the GPU
+ *   race.  *iterations (may be NULL) receives the total PCG iterations.  Returns when done.
+ */
+int mtk_field_smoothest_noalloc(int32_t nF, int32_t nRosy, const int32_t* nbr, const double* theta,
+                                const double* area, const double* x0, int32_t n_iter, double tol,
+                                int32_t max_iter, double* out, void* stream, int32_t* iterations);
+
 /* The deterministic start vector used by the pipeline: re/im of face f from splitmix64. */
 void mtk_seeded_init(int32_t n, int32_t seed, double* out);
 

@@ -20,7 +20,7 @@ PREC_FP64, PREC_MIXED = 0, 1
 EXPORTS = [
     "mtk_status_string", "mtk_last_error", "mtk_default_opts", "mtk_ctx_create", "mtk_ctx_destroy",
     "mtk_ctx_kernel_count", "mtk_field_smoothest", "mtk_iterative_rounding", "mtk_pipeline_run",
-    "mtk_seeded_init", "mtk_topology_from_field",
+    "mtk_seeded_init", "mtk_topology_from_field", "mtk_field_smoothest_noalloc",
 ]
 
 
@@ -82,6 +82,9 @@ def lib():
         L.mtk_topology_from_field.argtypes = [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
                                               C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                               C.c_void_p, C.c_void_p]
+        L.mtk_field_smoothest_noalloc.argtypes = [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                  C.c_void_p, C.c_int32, C.c_double, C.c_int32, C.c_void_p,
+                                                  C.c_void_p, C.POINTER(C.c_int32)]
         _lib = L
     return _lib
 
