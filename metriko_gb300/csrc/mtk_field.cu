@@ -16,8 +16,10 @@
 // Algorithmic bytes per SpMV row: FP32 3*(8+4) + 4 + 2*8 = 56 B, FP64 3*(16+4) + 8 + 2*16 = 100 B.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
+#include "mtk_amg.cuh"
 #include "mtk_ctx.cuh"
 
 namespace mtk {
@@ -84,7 +86,7 @@ __global__ void field_assemble(int n, int N, const int* __restrict__ nbr_in, con
 // barriers per iteration; all scalars are reduced in a fixed order, so the iterates are
 // bit-reproducible for a given grid size.  status: 0 converged, 3 cap, 4 breakdown, 5 timeout.
 template <typename T>
-__global__ void __launch_bounds__(kBlock) pcg_complex(ComplexEll<T> A, const T* __restrict__ minv,
+__global__ void __launch_bounds__(kBlock, 1) pcg_complex(ComplexEll<T> A, const T* __restrict__ minv,
                                                      const typename V2of<T>::type* __restrict__ b,
                                                      typename V2of<T>::type* x, typename V2of<T>::type* r,
                                                      typename V2of<T>::type* z, typename V2of<T>::type* p,
@@ -184,6 +186,202 @@ done:
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         out[0] = status;
         out[1] = it;
+    }
+}
+
+// ---------------------------------------------------------------------------- multigrid PCG
+// One CSR phase over all rows: out[row] = M x (+ M2 x2), rows spread thread-per-row (group 1)
+// or warp-per-row (group 32, fixed-order warp reduction) across the whole grid.
+template <typename T>
+__device__ __forceinline__ void csr_row_acc(const DevCsr<T>& M, int row, int lane, int g,
+                                            const typename V2of<T>::type* __restrict__ x, T& re, T& im) {
+    for (int p = M.ptr[row] + lane; p < M.ptr[row + 1]; p += g) {
+        const typename V2of<T>::type v = M.val[p], xv = __ldcg(x + M.col[p]);
+        re += v.x * xv.x - v.y * xv.y;
+        im += v.x * xv.y + v.y * xv.x;
+    }
+}
+
+template <typename T>
+__device__ void csr_phase(const DevCsr<T>& M, const typename V2of<T>::type* x, const DevCsr<T>* M2,
+                          const typename V2of<T>::type* x2, typename V2of<T>::type* out) {
+    using V2 = typename V2of<T>::type;
+    const int stride = gridDim.x * blockDim.x;
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (M.group == 1) {
+        for (int row = t0; row < M.n; row += stride) {
+            T re = T(0), im = T(0);
+            csr_row_acc(M, row, 0, 1, x, re, im);
+            if (M2) csr_row_acc(*M2, row, 0, 1, x2, re, im);
+            V2 o;
+            o.x = re;
+            o.y = im;
+            out[row] = o;
+        }
+    } else {
+        const int lane = threadIdx.x & 31;
+        for (int row = t0 >> 5; row < M.n; row += stride >> 5) {
+            T re = T(0), im = T(0);
+            csr_row_acc(M, row, lane, 32, x, re, im);
+            if (M2) csr_row_acc(*M2, row, lane, 32, x2, re, im);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                re += __shfl_xor_sync(0xffffffffu, re, o);
+                im += __shfl_xor_sync(0xffffffffu, im, o);
+            }
+            if (lane == 0) {
+                V2 v;
+                v.x = re;
+                v.y = im;
+                out[row] = v;
+            }
+        }
+    }
+}
+
+// V(1,1) cycle z = B r: down r_{l+1} = R r_l; coarse y = A_c^-1 r_c (dense, warp per row);
+// up y_l = S r_l + P y_{l+1}.  2 * nlev grid barriers.
+template <typename T>
+__device__ bool vcycle(const ComplexEll<T>& A0, const DevHierarchy<T>& H, const GridBarrier& bar) {
+    using V2 = typename V2of<T>::type;
+    (void)A0;
+    const int stride = gridDim.x * blockDim.x;
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int l = 0; l < H.nlev; l++) {
+        V2* rnext = (l + 1 < H.nlev) ? H.L[l + 1].r : H.rc;
+        csr_phase<T>(H.L[l].R, H.L[l].r, nullptr, nullptr, rnext);
+        if (!grid_sync(bar)) return false;
+    }
+    {
+        const int lane = threadIdx.x & 31;
+        for (int a = t0 >> 5; a < H.nc; a += stride >> 5) {
+            T re = T(0), im = T(0);
+            const V2* row = H.Ainv + (size_t)a * H.nc;
+            for (int b = lane; b < H.nc; b += 32) {
+                const V2 m = row[b], rb = __ldcg(H.rc + b);
+                re += m.x * rb.x - m.y * rb.y;
+                im += m.x * rb.y + m.y * rb.x;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                re += __shfl_xor_sync(0xffffffffu, re, o);
+                im += __shfl_xor_sync(0xffffffffu, im, o);
+            }
+            if (lane == 0) {
+                V2 v;
+                v.x = re;
+                v.y = im;
+                H.yc[a] = v;
+            }
+        }
+    }
+    if (!grid_sync(bar)) return false;
+    for (int l = H.nlev - 1; l >= 0; l--) {
+        const V2* yn = (l + 1 < H.nlev) ? H.L[l + 1].y : H.yc;
+        csr_phase<T>(H.L[l].S, H.L[l].r, &H.L[l].P, yn, H.L[l].y);
+        if (l > 0 && !grid_sync(bar)) return false;
+    }
+    return true;
+}
+
+// PCG with the V-cycle preconditioner (same structure and status codes as pcg_complex).
+template <typename T>
+__global__ void __launch_bounds__(kBlock, 1) pcg_complex_mg(ComplexEll<T> A, const DevHierarchy<T>* __restrict__ Hp,
+                                                        const typename V2of<T>::type* __restrict__ b,
+                                                        typename V2of<T>::type* x, typename V2of<T>::type* r,
+                                                        typename V2of<T>::type* z, typename V2of<T>::type* p,
+                                                        typename V2of<T>::type* q, T* partials, GridBarrier bar,
+                                                        double tol2, int maxit, int* out) {
+    using V2 = typename V2of<T>::type;
+    const DevHierarchy<T>& H = *Hp;
+    const int n = A.n;
+    const int stride = gridDim.x * blockDim.x;
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    T red2[2];
+    T red1[1];
+    int status = 3, it = 0;
+    T rr = T(0);
+    for (int i = t0; i < n; i += stride) {
+        V2 ax = A.row(i, x);
+        V2 bi = b[i];
+        V2 ri;
+        ri.x = bi.x - ax.x;
+        ri.y = bi.y - ax.y;
+        r[i] = ri;
+    }
+    if (!grid_sync(bar)) { status = 5; goto done; }
+    if (!vcycle(A, H, bar)) { status = 5; goto done; }
+    red2[0] = T(0);
+    red2[1] = T(0);
+    for (int i = t0; i < n; i += stride) {
+        V2 ri = r[i], zi = z[i];
+        p[i] = zi;
+        red2[0] += ri.x * zi.x + ri.y * zi.y;
+        red2[1] += ri.x * ri.x + ri.y * ri.y;
+    }
+    publish_partials<T, 2>(red2, partials);
+    if (!grid_sync(bar)) { status = 5; goto done; }
+    gather_partials<T, 2>(partials, red2);
+    {
+        T rz = red2[0];
+        rr = red2[1];
+        for (;;) {
+            if ((double)rr <= tol2) { status = 0; break; }
+            if (it >= maxit) { status = 3; break; }
+            red1[0] = T(0);
+            for (int i = t0; i < n; i += stride) {
+                V2 qi = A.row(i, p);
+                q[i] = qi;
+                V2 pi = p[i];
+                red1[0] += pi.x * qi.x + pi.y * qi.y;
+            }
+            publish_partials<T, 1>(red1, partials + 2 * gridDim.x);
+            if (!grid_sync(bar)) { status = 5; break; }
+            gather_partials<T, 1>(partials + 2 * gridDim.x, red1);
+            T pq = red1[0];
+            if (!(pq > T(0))) { status = 4; break; }
+            T alpha = rz / pq;
+            for (int i = t0; i < n; i += stride) {
+                V2 pi = p[i], qi = q[i], xi = x[i], ri = r[i];
+                xi.x += alpha * pi.x;
+                xi.y += alpha * pi.y;
+                ri.x -= alpha * qi.x;
+                ri.y -= alpha * qi.y;
+                x[i] = xi;
+                r[i] = ri;
+            }
+            if (!grid_sync(bar)) { status = 5; break; }
+            if (!vcycle(A, H, bar)) { status = 5; break; }
+            red2[0] = T(0);
+            red2[1] = T(0);
+            for (int i = t0; i < n; i += stride) {
+                V2 ri = r[i], zi = z[i];
+                red2[0] += ri.x * zi.x + ri.y * zi.y;
+                red2[1] += ri.x * ri.x + ri.y * ri.y;
+            }
+            publish_partials<T, 2>(red2, partials + 3 * gridDim.x);
+            if (!grid_sync(bar)) { status = 5; break; }
+            gather_partials<T, 2>(partials + 3 * gridDim.x, red2);
+            T rz_new = red2[0];
+            rr = red2[1];
+            if (rr != rr || !(rz_new > T(0))) { status = 4; break; }
+            T beta = rz_new / rz;
+            rz = rz_new;
+            for (int i = t0; i < n; i += stride) {
+                V2 zi = z[i], pi = p[i];
+                pi.x = zi.x + beta * pi.x;
+                pi.y = zi.y + beta * pi.y;
+                p[i] = pi;
+            }
+            it++;
+            if (!grid_sync(bar)) { status = 5; break; }
+        }
+    }
+done:
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        out[0] = status;
+        out[1] = it;
+        reinterpret_cast<double*>(out + 4)[0] = (double)rr;
     }
 }
 
@@ -402,7 +600,97 @@ struct FieldSolver {
     int grid = 0;
     double pcg_ms = 0, pcg_bytes = 0;
     long long pcg_launches = 0;
+    // multigrid hierarchy (host-built, device-resident), both precisions
+    struct CsrBufs {
+        DBuf<int> ptr, col;
+        DBuf<double2> v64;
+        DBuf<float2> v32;
+        int n = 0, group = 1;
+    };
+    struct LevelBufs {
+        CsrBufs R, S, P;
+        DBuf<double2> r64, y64;
+        DBuf<float2> r32, y32;
+    } lvb[kMaxLevels];
+    DBuf<double2> Ainv64, rc64, yc64;
+    DBuf<float2> Ainv32, rc32, yc32;
+    DevHierarchy<double> H64{};
+    DevHierarchy<float> H32{};
+    DBuf<unsigned char> hier_dev64, hier_dev32;   // device copies of the hierarchy descriptors
+    bool amg = false;
+    int amg_levels = 0, amg_coarse = 0;
 
+    int upload_csr(const HostCsr& M, CsrBufs& B, int group) {
+        cudaStream_t st = c->stream;
+        B.n = M.n;
+        B.group = group;
+        MTK_TRY(B.ptr.upload(M.ptr.data(), M.ptr.size(), st));
+        MTK_TRY(B.col.upload(M.col.data(), M.col.size(), st));
+        std::vector<double2> v64(M.val.size());
+        std::vector<float2> v32(M.val.size());
+        for (size_t i = 0; i < M.val.size(); i++) {
+            v64[i] = make_double2(M.val[i].real(), M.val[i].imag());
+            v32[i] = make_float2((float)M.val[i].real(), (float)M.val[i].imag());
+        }
+        MTK_TRY(B.v64.upload(v64.data(), v64.size(), st));
+        MTK_TRY(B.v32.upload(v32.data(), v32.size(), st));
+        return MTK_OK;
+    }
+
+    // Builds the aggregation hierarchy from theta (same off-diagonals as field_assemble).
+    int build_amg(const int* nbr_h, const double* theta_h, int N) {
+        const double pi = 3.14159265358979323846;
+        std::vector<int> nbr3(nbr_h, nbr_h + 3 * (size_t)n);
+        std::vector<std::complex<double>> vals(3 * (size_t)n);
+        for (int f = 0; f < n; f++)
+            for (int j = 0; j < 3; j++) {
+                double ang = (double)N * (theta_h[3 * f + j] + pi);
+                vals[(size_t)j * n + f] = std::complex<double>(-std::cos(ang), -std::sin(ang));
+            }
+        HostHierarchy HH;
+        if (!build_hierarchy(n, nbr3, vals, 3.0 + 1e-9, HH)) return MTK_OK;   // keep Jacobi
+        const int nl = (int)HH.lv.size();
+        if (nl == 0) return MTK_OK;
+        cudaStream_t st = c->stream;
+        auto grp = [](const HostCsr& M) { return M.n > 0 && (double)M.col.size() / M.n > 8.0 ? 32 : 1; };
+        for (int l = 0; l < nl; l++) {
+            const HostCycleOps& O = HH.ops[l];
+            LevelBufs& B = lvb[l];
+            const int up_group = (grp(O.S) == 32 || grp(O.P) == 32) ? 32 : 1;
+            MTK_TRY(upload_csr(O.R, B.R, grp(O.R)));
+            MTK_TRY(upload_csr(O.S, B.S, up_group));
+            MTK_TRY(upload_csr(O.P, B.P, up_group));
+            const int ln = O.S.n;
+            if (l > 0) {
+                MTK_TRY(B.r64.alloc(ln)); MTK_TRY(B.r32.alloc(ln));
+                MTK_TRY(B.y64.alloc(ln)); MTK_TRY(B.y32.alloc(ln));
+            }
+            auto mk64 = [](const CsrBufs& C) { return DevCsr<double>{C.n, C.group, C.ptr.p, C.col.p, C.v64.p}; };
+            auto mk32 = [](const CsrBufs& C) { return DevCsr<float>{C.n, C.group, C.ptr.p, C.col.p, C.v32.p}; };
+            H64.L[l] = DevLevel<double>{mk64(B.R), mk64(B.S), mk64(B.P), B.r64.p, B.y64.p};
+            H32.L[l] = DevLevel<float>{mk32(B.R), mk32(B.S), mk32(B.P), B.r32.p, B.y32.p};
+        }
+        std::vector<double2> a64(HH.Ainv.size());
+        std::vector<float2> a32(HH.Ainv.size());
+        for (size_t i = 0; i < HH.Ainv.size(); i++) {
+            a64[i] = make_double2(HH.Ainv[i].real(), HH.Ainv[i].imag());
+            a32[i] = make_float2((float)HH.Ainv[i].real(), (float)HH.Ainv[i].imag());
+        }
+        MTK_TRY(Ainv64.upload(a64.data(), a64.size(), st));
+        MTK_TRY(Ainv32.upload(a32.data(), a32.size(), st));
+        MTK_TRY(rc64.alloc(HH.nc)); MTK_TRY(yc64.alloc(HH.nc));
+        MTK_TRY(rc32.alloc(HH.nc)); MTK_TRY(yc32.alloc(HH.nc));
+        H64.nlev = nl; H64.nc = HH.nc; H64.Ainv = Ainv64.p; H64.rc = rc64.p; H64.yc = yc64.p;
+        H32.nlev = nl; H32.nc = HH.nc; H32.Ainv = Ainv32.p; H32.rc = rc32.p; H32.yc = yc32.p;
+        MTK_TRY(hier_dev64.alloc(sizeof(DevHierarchy<double>)));
+        MTK_TRY(hier_dev32.alloc(sizeof(DevHierarchy<float>)));
+        amg = true;
+        amg_levels = nl;
+        amg_coarse = HH.nc;
+        return MTK_OK;
+    }
+
+    template <typename T> DevHierarchy<T> hier() const;
     ComplexEll<double> A64() const { return {n, nbr.p, v64.p, d64.p}; }
     ComplexEll<float> A32() const { return {n, nbr.p, v32.p, d32.p}; }
 
@@ -424,8 +712,19 @@ struct FieldSolver {
         int g = 0;
         MTK_TRY(reset_barrier(c));
         MTK_CUDA_TRY(cudaEventRecord(c->ev_k0, c->stream));
-        MTK_TRY(launch_persistent(c, pcg_complex<T>, &g, A, minv, bb, xx, rr, zz, pp, qq,
-                                  reinterpret_cast<T*>(c->partials), barrier_of(c), tol2, maxit, c->dev_int));
+        if (amg) {
+            DevHierarchy<T> H = hier<T>();
+            H.L[0].r = rr;   // level 0 works on the PCG residual and writes the PCG z
+            H.L[0].y = zz;
+            DevHierarchy<T>* Hd = reinterpret_cast<DevHierarchy<T>*>(sizeof(T) == 8 ? hier_dev64.p : hier_dev32.p);
+            MTK_CUDA_TRY(cudaMemcpyAsync(Hd, &H, sizeof(H), cudaMemcpyHostToDevice, c->stream));
+            const DevHierarchy<T>* Hc = Hd;
+            MTK_TRY(launch_persistent(c, pcg_complex_mg<T>, &g, A, Hc, bb, xx, rr, zz, pp, qq,
+                                      reinterpret_cast<T*>(c->partials), barrier_of(c), tol2, maxit, c->dev_int));
+        } else {
+            MTK_TRY(launch_persistent(c, pcg_complex<T>, &g, A, minv, bb, xx, rr, zz, pp, qq,
+                                      reinterpret_cast<T*>(c->partials), barrier_of(c), tol2, maxit, c->dev_int));
+        }
         MTK_CUDA_TRY(cudaEventRecord(c->ev_k1, c->stream));
         MTK_CUDA_TRY(cudaMemcpyAsync(c->h_int, c->dev_int, 8 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
         MTK_CUDA_TRY(cudaStreamSynchronize(c->stream));
@@ -446,6 +745,9 @@ struct FieldSolver {
         return MTK_OK;
     }
 };
+
+template <> DevHierarchy<double> FieldSolver::hier<double>() const { return H64; }
+template <> DevHierarchy<float> FieldSolver::hier<float>() const { return H32; }
 
 }  // namespace
 
@@ -488,6 +790,7 @@ extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const 
                                          S.d32.p, S.inv64.p, S.inv32.p, S.area32.p);
     c->kernels++;
     MTK_CUDA_TRY(cudaGetLastError());
+    if (!getenv("MTK_NO_AMG")) MTK_TRY(S.build_amg(nbr_h, theta_h, nRosy));
 
     long long iters = 0, solves = 0, refines = 0;
     double worst = 0.0;

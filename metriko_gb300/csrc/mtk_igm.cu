@@ -204,7 +204,7 @@ __device__ void igm_apply_z(const IgmOp<T>& A, const ZProj<T>& P, const T* pz, T
 // mode 1: residual only, r = P(b - K x) written to r, |r|^2 in out.
 // out[0] status, out[1] iterations, (double*)(out+4): final |r|^2.
 template <typename T>
-__global__ void __launch_bounds__(kBlock) igm_pcg(IgmOp<T> A, ZProj<T> P, const unsigned char* __restrict__ fixy,
+__global__ void __launch_bounds__(kBlock, 1) igm_pcg(IgmOp<T> A, ZProj<T> P, const unsigned char* __restrict__ fixy,
                                                  const T* __restrict__ minvy, const T* __restrict__ b, T* x, T* r, T* z,
                                                  T* p, T* q, T* partials, GridBarrier bar, double tol2, int maxit,
                                                  int mode, int* out) {
