@@ -29,6 +29,7 @@
 #include <cmath>
 #include <vector>
 
+#include "mtk_amg_real.cuh"
 #include "mtk_ctx.cuh"
 
 namespace mtk {
@@ -207,7 +208,8 @@ template <typename T>
 __global__ void __launch_bounds__(kBlock, 1) igm_pcg(IgmOp<T> A, ZProj<T> P, const unsigned char* __restrict__ fixy,
                                                  const T* __restrict__ minvy, const T* __restrict__ b, T* x, T* r, T* z,
                                                  T* p, T* q, T* partials, GridBarrier bar, double tol2, int maxit,
-                                                 int mode, int* out) {
+                                                 int mode, int* out, const RDevHierarchy<T>* __restrict__ Hp,
+                                                 T mg_scale) {
     extern __shared__ unsigned char smem_raw[];
     ZSmem<T> zs;
     zs.bind(reinterpret_cast<T*>(smem_raw), A.nZ, A.nJ);
@@ -234,12 +236,21 @@ __global__ void __launch_bounds__(kBlock, 1) igm_pcg(IgmOp<T> A, ZProj<T> P, con
     for (int j = t0; j < nY; j += stride) {
         T rj = fixy[j] ? T(0) : b[j] - q[j];
         r[j] = rj;
-        T zj = minvy[j] * rj;
         part[1] += rj * rj;
-        if (mode == 0) {
+        if (mode == 0 && !Hp) {
+            T zj = minvy[j] * rj;
             z[j] = zj;
             p[j] = zj;
             part[0] += rj * zj;
+        }
+    }
+    if (mode == 0 && Hp) {   // multigrid on the free block: z_y = mask (B r_y) / scale
+        if (!grid_sync(bar)) { status = 5; goto done; }
+        if (!rvcycle(*Hp, mg_scale, fixy, bar)) { status = 5; goto done; }
+        for (int j = t0; j < nY; j += stride) {
+            T zj = z[j];
+            p[j] = zj;
+            part[0] += r[j] * zj;
         }
     }
     for (int j = threadIdx.x; j < nZ; j += blockDim.x) zs.rz[j] = __ldg(b + nY + j) - zs.qz[j];
@@ -291,10 +302,17 @@ __global__ void __launch_bounds__(kBlock, 1) igm_pcg(IgmOp<T> A, ZProj<T> P, con
                 T rj = r[j] - alpha * q[j];
                 x[j] += alpha * p[j];
                 r[j] = rj;
-                T zj = minvy[j] * rj;
-                z[j] = zj;
-                part[0] += rj * zj;
+                if (!Hp) {
+                    T zj = minvy[j] * rj;
+                    z[j] = zj;
+                    part[0] += rj * zj;
+                }
                 part[1] += rj * rj;
+            }
+            if (Hp) {
+                if (!grid_sync(bar)) { status = 5; break; }
+                if (!rvcycle(*Hp, mg_scale, fixy, bar)) { status = 5; break; }
+                for (int j = t0; j < nY; j += stride) part[0] += r[j] * z[j];
             }
             for (int j = threadIdx.x; j < nZ; j += blockDim.x) {
                 zs.xz[j] += alpha * zs.pz[j];
@@ -669,6 +687,65 @@ struct Igm {
     double pcg_ms = 0, pcg_bytes = 0;
     long long pcg_launches = 0;
     long long nnzW = 0, nnzS = 0, nnzYT = 0;
+    // multigrid on the free block (host-built)
+    struct RCsrBufs { DBuf<int> ptr, col; DBuf<double> v64; DBuf<float> v32; int n = 0, group = 1; };
+    struct RLevelBufs { RCsrBufs R, S, P; DBuf<double> r64, y64; DBuf<float> r32, y32; } rlv[kRMaxLevels];
+    DBuf<double> rAinv64, rrc64, ryc64;
+    DBuf<float> rAinv32, rrc32, ryc32;
+    DBuf<unsigned char> rh_dev64, rh_dev32;
+    RDevHierarchy<double> RH64{};
+    RDevHierarchy<float> RH32{};
+    bool mg = false;
+    int mg_levels = 0;
+    double cur_scale = 1.0;
+    template <typename T> RDevHierarchy<T> rhier() const;
+
+    int upload_rcsr(const RCsr& M, RCsrBufs& B, int group) {
+        B.n = M.n;
+        B.group = group;
+        MTK_TRY(B.ptr.upload(M.ptr.data(), M.ptr.size(), st));
+        MTK_TRY(B.col.upload(M.col.data(), M.col.size(), st));
+        MTK_TRY(B.v64.upload(M.val.data(), M.val.size(), st));
+        std::vector<float> v32(M.val.begin(), M.val.end());
+        MTK_TRY(B.v32.upload(v32.data(), v32.size(), st));
+        return MTK_OK;
+    }
+
+    int build_mg(RCsr K, std::vector<int> node, std::vector<int> comp, int nnode) {
+        RHierarchy HH;
+        if (!build_real_hierarchy(std::move(K), std::move(node), std::move(comp), nnode, HH)) return MTK_OK;
+        const int nl = (int)HH.lv.size();
+        if (nl == 0) return MTK_OK;
+        auto grp = [](const RCsr& M) { return M.n > 0 && (double)M.col.size() / M.n > 8.0 ? 32 : 1; };
+        for (int l = 0; l < nl; l++) {
+            const RCycleOps& O = HH.ops[l];
+            RLevelBufs& B = rlv[l];
+            const int up = (grp(O.S) == 32 || grp(O.P) == 32) ? 32 : 1;
+            MTK_TRY(upload_rcsr(O.R, B.R, grp(O.R)));
+            MTK_TRY(upload_rcsr(O.S, B.S, up));
+            MTK_TRY(upload_rcsr(O.P, B.P, up));
+            if (l > 0) {
+                MTK_TRY(B.r64.alloc(O.S.n)); MTK_TRY(B.y64.alloc(O.S.n));
+                MTK_TRY(B.r32.alloc(O.S.n)); MTK_TRY(B.y32.alloc(O.S.n));
+            }
+            auto m64 = [](const RCsrBufs& C) { return RDevCsr<double>{C.n, C.group, C.ptr.p, C.col.p, C.v64.p}; };
+            auto m32 = [](const RCsrBufs& C) { return RDevCsr<float>{C.n, C.group, C.ptr.p, C.col.p, C.v32.p}; };
+            RH64.L[l] = RDevLevel<double>{m64(B.R), m64(B.S), m64(B.P), B.r64.p, B.y64.p};
+            RH32.L[l] = RDevLevel<float>{m32(B.R), m32(B.S), m32(B.P), B.r32.p, B.y32.p};
+        }
+        MTK_TRY(rAinv64.upload(HH.Ainv.data(), HH.Ainv.size(), st));
+        std::vector<float> a32(HH.Ainv.begin(), HH.Ainv.end());
+        MTK_TRY(rAinv32.upload(a32.data(), a32.size(), st));
+        MTK_TRY(rrc64.alloc(HH.nc)); MTK_TRY(ryc64.alloc(HH.nc));
+        MTK_TRY(rrc32.alloc(HH.nc)); MTK_TRY(ryc32.alloc(HH.nc));
+        RH64.nlev = nl; RH64.nc = HH.nc; RH64.Ainv = rAinv64.p; RH64.rc = rrc64.p; RH64.yc = ryc64.p;
+        RH32.nlev = nl; RH32.nc = HH.nc; RH32.Ainv = rAinv32.p; RH32.rc = rrc32.p; RH32.yc = ryc32.p;
+        MTK_TRY(rh_dev64.alloc(sizeof(RDevHierarchy<double>)));
+        MTK_TRY(rh_dev32.alloc(sizeof(RDevHierarchy<float>)));
+        mg = true;
+        mg_levels = nl;
+        return MTK_OK;
+    }
 
     // Algorithmic bytes of one projected-PCG iteration (operator chain + vector updates):
     //   W gather   nnzW (tag 4 + val T + x T) + 2 nCut (ptr 4 + U write T)
@@ -703,8 +780,20 @@ struct Igm {
         T* partials = reinterpret_cast<T*>(c->partials);
         GridBarrier bar = barrier_of(c);
         int* out = c->dev_int;
+        const RDevHierarchy<T>* Hp = nullptr;
+        T mg_scale = T(0);
+        if (mg && mode == 0) {
+            RDevHierarchy<T> H = rhier<T>();
+            H.L[0].r = r;    // level 0 = the free block of the PCG residual / preconditioned residual
+            H.L[0].y = z;
+            unsigned char* dst = sizeof(T) == 8 ? rh_dev64.p : rh_dev32.p;
+            MTK_CUDA_TRY(cudaMemcpyAsync(dst, &H, sizeof(H), cudaMemcpyHostToDevice, st));
+            Hp = reinterpret_cast<const RDevHierarchy<T>*>(dst);
+            mg_scale = T(1.0 / cur_scale);
+        }
         void* params[] = {&A, &P, (void*)&fx, (void*)&minv, (void*)&b, (void*)&x, (void*)&r, (void*)&z, (void*)&p,
-                          (void*)&q, (void*)&partials, &bar, &tol2, &maxit, &mode, (void*)&out};
+                          (void*)&q, (void*)&partials, &bar, &tol2, &maxit, &mode, (void*)&out, (void*)&Hp,
+                          (void*)&mg_scale};
         MTK_TRY(reset_barrier(c));
         MTK_CUDA_TRY(cudaEventRecord(c->ev_k0, st));
         MTK_CUDA_TRY(cudaLaunchCooperativeKernel(reinterpret_cast<void*>(kern), dim3(grid), dim3(kBlock), params, smem, st));
@@ -766,6 +855,7 @@ struct Igm {
     // Solve K x = b (projected, x feasible on entry) to ||P(b - K x)|| <= tol ||P b||.
     int solve(double scale, double shift, const double* b, double* x, const mtk_solve_opts& o, mtk_stats* stats,
               double* rel_out) {
+        cur_scale = scale;
         long long iters = 0, refines = 0;
         double rr = 0, bb = 0;
         // ||P b||^2: residual mode with x = 0 gives P(b)
@@ -819,6 +909,9 @@ struct Igm {
         return MTK_OK;
     }
 };
+
+template <> RDevHierarchy<double> Igm::rhier<double>() const { return RH64; }
+template <> RDevHierarchy<float> Igm::rhier<float>() const { return RH32; }
 
 // Orthonormal rows (two-pass Gram-Schmidt); returns false if `row` is dependent.
 bool add_orthonormal(std::vector<std::vector<double>>& Q, std::vector<double> row) {
@@ -1011,10 +1104,70 @@ extern "C" int mtk_iterative_rounding(mtk_ctx* c, const mtk_igm_desc* d, const m
     // ---- dense z block of the normal matrix (host, FP64) for the block-Jacobi preconditioner:
     //      K_zz = scale * USmall^T (2 W_J^T S W_J) USmall + shift I.  Only faces touching J matter.
     std::vector<double> h_grad(6 * (size_t)nF);
+    MTK_CUDA_TRY(cudaMemcpyAsync(h_grad.data(), S.grad.p, sizeof(double) * h_grad.size(), cudaMemcpyDeviceToHost, st));
+    MTK_CUDA_TRY(cudaStreamSynchronize(st));
+    // ---- multigrid for the free block: K_pre = 2 W_y^T S W_y + delta I, delta = 1e-4 / length^2
+    //      (the seamless system is length^2 K_pre exactly; the naive one up to the shift)
+    if (nY > 0 && !getenv("MTK_NO_AMG")) {
+        std::vector<int> hs_ptr(nCut + 1, 0), hs_col;
+        std::vector<double> hs_val;
+        hs_col.reserve(8 * (size_t)nCut);
+        hs_val.reserve(8 * (size_t)nCut);
+        std::vector<std::pair<int, double>> rowbuf;
+        for (int c2 = 0; c2 < nCut; c2++) {
+            rowbuf.clear();
+            for (int k = vptr[c2]; k < vptr[c2 + 1]; k++) {
+                int f = vface[k];
+                int a = d->cutF[3 * f] == c2 ? 0 : (d->cutF[3 * f + 1] == c2 ? 1 : 2);
+                for (int j = 0; j < 3; j++) {
+                    double v = h_grad[6 * f + 2 * a] * h_grad[6 * f + 2 * j] + h_grad[6 * f + 2 * a + 1] * h_grad[6 * f + 2 * j + 1];
+                    int col = d->cutF[3 * f + j];
+                    bool found = false;
+                    for (auto& e : rowbuf) if (e.first == col) { e.second += v; found = true; break; }
+                    if (!found) rowbuf.emplace_back(col, v);
+                }
+            }
+            std::sort(rowbuf.begin(), rowbuf.end());
+            for (auto& e : rowbuf) { hs_col.push_back(e.first); hs_val.push_back(e.second); }
+            hs_ptr[c2 + 1] = (int)hs_col.size();
+        }
+        const double delta = 1e-4 / (d->length * d->length);
+        RCsr K;
+        K.n = nY;
+        K.ptr.assign(nY + 1, 0);
+        K.col.reserve(16 * (size_t)nY);
+        K.val.reserve(16 * (size_t)nY);
+        std::vector<double> acc(nY, 0.0);
+        std::vector<char> used(nY, 0);
+        std::vector<int> cols;
+        for (int j = 0; j < nY; j++) {
+            cols.clear();
+            for (int e = yptr[j]; e < yptr[j + 1]; e++) {
+                const int r = yrow[e], c2 = r >> 1, kk = r & 1;
+                const double w1 = yval[e];
+                for (int p = hs_ptr[c2]; p < hs_ptr[c2 + 1]; p++) {
+                    const int r2 = 2 * hs_col[p] + kk;
+                    const double sv = hs_val[p];
+                    for (int e2 = d->w_ptr[r2]; e2 < d->w_ptr[r2 + 1]; e2++) {
+                        const int y2 = tag[e2];
+                        if (y2 < 0) continue;
+                        if (!used[y2]) { used[y2] = 1; cols.push_back(y2); acc[y2] = 0; }
+                        acc[y2] += 2.0 * w1 * sv * d->w_val[e2];
+                    }
+                }
+            }
+            if (!used[j]) { used[j] = 1; cols.push_back(j); acc[j] = 0; }
+            acc[j] += delta;
+            std::sort(cols.begin(), cols.end());
+            for (int y2 : cols) { K.col.push_back(y2); K.val.push_back(acc[y2]); used[y2] = 0; }
+            K.ptr[j + 1] = (int)K.col.size();
+        }
+        std::vector<int> node(nY), comp(nY);
+        for (int j = 0; j < nY; j++) { node[j] = y2full[j] / 2; comp[j] = y2full[j] % 2; }
+        MTK_TRY(S.build_mg(std::move(K), std::move(node), std::move(comp), nFull / 2));
+    }
     std::vector<double> BJJ((size_t)nJ * nJ, 0.0);
     if (nJ > 0) {
-        MTK_CUDA_TRY(cudaMemcpyAsync(h_grad.data(), S.grad.p, sizeof(double) * h_grad.size(), cudaMemcpyDeviceToHost, st));
-        MTK_CUDA_TRY(cudaStreamSynchronize(st));
         std::vector<char> touchJ(nCut, 0);
         for (int r = 0; r < nW; r++)
             for (int e = d->w_ptr[r]; e < d->w_ptr[r + 1]; e++) if (tag[e] < 0) touchJ[r >> 1] = 1;
