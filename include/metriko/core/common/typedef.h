@@ -17,6 +17,14 @@
 #include <stdexcept>
 #include <vector>
 
+// Element-parallel host loops (each iteration writes only its own outputs, so results do not
+// depend on the thread count).
+#if defined(_OPENMP)
+#define METRIKO_PARALLEL_FOR _Pragma("omp parallel for schedule(static)")
+#else
+#define METRIKO_PARALLEL_FOR
+#endif
+
 namespace metriko {
     constexpr double PI = 3.14159265358979323846;
     constexpr double TwoPI = 2 * PI;

@@ -162,6 +162,7 @@ namespace metriko {
                 int a = F(f, i), b = F(f, (i + 1) % 3);
                 ent[fill[std::min(a, b)]++] = {std::max(a, b), f, i, a};
             }
+        METRIKO_PARALLEL_FOR
         for (int v = 0; v < nV; v++)
             std::sort(ent.begin() + cnt[v], ent.begin() + cnt[v + 1], [](const Ent& x, const Ent& y) {
                 if (x.hi != y.hi) return x.hi < y.hi;
@@ -231,11 +232,13 @@ namespace metriko {
         }
         for (int v = 0; v < nV; v++) if (vert2half[v] < 0) throw std::invalid_argument("isolated vertex");
         face2half3 = MatXi(nF, 3);
+        METRIKO_PARALLEL_FOR
         for (int f = 0; f < nF; f++)
             for (int j = 0; j < 3; j++) {
                 int e = face2edge(f, j);
                 face2half3(f, j) = 2 * e + (edge2face(e, 0) == f ? 0 : 1);
             }
+        METRIKO_PARALLEL_FOR
         for (int f = 0; f < nF; f++) {
             for (int j = 0; j < 3; j++) {
                 next[face2half3(f, j)] = face2half3(f, (j + 1) % 3);
@@ -249,6 +252,7 @@ namespace metriko {
                 crnr[h] = 3 * f + it;
             }
         }
+        METRIKO_PARALLEL_FOR
         for (int h = 0; h < nH; h++) head[h] = tail[next[h]];
         for (int i = 0; i < nF; i++) faces.push_back(Face{{i, this}});
         for (int i = 0; i < nV; i++) verts.push_back(Vert{{i, this}});
@@ -257,6 +261,7 @@ namespace metriko {
 
         faceBasisX = MatXd(nF, 3); faceBasisY = MatXd(nF, 3); faceNormal = MatXd(nF, 3); baryCenter = MatXd(nF, 3);
         faceArea = VecXd(nF); heArgOnFace = VecXd(nH); angleDefect = VecXd(nV);
+        METRIKO_PARALLEL_FOR
         for (int f = 0; f < nF; f++) {
             Row3d p0 = row3(pos, F(f, 0)), p1 = row3(pos, F(f, 1)), p2 = row3(pos, F(f, 2));
             Row3d x = p1 - p0;
@@ -268,6 +273,7 @@ namespace metriko {
             set_row3(baryCenter, f, (p0 + p1 + p2) / 3.0);
             faceArea[f] = n.norm() * 0.5;
         }
+        METRIKO_PARALLEL_FOR
         for (int f = 0; f < nF; f++) {     // hmesh.h:522-531
             double sum = 0;
             Row3d bx = row3(faceBasisX, f);
@@ -279,6 +285,7 @@ namespace metriko {
                 heArgOnFace[h.id] = sum;
             }
         }
+        METRIKO_PARALLEL_FOR
         for (int v = 0; v < nV; v++) {     // hmesh.h:599-610
             double sum = 0;
             for (Half h : verts[v].adjHalfs()) {

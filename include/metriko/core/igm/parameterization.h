@@ -15,6 +15,9 @@
 //
 #ifndef METRIKO_PARAMETERIZATION_H
 #define METRIKO_PARAMETERIZATION_H
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <map>
 #include <memory>
 #include <set>
@@ -202,7 +205,24 @@ namespace metriko {
                     if (mat(i, j) != 0) T.emplace_back(r0 + i, c0 + j, double(mat(i, j)));
         };
         int currConstraint = 0;
+        vT.reserve(size_t(N) * cut.nV + 64);
         for (int v = 0; v < raw.nV; v++) {       // setup.ipp:66-124
+            {   // vertices away from the seam: one cut copy, identity block, no constraint
+                const int g0 = raw.vert2half[v];
+                int g = g0;
+                bool onSeam = false;
+                do {
+                    if (seam[raw.edge[g]]) { onSeam = true; break; }
+                    g = raw.twin[raw.prev[g]];
+                } while (g != g0);
+                if (!onSeam) {
+                    const int f = raw.face[g0];
+                    int jVcut = -1;
+                    for (int j = 0; j < 3; j++) if (raw.idx(f, j) == v) jVcut = cut.idx(f, j);
+                    for (int i = 0; i < N; i++) vT.emplace_back(N * jVcut + i, N * v + i, 1.0);
+                    continue;
+                }
+            }
             std::vector<MatXi> pm{I};
             std::vector<int> pidx{v};
             int iVcut = -1;
@@ -378,7 +398,11 @@ namespace metriko {
 
     inline bool RosyParameterization::integ() {
         IntegSystem sys;
+        auto t0 = std::chrono::steady_clock::now();
         build_system(sys);
+        if (getenv("MTK_DEBUG") && getenv("MTK_DEBUG")[0] == '1')
+            fprintf(stderr, "[host] %-22s %8.1f ms\n", "integ build_system",
+                    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
         const SprsD& fullx2Nfunc = sys.fullx2Nfunc;
         bool success = iterative_rounding(sys.desc, fullx, naivex, fixOrder, fixVals);
 

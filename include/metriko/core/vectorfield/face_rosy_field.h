@@ -42,6 +42,7 @@ namespace metriko {
         void set_field_from_compressed() {
             const complex r = std::polar(1., TwoPI / rosyN);
             field = MatXc(mesh.nF, rosyN);
+            METRIKO_PARALLEL_FOR
             for (int f = 0; f < mesh.nF; f++) {
                 complex root = std::exp(std::log(std::polar(1., std::arg(compressed[f]))) * (1. / rosyN));
                 for (int i = 0; i < rosyN; i++) field(f, i) = root * (i ? std::exp(double(i) * std::log(r)) : complex(1, 0));
@@ -53,6 +54,7 @@ namespace metriko {
         void assembly_inputs(std::vector<int>& nbr, std::vector<double>& theta) const {
             nbr.resize(3 * size_t(mesh.nF));
             theta.resize(3 * size_t(mesh.nF));
+            METRIKO_PARALLEL_FOR
             for (int f = 0; f < mesh.nF; f++)
                 for (int j = 0; j < 3; j++) {
                     int h = mesh.face2half3(f, j), t = mesh.twin[h];
@@ -84,6 +86,7 @@ namespace metriko {
 
         void computeConnection() {      // face_rosy_field.h:135-143
             connection = VecXc(mesh.nE, complex(0, 0));
+            METRIKO_PARALLEL_FOR
             for (int e = 0; e < mesh.nE; e++) {
                 Row3d v = Half{{mesh.edge2half[e], &mesh}}.vec().normalized();
                 int f0 = mesh.edge2face(e, 0), f1 = mesh.edge2face(e, 1);
@@ -95,6 +98,7 @@ namespace metriko {
 
         void computeSingular(const VecXd& effort) {   // face_rosy_field.h:126-133
             singular = VecXi(mesh.nV, 1);
+            METRIKO_PARALLEL_FOR
             for (int v = 0; v < mesh.nV; v++) {
                 double sum = mesh.angleDefect[v] * rosyN;
                 int h0 = mesh.vert2half[v], h = h0;
@@ -117,6 +121,7 @@ namespace metriko {
 
     private:
         void pMatching(VecXd& effort) {    // face_rosy_field.h:164-193
+            METRIKO_PARALLEL_FOR
             for (int e = 0; e < mesh.nE; e++) {
                 int f0 = mesh.edge2face(e, 0), f1 = mesh.edge2face(e, 1);
                 complex conn = connection[e];
@@ -138,6 +143,7 @@ namespace metriko {
         }
 
         void cMatching(VecXd& effort) {    // face_rosy_field.h:195-228
+            METRIKO_PARALLEL_FOR
             for (int e = 0; e < mesh.nE; e++) {
                 int iM = 0;
                 double mn = 32767000.;
@@ -202,6 +208,7 @@ namespace metriko {
     // face_rosy_field.h:277-290 (N = 4)
     inline MatXd compute_extrinsic_field(const Hmesh& mesh, const FaceRosyField& fld, int rosyN) {
         MatXd ext(mesh.nF, 3 * rosyN);
+        METRIKO_PARALLEL_FOR
         for (int f = 0; f < mesh.nF; f++) {
             Row3d bx = row3(mesh.faceBasisX, f), by = row3(mesh.faceBasisY, f);
             for (int i = 0; i < rosyN; i++) {
@@ -333,8 +340,17 @@ namespace metriko {
         std::vector<int> in_cut(m.nV, 0);
         for (int f = 0; f < m.nF; f++) for (int j = 0; j < 3; j++) if (cuts(f, j)) in_cut[F(f, j)] = 1;
         std::vector<int> dist(m.nV, -1), prev(m.nV, -1), touched;
+        long long ncut = 0;
+        for (int v = 0; v < m.nV; v++) ncut += in_cut[v];
         for (int i = 0; i < singularities.size(); i++) {
             const int src = singularities[i];
+            if (ncut == 0) {
+                // no target at all: the search would exhaust the mesh and return -1, so the path
+                // is the singularity alone
+                in_cut[src] = 1;
+                ncut = 1;
+                continue;
+            }
             // unit-weight Dijkstra; pops ordered by (distance, id)
             for (int v : touched) { dist[v] = -1; prev[v] = -1; }
             touched.clear();
@@ -366,7 +382,7 @@ namespace metriko {
             std::vector<int> path;
             if (found == -1) path.push_back(src);
             else for (int v = found; v != -1; v = prev[v]) path.push_back(v);
-            for (int v : path) in_cut[v] = 1;
+            for (int v : path) { ncut += !in_cut[v]; in_cut[v] = 1; }
             for (size_t ii = 0; ii + 1 < path.size(); ii++) {
                 int v0 = path[ii], v1 = path[ii + 1];
                 int fi = -1;

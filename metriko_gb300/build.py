@@ -2,7 +2,8 @@
 
 Each translation unit is compiled in parallel; the shared library lands next to this file.
 Host C++ is compiled with -ffp-contract=off so that its floating-point results are the same
-on x86_64 and aarch64 (no fused multiply-add contraction of the topology arithmetic).
+on x86_64 and aarch64 (no fused multiply-add contraction of the topology arithmetic), and with
+OpenMP for the element-parallel host loops (each iteration writes only its own outputs).
 """
 from __future__ import annotations
 
@@ -55,13 +56,14 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         deps = [CSRC / src] + headers
         if force or _stale(obj, deps):
             jobs.append([nvcc, *ARCH, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
-                         "-Xcompiler", "-ffp-contract=off", *inc, "-c", str(CSRC / src), "-o", str(obj)])
+                         "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-fopenmp", *inc, "-c", str(CSRC / src),
+                         "-o", str(obj)])
     for src in CPP_SOURCES:
         obj = BUILD / (src + ".o")
         deps = [CSRC / src] + headers
         cuda_inc = str(Path(nvcc).resolve().parent.parent / "include")
         if force or _stale(obj, deps):
-            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", *inc, "-I" + cuda_inc,
+            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fopenmp", *inc, "-I" + cuda_inc,
                          "-c", str(CSRC / src), "-o", str(obj)])
     with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
         for r in ex.map(_run, jobs):
@@ -69,7 +71,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
                 print(r.stdout, r.stderr, file=sys.stderr)
     objs = [str(BUILD / (s + ".o")) for s in CU_SOURCES + CPP_SOURCES]
     if force or jobs or not OUT.exists():
-        _run([nvcc, *ARCH, "-shared", "-o", str(OUT), *objs, "-lcudart"])
+        _run([nvcc, *ARCH, "-shared", "-Xcompiler", "-fopenmp", "-o", str(OUT), *objs, "-lcudart", "-lgomp"])
     return OUT
 
 

@@ -19,10 +19,68 @@
 #include <cmath>
 #include <complex>
 #include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 #include "mtk_ctx.cuh"
 
 namespace mtk {
+
+// Builds CSR rows in parallel: fn(row, add) calls add(col, value) for the entries of `row`
+// (duplicates are summed); each thread owns a contiguous block of rows and the blocks are
+// concatenated in order, so the result does not depend on the thread count.
+template <typename V, typename RowFn>
+void build_rows_parallel(int nrows, int ncols, RowFn fn, std::vector<int>& ptr, std::vector<int>& col,
+                         std::vector<V>& val) {
+    int maxt = 1;
+#ifdef _OPENMP
+    maxt = omp_get_max_threads();
+#endif
+    std::vector<std::vector<int>> pcol(maxt), pcnt(maxt);
+    std::vector<std::vector<V>> pval(maxt);
+    std::vector<int> rbeg(maxt + 1, nrows);
+#pragma omp parallel
+    {
+        int t = 0, nt = 1;
+#ifdef _OPENMP
+        t = omp_get_thread_num();
+        nt = omp_get_num_threads();
+#endif
+        const int r0 = (int)((long long)nrows * t / nt), r1 = (int)((long long)nrows * (t + 1) / nt);
+        rbeg[t] = r0;
+        std::vector<V> acc(ncols, V(0));
+        std::vector<char> used(ncols, 0);
+        std::vector<int> cols;
+        auto& oc = pcol[t];
+        auto& ov = pval[t];
+        auto& on = pcnt[t];
+        on.reserve(r1 - r0);
+        for (int r = r0; r < r1; r++) {
+            cols.clear();
+            fn(r, [&](int c, V v) {
+                if (!used[c]) { used[c] = 1; cols.push_back(c); acc[c] = V(0); }
+                acc[c] += v;
+            });
+            std::sort(cols.begin(), cols.end());
+            for (int c : cols) { oc.push_back(c); ov.push_back(acc[c]); used[c] = 0; }
+            on.push_back((int)cols.size());
+        }
+    }
+    ptr.assign(nrows + 1, 0);
+    col.clear();
+    val.clear();
+    size_t total = 0;
+    for (int t = 0; t < maxt; t++) total += pcol[t].size();
+    col.reserve(total);
+    val.reserve(total);
+    int row = 0;
+    for (int t = 0; t < maxt; t++) {
+        for (size_t k = 0; k < pcnt[t].size(); k++, row++) ptr[row + 1] = ptr[row] + pcnt[t][k];
+        col.insert(col.end(), pcol[t].begin(), pcol[t].end());
+        val.insert(val.end(), pval[t].begin(), pval[t].end());
+    }
+}
 
 constexpr int kMaxLevels = 8;
 constexpr int kCoarseMax = 384;
@@ -135,41 +193,30 @@ inline void aggregate_level(HostLevel& L, HostCsr& next) {
         for (int i = 0; i < n; i++) L.mem[fill[L.agg[i]]++] = i;
     }
     L.dinv.resize(n);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < n; i++) {
         double d = 0;
         for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) if (A.col[p] == i) d = A.val[p].real();
         L.dinv[i] = d > 0 ? 1.0 / d : 1.0;
     }
-    // Galerkin coarse operator
+    // Galerkin coarse operator (rows = aggregates)
     next.n = na;
-    next.ptr.assign(na + 1, 0);
-    next.col.clear();
-    next.val.clear();
-    std::vector<std::complex<double>> acc(na, std::complex<double>(0, 0));
-    std::vector<char> used(na, 0);
-    std::vector<int> cols;
-    for (int a = 0; a < na; a++) {
-        cols.clear();
-        for (int m = L.mptr[a]; m < L.mptr[a + 1]; m++) {
-            int i = L.mem[m];
-            std::complex<double> ti = std::conj(L.T[i]);
-            for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) {
-                int j = A.col[p];
-                int b = L.agg[j];
-                if (!used[b]) { used[b] = 1; cols.push_back(b); acc[b] = 0; }
-                acc[b] += ti * A.val[p] * L.T[j];
+    build_rows_parallel<std::complex<double>>(
+        na, na,
+        [&](int a, auto add) {
+            for (int m = L.mptr[a]; m < L.mptr[a + 1]; m++) {
+                const int i = L.mem[m];
+                const std::complex<double> ti = std::conj(L.T[i]);
+                for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) {
+                    const int j = A.col[p];
+                    add(L.agg[j], ti * A.val[p] * L.T[j]);
+                }
             }
-        }
-        std::sort(cols.begin(), cols.end());
-        for (int b : cols) {
-            std::complex<double> v = acc[b];
-            if (b == a) v = std::complex<double>(v.real(), 0.0);   // Hermitian diagonal
-            next.col.push_back(b);
-            next.val.push_back(v);
-            used[b] = 0;
-        }
-        next.ptr[a + 1] = (int)next.col.size();
-    }
+        },
+        next.ptr, next.col, next.val);
+    for (int a = 0; a < na; a++)      // Hermitian diagonal
+        for (int p = next.ptr[a]; p < next.ptr[a + 1]; p++)
+            if (next.col[p] == a) next.val[p] = std::complex<double>(next.val[p].real(), 0.0);
 }
 
 // Hermitian positive definite inverse (complex Cholesky), returns false if not HPD.
@@ -212,17 +259,18 @@ inline bool build_hierarchy(int n, const std::vector<int>& nbr3, const std::vect
     HostCsr A0;
     A0.n = n;
     A0.ptr.resize(n + 1);
-    A0.col.reserve(4 * (size_t)n);
-    A0.val.reserve(4 * (size_t)n);
+    A0.col.resize(4 * (size_t)n);
+    A0.val.resize(4 * (size_t)n);
+#pragma omp parallel for schedule(static)
     for (int f = 0; f < n; f++) {
-        A0.ptr[f] = (int)A0.col.size();
+        A0.ptr[f] = 4 * f;
         struct E { int c; std::complex<double> v; } e[4];
         e[0] = {f, std::complex<double>(diag, 0)};
         for (int j = 0; j < 3; j++) e[1 + j] = {nbr3[3 * f + j], vals[(size_t)j * n + f]};
         std::sort(e, e + 4, [](const E& a, const E& b) { return a.c < b.c; });
-        for (auto& x : e) { A0.col.push_back(x.c); A0.val.push_back(x.v); }
+        for (int k = 0; k < 4; k++) { A0.col[4 * (size_t)f + k] = e[k].c; A0.val[4 * (size_t)f + k] = e[k].v; }
     }
-    A0.ptr[n] = (int)A0.col.size();
+    A0.ptr[n] = 4 * n;
     HostCsr cur = std::move(A0);
     while (cur.n > kCoarseMax && (int)H.lv.size() < kMaxLevels - 1) {
         HostLevel L;
@@ -250,6 +298,7 @@ inline bool build_hierarchy(int n, const std::vector<int>& nbr3, const std::vect
         O.S.ptr = A.ptr;
         O.S.col = A.col;
         O.S.val.resize(A.val.size());
+#pragma omp parallel for schedule(static)
         for (int i = 0; i < n; i++)
             for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) {
                 int j = A.col[p];
@@ -259,27 +308,16 @@ inline bool build_hierarchy(int n, const std::vector<int>& nbr3, const std::vect
             }
         // P: row i -> aggregates of i and of its neighbours
         O.P.n = n;
-        O.P.ptr.assign(n + 1, 0);
-        O.P.col.clear();
-        O.P.val.clear();
-        std::vector<cd> acc(na, cd(0, 0));
-        std::vector<char> used(na, 0);
-        std::vector<int> cols;
-        for (int i = 0; i < n; i++) {
-            cols.clear();
-            auto add = [&](int b, cd v) {
-                if (!used[b]) { used[b] = 1; cols.push_back(b); acc[b] = 0; }
-                acc[b] += v;
-            };
-            add(L.agg[i], alpha * L.T[i]);
-            for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) {
-                int j = A.col[p];
-                add(L.agg[j], -alpha * omega * L.dinv[i] * A.val[p] * L.T[j]);
-            }
-            std::sort(cols.begin(), cols.end());
-            for (int b : cols) { O.P.col.push_back(b); O.P.val.push_back(acc[b]); used[b] = 0; }
-            O.P.ptr[i + 1] = (int)O.P.col.size();
-        }
+        build_rows_parallel<cd>(
+            n, na,
+            [&](int i, auto add) {
+                add(L.agg[i], alpha * L.T[i]);
+                for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) {
+                    int j = A.col[p];
+                    add(L.agg[j], -alpha * omega * L.dinv[i] * A.val[p] * L.T[j]);
+                }
+            },
+            O.P.ptr, O.P.col, O.P.val);
         // R = P^H / alpha
         O.R.n = na;
         O.R.ptr.assign(na + 1, 0);

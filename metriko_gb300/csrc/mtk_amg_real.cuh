@@ -13,6 +13,7 @@
 #include <cmath>
 #include <vector>
 
+#include "mtk_amg.cuh"
 #include "mtk_ctx.cuh"
 
 namespace mtk {
@@ -136,26 +137,15 @@ inline void rcoarsen(RLevel& L, RCsr& next, std::vector<int>& cnode, std::vector
         for (int d = 0; d < n; d++) mem[fill[L.agg[d]]++] = d;
     }
     next.n = ncd;
-    next.ptr.assign(ncd + 1, 0);
-    next.col.clear();
-    next.val.clear();
-    std::vector<double> acc(ncd, 0.0);
-    std::vector<char> used(ncd, 0);
-    std::vector<int> cols;
-    for (int a = 0; a < ncd; a++) {
-        cols.clear();
-        for (int m = mptr[a]; m < mptr[a + 1]; m++) {
-            int i = mem[m];
-            for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) {
-                int b = L.agg[A.col[p]];
-                if (!used[b]) { used[b] = 1; cols.push_back(b); acc[b] = 0; }
-                acc[b] += L.T[i] * A.val[p] * L.T[A.col[p]];
+    build_rows_parallel<double>(
+        ncd, ncd,
+        [&](int a, auto add) {
+            for (int m = mptr[a]; m < mptr[a + 1]; m++) {
+                const int i = mem[m];
+                for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) add(L.agg[A.col[p]], L.T[i] * A.val[p] * L.T[A.col[p]]);
             }
-        }
-        std::sort(cols.begin(), cols.end());
-        for (int b : cols) { next.col.push_back(b); next.val.push_back(acc[b]); used[b] = 0; }
-        next.ptr[a + 1] = (int)next.col.size();
-    }
+        },
+        next.ptr, next.col, next.val);
 }
 
 inline bool spd_inverse_dense(std::vector<double>& A, int n) {
@@ -229,6 +219,7 @@ inline bool build_real_hierarchy(RCsr A0, std::vector<int> node, std::vector<int
         O.S.ptr = A.ptr;
         O.S.col = A.col;
         O.S.val.resize(A.val.size());
+#pragma omp parallel for schedule(static)
         for (int i = 0; i < n; i++)
             for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) {
                 int j = A.col[p];
@@ -237,24 +228,14 @@ inline bool build_real_hierarchy(RCsr A0, std::vector<int> node, std::vector<int
                 O.S.val[p] = omega * L.dinv[i] * v;
             }
         O.P.n = n;
-        O.P.ptr.assign(n + 1, 0);
-        O.P.col.clear();
-        O.P.val.clear();
-        std::vector<double> acc(na, 0.0);
-        std::vector<char> used(na, 0);
-        std::vector<int> cols;
-        for (int i = 0; i < n; i++) {
-            cols.clear();
-            auto add = [&](int b, double v) {
-                if (!used[b]) { used[b] = 1; cols.push_back(b); acc[b] = 0; }
-                acc[b] += v;
-            };
-            add(L.agg[i], alpha * L.T[i]);
-            for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) add(L.agg[A.col[p]], -alpha * omega * L.dinv[i] * A.val[p] * L.T[A.col[p]]);
-            std::sort(cols.begin(), cols.end());
-            for (int b : cols) { O.P.col.push_back(b); O.P.val.push_back(acc[b]); used[b] = 0; }
-            O.P.ptr[i + 1] = (int)O.P.col.size();
-        }
+        build_rows_parallel<double>(
+            n, na,
+            [&](int i, auto add) {
+                add(L.agg[i], alpha * L.T[i]);
+                for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++)
+                    add(L.agg[A.col[p]], -alpha * omega * L.dinv[i] * A.val[p] * L.T[A.col[p]]);
+            },
+            O.P.ptr, O.P.col, O.P.val);
         O.R.n = na;
         O.R.ptr.assign(na + 1, 0);
         for (int b : O.P.col) O.R.ptr[b + 1]++;

@@ -15,7 +15,9 @@
 //   d64[f], d32[f]        diagonal (#neighbours + 1e-9)     inv32/inv64: Jacobi inverse
 // Algorithmic bytes per SpMV row: FP32 3*(8+4) + 4 + 2*8 = 56 B, FP64 3*(16+4) + 8 + 2*16 = 100 B.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <vector>
 
@@ -619,6 +621,7 @@ struct FieldSolver {
     DBuf<unsigned char> hier_dev64, hier_dev32;   // device copies of the hierarchy descriptors
     bool amg = false;
     int amg_levels = 0, amg_coarse = 0;
+    double vcycle_bytes64 = 0, vcycle_bytes32 = 0;   // algorithmic bytes of one V-cycle
 
     int upload_csr(const HostCsr& M, CsrBufs& B, int group) {
         cudaStream_t st = c->stream;
@@ -642,6 +645,7 @@ struct FieldSolver {
         const double pi = 3.14159265358979323846;
         std::vector<int> nbr3(nbr_h, nbr_h + 3 * (size_t)n);
         std::vector<std::complex<double>> vals(3 * (size_t)n);
+#pragma omp parallel for schedule(static)
         for (int f = 0; f < n; f++)
             for (int j = 0; j < 3; j++) {
                 double ang = (double)N * (theta_h[3 * f + j] + pi);
@@ -682,6 +686,22 @@ struct FieldSolver {
         MTK_TRY(rc32.alloc(HH.nc)); MTK_TRY(yc32.alloc(HH.nc));
         H64.nlev = nl; H64.nc = HH.nc; H64.Ainv = Ainv64.p; H64.rc = rc64.p; H64.yc = yc64.p;
         H32.nlev = nl; H32.nc = HH.nc; H32.Ainv = Ainv32.p; H32.rc = rc32.p; H32.yc = yc32.p;
+        // V-cycle traffic: every matrix entry once (value + column), each level vector read/written
+        {
+            auto cyc = [&](double T) {
+                double b = 0;
+                for (int l = 0; l < nl; l++) {
+                    const HostCycleOps& O = HH.ops[l];
+                    const double nnz = (double)O.R.col.size() + O.S.col.size() + O.P.col.size();
+                    b += nnz * (2 * T + 4) + 4.0 * (O.R.n + 2.0 * O.S.n);                 // entries + row pointers
+                    b += 2 * T * (2.0 * O.S.n + 2.0 * O.R.n + O.S.n);                       // r_l twice, r/y_{l+1}, y_l
+                }
+                b += (double)HH.nc * HH.nc * 2 * T + 4.0 * HH.nc * T;
+                return b;
+            };
+            vcycle_bytes64 = cyc(8);
+            vcycle_bytes32 = cyc(4);
+        }
         MTK_TRY(hier_dev64.alloc(sizeof(DevHierarchy<double>)));
         MTK_TRY(hier_dev32.alloc(sizeof(DevHierarchy<float>)));
         amg = true;
@@ -732,10 +752,13 @@ struct FieldSolver {
         cudaEventElapsedTime(&kms, c->ev_k0, c->ev_k1);
         pcg_ms += kms;
         pcg_launches++;
-        // algorithmic bytes per iteration and row: SpMV 3*(2T+4) + T + 2*2T, x/r/p updates
-        // 3 * 3*2T, z = M^-1 r: T + 2T (the r read is shared with the r update)
-        const double per_row = 3.0 * (2 * sizeof(T) + 4) + sizeof(T) + 4.0 * sizeof(T) + 18.0 * sizeof(T) + 3.0 * sizeof(T);
-        pcg_bytes += per_row * (double)n * (double)(c->h_int[1] + 1);
+        // algorithmic bytes per iteration: SpMV 3*(2T+4) + T + 2*2T per row, x/r/p updates
+        // 3 * 3*2T, z = M^-1 r: T + 2T (Jacobi) -- or the V-cycle traffic (R, S, P matrices and
+        // level vectors, counted in build_amg) when the multigrid preconditioner is used
+        const double per_row = 3.0 * (2 * sizeof(T) + 4) + sizeof(T) + 4.0 * sizeof(T) + 18.0 * sizeof(T) +
+                               (amg ? 4.0 * sizeof(T) : 3.0 * sizeof(T));
+        const double cyc = amg ? (sizeof(T) == 8 ? vcycle_bytes64 : vcycle_bytes32) : 0.0;
+        pcg_bytes += (per_row * (double)n + cyc) * (double)(c->h_int[1] + 1);
         *iters += c->h_int[1];
         if (final_rr) *final_rr = reinterpret_cast<double*>(c->h_int + 4)[0];
         int st = c->h_int[0];
@@ -790,7 +813,15 @@ extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const 
                                          S.d32.p, S.inv64.p, S.inv32.p, S.area32.p);
     c->kernels++;
     MTK_CUDA_TRY(cudaGetLastError());
-    if (!getenv("MTK_NO_AMG")) MTK_TRY(S.build_amg(nbr_h, theta_h, nRosy));
+    {
+        auto th0 = std::chrono::steady_clock::now();
+        if (!getenv("MTK_NO_AMG")) MTK_TRY(S.build_amg(nbr_h, theta_h, nRosy));
+        const char* dbg = getenv("MTK_DEBUG");
+        if (dbg && dbg[0] == '1')
+            fprintf(stderr, "[field host] multigrid set-up %.1f ms (levels %d, coarse %d)\n",
+                    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - th0).count(), S.amg_levels,
+                    S.amg_coarse);
+    }
 
     long long iters = 0, solves = 0, refines = 0;
     double worst = 0.0;

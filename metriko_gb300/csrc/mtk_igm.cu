@@ -697,6 +697,7 @@ struct Igm {
     RDevHierarchy<float> RH32{};
     bool mg = false;
     int mg_levels = 0;
+    double mg_bytes64 = 0, mg_bytes32 = 0;   // algorithmic bytes of one V-cycle
     double cur_scale = 1.0;
     template <typename T> RDevHierarchy<T> rhier() const;
 
@@ -740,6 +741,19 @@ struct Igm {
         MTK_TRY(rrc32.alloc(HH.nc)); MTK_TRY(ryc32.alloc(HH.nc));
         RH64.nlev = nl; RH64.nc = HH.nc; RH64.Ainv = rAinv64.p; RH64.rc = rrc64.p; RH64.yc = ryc64.p;
         RH32.nlev = nl; RH32.nc = HH.nc; RH32.Ainv = rAinv32.p; RH32.rc = rrc32.p; RH32.yc = ryc32.p;
+        {
+            auto cyc = [&](double T) {
+                double b = 0;
+                for (int l = 0; l < nl; l++) {
+                    const RCycleOps& O = HH.ops[l];
+                    const double nnz = (double)O.R.col.size() + O.S.col.size() + O.P.col.size();
+                    b += nnz * (T + 4) + 4.0 * (O.R.n + 2.0 * O.S.n) + T * (3.0 * O.S.n + 2.0 * O.R.n);
+                }
+                return b + (double)HH.nc * HH.nc * T + 2.0 * HH.nc * T;
+            };
+            mg_bytes64 = cyc(8);
+            mg_bytes32 = cyc(4);
+        }
         MTK_TRY(rh_dev64.alloc(sizeof(RDevHierarchy<double>)));
         MTK_TRY(rh_dev32.alloc(sizeof(RDevHierarchy<float>)));
         mg = true;
@@ -805,7 +819,8 @@ struct Igm {
         cudaEventElapsedTime(&kms, c->ev_k0, c->ev_k1);
         pcg_ms += kms;
         pcg_launches++;
-        pcg_bytes += iter_bytes(sizeof(T)) * (double)(c->h_int[1] + 1);
+        pcg_bytes += (iter_bytes(sizeof(T)) + (Hp ? (sizeof(T) == 8 ? mg_bytes64 : mg_bytes32) : 0.0)) *
+                     (double)(c->h_int[1] + 1);
         if (iters) *iters += c->h_int[1];
         if (rr_out) *rr_out = reinterpret_cast<double*>(c->h_int + 4)[0];
         int s = c->h_int[0];
@@ -1108,64 +1123,50 @@ extern "C" int mtk_iterative_rounding(mtk_ctx* c, const mtk_igm_desc* d, const m
     MTK_CUDA_TRY(cudaStreamSynchronize(st));
     // ---- multigrid for the free block: K_pre = 2 W_y^T S W_y + delta I, delta = 1e-4 / length^2
     //      (the seamless system is length^2 K_pre exactly; the naive one up to the shift)
+    auto th0 = std::chrono::steady_clock::now();
     if (nY > 0 && !getenv("MTK_NO_AMG")) {
-        std::vector<int> hs_ptr(nCut + 1, 0), hs_col;
+        std::vector<int> hs_ptr, hs_col;
         std::vector<double> hs_val;
-        hs_col.reserve(8 * (size_t)nCut);
-        hs_val.reserve(8 * (size_t)nCut);
-        std::vector<std::pair<int, double>> rowbuf;
-        for (int c2 = 0; c2 < nCut; c2++) {
-            rowbuf.clear();
-            for (int k = vptr[c2]; k < vptr[c2 + 1]; k++) {
-                int f = vface[k];
-                int a = d->cutF[3 * f] == c2 ? 0 : (d->cutF[3 * f + 1] == c2 ? 1 : 2);
-                for (int j = 0; j < 3; j++) {
-                    double v = h_grad[6 * f + 2 * a] * h_grad[6 * f + 2 * j] + h_grad[6 * f + 2 * a + 1] * h_grad[6 * f + 2 * j + 1];
-                    int col = d->cutF[3 * f + j];
-                    bool found = false;
-                    for (auto& e : rowbuf) if (e.first == col) { e.second += v; found = true; break; }
-                    if (!found) rowbuf.emplace_back(col, v);
+        build_rows_parallel<double>(
+            nCut, nCut,
+            [&](int c2, auto add) {
+                for (int k = vptr[c2]; k < vptr[c2 + 1]; k++) {
+                    const int f = vface[k];
+                    const int a = d->cutF[3 * f] == c2 ? 0 : (d->cutF[3 * f + 1] == c2 ? 1 : 2);
+                    for (int j = 0; j < 3; j++)
+                        add(d->cutF[3 * f + j], h_grad[6 * f + 2 * a] * h_grad[6 * f + 2 * j] +
+                                                    h_grad[6 * f + 2 * a + 1] * h_grad[6 * f + 2 * j + 1]);
                 }
-            }
-            std::sort(rowbuf.begin(), rowbuf.end());
-            for (auto& e : rowbuf) { hs_col.push_back(e.first); hs_val.push_back(e.second); }
-            hs_ptr[c2 + 1] = (int)hs_col.size();
-        }
+            },
+            hs_ptr, hs_col, hs_val);
         const double delta = 1e-4 / (d->length * d->length);
         RCsr K;
         K.n = nY;
-        K.ptr.assign(nY + 1, 0);
-        K.col.reserve(16 * (size_t)nY);
-        K.val.reserve(16 * (size_t)nY);
-        std::vector<double> acc(nY, 0.0);
-        std::vector<char> used(nY, 0);
-        std::vector<int> cols;
-        for (int j = 0; j < nY; j++) {
-            cols.clear();
-            for (int e = yptr[j]; e < yptr[j + 1]; e++) {
-                const int r = yrow[e], c2 = r >> 1, kk = r & 1;
-                const double w1 = yval[e];
-                for (int p = hs_ptr[c2]; p < hs_ptr[c2 + 1]; p++) {
-                    const int r2 = 2 * hs_col[p] + kk;
-                    const double sv = hs_val[p];
-                    for (int e2 = d->w_ptr[r2]; e2 < d->w_ptr[r2 + 1]; e2++) {
-                        const int y2 = tag[e2];
-                        if (y2 < 0) continue;
-                        if (!used[y2]) { used[y2] = 1; cols.push_back(y2); acc[y2] = 0; }
-                        acc[y2] += 2.0 * w1 * sv * d->w_val[e2];
+        build_rows_parallel<double>(
+            nY, nY,
+            [&](int j, auto add) {
+                for (int e = yptr[j]; e < yptr[j + 1]; e++) {
+                    const int r = yrow[e], c2 = r >> 1, kk = r & 1;
+                    const double w1 = yval[e];
+                    for (int p = hs_ptr[c2]; p < hs_ptr[c2 + 1]; p++) {
+                        const int r2 = 2 * hs_col[p] + kk;
+                        const double sv = hs_val[p];
+                        for (int e2 = d->w_ptr[r2]; e2 < d->w_ptr[r2 + 1]; e2++) {
+                            const int y2 = tag[e2];
+                            if (y2 >= 0) add(y2, 2.0 * w1 * sv * d->w_val[e2]);
+                        }
                     }
                 }
-            }
-            if (!used[j]) { used[j] = 1; cols.push_back(j); acc[j] = 0; }
-            acc[j] += delta;
-            std::sort(cols.begin(), cols.end());
-            for (int y2 : cols) { K.col.push_back(y2); K.val.push_back(acc[y2]); used[y2] = 0; }
-            K.ptr[j + 1] = (int)K.col.size();
-        }
+                add(j, delta);
+            },
+            K.ptr, K.col, K.val);
         std::vector<int> node(nY), comp(nY);
         for (int j = 0; j < nY; j++) { node[j] = y2full[j] / 2; comp[j] = y2full[j] % 2; }
         MTK_TRY(S.build_mg(std::move(K), std::move(node), std::move(comp), nFull / 2));
     }
+    if (Igm::debug())
+        fprintf(stderr, "[igm host] multigrid set-up %.1f ms (levels %d)\n",
+                std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - th0).count(), S.mg_levels);
     std::vector<double> BJJ((size_t)nJ * nJ, 0.0);
     if (nJ > 0) {
         std::vector<char> touchJ(nCut, 0);

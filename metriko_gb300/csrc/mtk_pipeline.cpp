@@ -2,6 +2,8 @@
 // (include/metriko/...), with host buffers in and out.  Topology stages run on the host, the
 // field and the integration / rounding solves on the GPU.
 #include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 #include "metriko/core/igm/parameterization.h"
@@ -20,6 +22,13 @@ extern "C" int mtk_pipeline_run(mtk_ctx* ctx, int32_t nV, int32_t nF, const doub
     if (!ctx || nV <= 0 || nF <= 0 || !Vb || !Fb || !popts) return MTK_ERR_BAD_INPUT;
     using clk = std::chrono::steady_clock;
     auto t0 = clk::now();
+    const bool dbg = getenv("MTK_DEBUG") && getenv("MTK_DEBUG")[0] == '1';
+    auto stamp = [&](const char* what, clk::time_point& a) {
+        auto b = clk::now();
+        if (dbg) fprintf(stderr, "[host] %-22s %8.1f ms\n", what, std::chrono::duration<double, std::milli>(b - a).count());
+        a = b;
+    };
+    auto ts2 = clk::now();
     double host_ms = 0;
     auto lap = [&](clk::time_point& a) {
         auto b = clk::now();
@@ -41,9 +50,12 @@ extern "C" int mtk_pipeline_run(mtk_ctx* ctx, int32_t nV, int32_t nF, const doub
         std::memcpy(F.data(), Fb, sizeof(int32_t) * 3 * size_t(nF));
         auto mesh = std::make_unique<Hmesh>(V, F);
         lap(ts);
+        stamp("hmesh", ts2);
         FaceRosyField rawf(*mesh, 4, FieldType::Smoothest);
+        stamp("field (gpu)", ts2);
         ts = clk::now();
         rawf.computeMatching(MatchingType::Curl);
+        stamp("matching+singular", ts2);
         if (compressed)
             for (int f = 0; f < nF; f++) { compressed[2 * f] = rawf.compressed[f].real(); compressed[2 * f + 1] = rawf.compressed[f].imag(); }
         if (singular) std::memcpy(singular, rawf.singular.data(), sizeof(int32_t) * nV);
@@ -55,15 +67,20 @@ extern "C" int mtk_pipeline_run(mtk_ctx* ctx, int32_t nV, int32_t nF, const doub
             return MTK_OK;
         }
         auto seam = compute_seam(rawf);
+        stamp("seam", ts2);
         auto cutm = compute_cut_mesh(*mesh, seam);
+        stamp("cut mesh", ts2);
         auto cmbf = compute_combbed_field(rawf, seam);
         MatXd extf = compute_extrinsic_field(*mesh, *cmbf, 4);
+        stamp("combing+extrinsic", ts2);
         RosyParameterization rp(*mesh, *cutm, extf, cmbf->singular, cmbf->matching, seam, 4, popts->ratio);
         rp.seamless = popts->seamless != 0;
         rp.localInjectivity = false;
         rp.roundSeams = popts->round_seams != 0;
         rp.verbose = false;
+        stamp("transitions", ts2);
         rp.setup();
+        stamp("setup", ts2);
         lap(ts);
         if (matching) std::memcpy(matching, cmbf->matching.data(), sizeof(int32_t) * mesh->nE);
         if (seam_out) for (int e = 0; e < mesh->nE; e++) seam_out[e] = seam[e] ? 1 : 0;
@@ -77,6 +94,7 @@ extern "C" int mtk_pipeline_run(mtk_ctx* ctx, int32_t nV, int32_t nF, const doub
             return MTK_OK;
         }
         bool ok = rp.integ();
+        stamp("integ (host+gpu)", ts2);
         const int nFull = rp.fullx.size();
         if (counts) { counts[5] = rp.nJ; counts[6] = rp.nZ; counts[7] = nFull; }
         if (n_full) *n_full = nFull;
