@@ -349,7 +349,7 @@ template <typename T>
 struct DevCsr {
     using V2 = typename Cv<T>::V2;
     int n;           // rows
-    int group;       // threads per row (1 or 32)
+    int group;       // lanes per row (power of two, 1..32)
     const int* ptr;
     const int* col;
     const V2* val;

@@ -287,27 +287,32 @@ __device__ __forceinline__ T rcsr_row(const RDevCsr<T>& M, int row, int lane, in
     return s;
 }
 
-// out[row] = scale * (M x + M2 x2); mask (may be null) zeroes rows where mask != 0
+// out[row] = scale * (M x + M2 x2); mask (may be null) zeroes rows where mask != 0.  Rows are
+// spread over groups of M.group lanes (1..32) with a warp-uniform loop and fixed-order reduction.
 template <typename T>
 __device__ void rcsr_phase(const RDevCsr<T>& M, const T* x, const RDevCsr<T>* M2, const T* x2, T* out, T scale,
                            const unsigned char* mask) {
     const int stride = gridDim.x * blockDim.x;
     const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
-    if (M.group == 1) {
+    const int g = M.group;
+    if (g == 1) {
         for (int row = t0; row < M.n; row += stride) {
             T s = rcsr_row(M, row, 0, 1, x);
             if (M2) s += rcsr_row(*M2, row, 0, 1, x2);
             out[row] = (mask && mask[row]) ? T(0) : scale * s;
         }
-    } else {
-        const int lane = threadIdx.x & 31;
-        for (int row = t0 >> 5; row < M.n; row += stride >> 5) {
-            T s = rcsr_row(M, row, lane, 32, x);
-            if (M2) s += rcsr_row(*M2, row, lane, 32, x2);
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-            if (lane == 0) out[row] = (mask && mask[row]) ? T(0) : scale * s;
+        return;
+    }
+    const int lane = threadIdx.x & 31, gpw = 32 / g, sub = lane / g, sl = lane % g;
+    for (int rbase = (t0 >> 5) * gpw; rbase < M.n; rbase += (stride >> 5) * gpw) {   // warp-uniform
+        const int row = rbase + sub;
+        T s = T(0);
+        if (row < M.n) {
+            s = rcsr_row(M, row, sl, g, x);
+            if (M2) s += rcsr_row(*M2, row, sl, g, x2);
         }
+        for (int o = g >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (sl == 0 && row < M.n) out[row] = (mask && mask[row]) ? T(0) : scale * s;
     }
 }
 

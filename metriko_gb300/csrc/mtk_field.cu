@@ -192,8 +192,8 @@ done:
 }
 
 // ---------------------------------------------------------------------------- multigrid PCG
-// One CSR phase over all rows: out[row] = M x (+ M2 x2), rows spread thread-per-row (group 1)
-// or warp-per-row (group 32, fixed-order warp reduction) across the whole grid.
+// One CSR phase over all rows: out[row] = M x (+ M2 x2), each row on a group of M.group lanes
+// (1, 2, ..., 32; lanes stride the row, then a fixed-order butterfly reduction) across the grid.
 template <typename T>
 __device__ __forceinline__ void csr_row_acc(const DevCsr<T>& M, int row, int lane, int g,
                                             const typename V2of<T>::type* __restrict__ x, T& re, T& im) {
@@ -210,7 +210,8 @@ __device__ void csr_phase(const DevCsr<T>& M, const typename V2of<T>::type* x, c
     using V2 = typename V2of<T>::type;
     const int stride = gridDim.x * blockDim.x;
     const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
-    if (M.group == 1) {
+    const int g = M.group;   // lanes per row: 1, 2, 4, 8, 16 or 32
+    if (g == 1) {
         for (int row = t0; row < M.n; row += stride) {
             T re = T(0), im = T(0);
             csr_row_acc(M, row, 0, 1, x, re, im);
@@ -220,29 +221,32 @@ __device__ void csr_phase(const DevCsr<T>& M, const typename V2of<T>::type* x, c
             o.y = im;
             out[row] = o;
         }
-    } else {
-        const int lane = threadIdx.x & 31;
-        for (int row = t0 >> 5; row < M.n; row += stride >> 5) {
-            T re = T(0), im = T(0);
-            csr_row_acc(M, row, lane, 32, x, re, im);
-            if (M2) csr_row_acc(*M2, row, lane, 32, x2, re, im);
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                re += __shfl_xor_sync(0xffffffffu, re, o);
-                im += __shfl_xor_sync(0xffffffffu, im, o);
-            }
-            if (lane == 0) {
-                V2 v;
-                v.x = re;
-                v.y = im;
-                out[row] = v;
-            }
+        return;
+    }
+    const int lane = threadIdx.x & 31, gpw = 32 / g, sub = lane / g, sl = lane % g;
+    for (int rbase = (t0 >> 5) * gpw; rbase < M.n; rbase += (stride >> 5) * gpw) {   // warp-uniform
+        const int row = rbase + sub;
+        T re = T(0), im = T(0);
+        if (row < M.n) {
+            csr_row_acc(M, row, sl, g, x, re, im);
+            if (M2) csr_row_acc(*M2, row, sl, g, x2, re, im);
+        }
+        for (int o = g >> 1; o > 0; o >>= 1) {
+            re += __shfl_xor_sync(0xffffffffu, re, o);
+            im += __shfl_xor_sync(0xffffffffu, im, o);
+        }
+        if (sl == 0 && row < M.n) {
+            V2 v;
+            v.x = re;
+            v.y = im;
+            out[row] = v;
         }
     }
 }
 
 // V(1,1) cycle z = B r: down r_{l+1} = R r_l; coarse y = A_c^-1 r_c (dense, warp per row);
-// up y_l = S r_l + P y_{l+1}.  2 * nlev grid barriers.
+// up y_l = S r_l + P y_{l+1}.  2 * nlev grid barriers; the level-0 up phase (one lane per row)
+// leaves each z[i] to the thread that owns row i in the PCG loops, so it needs no barrier.
 template <typename T>
 __device__ bool vcycle(const ComplexEll<T>& A0, const DevHierarchy<T>& H, const GridBarrier& bar) {
     using V2 = typename V2of<T>::type;
@@ -656,11 +660,19 @@ struct FieldSolver {
         const int nl = (int)HH.lv.size();
         if (nl == 0) return MTK_OK;
         cudaStream_t st = c->stream;
-        auto grp = [](const HostCsr& M) { return M.n > 0 && (double)M.col.size() / M.n > 8.0 ? 32 : 1; };
+        // lanes per row: about two entries per lane (power of two, 1..32)
+        auto grp = [](const HostCsr& M) {
+            double avg = M.n > 0 ? (double)M.col.size() / M.n : 0.0;
+            int g = 1;
+            while (g < 32 && 2.0 * g < avg) g <<= 1;
+            return g;
+        };
         for (int l = 0; l < nl; l++) {
             const HostCycleOps& O = HH.ops[l];
             LevelBufs& B = lvb[l];
-            const int up_group = (grp(O.S) == 32 || grp(O.P) == 32) ? 32 : 1;
+            // level 0's up phase writes z with the thread-per-row mapping of the PCG vector loops,
+            // which read it with no grid barrier in between: keep it at one lane per row
+            const int up_group = l == 0 ? 1 : std::max(grp(O.S), grp(O.P));
             MTK_TRY(upload_csr(O.R, B.R, grp(O.R)));
             MTK_TRY(upload_csr(O.S, B.S, up_group));
             MTK_TRY(upload_csr(O.P, B.P, up_group));

@@ -648,17 +648,6 @@ __global__ void add_z_projected(int nY, int nZ, int kq, const double* __restrict
         x[nY + j] += v;
     }
 }
-__global__ void dot_partial(int n, const double* __restrict__ a, const double* __restrict__ b, double* partials) {
-    double v[1] = {0};
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[0] += a[i] * b[i];
-    publish_partials<double, 1>(v, partials);
-}
-__global__ void finalize1(const double* partials, int nb, double* out) {
-    double v[1] = {0};
-    for (int i = threadIdx.x; i < nb; i += blockDim.x) v[0] += partials[i];
-    block_sum<double, 1>(v);
-    if (threadIdx.x == 0) out[0] = v[0];
-}
 
 }  // namespace mtk
 
@@ -717,11 +706,18 @@ struct Igm {
         if (!build_real_hierarchy(std::move(K), std::move(node), std::move(comp), nnode, HH)) return MTK_OK;
         const int nl = (int)HH.lv.size();
         if (nl == 0) return MTK_OK;
-        auto grp = [](const RCsr& M) { return M.n > 0 && (double)M.col.size() / M.n > 8.0 ? 32 : 1; };
+        auto grp = [](const RCsr& M) {   // lanes per row: about two entries per lane
+            double avg = M.n > 0 ? (double)M.col.size() / M.n : 0.0;
+            int g = 1;
+            while (g < 32 && 2.0 * g < avg) g <<= 1;
+            return g;
+        };
         for (int l = 0; l < nl; l++) {
             const RCycleOps& O = HH.ops[l];
             RLevelBufs& B = rlv[l];
-            const int up = (grp(O.S) == 32 || grp(O.P) == 32) ? 32 : 1;
+            // level 0's up phase writes z with the thread-per-row mapping of the PCG vector loops,
+            // which read it with no grid barrier in between: keep it at one lane per row
+            const int up = l == 0 ? 1 : std::max(grp(O.S), grp(O.P));
             MTK_TRY(upload_rcsr(O.R, B.R, grp(O.R)));
             MTK_TRY(upload_rcsr(O.S, B.S, up));
             MTK_TRY(upload_rcsr(O.P, B.P, up));
@@ -853,17 +849,6 @@ struct Igm {
         rhs_reduce_z<<<1, kStream, 0, st>>>(nY, nZ, nJ, Us.p, XbJ.p, scale, shift, prevx, b);
         c->kernels += 3;
         MTK_CUDA_TRY(cudaGetLastError());
-        return MTK_OK;
-    }
-
-    int dot(const double* a, const double* b, int n, double* out) {
-        int G = grid();
-        dot_partial<<<G, kStream, 0, st>>>(n, a, b, c->partials);
-        finalize1<<<1, kStream, 0, st>>>(c->partials, G, c->scalars);
-        c->kernels += 2;
-        MTK_CUDA_TRY(cudaMemcpyAsync(c->h_scalars, c->scalars, sizeof(double), cudaMemcpyDeviceToHost, st));
-        MTK_CUDA_TRY(cudaStreamSynchronize(st));
-        *out = c->h_scalars[0];
         return MTK_OK;
     }
 
