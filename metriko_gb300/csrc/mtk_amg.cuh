@@ -84,6 +84,8 @@ void build_rows_parallel(int nrows, int ncols, RowFn fn, std::vector<int>& ptr, 
 
 constexpr int kMaxLevels = 8;
 constexpr int kCoarseMax = 384;
+constexpr double kOmega = 0.8;   // Jacobi weight of the pre- and post-smoothing
+constexpr double kAlpha = 1.8;   // coarse-correction scale
 
 // ------------------------------------------------------------------ host hierarchy
 struct HostCsr {
@@ -252,9 +254,11 @@ inline bool hpd_inverse(std::vector<std::complex<double>>& A, int n) {
     return true;
 }
 
-// Builds the hierarchy from the level-0 ELL rows (nbr[3*f+j], val[j*n+f], diag d).
+// Builds the hierarchy from the level-0 ELL rows (nbr[3*f+j], val[j*n+f], diag d).  The cycle
+// operators R, S, P are formed for levels >= first_ops (the device applies level 0 directly from
+// the ELL rows, the aggregates and T).
 inline bool build_hierarchy(int n, const std::vector<int>& nbr3, const std::vector<std::complex<double>>& vals,
-                            double diag, HostHierarchy& H) {
+                            double diag, HostHierarchy& H, int first_ops = 0) {
     H.lv.clear();
     HostCsr A0;
     A0.n = n;
@@ -285,9 +289,9 @@ inline bool build_hierarchy(int n, const std::vector<int>& nbr3, const std::vect
     H.nc = cur.n;
     // cycle operators
     using cd = std::complex<double>;
-    const double omega = 0.8, alpha = 1.8;
+    const double omega = kOmega, alpha = kAlpha;
     H.ops.resize(H.lv.size());
-    for (size_t l = 0; l < H.lv.size(); l++) {
+    for (size_t l = (size_t)std::max(first_ops, 0); l < H.lv.size(); l++) {
         const HostLevel& L = H.lv[l];
         const HostCsr& A = L.A;
         const int n = A.n;
@@ -372,6 +376,20 @@ struct DevHierarchy {
     const V2* Ainv;              // nc x nc dense
     V2* rc;                      // coarsest right-hand side
     V2* yc;                      // coarsest solution
+};
+
+// Level 0 applied from the ELL rows of the operator: rows are numbered by aggregate (aggregate a
+// owns rows cptr[a] .. cptr[a+1]-1), and chunk w of at most 32 rows, chunk[w] .. chunk[w+1]-1,
+// holds whole aggregates, so one warp forms the restriction of a chunk with a segmented sum.
+template <typename T>
+struct DevLevel0 {
+    using V2 = typename Cv<T>::V2;
+    int nagg, nchunk;
+    const int* agg;      // aggregate (level-1 row) of each row
+    const V2* t;         // T(k, agg k): transported near-null coefficient / sqrt|aggregate|
+    const int* chunk;    // chunk starts, nchunk + 1 entries
+    T dinv;              // 1 / diagonal (every row of a closed mesh has three neighbours)
+    T omega, alpha;
 };
 
 template <typename V2> __device__ __forceinline__ V2 cmulv(V2 a, V2 b) {

@@ -192,25 +192,56 @@ done:
 }
 
 // ---------------------------------------------------------------------------- multigrid PCG
-// One CSR phase over all rows: out[row] = M x (+ M2 x2), each row on a group of M.group lanes
-// (1, 2, ..., 32; lanes stride the row, then a fixed-order butterfly reduction) across the grid.
+// Levels >= 1 are CSR cycle operators (csr_phase); level 0 is applied straight from the ELL rows
+// of A, the aggregates and T (DevLevel0), fused with the CG vector updates.
+
+template <typename T> __device__ __forceinline__ T fmaT(T a, T b, T c);
+template <> __device__ __forceinline__ float fmaT<float>(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+template <> __device__ __forceinline__ double fmaT<double>(double a, double b, double c) { return __fma_rn(a, b, c); }
+// a x + y for a real scalar a, one rounding per component (owners and neighbours that recompute
+// the same value get the same bits)
+template <typename V2, typename T> __device__ __forceinline__ V2 axpy2(T a, V2 x, V2 y) {
+    V2 o;
+    o.x = fmaT<T>(a, x.x, y.x);
+    o.y = fmaT<T>(a, x.y, y.y);
+    return o;
+}
+
+// Accumulates row `row` of M x over the entries lane, lane + g, ... with four loads in flight.
 template <typename T>
 __device__ __forceinline__ void csr_row_acc(const DevCsr<T>& M, int row, int lane, int g,
                                             const typename V2of<T>::type* __restrict__ x, T& re, T& im) {
-    for (int p = M.ptr[row] + lane; p < M.ptr[row + 1]; p += g) {
-        const typename V2of<T>::type v = M.val[p], xv = __ldcg(x + M.col[p]);
-        re += v.x * xv.x - v.y * xv.y;
-        im += v.x * xv.y + v.y * xv.x;
+    using V2 = typename V2of<T>::type;
+    const int e = __ldg(M.ptr + row + 1);
+    for (int p = __ldg(M.ptr + row) + lane; p < e; p += 4 * g) {
+        int c[4];
+        V2 v[4], xv[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int pu = p + u * g;
+            c[u] = pu < e ? __ldg(M.col + pu) : -1;
+            v[u] = pu < e ? __ldg(M.val + pu) : V2{};
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) xv[u] = c[u] >= 0 ? __ldcg(x + c[u]) : V2{};
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            if (c[u] >= 0) {
+                re += v[u].x * xv[u].x - v[u].y * xv[u].y;
+                im += v[u].x * xv[u].y + v[u].y * xv[u].x;
+            }
     }
 }
 
+// One CSR phase over all rows: out[row] = M x (+ M2 x2), each row on a group of M.group lanes
+// (1, 2, ..., 32; lanes stride the row, then a fixed-order butterfly reduction) across the grid.
 template <typename T>
 __device__ void csr_phase(const DevCsr<T>& M, const typename V2of<T>::type* x, const DevCsr<T>* M2,
                           const typename V2of<T>::type* x2, typename V2of<T>::type* out) {
     using V2 = typename V2of<T>::type;
     const int stride = gridDim.x * blockDim.x;
     const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
-    const int g = M.group;   // lanes per row: 1, 2, 4, 8, 16 or 32
+    const int g = M.group;
     if (g == 1) {
         for (int row = t0; row < M.n; row += stride) {
             T re = T(0), im = T(0);
@@ -244,13 +275,12 @@ __device__ void csr_phase(const DevCsr<T>& M, const typename V2of<T>::type* x, c
     }
 }
 
-// V(1,1) cycle z = B r: down r_{l+1} = R r_l; coarse y = A_c^-1 r_c (dense, warp per row);
-// up y_l = S r_l + P y_{l+1}.  2 * nlev grid barriers; the level-0 up phase (one lane per row)
-// leaves each z[i] to the thread that owns row i in the PCG loops, so it needs no barrier.
+// Inner V-cycle over the CSR levels (the first of them is level 1): down r_{l+1} = R r_l,
+// coarsest y = A_c^-1 r_c (dense, warp per row), up y_l = S r_l + P y_{l+1}; a grid barrier
+// after every phase (2 nlev + 1).
 template <typename T>
-__device__ bool vcycle(const ComplexEll<T>& A0, const DevHierarchy<T>& H, const GridBarrier& bar) {
+__device__ bool vcycle_inner(const DevHierarchy<T>& H, const GridBarrier& bar) {
     using V2 = typename V2of<T>::type;
-    (void)A0;
     const int stride = gridDim.x * blockDim.x;
     const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
     for (int l = 0; l < H.nlev; l++) {
@@ -285,21 +315,190 @@ __device__ bool vcycle(const ComplexEll<T>& A0, const DevHierarchy<T>& H, const 
     for (int l = H.nlev - 1; l >= 0; l--) {
         const V2* yn = (l + 1 < H.nlev) ? H.L[l + 1].y : H.yc;
         csr_phase<T>(H.L[l].S, H.L[l].r, &H.L[l].P, yn, H.L[l].y);
-        if (l > 0 && !grid_sync(bar)) return false;
+        if (!grid_sync(bar)) return false;
     }
     return true;
 }
 
-// PCG with the V-cycle preconditioner (same structure and status codes as pcg_complex).
+// Level-0 phase A: p = z + beta p_old (own row, and recomputed for the three neighbours), q = A p
+// with the uniform diagonal dg; writes p to pn and q; returns the partial Re p^H q.
 template <typename T>
-__global__ void __launch_bounds__(kBlock, 1) pcg_complex_mg(ComplexEll<T> A, const DevHierarchy<T>* __restrict__ Hp,
+__device__ __forceinline__ T l0_direction_spmv(const ComplexEll<T>& A, T dg, const typename V2of<T>::type* z,
+                                               const typename V2of<T>::type* po, T beta,
+                                               typename V2of<T>::type* __restrict__ pn,
+                                               typename V2of<T>::type* __restrict__ q) {
+    using V2 = typename V2of<T>::type;
+    const int n = A.n, stride = gridDim.x * blockDim.x;
+    T pq = T(0);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+        int c[3];
+        V2 a[3], zc[3], pc[3];
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            c[j] = __ldg(A.nbr + j * n + k);
+            a[j] = __ldg(A.val + j * n + k);
+        }
+        const V2 zk = __ldcg(z + k), pk = __ldcg(po + k);
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            zc[j] = __ldcg(z + c[j]);
+            pc[j] = __ldcg(po + c[j]);
+        }
+        const V2 pown = axpy2(beta, pk, zk);
+        T re = dg * pown.x, im = dg * pown.y;
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            const V2 pj = axpy2(beta, pc[j], zc[j]);
+            re += a[j].x * pj.x - a[j].y * pj.y;
+            im += a[j].x * pj.y + a[j].y * pj.x;
+        }
+        V2 qk;
+        qk.x = re;
+        qk.y = im;
+        pn[k] = pown;
+        q[k] = qk;
+        pq += pown.x * re + pown.y * im;
+    }
+    return pq;
+}
+
+// Level-0 phase B: r' = r - alpha q (own row and neighbours), and when `update` x += alpha p and
+// rn = r'.  Restriction r1[a] = sum over rows k of aggregate a of conj(T_k) (r'_k - omega/d
+// sum_j A_kj r'_j) (A_kk = d): one warp per chunk, inclusive segmented scan over the lanes of
+// each aggregate (fixed order), the last lane of an aggregate writes it.
+template <typename T>
+__device__ __forceinline__ void l0_update_restrict(const ComplexEll<T>& A, const DevLevel0<T>& L0,
+                                                   const typename V2of<T>::type* r, const typename V2of<T>::type* q,
+                                                   T alpha, const typename V2of<T>::type* p,
+                                                   typename V2of<T>::type* x, typename V2of<T>::type* rn,
+                                                   typename V2of<T>::type* r1, bool update) {
+    using V2 = typename V2of<T>::type;
+    const int n = A.n;
+    const int lane = threadIdx.x & 31;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const T od = L0.omega * L0.dinv, keep = T(1) - L0.omega;
+    for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < L0.nchunk; w += nwarps) {
+        const int beg = __ldg(L0.chunk + w), end = __ldg(L0.chunk + w + 1);
+        const bool act = beg + lane < end;
+        const int k = act ? beg + lane : beg;   // inactive lanes read a valid row, store nothing
+        int c[3];
+        V2 a[3], rc[3];
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            c[j] = __ldg(A.nbr + j * n + k);
+            a[j] = __ldg(A.val + j * n + k);
+        }
+        const int ag = act ? __ldg(L0.agg + k) : -1;
+        const V2 tk = __ldg(L0.t + k);
+        V2 rk = __ldcg(r + k);
+#pragma unroll
+        for (int j = 0; j < 3; j++) rc[j] = __ldcg(r + c[j]);
+        if (update) {
+            V2 qc[3];
+            const V2 qk = __ldcg(q + k);
+#pragma unroll
+            for (int j = 0; j < 3; j++) qc[j] = __ldcg(q + c[j]);
+            rk = axpy2(-alpha, qk, rk);
+#pragma unroll
+            for (int j = 0; j < 3; j++) rc[j] = axpy2(-alpha, qc[j], rc[j]);
+            if (act) {
+                const V2 pk = __ldcg(p + k), xk = __ldcg(x + k);
+                x[k] = axpy2(alpha, pk, xk);
+                rn[k] = rk;
+            }
+        }
+        T sr = keep * rk.x, si = keep * rk.y;
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            sr -= od * (a[j].x * rc[j].x - a[j].y * rc[j].y);
+            si -= od * (a[j].x * rc[j].y + a[j].y * rc[j].x);
+        }
+        T vx = act ? tk.x * sr + tk.y * si : T(0);   // conj(T_k) * s
+        T vy = act ? tk.x * si - tk.y * sr : T(0);
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const T ux = __shfl_up_sync(0xffffffffu, vx, o), uy = __shfl_up_sync(0xffffffffu, vy, o);
+            const int ua = __shfl_up_sync(0xffffffffu, ag, o);
+            if (lane >= o && ua == ag) {
+                vx += ux;
+                vy += uy;
+            }
+        }
+        const int next = __shfl_down_sync(0xffffffffu, ag, 1);
+        if (act && (lane == 31 || next != ag)) {
+            V2 v;
+            v.x = vx;
+            v.y = vy;
+            r1[ag] = v;
+        }
+    }
+}
+
+// Level-0 up phase: z = S r + P y1, i.e. z_k = omega/d (2 r_k - sum_j A_kj w_j) + alpha T_k y1[agg k]
+// with w_j = omega/d r_j + alpha T_j y1[agg j] over j = k and its neighbours (A_kk = d).
+// Adds the partials Re r^H z and |r|^2.
+template <typename T>
+__device__ __forceinline__ void l0_smooth_prolong(const ComplexEll<T>& A, const DevLevel0<T>& L0, T dg,
+                                                  const typename V2of<T>::type* r, const typename V2of<T>::type* y1,
+                                                  typename V2of<T>::type* __restrict__ z, T& rz, T& rr) {
+    using V2 = typename V2of<T>::type;
+    const int n = A.n, stride = gridDim.x * blockDim.x;
+    const T od = L0.omega * L0.dinv, al = L0.alpha;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+        int c[3], ac[3];
+        V2 a[3], tc[3], rc[3], yc[3];
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            c[j] = __ldg(A.nbr + j * n + k);
+            a[j] = __ldg(A.val + j * n + k);
+        }
+        const int ak = __ldg(L0.agg + k);
+        const V2 tk = __ldg(L0.t + k), rk = __ldcg(r + k);
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            ac[j] = __ldg(L0.agg + c[j]);
+            tc[j] = __ldg(L0.t + c[j]);
+            rc[j] = __ldcg(r + c[j]);
+        }
+        const V2 yk = __ldcg(y1 + ak);
+#pragma unroll
+        for (int j = 0; j < 3; j++) yc[j] = __ldcg(y1 + ac[j]);
+        const T tyx = tk.x * yk.x - tk.y * yk.y, tyy = tk.x * yk.y + tk.y * yk.x;
+        T sx = T(2) * rk.x - dg * (od * rk.x + al * tyx);
+        T sy = T(2) * rk.y - dg * (od * rk.y + al * tyy);
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            const T wx = od * rc[j].x + al * (tc[j].x * yc[j].x - tc[j].y * yc[j].y);
+            const T wy = od * rc[j].y + al * (tc[j].x * yc[j].y + tc[j].y * yc[j].x);
+            sx -= a[j].x * wx - a[j].y * wy;
+            sy -= a[j].x * wy + a[j].y * wx;
+        }
+        V2 zk;
+        zk.x = od * sx + al * tyx;
+        zk.y = od * sy + al * tyy;
+        z[k] = zk;
+        rz += rk.x * zk.x + rk.y * zk.y;
+        rr += rk.x * rk.x + rk.y * rk.y;
+    }
+}
+
+// PCG with the V-cycle preconditioner (status codes as pcg_complex).  Per iteration: phase A
+// (direction + SpMV), phase B (residual, solution, restriction), the inner cycle, the level-0 up
+// phase (z and the r^H z, |r|^2 partials): 2 nlev_inner + 4 grid barriers.  Residual and
+// direction are double-buffered (r0/r1, p0/p1) because neighbours recompute them.
+template <typename T>
+__global__ void __launch_bounds__(kBlock, 1) pcg_complex_mg(ComplexEll<T> A, DevLevel0<T> L0, T dg,
+                                                        const DevHierarchy<T>* __restrict__ Hp,
                                                         const typename V2of<T>::type* __restrict__ b,
-                                                        typename V2of<T>::type* x, typename V2of<T>::type* r,
-                                                        typename V2of<T>::type* z, typename V2of<T>::type* p,
+                                                        typename V2of<T>::type* x, typename V2of<T>::type* r0,
+                                                        typename V2of<T>::type* r1, typename V2of<T>::type* z,
+                                                        typename V2of<T>::type* p0, typename V2of<T>::type* p1,
                                                         typename V2of<T>::type* q, T* partials, GridBarrier bar,
                                                         double tol2, int maxit, int* out) {
     using V2 = typename V2of<T>::type;
     const DevHierarchy<T>& H = *Hp;
+    V2* rl1 = H.nlev > 0 ? H.L[0].r : H.rc;
+    const V2* yl1 = H.nlev > 0 ? H.L[0].y : H.yc;
     const int n = A.n;
     const int stride = gridDim.x * blockDim.x;
     const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
@@ -307,80 +506,64 @@ __global__ void __launch_bounds__(kBlock, 1) pcg_complex_mg(ComplexEll<T> A, con
     T red1[1];
     int status = 3, it = 0;
     T rr = T(0);
+    V2* rcur = r0;
+    V2* rnext = r1;
     for (int i = t0; i < n; i += stride) {
         V2 ax = A.row(i, x);
         V2 bi = b[i];
         V2 ri;
         ri.x = bi.x - ax.x;
         ri.y = bi.y - ax.y;
-        r[i] = ri;
+        rcur[i] = ri;
     }
     if (!grid_sync(bar)) { status = 5; goto done; }
-    if (!vcycle(A, H, bar)) { status = 5; goto done; }
+    l0_update_restrict<T>(A, L0, rcur, nullptr, T(0), nullptr, nullptr, nullptr, rl1, false);
+    if (!grid_sync(bar)) { status = 5; goto done; }
+    if (!vcycle_inner(H, bar)) { status = 5; goto done; }
     red2[0] = T(0);
     red2[1] = T(0);
-    for (int i = t0; i < n; i += stride) {
-        V2 ri = r[i], zi = z[i];
-        p[i] = zi;
-        red2[0] += ri.x * zi.x + ri.y * zi.y;
-        red2[1] += ri.x * ri.x + ri.y * ri.y;
-    }
+    l0_smooth_prolong<T>(A, L0, dg, rcur, yl1, z, red2[0], red2[1]);
     publish_partials<T, 2>(red2, partials);
     if (!grid_sync(bar)) { status = 5; goto done; }
     gather_partials<T, 2>(partials, red2);
     {
         T rz = red2[0];
         rr = red2[1];
+        T beta = T(0);
+        const V2* pold = z;   // first direction p = z
+        V2* pw = p0;
         for (;;) {
             if ((double)rr <= tol2) { status = 0; break; }
             if (it >= maxit) { status = 3; break; }
-            red1[0] = T(0);
-            for (int i = t0; i < n; i += stride) {
-                V2 qi = A.row(i, p);
-                q[i] = qi;
-                V2 pi = p[i];
-                red1[0] += pi.x * qi.x + pi.y * qi.y;
-            }
+            red1[0] = l0_direction_spmv<T>(A, dg, z, pold, beta, pw, q);
             publish_partials<T, 1>(red1, partials + 2 * gridDim.x);
             if (!grid_sync(bar)) { status = 5; break; }
             gather_partials<T, 1>(partials + 2 * gridDim.x, red1);
-            T pq = red1[0];
+            const T pq = red1[0];
             if (!(pq > T(0))) { status = 4; break; }
-            T alpha = rz / pq;
-            for (int i = t0; i < n; i += stride) {
-                V2 pi = p[i], qi = q[i], xi = x[i], ri = r[i];
-                xi.x += alpha * pi.x;
-                xi.y += alpha * pi.y;
-                ri.x -= alpha * qi.x;
-                ri.y -= alpha * qi.y;
-                x[i] = xi;
-                r[i] = ri;
-            }
+            const T alpha = rz / pq;
+            l0_update_restrict<T>(A, L0, rcur, q, alpha, pw, x, rnext, rl1, true);
             if (!grid_sync(bar)) { status = 5; break; }
-            if (!vcycle(A, H, bar)) { status = 5; break; }
+            {
+                V2* tmp = rcur;
+                rcur = rnext;
+                rnext = tmp;
+            }
+            if (!vcycle_inner(H, bar)) { status = 5; break; }
             red2[0] = T(0);
             red2[1] = T(0);
-            for (int i = t0; i < n; i += stride) {
-                V2 ri = r[i], zi = z[i];
-                red2[0] += ri.x * zi.x + ri.y * zi.y;
-                red2[1] += ri.x * ri.x + ri.y * ri.y;
-            }
+            l0_smooth_prolong<T>(A, L0, dg, rcur, yl1, z, red2[0], red2[1]);
             publish_partials<T, 2>(red2, partials + 3 * gridDim.x);
             if (!grid_sync(bar)) { status = 5; break; }
             gather_partials<T, 2>(partials + 3 * gridDim.x, red2);
-            T rz_new = red2[0];
+            const T rz_new = red2[0];
             rr = red2[1];
             if (rr != rr || !(rz_new > T(0))) { status = 4; break; }
-            T beta = rz_new / rz;
+            beta = rz_new / rz;
             rz = rz_new;
-            for (int i = t0; i < n; i += stride) {
-                V2 zi = z[i], pi = p[i];
-                pi.x = zi.x + beta * pi.x;
-                pi.y = zi.y + beta * pi.y;
-                p[i] = pi;
-            }
+            pold = pw;
+            pw = (pw == p0) ? p1 : p0;
             it++;
-            if (!grid_sync(bar)) { status = 5; break; }
         }
     }
 done:
@@ -623,9 +806,16 @@ struct FieldSolver {
     DevHierarchy<double> H64{};
     DevHierarchy<float> H32{};
     DBuf<unsigned char> hier_dev64, hier_dev32;   // device copies of the hierarchy descriptors
+    // level 0 (applied from the ELL rows): rows renumbered by aggregate, perm[new] = old
+    std::vector<int> perm;
+    DBuf<int> agg0, chunk0;
+    DBuf<double2> t064, rb64, pb64;
+    DBuf<float2> t032, rb32, pb32;
+    DevLevel0<double> L064{};
+    DevLevel0<float> L032{};
     bool amg = false;
     int amg_levels = 0, amg_coarse = 0;
-    double vcycle_bytes64 = 0, vcycle_bytes32 = 0;   // algorithmic bytes of one V-cycle
+    double vcycle_bytes64 = 0, vcycle_bytes32 = 0;   // algorithmic bytes of one inner cycle (levels >= 1)
 
     int upload_csr(const HostCsr& M, CsrBufs& B, int group) {
         cudaStream_t st = c->stream;
@@ -644,7 +834,10 @@ struct FieldSolver {
         return MTK_OK;
     }
 
-    // Builds the aggregation hierarchy from theta (same off-diagonals as field_assemble).
+    // Builds the aggregation hierarchy from theta (same off-diagonals as field_assemble) on the
+    // original face numbering and sets perm (rows numbered by level-0 aggregate).  Level 0 keeps
+    // no matrices; levels >= 1 are uploaded as CSR cycle operators.  Leaves amg false (Jacobi)
+    // when the mesh is too small to coarsen.
     int build_amg(const int* nbr_h, const double* theta_h, int N) {
         const double pi = 3.14159265358979323846;
         std::vector<int> nbr3(nbr_h, nbr_h + 3 * (size_t)n);
@@ -656,35 +849,70 @@ struct FieldSolver {
                 vals[(size_t)j * n + f] = std::complex<double>(-std::cos(ang), -std::sin(ang));
             }
         HostHierarchy HH;
-        if (!build_hierarchy(n, nbr3, vals, 3.0 + 1e-9, HH)) return MTK_OK;   // keep Jacobi
+        if (!build_hierarchy(n, nbr3, vals, 3.0 + 1e-9, HH, 1)) return MTK_OK;   // keep Jacobi
         const int nl = (int)HH.lv.size();
         if (nl == 0) return MTK_OK;
+        const HostLevel& L0 = HH.lv[0];
+        const int nagg = (int)L0.mptr.size() - 1;
+        // chunks of <= 32 rows holding whole aggregates
+        std::vector<int> chunk{0};
+        for (int a2 = 0; a2 < nagg; a2++) {
+            const int sz = L0.mptr[a2 + 1] - L0.mptr[a2];
+            if (sz > 32) return MTK_OK;   // a chunk must hold a whole aggregate
+            if (L0.mptr[a2 + 1] - chunk.back() > 32) chunk.push_back(L0.mptr[a2]);
+        }
+        chunk.push_back(n);
+        perm = L0.mem;
         cudaStream_t st = c->stream;
-        // lanes per row: about two entries per lane (power of two, 1..32)
-        auto grp = [](const HostCsr& M) {
-            double avg = M.n > 0 ? (double)M.col.size() / M.n : 0.0;
-            int g = 1;
-            while (g < 32 && 2.0 * g < avg) g <<= 1;
-            return g;
-        };
-        for (int l = 0; l < nl; l++) {
-            const HostCycleOps& O = HH.ops[l];
-            LevelBufs& B = lvb[l];
-            // level 0's up phase writes z with the thread-per-row mapping of the PCG vector loops,
-            // which read it with no grid barrier in between: keep it at one lane per row
-            const int up_group = l == 0 ? 1 : std::max(grp(O.S), grp(O.P));
-            MTK_TRY(upload_csr(O.R, B.R, grp(O.R)));
-            MTK_TRY(upload_csr(O.S, B.S, up_group));
-            MTK_TRY(upload_csr(O.P, B.P, up_group));
-            const int ln = O.S.n;
-            if (l > 0) {
-                MTK_TRY(B.r64.alloc(ln)); MTK_TRY(B.r32.alloc(ln));
-                MTK_TRY(B.y64.alloc(ln)); MTK_TRY(B.y32.alloc(ln));
+        {
+            std::vector<int> ag(n);
+            std::vector<double2> t64(n);
+            std::vector<float2> t32(n);
+            for (int a2 = 0; a2 < nagg; a2++)
+                for (int k = L0.mptr[a2]; k < L0.mptr[a2 + 1]; k++) {
+                    const std::complex<double> tv = L0.T[perm[k]];
+                    ag[k] = a2;
+                    t64[k] = make_double2(tv.real(), tv.imag());
+                    t32[k] = make_float2((float)tv.real(), (float)tv.imag());
+                }
+            MTK_TRY(agg0.upload(ag.data(), ag.size(), st));
+            MTK_TRY(t064.upload(t64.data(), t64.size(), st));
+            MTK_TRY(t032.upload(t32.data(), t32.size(), st));
+            MTK_TRY(chunk0.upload(chunk.data(), chunk.size(), st));
+        }
+        const int nchunk = (int)chunk.size() - 1;
+        const double dg = 3.0 + 1e-9;
+        L064 = DevLevel0<double>{nagg, nchunk, agg0.p, t064.p, chunk0.p, 1.0 / dg, kOmega, kAlpha};
+        L032 = DevLevel0<float>{nagg, nchunk, agg0.p, t032.p, chunk0.p, (float)(1.0 / dg), (float)kOmega, (float)kAlpha};
+        // lanes per row of a CSR phase: fewest rounds x dependent loads (ptr, then batches of four
+        // entries per lane, each a column load and a gather) over the persistent grid
+        const double threads = (double)c->num_sms * kBlock;
+        auto grp = [&](int rows, double avg) {
+            int best = 1;
+            double bc = 1e300;
+            for (int g = 1; g <= 32; g <<= 1) {
+                const double rounds = std::ceil(rows * (double)g / threads);
+                const double cost = rounds * (1.0 + 2.0 * std::ceil(avg / (4.0 * g)));
+                if (cost < bc - 1e-9) { bc = cost; best = g; }
             }
+            return best;
+        };
+        auto avg = [](const HostCsr& M) { return M.n > 0 ? (double)M.col.size() / M.n : 0.0; };
+        const int ni = nl - 1;   // inner (CSR) levels
+        for (int i = 0; i < ni; i++) {
+            const HostCycleOps& O = HH.ops[i + 1];
+            LevelBufs& B = lvb[i];
+            MTK_TRY(upload_csr(O.R, B.R, grp(O.R.n, avg(O.R))));
+            const int up = grp(O.S.n, std::max(avg(O.S), avg(O.P)));
+            MTK_TRY(upload_csr(O.S, B.S, up));
+            MTK_TRY(upload_csr(O.P, B.P, up));
+            const int ln = O.S.n;
+            MTK_TRY(B.r64.alloc(ln)); MTK_TRY(B.r32.alloc(ln));
+            MTK_TRY(B.y64.alloc(ln)); MTK_TRY(B.y32.alloc(ln));
             auto mk64 = [](const CsrBufs& C) { return DevCsr<double>{C.n, C.group, C.ptr.p, C.col.p, C.v64.p}; };
             auto mk32 = [](const CsrBufs& C) { return DevCsr<float>{C.n, C.group, C.ptr.p, C.col.p, C.v32.p}; };
-            H64.L[l] = DevLevel<double>{mk64(B.R), mk64(B.S), mk64(B.P), B.r64.p, B.y64.p};
-            H32.L[l] = DevLevel<float>{mk32(B.R), mk32(B.S), mk32(B.P), B.r32.p, B.y32.p};
+            H64.L[i] = DevLevel<double>{mk64(B.R), mk64(B.S), mk64(B.P), B.r64.p, B.y64.p};
+            H32.L[i] = DevLevel<float>{mk32(B.R), mk32(B.S), mk32(B.P), B.r32.p, B.y32.p};
         }
         std::vector<double2> a64(HH.Ainv.size());
         std::vector<float2> a32(HH.Ainv.size());
@@ -696,20 +924,23 @@ struct FieldSolver {
         MTK_TRY(Ainv32.upload(a32.data(), a32.size(), st));
         MTK_TRY(rc64.alloc(HH.nc)); MTK_TRY(yc64.alloc(HH.nc));
         MTK_TRY(rc32.alloc(HH.nc)); MTK_TRY(yc32.alloc(HH.nc));
-        H64.nlev = nl; H64.nc = HH.nc; H64.Ainv = Ainv64.p; H64.rc = rc64.p; H64.yc = yc64.p;
-        H32.nlev = nl; H32.nc = HH.nc; H32.Ainv = Ainv32.p; H32.rc = rc32.p; H32.yc = yc32.p;
-        // V-cycle traffic: every matrix entry once (value + column), each level vector read/written
+        H64.nlev = ni; H64.nc = HH.nc; H64.Ainv = Ainv64.p; H64.rc = rc64.p; H64.yc = yc64.p;
+        H32.nlev = ni; H32.nc = HH.nc; H32.Ainv = Ainv32.p; H32.rc = rc32.p; H32.yc = yc32.p;
+        // inner-cycle traffic: every matrix entry once (value + column) plus row pointers, each
+        // level vector read / written once per use, the dense coarsest inverse; plus the level-1
+        // right-hand side written by the restriction and read by the level-0 prolongation
         {
             auto cyc = [&](double T) {
-                double b = 0;
-                for (int l = 0; l < nl; l++) {
-                    const HostCycleOps& O = HH.ops[l];
+                double bt = 0;
+                for (int i = 0; i < ni; i++) {
+                    const HostCycleOps& O = HH.ops[i + 1];
                     const double nnz = (double)O.R.col.size() + O.S.col.size() + O.P.col.size();
-                    b += nnz * (2 * T + 4) + 4.0 * (O.R.n + 2.0 * O.S.n);                 // entries + row pointers
-                    b += 2 * T * (2.0 * O.S.n + 2.0 * O.R.n + O.S.n);                       // r_l twice, r/y_{l+1}, y_l
+                    bt += nnz * (2 * T + 4) + 4.0 * (O.R.n + 2.0 * O.S.n);
+                    bt += 2 * T * (2.0 * O.S.n + 2.0 * O.R.n + O.S.n);
                 }
-                b += (double)HH.nc * HH.nc * 2 * T + 4.0 * HH.nc * T;
-                return b;
+                bt += (double)HH.nc * HH.nc * 2 * T + 4.0 * HH.nc * T;
+                bt += 2.0 * nagg * 2 * T;
+                return bt;
             };
             vcycle_bytes64 = cyc(8);
             vcycle_bytes32 = cyc(4);
@@ -737,21 +968,22 @@ struct FieldSolver {
         MTK_CUDA_TRY(cudaStreamSynchronize(c->stream));
         return MTK_OK;
     }
-    // Runs the persistent PCG and returns its status, iterations in *iters.
+    // Runs the persistent PCG and returns its status, iterations in *iters.  rb / pb are the
+    // second residual and direction buffers of the multigrid kernel.
     template <typename T, typename V2>
-    int pcg(ComplexEll<T> A, const T* minv, const V2* bb, V2* xx, V2* rr, V2* zz, V2* pp, V2* qq, double tol2,
-            int maxit, long long* iters, double* final_rr) {
+    int pcg(ComplexEll<T> A, const T* minv, const V2* bb, V2* xx, V2* rr, V2* zz, V2* pp, V2* qq, V2* rb, V2* pb,
+            double tol2, int maxit, long long* iters, double* final_rr) {
         int g = 0;
         MTK_TRY(reset_barrier(c));
         MTK_CUDA_TRY(cudaEventRecord(c->ev_k0, c->stream));
         if (amg) {
             DevHierarchy<T> H = hier<T>();
-            H.L[0].r = rr;   // level 0 works on the PCG residual and writes the PCG z
-            H.L[0].y = zz;
             DevHierarchy<T>* Hd = reinterpret_cast<DevHierarchy<T>*>(sizeof(T) == 8 ? hier_dev64.p : hier_dev32.p);
             MTK_CUDA_TRY(cudaMemcpyAsync(Hd, &H, sizeof(H), cudaMemcpyHostToDevice, c->stream));
             const DevHierarchy<T>* Hc = Hd;
-            MTK_TRY(launch_persistent(c, pcg_complex_mg<T>, &g, A, Hc, bb, xx, rr, zz, pp, qq,
+            const DevLevel0<T> L0 = level0<T>();
+            const T dg = (T)(3.0 + 1e-9);
+            MTK_TRY(launch_persistent(c, pcg_complex_mg<T>, &g, A, L0, dg, Hc, bb, xx, rr, rb, zz, pp, pb, qq,
                                       reinterpret_cast<T*>(c->partials), barrier_of(c), tol2, maxit, c->dev_int));
         } else {
             MTK_TRY(launch_persistent(c, pcg_complex<T>, &g, A, minv, bb, xx, rr, zz, pp, qq,
@@ -764,11 +996,15 @@ struct FieldSolver {
         cudaEventElapsedTime(&kms, c->ev_k0, c->ev_k1);
         pcg_ms += kms;
         pcg_launches++;
-        // algorithmic bytes per iteration: SpMV 3*(2T+4) + T + 2*2T per row, x/r/p updates
-        // 3 * 3*2T, z = M^-1 r: T + 2T (Jacobi) -- or the V-cycle traffic (R, S, P matrices and
-        // level vectors, counted in build_amg) when the multigrid preconditioner is used
-        const double per_row = 3.0 * (2 * sizeof(T) + 4) + sizeof(T) + 4.0 * sizeof(T) + 18.0 * sizeof(T) +
-                               (amg ? 4.0 * sizeof(T) : 3.0 * sizeof(T));
+        // algorithmic bytes per iteration and row.  Jacobi: SpMV 3*(2T+4) + T + 2*2T, x/r/p
+        // updates 3*3*2T, z = M^-1 r T + 2T.  Multigrid, level 0 from the ELL rows (3*(2T+4) per
+        // pass): direction + SpMV z, p_old in, p, q out (8T); update + restriction r, q, p, x
+        // in, x, r out (12T) + agg + T_k (4 + 2T); up phase r in, z out (4T) + agg + T_k; plus the
+        // inner cycle (counted in build_amg)
+        const double T_ = (double)sizeof(T);
+        const double ell = 3.0 * (2 * T_ + 4);
+        const double per_row = amg ? 3 * ell + 8 * T_ + 12 * T_ + 2 * (4 + 2 * T_) + 4 * T_
+                                   : ell + T_ + 4.0 * T_ + 18.0 * T_ + 3.0 * T_;
         const double cyc = amg ? (sizeof(T) == 8 ? vcycle_bytes64 : vcycle_bytes32) : 0.0;
         pcg_bytes += (per_row * (double)n + cyc) * (double)(c->h_int[1] + 1);
         *iters += c->h_int[1];
@@ -779,8 +1015,11 @@ struct FieldSolver {
         if (st == 3) return MTK_ERR_NOT_CONVERGED;
         return MTK_OK;
     }
+    template <typename T> DevLevel0<T> level0() const;
 };
 
+template <> DevLevel0<double> FieldSolver::level0<double>() const { return L064; }
+template <> DevLevel0<float> FieldSolver::level0<float>() const { return L032; }
 template <> DevHierarchy<double> FieldSolver::hier<double>() const { return H64; }
 template <> DevHierarchy<float> FieldSolver::hier<float>() const { return H32; }
 
@@ -802,12 +1041,50 @@ extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const 
     const int n = nF;
     cudaStream_t st = c->stream;
     MTK_CUDA_TRY(cudaEventRecord(c->ev_a, st));
-    MTK_TRY(S.nbr_in.upload(nbr_h, 3 * (size_t)n, st));
-    MTK_TRY(S.theta.upload(theta_h, 3 * (size_t)n, st));
-    MTK_TRY(S.area.upload(area_h, n, st));
+    const char* dbg_env = getenv("MTK_DEBUG");
+    const bool debug = dbg_env && dbg_env[0] == '1';
+    {
+        auto th0 = std::chrono::steady_clock::now();
+        if (!getenv("MTK_NO_AMG")) MTK_TRY(S.build_amg(nbr_h, theta_h, nRosy));
+        if (debug)
+            fprintf(stderr, "[field host] multigrid set-up %.1f ms (levels %d, coarse %d)\n",
+                    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - th0).count(), S.amg_levels,
+                    S.amg_coarse);
+    }
+    // with the multigrid the solver works on faces numbered by level-0 aggregate
+    std::vector<int32_t> nbr_p;
+    std::vector<double> theta_p, area_p, x0_p;
+    const int32_t* nbr_u = nbr_h;
+    const double *theta_u = theta_h, *area_u = area_h, *x0_u = x0;
+    if (S.amg) {
+        std::vector<int> inv(n);
+        for (int k = 0; k < n; k++) inv[S.perm[k]] = k;
+        nbr_p.resize(3 * (size_t)n);
+        theta_p.resize(3 * (size_t)n);
+        area_p.resize(n);
+        x0_p.resize(2 * (size_t)n);
+#pragma omp parallel for schedule(static)
+        for (int k = 0; k < n; k++) {
+            const int f = S.perm[k];
+            for (int j = 0; j < 3; j++) {
+                nbr_p[3 * (size_t)k + j] = inv[nbr_h[3 * (size_t)f + j]];
+                theta_p[3 * (size_t)k + j] = theta_h[3 * (size_t)f + j];
+            }
+            area_p[k] = area_h[f];
+            x0_p[2 * (size_t)k] = x0[2 * (size_t)f];
+            x0_p[2 * (size_t)k + 1] = x0[2 * (size_t)f + 1];
+        }
+        nbr_u = nbr_p.data();
+        theta_u = theta_p.data();
+        area_u = area_p.data();
+        x0_u = x0_p.data();
+    }
+    MTK_TRY(S.nbr_in.upload(nbr_u, 3 * (size_t)n, st));
+    MTK_TRY(S.theta.upload(theta_u, 3 * (size_t)n, st));
+    MTK_TRY(S.area.upload(area_u, n, st));
     const int ring = std::min(kRing, std::max(n_iter, 1));
     for (int j = 0; j < ring; j++) { MTK_TRY(S.ringU[j].alloc(n)); MTK_TRY(S.ringL[j].alloc(n)); }
-    MTK_CUDA_TRY(cudaMemcpyAsync(S.ringU[0].p, x0, sizeof(double2) * n, cudaMemcpyHostToDevice, st));
+    MTK_CUDA_TRY(cudaMemcpyAsync(S.ringU[0].p, x0_u, sizeof(double2) * n, cudaMemcpyHostToDevice, st));
     MTK_TRY(S.nbr.alloc(3 * (size_t)n));
     MTK_TRY(S.v64.alloc(3 * (size_t)n));
     MTK_TRY(S.v32.alloc(3 * (size_t)n));
@@ -817,23 +1094,16 @@ extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const 
     const bool mixed = opts.precision == MTK_PREC_MIXED;
     if (mixed) {
         MTK_TRY(S.r32.alloc(n)); MTK_TRY(S.e32.alloc(n)); MTK_TRY(S.z32.alloc(n)); MTK_TRY(S.p32.alloc(n)); MTK_TRY(S.q32.alloc(n));
+        if (S.amg) { MTK_TRY(S.rb32.alloc(n)); MTK_TRY(S.pb32.alloc(n)); }
     } else {
         MTK_TRY(S.z64.alloc(n)); MTK_TRY(S.p64.alloc(n)); MTK_TRY(S.q64.alloc(n));
+        if (S.amg) { MTK_TRY(S.rb64.alloc(n)); MTK_TRY(S.pb64.alloc(n)); }
     }
     const int G = stream_grid(c);
     field_assemble<<<G, kStream, 0, st>>>(n, nRosy, S.nbr_in.p, S.theta.p, S.area.p, S.nbr.p, S.v64.p, S.v32.p, S.d64.p,
                                          S.d32.p, S.inv64.p, S.inv32.p, S.area32.p);
     c->kernels++;
     MTK_CUDA_TRY(cudaGetLastError());
-    {
-        auto th0 = std::chrono::steady_clock::now();
-        if (!getenv("MTK_NO_AMG")) MTK_TRY(S.build_amg(nbr_h, theta_h, nRosy));
-        const char* dbg = getenv("MTK_DEBUG");
-        if (dbg && dbg[0] == '1')
-            fprintf(stderr, "[field host] multigrid set-up %.1f ms (levels %d, coarse %d)\n",
-                    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - th0).count(), S.amg_levels,
-                    S.amg_coarse);
-    }
 
     long long iters = 0, solves = 0, refines = 0;
     double worst = 0.0;
@@ -893,11 +1163,13 @@ extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const 
         const double bnorm2 = c->h_scalars[2];
         double rr = c->h_scalars[3];
         const double goal2 = tol * tol * bnorm2;
+        const double start_rel = bnorm2 > 0 ? std::sqrt(rr / bnorm2) : 0.0;
         solves++;
         refines++;
         if (!mixed) {
             double frr = 0;
-            int s = S.pcg<double, double2>(S.A64(), S.inv64.p, S.b.p, S.x.p, S.r.p, S.z64.p, S.p64.p, S.q64.p, goal2,
+            int s = S.pcg<double, double2>(S.A64(), S.inv64.p, S.b.p, S.x.p, S.r.p, S.z64.p, S.p64.p, S.q64.p, S.rb64.p,
+                                           S.pb64.p, goal2,
                                            opts.max_iter, &iters, &frr);
             if (s != MTK_OK) return s;
             // true FP64 residual of the result
@@ -919,7 +1191,8 @@ extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const 
                 zero_f2<<<G, kStream, 0, st>>>(n, S.e32.p);
                 c->kernels++;
                 int s = S.pcg<float, float2>(S.A32(), S.inv32.p, S.r32.p, S.e32.p, S.z32.p /*r*/, S.p32.p /*z*/,
-                                             S.q32.p /*p*/, reinterpret_cast<float2*>(S.Lu.p) /*q*/, itol * itol * rr,
+                                             S.q32.p /*p*/, reinterpret_cast<float2*>(S.Lu.p) /*q*/, S.rb32.p, S.pb32.p,
+                                             itol * itol * rr,
                                              opts.max_iter, &iters, nullptr);
                 if (s == MTK_ERR_TIMEOUT || s == MTK_ERR_BREAKDOWN) return s;
                 add_correction<<<G, kStream, 0, st>>>(n, S.e32.p, S.x.p);
@@ -933,6 +1206,9 @@ extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const 
         }
         double rel = bnorm2 > 0 ? std::sqrt(rr / bnorm2) : 0.0;
         if (rel > worst) worst = rel;
+        if (debug)
+            fprintf(stderr, "[field] power step %d: pcg iterations %lld (total), refinements %lld, start residual %.2e, final %.2e\n",
+                    k, iters, refines, start_rel, rel);
         // x /= sqrt|x^H M x|; u = x
         mnorm_partial<<<G, kStream, 0, st>>>(n, S.area.p, S.x.p, c->partials);
         c->kernels++;
@@ -941,9 +1217,22 @@ extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const 
         c->kernels++;
         MTK_CUDA_TRY(cudaGetLastError());
     }
-    MTK_CUDA_TRY(cudaMemcpyAsync(out, S.ringU[n_iter % ring].p, sizeof(double2) * n, cudaMemcpyDeviceToHost, st));
+    std::vector<double> out_p;
+    double* out_u = out;
+    if (S.amg) {
+        out_p.resize(2 * (size_t)n);
+        out_u = out_p.data();
+    }
+    MTK_CUDA_TRY(cudaMemcpyAsync(out_u, S.ringU[n_iter % ring].p, sizeof(double2) * n, cudaMemcpyDeviceToHost, st));
     MTK_CUDA_TRY(cudaEventRecord(c->ev_b, st));
     MTK_CUDA_TRY(cudaStreamSynchronize(st));
+    if (S.amg) {
+#pragma omp parallel for schedule(static)
+        for (int k = 0; k < n; k++) {
+            out[2 * (size_t)S.perm[k]] = out_p[2 * (size_t)k];
+            out[2 * (size_t)S.perm[k] + 1] = out_p[2 * (size_t)k + 1];
+        }
+    }
     float ms = 0;
     cudaEventElapsedTime(&ms, c->ev_a, c->ev_b);
     if (stats) {
