@@ -28,57 +28,47 @@
 namespace mtk {
 
 // Builds CSR rows in parallel: fn(row, add) calls add(col, value) for the entries of `row`
-// (duplicates are summed); each thread owns a contiguous block of rows and the blocks are
-// concatenated in order, so the result does not depend on the thread count.
+// (duplicates are summed).  Two passes over the rows: the first counts the distinct columns of
+// every row, the second writes each row (sorted by column) straight into the final arrays, so
+// there are no per-thread buffers to grow and concatenate.  Every row is formed by one thread
+// in the same order whatever the thread count, so the result does not depend on it.
 template <typename V, typename RowFn>
 void build_rows_parallel(int nrows, int ncols, RowFn fn, std::vector<int>& ptr, std::vector<int>& col,
                          std::vector<V>& val) {
-    int maxt = 1;
-#ifdef _OPENMP
-    maxt = omp_get_max_threads();
-#endif
-    std::vector<std::vector<int>> pcol(maxt), pcnt(maxt);
-    std::vector<std::vector<V>> pval(maxt);
-    std::vector<int> rbeg(maxt + 1, nrows);
+    ptr.assign(nrows + 1, 0);
 #pragma omp parallel
     {
-        int t = 0, nt = 1;
-#ifdef _OPENMP
-        t = omp_get_thread_num();
-        nt = omp_get_num_threads();
-#endif
-        const int r0 = (int)((long long)nrows * t / nt), r1 = (int)((long long)nrows * (t + 1) / nt);
-        rbeg[t] = r0;
+        std::vector<char> used(ncols, 0);
+        std::vector<int> cols;
+#pragma omp for schedule(static)
+        for (int r = 0; r < nrows; r++) {
+            cols.clear();
+            fn(r, [&](int c, V) {
+                if (!used[c]) { used[c] = 1; cols.push_back(c); }
+            });
+            for (int c : cols) used[c] = 0;
+            ptr[r + 1] = (int)cols.size();
+        }
+    }
+    for (int r = 0; r < nrows; r++) ptr[r + 1] += ptr[r];
+    col.resize(ptr[nrows]);
+    val.resize(ptr[nrows]);
+#pragma omp parallel
+    {
         std::vector<V> acc(ncols, V(0));
         std::vector<char> used(ncols, 0);
         std::vector<int> cols;
-        auto& oc = pcol[t];
-        auto& ov = pval[t];
-        auto& on = pcnt[t];
-        on.reserve(r1 - r0);
-        for (int r = r0; r < r1; r++) {
+#pragma omp for schedule(static)
+        for (int r = 0; r < nrows; r++) {
             cols.clear();
             fn(r, [&](int c, V v) {
                 if (!used[c]) { used[c] = 1; cols.push_back(c); acc[c] = V(0); }
                 acc[c] += v;
             });
             std::sort(cols.begin(), cols.end());
-            for (int c : cols) { oc.push_back(c); ov.push_back(acc[c]); used[c] = 0; }
-            on.push_back((int)cols.size());
+            int q = ptr[r];
+            for (int c : cols) { col[q] = c; val[q] = acc[c]; used[c] = 0; q++; }
         }
-    }
-    ptr.assign(nrows + 1, 0);
-    col.clear();
-    val.clear();
-    size_t total = 0;
-    for (int t = 0; t < maxt; t++) total += pcol[t].size();
-    col.reserve(total);
-    val.reserve(total);
-    int row = 0;
-    for (int t = 0; t < maxt; t++) {
-        for (size_t k = 0; k < pcnt[t].size(); k++, row++) ptr[row + 1] = ptr[row] + pcnt[t][k];
-        col.insert(col.end(), pcol[t].begin(), pcol[t].end());
-        val.insert(val.end(), pval[t].begin(), pval[t].end());
     }
 }
 

@@ -1,17 +1,21 @@
-// Aggregation multigrid for the free-variable block of the IGM normal operator.
+// Smoothed-aggregation multigrid for the free-variable block of the IGM normal operator.
 //
 // K_yy = 2 W_y^T S W_y couples the two parametric functions (u, v) of every raw vertex; away
 // from seams the 2x2 block between two vertices is a multiple of the identity and the smooth
 // (near-null) vectors are the constants of each function.  Across a seam the transition
 // rotates (u, v), so aggregation only follows identity-coupled vertex pairs: no aggregate
 // straddles a seam rotation, and constants per component stay the right near-null vectors.
-// Coarse dofs are (aggregate, component); the coarse operators are Galerkin products, and the
-// V(1,1) cycle is written as R / S / P sparse operators per level exactly as for the field:
+// Coarse dofs are (aggregate, component).  The tentative prolongation is smoothed by one
+// Jacobi step, coarse operators are Galerkin products with the smoothed prolongation, and the
+// V(1,1) cycle is written as R / S / P sparse operators per level:
 //   down r_{l+1} = R r_l,  up y_l = S r_l + P y_{l+1}.
 #pragma once
 #include <algorithm>
 #include <cmath>
 #include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 #include "mtk_amg.cuh"
 #include "mtk_ctx.cuh"
@@ -51,42 +55,67 @@ inline double rcsr_at(const RCsr& A, int i, int j) {
     return (it != e && *it == j) ? A.val[A.ptr[i] + (it - A.col.begin() - A.ptr[i])] : 0.0;
 }
 
-// One coarsening step.  Fills L.agg / L.T / L.dinv, returns the coarse operator and the coarse
-// dof -> (node, comp) map.
-inline void rcoarsen(RLevel& L, RCsr& next, std::vector<int>& cnode, std::vector<int>& ccomp, int& cnnode) {
+// Aggregation of one level.  Fills L.agg (dof -> coarse dof), L.T (tentative prolongation
+// weight 1/sqrt|aggregate|, so T has orthonormal columns), L.dinv, and the coarse dof ->
+// (node, comp) map.  Returns the number of coarse dofs.
+inline int raggregate(RLevel& L, std::vector<int>& cnode, std::vector<int>& ccomp, int& cnnode) {
     const RCsr& A = L.A;
     const int n = A.n, nn = L.nnode;
-    // node dof lists
     std::vector<int> nd0(nn, -1), nd1(nn, -1);
     for (int d = 0; d < n; d++) (L.comp[d] == 0 ? nd0 : nd1)[L.node[d]] = d;
     auto paired = [&](int v) { return nd0[v] >= 0 && nd1[v] >= 0; };
-    // identity-coupled node neighbours
+    // identity-coupled node neighbours (the 2x2 block between the two nodes is a multiple of I)
     std::vector<int> nptr(nn + 1, 0), nadj;
     {
-        std::vector<std::vector<int>> tmp(nn);
+        auto coupled = [&](int v, int p) {
+            const int e = A.col[p], w = L.node[e];
+            if (w == v || L.comp[e] != 0 || !paired(w)) return false;
+            const double uu = A.val[p];
+            const double vv = rcsr_at(A, nd1[v], nd1[w]);
+            const double uv = rcsr_at(A, nd0[v], nd1[w]), vu = rcsr_at(A, nd1[v], nd0[w]);
+            const double sm = std::fabs(uu) + std::fabs(vv);
+            if (sm == 0) return false;
+            return !(std::fabs(uv) + std::fabs(vu) > 1e-9 * sm || std::fabs(uu - vv) > 1e-9 * sm);
+        };
+#pragma omp parallel for schedule(static)
+        for (int v = 0; v < nn; v++) {
+            int cnt = 0;
+            if (paired(v))
+                for (int p = A.ptr[nd0[v]]; p < A.ptr[nd0[v] + 1]; p++) cnt += coupled(v, p) ? 1 : 0;
+            nptr[v + 1] = cnt;
+        }
+        for (int v = 0; v < nn; v++) nptr[v + 1] += nptr[v];
+        nadj.resize(nptr[nn]);
+#pragma omp parallel for schedule(static)
         for (int v = 0; v < nn; v++) {
             if (!paired(v)) continue;
-            int du = nd0[v], dv = nd1[v];
-            for (int p = A.ptr[du]; p < A.ptr[du + 1]; p++) {
-                int e = A.col[p];
-                int w = L.node[e];
-                if (w == v || L.comp[e] != 0 || !paired(w)) continue;
-                double uu = A.val[p];
-                double vv = rcsr_at(A, dv, nd1[w]);
-                double uv = rcsr_at(A, du, nd1[w]), vu = rcsr_at(A, dv, nd0[w]);
-                double s = std::fabs(uu) + std::fabs(vv);
-                if (s == 0) continue;
-                if (std::fabs(uv) + std::fabs(vu) > 1e-9 * s || std::fabs(uu - vv) > 1e-9 * s) continue;
-                tmp[v].push_back(w);
+            int q = nptr[v];
+            for (int p = A.ptr[nd0[v]]; p < A.ptr[nd0[v] + 1]; p++)
+                if (coupled(v, p)) nadj[q++] = L.node[A.col[p]];
+        }
+    }
+    // visiting order: breadth-first over the identity-coupled graph, so that roots are packed
+    // next to each other whatever the input numbering (index order on a subdivided mesh puts the
+    // coarse vertices first and leaves large remainders for pass 2)
+    std::vector<int> order;
+    order.reserve(nn);
+    {
+        std::vector<char> seen(nn, 0);
+        for (int s0 = 0; s0 < nn; s0++) {
+            if (seen[s0]) continue;
+            seen[s0] = 1;
+            size_t head = order.size();
+            order.push_back(s0);
+            while (head < order.size()) {
+                const int v = order[head++];
+                for (int p = nptr[v]; p < nptr[v + 1]; p++)
+                    if (!seen[nadj[p]]) { seen[nadj[p]] = 1; order.push_back(nadj[p]); }
             }
         }
-        for (int v = 0; v < nn; v++) nptr[v + 1] = nptr[v] + (int)tmp[v].size();
-        nadj.reserve(nptr[nn]);
-        for (int v = 0; v < nn; v++) nadj.insert(nadj.end(), tmp[v].begin(), tmp[v].end());
     }
     std::vector<int> nagg(nn, -1);
     int na = 0;
-    for (int v = 0; v < nn; v++) {   // pass 1
+    for (int v : order) {   // pass 1: a free node with free neighbours roots an aggregate
         if (nagg[v] >= 0 || !paired(v)) continue;
         bool ok = true;
         for (int p = nptr[v]; p < nptr[v + 1]; p++) if (nagg[nadj[p]] >= 0) { ok = false; break; }
@@ -95,57 +124,107 @@ inline void rcoarsen(RLevel& L, RCsr& next, std::vector<int>& cnode, std::vector
         for (int p = nptr[v]; p < nptr[v + 1]; p++) nagg[nadj[p]] = na;
         na++;
     }
-    for (int v = 0; v < nn; v++) {   // pass 2
-        if (nagg[v] >= 0 || !paired(v)) continue;
-        for (int p = nptr[v]; p < nptr[v + 1]; p++)
-            if (nagg[nadj[p]] >= 0) { nagg[v] = nagg[nadj[p]]; break; }
-    }
-    for (int v = 0; v < nn; v++) if (nagg[v] < 0) nagg[v] = na++;   // pass 3
     std::vector<int> size(na, 0);
-    for (int v = 0; v < nn; v++) size[nagg[v]]++;
-    // coarse dofs: (aggregate, comp) for the comps present
+    for (int v = 0; v < nn; v++) if (nagg[v] >= 0) size[nagg[v]]++;
+    std::vector<int> attach(nn, -1);
+    for (int v : order) {   // pass 2: join the smallest neighbouring pass-1 aggregate
+        if (nagg[v] >= 0 || !paired(v)) continue;
+        int best = -1;
+        for (int p = nptr[v]; p < nptr[v + 1]; p++) {
+            const int a2 = nagg[nadj[p]];
+            if (a2 >= 0 && (best < 0 || size[a2] < size[best])) best = a2;
+        }
+        attach[v] = best;
+    }
+    for (int v = 0; v < nn; v++)
+        if (attach[v] >= 0) { nagg[v] = attach[v]; size[attach[v]]++; }
+    for (int v : order) {   // pass 3: what is left forms aggregates with its free neighbours
+        if (nagg[v] >= 0) continue;
+        nagg[v] = na;
+        int cnt = 1;
+        for (int p = nptr[v]; p < nptr[v + 1]; p++) if (nagg[nadj[p]] < 0) { nagg[nadj[p]] = na; cnt++; }
+        size.push_back(cnt);
+        na++;
+    }
+    // coarse dofs: (aggregate, comp) for the comps present, numbered by aggregate
     std::vector<int> cd0(na, -1), cd1(na, -1);
+    for (int v = 0; v < nn; v++) {
+        const int a2 = nagg[v];
+        if (nd0[v] >= 0) cd0[a2] = 0;
+        if (nd1[v] >= 0) cd1[a2] = 0;
+    }
     cnnode = na;
     cnode.clear();
     ccomp.clear();
-    for (int v = 0; v < nn; v++) {
-        int a = nagg[v];
-        if (nd0[v] >= 0 && cd0[a] < 0) { cd0[a] = 0; }
-        if (nd1[v] >= 0 && cd1[a] < 0) { cd1[a] = 0; }
-    }
     int ncd = 0;
-    for (int a = 0; a < na; a++) {
-        if (cd0[a] >= 0) { cd0[a] = ncd++; cnode.push_back(a); ccomp.push_back(0); }
-        if (cd1[a] >= 0) { cd1[a] = ncd++; cnode.push_back(a); ccomp.push_back(1); }
+    for (int a2 = 0; a2 < na; a2++) {
+        if (cd0[a2] >= 0) { cd0[a2] = ncd++; cnode.push_back(a2); ccomp.push_back(0); }
+        if (cd1[a2] >= 0) { cd1[a2] = ncd++; cnode.push_back(a2); ccomp.push_back(1); }
     }
     L.agg.resize(n);
     L.T.resize(n);
     L.dinv.resize(n);
+#pragma omp parallel for schedule(static)
     for (int d = 0; d < n; d++) {
-        int a = nagg[L.node[d]];
-        L.agg[d] = L.comp[d] == 0 ? cd0[a] : cd1[a];
-        L.T[d] = 1.0 / std::sqrt((double)size[a]);
-        double dg = rcsr_at(A, d, d);
+        const int a2 = nagg[L.node[d]];
+        L.agg[d] = L.comp[d] == 0 ? cd0[a2] : cd1[a2];
+        L.T[d] = 1.0 / std::sqrt((double)size[a2]);
+        const double dg = rcsr_at(A, d, d);
         L.dinv[d] = dg > 0 ? 1.0 / dg : 1.0;
     }
-    // members of each coarse dof, Galerkin product
-    std::vector<int> mptr(ncd + 1, 0), mem(n);
-    for (int d = 0; d < n; d++) mptr[L.agg[d] + 1]++;
-    for (int a = 0; a < ncd; a++) mptr[a + 1] += mptr[a];
+    return ncd;
+}
+
+// Transpose of an n x m CSR.  Threads count the columns of contiguous row blocks, offsets are
+// laid out block by block, so every output row lists its entries in ascending input row: the
+// same arrays as a serial transpose, for any thread count.
+inline RCsr rcsr_transpose(const RCsr& M, int m) {
+    RCsr Tm;
+    Tm.n = m;
+    Tm.ptr.assign(m + 1, 0);
+    Tm.col.resize(M.col.size());
+    Tm.val.resize(M.col.size());
+    int nt = 1;
+#ifdef _OPENMP
+    nt = omp_get_max_threads();
+#endif
+    std::vector<std::vector<int>> cnt(nt);
+#pragma omp parallel num_threads(nt)
     {
-        std::vector<int> fill(mptr.begin(), mptr.end() - 1);
-        for (int d = 0; d < n; d++) mem[fill[L.agg[d]]++] = d;
-    }
-    next.n = ncd;
-    build_rows_parallel<double>(
-        ncd, ncd,
-        [&](int a, auto add) {
-            for (int m = mptr[a]; m < mptr[a + 1]; m++) {
-                const int i = mem[m];
-                for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) add(L.agg[A.col[p]], L.T[i] * A.val[p] * L.T[A.col[p]]);
+        int t = 0;
+#ifdef _OPENMP
+        t = omp_get_thread_num();
+#endif
+        const int r0 = (int)((long long)M.n * t / nt), r1 = (int)((long long)M.n * (t + 1) / nt);
+        std::vector<int>& c = cnt[t];
+        c.assign(m, 0);
+        for (int p = M.ptr[r0]; p < M.ptr[r1]; p++) c[M.col[p]]++;
+#pragma omp barrier
+#pragma omp single
+        {
+            for (int a = 0; a < m; a++) {
+                int s = 0;
+                for (int u = 0; u < nt; u++) s += cnt[u][a];
+                Tm.ptr[a + 1] = s;
             }
-        },
-        next.ptr, next.col, next.val);
+            for (int a = 0; a < m; a++) Tm.ptr[a + 1] += Tm.ptr[a];
+            for (int a = 0; a < m; a++) {   // cnt becomes the write offset of each block
+                int off = Tm.ptr[a];
+                for (int u = 0; u < nt; u++) {
+                    const int k = cnt[u][a];
+                    cnt[u][a] = off;
+                    off += k;
+                }
+            }
+        }
+        for (int i = r0; i < r1; i++)
+            for (int p = M.ptr[i]; p < M.ptr[i + 1]; p++) {
+                const int q = c[M.col[p]]++;
+                Tm.col[q] = i;
+                Tm.val[q] = M.val[p];
+            }
+    }
+    return Tm;
 }
 
 inline bool spd_inverse_dense(std::vector<double>& A, int n) {
@@ -179,9 +258,14 @@ inline bool spd_inverse_dense(std::vector<double>& A, int n) {
     return true;
 }
 
-// A0: the level-0 operator (symmetric positive definite), node/comp of its dofs.
+// Smoothed-aggregation hierarchy.  Per level: aggregates and T (raggregate), the smoothed
+// prolongator P_sa = (I - w_p D^-1 A) T with w_p = (4/3) / rho, rho the Gershgorin bound of
+// D^-1 A, and the Galerkin coarse operator P_sa^T A P_sa.  Cycle operators (V(1,1), Jacobi
+// weight omega, coarse correction scaled by alpha):
+//   R = P_sa^T (I - omega A D^-1),  S = omega D^-1 (2 I - A omega D^-1),
+//   P = alpha (I - omega D^-1 A) P_sa = alpha (P_sa - omega D^-1 (A P_sa)) = alpha R^T.
 inline bool build_real_hierarchy(RCsr A0, std::vector<int> node, std::vector<int> comp, int nnode, RHierarchy& H,
-                                 double omega = 0.8, double alpha = 1.8) {
+                                 double omega = 0.85, double alpha = 1.0) {
     H.lv.clear();
     H.ops.clear();
     RLevel cur;
@@ -190,14 +274,114 @@ inline bool build_real_hierarchy(RCsr A0, std::vector<int> node, std::vector<int
     cur.comp = std::move(comp);
     cur.nnode = nnode;
     while (cur.A.n > kRCoarseMax && (int)H.lv.size() < kRMaxLevels - 1) {
-        RCsr next;
         std::vector<int> cn, cc;
         int cnn = 0;
-        rcoarsen(cur, next, cn, cc, cnn);
-        if (next.n >= cur.A.n * 0.9) return false;   // stalled coarsening
+        const int na = raggregate(cur, cn, cc, cnn);
+        if (na >= cur.A.n * 0.9) return false;   // stalled coarsening
+        const RCsr& A = cur.A;
+        const int n = A.n;
+        // spectral radius of D^-1 A: 12 power steps (Rayleigh quotient in the D inner product) from
+        // a fixed oscillating start; the estimate is below rho, so it is raised by 5 percent
+        double rho = 0;
+        {
+            std::vector<double> v(n), w(n);
+#pragma omp parallel for schedule(static)
+            for (int i = 0; i < n; i++) v[i] = (i & 1) ? 1.0 : -1.0 + 0.25 * ((i * 7919) % 5);
+            for (int it = 0; it < 12; it++) {
+                double num = 0, den = 0, nw = 0;
+#pragma omp parallel for schedule(static) reduction(+ : num, den, nw)
+                for (int i = 0; i < n; i++) {
+                    double av = 0;
+                    for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) av += A.val[p] * v[A.col[p]];
+                    w[i] = cur.dinv[i] * av;
+                    num += v[i] * av;
+                    den += v[i] * v[i] / cur.dinv[i];
+                    nw += w[i] * w[i];
+                }
+                rho = den > 0 ? num / den : 0.0;
+                const double sc = nw > 0 ? 1.0 / std::sqrt(nw) : 0.0;
+#pragma omp parallel for schedule(static)
+                for (int i = 0; i < n; i++) v[i] = w[i] * sc;
+            }
+            rho *= 1.05;
+        }
+        const double wp = rho > 0 ? (4.0 / 3.0) / rho : 0.0;
+        RCsr Psa, AP;
+        Psa.n = n;
+        build_rows_parallel<double>(
+            n, na,
+            [&](int i, auto add) {
+                add(cur.agg[i], cur.T[i]);
+                for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++)
+                    add(cur.agg[A.col[p]], -wp * cur.dinv[i] * A.val[p] * cur.T[A.col[p]]);
+            },
+            Psa.ptr, Psa.col, Psa.val);
+        AP.n = n;
+        build_rows_parallel<double>(
+            n, na,
+            [&](int i, auto add) {
+                for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) {
+                    const int k = A.col[p];
+                    for (int q = Psa.ptr[k]; q < Psa.ptr[k + 1]; q++) add(Psa.col[q], A.val[p] * Psa.val[q]);
+                }
+            },
+            AP.ptr, AP.col, AP.val);
+        const RCsr Pt = rcsr_transpose(Psa, na);
+        RLevel nxt;
+        nxt.A.n = na;
+        build_rows_parallel<double>(
+            na, na,
+            [&](int a2, auto add) {
+                for (int t = Pt.ptr[a2]; t < Pt.ptr[a2 + 1]; t++) {
+                    const int i = Pt.col[t];
+                    const double pv = Pt.val[t];
+                    for (int q = AP.ptr[i]; q < AP.ptr[i + 1]; q++) add(AP.col[q], pv * AP.val[q]);
+                }
+            },
+            nxt.A.ptr, nxt.A.col, nxt.A.val);
+        // cycle operators of this level
+        RCycleOps O;
+        O.S.n = n;
+        O.S.ptr = A.ptr;
+        O.S.col = A.col;
+        O.S.val.resize(A.val.size());
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < n; i++)
+            for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) {
+                const int j = A.col[p];
+                double v = -A.val[p] * omega * cur.dinv[j];
+                if (j == i) v += 2.0;
+                O.S.val[p] = omega * cur.dinv[i] * v;
+            }
+        // P row i = alpha (Psa row - omega dinv_i AP row): merge of two column-sorted rows
+        O.P.n = n;
+        O.P.ptr.assign(n + 1, 0);
+        auto merge_row = [&](int i, int* oc, double* ov) {
+            int a = Psa.ptr[i], ae = Psa.ptr[i + 1], b = AP.ptr[i], be = AP.ptr[i + 1], k = 0;
+            const double sb = -alpha * omega * cur.dinv[i];
+            while (a < ae || b < be) {
+                int c2;
+                double v = 0;
+                if (b >= be || (a < ae && Psa.col[a] < AP.col[b])) { c2 = Psa.col[a]; v = alpha * Psa.val[a++]; }
+                else if (a >= ae || AP.col[b] < Psa.col[a]) { c2 = AP.col[b]; v = sb * AP.val[b++]; }
+                else { c2 = Psa.col[a]; v = alpha * Psa.val[a++] + sb * AP.val[b++]; }
+                if (oc) { oc[k] = c2; ov[k] = v; }
+                k++;
+            }
+            return k;
+        };
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < n; i++) O.P.ptr[i + 1] = merge_row(i, nullptr, nullptr);
+        for (int i = 0; i < n; i++) O.P.ptr[i + 1] += O.P.ptr[i];
+        O.P.col.resize(O.P.ptr[n]);
+        O.P.val.resize(O.P.ptr[n]);
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < n; i++) merge_row(i, O.P.col.data() + O.P.ptr[i], O.P.val.data() + O.P.ptr[i]);
+        O.R = rcsr_transpose(O.P, na);
+        for (double& v : O.R.val) v /= alpha;
+        H.ops.push_back(std::move(O));
         H.lv.push_back(std::move(cur));
-        cur = RLevel();
-        cur.A = std::move(next);
+        cur = std::move(nxt);
         cur.node = std::move(cn);
         cur.comp = std::move(cc);
         cur.nnode = cnn;
@@ -207,51 +391,13 @@ inline bool build_real_hierarchy(RCsr A0, std::vector<int> node, std::vector<int
     H.Ainv.assign((size_t)H.nc * H.nc, 0.0);
     for (int i = 0; i < H.nc; i++)
         for (int p = cur.A.ptr[i]; p < cur.A.ptr[i + 1]; p++) H.Ainv[(size_t)i * H.nc + cur.A.col[p]] = cur.A.val[p];
-    if (!spd_inverse_dense(H.Ainv, H.nc)) return false;
-    H.ops.resize(H.lv.size());
-    for (size_t l = 0; l < H.lv.size(); l++) {
-        const RLevel& L = H.lv[l];
-        const RCsr& A = L.A;
-        const int n = A.n;
-        const int na = (l + 1 < H.lv.size()) ? H.lv[l + 1].A.n : H.nc;
-        RCycleOps& O = H.ops[l];
-        O.S.n = n;
-        O.S.ptr = A.ptr;
-        O.S.col = A.col;
-        O.S.val.resize(A.val.size());
-#pragma omp parallel for schedule(static)
-        for (int i = 0; i < n; i++)
-            for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) {
-                int j = A.col[p];
-                double v = -A.val[p] * omega * L.dinv[j];
-                if (j == i) v += 2.0;
-                O.S.val[p] = omega * L.dinv[i] * v;
-            }
-        O.P.n = n;
-        build_rows_parallel<double>(
-            n, na,
-            [&](int i, auto add) {
-                add(L.agg[i], alpha * L.T[i]);
-                for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++)
-                    add(L.agg[A.col[p]], -alpha * omega * L.dinv[i] * A.val[p] * L.T[A.col[p]]);
-            },
-            O.P.ptr, O.P.col, O.P.val);
-        O.R.n = na;
-        O.R.ptr.assign(na + 1, 0);
-        for (int b : O.P.col) O.R.ptr[b + 1]++;
-        for (int a = 0; a < na; a++) O.R.ptr[a + 1] += O.R.ptr[a];
-        O.R.col.resize(O.P.col.size());
-        O.R.val.resize(O.P.col.size());
-        std::vector<int> fill(O.R.ptr.begin(), O.R.ptr.end() - 1);
-        for (int i = 0; i < n; i++)
-            for (int p = O.P.ptr[i]; p < O.P.ptr[i + 1]; p++) {
-                int a = O.P.col[p];
-                int q = fill[a]++;
-                O.R.col[q] = i;
-                O.R.val[q] = O.P.val[p] / alpha;
-            }
-    }
-    return true;
+    for (int i = 0; i < H.nc; i++)   // symmetrise the round-off of the Galerkin products
+        for (int j = 0; j < i; j++) {
+            const double m = 0.5 * (H.Ainv[(size_t)i * H.nc + j] + H.Ainv[(size_t)j * H.nc + i]);
+            H.Ainv[(size_t)i * H.nc + j] = m;
+            H.Ainv[(size_t)j * H.nc + i] = m;
+        }
+    return spd_inverse_dense(H.Ainv, H.nc);
 }
 
 // ------------------------------------------------------------------ device side
@@ -283,7 +429,22 @@ struct RDevHierarchy {
 template <typename T>
 __device__ __forceinline__ T rcsr_row(const RDevCsr<T>& M, int row, int lane, int g, const T* __restrict__ x) {
     T s = T(0);
-    for (int p = M.ptr[row] + lane; p < M.ptr[row + 1]; p += g) s += M.val[p] * __ldcg(x + M.col[p]);
+    const int e = __ldg(M.ptr + row + 1);
+    for (int p = __ldg(M.ptr + row) + lane; p < e; p += 4 * g) {   // four loads in flight per lane
+        int c[4];
+        T v[4], xv[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int pu = p + u * g;
+            c[u] = pu < e ? __ldg(M.col + pu) : -1;
+            v[u] = pu < e ? __ldg(M.val + pu) : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) xv[u] = c[u] >= 0 ? __ldcg(x + c[u]) : T(0);
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            if (c[u] >= 0) s += v[u] * xv[u];
+    }
     return s;
 }
 

@@ -706,11 +706,18 @@ struct Igm {
         if (!build_real_hierarchy(std::move(K), std::move(node), std::move(comp), nnode, HH)) return MTK_OK;
         const int nl = (int)HH.lv.size();
         if (nl == 0) return MTK_OK;
-        auto grp = [](const RCsr& M) {   // lanes per row: about two entries per lane
-            double avg = M.n > 0 ? (double)M.col.size() / M.n : 0.0;
-            int g = 1;
-            while (g < 32 && 2.0 * g < avg) g <<= 1;
-            return g;
+        // lanes per row of a CSR phase: fewest rounds x dependent loads (ptr, then batches of four
+        // entries per lane, each a column load and a gather) over the persistent grid
+        const double threads = (double)c->num_sms * kBlock;
+        auto grp = [&](const RCsr& M) {
+            const double avg = M.n > 0 ? (double)M.col.size() / M.n : 0.0;
+            int best = 1;
+            double bc = 1e300;
+            for (int g = 1; g <= 32; g <<= 1) {
+                const double cost = std::ceil(M.n * (double)g / threads) * (1.0 + 2.0 * std::ceil(avg / (4.0 * g)));
+                if (cost < bc - 1e-9) { bc = cost; best = g; }
+            }
+            return best;
         };
         for (int l = 0; l < nl; l++) {
             const RCycleOps& O = HH.ops[l];
