@@ -1,4 +1,5 @@
-// Aggregation multigrid for the complex Hermitian connection Laplacian of the field solve.
+// Smoothed-aggregation multigrid for the complex Hermitian connection Laplacian of the field
+// solve.
 //
 // Host set-up (once per field solve, the matrix is fixed across the 50 inverse iterations):
 //  * greedy aggregation on the matrix graph: pass 1 makes an aggregate of every node whose
@@ -7,13 +8,12 @@
 //  * tentative prolongation with a parallel-transported near-null vector: smooth vectors of L
 //    satisfy x_j ~ -(A_ji / |A_ji|) x_i along an edge, so t is propagated from each root
 //    along the aggregation tree and T(i, agg i) = t_i / sqrt|agg|;
-//  * Galerkin coarse operators A_{l+1} = T^H A_l T, down to <= kCoarseMax rows, whose dense
-//    inverse is applied on the device.
+//  * the prolongation smoothed by one Jacobi step, P_sa = (I - w_p D^-1 A) T, and Galerkin
+//    coarse operators A_{l+1} = P_sa^H A_l P_sa, down to <= kCoarseMax rows, whose dense inverse
+//    is applied on the device.
 // Device V(1,1) cycle with weighted Jacobi (omega = 0.8, symmetric pre/post smoothing, exact
-// coarse solve) and the coarse correction scaled by alpha = 1.8 (plain aggregation
-// under-corrects; any alpha < 2 keeps the cycle Hermitian positive definite).  Pre-smoothing,
-// residual and restriction are fused per aggregate, prolongation and post-smoothing per row,
-// so a cycle costs two grid barriers per level.
+// coarse solve).  Pre-smoothing, residual and restriction are one operator R per level,
+// prolongation and post-smoothing another (P), so a level costs two grid barriers.
 #pragma once
 #include <algorithm>
 #include <cmath>
@@ -75,7 +75,7 @@ void build_rows_parallel(int nrows, int ncols, RowFn fn, std::vector<int>& ptr, 
 constexpr int kMaxLevels = 8;
 constexpr int kCoarseMax = 384;
 constexpr double kOmega = 0.8;   // Jacobi weight of the pre- and post-smoothing
-constexpr double kAlpha = 1.8;   // coarse-correction scale
+constexpr double kAlpha = 1.0;   // coarse-correction scale
 
 // ------------------------------------------------------------------ host hierarchy
 struct HostCsr {
@@ -90,6 +90,7 @@ struct HostLevel {
     std::vector<std::complex<double>> T;       // tentative prolongation coefficient per row
     std::vector<int> mptr, mem;                // members of each aggregate
     std::vector<double> dinv;                  // 1 / diag
+    double wp = 0;                             // prolongation smoothing weight
 };
 
 // The V(1,1) cycle written as three sparse operators per level (x = omega D^-1 r pre-smoothing,
@@ -108,7 +109,7 @@ struct HostHierarchy {
     std::vector<std::complex<double>> Ainv;    // dense inverse of the coarsest operator
 };
 
-inline void aggregate_level(HostLevel& L, HostCsr& next) {
+inline int aggregate_level(HostLevel& L) {
     const HostCsr& A = L.A;
     const int n = A.n;
     L.agg.assign(n, -1);
@@ -191,24 +192,7 @@ inline void aggregate_level(HostLevel& L, HostCsr& next) {
         for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) if (A.col[p] == i) d = A.val[p].real();
         L.dinv[i] = d > 0 ? 1.0 / d : 1.0;
     }
-    // Galerkin coarse operator (rows = aggregates)
-    next.n = na;
-    build_rows_parallel<std::complex<double>>(
-        na, na,
-        [&](int a, auto add) {
-            for (int m = L.mptr[a]; m < L.mptr[a + 1]; m++) {
-                const int i = L.mem[m];
-                const std::complex<double> ti = std::conj(L.T[i]);
-                for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) {
-                    const int j = A.col[p];
-                    add(L.agg[j], ti * A.val[p] * L.T[j]);
-                }
-            }
-        },
-        next.ptr, next.col, next.val);
-    for (int a = 0; a < na; a++)      // Hermitian diagonal
-        for (int p = next.ptr[a]; p < next.ptr[a + 1]; p++)
-            if (next.col[p] == a) next.val[p] = std::complex<double>(next.val[p].real(), 0.0);
+    return na;
 }
 
 // Hermitian positive definite inverse (complex Cholesky), returns false if not HPD.
@@ -244,12 +228,39 @@ inline bool hpd_inverse(std::vector<std::complex<double>>& A, int n) {
     return true;
 }
 
-// Builds the hierarchy from the level-0 ELL rows (nbr[3*f+j], val[j*n+f], diag d).  The cycle
-// operators R, S, P are formed for levels >= first_ops (the device applies level 0 directly from
-// the ELL rows, the aggregates and T).
+// Hermitian transpose of an n x m complex CSR (serial; output rows in ascending input row).
+inline HostCsr hcsr_adjoint(const HostCsr& M, int m) {
+    HostCsr Tm;
+    Tm.n = m;
+    Tm.ptr.assign(m + 1, 0);
+    for (int c : M.col) Tm.ptr[c + 1]++;
+    for (int a = 0; a < m; a++) Tm.ptr[a + 1] += Tm.ptr[a];
+    Tm.col.resize(M.col.size());
+    Tm.val.resize(M.col.size());
+    std::vector<int> fill(Tm.ptr.begin(), Tm.ptr.end() - 1);
+    for (int i = 0; i < M.n; i++)
+        for (int p = M.ptr[i]; p < M.ptr[i + 1]; p++) {
+            const int q = fill[M.col[p]]++;
+            Tm.col[q] = i;
+            Tm.val[q] = std::conj(M.val[p]);
+        }
+    return Tm;
+}
+
+// Builds the smoothed-aggregation hierarchy from the level-0 ELL rows (nbr[3*f+j], val[j*n+f],
+// diag d).  Per level: aggregates and T (aggregate_level), the smoothed prolongation
+// P_sa = (I - w_p D^-1 A) T with w_p = (4/3) / rho(D^-1 A) (power estimate raised by 5 percent),
+// and the Galerkin coarse operator P_sa^H A P_sa.  The cycle operators (V(1,1), Jacobi weight
+// kOmega, coarse correction scale kAlpha)
+//   R = P_sa^H (I - omega A D^-1),  S = omega D^-1 (2 I - A omega D^-1),
+//   P = alpha (I - omega D^-1 A) P_sa = alpha R^H
+// are formed for levels >= first_ops (the device applies level 0 from the ELL rows, the
+// aggregates, T and w_p).
 inline bool build_hierarchy(int n, const std::vector<int>& nbr3, const std::vector<std::complex<double>>& vals,
                             double diag, HostHierarchy& H, int first_ops = 0) {
+    using cd = std::complex<double>;
     H.lv.clear();
+    H.ops.clear();
     HostCsr A0;
     A0.n = n;
     A0.ptr.resize(n + 1);
@@ -258,79 +269,122 @@ inline bool build_hierarchy(int n, const std::vector<int>& nbr3, const std::vect
 #pragma omp parallel for schedule(static)
     for (int f = 0; f < n; f++) {
         A0.ptr[f] = 4 * f;
-        struct E { int c; std::complex<double> v; } e[4];
-        e[0] = {f, std::complex<double>(diag, 0)};
+        struct E { int c; cd v; } e[4];
+        e[0] = {f, cd(diag, 0)};
         for (int j = 0; j < 3; j++) e[1 + j] = {nbr3[3 * f + j], vals[(size_t)j * n + f]};
         std::sort(e, e + 4, [](const E& a, const E& b) { return a.c < b.c; });
         for (int k = 0; k < 4; k++) { A0.col[4 * (size_t)f + k] = e[k].c; A0.val[4 * (size_t)f + k] = e[k].v; }
     }
     A0.ptr[n] = 4 * n;
     HostCsr cur = std::move(A0);
+    const double omega = kOmega, alpha = kAlpha;
     while (cur.n > kCoarseMax && (int)H.lv.size() < kMaxLevels - 1) {
         HostLevel L;
         L.A = std::move(cur);
+        const int na = aggregate_level(L);
+        if (na >= L.A.n) return false;   // no coarsening
+        const HostCsr& A = L.A;
+        const int ln = A.n;
+        double rho = 0;
+        {
+            std::vector<cd> v(ln), w(ln);
+#pragma omp parallel for schedule(static)
+            for (int i = 0; i < ln; i++) v[i] = cd((i & 1) ? 1.0 : -1.0 + 0.25 * ((i * 7919) % 5), 0.1 * ((i * 104729) % 7));
+            for (int it = 0; it < 12; it++) {
+                double num = 0, den = 0, nw = 0;
+#pragma omp parallel for schedule(static) reduction(+ : num, den, nw)
+                for (int i = 0; i < ln; i++) {
+                    cd av = 0;
+                    for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) av += A.val[p] * v[A.col[p]];
+                    w[i] = L.dinv[i] * av;
+                    num += (std::conj(v[i]) * av).real();
+                    den += std::norm(v[i]) / L.dinv[i];
+                    nw += std::norm(w[i]);
+                }
+                rho = den > 0 ? num / den : 0.0;
+                const double sc = nw > 0 ? 1.0 / std::sqrt(nw) : 0.0;
+#pragma omp parallel for schedule(static)
+                for (int i = 0; i < ln; i++) v[i] = w[i] * sc;
+            }
+            rho *= 1.05;
+        }
+        L.wp = rho > 0 ? (4.0 / 3.0) / rho : 0.0;
+        const double wp = L.wp;
+        HostCsr Psa, AP;
+        Psa.n = ln;
+        build_rows_parallel<cd>(
+            ln, na,
+            [&](int i, auto add) {
+                add(L.agg[i], L.T[i]);
+                for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) add(L.agg[A.col[p]], -wp * L.dinv[i] * A.val[p] * L.T[A.col[p]]);
+            },
+            Psa.ptr, Psa.col, Psa.val);
+        AP.n = ln;
+        build_rows_parallel<cd>(
+            ln, na,
+            [&](int i, auto add) {
+                for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) {
+                    const int k = A.col[p];
+                    for (int q = Psa.ptr[k]; q < Psa.ptr[k + 1]; q++) add(Psa.col[q], A.val[p] * Psa.val[q]);
+                }
+            },
+            AP.ptr, AP.col, AP.val);
+        const HostCsr Ph = hcsr_adjoint(Psa, na);
         HostCsr next;
-        aggregate_level(L, next);
-        if (next.n >= L.A.n) return false;   // no coarsening
+        next.n = na;
+        build_rows_parallel<cd>(
+            na, na,
+            [&](int a2, auto add) {
+                for (int t = Ph.ptr[a2]; t < Ph.ptr[a2 + 1]; t++) {
+                    const int i = Ph.col[t];
+                    const cd pv = Ph.val[t];
+                    for (int q = AP.ptr[i]; q < AP.ptr[i + 1]; q++) add(AP.col[q], pv * AP.val[q]);
+                }
+            },
+            next.ptr, next.col, next.val);
+        for (int a2 = 0; a2 < na; a2++)   // Hermitian diagonal
+            for (int p = next.ptr[a2]; p < next.ptr[a2 + 1]; p++)
+                if (next.col[p] == a2) next.val[p] = cd(next.val[p].real(), 0.0);
+        HostCycleOps O;
+        if ((int)H.lv.size() >= first_ops) {
+            O.S.n = ln;
+            O.S.ptr = A.ptr;
+            O.S.col = A.col;
+            O.S.val.resize(A.val.size());
+#pragma omp parallel for schedule(static)
+            for (int i = 0; i < ln; i++)
+                for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) {
+                    const int j = A.col[p];
+                    cd v = -A.val[p] * (omega * L.dinv[j]);
+                    if (j == i) v += 2.0;
+                    O.S.val[p] = omega * L.dinv[i] * v;
+                }
+            O.P.n = ln;
+            build_rows_parallel<cd>(
+                ln, na,
+                [&](int i, auto add) {
+                    for (int q = Psa.ptr[i]; q < Psa.ptr[i + 1]; q++) add(Psa.col[q], alpha * Psa.val[q]);
+                    for (int q = AP.ptr[i]; q < AP.ptr[i + 1]; q++) add(AP.col[q], -alpha * omega * L.dinv[i] * AP.val[q]);
+                },
+                O.P.ptr, O.P.col, O.P.val);
+            O.R = hcsr_adjoint(O.P, na);
+            for (cd& v : O.R.val) v /= alpha;
+        }
+        H.ops.push_back(std::move(O));
         H.lv.push_back(std::move(L));
         cur = std::move(next);
     }
     if (cur.n > kCoarseMax) return false;
     H.nc = cur.n;
-    // cycle operators
-    using cd = std::complex<double>;
-    const double omega = kOmega, alpha = kAlpha;
-    H.ops.resize(H.lv.size());
-    for (size_t l = (size_t)std::max(first_ops, 0); l < H.lv.size(); l++) {
-        const HostLevel& L = H.lv[l];
-        const HostCsr& A = L.A;
-        const int n = A.n;
-        const int na = (int)L.mptr.size() - 1;
-        HostCycleOps& O = H.ops[l];
-        // S: same pattern as A
-        O.S.n = n;
-        O.S.ptr = A.ptr;
-        O.S.col = A.col;
-        O.S.val.resize(A.val.size());
-#pragma omp parallel for schedule(static)
-        for (int i = 0; i < n; i++)
-            for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) {
-                int j = A.col[p];
-                cd v = -A.val[p] * (omega * L.dinv[j]);
-                if (j == i) v += 2.0;
-                O.S.val[p] = omega * L.dinv[i] * v;
-            }
-        // P: row i -> aggregates of i and of its neighbours
-        O.P.n = n;
-        build_rows_parallel<cd>(
-            n, na,
-            [&](int i, auto add) {
-                add(L.agg[i], alpha * L.T[i]);
-                for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) {
-                    int j = A.col[p];
-                    add(L.agg[j], -alpha * omega * L.dinv[i] * A.val[p] * L.T[j]);
-                }
-            },
-            O.P.ptr, O.P.col, O.P.val);
-        // R = P^H / alpha
-        O.R.n = na;
-        O.R.ptr.assign(na + 1, 0);
-        for (int b : O.P.col) O.R.ptr[b + 1]++;
-        for (int a = 0; a < na; a++) O.R.ptr[a + 1] += O.R.ptr[a];
-        O.R.col.resize(O.P.col.size());
-        O.R.val.resize(O.P.col.size());
-        std::vector<int> fill(O.R.ptr.begin(), O.R.ptr.end() - 1);
-        for (int i = 0; i < n; i++)
-            for (int p = O.P.ptr[i]; p < O.P.ptr[i + 1]; p++) {
-                int a = O.P.col[p];
-                int q = fill[a]++;
-                O.R.col[q] = i;
-                O.R.val[q] = std::conj(O.P.val[p]) / alpha;
-            }
-    }
     H.Ainv.assign((size_t)cur.n * cur.n, 0.0);
     for (int i = 0; i < cur.n; i++)
         for (int p = cur.ptr[i]; p < cur.ptr[i + 1]; p++) H.Ainv[(size_t)i * cur.n + cur.col[p]] = cur.val[p];
+    for (int i = 0; i < cur.n; i++)   // Hermitian part (round-off of the Galerkin products)
+        for (int j = 0; j < i; j++) {
+            const cd m = 0.5 * (H.Ainv[(size_t)i * cur.n + j] + std::conj(H.Ainv[(size_t)j * cur.n + i]));
+            H.Ainv[(size_t)i * cur.n + j] = m;
+            H.Ainv[(size_t)j * cur.n + i] = std::conj(m);
+        }
     return hpd_inverse(H.Ainv, cur.n);
 }
 
@@ -379,7 +433,7 @@ struct DevLevel0 {
     const V2* t;         // T(k, agg k): transported near-null coefficient / sqrt|aggregate|
     const int* chunk;    // chunk starts, nchunk + 1 entries
     T dinv;              // 1 / diagonal (every row of a closed mesh has three neighbours)
-    T omega, alpha;
+    T omega, alpha, wp;  // smoothing weight, coarse-correction scale, prolongation smoothing
 };
 
 template <typename V2> __device__ __forceinline__ V2 cmulv(V2 a, V2 b) {

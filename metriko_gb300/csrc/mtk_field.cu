@@ -362,25 +362,41 @@ __device__ __forceinline__ T l0_direction_spmv(const ComplexEll<T>& A, T dg, con
     return pq;
 }
 
-// Level-0 phase B: r' = r - alpha q (own row and neighbours), and when `update` x += alpha p and
-// rn = r'.  Restriction r1[a] = sum over rows k of aggregate a of conj(T_k) (r'_k - omega/d
-// sum_j A_kj r'_j) (A_kk = d): one warp per chunk, inclusive segmented scan over the lanes of
-// each aggregate (fixed order), the last lane of an aggregate writes it.
+// sum over the three neighbours of A_kj x_j (the ELL off-diagonals of row k)
 template <typename T>
-__device__ __forceinline__ void l0_update_restrict(const ComplexEll<T>& A, const DevLevel0<T>& L0,
-                                                   const typename V2of<T>::type* r, const typename V2of<T>::type* q,
-                                                   T alpha, const typename V2of<T>::type* p,
-                                                   typename V2of<T>::type* x, typename V2of<T>::type* rn,
-                                                   typename V2of<T>::type* r1, bool update) {
+__device__ __forceinline__ void ell_offdiag(const ComplexEll<T>& A, int k, const typename V2of<T>::type* x, T& re,
+                                            T& im) {
     using V2 = typename V2of<T>::type;
-    const int n = A.n;
-    const int lane = threadIdx.x & 31;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    int c[3];
+    V2 a[3], xc[3];
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        c[j] = __ldg(A.nbr + j * A.n + k);
+        a[j] = __ldg(A.val + j * A.n + k);
+    }
+#pragma unroll
+    for (int j = 0; j < 3; j++) xc[j] = __ldcg(x + c[j]);
+    re = T(0);
+    im = T(0);
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        re += a[j].x * xc[j].x - a[j].y * xc[j].y;
+        im += a[j].x * xc[j].y + a[j].y * xc[j].x;
+    }
+}
+
+// Level-0 phase B: r' = r - alpha q (own row and neighbours), and when `update` x += alpha p and
+// rn = r'; s = (I - omega A / d) r' (the pre-smoothed residual, first factor of the restriction).
+template <typename T>
+__device__ __forceinline__ void l0_update_smooth(const ComplexEll<T>& A, const DevLevel0<T>& L0,
+                                                 const typename V2of<T>::type* r, const typename V2of<T>::type* q,
+                                                 T alpha, const typename V2of<T>::type* p,
+                                                 typename V2of<T>::type* x, typename V2of<T>::type* rn,
+                                                 typename V2of<T>::type* __restrict__ sv, bool update) {
+    using V2 = typename V2of<T>::type;
+    const int n = A.n, stride = gridDim.x * blockDim.x;
     const T od = L0.omega * L0.dinv, keep = T(1) - L0.omega;
-    for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < L0.nchunk; w += nwarps) {
-        const int beg = __ldg(L0.chunk + w), end = __ldg(L0.chunk + w + 1);
-        const bool act = beg + lane < end;
-        const int k = act ? beg + lane : beg;   // inactive lanes read a valid row, store nothing
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
         int c[3];
         V2 a[3], rc[3];
 #pragma unroll
@@ -388,8 +404,6 @@ __device__ __forceinline__ void l0_update_restrict(const ComplexEll<T>& A, const
             c[j] = __ldg(A.nbr + j * n + k);
             a[j] = __ldg(A.val + j * n + k);
         }
-        const int ag = act ? __ldg(L0.agg + k) : -1;
-        const V2 tk = __ldg(L0.t + k);
         V2 rk = __ldcg(r + k);
 #pragma unroll
         for (int j = 0; j < 3; j++) rc[j] = __ldcg(r + c[j]);
@@ -401,11 +415,9 @@ __device__ __forceinline__ void l0_update_restrict(const ComplexEll<T>& A, const
             rk = axpy2(-alpha, qk, rk);
 #pragma unroll
             for (int j = 0; j < 3; j++) rc[j] = axpy2(-alpha, qc[j], rc[j]);
-            if (act) {
-                const V2 pk = __ldcg(p + k), xk = __ldcg(x + k);
-                x[k] = axpy2(alpha, pk, xk);
-                rn[k] = rk;
-            }
+            const V2 pk = __ldcg(p + k), xk = __ldcg(x + k);
+            x[k] = axpy2(alpha, pk, xk);
+            rn[k] = rk;
         }
         T sr = keep * rk.x, si = keep * rk.y;
 #pragma unroll
@@ -413,7 +425,33 @@ __device__ __forceinline__ void l0_update_restrict(const ComplexEll<T>& A, const
             sr -= od * (a[j].x * rc[j].x - a[j].y * rc[j].y);
             si -= od * (a[j].x * rc[j].y + a[j].y * rc[j].x);
         }
-        T vx = act ? tk.x * sr + tk.y * si : T(0);   // conj(T_k) * s
+        V2 o;
+        o.x = sr;
+        o.y = si;
+        sv[k] = o;
+    }
+}
+
+// Level-0 phase C: s' = (I - w_p A / d) s and r1[a] = sum over the rows k of aggregate a of
+// conj(T_k) s'_k: one warp per chunk, inclusive segmented scan over the lanes of each aggregate
+// (fixed order), the last lane of an aggregate writes it.
+template <typename T>
+__device__ __forceinline__ void l0_restrict(const ComplexEll<T>& A, const DevLevel0<T>& L0,
+                                            const typename V2of<T>::type* sv, typename V2of<T>::type* r1) {
+    using V2 = typename V2of<T>::type;
+    const int lane = threadIdx.x & 31;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const T opd = L0.wp * L0.dinv, keep = T(1) - L0.wp;
+    for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < L0.nchunk; w += nwarps) {
+        const int beg = __ldg(L0.chunk + w), end = __ldg(L0.chunk + w + 1);
+        const bool act = beg + lane < end;
+        const int k = act ? beg + lane : beg;   // inactive lanes read a valid row, store nothing
+        const int ag = act ? __ldg(L0.agg + k) : -1;
+        const V2 tk = __ldg(L0.t + k), sk = __ldcg(sv + k);
+        T nr, ni;
+        ell_offdiag(A, k, sv, nr, ni);
+        const T sr = keep * sk.x - opd * nr, si = keep * sk.y - opd * ni;
+        T vx = act ? tk.x * sr + tk.y * si : T(0);   // conj(T_k) * s'
         T vy = act ? tk.x * si - tk.y * sr : T(0);
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -434,48 +472,81 @@ __device__ __forceinline__ void l0_update_restrict(const ComplexEll<T>& A, const
     }
 }
 
-// Level-0 up phase: z = S r + P y1, i.e. z_k = omega/d (2 r_k - sum_j A_kj w_j) + alpha T_k y1[agg k]
-// with w_j = omega/d r_j + alpha T_j y1[agg j] over j = k and its neighbours (A_kk = d).
-// Adds the partials Re r^H z and |r|^2.
+// Level-0 phase D: v = P_sa y1 = (I - w_p A / d) u with u_k = T_k y1[agg k].
 template <typename T>
-__device__ __forceinline__ void l0_smooth_prolong(const ComplexEll<T>& A, const DevLevel0<T>& L0, T dg,
-                                                  const typename V2of<T>::type* r, const typename V2of<T>::type* y1,
-                                                  typename V2of<T>::type* __restrict__ z, T& rz, T& rr) {
+__device__ __forceinline__ void l0_prolong(const ComplexEll<T>& A, const DevLevel0<T>& L0,
+                                           const typename V2of<T>::type* y1, typename V2of<T>::type* __restrict__ vv) {
     using V2 = typename V2of<T>::type;
     const int n = A.n, stride = gridDim.x * blockDim.x;
-    const T od = L0.omega * L0.dinv, al = L0.alpha;
+    const T opd = L0.wp * L0.dinv, keep = T(1) - L0.wp;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
         int c[3], ac[3];
-        V2 a[3], tc[3], rc[3], yc[3];
+        V2 a[3], tc[3], yc[3];
 #pragma unroll
         for (int j = 0; j < 3; j++) {
             c[j] = __ldg(A.nbr + j * n + k);
             a[j] = __ldg(A.val + j * n + k);
         }
         const int ak = __ldg(L0.agg + k);
-        const V2 tk = __ldg(L0.t + k), rk = __ldcg(r + k);
+        const V2 tk = __ldg(L0.t + k);
 #pragma unroll
         for (int j = 0; j < 3; j++) {
             ac[j] = __ldg(L0.agg + c[j]);
             tc[j] = __ldg(L0.t + c[j]);
-            rc[j] = __ldcg(r + c[j]);
         }
         const V2 yk = __ldcg(y1 + ak);
 #pragma unroll
         for (int j = 0; j < 3; j++) yc[j] = __ldcg(y1 + ac[j]);
-        const T tyx = tk.x * yk.x - tk.y * yk.y, tyy = tk.x * yk.y + tk.y * yk.x;
-        T sx = T(2) * rk.x - dg * (od * rk.x + al * tyx);
-        T sy = T(2) * rk.y - dg * (od * rk.y + al * tyy);
+        T sx = keep * (tk.x * yk.x - tk.y * yk.y), sy = keep * (tk.x * yk.y + tk.y * yk.x);
 #pragma unroll
         for (int j = 0; j < 3; j++) {
-            const T wx = od * rc[j].x + al * (tc[j].x * yc[j].x - tc[j].y * yc[j].y);
-            const T wy = od * rc[j].y + al * (tc[j].x * yc[j].y + tc[j].y * yc[j].x);
-            sx -= a[j].x * wx - a[j].y * wy;
-            sy -= a[j].x * wy + a[j].y * wx;
+            const T ux = tc[j].x * yc[j].x - tc[j].y * yc[j].y, uy = tc[j].x * yc[j].y + tc[j].y * yc[j].x;
+            sx -= opd * (a[j].x * ux - a[j].y * uy);
+            sy -= opd * (a[j].x * uy + a[j].y * ux);
+        }
+        V2 o;
+        o.x = sx;
+        o.y = sy;
+        vv[k] = o;
+    }
+}
+
+// Level-0 phase E: z = S r + alpha (I - omega A / d) v, i.e.
+// z_k = omega/d ((2 - omega) r_k - omega/d sum_j A_kj r_j) + alpha ((1 - omega) v_k - omega/d sum_j A_kj v_j)
+// over the three neighbours; adds the partials Re r^H z and |r|^2.
+template <typename T>
+__device__ __forceinline__ void l0_smooth_up(const ComplexEll<T>& A, const DevLevel0<T>& L0,
+                                             const typename V2of<T>::type* r, const typename V2of<T>::type* vv,
+                                             typename V2of<T>::type* __restrict__ z, T& rz, T& rr) {
+    using V2 = typename V2of<T>::type;
+    const int n = A.n, stride = gridDim.x * blockDim.x;
+    const T om = L0.omega, od = L0.omega * L0.dinv, al = L0.alpha;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+        int c[3];
+        V2 a[3], rc[3], vc[3];
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            c[j] = __ldg(A.nbr + j * n + k);
+            a[j] = __ldg(A.val + j * n + k);
+        }
+        const V2 rk = __ldcg(r + k), vk = __ldcg(vv + k);
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            rc[j] = __ldcg(r + c[j]);
+            vc[j] = __ldcg(vv + c[j]);
+        }
+        T sx = (T(2) - om) * rk.x, sy = (T(2) - om) * rk.y;
+        T ux = (T(1) - om) * vk.x, uy = (T(1) - om) * vk.y;
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            sx -= od * (a[j].x * rc[j].x - a[j].y * rc[j].y);
+            sy -= od * (a[j].x * rc[j].y + a[j].y * rc[j].x);
+            ux -= od * (a[j].x * vc[j].x - a[j].y * vc[j].y);
+            uy -= od * (a[j].x * vc[j].y + a[j].y * vc[j].x);
         }
         V2 zk;
-        zk.x = od * sx + al * tyx;
-        zk.y = od * sy + al * tyy;
+        zk.x = od * sx + al * ux;
+        zk.y = od * sy + al * uy;
         z[k] = zk;
         rz += rk.x * zk.x + rk.y * zk.y;
         rr += rk.x * rk.x + rk.y * rk.y;
@@ -483,9 +554,10 @@ __device__ __forceinline__ void l0_smooth_prolong(const ComplexEll<T>& A, const 
 }
 
 // PCG with the V-cycle preconditioner (status codes as pcg_complex).  Per iteration: phase A
-// (direction + SpMV), phase B (residual, solution, restriction), the inner cycle, the level-0 up
-// phase (z and the r^H z, |r|^2 partials): 2 nlev_inner + 4 grid barriers.  Residual and
-// direction are double-buffered (r0/r1, p0/p1) because neighbours recompute them.
+// (direction + SpMV), B (residual, solution, pre-smoothed residual), C (restriction), the inner
+// cycle, D (smoothed prolongation), E (post-smoothing, z and the r^H z, |r|^2 partials):
+// 2 nlev_inner + 6 grid barriers.  Residual and direction are double-buffered (r0/r1, p0/p1)
+// because neighbours recompute them; sv and vv hold the level-0 intermediates.
 template <typename T>
 __global__ void __launch_bounds__(kBlock, 1) pcg_complex_mg(ComplexEll<T> A, DevLevel0<T> L0, T dg,
                                                         const DevHierarchy<T>* __restrict__ Hp,
@@ -493,7 +565,8 @@ __global__ void __launch_bounds__(kBlock, 1) pcg_complex_mg(ComplexEll<T> A, Dev
                                                         typename V2of<T>::type* x, typename V2of<T>::type* r0,
                                                         typename V2of<T>::type* r1, typename V2of<T>::type* z,
                                                         typename V2of<T>::type* p0, typename V2of<T>::type* p1,
-                                                        typename V2of<T>::type* q, T* partials, GridBarrier bar,
+                                                        typename V2of<T>::type* q, typename V2of<T>::type* sv,
+                                                        typename V2of<T>::type* vv, T* partials, GridBarrier bar,
                                                         double tol2, int maxit, int* out) {
     using V2 = typename V2of<T>::type;
     const DevHierarchy<T>& H = *Hp;
@@ -517,12 +590,16 @@ __global__ void __launch_bounds__(kBlock, 1) pcg_complex_mg(ComplexEll<T> A, Dev
         rcur[i] = ri;
     }
     if (!grid_sync(bar)) { status = 5; goto done; }
-    l0_update_restrict<T>(A, L0, rcur, nullptr, T(0), nullptr, nullptr, nullptr, rl1, false);
+    l0_update_smooth<T>(A, L0, rcur, nullptr, T(0), nullptr, nullptr, nullptr, sv, false);
+    if (!grid_sync(bar)) { status = 5; goto done; }
+    l0_restrict<T>(A, L0, sv, rl1);
     if (!grid_sync(bar)) { status = 5; goto done; }
     if (!vcycle_inner(H, bar)) { status = 5; goto done; }
+    l0_prolong<T>(A, L0, yl1, vv);
+    if (!grid_sync(bar)) { status = 5; goto done; }
     red2[0] = T(0);
     red2[1] = T(0);
-    l0_smooth_prolong<T>(A, L0, dg, rcur, yl1, z, red2[0], red2[1]);
+    l0_smooth_up<T>(A, L0, rcur, vv, z, red2[0], red2[1]);
     publish_partials<T, 2>(red2, partials);
     if (!grid_sync(bar)) { status = 5; goto done; }
     gather_partials<T, 2>(partials, red2);
@@ -542,17 +619,21 @@ __global__ void __launch_bounds__(kBlock, 1) pcg_complex_mg(ComplexEll<T> A, Dev
             const T pq = red1[0];
             if (!(pq > T(0))) { status = 4; break; }
             const T alpha = rz / pq;
-            l0_update_restrict<T>(A, L0, rcur, q, alpha, pw, x, rnext, rl1, true);
+            l0_update_smooth<T>(A, L0, rcur, q, alpha, pw, x, rnext, sv, true);
             if (!grid_sync(bar)) { status = 5; break; }
             {
                 V2* tmp = rcur;
                 rcur = rnext;
                 rnext = tmp;
             }
+            l0_restrict<T>(A, L0, sv, rl1);
+            if (!grid_sync(bar)) { status = 5; break; }
             if (!vcycle_inner(H, bar)) { status = 5; break; }
+            l0_prolong<T>(A, L0, yl1, vv);
+            if (!grid_sync(bar)) { status = 5; break; }
             red2[0] = T(0);
             red2[1] = T(0);
-            l0_smooth_prolong<T>(A, L0, dg, rcur, yl1, z, red2[0], red2[1]);
+            l0_smooth_up<T>(A, L0, rcur, vv, z, red2[0], red2[1]);
             publish_partials<T, 2>(red2, partials + 3 * gridDim.x);
             if (!grid_sync(bar)) { status = 5; break; }
             gather_partials<T, 2>(partials + 3 * gridDim.x, red2);
@@ -809,8 +890,8 @@ struct FieldSolver {
     // level 0 (applied from the ELL rows): rows renumbered by aggregate, perm[new] = old
     std::vector<int> perm;
     DBuf<int> agg0, chunk0;
-    DBuf<double2> t064, rb64, pb64;
-    DBuf<float2> t032, rb32, pb32;
+    DBuf<double2> t064, rb64, pb64, sv64, vv64;
+    DBuf<float2> t032, rb32, pb32, sv32, vv32;
     DevLevel0<double> L064{};
     DevLevel0<float> L032{};
     bool amg = false;
@@ -882,8 +963,9 @@ struct FieldSolver {
         }
         const int nchunk = (int)chunk.size() - 1;
         const double dg = 3.0 + 1e-9;
-        L064 = DevLevel0<double>{nagg, nchunk, agg0.p, t064.p, chunk0.p, 1.0 / dg, kOmega, kAlpha};
-        L032 = DevLevel0<float>{nagg, nchunk, agg0.p, t032.p, chunk0.p, (float)(1.0 / dg), (float)kOmega, (float)kAlpha};
+        L064 = DevLevel0<double>{nagg, nchunk, agg0.p, t064.p, chunk0.p, 1.0 / dg, kOmega, kAlpha, L0.wp};
+        L032 = DevLevel0<float>{nagg, nchunk, agg0.p, t032.p, chunk0.p, (float)(1.0 / dg), (float)kOmega, (float)kAlpha,
+                                (float)L0.wp};
         // lanes per row of a CSR phase: fewest rounds x dependent loads (ptr, then batches of four
         // entries per lane, each a column load and a gather) over the persistent grid
         const double threads = (double)c->num_sms * kBlock;
@@ -972,7 +1054,7 @@ struct FieldSolver {
     // second residual and direction buffers of the multigrid kernel.
     template <typename T, typename V2>
     int pcg(ComplexEll<T> A, const T* minv, const V2* bb, V2* xx, V2* rr, V2* zz, V2* pp, V2* qq, V2* rb, V2* pb,
-            double tol2, int maxit, long long* iters, double* final_rr) {
+            V2* sb, V2* vb, double tol2, int maxit, long long* iters, double* final_rr) {
         int g = 0;
         MTK_TRY(reset_barrier(c));
         MTK_CUDA_TRY(cudaEventRecord(c->ev_k0, c->stream));
@@ -983,7 +1065,7 @@ struct FieldSolver {
             const DevHierarchy<T>* Hc = Hd;
             const DevLevel0<T> L0 = level0<T>();
             const T dg = (T)(3.0 + 1e-9);
-            MTK_TRY(launch_persistent(c, pcg_complex_mg<T>, &g, A, L0, dg, Hc, bb, xx, rr, rb, zz, pp, pb, qq,
+            MTK_TRY(launch_persistent(c, pcg_complex_mg<T>, &g, A, L0, dg, Hc, bb, xx, rr, rb, zz, pp, pb, qq, sb, vb,
                                       reinterpret_cast<T*>(c->partials), barrier_of(c), tol2, maxit, c->dev_int));
         } else {
             MTK_TRY(launch_persistent(c, pcg_complex<T>, &g, A, minv, bb, xx, rr, zz, pp, qq,
@@ -998,12 +1080,12 @@ struct FieldSolver {
         pcg_launches++;
         // algorithmic bytes per iteration and row.  Jacobi: SpMV 3*(2T+4) + T + 2*2T, x/r/p
         // updates 3*3*2T, z = M^-1 r T + 2T.  Multigrid, level 0 from the ELL rows (3*(2T+4) per
-        // pass): direction + SpMV z, p_old in, p, q out (8T); update + restriction r, q, p, x
-        // in, x, r out (12T) + agg + T_k (4 + 2T); up phase r in, z out (4T) + agg + T_k; plus the
-        // inner cycle (counted in build_amg)
+        // pass, five passes): A z, p_old in, p, q out (8T); B r, q, p, x in, x, r, s out (14T);
+        // C s in + agg + T_k (2T + 4 + 2T); D agg + T_k, v out (4 + 4T); E r, v in, z out (6T);
+        // plus the inner cycle (counted in build_amg)
         const double T_ = (double)sizeof(T);
         const double ell = 3.0 * (2 * T_ + 4);
-        const double per_row = amg ? 3 * ell + 8 * T_ + 12 * T_ + 2 * (4 + 2 * T_) + 4 * T_
+        const double per_row = amg ? 5 * ell + 8 * T_ + 14 * T_ + (4 + 4 * T_) + (4 + 4 * T_) + 6 * T_
                                    : ell + T_ + 4.0 * T_ + 18.0 * T_ + 3.0 * T_;
         const double cyc = amg ? (sizeof(T) == 8 ? vcycle_bytes64 : vcycle_bytes32) : 0.0;
         pcg_bytes += (per_row * (double)n + cyc) * (double)(c->h_int[1] + 1);
@@ -1094,10 +1176,10 @@ extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const 
     const bool mixed = opts.precision == MTK_PREC_MIXED;
     if (mixed) {
         MTK_TRY(S.r32.alloc(n)); MTK_TRY(S.e32.alloc(n)); MTK_TRY(S.z32.alloc(n)); MTK_TRY(S.p32.alloc(n)); MTK_TRY(S.q32.alloc(n));
-        if (S.amg) { MTK_TRY(S.rb32.alloc(n)); MTK_TRY(S.pb32.alloc(n)); }
+        if (S.amg) { MTK_TRY(S.rb32.alloc(n)); MTK_TRY(S.pb32.alloc(n)); MTK_TRY(S.sv32.alloc(n)); MTK_TRY(S.vv32.alloc(n)); }
     } else {
         MTK_TRY(S.z64.alloc(n)); MTK_TRY(S.p64.alloc(n)); MTK_TRY(S.q64.alloc(n));
-        if (S.amg) { MTK_TRY(S.rb64.alloc(n)); MTK_TRY(S.pb64.alloc(n)); }
+        if (S.amg) { MTK_TRY(S.rb64.alloc(n)); MTK_TRY(S.pb64.alloc(n)); MTK_TRY(S.sv64.alloc(n)); MTK_TRY(S.vv64.alloc(n)); }
     }
     const int G = stream_grid(c);
     field_assemble<<<G, kStream, 0, st>>>(n, nRosy, S.nbr_in.p, S.theta.p, S.area.p, S.nbr.p, S.v64.p, S.v32.p, S.d64.p,
@@ -1169,7 +1251,7 @@ extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const 
         if (!mixed) {
             double frr = 0;
             int s = S.pcg<double, double2>(S.A64(), S.inv64.p, S.b.p, S.x.p, S.r.p, S.z64.p, S.p64.p, S.q64.p, S.rb64.p,
-                                           S.pb64.p, goal2,
+                                           S.pb64.p, S.sv64.p, S.vv64.p, goal2,
                                            opts.max_iter, &iters, &frr);
             if (s != MTK_OK) return s;
             // true FP64 residual of the result
@@ -1192,7 +1274,7 @@ extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const 
                 c->kernels++;
                 int s = S.pcg<float, float2>(S.A32(), S.inv32.p, S.r32.p, S.e32.p, S.z32.p /*r*/, S.p32.p /*z*/,
                                              S.q32.p /*p*/, reinterpret_cast<float2*>(S.Lu.p) /*q*/, S.rb32.p, S.pb32.p,
-                                             itol * itol * rr,
+                                             S.sv32.p, S.vv32.p, itol * itol * rr,
                                              opts.max_iter, &iters, nullptr);
                 if (s == MTK_ERR_TIMEOUT || s == MTK_ERR_BREAKDOWN) return s;
                 add_correction<<<G, kStream, 0, st>>>(n, S.e32.p, S.x.p);
