@@ -156,31 +156,55 @@ namespace metriko {
         int nonZeros() const { return static_cast<int>(idx.size()); }
         void resize(int rows, int cols) { nr = rows; nc = cols; ptr.assign(rows + 1, 0); idx.clear(); val.clear(); }
 
-        // Duplicates are summed (Eigen setFromTriplets semantics).
+        // Duplicates are summed in input order (Eigen setFromTriplets semantics).  Stable scatter
+        // by row, then every row is sorted by column (stable) and merged in parallel.
         template <typename It>
         void setFromTriplets(It b, It e) {
-            ptr.assign(nr + 1, 0);
+            std::vector<int> cnt(nr + 1, 0);
             size_t n = 0;
-            for (It it = b; it != e; ++it) { ptr[it->r + 1]++; n++; }
-            for (int i = 0; i < nr; i++) ptr[i + 1] += ptr[i];
+            for (It it = b; it != e; ++it) { cnt[it->r + 1]++; n++; }
+            for (int i = 0; i < nr; i++) cnt[i + 1] += cnt[i];
             std::vector<int> ci(n);
             std::vector<T> cv(n);
-            std::vector<int> fill(ptr.begin(), ptr.end() - 1);
-            for (It it = b; it != e; ++it) { int p = fill[it->r]++; ci[p] = it->c; cv[p] = it->v; }
-            idx.clear(); val.clear();
-            std::vector<int> nptr(nr + 1, 0);
-            std::vector<std::pair<int, T>> rowbuf;
-            for (int i = 0; i < nr; i++) {
-                rowbuf.clear();
-                for (int p = ptr[i]; p < ptr[i + 1]; p++) rowbuf.emplace_back(ci[p], cv[p]);
-                std::stable_sort(rowbuf.begin(), rowbuf.end(), [](auto& a, auto& b2) { return a.first < b2.first; });
-                for (size_t k = 0; k < rowbuf.size(); k++) {
-                    if (!idx.empty() && int(idx.size()) > nptr[i] && idx.back() == rowbuf[k].first) val.back() += rowbuf[k].second;
-                    else { idx.push_back(rowbuf[k].first); val.push_back(rowbuf[k].second); }
-                }
-                nptr[i + 1] = static_cast<int>(idx.size());
+            {
+                std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+                for (It it = b; it != e; ++it) { int p = fill[it->r]++; ci[p] = it->c; cv[p] = it->v; }
             }
-            ptr = std::move(nptr);
+            std::vector<int> ucnt(nr + 1, 0);
+            METRIKO_PARALLEL_FOR
+            for (int i = 0; i < nr; i++) {
+                const int b0 = cnt[i], e0 = cnt[i + 1], k = e0 - b0;
+                if (k > 32) {
+                    std::vector<std::pair<int, T>> rb(k);
+                    for (int q = 0; q < k; q++) rb[q] = {ci[b0 + q], cv[b0 + q]};
+                    std::stable_sort(rb.begin(), rb.end(), [](const auto& x, const auto& y) { return x.first < y.first; });
+                    for (int q = 0; q < k; q++) { ci[b0 + q] = rb[q].first; cv[b0 + q] = rb[q].second; }
+                } else {
+                    for (int q = b0 + 1; q < e0; q++) {   // insertion sort (stable)
+                        const int c = ci[q];
+                        const T v = cv[q];
+                        int r = q - 1;
+                        while (r >= b0 && ci[r] > c) { ci[r + 1] = ci[r]; cv[r + 1] = cv[r]; r--; }
+                        ci[r + 1] = c;
+                        cv[r + 1] = v;
+                    }
+                }
+                int u = 0;
+                for (int q = b0; q < e0; q++) if (q == b0 || ci[q] != ci[q - 1]) u++;
+                ucnt[i + 1] = u;
+            }
+            for (int i = 0; i < nr; i++) ucnt[i + 1] += ucnt[i];
+            idx.assign(ucnt[nr], 0);
+            val.assign(ucnt[nr], T(0));
+            METRIKO_PARALLEL_FOR
+            for (int i = 0; i < nr; i++) {
+                int o = ucnt[i] - 1;
+                for (int q = cnt[i]; q < cnt[i + 1]; q++) {
+                    if (q == cnt[i] || ci[q] != ci[q - 1]) { o++; idx[o] = ci[q]; val[o] = cv[q]; }
+                    else val[o] += cv[q];
+                }
+            }
+            ptr = std::move(ucnt);
         }
         // Removes entries with |v| <= |reference| * epsilon (Eigen prune semantics).
         void prune(double reference, double epsilon = 1e-12) {

@@ -218,6 +218,7 @@ namespace metriko {
         crnr2half.assign(nC, -1);
         next.assign(nH, -1); prev.assign(nH, -1); twin.resize(nH); tail.resize(nH);
         head.resize(nH); edge.resize(nH); face.resize(nH); crnr.assign(nH, -1);
+        METRIKO_PARALLEL_FOR
         for (int e = 0; e < nE; e++) {
             tail[2 * e] = edge2vert(e, 0);
             tail[2 * e + 1] = edge2vert(e, 1);
@@ -227,7 +228,9 @@ namespace metriko {
             twin[2 * e + 1] = 2 * e;
             edge[2 * e] = edge[2 * e + 1] = e;
             edge2half[e] = 2 * e;
-            vert2half[edge2vert(e, 0)] = 2 * e;       // last write wins (dcel, hmesh.h:314-323)
+        }
+        for (int e = 0; e < nE; e++) {                // last write wins (dcel, hmesh.h:314-323)
+            vert2half[edge2vert(e, 0)] = 2 * e;
             vert2half[edge2vert(e, 1)] = 2 * e + 1;
         }
         for (int v = 0; v < nV; v++) if (vert2half[v] < 0) throw std::invalid_argument("isolated vertex");
@@ -254,10 +257,17 @@ namespace metriko {
         }
         METRIKO_PARALLEL_FOR
         for (int h = 0; h < nH; h++) head[h] = tail[next[h]];
-        for (int i = 0; i < nF; i++) faces.push_back(Face{{i, this}});
-        for (int i = 0; i < nV; i++) verts.push_back(Vert{{i, this}});
-        for (int i = 0; i < nE; i++) edges.push_back(Edge{{i, this}});
-        for (int i = 0; i < nH; i++) halfs.push_back(Half{{i, this}});
+        faces.resize(nF);
+        verts.resize(nV);
+        edges.resize(nE);
+        halfs.resize(nH);
+        METRIKO_PARALLEL_FOR
+        for (int i = 0; i < nH; i++) {
+            halfs[i] = Half{{i, this}};
+            if (i < nF) faces[i] = Face{{i, this}};
+            if (i < nV) verts[i] = Vert{{i, this}};
+            if (i < nE) edges[i] = Edge{{i, this}};
+        }
 
         faceBasisX = MatXd(nF, 3); faceBasisY = MatXd(nF, 3); faceNormal = MatXd(nF, 3); baryCenter = MatXd(nF, 3);
         faceArea = VecXd(nF); heArgOnFace = VecXd(nH); angleDefect = VecXd(nV);

@@ -38,27 +38,43 @@ namespace metriko {
         auto cm = std::make_unique<CutMesh>();
         cm->nF = m.nF;
         cm->idx = MatXi(m.nF, 3, -1);
-        std::vector<int> cut2raw;
+        // copies are numbered vertex by vertex in ascending order, so the count pass, a prefix
+        // sum and an assignment pass (both parallel over vertices) give the serial numbering
+        std::vector<int> bgn(m.nV), base(m.nV + 1, 0);
+        METRIKO_PARALLEL_FOR
         for (int v = 0; v < m.nV; v++) {
-            int bgn = m.vert2half[v];
+            int b = m.vert2half[v];
             {   // first seam halfedge in cw order from v.half()
-                int h0 = bgn, h = h0;
+                int h0 = b, h = h0;
                 do {
-                    if (seam[m.edge[h]]) { bgn = h; break; }
+                    if (seam[m.edge[h]]) { b = h; break; }
                     h = m.next[m.twin[h]];
                 } while (h != h0);
             }
-            int h = bgn;
+            bgn[v] = b;
+            int cnt = 0, h = b;
             do {
-                if (seam[m.edge[h]] || h == bgn) cut2raw.push_back(v);
-                int f = m.face[h];
-                for (int j = 0; j < 3; j++) if (m.idx(f, j) == v) cm->idx(f, j) = int(cut2raw.size()) - 1;
+                if (seam[m.edge[h]] || h == b) cnt++;
                 h = m.twin[m.prev[h]];
-            } while (h != bgn);
+            } while (h != b);
+            base[v + 1] = cnt;
         }
-        cm->nV = int(cut2raw.size());
+        for (int v = 0; v < m.nV; v++) base[v + 1] += base[v];
+        cm->nV = base[m.nV];
         cm->pos = MatXd(cm->nV, 3);
-        for (int i = 0; i < cm->nV; i++) for (int k = 0; k < 3; k++) cm->pos(i, k) = m.pos(cut2raw[i], k);
+        METRIKO_PARALLEL_FOR
+        for (int v = 0; v < m.nV; v++) {
+            int c = base[v] - 1, h = bgn[v];
+            do {
+                if (seam[m.edge[h]] || h == bgn[v]) {
+                    c++;
+                    for (int k = 0; k < 3; k++) cm->pos(c, k) = m.pos(v, k);
+                }
+                const int f = m.face[h];
+                for (int j = 0; j < 3; j++) if (m.idx(f, j) == v) cm->idx(f, j) = c;
+                h = m.twin[m.prev[h]];
+            } while (h != bgn[v]);
+        }
         return cm;
     }
 
@@ -205,24 +221,24 @@ namespace metriko {
                     if (mat(i, j) != 0) T.emplace_back(r0 + i, c0 + j, double(mat(i, j)));
         };
         int currConstraint = 0;
-        vT.reserve(size_t(N) * cut.nV + 64);
-        for (int v = 0; v < raw.nV; v++) {       // setup.ipp:66-124
-            {   // vertices away from the seam: one cut copy, identity block, no constraint
-                const int g0 = raw.vert2half[v];
-                int g = g0;
-                bool onSeam = false;
-                do {
-                    if (seam[raw.edge[g]]) { onSeam = true; break; }
-                    g = raw.twin[raw.prev[g]];
-                } while (g != g0);
-                if (!onSeam) {
-                    const int f = raw.face[g0];
-                    int jVcut = -1;
-                    for (int j = 0; j < 3; j++) if (raw.idx(f, j) == v) jVcut = cut.idx(f, j);
-                    for (int i = 0; i < N; i++) vT.emplace_back(N * jVcut + i, N * v + i, 1.0);
-                    continue;
-                }
-            }
+        // vertices away from the seam: one cut copy, identity block, no constraint (found in
+        // parallel; their rows of vtrans2cut are written directly below)
+        std::vector<int> plainCut(raw.nV, -1);
+        METRIKO_PARALLEL_FOR
+        for (int v = 0; v < raw.nV; v++) {
+            const int g0 = raw.vert2half[v];
+            int g = g0;
+            bool onSeam = false;
+            do {
+                if (seam[raw.edge[g]]) { onSeam = true; break; }
+                g = raw.twin[raw.prev[g]];
+            } while (g != g0);
+            if (onSeam) continue;
+            const int f = raw.face[g0];
+            for (int j = 0; j < 3; j++) if (raw.idx(f, j) == v) plainCut[v] = cut.idx(f, j);
+        }
+        for (int v = 0; v < raw.nV; v++) {       // setup.ipp:66-124, vertices on the seam
+            if (plainCut[v] >= 0) continue;
             std::vector<MatXi> pm{I};
             std::vector<int> pidx{v};
             int iVcut = -1;
@@ -267,19 +283,59 @@ namespace metriko {
                 currConstraint++;
             }
         }
-        vtrans2cut = SprsD(N * cut.nV, N * nR);
-        vtrans2cut.setFromTriplets(vT.begin(), vT.end());
-        vtrans2cut.prune(1e-3);
+        {   // vtrans2cut: seam rows from their triplets (summed, pruned), the other rows one 1 each
+            SprsD seamRows(N * cut.nV, N * nR);
+            seamRows.setFromTriplets(vT.begin(), vT.end());
+            seamRows.prune(1e-3);
+            std::vector<int> plainRow(N * (size_t)cut.nV, -1);   // row -> column of its single 1
+            METRIKO_PARALLEL_FOR
+            for (int v = 0; v < raw.nV; v++)
+                if (plainCut[v] >= 0)
+                    for (int i = 0; i < N; i++) plainRow[(size_t)N * plainCut[v] + i] = N * v + i;
+            const int rows = N * cut.nV;
+            vtrans2cut = SprsD(rows, N * nR);
+            std::vector<int>& vp = vtrans2cut.ptr;
+            for (int r = 0; r < rows; r++)
+                vp[r + 1] = vp[r] + (plainRow[r] >= 0 ? 1 : seamRows.ptr[r + 1] - seamRows.ptr[r]);
+            vtrans2cut.idx.resize(vp[rows]);
+            vtrans2cut.val.resize(vp[rows]);
+            METRIKO_PARALLEL_FOR
+            for (int r = 0; r < rows; r++) {
+                int o = vp[r];
+                if (plainRow[r] >= 0) { vtrans2cut.idx[o] = plainRow[r]; vtrans2cut.val[o] = 1.0; continue; }
+                for (int q = seamRows.ptr[r]; q < seamRows.ptr[r + 1]; q++, o++) {
+                    vtrans2cut.idx[o] = seamRows.idx[q];
+                    vtrans2cut.val[o] = seamRows.val[q];
+                }
+            }
+        }
         constraint = SprsD(N * currConstraint, N * nR);
         constraint.setFromTriplets(cT.begin(), cT.end());
         constraint.prune(1e-3);
-        std::vector<TripD> buff;
-        for (int i = 0; i < N * nR; i += N)
-            for (int a = 0; a < N; a++)
-                for (int b = 0; b < n; b++)
-                    if (lreductor(a, b) != 0) buff.emplace_back(i + a, i * n / N + b, double(lreductor(a, b)));
-        uncompress = SprsD(N * nR, n * nR);
-        uncompress.setFromTriplets(buff.begin(), buff.end());
+        {   // uncompress: block-diagonal copies of lreductor (at most one entry per row)
+            uncompress = SprsD(N * nR, n * nR);
+            std::vector<int> rc(N), rv(N);
+            for (int a = 0; a < N; a++) {
+                rc[a] = -1;
+                for (int b2 = 0; b2 < n; b2++)
+                    if (lreductor(a, b2) != 0) {
+                        if (rc[a] >= 0) throw std::runtime_error("lreductor row with two entries");
+                        rc[a] = b2;
+                        rv[a] = lreductor(a, b2);
+                    }
+            }
+            std::vector<int>& up = uncompress.ptr;
+            for (int i = 0; i < N * nR; i++) up[i + 1] = up[i] + (rc[i % N] >= 0 ? 1 : 0);
+            uncompress.idx.resize(up[N * nR]);
+            uncompress.val.resize(up[N * nR]);
+            METRIKO_PARALLEL_FOR
+            for (int i = 0; i < N * nR; i++) {
+                const int a = i % N;
+                if (rc[a] < 0) continue;
+                uncompress.idx[up[i]] = (i - a) * n / N + rc[a];
+                uncompress.val[up[i]] = double(rv[a]);
+            }
+        }
 
         fixedIdcs = VecXi(n);
         if (nS == 0) {

@@ -276,6 +276,39 @@ namespace metriko {
                     for (int s = 0; s < 3; s++)
                         if (seams(f, s)) { vpos[fill[F(f, s)]++] = 3 * f + s; vpos[fill[F(f, (s + 1) % 3)]++] = 3 * f + s; }
             }
+            // Leaf pruning reaches the same fixed point in any order (what is left is the unique
+            // subgraph without degree-1 vertices), and the reference's pass loop stops only at that
+            // fixed point unless it hits its pass cap (10001 passes).  Every pass removes at least
+            // all edges that are leaves when it starts, so the number of passes is at most the
+            // depth of simultaneous peeling: when that depth is within the cap the fixed point is
+            // the answer, computed here in O(E); otherwise the passes are simulated exactly below.
+            {
+                std::vector<int> deg(e);
+                MatXi pruned = seams;
+                std::vector<int> layer, next_layer;
+                for (int v = 0; v < m.nV; v++) if (deg[v] == 1) layer.push_back(v);
+                int depth = 0;
+                while (!layer.empty() && depth <= 10000) {
+                    depth++;
+                    next_layer.clear();
+                    for (int v : layer) {
+                        if (deg[v] != 1) continue;
+                        for (int k = vptr[v]; k < vptr[v + 1]; k++) {
+                            const int qp = vpos[k], f = qp / 3, s2 = qp % 3;
+                            if (!pruned(f, s2)) continue;
+                            const int a = F(f, s2), b = F(f, (s2 + 1) % 3), w = a == v ? b : a;
+                            pruned(f, s2) = 0;
+                            pruned(TT(f, s2), TTi(f, s2)) = 0;
+                            deg[v]--;
+                            deg[w]--;
+                            if (deg[w] == 1) next_layer.push_back(w);
+                            break;
+                        }
+                    }
+                    layer.swap(next_layer);
+                }
+                if (layer.empty()) return pruned;
+            }
             auto leaf_edge = [&](int p) { int f = p / 3, s = p % 3; return e[F(f, s)] == 1 || e[F(f, (s + 1) % 3)] == 1; };
             std::priority_queue<int, std::vector<int>, std::greater<int>> cur;
             for (int f = 0; f < nF; f++)
@@ -351,33 +384,33 @@ namespace metriko {
                 ncut = 1;
                 continue;
             }
-            // unit-weight Dijkstra; pops ordered by (distance, id)
+            // unit-weight Dijkstra with pops ordered by (distance, id), run as a breadth-first
+            // search whose levels are visited in ascending id: the same pop order, and every vertex
+            // keeps as predecessor the first popped neighbour that reached it
             for (int v : touched) { dist[v] = -1; prev[v] = -1; }
             touched.clear();
-            std::priority_queue<std::pair<int, int>, std::vector<std::pair<int, int>>, std::greater<>> pq;
             dist[src] = 0;
             touched.push_back(src);
-            pq.emplace(0, src);
+            std::vector<int> level{src}, nlevel;
             int found = -1;
-            while (!pq.empty()) {
-                auto [d, u] = pq.top();
-                pq.pop();
-                if (d > dist[u]) continue;
-                if (in_cut[u]) { found = u; break; }
-                // neighbours of u: the other corners of its faces (order is irrelevant)
-                for (int k = fptr[u]; k < fptr[u + 1]; k++) {
-                    int f = vf[k];
-                    for (int j = 0; j < 3; j++) {
-                        int w = F(f, j);
-                        if (w == u) continue;
-                        if (dist[w] < 0 || d + 1 < dist[w]) {
-                            if (dist[w] < 0) touched.push_back(w);
+            for (int d = 0; !level.empty() && found < 0; d++) {
+                std::sort(level.begin(), level.end());
+                nlevel.clear();
+                for (int u : level) {
+                    if (in_cut[u]) { found = u; break; }
+                    for (int k = fptr[u]; k < fptr[u + 1]; k++) {
+                        const int f = vf[k];
+                        for (int j = 0; j < 3; j++) {
+                            const int w = F(f, j);
+                            if (w == u || dist[w] >= 0) continue;
                             dist[w] = d + 1;
                             prev[w] = u;
-                            pq.emplace(d + 1, w);
+                            touched.push_back(w);
+                            nlevel.push_back(w);
                         }
                     }
                 }
+                level.swap(nlevel);
             }
             std::vector<int> path;
             if (found == -1) path.push_back(src);

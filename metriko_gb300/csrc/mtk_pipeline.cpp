@@ -127,28 +127,44 @@ extern "C" int mtk_topology_from_field(int32_t nV, int32_t nF, const double* Vb,
                                        int32_t* singular, int32_t* matching, uint8_t* seam_out, int32_t* cutF,
                                        int32_t* counts, double* length) {
     if (nV <= 0 || nF <= 0 || !Vb || !Fb || !compressed) return MTK_ERR_BAD_INPUT;
+    using clk = std::chrono::steady_clock;
+    const bool dbg = getenv("MTK_DEBUG") && getenv("MTK_DEBUG")[0] == '1';
+    auto ts = clk::now();
+    auto stamp = [&](const char* what) {
+        auto b = clk::now();
+        if (dbg) fprintf(stderr, "[host] %-22s %8.1f ms\n", what, std::chrono::duration<double, std::milli>(b - ts).count());
+        ts = b;
+    };
     try {
         MatXd V(nV, 3);
         MatXi F(nF, 3);
         std::memcpy(V.data(), Vb, sizeof(double) * 3 * size_t(nV));
         std::memcpy(F.data(), Fb, sizeof(int32_t) * 3 * size_t(nF));
         auto mesh = std::make_unique<Hmesh>(V, F);
+        stamp("hmesh");
         FaceRosyField rawf(*mesh, 4);
         rawf.compressed = VecXc(nF);
         for (int f = 0; f < nF; f++) rawf.compressed[f] = complex(compressed[2 * f], compressed[2 * f + 1]);
         rawf.set_field_from_compressed();
         rawf.computeMatching(MatchingType::Curl);
+        stamp("matching+singular");
         if (singular) std::memcpy(singular, rawf.singular.data(), sizeof(int32_t) * nV);
         auto seam = compute_seam(rawf);
+        stamp("seam");
         auto cutm = compute_cut_mesh(*mesh, seam);
+        stamp("cut mesh");
         auto cmbf = compute_combbed_field(rawf, seam);
         MatXd extf = compute_extrinsic_field(*mesh, *cmbf, 4);
+        stamp("combing+extrinsic");
         RosyParameterization rp(*mesh, *cutm, extf, cmbf->singular, cmbf->matching, seam, 4, ratio);
         rp.seamless = true;
         rp.roundSeams = round_seams != 0;
+        stamp("transitions");
         rp.setup();
+        stamp("setup");
         IntegSystem sys;
         rp.build_system(sys);
+        stamp("integ build_system");
         if (matching) std::memcpy(matching, cmbf->matching.data(), sizeof(int32_t) * mesh->nE);
         if (seam_out) for (int e = 0; e < mesh->nE; e++) seam_out[e] = seam[e] ? 1 : 0;
         if (cutF) std::memcpy(cutF, cutm->idx.data(), sizeof(int32_t) * 3 * size_t(nF));
