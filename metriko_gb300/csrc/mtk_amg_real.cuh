@@ -452,7 +452,7 @@ __device__ __forceinline__ T rcsr_row(const RDevCsr<T>& M, int row, int lane, in
 // spread over groups of M.group lanes (1..32) with a warp-uniform loop and fixed-order reduction.
 template <typename T>
 __device__ void rcsr_phase(const RDevCsr<T>& M, const T* x, const RDevCsr<T>* M2, const T* x2, T* out, T scale,
-                           const unsigned char* mask) {
+                           const unsigned char* mask, T* xdot = nullptr) {
     const int stride = gridDim.x * blockDim.x;
     const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
     const int g = M.group;
@@ -460,7 +460,9 @@ __device__ void rcsr_phase(const RDevCsr<T>& M, const T* x, const RDevCsr<T>* M2
         for (int row = t0; row < M.n; row += stride) {
             T s = rcsr_row(M, row, 0, 1, x);
             if (M2) s += rcsr_row(*M2, row, 0, 1, x2);
-            out[row] = (mask && mask[row]) ? T(0) : scale * s;
+            const T o = (mask && mask[row]) ? T(0) : scale * s;
+            out[row] = o;
+            if (xdot) *xdot += __ldcg(x + row) * o;
         }
         return;
     }
@@ -473,13 +475,19 @@ __device__ void rcsr_phase(const RDevCsr<T>& M, const T* x, const RDevCsr<T>* M2
             if (M2) s += rcsr_row(*M2, row, sl, g, x2);
         }
         for (int o = g >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (sl == 0 && row < M.n) out[row] = (mask && mask[row]) ? T(0) : scale * s;
+        if (sl == 0 && row < M.n) {
+            const T o = (mask && mask[row]) ? T(0) : scale * s;
+            out[row] = o;
+            if (xdot) *xdot += __ldcg(x + row) * o;
+        }
     }
 }
 
-// z = out_scale * B r on the hierarchy; level 0 reads H.L[0].r and writes H.L[0].y (masked).
+// z = out_scale * B r on the hierarchy; level 0 reads H.L[0].r and writes H.L[0].y (masked);
+// rz (may be null) accumulates this thread's share of r . z.
 template <typename T>
-__device__ bool rvcycle(const RDevHierarchy<T>& H, T out_scale, const unsigned char* mask0, const GridBarrier& bar) {
+__device__ bool rvcycle(const RDevHierarchy<T>& H, T out_scale, const unsigned char* mask0, const GridBarrier& bar,
+                        T* rz = nullptr) {
     const int stride = gridDim.x * blockDim.x;
     const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
     for (int l = 0; l < H.nlev; l++) {
@@ -501,7 +509,8 @@ __device__ bool rvcycle(const RDevHierarchy<T>& H, T out_scale, const unsigned c
     if (!grid_sync(bar)) return false;
     for (int l = H.nlev - 1; l >= 0; l--) {
         const T* yn = (l + 1 < H.nlev) ? H.L[l + 1].y : H.yc;
-        rcsr_phase<T>(H.L[l].S, H.L[l].r, &H.L[l].P, yn, H.L[l].y, l == 0 ? out_scale : T(1), l == 0 ? mask0 : nullptr);
+        rcsr_phase<T>(H.L[l].S, H.L[l].r, &H.L[l].P, yn, H.L[l].y, l == 0 ? out_scale : T(1), l == 0 ? mask0 : nullptr,
+                      l == 0 ? rz : nullptr);
         if (l > 0 && !grid_sync(bar)) return false;
     }
     return true;

@@ -98,6 +98,11 @@ __device__ __forceinline__ bool grid_sync(const GridBarrier& b) {
 }
 
 // Fixed-order block reduction of K values per thread; result valid in all threads.
+// a * b + c with one rounding (values recomputed by several threads come out bit-identical)
+template <typename T> __device__ __forceinline__ T fmaT(T a, T b, T c);
+template <> __device__ __forceinline__ float fmaT<float>(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+template <> __device__ __forceinline__ double fmaT<double>(double a, double b, double c) { return __fma_rn(a, b, c); }
+
 template <typename T, int K>
 __device__ __forceinline__ void block_sum(T (&v)[K]) {
     __shared__ T s_red[K][kWarps];

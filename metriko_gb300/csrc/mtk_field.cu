@@ -195,9 +195,6 @@ done:
 // Levels >= 1 are CSR cycle operators (csr_phase); level 0 is applied straight from the ELL rows
 // of A, the aggregates and T (DevLevel0), fused with the CG vector updates.
 
-template <typename T> __device__ __forceinline__ T fmaT(T a, T b, T c);
-template <> __device__ __forceinline__ float fmaT<float>(float a, float b, float c) { return __fmaf_rn(a, b, c); }
-template <> __device__ __forceinline__ double fmaT<double>(double a, double b, double c) { return __fma_rn(a, b, c); }
 // a x + y for a real scalar a, one rounding per component (owners and neighbours that recompute
 // the same value get the same bits)
 template <typename V2, typename T> __device__ __forceinline__ V2 axpy2(T a, V2 x, V2 y) {

@@ -119,10 +119,13 @@ __device__ T smem_dot(const T* a, const T* b, int n) {
 
 // Operator K p, with p = [py (global) ; pz (smem)].  Result: qy (global, masked, projected)
 // and qz (smem, projected).  Returns partial <py, qy> of this block in *pq_part and false on
-// a barrier failure.  Three grid barriers.
+// a barrier failure.  Three grid barriers.  With pnew set, the free part of the direction is
+// formed on the fly, p_y = zy + beta py (every reader recomputes it with one rounding), and
+// written to pnew by the thread that owns the row in phase D.
 template <typename T>
 __device__ bool igm_apply(const IgmOp<T>& A, const ZProj<T>& P, const unsigned char* __restrict__ fixy,
-                          const T* py, const T* pz, T* qy, T* qz, ZSmem<T>& zs, const GridBarrier& bar, T& pq_part) {
+                          const T* py, const T* pz, T* qy, T* qz, ZSmem<T>& zs, const GridBarrier& bar, T& pq_part,
+                          const T* zy = nullptr, T beta = T(0), T* pnew = nullptr) {
     const int stride = gridDim.x * blockDim.x;
     const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
     // A (replicated): XJ = USmall pz
@@ -138,7 +141,10 @@ __device__ bool igm_apply(const IgmOp<T>& A, const ZProj<T>& P, const unsigned c
         T acc = T(0);
         for (int e = A.w_ptr[r]; e < A.w_ptr[r + 1]; e++) {
             int tag = A.w_tag[e];
-            T xv = tag >= 0 ? __ldcg(py + tag) : zs.XJ[-1 - tag];
+            T xv;
+            if (tag < 0) xv = zs.XJ[-1 - tag];
+            else if (pnew) xv = fmaT<T>(beta, __ldcg(py + tag), __ldcg(zy + tag));
+            else xv = __ldcg(py + tag);
             acc += A.w_val[e] * xv;
         }
         A.U[r] = acc;
@@ -163,7 +169,13 @@ __device__ bool igm_apply(const IgmOp<T>& A, const ZProj<T>& P, const unsigned c
     for (int j = t0; j < A.nY; j += stride) {
         T acc = T(0);
         for (int e = A.yt_ptr[j]; e < A.yt_ptr[j + 1]; e++) acc += A.yt_val[e] * __ldcg(A.Qc + A.yt_row[e]);
-        T pj = py[j];
+        T pj;
+        if (pnew) {
+            pj = fmaT<T>(beta, __ldcg(py + j), __ldcg(zy + j));
+            pnew[j] = pj;
+        } else {
+            pj = __ldcg(py + j);
+        }
         T qv = fixy[j] ? T(0) : two_scale * acc + A.shift * pj;
         qy[j] = qv;
         part += pj * qv;
@@ -207,9 +219,9 @@ __device__ void igm_apply_z(const IgmOp<T>& A, const ZProj<T>& P, const T* pz, T
 template <typename T>
 __global__ void __launch_bounds__(kBlock, 1) igm_pcg(IgmOp<T> A, ZProj<T> P, const unsigned char* __restrict__ fixy,
                                                  const T* __restrict__ minvy, const T* __restrict__ b, T* x, T* r, T* z,
-                                                 T* p, T* q, T* partials, GridBarrier bar, double tol2, int maxit,
-                                                 int mode, int* out, const RDevHierarchy<T>* __restrict__ Hp,
-                                                 T mg_scale) {
+                                                 T* p, T* p2, T* q, T* partials, GridBarrier bar, double tol2,
+                                                 int maxit, int mode, int* out,
+                                                 const RDevHierarchy<T>* __restrict__ Hp, T mg_scale) {
     extern __shared__ unsigned char smem_raw[];
     ZSmem<T> zs;
     zs.bind(reinterpret_cast<T*>(smem_raw), A.nZ, A.nJ);
@@ -240,18 +252,12 @@ __global__ void __launch_bounds__(kBlock, 1) igm_pcg(IgmOp<T> A, ZProj<T> P, con
         if (mode == 0 && !Hp) {
             T zj = minvy[j] * rj;
             z[j] = zj;
-            p[j] = zj;
             part[0] += rj * zj;
         }
     }
     if (mode == 0 && Hp) {   // multigrid on the free block: z_y = mask (B r_y) / scale
         if (!grid_sync(bar)) { status = 5; goto done; }
-        if (!rvcycle(*Hp, mg_scale, fixy, bar)) { status = 5; goto done; }
-        for (int j = t0; j < nY; j += stride) {
-            T zj = z[j];
-            p[j] = zj;
-            part[0] += r[j] * zj;
-        }
+        if (!rvcycle(*Hp, mg_scale, fixy, bar, &part[0])) { status = 5; goto done; }
     }
     for (int j = threadIdx.x; j < nZ; j += blockDim.x) zs.rz[j] = __ldg(b + nY + j) - zs.qz[j];
     __syncthreads();
@@ -274,12 +280,15 @@ __global__ void __launch_bounds__(kBlock, 1) igm_pcg(IgmOp<T> A, ZProj<T> P, con
             status = 0;
             goto done;
         }
+        T beta = T(0);
+        const T* pold = z;   // first direction p = z (beta = 0)
+        T* pw = p;
         for (;;) {
             if ((double)rr <= tol2) { status = 0; break; }
             if (it >= maxit) { status = 3; break; }
-            // q = K p
+            // q = K p, p = z + beta p_old formed on the fly and stored in pw
             T pq_part = T(0);
-            if (!igm_apply(A, P, fixy, p, zs.pz, q, zs.qz, zs, bar, pq_part)) { status = 5; break; }
+            if (!igm_apply(A, P, fixy, pold, zs.pz, q, zs.qz, zs, bar, pq_part, z, beta, pw)) { status = 5; break; }
             pq1[0] = pq_part;
             publish_partials<T, 1>(pq1, partials + 2 * gridDim.x);
             if (!grid_sync(bar)) { status = 5; break; }
@@ -300,7 +309,7 @@ __global__ void __launch_bounds__(kBlock, 1) igm_pcg(IgmOp<T> A, ZProj<T> P, con
             part[1] = T(0);
             for (int j = t0; j < nY; j += stride) {
                 T rj = r[j] - alpha * q[j];
-                x[j] += alpha * p[j];
+                x[j] += alpha * pw[j];
                 r[j] = rj;
                 if (!Hp) {
                     T zj = minvy[j] * rj;
@@ -311,8 +320,7 @@ __global__ void __launch_bounds__(kBlock, 1) igm_pcg(IgmOp<T> A, ZProj<T> P, con
             }
             if (Hp) {
                 if (!grid_sync(bar)) { status = 5; break; }
-                if (!rvcycle(*Hp, mg_scale, fixy, bar)) { status = 5; break; }
-                for (int j = t0; j < nY; j += stride) part[0] += r[j] * z[j];
+                if (!rvcycle(*Hp, mg_scale, fixy, bar, &part[0])) { status = 5; break; }
             }
             for (int j = threadIdx.x; j < nZ; j += blockDim.x) {
                 zs.xz[j] += alpha * zs.pz[j];
@@ -327,13 +335,13 @@ __global__ void __launch_bounds__(kBlock, 1) igm_pcg(IgmOp<T> A, ZProj<T> P, con
             T rz_new = part[0] + smem_dot(zs.rz, zs.zz, nZ);
             rr = part[1] + smem_dot(zs.rz, zs.rz, nZ);
             if (rr != rr) { status = 4; break; }
-            T beta = rz_new / rz;
+            beta = rz_new / rz;
             rz = rz_new;
-            for (int j = t0; j < nY; j += stride) p[j] = z[j] + beta * p[j];
             for (int j = threadIdx.x; j < nZ; j += blockDim.x) zs.pz[j] = zs.zz[j] + beta * zs.pz[j];
             __syncthreads();
+            pold = pw;
+            pw = (pw == p) ? p2 : p;
             it++;
-            if (!grid_sync(bar)) { status = 5; break; }
         }
         if (blockIdx.x == 0)
             for (int j = threadIdx.x; j < nZ; j += blockDim.x) x[nY + j] = zs.xz[j];
@@ -668,7 +676,8 @@ struct Igm {
     DBuf<double> cutV, grad, s_val, s_diag, w_val, yt_val, jt_val, Us, F2, Fsi, hb, XbJ, U, Qc, XoJ, minvy, Mz, Qz;
     DBuf<float> s_val32, w_val32, yt_val32, jt_val32, Us32, minvy32, Mz32, Qz32, U32, Qc32, XoJ32;
     DBuf<double> xs, bsys, r64, z64, p64, q64, prev, Xfull, XJ64, scratch;
-    DBuf<float> r32, e32, z32, p32, q32;
+    DBuf<float> r32, e32, z32, p32, q32, pb32;
+    DBuf<double> pb64;   // second direction buffers of the PCG (double-buffered p)
     DBuf<unsigned char> fixy;
     std::vector<unsigned char> h_fixy;
     int kq = 0;
@@ -765,13 +774,13 @@ struct Igm {
     }
 
     // Algorithmic bytes of one projected-PCG iteration (operator chain + vector updates):
-    //   W gather   nnzW (tag 4 + val T + x T) + 2 nCut (ptr 4 + U write T)
+    //   W gather   nnzW (tag 4 + val T + z, p_old 2T) + 2 nCut (ptr 4 + U write T)
     //   S product  nnzS (col 4 + val T) + nCut ptr 4 + U read 2T + Qc write 2T
-    //   W^T gather nnzYT (row 4 + val T + Qc T) + nY (ptr 4 + p T + q write T)
-    //   vectors    nY * 11 T  (x, r, p read+write; z = M^-1 r: minv read + z write)
+    //   W^T gather nnzYT (row 4 + val T + Qc T) + nY (ptr 4 + z, p_old read 2T + p, q write 2T)
+    //   updates    nY * 6 T  (x, r, p, q read; x, r write); the preconditioner is counted apart
     double iter_bytes(size_t T) const {
-        return (double)nnzW * (4 + 2 * T) + 2.0 * nCut * (4 + T) + (double)nnzS * (4 + T) + nCut * (4.0 + 4 * T) +
-               (double)nnzYT * (4 + 2 * T) + (double)nY * (4 + 2 * T) + (double)nY * 11 * T;
+        return (double)nnzW * (4 + 3 * T) + 2.0 * nCut * (4 + T) + (double)nnzS * (4 + T) + nCut * (4.0 + 4 * T) +
+               (double)nnzYT * (4 + 2 * T) + (double)nY * (4 + 4 * T) + (double)nY * 6 * T;
     }
 
     IgmOp<double> op64(double scale, double shift) {
@@ -808,9 +817,10 @@ struct Igm {
             Hp = reinterpret_cast<const RDevHierarchy<T>*>(dst);
             mg_scale = T(1.0 / cur_scale);
         }
+        T* p2 = sizeof(T) == 8 ? reinterpret_cast<T*>(pb64.p) : reinterpret_cast<T*>(pb32.p);
         void* params[] = {&A, &P, (void*)&fx, (void*)&minv, (void*)&b, (void*)&x, (void*)&r, (void*)&z, (void*)&p,
-                          (void*)&q, (void*)&partials, &bar, &tol2, &maxit, &mode, (void*)&out, (void*)&Hp,
-                          (void*)&mg_scale};
+                          (void*)&p2, (void*)&q, (void*)&partials, &bar, &tol2, &maxit, &mode, (void*)&out,
+                          (void*)&Hp, (void*)&mg_scale};
         MTK_TRY(reset_barrier(c));
         MTK_CUDA_TRY(cudaEventRecord(c->ev_k0, st));
         MTK_CUDA_TRY(cudaLaunchCooperativeKernel(reinterpret_cast<void*>(kern), dim3(grid), dim3(kBlock), params, smem, st));
@@ -1090,7 +1100,7 @@ extern "C" int mtk_iterative_rounding(mtk_ctx* c, const mtk_igm_desc* d, const m
     MTK_TRY(S.Xfull.alloc(std::max(nFull, nRed)));
     MTK_TRY(S.XJ64.alloc(std::max(nJ, 1)));
     MTK_TRY(S.r32.alloc(nRed)); MTK_TRY(S.e32.alloc(nRed)); MTK_TRY(S.z32.alloc(nRed)); MTK_TRY(S.p32.alloc(nRed));
-    MTK_TRY(S.q32.alloc(nRed));
+    MTK_TRY(S.q32.alloc(nRed)); MTK_TRY(S.pb32.alloc(nRed)); MTK_TRY(S.pb64.alloc(nRed));
     S.h_fixy.assign(std::max(nY, 1), 0);
     MTK_TRY(S.fixy.upload(S.h_fixy.data(), S.h_fixy.size(), st));
     const int nLeftCap = std::max(1, d->nSingular + d->nInteger);
