@@ -189,7 +189,6 @@ namespace metriko {
             if (visit[i]) continue;
             visit[i] = 1;
             turns[i] = mm;
-            for (int k = 0; k < N; k++) F->field(i, k) = fld.field(i, (k + mm) % N);
             for (int j = 0; j < 3; j++) {
                 int e = m.edge[m.face2half3(i, j)];
                 bool b = m.edge2face(e, 0) == i;
@@ -199,7 +198,12 @@ namespace metriko {
                 if (!visit[fn] && !seam[e]) q.emplace_back(fn, n);
             }
         }
+        METRIKO_PARALLEL_FOR
+        for (int i = 0; i < m.nF; i++)
+            if (visit[i])
+                for (int k = 0; k < N; k++) F->field(i, k) = fld.field(i, (k + turns[i]) % N);
         F->matching = VecXi(m.nE, -1);
+        METRIKO_PARALLEL_FOR
         for (int e = 0; e < m.nE; e++)
             F->matching[e] = (turns[m.edge2face(e, 0)] - turns[m.edge2face(e, 1)] + fld.matching[e] + 1000 * N) % N;
         return F;
@@ -225,6 +229,7 @@ namespace metriko {
         inline void triangle_adjacency(const Hmesh& m, MatXi& TT, MatXi& TTi) {
             TT = MatXi(m.nF, 3);
             TTi = MatXi(m.nF, 3);
+            METRIKO_PARALLEL_FOR
             for (int f = 0; f < m.nF; f++)
                 for (int s = 0; s < 3; s++) {
                     int t = m.twin[m.face2half3(f, s)];
@@ -361,14 +366,20 @@ namespace metriko {
         MatXi TT, TTi;
         detail::triangle_adjacency(m, TT, TTi);
         cuts = detail::spanning_cut(m, TT, TTi);
-        // vertex -> faces (ascending) and vertex -> vertices (sorted, unique)
-        std::vector<int> fptr(m.nV + 1, 0);
-        for (int f = 0; f < m.nF; f++) for (int j = 0; j < 3; j++) fptr[F(f, j) + 1]++;
-        for (int v = 0; v < m.nV; v++) fptr[v + 1] += fptr[v];
-        std::vector<int> vf(fptr[m.nV]);
-        {
-            std::vector<int> fill(fptr.begin(), fptr.end() - 1);
-            for (int f = 0; f < m.nF; f++) for (int j = 0; j < 3; j++) vf[fill[F(f, j)]++] = f;
+        // vertex -> neighbouring vertices (one per outgoing halfedge), built in parallel
+        std::vector<int> vptr(m.nV + 1, 0);
+        METRIKO_PARALLEL_FOR
+        for (int v = 0; v < m.nV; v++) {
+            int cnt = 0, h = m.vert2half[v];
+            do { cnt++; h = m.twin[m.prev[h]]; } while (h != m.vert2half[v]);
+            vptr[v + 1] = cnt;
+        }
+        for (int v = 0; v < m.nV; v++) vptr[v + 1] += vptr[v];
+        std::vector<int> vv(vptr[m.nV]);
+        METRIKO_PARALLEL_FOR
+        for (int v = 0; v < m.nV; v++) {
+            int q = vptr[v], h = m.vert2half[v];
+            do { vv[q++] = m.head[h]; h = m.twin[m.prev[h]]; } while (h != m.vert2half[v]);
         }
         std::vector<int> in_cut(m.nV, 0);
         for (int f = 0; f < m.nF; f++) for (int j = 0; j < 3; j++) if (cuts(f, j)) in_cut[F(f, j)] = 1;
@@ -386,7 +397,8 @@ namespace metriko {
             }
             // unit-weight Dijkstra with pops ordered by (distance, id), run as a breadth-first
             // search whose levels are visited in ascending id: the same pop order, and every vertex
-            // keeps as predecessor the first popped neighbour that reached it
+            // keeps as predecessor the first popped neighbour that reached it (the order in which
+            // a vertex lists its neighbours does not matter)
             for (int v : touched) { dist[v] = -1; prev[v] = -1; }
             touched.clear();
             dist[src] = 0;
@@ -398,16 +410,13 @@ namespace metriko {
                 nlevel.clear();
                 for (int u : level) {
                     if (in_cut[u]) { found = u; break; }
-                    for (int k = fptr[u]; k < fptr[u + 1]; k++) {
-                        const int f = vf[k];
-                        for (int j = 0; j < 3; j++) {
-                            const int w = F(f, j);
-                            if (w == u || dist[w] >= 0) continue;
-                            dist[w] = d + 1;
-                            prev[w] = u;
-                            touched.push_back(w);
-                            nlevel.push_back(w);
-                        }
+                    for (int k = vptr[u]; k < vptr[u + 1]; k++) {
+                        const int w = vv[k];
+                        if (dist[w] >= 0) continue;
+                        dist[w] = d + 1;
+                        prev[w] = u;
+                        touched.push_back(w);
+                        nlevel.push_back(w);
                     }
                 }
                 level.swap(nlevel);
@@ -417,11 +426,11 @@ namespace metriko {
             else for (int v = found; v != -1; v = prev[v]) path.push_back(v);
             for (int v : path) { ncut += !in_cut[v]; in_cut[v] = 1; }
             for (size_t ii = 0; ii + 1 < path.size(); ii++) {
-                int v0 = path[ii], v1 = path[ii + 1];
-                int fi = -1;
-                for (int k = fptr[v0]; k < fptr[v0 + 1] && fi < 0; k++)
-                    for (int k2 = fptr[v1]; k2 < fptr[v1 + 1]; k2++)
-                        if (vf[k] == vf[k2]) { fi = vf[k]; break; }
+                // the edge v0 v1 is cut on both of its faces
+                const int v0 = path[ii], v1 = path[ii + 1];
+                int h = m.vert2half[v0];
+                while (m.head[h] != v1) h = m.twin[m.prev[h]];
+                const int fi = m.face[h];
                 int j = -1;
                 for (int z = 0; z < 3; z++)
                     if ((F(fi, z) == v0 && F(fi, (z + 1) % 3) == v1) || (F(fi, z) == v1 && F(fi, (z + 1) % 3) == v0)) j = z;

@@ -195,7 +195,8 @@ inline int aggregate_level(HostLevel& L) {
     return na;
 }
 
-// Hermitian positive definite inverse (complex Cholesky), returns false if not HPD.
+// Hermitian positive definite inverse (complex Cholesky), returns false if not HPD.  Column
+// updates and the n substitutions run in parallel (each entry is still a sequential sum).
 inline bool hpd_inverse(std::vector<std::complex<double>>& A, int n) {
     using cd = std::complex<double>;
     std::vector<cd> L(A);
@@ -205,45 +206,85 @@ inline bool hpd_inverse(std::vector<std::complex<double>>& A, int n) {
         if (!(d > 0)) return false;
         d = std::sqrt(d);
         L[(size_t)j * n + j] = d;
+#pragma omp parallel for schedule(static) if (n - j > 64)
         for (int i = j + 1; i < n; i++) {
             cd s = L[(size_t)i * n + j];
             for (int k = 0; k < j; k++) s -= L[(size_t)i * n + k] * std::conj(L[(size_t)j * n + k]);
             L[(size_t)i * n + j] = s / d;
         }
     }
-    std::vector<cd> inv((size_t)n * n, 0.0), y(n);
-    for (int col = 0; col < n; col++) {
-        for (int i = 0; i < n; i++) {
-            cd s = i == col ? cd(1, 0) : cd(0, 0);
-            for (int k = 0; k < i; k++) s -= L[(size_t)i * n + k] * y[k];
-            y[i] = s / L[(size_t)i * n + i].real();
-        }
-        for (int i = n - 1; i >= 0; i--) {
-            cd s = y[i];
-            for (int k = i + 1; k < n; k++) s -= std::conj(L[(size_t)k * n + i]) * inv[(size_t)k * n + col];
-            inv[(size_t)i * n + col] = s / L[(size_t)i * n + i].real();
+    std::vector<cd> inv((size_t)n * n, 0.0);
+#pragma omp parallel
+    {
+        std::vector<cd> y(n), xcol(n);
+#pragma omp for schedule(static)
+        for (int col = 0; col < n; col++) {
+            for (int i = 0; i < n; i++) {
+                cd s = i == col ? cd(1, 0) : cd(0, 0);
+                for (int k = 0; k < i; k++) s -= L[(size_t)i * n + k] * y[k];
+                y[i] = s / L[(size_t)i * n + i].real();
+            }
+            for (int i = n - 1; i >= 0; i--) {
+                cd s = y[i];
+                for (int k = i + 1; k < n; k++) s -= std::conj(L[(size_t)k * n + i]) * xcol[k];
+                xcol[i] = s / L[(size_t)i * n + i].real();
+            }
+            for (int i = 0; i < n; i++) inv[(size_t)i * n + col] = xcol[i];
         }
     }
     A.swap(inv);
     return true;
 }
 
-// Hermitian transpose of an n x m complex CSR (serial; output rows in ascending input row).
+// Hermitian transpose of an n x m complex CSR.  Threads count the columns of contiguous row
+// blocks and offsets are laid out block by block, so every output row lists its entries in
+// ascending input row (the serial result, for any thread count).
 inline HostCsr hcsr_adjoint(const HostCsr& M, int m) {
     HostCsr Tm;
     Tm.n = m;
     Tm.ptr.assign(m + 1, 0);
-    for (int c : M.col) Tm.ptr[c + 1]++;
-    for (int a = 0; a < m; a++) Tm.ptr[a + 1] += Tm.ptr[a];
     Tm.col.resize(M.col.size());
     Tm.val.resize(M.col.size());
-    std::vector<int> fill(Tm.ptr.begin(), Tm.ptr.end() - 1);
-    for (int i = 0; i < M.n; i++)
-        for (int p = M.ptr[i]; p < M.ptr[i + 1]; p++) {
-            const int q = fill[M.col[p]]++;
-            Tm.col[q] = i;
-            Tm.val[q] = std::conj(M.val[p]);
+    int nt = 1;
+#ifdef _OPENMP
+    nt = omp_get_max_threads();
+#endif
+    std::vector<std::vector<int>> cnt(nt);
+#pragma omp parallel num_threads(nt)
+    {
+        int t = 0;
+#ifdef _OPENMP
+        t = omp_get_thread_num();
+#endif
+        const int r0 = (int)((long long)M.n * t / nt), r1 = (int)((long long)M.n * (t + 1) / nt);
+        std::vector<int>& c = cnt[t];
+        c.assign(m, 0);
+        for (int p = M.ptr[r0]; p < M.ptr[r1]; p++) c[M.col[p]]++;
+#pragma omp barrier
+#pragma omp single
+        {
+            for (int a = 0; a < m; a++) {
+                int s = 0;
+                for (int u = 0; u < nt; u++) s += cnt[u][a];
+                Tm.ptr[a + 1] = s;
+            }
+            for (int a = 0; a < m; a++) Tm.ptr[a + 1] += Tm.ptr[a];
+            for (int a = 0; a < m; a++) {
+                int off = Tm.ptr[a];
+                for (int u = 0; u < nt; u++) {
+                    const int k = cnt[u][a];
+                    cnt[u][a] = off;
+                    off += k;
+                }
+            }
         }
+        for (int i = r0; i < r1; i++)
+            for (int p = M.ptr[i]; p < M.ptr[i + 1]; p++) {
+                const int q = c[M.col[p]]++;
+                Tm.col[q] = i;
+                Tm.val[q] = std::conj(M.val[p]);
+            }
+    }
     return Tm;
 }
 

@@ -227,31 +227,43 @@ inline RCsr rcsr_transpose(const RCsr& M, int m) {
     return Tm;
 }
 
+// Inverse of an SPD matrix (n x n, row-major) by Cholesky; false if not SPD.  The updates of a
+// column and the n substitutions are independent, so both run in parallel (same arithmetic as
+// the serial order: every entry is still a sequential sum).
 inline bool spd_inverse_dense(std::vector<double>& A, int n) {
     std::vector<double> L(A);
-    for (int j = 0; j < n; j++) {
+    bool ok = true;
+    for (int j = 0; j < n && ok; j++) {
         double d = L[(size_t)j * n + j];
         for (int k = 0; k < j; k++) d -= L[(size_t)j * n + k] * L[(size_t)j * n + k];
-        if (!(d > 0)) return false;
+        if (!(d > 0)) { ok = false; break; }
         d = std::sqrt(d);
         L[(size_t)j * n + j] = d;
+#pragma omp parallel for schedule(static) if (n - j > 64)
         for (int i = j + 1; i < n; i++) {
             double s = L[(size_t)i * n + j];
             for (int k = 0; k < j; k++) s -= L[(size_t)i * n + k] * L[(size_t)j * n + k];
             L[(size_t)i * n + j] = s / d;
         }
     }
-    std::vector<double> inv((size_t)n * n, 0.0), y(n);
-    for (int col = 0; col < n; col++) {
-        for (int i = 0; i < n; i++) {
-            double s = i == col ? 1.0 : 0.0;
-            for (int k = 0; k < i; k++) s -= L[(size_t)i * n + k] * y[k];
-            y[i] = s / L[(size_t)i * n + i];
-        }
-        for (int i = n - 1; i >= 0; i--) {
-            double s = y[i];
-            for (int k = i + 1; k < n; k++) s -= L[(size_t)k * n + i] * inv[(size_t)k * n + col];
-            inv[(size_t)i * n + col] = s / L[(size_t)i * n + i];
+    if (!ok) return false;
+    std::vector<double> inv((size_t)n * n, 0.0);
+#pragma omp parallel
+    {
+        std::vector<double> y(n), xcol(n);
+#pragma omp for schedule(static)
+        for (int col = 0; col < n; col++) {
+            for (int i = 0; i < n; i++) {
+                double s = i == col ? 1.0 : 0.0;
+                for (int k = 0; k < i; k++) s -= L[(size_t)i * n + k] * y[k];
+                y[i] = s / L[(size_t)i * n + i];
+            }
+            for (int i = n - 1; i >= 0; i--) {
+                double s = y[i];
+                for (int k = i + 1; k < n; k++) s -= L[(size_t)k * n + i] * xcol[k];
+                xcol[i] = s / L[(size_t)i * n + i];
+            }
+            for (int i = 0; i < n; i++) inv[(size_t)i * n + col] = xcol[i];
         }
     }
     A.swap(inv);
