@@ -72,6 +72,26 @@ void build_rows_parallel(int nrows, int ncols, RowFn fn, std::vector<int>& ptr, 
     }
 }
 
+// Sums K per-row terms over rows [0, n) in an order that does not depend on the thread count
+// or on scheduling: fixed blocks of 4096 rows are summed in parallel, the block sums in order.
+// fn(i, acc) adds row i's terms to acc[0..K).
+template <int K, typename Fn>
+void det_row_sums(int n, Fn fn, double (&out)[K]) {
+    constexpr int kRows = 4096;
+    const int nb = (n + kRows - 1) / kRows;
+    std::vector<double> part((size_t)nb * K, 0.0);
+#pragma omp parallel for schedule(static)
+    for (int b = 0; b < nb; b++) {
+        double acc[K] = {};
+        const int e = std::min(n, (b + 1) * kRows);
+        for (int i = b * kRows; i < e; i++) fn(i, acc);
+        for (int k = 0; k < K; k++) part[(size_t)b * K + k] = acc[k];
+    }
+    for (int k = 0; k < K; k++) out[k] = 0.0;
+    for (int b = 0; b < nb; b++)
+        for (int k = 0; k < K; k++) out[k] += part[(size_t)b * K + k];
+}
+
 constexpr int kMaxLevels = 8;
 constexpr int kCoarseMax = 384;
 constexpr double kOmega = 0.8;   // Jacobi weight of the pre- and post-smoothing
@@ -332,18 +352,20 @@ inline bool build_hierarchy(int n, const std::vector<int>& nbr3, const std::vect
 #pragma omp parallel for schedule(static)
             for (int i = 0; i < ln; i++) v[i] = cd((i & 1) ? 1.0 : -1.0 + 0.25 * ((i * 7919) % 5), 0.1 * ((i * 104729) % 7));
             for (int it = 0; it < 12; it++) {
-                double num = 0, den = 0, nw = 0;
-#pragma omp parallel for schedule(static) reduction(+ : num, den, nw)
-                for (int i = 0; i < ln; i++) {
-                    cd av = 0;
-                    for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) av += A.val[p] * v[A.col[p]];
-                    w[i] = L.dinv[i] * av;
-                    num += (std::conj(v[i]) * av).real();
-                    den += std::norm(v[i]) / L.dinv[i];
-                    nw += std::norm(w[i]);
-                }
-                rho = den > 0 ? num / den : 0.0;
-                const double sc = nw > 0 ? 1.0 / std::sqrt(nw) : 0.0;
+                double red[3];   // v^H A v, v^H D v, |w|^2
+                det_row_sums<3>(
+                    ln,
+                    [&](int i, double* acc) {
+                        cd av = 0;
+                        for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) av += A.val[p] * v[A.col[p]];
+                        w[i] = L.dinv[i] * av;
+                        acc[0] += (std::conj(v[i]) * av).real();
+                        acc[1] += std::norm(v[i]) / L.dinv[i];
+                        acc[2] += std::norm(w[i]);
+                    },
+                    red);
+                rho = red[1] > 0 ? red[0] / red[1] : 0.0;
+                const double sc = red[2] > 0 ? 1.0 / std::sqrt(red[2]) : 0.0;
 #pragma omp parallel for schedule(static)
                 for (int i = 0; i < ln; i++) v[i] = w[i] * sc;
             }

@@ -300,18 +300,20 @@ inline bool build_real_hierarchy(RCsr A0, std::vector<int> node, std::vector<int
 #pragma omp parallel for schedule(static)
             for (int i = 0; i < n; i++) v[i] = (i & 1) ? 1.0 : -1.0 + 0.25 * ((i * 7919) % 5);
             for (int it = 0; it < 12; it++) {
-                double num = 0, den = 0, nw = 0;
-#pragma omp parallel for schedule(static) reduction(+ : num, den, nw)
-                for (int i = 0; i < n; i++) {
-                    double av = 0;
-                    for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) av += A.val[p] * v[A.col[p]];
-                    w[i] = cur.dinv[i] * av;
-                    num += v[i] * av;
-                    den += v[i] * v[i] / cur.dinv[i];
-                    nw += w[i] * w[i];
-                }
-                rho = den > 0 ? num / den : 0.0;
-                const double sc = nw > 0 ? 1.0 / std::sqrt(nw) : 0.0;
+                double red[3];   // v^T A v, v^T D v, |w|^2
+                det_row_sums<3>(
+                    n,
+                    [&](int i, double* acc) {
+                        double av = 0;
+                        for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) av += A.val[p] * v[A.col[p]];
+                        w[i] = cur.dinv[i] * av;
+                        acc[0] += v[i] * av;
+                        acc[1] += v[i] * v[i] / cur.dinv[i];
+                        acc[2] += w[i] * w[i];
+                    },
+                    red);
+                rho = red[1] > 0 ? red[0] / red[1] : 0.0;
+                const double sc = red[2] > 0 ? 1.0 / std::sqrt(red[2]) : 0.0;
 #pragma omp parallel for schedule(static)
                 for (int i = 0; i < n; i++) v[i] = w[i] * sc;
             }
