@@ -145,6 +145,10 @@ namespace metriko {
 
         void setup();
         void build_system(IntegSystem& sys);   // host part of integ()
+        // Size-field gradient of the naive integration (mtk_size_field_gradient); no counterpart
+        // in the reference.  s: log-size per raw vertex; T: per-face loss target (8 per face) or
+        // nullptr for the integration target.  Fills fullx with x(s).
+        double size_field_gradient(const VecXd& s, const VecXd* T, double mu, VecXd& grad_s);
         bool integ();
 
     private:
@@ -450,6 +454,20 @@ namespace metriko {
         d.nInteger = integerIdcs.size(); d.integerIdcs = integerIdcs.data();
         d.seamless = seamless; d.roundSeams = roundSeams;
         if (localInjectivity) throw std::invalid_argument("localInjectivity is not part of this build");
+    }
+
+    inline double RosyParameterization::size_field_gradient(const VecXd& s, const VecXd* T, double mu, VecXd& grad_s) {
+        IntegSystem sys;
+        build_system(sys);
+        if (s.size() != raw.nV || (T && T->size() != 8 * raw.nF)) throw std::invalid_argument("size field: bad sizes");
+        grad_s = VecXd(raw.nV);
+        fullx = VecXd(sys.desc.nFull);
+        double loss = 0;
+        gpu::check(mtk_size_field_gradient(gpu::context(), &sys.desc, &gpu::options().solve, raw.nV, raw.idx.data(),
+                                           s.data(), T ? T->data() : nullptr, mu, &loss, grad_s.data(), fullx.data(),
+                                           &gpu::stats()),
+                   "mtk_size_field_gradient");
+        return loss;
     }
 
     inline bool RosyParameterization::integ() {

@@ -213,6 +213,39 @@ int mtk_field_smoothest_noalloc(int32_t nF, int32_t nRosy, const int32_t* nbr, c
                                 const double* area, const double* x0, int32_t n_iter, double tol,
                                 int32_t max_iter, double* out, void* stream, int32_t* iterations);
 
+/*
+ * Gradient of a parameterization-quality loss with respect to a per-vertex log-size field
+ * (adjoint of the naive integration).  No counterpart in the reference, which has no
+ * differentiation; it serves size-field optimisation on top of the integration of
+ * iter_rounding_init.h:171-212.  The naive integration is run with the target of face f scaled
+ * by exp(sbar_f), sbar_f the mean of s over the face's corners:
+ *   length X2F^T X2F x = X2F^T (exp(sbar) F2),  anchored as in mtk_iterative_rounding,
+ * and the loss
+ *   l(s) = sum_f |length X2F_f x(s) - exp(sbar_f) T_f|^2 + mu sum_edges (s_i - s_j)^2
+ * is differentiated by one adjoint solve with the same (symmetric) operator, K lambda = dl/dx,
+ * plus the assembly backward of the right-hand side; the solver iterates are not stored.
+ *   F[3*nF]      raw mesh faces (corner vertex ids < nV; the rows of the cut faces)
+ *   s[nV]        log-size per raw vertex
+ *   T[8*nF]      loss target per face in the F2 layout, or NULL for the integration target F2
+ *   mu >= 0      edge smoothness weight (every edge of a closed mesh lies in two faces)
+ *   loss, grad_s[nV], fullx[nFull] (the integration result x(s) in full variables)
+ * desc->seamless and the rounding fields are not used.
+ */
+int mtk_size_field_gradient(mtk_ctx* ctx, const mtk_igm_desc* desc, const mtk_solve_opts* opts, int32_t nV,
+                            const int32_t* F, const double* s, const double* T, double mu, double* loss,
+                            double* grad_s, double* fullx, mtk_stats* stats);
+
+/*
+ * mtk_size_field_gradient on the whole example_igm.cpp path with host buffers: Hmesh ->
+ * field -> topology -> RosyParameterization::setup() -> the size-field gradient (instead of
+ * integ()).  No counterpart in the reference.  fullx capacity fullx_cap, *n_full its length.
+ */
+int mtk_pipeline_size_field_gradient(mtk_ctx* ctx, int32_t nV, int32_t nF, const double* V, const int32_t* F,
+                                     const mtk_pipeline_opts* popts, const mtk_solve_opts* sopts,
+                                     const double* s, const double* T, double mu, double* loss,
+                                     double* grad_s, double* fullx, int32_t fullx_cap, int32_t* n_full,
+                                     mtk_stats* stats);
+
 /* The deterministic start vector used by the pipeline: re/im of face f from splitmix64. */
 void mtk_seeded_init(int32_t n, int32_t seed, double* out);
 

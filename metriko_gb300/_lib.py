@@ -20,7 +20,8 @@ PREC_FP64, PREC_MIXED = 0, 1
 EXPORTS = [
     "mtk_status_string", "mtk_last_error", "mtk_default_opts", "mtk_ctx_create", "mtk_ctx_destroy",
     "mtk_ctx_kernel_count", "mtk_field_smoothest", "mtk_iterative_rounding", "mtk_pipeline_run",
-    "mtk_seeded_init", "mtk_topology_from_field", "mtk_field_smoothest_noalloc",
+    "mtk_seeded_init", "mtk_topology_from_field", "mtk_field_smoothest_noalloc", "mtk_size_field_gradient",
+    "mtk_pipeline_size_field_gradient",
 ]
 
 
@@ -85,6 +86,10 @@ def lib():
         L.mtk_field_smoothest_noalloc.argtypes = [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
                                                   C.c_void_p, C.c_int32, C.c_double, C.c_int32, C.c_void_p,
                                                   C.c_void_p, C.POINTER(C.c_int32)]
+        L.mtk_pipeline_size_field_gradient.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
+                                                       C.POINTER(PipelineOpts), C.POINTER(SolveOpts), C.c_void_p,
+                                                       C.c_void_p, C.c_double, C.POINTER(C.c_double), C.c_void_p,
+                                                       C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(Stats)]
         _lib = L
     return _lib
 
@@ -196,6 +201,39 @@ def pipeline(ctx: Context, V, F, ratio=0.02, seed=0, round_seams=False, seamless
                 fix_order=fix_order[:nfix].copy(), fix_vals=fix_vals[:nfix].copy(),
                 counts=dict(zip(["nV", "nE", "nCut", "nT", "nS", "nJ", "nZ", "nFull"], counts.tolist())),
                 stats=st.as_dict())
+
+
+def size_field_gradient(ctx: Context, V, F, s, T=None, mu=0.0, ratio=0.02, seed=0, round_seams=False, n_iter=50,
+                        opts=None):
+    """mtk_pipeline_size_field_gradient: loss l(s) = sum_f |length X2F_f x(s) - exp(sbar_f) T_f|^2 +
+    mu sum_edges (s_i - s_j)^2 of the naive integration x(s) with size-scaled targets, and dl/ds
+    by the adjoint solve.  T (nF x 8) defaults to the integration target."""
+    V = np.ascontiguousarray(V, np.float64)
+    F = np.ascontiguousarray(F, np.int32)
+    nV, nF = len(V), len(F)
+    s = np.ascontiguousarray(s, np.float64)
+    if s.shape != (nV,):
+        raise ValueError("s must have one value per vertex")
+    Tp = None
+    if T is not None:
+        T = np.ascontiguousarray(T, np.float64).reshape(-1)
+        if T.size != 8 * nF:
+            raise ValueError("T must have 8 values per face")
+        Tp = _ptr(T)
+    nE = 3 * nF // 2
+    cap = 2 * (nV + 4 * nE) + 16
+    fullx = np.zeros(cap)
+    grad = np.zeros(nV)
+    loss = C.c_double(0)
+    n_full = C.c_int32(0)
+    p = PipelineOpts(seed, n_iter, ratio, int(round_seams), 0, 0)
+    o = opts or solve_opts()
+    st = Stats()
+    _check(lib().mtk_pipeline_size_field_gradient(ctx.handle, nV, nF, _ptr(V), _ptr(F), C.byref(p), C.byref(o), _ptr(s),
+                                                  Tp, float(mu), C.byref(loss), _ptr(grad), _ptr(fullx), cap,
+                                                  C.byref(n_full), C.byref(st)),
+           "mtk_pipeline_size_field_gradient")
+    return dict(loss=loss.value, grad=grad, fullx=fullx[:n_full.value].copy(), stats=st.as_dict())
 
 
 def topology_from_field(V, F, compressed, ratio=0.02, round_seams=False):

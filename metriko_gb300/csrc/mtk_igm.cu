@@ -657,11 +657,84 @@ __global__ void add_z_projected(int nY, int nZ, int kq, const double* __restrict
     }
 }
 
+// Size-field loss, per face (functions k = 0..3 with k >= 2 the negatives of k - 2): the
+// gradient g of the parameterization U, r = length g - es_f T_f (8 values), rT_f = r . T_f, and
+// the partial sum of |r|^2.
+__global__ void face_residual(int nF, const int* __restrict__ cutF, const double* __restrict__ grad,
+                              const double* __restrict__ U, double length, const double* __restrict__ es,
+                              const double* __restrict__ T, double* r, double* rT, double* partials) {
+    double red[1] = {0};
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nF; f += gridDim.x * blockDim.x) {
+        double g[2][2] = {{0, 0}, {0, 0}};
+        for (int a = 0; a < 3; a++) {
+            const int c = cutF[3 * f + a];
+            const double gx = grad[6 * f + 2 * a], gy = grad[6 * f + 2 * a + 1];
+            for (int k = 0; k < 2; k++) { g[k][0] += gx * U[2 * c + k]; g[k][1] += gy * U[2 * c + k]; }
+        }
+        double dot = 0, sq = 0;
+        for (int k = 0; k < 4; k++) {
+            const double sgn = k < 2 ? 1.0 : -1.0;
+            for (int comp = 0; comp < 2; comp++) {
+                const double t = T[8 * f + 2 * k + comp];
+                const double v = length * sgn * g[k & 1][comp] - es[f] * t;
+                r[8 * f + 2 * k + comp] = v;
+                dot += v * t;
+                sq += v * v;
+            }
+        }
+        rT[f] = dot;
+        red[0] += sq;
+    }
+    publish_partials<double, 1>(red, partials);
+}
+
+// Fixed-order sum of one partial per block (written by publish_partials over nb blocks).
+__global__ void finalize1(const double* partials, int nb, double* out) {
+    double v[1] = {0};
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) v[0] += partials[i];
+    block_sum<double, 1>(v);
+    if (threadIdx.x == 0) out[0] = v[0];
+}
+
+// q_f = (X2F lambda)_f . F2_f: the gradient of the parameterization U(lambda) against the target.
+__global__ void face_target_dot(int nF, const int* __restrict__ cutF, const double* __restrict__ grad,
+                                const double* __restrict__ U, const double* __restrict__ F2, double* q) {
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nF; f += gridDim.x * blockDim.x) {
+        double g[2][2] = {{0, 0}, {0, 0}};
+        for (int a = 0; a < 3; a++) {
+            const int c = cutF[3 * f + a];
+            const double gx = grad[6 * f + 2 * a], gy = grad[6 * f + 2 * a + 1];
+            for (int k = 0; k < 2; k++) { g[k][0] += gx * U[2 * c + k]; g[k][1] += gy * U[2 * c + k]; }
+        }
+        double dot = 0;
+        for (int k = 0; k < 4; k++) {
+            const double sgn = k < 2 ? 1.0 : -1.0;
+            for (int comp = 0; comp < 2; comp++) dot += sgn * g[k & 1][comp] * F2[8 * f + 2 * k + comp];
+        }
+        q[f] = dot;
+    }
+}
+
 }  // namespace mtk
 
 using namespace mtk;
 
 namespace {
+
+// Differentiation of the naive integration with a per-vertex log-size field s: the target of
+// face f is exp(mean of s over its corners) * F2_f, and the loss
+//   l(s) = sum_f |length X2F_f x(s) - exp(sbar_f) T_f|^2 + mu sum_edges (s_i - s_j)^2
+// is differentiated by one adjoint solve K lambda = dl/dx (the forward system, symmetric) and
+// the assembly backward of the right-hand side.
+struct SizeFieldJob {
+    int nV;
+    const int32_t* F;   // raw faces (nF x 3)
+    const double* s;    // log-size per raw vertex
+    const double* T;    // loss target per face (8 values), null: the integration target F2
+    double mu;
+    double* loss;
+    double* grad_s;     // nV
+};
 
 struct Igm {
     mtk_ctx* c = nullptr;
@@ -986,9 +1059,9 @@ bool spd_inverse(std::vector<double>& A, int n) {
 
 }  // namespace
 
-extern "C" int mtk_iterative_rounding(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts_in, double* fullx,
-                                      int32_t* fix_order, int32_t* fix_vals, int32_t* n_fixed, double* x_naive,
-                                      mtk_stats* stats) {
+namespace {
+int igm_run(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts_in, double* fullx, int32_t* fix_order,
+            int32_t* fix_vals, int32_t* n_fixed, double* x_naive, mtk_stats* stats, const SizeFieldJob* job) {
     if (!c || !d || !fullx) return MTK_ERR_BAD_INPUT;
     if (d->N != 4 || d->n != 2) { mtk_set_last_error("only N = 4 (n = 2) is supported", __FILE__, __LINE__); return MTK_ERR_BAD_INPUT; }
     if (d->nF <= 0 || d->nCut <= 0 || d->nFull <= 0 || !d->cutF || !d->cutV || !d->w_ptr || !d->full2y || !d->F2)
@@ -1347,9 +1420,80 @@ extern "C" int mtk_iterative_rounding(mtk_ctx* c, const mtk_igm_desc* d, const m
     MTK_CUDA_TRY(cudaMemsetAsync(S.xs.p, 0, sizeof(double) * nRed, st));
     for (int k = 0; k < d->nFixed; k++) MTK_TRY(add_constraint(d->fixedIdcs[k], d->fixedVals[k]));
     MTK_TRY(upload_constraints(length, 0.0));
-    MTK_TRY(S.build_rhs(S.F2.p, 1.0, 0.0, nullptr, S.bsys.p));
+    std::vector<double> es;   // size-field job: exp(sbar_f) per face, target es_f * F2_f
+    if (job) {
+        es.resize(nF);
+        std::vector<double> ft(8 * (size_t)nF);
+        for (int f = 0; f < nF; f++) {
+            es[f] = std::exp((job->s[job->F[3 * f]] + job->s[job->F[3 * f + 1]] + job->s[job->F[3 * f + 2]]) / 3.0);
+            for (int k = 0; k < 8; k++) ft[8 * (size_t)f + k] = es[f] * d->F2[8 * (size_t)f + k];
+        }
+        MTK_CUDA_TRY(cudaMemcpyAsync(S.Fsi.p, ft.data(), sizeof(double) * ft.size(), cudaMemcpyHostToDevice, st));
+        MTK_CUDA_TRY(cudaStreamSynchronize(st));
+    }
+    MTK_TRY(S.build_rhs(job ? S.Fsi.p : S.F2.p, 1.0, 0.0, nullptr, S.bsys.p));
     double rel = 0;
     MTK_TRY(S.solve(length, 0.0, S.bsys.p, S.xs.p, o, stt, &rel));
+    if (job) {
+        // loss terms per face, dl/dx = 2 length X2F^T r, the adjoint solve, then (X2F lambda) . F2
+        DBuf<double> d_es, d_T, r8, rT, q, lam;
+        MTK_TRY(d_es.upload(es.data(), nF, st));
+        if (job->T) MTK_TRY(d_T.upload(job->T, 8 * (size_t)nF, st));
+        MTK_TRY(r8.alloc(8 * (size_t)nF)); MTK_TRY(rT.alloc(nF)); MTK_TRY(q.alloc(nF)); MTK_TRY(lam.alloc(nRed));
+        xj_from_z<<<G, kStream, 0, st>>>(nJ, nY, nZ, S.Us.p, S.xs.p, S.XJ64.p);
+        gather_U<<<G, kStream, 0, st>>>(nCut, S.w_ptr.p, S.w_tag.p, S.w_val.p, S.xs.p, S.XJ64.p, S.U.p);
+        face_residual<<<G, kStream, 0, st>>>(nF, S.cutF.p, S.grad.p, S.U.p, length, d_es.p, job->T ? d_T.p : S.F2.p, r8.p,
+                                             rT.p, c->partials);
+        finalize1<<<1, kStream, 0, st>>>(c->partials, G, c->scalars);
+        c->kernels += 4;
+        MTK_CUDA_TRY(cudaGetLastError());
+        double lsum = 0;
+        MTK_CUDA_TRY(cudaMemcpyAsync(&lsum, c->scalars, sizeof(double), cudaMemcpyDeviceToHost, st));
+        MTK_TRY(S.build_rhs(r8.p, 2.0 * length, 0.0, nullptr, S.bsys.p));
+        MTK_CUDA_TRY(cudaMemsetAsync(lam.p, 0, sizeof(double) * nRed, st));   // feasible: fixed entries 0
+        double rel2 = 0;
+        MTK_TRY(S.solve(length, 0.0, S.bsys.p, lam.p, o, stt, &rel2));
+        xj_from_z<<<G, kStream, 0, st>>>(nJ, nY, nZ, S.Us.p, lam.p, S.XJ64.p);
+        gather_U<<<G, kStream, 0, st>>>(nCut, S.w_ptr.p, S.w_tag.p, S.w_val.p, lam.p, S.XJ64.p, S.U.p);
+        face_target_dot<<<G, kStream, 0, st>>>(nF, S.cutF.p, S.grad.p, S.U.p, S.F2.p, q.p);
+        c->kernels += 3;
+        MTK_CUDA_TRY(cudaGetLastError());
+        std::vector<double> h_rT(nF), h_q(nF);
+        MTK_CUDA_TRY(cudaMemcpyAsync(h_rT.data(), rT.p, sizeof(double) * nF, cudaMemcpyDeviceToHost, st));
+        MTK_CUDA_TRY(cudaMemcpyAsync(h_q.data(), q.p, sizeof(double) * nF, cudaMemcpyDeviceToHost, st));
+        MTK_CUDA_TRY(cudaStreamSynchronize(st));
+        // assembly backward: dsbar_f / ds_v = 1/3 for the corners of f; smoothness over edges
+        // (every edge of a closed mesh lies in two faces, each contributing half)
+        const double* sv = job->s;
+        double smooth = 0;
+        std::fill(job->grad_s, job->grad_s + job->nV, 0.0);
+        for (int f = 0; f < nF; f++) {
+            const double gf = es[f] / 3.0 * (h_q[f] - 2.0 * h_rT[f]);
+            for (int j = 0; j < 3; j++) {
+                const int a = job->F[3 * f + j], b = job->F[3 * f + (j + 1) % 3];
+                job->grad_s[a] += gf;
+                const double dsv = sv[a] - sv[b];
+                smooth += 0.5 * dsv * dsv;
+                job->grad_s[a] += job->mu * dsv;
+                job->grad_s[b] -= job->mu * dsv;
+            }
+        }
+        *job->loss = lsum + job->mu * smooth;
+        MTK_CUDA_TRY(cudaEventRecord(c->ev_b, st));
+        MTK_CUDA_TRY(cudaStreamSynchronize(st));
+        float msj = 0;
+        cudaEventElapsedTime(&msj, c->ev_a, c->ev_b);
+        stt->ms_integrate += msj;
+        stt->igm_pcg_launches += S.pcg_launches;
+        stt->igm_pcg_ms += S.pcg_ms;
+        stt->igm_pcg_bytes += S.pcg_bytes;
+        expand_full<<<G, kStream, 0, st>>>(nFull, S.d_full2y.p, S.d_full2j.p, nY, nZ, S.Us.p, S.xs.p, S.Xfull.p);
+        c->kernels++;
+        MTK_CUDA_TRY(cudaMemcpyAsync(fullx, S.Xfull.p, sizeof(double) * nFull, cudaMemcpyDeviceToHost, st));
+        MTK_CUDA_TRY(cudaStreamSynchronize(st));
+        stt->kernel_launches = c->kernels;
+        return MTK_OK;
+    }
     if (x_naive) {
         expand_full<<<G, kStream, 0, st>>>(nFull, S.d_full2y.p, S.d_full2j.p, nY, nZ, S.Us.p, S.xs.p, S.Xfull.p);
         c->kernels++;
@@ -1464,4 +1608,21 @@ extern "C" int mtk_iterative_rounding(mtk_ctx* c, const mtk_igm_desc* d, const m
     stt->min_order_margin = std::min(stt->min_order_margin == 0 ? 1e300 : stt->min_order_margin, min_margin);
     if (!rounded) return finish(x0red.p);
     return finish(S.xs.p);
+}
+}  // namespace
+
+extern "C" int mtk_iterative_rounding(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts_in, double* fullx,
+                                      int32_t* fix_order, int32_t* fix_vals, int32_t* n_fixed, double* x_naive,
+                                      mtk_stats* stats) {
+    return igm_run(c, d, opts_in, fullx, fix_order, fix_vals, n_fixed, x_naive, stats, nullptr);
+}
+
+extern "C" int mtk_size_field_gradient(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts, int32_t nV,
+                                       const int32_t* F, const double* s, const double* T, double mu, double* loss,
+                                       double* grad_s, double* fullx, mtk_stats* stats) {
+    if (!c || !d || !F || !s || !loss || !grad_s || !fullx || nV <= 0 || !(mu >= 0)) return MTK_ERR_BAD_INPUT;
+    for (int64_t i = 0; i < 3 * (int64_t)d->nF; i++)
+        if (F[i] < 0 || F[i] >= nV) return MTK_ERR_BAD_INPUT;
+    SizeFieldJob job{nV, F, s, T, mu, loss, grad_s};
+    return igm_run(c, d, opts, fullx, nullptr, nullptr, nullptr, nullptr, stats, &job);
 }

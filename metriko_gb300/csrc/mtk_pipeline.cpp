@@ -122,6 +122,56 @@ extern "C" int mtk_pipeline_run(mtk_ctx* ctx, int32_t nV, int32_t nF, const doub
     }
 }
 
+extern "C" int mtk_pipeline_size_field_gradient(mtk_ctx* ctx, int32_t nV, int32_t nF, const double* Vb, const int32_t* Fb,
+                                                const mtk_pipeline_opts* popts, const mtk_solve_opts* sopts,
+                                                const double* s, const double* T, double mu, double* loss,
+                                                double* grad_s, double* fullx_out, int32_t fullx_cap, int32_t* n_full,
+                                                mtk_stats* stats) {
+    if (!ctx || nV <= 0 || nF <= 0 || !Vb || !Fb || !popts || !s || !loss || !grad_s) return MTK_ERR_BAD_INPUT;
+    gpu::bound_context() = ctx;
+    struct Unbind { ~Unbind() { gpu::bound_context() = nullptr; } } unbind;
+    gpu::stats() = mtk_stats{};
+    if (sopts) gpu::options().solve = *sopts;
+    else mtk_default_opts(&gpu::options().solve);
+    gpu::options().seed = popts->seed;
+    gpu::options().n_iter = popts->n_iter > 0 ? popts->n_iter : 50;
+    try {
+        MatXd V(nV, 3);
+        MatXi F(nF, 3);
+        std::memcpy(V.data(), Vb, sizeof(double) * 3 * size_t(nV));
+        std::memcpy(F.data(), Fb, sizeof(int32_t) * 3 * size_t(nF));
+        auto mesh = std::make_unique<Hmesh>(V, F);
+        FaceRosyField rawf(*mesh, 4, FieldType::Smoothest);
+        rawf.computeMatching(MatchingType::Curl);
+        auto seam = compute_seam(rawf);
+        auto cutm = compute_cut_mesh(*mesh, seam);
+        auto cmbf = compute_combbed_field(rawf, seam);
+        MatXd extf = compute_extrinsic_field(*mesh, *cmbf, 4);
+        RosyParameterization rp(*mesh, *cutm, extf, cmbf->singular, cmbf->matching, seam, 4, popts->ratio);
+        rp.seamless = false;
+        rp.localInjectivity = false;
+        rp.roundSeams = popts->round_seams != 0;
+        rp.verbose = false;
+        rp.setup();
+        VecXd sv(std::vector<double>(s, s + nV)), grad;
+        VecXd Tv;
+        if (T) Tv = VecXd(std::vector<double>(T, T + 8 * size_t(nF)));
+        *loss = rp.size_field_gradient(sv, T ? &Tv : nullptr, mu, grad);
+        std::memcpy(grad_s, grad.data(), sizeof(double) * nV);
+        const int nFull = rp.fullx.size();
+        if (n_full) *n_full = nFull;
+        if (fullx_out && fullx_cap >= nFull) std::memcpy(fullx_out, rp.fullx.data(), sizeof(double) * nFull);
+        if (stats) *stats = gpu::stats();
+        return MTK_OK;
+    } catch (const std::invalid_argument& e) {
+        mtk_set_last_error(e.what(), __FILE__, __LINE__);
+        return MTK_ERR_BAD_INPUT;
+    } catch (const std::exception& e) {
+        mtk_set_last_error(e.what(), __FILE__, __LINE__);
+        return MTK_ERR_CUDA;
+    }
+}
+
 extern "C" int mtk_topology_from_field(int32_t nV, int32_t nF, const double* Vb, const int32_t* Fb,
                                        const double* compressed, double ratio, int32_t round_seams,
                                        int32_t* singular, int32_t* matching, uint8_t* seam_out, int32_t* cutF,

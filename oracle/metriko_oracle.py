@@ -1128,3 +1128,54 @@ def pipeline(V, F, ratio=0.02, N=4, seed=0, seamless=True, round_seams=False, n_
     out.update(Cfull=Cfull, G2=G2, F2=F2, length=length, success=ok, fullx=fullx, nfn=nfn,
                cfn=cfn, info=info, stats=stats, fullx2N=fullx2N)
     return out
+
+
+# --------------------------------------------------------------------------------------------
+# Size-field gradient of the naive integration (differentiation; no counterpart in the
+# reference).  Restates mtk_size_field_gradient with direct KKT solves: the target of face f is
+# exp(sbar_f) F2_f (sbar_f the mean of s over the face's corners), x(s) solves the anchored
+# naive-integration KKT system of iter_rounding_init.h:171-212, and
+#   l(s) = sum_f |length X2F_f x - exp(sbar_f) T_f|^2 + mu sum_edges (s_i - s_j)^2
+# is differentiated through one adjoint KKT solve with the same matrix.
+# --------------------------------------------------------------------------------------------
+def size_field_gradient(out, F, s, T=None, mu=0.0):
+    """out: the dict of pipeline(...) (needs G2, fullx2N, Cfull, F2, length, setup).
+    Returns (loss, grad_s, fullx(s))."""
+    F = np.asarray(F)
+    nF = len(F)
+    st = out["setup"]
+    G2full = (out["G2"] @ out["fullx2N"]).tocsr()
+    UFull = build_ufull(out["Cfull"])[0]
+    X2F = (G2full @ UFull).tocsr()
+    length = out["length"]
+    F2 = out["F2"]
+    T = F2 if T is None else np.asarray(T, float).reshape(-1)
+    sbar = s[F].mean(axis=1)
+    es = np.exp(sbar)
+    es8 = np.repeat(es, 8)
+    fixedIdcs = np.asarray(st["fixedIdcs"])
+    fixedVals = np.asarray(st["fixedVals"], float)
+    Cfix = UFull[fixedIdcs, :]
+    nd = X2F.shape[1]
+    K = sp.bmat([[(X2F.T @ X2F) * length, Cfix.T], [Cfix, None]]).tocsc()
+    lu = spla.splu(K)
+    xs = lu.solve(np.concatenate([X2F.T @ (es8 * F2), fixedVals]))[:nd]
+    r = length * (X2F @ xs) - es8 * T
+    loss = float(r @ r)
+    gx = 2.0 * length * (X2F.T @ r)
+    lam = lu.solve(np.concatenate([gx, np.zeros(len(fixedIdcs))]))[:nd]
+    q = ((X2F @ lam) * F2).reshape(nF, 8).sum(1)
+    rT = (r * T).reshape(nF, 8).sum(1)
+    gf = es / 3.0 * (q - 2.0 * rT)
+    grad = np.zeros(len(s))
+    for j in range(3):
+        np.add.at(grad, F[:, j], gf)
+    # smoothness: each edge of a closed mesh lies in two faces, each contributing half
+    smooth = 0.0
+    for j in range(3):
+        a, b = F[:, j], F[:, (j + 1) % 3]
+        d = s[a] - s[b]
+        smooth += 0.5 * float(d @ d)
+        np.add.at(grad, a, mu * d)
+        np.add.at(grad, b, -mu * d)
+    return loss + mu * smooth, grad, UFull @ xs

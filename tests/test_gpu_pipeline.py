@@ -61,17 +61,24 @@ def test_pipeline_deterministic(gpu_ctx):
     assert list(a["fix_order"]) == list(b["fix_order"])
 
 
-@pytest.mark.parametrize("name", ["ico6_sh8"])
-def test_pipeline_size_independent_properties(gpu_ctx, name):
-    """At sizes beyond the oracle: sum of indices = 8 on a sphere, every rounded value within
-    1e-6 of an integer and equal to the reported value, all solves at the requested residual."""
+# full-size workloads: level-7 sphere (327,680 faces), the 1024 x 512 torus (1,048,576 faces,
+# seams rounded), the level-9 sphere with degree-16 displacement (5,242,880 faces)
+@pytest.mark.parametrize("name,prec,chi", [("ico6_sh8", "mixed", 2), ("ico7_sh8", "mixed", 2), ("ico7_sh8", "fp64", 2),
+                                           ("torus_1024x512", "mixed", 0), ("ico9_sh16", "mixed", 2)])
+def test_pipeline_size_independent_properties(gpu_ctx, name, prec, chi):
+    """At sizes beyond the oracle: sum of indices = 4 chi (Poincare-Hopf), every rounded value
+    within 1e-6 of an integer and equal to the reported value, all solves at the requested
+    residual."""
     V, F, ratio, rs = meshgen.workload(name)
-    r = M.pipeline(gpu_ctx, V, F, ratio=ratio, round_seams=rs, opts=M.solve_opts("mixed", tol=1e-8))
+    r = M.pipeline(gpu_ctx, V, F, ratio=ratio, round_seams=rs, opts=M.solve_opts(prec, tol=1e-8))
     assert r["status"] == 0
-    assert r["singular"].sum() == 8
+    assert r["singular"].sum() == 4 * chi
     X = r["fullx"]
     fo = r["fix_order"]
-    assert len(fo) == 2 * (r["counts"]["nS"] + r["counts"]["nT"])
+    if chi != 0:
+        assert len(fo) == 2 * (r["counts"]["nS"] + r["counts"]["nT"])
+    else:   # torus with round_seams: the translations of every transition are rounded
+        assert len(fo) == 2 * r["counts"]["nT"] and len(fo) > 0
     assert np.abs(X[fo] - np.round(X[fo])).max() <= 1e-6
     assert np.array_equal(np.round(X[fo]).astype(int), r["fix_vals"])
     assert r["stats"]["max_rel_residual"] <= 1e-8 * 1.0001
