@@ -59,7 +59,7 @@ typedef struct {
     double tol;                 /* relative residual ||b - A x|| / ||b|| per solve       */
     int32_t max_iter;           /* PCG iteration cap per inner solve                     */
     int32_t max_refine;         /* outer FP64 refinement steps (MIXED)                   */
-    double inner_tol;           /* relative tolerance of each inner FP32 solve (MIXED)   */
+    double inner_tol;           /* relative tolerance of each inner FP32 solve (MIXED; default 3e-6) */
 } mtk_solve_opts;
 
 typedef struct {

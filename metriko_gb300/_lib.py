@@ -104,7 +104,7 @@ def _ptr(a):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
 
 
-def solve_opts(precision="mixed", tol=1e-8, max_iter=50000, max_refine=12, inner_tol=1e-4):
+def solve_opts(precision="mixed", tol=1e-8, max_iter=50000, max_refine=12, inner_tol=3e-6):
     o = SolveOpts()
     lib().mtk_default_opts(C.byref(o))
     o.precision = PREC_MIXED if precision == "mixed" else PREC_FP64

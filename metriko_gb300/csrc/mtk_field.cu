@@ -1273,7 +1273,11 @@ extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const 
                                              S.q32.p /*p*/, reinterpret_cast<float2*>(S.Lu.p) /*q*/, S.rb32.p, S.pb32.p,
                                              S.sv32.p, S.vv32.p, itol * itol * rr,
                                              opts.max_iter, &iters, nullptr);
-                if (s == MTK_ERR_TIMEOUT || s == MTK_ERR_BREAKDOWN) return s;
+                // an FP32 breakdown (p^H A p <= 0 in single precision) means the inner solve has
+                // stagnated: its last iterate is still a valid correction, and the FP64 refinement
+                // decides what comes next (bounded by max_refine, stopped when it makes no progress)
+                if (s == MTK_ERR_TIMEOUT) return s;
+                const double rr_prev = rr;
                 add_correction<<<G, kStream, 0, st>>>(n, S.e32.p, S.x.p);
                 residual64<<<G, kStream, 0, st>>>(S.A64(), S.b.p, S.x.p, S.r.p, S.r32.p, c->partials);
                 c->kernels += 2;
@@ -1281,6 +1285,8 @@ extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const 
                 MTK_TRY(S.read_scalars(1));
                 rr = c->h_scalars[0];
                 refines++;
+                if (!(rr == rr)) return MTK_ERR_BREAKDOWN;
+                if (rr > goal2 && rr >= rr_prev) return MTK_ERR_NOT_CONVERGED;
             }
         }
         double rel = bnorm2 > 0 ? std::sqrt(rr / bnorm2) : 0.0;

@@ -977,7 +977,11 @@ struct Igm {
                 int s = run_pcg<float>(op32(scale, shift), ZProj<float>{kq, Qz32.p, Mz32.p}, minvy32.p, r32.p, e32.p,
                                        z32.p /*r*/, p32.p /*z*/, q32.p /*p*/, reinterpret_cast<float*>(Xfull.p) /*q*/,
                                        itol * itol * rr, o.max_iter, 0, smem32, &iters, nullptr);
-                if (s == MTK_ERR_TIMEOUT || s == MTK_ERR_BREAKDOWN) return s;
+                // an FP32 breakdown (p^H A p <= 0 in single precision) means the inner solve has
+                // stagnated: its last iterate is still a valid correction, and the FP64 refinement
+                // decides what comes next (bounded by max_refine, stopped when it makes no progress)
+                if (s == MTK_ERR_TIMEOUT) return s;
+                const double rr_prev = rr;
                 add_f32<<<grid(), kStream, 0, st>>>(nY, e32.p, x);
                 if (nZ > 0)
                     add_z_projected<<<1, kStream, sizeof(double) * 2 * (size_t)nZ, st>>>(nY, nZ, kq, Qz.p, e32.p, x);
@@ -985,6 +989,8 @@ struct Igm {
                 MTK_TRY(run_pcg<double>(op64(scale, shift), ZProj<double>{kq, Qz.p, Mz.p}, minvy.p, b, x, r64.p, z64.p,
                                         p64.p, q64.p, 0.0, 0, 1, smem64, nullptr, &rr));
                 refines++;
+                if (!(rr == rr)) return MTK_ERR_BREAKDOWN;
+                if (rr > goal2 && rr >= rr_prev) return MTK_ERR_NOT_CONVERGED;
             }
         }
         double rel = bb > 0 ? std::sqrt(rr / bb) : 0.0;
