@@ -28,26 +28,39 @@
 namespace mtk {
 
 // Builds CSR rows in parallel: fn(row, add) calls add(col, value) for the entries of `row`
-// (duplicates are summed).  Two passes over the rows: the first counts the distinct columns of
-// every row, the second writes each row (sorted by column) straight into the final arrays, so
-// there are no per-thread buffers to grow and concatenate.  Every row is formed by one thread
-// in the same order whatever the thread count, so the result does not depend on it.
+// (duplicates are summed in call order).  Two passes over the rows: the first counts the
+// distinct columns of every row, the second writes each row (sorted by column) straight into
+// the final arrays.  A row is accumulated in a dense per-thread array of the column count when
+// those arrays stay below 256 MB over all threads, otherwise as (column, value) pairs that
+// are stably sorted; both sum duplicates in call order, so the arrays are the same either way.
+// Every row is formed by one thread in the same order whatever the thread count.
 template <typename V, typename RowFn>
 void build_rows_parallel(int nrows, int ncols, RowFn fn, std::vector<int>& ptr, std::vector<int>& col,
                          std::vector<V>& val) {
+    int nt = 1;
+#ifdef _OPENMP
+    nt = omp_get_max_threads();
+#endif
+    const bool dense = (double)ncols * nt * (sizeof(V) + 1) <= 256.0 * 1024 * 1024;
     ptr.assign(nrows + 1, 0);
 #pragma omp parallel
     {
-        std::vector<char> used(ncols, 0);
         std::vector<int> cols;
+        std::vector<char> used(dense ? ncols : 0, 0);
 #pragma omp for schedule(static)
         for (int r = 0; r < nrows; r++) {
             cols.clear();
-            fn(r, [&](int c, V) {
-                if (!used[c]) { used[c] = 1; cols.push_back(c); }
-            });
-            for (int c : cols) used[c] = 0;
-            ptr[r + 1] = (int)cols.size();
+            if (dense) {
+                fn(r, [&](int c, V) {
+                    if (!used[c]) { used[c] = 1; cols.push_back(c); }
+                });
+                for (int c : cols) used[c] = 0;
+                ptr[r + 1] = (int)cols.size();
+            } else {
+                fn(r, [&](int c, V) { cols.push_back(c); });
+                std::sort(cols.begin(), cols.end());
+                ptr[r + 1] = (int)(std::unique(cols.begin(), cols.end()) - cols.begin());
+            }
         }
     }
     for (int r = 0; r < nrows; r++) ptr[r + 1] += ptr[r];
@@ -55,19 +68,36 @@ void build_rows_parallel(int nrows, int ncols, RowFn fn, std::vector<int>& ptr, 
     val.resize(ptr[nrows]);
 #pragma omp parallel
     {
-        std::vector<V> acc(ncols, V(0));
-        std::vector<char> used(ncols, 0);
         std::vector<int> cols;
+        std::vector<V> acc(dense ? ncols : 0, V(0));
+        std::vector<char> used(dense ? ncols : 0, 0);
+        std::vector<std::pair<int, V>> ent;
 #pragma omp for schedule(static)
         for (int r = 0; r < nrows; r++) {
-            cols.clear();
-            fn(r, [&](int c, V v) {
-                if (!used[c]) { used[c] = 1; cols.push_back(c); acc[c] = V(0); }
-                acc[c] += v;
-            });
-            std::sort(cols.begin(), cols.end());
             int q = ptr[r];
-            for (int c : cols) { col[q] = c; val[q] = acc[c]; used[c] = 0; q++; }
+            if (dense) {
+                cols.clear();
+                fn(r, [&](int c, V v) {
+                    if (!used[c]) { used[c] = 1; cols.push_back(c); acc[c] = V(0); }
+                    acc[c] += v;
+                });
+                std::sort(cols.begin(), cols.end());
+                for (int c : cols) { col[q] = c; val[q] = acc[c]; used[c] = 0; q++; }
+            } else {
+                ent.clear();
+                fn(r, [&](int c, V v) { ent.emplace_back(c, v); });
+                std::stable_sort(ent.begin(), ent.end(), [](const auto& x, const auto& y) { return x.first < y.first; });
+                q--;
+                for (size_t k = 0; k < ent.size(); k++) {
+                    if (k == 0 || ent[k].first != ent[k - 1].first) {
+                        q++;
+                        col[q] = ent[k].first;
+                        val[q] = ent[k].second;
+                    } else {
+                        val[q] += ent[k].second;
+                    }
+                }
+            }
         }
     }
 }
