@@ -31,8 +31,7 @@ namespace metriko {
             : BaseVectorField(m, nRosy) {
             switch (type) {
                 case FieldType::Smoothest: compressed = solveSmoothest(start); break;
-                case FieldType::CurvatureAligned:
-                    throw std::invalid_argument("FieldType::CurvatureAligned is not part of this build");
+                case FieldType::CurvatureAligned: compressed = solveCurvatureAligned(); break;
                 default: break;
             }
             if (compressed.size() == m.nF) set_field_from_compressed();
@@ -79,6 +78,57 @@ namespace metriko {
             gpu::check(mtk_field_smoothest(gpu::context(), mesh.nF, rosyN, nbr.data(), theta.data(), mesh.faceArea.data(),
                                            x0.data(), nIter, &gpu::options().solve, out.data(), &gpu::stats()),
                        "mtk_field_smoothest");
+            VecXc c(mesh.nF);
+            for (int f = 0; f < mesh.nF; f++) c[f] = complex(out[2 * f], out[2 * f + 1]);
+            return c;
+        }
+
+        // face_rosy_field.h:86-98: D_f = 1/4 sum over the halfedges h of f of
+        // -(e^{i farg(h)} |h|)^2 / |h| * dihedral(h), with the dihedral angle of h
+        // atan2(v . (n1 x n2), n1 . n2) (v = h / |h|, n1, n2 the normals of h's and twin(h)'s faces,
+        // hmesh.h:508-519).
+        VecXc principalCurvatureDir() const {
+            VecXc D(mesh.nF);
+            METRIKO_PARALLEL_FOR
+            for (int f = 0; f < mesh.nF; f++) {
+                complex dir(0, 0);
+                for (int j = 0; j < 3; j++) {
+                    const int h = mesh.face2half3(f, j);
+                    const Half hh{{h, &mesh}};
+                    const Row3d vec = hh.vec();
+                    const double l = vec.norm();
+                    const Row3d n1 = row3(mesh.faceNormal, f), n2 = row3(mesh.faceNormal, mesh.face[mesh.twin[h]]);
+                    const double darg = std::atan2((vec / l).dot(n1.cross(n2)), n1.dot(n2));
+                    const complex c = std::polar(1., mesh.heArgOnFace[h]) * l;
+                    dir += -c * c / l * darg;
+                }
+                D[f] = dir * 0.25;
+            }
+            return D;
+        }
+
+        // face_rosy_field.h:23-32 (lambda = 0): D (squared for N = 4), rhs = M D / sqrt|D^H M D|,
+        // compressed = L^-1 rhs by one device solve (mtk_field_solve).
+        VecXc solveCurvatureAligned() {
+            if (rosyN != 2 && rosyN != 4) throw std::invalid_argument("CurvatureAligned needs N = 2 or 4");
+            VecXc D = principalCurvatureDir();
+            if (rosyN == 4) for (int f = 0; f < mesh.nF; f++) D[f] = D[f] * D[f];
+            double dmd = 0;
+            for (int f = 0; f < mesh.nF; f++) dmd += mesh.faceArea[f] * std::norm(D[f]);
+            const double sc = 1.0 / std::sqrt(std::abs(dmd));
+            std::vector<double> rhs(2 * size_t(mesh.nF));
+            for (int f = 0; f < mesh.nF; f++) {
+                const complex v = mesh.faceArea[f] * D[f] * sc;
+                rhs[2 * f] = v.real();
+                rhs[2 * f + 1] = v.imag();
+            }
+            std::vector<int> nbr;
+            std::vector<double> theta;
+            assembly_inputs(nbr, theta);
+            std::vector<double> out(2 * size_t(mesh.nF));
+            gpu::check(mtk_field_solve(gpu::context(), mesh.nF, rosyN, nbr.data(), theta.data(), mesh.faceArea.data(),
+                                       rhs.data(), &gpu::options().solve, out.data(), &gpu::stats()),
+                       "mtk_field_solve");
             VecXc c(mesh.nF);
             for (int f = 0; f < mesh.nF; f++) c[f] = complex(out[2 * f], out[2 * f + 1]);
             return c;

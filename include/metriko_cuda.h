@@ -173,6 +173,7 @@ typedef struct {
     int32_t round_seams;        /* RosyParameterization::roundSeams                       */
     int32_t seamless;           /* RosyParameterization::seamless                         */
     int32_t stop_after;         /* 0 = full path, 1 = after field+matching, 2 = after setup */
+    int32_t field_type;         /* 0 = FieldType::Smoothest, 1 = FieldType::CurvatureAligned */
 } mtk_pipeline_opts;
 
 int mtk_pipeline_run(mtk_ctx* ctx, int32_t nV, int32_t nF, const double* V, const int32_t* F,
@@ -212,6 +213,16 @@ int mtk_topology_from_field(int32_t nV, int32_t nF, const double* V, const int32
 int mtk_field_smoothest_noalloc(int32_t nF, int32_t nRosy, const int32_t* nbr, const double* theta,
                                 const double* area, const double* x0, int32_t n_iter, double tol,
                                 int32_t max_iter, double* out, void* stream, int32_t* iterations);
+
+/*
+ * One solve L x = rhs with the connection Laplacian of mtk_field_smoothest (same inputs, same
+ * assembly, preconditioner and precision options).  Replaces solveSquare(lhs, rhs) of
+ * face_rosy_field.h:23-32 / sparse_linear_solver.h:16-27 for FieldType::CurvatureAligned
+ * (lambda = 0, so lhs = L).  rhs[2*nF] and out[2*nF] are (re, im) per face.
+ */
+int mtk_field_solve(mtk_ctx* ctx, int32_t nF, int32_t nRosy, const int32_t* nbr, const double* theta,
+                    const double* area, const double* rhs, const mtk_solve_opts* opts, double* out,
+                    mtk_stats* stats);
 
 /*
  * Gradient of a parameterization-quality loss with respect to a per-vertex log-size field

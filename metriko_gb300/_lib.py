@@ -21,7 +21,7 @@ EXPORTS = [
     "mtk_status_string", "mtk_last_error", "mtk_default_opts", "mtk_ctx_create", "mtk_ctx_destroy",
     "mtk_ctx_kernel_count", "mtk_field_smoothest", "mtk_iterative_rounding", "mtk_pipeline_run",
     "mtk_seeded_init", "mtk_topology_from_field", "mtk_field_smoothest_noalloc", "mtk_size_field_gradient",
-    "mtk_pipeline_size_field_gradient",
+    "mtk_pipeline_size_field_gradient", "mtk_field_solve",
 ]
 
 
@@ -52,7 +52,8 @@ class Stats(C.Structure):
 
 class PipelineOpts(C.Structure):
     _fields_ = [("seed", C.c_int32), ("n_iter", C.c_int32), ("ratio", C.c_double),
-                ("round_seams", C.c_int32), ("seamless", C.c_int32), ("stop_after", C.c_int32)]
+                ("round_seams", C.c_int32), ("seamless", C.c_int32), ("stop_after", C.c_int32),
+                ("field_type", C.c_int32)]
 
 
 _lib = None
@@ -86,6 +87,8 @@ def lib():
         L.mtk_field_smoothest_noalloc.argtypes = [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
                                                   C.c_void_p, C.c_int32, C.c_double, C.c_int32, C.c_void_p,
                                                   C.c_void_p, C.POINTER(C.c_int32)]
+        L.mtk_field_solve.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.c_void_p, C.POINTER(SolveOpts), C.c_void_p, C.POINTER(Stats)]
         L.mtk_pipeline_size_field_gradient.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
                                                        C.POINTER(PipelineOpts), C.POINTER(SolveOpts), C.c_void_p,
                                                        C.c_void_p, C.c_double, C.POINTER(C.c_double), C.c_void_p,
@@ -164,7 +167,7 @@ def field_smoothest(ctx: Context, nbr, theta, area, x0, n_rosy=4, n_iter=50, opt
 
 
 def pipeline(ctx: Context, V, F, ratio=0.02, seed=0, round_seams=False, seamless=True, n_iter=50,
-             opts=None, stop_after=0, check=True):
+             opts=None, stop_after=0, check=True, field_type="smoothest"):
     """mtk_pipeline_run: Hmesh -> smoothest field -> Curl matching -> seams -> cut mesh ->
     combing -> RosyParameterization setup()/integ() (example_igm.cpp:13-31)."""
     V = np.ascontiguousarray(V, np.float64)
@@ -185,7 +188,8 @@ def pipeline(ctx: Context, V, F, ratio=0.02, seed=0, round_seams=False, seamless
     counts = np.zeros(8, np.int32)
     n_full = C.c_int32(0)
     n_fixed = C.c_int32(0)
-    p = PipelineOpts(seed, n_iter, ratio, int(round_seams), int(seamless), stop_after)
+    p = PipelineOpts(seed, n_iter, ratio, int(round_seams), int(seamless), stop_after,
+                     {"smoothest": 0, "curvature_aligned": 1}[field_type])
     o = opts or solve_opts()
     st = Stats()
     status = lib().mtk_pipeline_run(ctx.handle, nV, nF, _ptr(V), _ptr(F), C.byref(p), C.byref(o),
@@ -201,6 +205,22 @@ def pipeline(ctx: Context, V, F, ratio=0.02, seed=0, round_seams=False, seamless
                 fix_order=fix_order[:nfix].copy(), fix_vals=fix_vals[:nfix].copy(),
                 counts=dict(zip(["nV", "nE", "nCut", "nT", "nS", "nJ", "nZ", "nFull"], counts.tolist())),
                 stats=st.as_dict())
+
+
+def field_solve(ctx: Context, nbr, theta, area, rhs, n_rosy=4, opts=None):
+    """mtk_field_solve: one solve L x = rhs with the field's connection Laplacian."""
+    nbr = np.ascontiguousarray(nbr, np.int32).reshape(-1)
+    theta = np.ascontiguousarray(theta, np.float64).reshape(-1)
+    area = np.ascontiguousarray(area, np.float64)
+    nF = len(area)
+    r = np.empty(2 * nF)
+    r[0::2], r[1::2] = np.real(rhs), np.imag(rhs)
+    out = np.empty(2 * nF)
+    st = Stats()
+    o = opts or solve_opts()
+    _check(lib().mtk_field_solve(ctx.handle, nF, n_rosy, _ptr(nbr), _ptr(theta), _ptr(area), _ptr(r), C.byref(o),
+                                 _ptr(out), C.byref(st)), "mtk_field_solve")
+    return out[0::2] + 1j * out[1::2], st.as_dict()
 
 
 def size_field_gradient(ctx: Context, V, F, s, T=None, mu=0.0, ratio=0.02, seed=0, round_seams=False, n_iter=50,
@@ -226,7 +246,7 @@ def size_field_gradient(ctx: Context, V, F, s, T=None, mu=0.0, ratio=0.02, seed=
     grad = np.zeros(nV)
     loss = C.c_double(0)
     n_full = C.c_int32(0)
-    p = PipelineOpts(seed, n_iter, ratio, int(round_seams), 0, 0)
+    p = PipelineOpts(seed, n_iter, ratio, int(round_seams), 0, 0, 0)
     o = opts or solve_opts()
     st = Stats()
     _check(lib().mtk_pipeline_size_field_gradient(ctx.handle, nV, nF, _ptr(V), _ptr(F), C.byref(p), C.byref(o), _ptr(s),

@@ -784,6 +784,20 @@ __global__ void normalize_to(int n, const double* __restrict__ scal, const doubl
     }
 }
 
+// Start of a plain solve L x = b: x = 0, r = b, r32 = r, partial |b|^2.
+__global__ void start_from_rhs(int n, const double2* __restrict__ b, double2* x, double2* r, float2* r32,
+                               double* partials) {
+    double red[1] = {0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double2 bi = b[i];
+        x[i] = make_double2(0.0, 0.0);
+        r[i] = bi;
+        if (r32) r32[i] = make_float2((float)bi.x, (float)bi.y);
+        red[0] += bi.x * bi.x + bi.y * bi.y;
+    }
+    publish_partials<double, 1>(red, partials);
+}
+
 __global__ void zero_f2(int n, float2* e) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) e[i] = make_float2(0.f, 0.f);
 }
@@ -1104,10 +1118,15 @@ template <> DevHierarchy<float> FieldSolver::hier<float>() const { return H32; }
 
 }  // namespace
 
-extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const int32_t* nbr_h,
-                                   const double* theta_h, const double* area_h, const double* x0,
-                                   int32_t n_iter, const mtk_solve_opts* opts_in, double* out, mtk_stats* stats) {
-    if (!c || nF <= 0 || nRosy <= 0 || !nbr_h || !theta_h || !area_h || !x0 || !out || n_iter < 0) return MTK_ERR_BAD_INPUT;
+namespace {
+// The field solves: with rhs == nullptr the inverse power iteration from x0 (n_iter steps,
+// M-normalised), otherwise one solve L x = rhs from x = 0 (x0 and n_iter unused).
+int field_run(mtk_ctx* c, int32_t nF, int32_t nRosy, const int32_t* nbr_h, const double* theta_h, const double* area_h,
+              const double* x0, int32_t n_iter, const mtk_solve_opts* opts_in, double* out, mtk_stats* stats,
+              const double* rhs) {
+    if (rhs) n_iter = 1;
+    if (!c || nF <= 0 || nRosy <= 0 || !nbr_h || !theta_h || !area_h || (!x0 && !rhs) || !out || n_iter < 0)
+        return MTK_ERR_BAD_INPUT;
     for (int64_t i = 0; i < 3 * (int64_t)nF; i++)
         if (nbr_h[i] < 0 || nbr_h[i] >= nF) { mtk_set_last_error("face neighbour out of range (closed meshes only)", __FILE__, __LINE__); return MTK_ERR_BAD_INPUT; }
     mtk_solve_opts opts;
@@ -1150,26 +1169,30 @@ extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const 
                 theta_p[3 * (size_t)k + j] = theta_h[3 * (size_t)f + j];
             }
             area_p[k] = area_h[f];
-            x0_p[2 * (size_t)k] = x0[2 * (size_t)f];
-            x0_p[2 * (size_t)k + 1] = x0[2 * (size_t)f + 1];
+            const double* src = rhs ? rhs : x0;   // the vector that enters in face order
+            x0_p[2 * (size_t)k] = src[2 * (size_t)f];
+            x0_p[2 * (size_t)k + 1] = src[2 * (size_t)f + 1];
         }
         nbr_u = nbr_p.data();
         theta_u = theta_p.data();
         area_u = area_p.data();
         x0_u = x0_p.data();
+    } else if (rhs) {
+        x0_u = rhs;
     }
     MTK_TRY(S.nbr_in.upload(nbr_u, 3 * (size_t)n, st));
     MTK_TRY(S.theta.upload(theta_u, 3 * (size_t)n, st));
     MTK_TRY(S.area.upload(area_u, n, st));
     const int ring = std::min(kRing, std::max(n_iter, 1));
     for (int j = 0; j < ring; j++) { MTK_TRY(S.ringU[j].alloc(n)); MTK_TRY(S.ringL[j].alloc(n)); }
-    MTK_CUDA_TRY(cudaMemcpyAsync(S.ringU[0].p, x0_u, sizeof(double2) * n, cudaMemcpyHostToDevice, st));
+    if (!rhs) MTK_CUDA_TRY(cudaMemcpyAsync(S.ringU[0].p, x0_u, sizeof(double2) * n, cudaMemcpyHostToDevice, st));
     MTK_TRY(S.nbr.alloc(3 * (size_t)n));
     MTK_TRY(S.v64.alloc(3 * (size_t)n));
     MTK_TRY(S.v32.alloc(3 * (size_t)n));
     MTK_TRY(S.d64.alloc(n)); MTK_TRY(S.inv64.alloc(n)); MTK_TRY(S.d32.alloc(n)); MTK_TRY(S.inv32.alloc(n));
     MTK_TRY(S.area32.alloc(n));
     MTK_TRY(S.b.alloc(n)); MTK_TRY(S.Lu.alloc(n)); MTK_TRY(S.x.alloc(n)); MTK_TRY(S.r.alloc(n));
+    if (rhs) MTK_CUDA_TRY(cudaMemcpyAsync(S.b.p, x0_u, sizeof(double2) * n, cudaMemcpyHostToDevice, st));
     const bool mixed = opts.precision == MTK_PREC_MIXED;
     if (mixed) {
         MTK_TRY(S.r32.alloc(n)); MTK_TRY(S.e32.alloc(n)); MTK_TRY(S.z32.alloc(n)); MTK_TRY(S.p32.alloc(n)); MTK_TRY(S.q32.alloc(n));
@@ -1189,58 +1212,67 @@ extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const 
     std::vector<double> Gr(kRing * kRing, 0.0), Gi(kRing * kRing, 0.0);
     const double tol = opts.tol;
     for (int k = 0; k < n_iter; k++) {
-        // b = M u_k, L u_k kept in the ring; Galerkin start on the last `ring` iterates
-        const int slot = k % ring;
-        const int cnt = std::min(k + 1, ring);
-        double2* uk = S.ringU[slot].p;
-        power_prepare<<<G, kStream, 0, st>>>(S.A64(), S.area.p, uk, S.b.p, S.ringL[slot].p, c->partials);
-        c->kernels++;
-        MTK_TRY(S.finalize(G, 3));
-        MTK_CUDA_TRY(cudaMemcpyAsync(c->h_scalars, c->scalars, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
-        RingPtrs R{};
-        std::vector<int> slots(cnt);
-        for (int j = 0; j < cnt; j++) {
-            int sj = (slot - j + ring) % ring;
-            slots[j] = sj;
-            R.V[j] = S.ringU[sj].p;
-            R.LV[j] = S.ringL[sj].p;
-        }
-        R.cnt = cnt;
-        gram_row<<<G, kStream, 0, st>>>(n, R, uk, S.b.p, c->partials);
-        c->kernels++;
-        MTK_TRY(S.finalize(G, 4 * cnt));
-        MTK_CUDA_TRY(cudaMemcpyAsync(c->h_scalars + 8, c->scalars, 4 * cnt * sizeof(double), cudaMemcpyDeviceToHost, st));
-        MTK_CUDA_TRY(cudaStreamSynchronize(st));
-        // row / column of the new iterate; older entries stay valid (their vectors are unchanged)
-        for (int j = 0; j < cnt; j++) {
-            int sj = slots[j];
-            double gr = c->h_scalars[8 + 4 * j], gi = c->h_scalars[8 + 4 * j + 1];
-            Gr[slot * kRing + sj] = gr;
-            Gi[slot * kRing + sj] = gi;
-            Gr[sj * kRing + slot] = gr;
-            Gi[sj * kRing + slot] = -gi;
-            if (sj == slot) Gi[slot * kRing + slot] = 0.0;
-        }
-        std::vector<double> gr_sub(kRing * kRing), gi_sub(kRing * kRing), hr(cnt), hi(cnt), yr, yi;
-        for (int a = 0; a < cnt; a++) {
-            for (int b2 = 0; b2 < cnt; b2++) {
-                gr_sub[a * kRing + b2] = Gr[slots[a] * kRing + slots[b2]];
-                gi_sub[a * kRing + b2] = Gi[slots[a] * kRing + slots[b2]];
+        double bnorm2 = 0, rr = 0;
+        if (rhs) {   // plain solve: x = 0, r = b
+            start_from_rhs<<<G, kStream, 0, st>>>(n, S.b.p, S.x.p, S.r.p, mixed ? S.r32.p : nullptr, c->partials);
+            c->kernels++;
+            MTK_TRY(S.finalize(G, 1));
+            MTK_TRY(S.read_scalars(1));
+            bnorm2 = rr = c->h_scalars[0];
+        } else {
+            // b = M u_k, L u_k kept in the ring; Galerkin start on the last `ring` iterates
+            const int slot = k % ring;
+            const int cnt = std::min(k + 1, ring);
+            double2* uk = S.ringU[slot].p;
+            power_prepare<<<G, kStream, 0, st>>>(S.A64(), S.area.p, uk, S.b.p, S.ringL[slot].p, c->partials);
+            c->kernels++;
+            MTK_TRY(S.finalize(G, 3));
+            MTK_CUDA_TRY(cudaMemcpyAsync(c->h_scalars, c->scalars, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+            RingPtrs R{};
+            std::vector<int> slots(cnt);
+            for (int j = 0; j < cnt; j++) {
+                int sj = (slot - j + ring) % ring;
+                slots[j] = sj;
+                R.V[j] = S.ringU[sj].p;
+                R.LV[j] = S.ringL[sj].p;
             }
-            hr[a] = c->h_scalars[8 + 4 * a + 2];
-            hi[a] = c->h_scalars[8 + 4 * a + 3];
+            R.cnt = cnt;
+            gram_row<<<G, kStream, 0, st>>>(n, R, uk, S.b.p, c->partials);
+            c->kernels++;
+            MTK_TRY(S.finalize(G, 4 * cnt));
+            MTK_CUDA_TRY(cudaMemcpyAsync(c->h_scalars + 8, c->scalars, 4 * cnt * sizeof(double), cudaMemcpyDeviceToHost, st));
+            MTK_CUDA_TRY(cudaStreamSynchronize(st));
+            // row / column of the new iterate; older entries stay valid (their vectors are unchanged)
+            for (int j = 0; j < cnt; j++) {
+                int sj = slots[j];
+                double gr = c->h_scalars[8 + 4 * j], gi = c->h_scalars[8 + 4 * j + 1];
+                Gr[slot * kRing + sj] = gr;
+                Gi[slot * kRing + sj] = gi;
+                Gr[sj * kRing + slot] = gr;
+                Gi[sj * kRing + slot] = -gi;
+                if (sj == slot) Gi[slot * kRing + slot] = 0.0;
+            }
+            std::vector<double> gr_sub(kRing * kRing), gi_sub(kRing * kRing), hr(cnt), hi(cnt), yr, yi;
+            for (int a = 0; a < cnt; a++) {
+                for (int b2 = 0; b2 < cnt; b2++) {
+                    gr_sub[a * kRing + b2] = Gr[slots[a] * kRing + slots[b2]];
+                    gi_sub[a * kRing + b2] = Gi[slots[a] * kRing + slots[b2]];
+                }
+                hr[a] = c->h_scalars[8 + 4 * a + 2];
+                hi[a] = c->h_scalars[8 + 4 * a + 3];
+            }
+            hermitian_pinv_solve(gr_sub, gi_sub, hr, hi, cnt, yr, yi);
+            StartCoef sc{};
+            for (int j = 0; j < cnt; j++) { sc.re[j] = yr[j]; sc.im[j] = yi[j]; sc.V[j] = R.V[j]; sc.LV[j] = R.LV[j]; }
+            sc.cnt = cnt;
+            combine_start<<<G, kStream, 0, st>>>(n, sc, S.b.p, S.x.p, S.r.p, mixed ? S.r32.p : nullptr, c->partials);
+            c->kernels++;
+            MTK_TRY(S.finalize(G, 1));
+            MTK_CUDA_TRY(cudaMemcpyAsync(c->h_scalars + 3, c->scalars, sizeof(double), cudaMemcpyDeviceToHost, st));
+            MTK_CUDA_TRY(cudaStreamSynchronize(st));
+            bnorm2 = c->h_scalars[2];
+            rr = c->h_scalars[3];
         }
-        hermitian_pinv_solve(gr_sub, gi_sub, hr, hi, cnt, yr, yi);
-        StartCoef sc{};
-        for (int j = 0; j < cnt; j++) { sc.re[j] = yr[j]; sc.im[j] = yi[j]; sc.V[j] = R.V[j]; sc.LV[j] = R.LV[j]; }
-        sc.cnt = cnt;
-        combine_start<<<G, kStream, 0, st>>>(n, sc, S.b.p, S.x.p, S.r.p, mixed ? S.r32.p : nullptr, c->partials);
-        c->kernels++;
-        MTK_TRY(S.finalize(G, 1));
-        MTK_CUDA_TRY(cudaMemcpyAsync(c->h_scalars + 3, c->scalars, sizeof(double), cudaMemcpyDeviceToHost, st));
-        MTK_CUDA_TRY(cudaStreamSynchronize(st));
-        const double bnorm2 = c->h_scalars[2];
-        double rr = c->h_scalars[3];
         const double goal2 = tol * tol * bnorm2;
         const double start_rel = bnorm2 > 0 ? std::sqrt(rr / bnorm2) : 0.0;
         solves++;
@@ -1294,6 +1326,7 @@ extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const 
         if (debug)
             fprintf(stderr, "[field] power step %d: pcg iterations %lld (total), refinements %lld, start residual %.2e, final %.2e\n",
                     k, iters, refines, start_rel, rel);
+        if (rhs) break;
         // x /= sqrt|x^H M x|; u = x
         mnorm_partial<<<G, kStream, 0, st>>>(n, S.area.p, S.x.p, c->partials);
         c->kernels++;
@@ -1308,7 +1341,8 @@ extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const 
         out_p.resize(2 * (size_t)n);
         out_u = out_p.data();
     }
-    MTK_CUDA_TRY(cudaMemcpyAsync(out_u, S.ringU[n_iter % ring].p, sizeof(double2) * n, cudaMemcpyDeviceToHost, st));
+    MTK_CUDA_TRY(cudaMemcpyAsync(out_u, rhs ? S.x.p : S.ringU[n_iter % ring].p, sizeof(double2) * n,
+                                 cudaMemcpyDeviceToHost, st));
     MTK_CUDA_TRY(cudaEventRecord(c->ev_b, st));
     MTK_CUDA_TRY(cudaStreamSynchronize(st));
     if (S.amg) {
@@ -1333,4 +1367,19 @@ extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const 
         stats->kernel_launches = c->kernels;
     }
     return MTK_OK;
+}
+}  // namespace
+
+extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const int32_t* nbr_h,
+                                   const double* theta_h, const double* area_h, const double* x0,
+                                   int32_t n_iter, const mtk_solve_opts* opts_in, double* out, mtk_stats* stats) {
+    if (!x0) return MTK_ERR_BAD_INPUT;
+    return field_run(c, nF, nRosy, nbr_h, theta_h, area_h, x0, n_iter, opts_in, out, stats, nullptr);
+}
+
+extern "C" int mtk_field_solve(mtk_ctx* c, int32_t nF, int32_t nRosy, const int32_t* nbr_h, const double* theta_h,
+                               const double* area_h, const double* rhs, const mtk_solve_opts* opts_in, double* out,
+                               mtk_stats* stats) {
+    if (!rhs) return MTK_ERR_BAD_INPUT;
+    return field_run(c, nF, nRosy, nbr_h, theta_h, area_h, nullptr, 1, opts_in, out, stats, rhs);
 }

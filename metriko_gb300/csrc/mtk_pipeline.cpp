@@ -51,7 +51,7 @@ extern "C" int mtk_pipeline_run(mtk_ctx* ctx, int32_t nV, int32_t nF, const doub
         auto mesh = std::make_unique<Hmesh>(V, F);
         lap(ts);
         stamp("hmesh", ts2);
-        FaceRosyField rawf(*mesh, 4, FieldType::Smoothest);
+        FaceRosyField rawf(*mesh, 4, popts->field_type == 1 ? FieldType::CurvatureAligned : FieldType::Smoothest);
         stamp("field (gpu)", ts2);
         ts = clk::now();
         rawf.computeMatching(MatchingType::Curl);
@@ -141,7 +141,7 @@ extern "C" int mtk_pipeline_size_field_gradient(mtk_ctx* ctx, int32_t nV, int32_
         std::memcpy(V.data(), Vb, sizeof(double) * 3 * size_t(nV));
         std::memcpy(F.data(), Fb, sizeof(int32_t) * 3 * size_t(nF));
         auto mesh = std::make_unique<Hmesh>(V, F);
-        FaceRosyField rawf(*mesh, 4, FieldType::Smoothest);
+        FaceRosyField rawf(*mesh, 4, popts->field_type == 1 ? FieldType::CurvatureAligned : FieldType::Smoothest);
         rawf.computeMatching(MatchingType::Curl);
         auto seam = compute_seam(rawf);
         auto cutm = compute_cut_mesh(*mesh, seam);

@@ -1179,3 +1179,33 @@ def size_field_gradient(out, F, s, T=None, mu=0.0):
         np.add.at(grad, a, mu * d)
         np.add.at(grad, b, -mu * d)
     return loss + mu * smooth, grad, UFull @ xs
+
+
+# --------------------------------------------------------------------------------------------
+# CurvatureAligned field (face_rosy_field.h:23-32, principalCurvatureDir :86-98, the dihedral
+# angle of hmesh.h:508-519, solveSquare sparse_linear_solver.h:16-27 with lambda = 0).
+# --------------------------------------------------------------------------------------------
+def principal_curvature_dir(m: Hmesh):
+    """D_f = 1/4 sum_h -(e^{i farg(h)} |h|)^2 / |h| * darg(h), darg(h) = atan2(v . (n1 x n2), n1 . n2)."""
+    D = np.zeros(m.nF, complex)
+    for j in range(3):
+        h = m.FH[:, j]
+        vec = m.hvec[h]
+        l = _norm3(vec)
+        n1 = m.faceNormal[m.face[h]]
+        n2 = m.faceNormal[m.face[m.twin[h]]]
+        darg = np.arctan2(_dot3(vec / l[:, None], np.cross(n1, n2)), _dot3(n1, n2))
+        c = np.exp(1j * m.farg[h]) * l
+        D += -c * c / l * darg
+    return D * 0.25
+
+
+def curvature_aligned(m: Hmesh, N: int = 4):
+    """compressed = L^-1 (M D / sqrt|D^H M D|), D squared for N = 4 (direct sparse LU)."""
+    D = principal_curvature_dir(m)
+    if N == 4:
+        D = D * D
+    L = connection_laplacian(m, N)
+    Mm = mass_matrix(m)
+    rhs = (Mm @ D) / np.sqrt(abs(np.vdot(D, Mm @ D)))
+    return spla.splu(L.tocsc()).solve(rhs), rhs

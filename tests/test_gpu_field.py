@@ -63,3 +63,32 @@ def test_field_rejects_bad_neighbour(gpu_ctx):
     with pytest.raises(M.MetrikoError) as e:
         M.field_smoothest(gpu_ctx, nbr, theta, m.faceArea, O.seeded_init(m.nF, 0))
     assert e.value.status == M._lib.BAD_INPUT
+
+
+@pytest.mark.parametrize("name", ["ico3_noise", "torus_32x16"])
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+def test_field_solve_matches_oracle(gpu_ctx, name, prec):
+    """mtk_field_solve (L x = rhs, the CurvatureAligned solve) against a direct sparse LU."""
+    m, nbr, theta = _inputs(name)
+    c_ref, rhs = O.curvature_aligned(m)
+    c, st = M.field_solve(gpu_ctx, nbr, theta, m.faceArea, rhs, opts=M.solve_opts(prec, tol=1e-10))
+    assert np.abs(c - c_ref).max() <= 1e-8 * np.abs(c_ref).max()
+    assert st["max_rel_residual"] <= 1e-10
+
+
+@pytest.mark.parametrize("name", ["ico4_noise", "torus_32x16"])
+def test_curvature_aligned_pipeline_field_matches_oracle(gpu_ctx, name):
+    """FieldType::CurvatureAligned through the pipeline: the host principal-curvature right-hand
+    side and the device solve against the oracle; then the whole path runs to integral values."""
+    V, F, ratio, rs = meshgen.workload(name)
+    m = O.Hmesh(V, F)
+    c_ref, _ = O.curvature_aligned(m)
+    r = M.pipeline(gpu_ctx, V, F, ratio=ratio, round_seams=rs, field_type="curvature_aligned",
+                   opts=M.solve_opts("fp64", tol=1e-10), stop_after=1)
+    assert np.abs(r["compressed"] - c_ref).max() <= 1e-8 * np.abs(c_ref).max()
+    full = M.pipeline(gpu_ctx, V, F, ratio=ratio, round_seams=rs, field_type="curvature_aligned")
+    assert full["status"] == 0
+    chi = 2 if name.startswith("ico") else 0
+    assert full["singular"].sum() == 4 * chi
+    X, fo = full["fullx"], full["fix_order"]
+    assert np.abs(X[fo] - np.round(X[fo])).max() <= 1e-6
