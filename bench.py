@@ -152,6 +152,21 @@ def run_ours(args):
     else:
         r64, st64, wall64 = step(opts_fp64)
         fp64_ms = st64["ms_field"] + st64["ms_integrate"] + st64["ms_rounding"]
+    # stand-alone SpMV of the field operator (after the timed region): FP32 and FP64, each SpMV
+    # after an L2 flush, CUDA events around the kernel alone
+    spmv = None
+    if not args.no_spmv:
+        nbr, theta, _ = M.field_inputs(V, F)
+        ms32, by32 = M.spmv_bench(ctx, nbr, theta, "mixed", reps=20)
+        ms64, by64 = M.spmv_bench(ctx, nbr, theta, "fp64", reps=20)
+        pk, pk_kind = load_peaks()
+        spmv = {"kernel": "spmv_ell<float>", "bytes_per_spmv": int(by32), "ms": round(ms32, 4),
+                "achieved": round(by32 / (ms32 * 1e-3) / 1e9, 1), "peak": pk, "unit": "GB/s",
+                "frac": round(by32 / (ms32 * 1e-3) / 1e9 / pk, 4), "peak_kind": pk_kind,
+                "fp64": {"bytes_per_spmv": int(by64), "ms": round(ms64, 4),
+                         "achieved": round(by64 / (ms64 * 1e-3) / 1e9, 1),
+                         "frac": round(by64 / (ms64 * 1e-3) / 1e9 / pk, 4)},
+                "l2": "flushed (256 MiB write) before every SpMV", "reps": 20}
     if world > 1:
         t = torch.tensor([max(dev_ms)], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -187,6 +202,7 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1) if achieved else None,
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
                      "peak_kind": peak_kind, "traffic": None},
+        "spmv": spmv,
         "clocks": clocks,
         "cpu_baseline": cpu,
     }
@@ -250,6 +266,7 @@ def main():
     ap.add_argument("--tol", type=float, default=1e-8)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 GPU comparison run (profiling runs)")
+    ap.add_argument("--no-spmv", action="store_true", help="skip the stand-alone SpMV measurement (profiling runs)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

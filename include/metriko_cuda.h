@@ -257,6 +257,23 @@ int mtk_pipeline_size_field_gradient(mtk_ctx* ctx, int32_t nV, int32_t nF, const
                                      double* grad_s, double* fullx, int32_t fullx_cap, int32_t* n_full,
                                      mtk_stats* stats);
 
+/*
+ * The inputs of mtk_field_smoothest for a closed mesh (host only): nbr[3*nF] the face across
+ * each face halfedge, theta[3*nF] = farg(h) - farg(twin h) (face_rosy_field.h:72-102), and
+ * area[nF] (may be NULL).
+ */
+int mtk_field_inputs(int32_t nV, int32_t nF, const double* V, const int32_t* F, int32_t* nbr, double* theta,
+                     double* area);
+
+/*
+ * SpMV roofline measurement (no counterpart in the reference): assembles the field operator
+ * of mtk_field_smoothest and times `reps` stand-alone SpMVs y = L x (FP32 or FP64), each after
+ * an L2 flush and with its own CUDA events.  *bytes_per_spmv: algorithmic bytes per SpMV
+ * (per row 3 x (value + column) + diagonal + x_i + y_i).
+ */
+int mtk_field_spmv_bench(mtk_ctx* ctx, int32_t nF, int32_t nRosy, const int32_t* nbr, const double* theta,
+                         int32_t precision, int32_t reps, double* ms_per_spmv, double* bytes_per_spmv);
+
 /* The deterministic start vector used by the pipeline: re/im of face f from splitmix64. */
 void mtk_seeded_init(int32_t n, int32_t seed, double* out);
 

@@ -21,7 +21,7 @@ EXPORTS = [
     "mtk_status_string", "mtk_last_error", "mtk_default_opts", "mtk_ctx_create", "mtk_ctx_destroy",
     "mtk_ctx_kernel_count", "mtk_field_smoothest", "mtk_iterative_rounding", "mtk_pipeline_run",
     "mtk_seeded_init", "mtk_topology_from_field", "mtk_field_smoothest_noalloc", "mtk_size_field_gradient",
-    "mtk_pipeline_size_field_gradient", "mtk_field_solve",
+    "mtk_pipeline_size_field_gradient", "mtk_field_solve", "mtk_field_inputs", "mtk_field_spmv_bench",
 ]
 
 
@@ -87,6 +87,9 @@ def lib():
         L.mtk_field_smoothest_noalloc.argtypes = [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
                                                   C.c_void_p, C.c_int32, C.c_double, C.c_int32, C.c_void_p,
                                                   C.c_void_p, C.POINTER(C.c_int32)]
+        L.mtk_field_inputs.argtypes = [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.mtk_field_spmv_bench.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
+                                           C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.mtk_field_solve.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.c_void_p, C.POINTER(SolveOpts), C.c_void_p, C.POINTER(Stats)]
         L.mtk_pipeline_size_field_gradient.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
@@ -205,6 +208,29 @@ def pipeline(ctx: Context, V, F, ratio=0.02, seed=0, round_seams=False, seamless
                 fix_order=fix_order[:nfix].copy(), fix_vals=fix_vals[:nfix].copy(),
                 counts=dict(zip(["nV", "nE", "nCut", "nT", "nS", "nJ", "nZ", "nFull"], counts.tolist())),
                 stats=st.as_dict())
+
+
+def field_inputs(V, F):
+    """mtk_field_inputs: (nbr (nF x 3), theta (nF x 3), area (nF)) of the field operator."""
+    V = np.ascontiguousarray(V, np.float64)
+    F = np.ascontiguousarray(F, np.int32)
+    nF = len(F)
+    nbr = np.empty(3 * nF, np.int32)
+    theta = np.empty(3 * nF)
+    area = np.empty(nF)
+    _check(lib().mtk_field_inputs(len(V), nF, _ptr(V), _ptr(F), _ptr(nbr), _ptr(theta), _ptr(area)), "mtk_field_inputs")
+    return nbr.reshape(nF, 3), theta.reshape(nF, 3), area
+
+
+def spmv_bench(ctx: Context, nbr, theta, precision="mixed", reps=20):
+    """mtk_field_spmv_bench: (ms per SpMV, algorithmic bytes per SpMV); "mixed" times FP32."""
+    nbr = np.ascontiguousarray(nbr, np.int32).reshape(-1)
+    theta = np.ascontiguousarray(theta, np.float64).reshape(-1)
+    ms, by = C.c_double(0), C.c_double(0)
+    _check(lib().mtk_field_spmv_bench(ctx.handle, len(nbr) // 3, 4, _ptr(nbr), _ptr(theta),
+                                      PREC_FP64 if precision == "fp64" else PREC_MIXED, reps, C.byref(ms), C.byref(by)),
+           "mtk_field_spmv_bench")
+    return ms.value, by.value
 
 
 def field_solve(ctx: Context, nbr, theta, area, rhs, n_rosy=4, opts=None):

@@ -784,6 +784,37 @@ __global__ void normalize_to(int n, const double* __restrict__ scal, const doubl
     }
 }
 
+// Stand-alone SpMV y = L x over the ELL rows (read-only x: gathers through the read-only path),
+// one thread per row at full occupancy; used to measure the SpMV against the HBM roofline.
+template <typename T>
+__global__ void __launch_bounds__(256) spmv_ell(ComplexEll<T> A, const typename V2of<T>::type* __restrict__ x,
+                                                typename V2of<T>::type* __restrict__ y) {
+    using V2 = typename V2of<T>::type;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.n) return;
+    int c[3];
+    V2 a[3], xc[3];
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        c[j] = __ldg(A.nbr + j * A.n + i);
+        a[j] = __ldg(A.val + j * A.n + i);
+    }
+    const V2 xi = __ldg(x + i);
+    const T d = __ldg(A.diag + i);
+#pragma unroll
+    for (int j = 0; j < 3; j++) xc[j] = __ldg(x + c[j]);
+    T re = d * xi.x, im = d * xi.y;
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        re += a[j].x * xc[j].x - a[j].y * xc[j].y;
+        im += a[j].x * xc[j].y + a[j].y * xc[j].x;
+    }
+    V2 o;
+    o.x = re;
+    o.y = im;
+    y[i] = o;
+}
+
 // Start of a plain solve L x = b: x = 0, r = b, r32 = r, partial |b|^2.
 __global__ void start_from_rhs(int n, const double2* __restrict__ b, double2* x, double2* r, float2* r32,
                                double* partials) {
@@ -1382,4 +1413,64 @@ extern "C" int mtk_field_solve(mtk_ctx* c, int32_t nF, int32_t nRosy, const int3
                                mtk_stats* stats) {
     if (!rhs) return MTK_ERR_BAD_INPUT;
     return field_run(c, nF, nRosy, nbr_h, theta_h, area_h, nullptr, 1, opts_in, out, stats, rhs);
+}
+
+// SpMV roofline measurement: assembles the field operator and times `reps` stand-alone SpMVs,
+// each after an L2 flush (a 256 MiB write), each with its own CUDA-event pair on the stream.
+extern "C" int mtk_field_spmv_bench(mtk_ctx* c, int32_t nF, int32_t nRosy, const int32_t* nbr_h, const double* theta_h,
+                                    int32_t precision, int32_t reps, double* ms_per_spmv, double* bytes_per_spmv) {
+    if (!c || nF <= 0 || !nbr_h || !theta_h || reps <= 0 || !ms_per_spmv || !bytes_per_spmv) return MTK_ERR_BAD_INPUT;
+    for (int64_t i = 0; i < 3 * (int64_t)nF; i++)
+        if (nbr_h[i] < 0 || nbr_h[i] >= nF) return MTK_ERR_BAD_INPUT;
+    MTK_CUDA_TRY(cudaSetDevice(c->device));
+    cudaStream_t st = c->stream;
+    const int n = nF;
+    DBuf<int> nbr_in, nbr;
+    DBuf<double> theta, area, d64, inv64;
+    DBuf<float> d32, inv32, area32;
+    DBuf<double2> v64, x64, y64;
+    DBuf<float2> v32, x32, y32;
+    DBuf<unsigned char> flush;
+    MTK_TRY(nbr_in.upload(nbr_h, 3 * (size_t)n, st));
+    MTK_TRY(theta.upload(theta_h, 3 * (size_t)n, st));
+    std::vector<double> ones(n, 1.0);
+    MTK_TRY(area.upload(ones.data(), n, st));
+    MTK_TRY(nbr.alloc(3 * (size_t)n)); MTK_TRY(v64.alloc(3 * (size_t)n)); MTK_TRY(v32.alloc(3 * (size_t)n));
+    MTK_TRY(d64.alloc(n)); MTK_TRY(inv64.alloc(n)); MTK_TRY(d32.alloc(n)); MTK_TRY(inv32.alloc(n)); MTK_TRY(area32.alloc(n));
+    const int G = stream_grid(c);
+    field_assemble<<<G, kStream, 0, st>>>(n, nRosy, nbr_in.p, theta.p, area.p, nbr.p, v64.p, v32.p, d64.p, d32.p,
+                                         inv64.p, inv32.p, area32.p);
+    const size_t kFlush = 256u << 20;
+    MTK_TRY(flush.alloc(kFlush));
+    const bool fp64 = precision == MTK_PREC_FP64;
+    std::vector<double> xh(2 * (size_t)n);
+    for (int i = 0; i < n; i++) { xh[2 * i] = 1.0 / (1 + i % 7); xh[2 * i + 1] = 0.5 / (1 + i % 5); }
+    if (fp64) {
+        MTK_TRY(x64.upload(reinterpret_cast<const double2*>(xh.data()), n, st));
+        MTK_TRY(y64.alloc(n));
+    } else {
+        std::vector<float2> xf(n);
+        for (int i = 0; i < n; i++) xf[i] = make_float2((float)xh[2 * i], (float)xh[2 * i + 1]);
+        MTK_TRY(x32.upload(xf.data(), n, st));
+        MTK_TRY(y32.alloc(n));
+    }
+    const int blocks = (n + 255) / 256;
+    double total = 0;
+    for (int rep = -1; rep < reps; rep++) {   // rep -1: warm-up
+        MTK_CUDA_TRY(cudaMemsetAsync(flush.p, rep & 0xff, kFlush, st));
+        MTK_CUDA_TRY(cudaEventRecord(c->ev_k0, st));
+        if (fp64) spmv_ell<double><<<blocks, 256, 0, st>>>(ComplexEll<double>{n, nbr.p, v64.p, d64.p}, x64.p, y64.p);
+        else spmv_ell<float><<<blocks, 256, 0, st>>>(ComplexEll<float>{n, nbr.p, v32.p, d32.p}, x32.p, y32.p);
+        MTK_CUDA_TRY(cudaEventRecord(c->ev_k1, st));
+        MTK_CUDA_TRY(cudaEventSynchronize(c->ev_k1));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, c->ev_k0, c->ev_k1);
+        if (rep >= 0) total += ms;
+        c->kernels++;
+    }
+    MTK_CUDA_TRY(cudaGetLastError());
+    *ms_per_spmv = total / reps;
+    // algorithmic bytes per row: 3 x (value + column) + diagonal + own x + y (gathered x not counted)
+    *bytes_per_spmv = (double)n * (fp64 ? 3.0 * (16 + 4) + 8 + 16 + 16 : 3.0 * (8 + 4) + 4 + 8 + 8);
+    return MTK_OK;
 }

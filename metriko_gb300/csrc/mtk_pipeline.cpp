@@ -232,3 +232,26 @@ extern "C" int mtk_topology_from_field(int32_t nV, int32_t nF, const double* Vb,
         return MTK_ERR_BAD_INPUT;
     }
 }
+
+extern "C" int mtk_field_inputs(int32_t nV, int32_t nF, const double* Vb, const int32_t* Fb, int32_t* nbr,
+                                double* theta, double* area) {
+    if (nV <= 0 || nF <= 0 || !Vb || !Fb || !nbr || !theta) return MTK_ERR_BAD_INPUT;
+    try {
+        MatXd V(nV, 3);
+        MatXi F(nF, 3);
+        std::memcpy(V.data(), Vb, sizeof(double) * 3 * size_t(nV));
+        std::memcpy(F.data(), Fb, sizeof(int32_t) * 3 * size_t(nF));
+        Hmesh mesh(V, F);
+        FaceRosyField fld(mesh, 4);
+        std::vector<int> nb;
+        std::vector<double> th;
+        fld.assembly_inputs(nb, th);
+        std::memcpy(nbr, nb.data(), sizeof(int32_t) * nb.size());
+        std::memcpy(theta, th.data(), sizeof(double) * th.size());
+        if (area) std::memcpy(area, mesh.faceArea.data(), sizeof(double) * nF);
+        return MTK_OK;
+    } catch (const std::exception& e) {
+        mtk_set_last_error(e.what(), __FILE__, __LINE__);
+        return MTK_ERR_BAD_INPUT;
+    }
+}

@@ -44,3 +44,13 @@ def test_seam_is_tree_through_singularities():
     verts = np.unique(E)
     assert len(E) == len(verts) - 1          # a tree
     assert set(np.flatnonzero(res["singular"])) <= set(verts.tolist())
+
+
+def test_field_inputs_match_oracle():
+    """mtk_field_inputs (host): the neighbour and transport-angle inputs of the field solve."""
+    V, F, _, _ = meshgen.workload("ico3_noise")
+    nbr, theta, area = M.field_inputs(V, F)
+    m = O.Hmesh(V, F)
+    assert np.array_equal(nbr, m.face[m.twin[m.FH]])
+    assert np.abs(theta - (m.farg[m.FH] - m.farg[m.twin[m.FH]])).max() < 1e-12
+    assert np.array_equal(area, m.faceArea)
