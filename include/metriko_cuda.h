@@ -269,10 +269,13 @@ int mtk_field_inputs(int32_t nV, int32_t nF, const double* V, const int32_t* F, 
  * SpMV roofline measurement (no counterpart in the reference): assembles the field operator
  * of mtk_field_smoothest and times `reps` stand-alone SpMVs y = L x (FP32 or FP64), each after
  * an L2 flush and with its own CUDA events.  *bytes_per_spmv: algorithmic bytes per SpMV
- * (per row 3 x (value + column) + diagonal + x_i + y_i).
+ * (per row 3 x (value + column) + diagonal + x_i + y_i).  *ms_copy_same_bytes (may be NULL): a
+ * device-to-device copy moving the same bytes under the same flush and timing, the bandwidth a
+ * kernel of that size can reach.
  */
 int mtk_field_spmv_bench(mtk_ctx* ctx, int32_t nF, int32_t nRosy, const int32_t* nbr, const double* theta,
-                         int32_t precision, int32_t reps, double* ms_per_spmv, double* bytes_per_spmv);
+                         int32_t precision, int32_t reps, double* ms_per_spmv, double* bytes_per_spmv,
+                         double* ms_copy_same_bytes);
 
 /* The deterministic start vector used by the pipeline: re/im of face f from splitmix64. */
 void mtk_seeded_init(int32_t n, int32_t seed, double* out);

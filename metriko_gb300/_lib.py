@@ -89,7 +89,8 @@ def lib():
                                                   C.c_void_p, C.POINTER(C.c_int32)]
         L.mtk_field_inputs.argtypes = [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.mtk_field_spmv_bench.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
-                                           C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+                                           C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                           C.POINTER(C.c_double)]
         L.mtk_field_solve.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.c_void_p, C.POINTER(SolveOpts), C.c_void_p, C.POINTER(Stats)]
         L.mtk_pipeline_size_field_gradient.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
@@ -223,14 +224,16 @@ def field_inputs(V, F):
 
 
 def spmv_bench(ctx: Context, nbr, theta, precision="mixed", reps=20):
-    """mtk_field_spmv_bench: (ms per SpMV, algorithmic bytes per SpMV); "mixed" times FP32."""
+    """mtk_field_spmv_bench: (ms per SpMV, algorithmic bytes per SpMV, ms of a device copy of the
+    same bytes); "mixed" times FP32."""
     nbr = np.ascontiguousarray(nbr, np.int32).reshape(-1)
     theta = np.ascontiguousarray(theta, np.float64).reshape(-1)
-    ms, by = C.c_double(0), C.c_double(0)
+    ms, by, cp = C.c_double(0), C.c_double(0), C.c_double(0)
     _check(lib().mtk_field_spmv_bench(ctx.handle, len(nbr) // 3, 4, _ptr(nbr), _ptr(theta),
-                                      PREC_FP64 if precision == "fp64" else PREC_MIXED, reps, C.byref(ms), C.byref(by)),
+                                      PREC_FP64 if precision == "fp64" else PREC_MIXED, reps, C.byref(ms), C.byref(by),
+                                      C.byref(cp)),
            "mtk_field_spmv_bench")
-    return ms.value, by.value
+    return ms.value, by.value, cp.value
 
 
 def field_solve(ctx: Context, nbr, theta, area, rhs, n_rosy=4, opts=None):

@@ -1418,7 +1418,8 @@ extern "C" int mtk_field_solve(mtk_ctx* c, int32_t nF, int32_t nRosy, const int3
 // SpMV roofline measurement: assembles the field operator and times `reps` stand-alone SpMVs,
 // each after an L2 flush (a 256 MiB write), each with its own CUDA-event pair on the stream.
 extern "C" int mtk_field_spmv_bench(mtk_ctx* c, int32_t nF, int32_t nRosy, const int32_t* nbr_h, const double* theta_h,
-                                    int32_t precision, int32_t reps, double* ms_per_spmv, double* bytes_per_spmv) {
+                                    int32_t precision, int32_t reps, double* ms_per_spmv, double* bytes_per_spmv,
+                                    double* ms_copy_same_bytes) {
     if (!c || nF <= 0 || !nbr_h || !theta_h || reps <= 0 || !ms_per_spmv || !bytes_per_spmv) return MTK_ERR_BAD_INPUT;
     for (int64_t i = 0; i < 3 * (int64_t)nF; i++)
         if (nbr_h[i] < 0 || nbr_h[i] >= nF) return MTK_ERR_BAD_INPUT;
@@ -1472,5 +1473,24 @@ extern "C" int mtk_field_spmv_bench(mtk_ctx* c, int32_t nF, int32_t nRosy, const
     *ms_per_spmv = total / reps;
     // algorithmic bytes per row: 3 x (value + column) + diagonal + own x + y (gathered x not counted)
     *bytes_per_spmv = (double)n * (fp64 ? 3.0 * (16 + 4) + 8 + 16 + 16 : 3.0 * (8 + 4) + 4 + 8 + 8);
+    if (ms_copy_same_bytes) {   // a device copy moving the same bytes (read + write), same flush and timing
+        const size_t half = ((size_t)(*bytes_per_spmv / 2) + 255) & ~(size_t)255;
+        DBuf<unsigned char> src, dst;
+        MTK_TRY(src.alloc(half));
+        MTK_TRY(dst.alloc(half));
+        MTK_CUDA_TRY(cudaMemsetAsync(src.p, 1, half, st));
+        double tc = 0;
+        for (int rep = -1; rep < reps; rep++) {
+            MTK_CUDA_TRY(cudaMemsetAsync(flush.p, rep & 0xff, kFlush, st));
+            MTK_CUDA_TRY(cudaEventRecord(c->ev_k0, st));
+            MTK_CUDA_TRY(cudaMemcpyAsync(dst.p, src.p, half, cudaMemcpyDeviceToDevice, st));
+            MTK_CUDA_TRY(cudaEventRecord(c->ev_k1, st));
+            MTK_CUDA_TRY(cudaEventSynchronize(c->ev_k1));
+            float ms = 0;
+            cudaEventElapsedTime(&ms, c->ev_k0, c->ev_k1);
+            if (rep >= 0) tc += ms;
+        }
+        *ms_copy_same_bytes = tc / reps;
+    }
     return MTK_OK;
 }
