@@ -270,14 +270,15 @@ inline bool spd_inverse_dense(std::vector<double>& A, int n) {
     return true;
 }
 
-// Smoothed-aggregation hierarchy.  Per level: aggregates and T (raggregate), the smoothed
-// prolongator P_sa = (I - w_p D^-1 A) T with w_p = (4/3) / rho, rho the Gershgorin bound of
-// D^-1 A, and the Galerkin coarse operator P_sa^T A P_sa.  Cycle operators (V(1,1), Jacobi
-// weight omega, coarse correction scaled by alpha):
+// Smoothed-aggregation hierarchy.  Per level: aggregates and T (raggregate), rho = the spectral
+// radius of D^-1 A (power estimate), the smoothed prolongator P_sa = (I - w_p D^-1 A) T with
+// w_p = (4/3) / rho, and the Galerkin coarse operator P_sa^T A P_sa.  Cycle operators (V(1,1),
+// Jacobi weight omega = min(omega_cap, 1.5 / rho), so omega rho <= 1.5 < 2 keeps the smoother
+// convergent; coarse correction scaled by alpha):
 //   R = P_sa^T (I - omega A D^-1),  S = omega D^-1 (2 I - A omega D^-1),
 //   P = alpha (I - omega D^-1 A) P_sa = alpha (P_sa - omega D^-1 (A P_sa)) = alpha R^T.
 inline bool build_real_hierarchy(RCsr A0, std::vector<int> node, std::vector<int> comp, int nnode, RHierarchy& H,
-                                 double omega = 0.85, double alpha = 1.0) {
+                                 double omega_cap = 1.0, double alpha = 1.0) {
     H.lv.clear();
     H.ops.clear();
     RLevel cur;
@@ -320,6 +321,7 @@ inline bool build_real_hierarchy(RCsr A0, std::vector<int> node, std::vector<int
             rho *= 1.05;
         }
         const double wp = rho > 0 ? (4.0 / 3.0) / rho : 0.0;
+        const double omega = rho > 0 ? std::min(omega_cap, 1.5 / rho) : omega_cap;
         RCsr Psa, AP;
         Psa.n = n;
         build_rows_parallel<double>(
