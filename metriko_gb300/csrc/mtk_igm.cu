@@ -56,6 +56,17 @@ struct IgmOp {
     T* U;               // 2*nCut gather buffer
     T* Qc;              // 2*nCut stiffness product
     T* XoJ;             // nJ
+    // assembled operator (FP32 inner solves; null: the matrix-free chain above)
+    const int* ka_ptr;  // K_yy = 2 W_y^T S W_y, nY rows (CSR)
+    const int* ka_col;
+    const T* ka_val;
+    const int* cy_ptr;  // C_yJ = 2 W_y^T S W_J, nY rows, J columns
+    const int* cy_col;
+    const T* cy_val;
+    const int* cj_ptr;  // C_Jy = C_yJ^T, nJ rows, y columns
+    const int* cj_col;
+    const T* cj_val;
+    const T* BJJ;       // 2 W_J^T S W_J, nJ x nJ (row-major)
 };
 
 // Shared-memory layout of the replicated z state.
@@ -199,6 +210,76 @@ __device__ bool igm_apply(const IgmOp<T>& A, const ZProj<T>& P, const unsigned c
     // (E is done by the caller after the next barrier: igm_apply_z)
 }
 
+// The same operator from the assembled blocks, in one phase and one grid barrier (taken by the
+// caller): XJ = USmall pz (replicated); per free row q_y = scale (K_yy p + C_yJ XJ) + shift p
+// (masked), and per translation XoJ = C_Jy p + BJJ XJ (one warp each, fixed lane order).  The
+// direction is formed on the fly as in igm_apply.
+template <typename T>
+__device__ bool igm_apply_asm(const IgmOp<T>& A, const unsigned char* __restrict__ fixy, const T* py, const T* pz,
+                              T* qy, ZSmem<T>& zs, T& pq_part, const T* zy = nullptr, T beta = T(0),
+                              T* pnew = nullptr) {
+    const int stride = gridDim.x * blockDim.x;
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int s = threadIdx.x; s < A.nJ; s += blockDim.x) {
+        T acc = T(0);
+        const T* row = A.Us + (size_t)s * A.nZ;
+        for (int j = 0; j < A.nZ; j++) acc += row[j] * pz[j];
+        zs.XJ[s] = acc;
+    }
+    __syncthreads();
+    T part = T(0);
+    for (int j = t0; j < A.nY; j += stride) {
+        T pj;
+        if (pnew) {
+            pj = fmaT<T>(beta, __ldcg(py + j), __ldcg(zy + j));
+            pnew[j] = pj;
+        } else {
+            pj = __ldcg(py + j);
+        }
+        T acc = T(0);
+        const int e1 = __ldg(A.ka_ptr + j + 1);
+        for (int e = __ldg(A.ka_ptr + j); e < e1; e += 4) {   // four gathers in flight
+            int cc[4];
+            T vv[4], pc[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                cc[u] = e + u < e1 ? __ldg(A.ka_col + e + u) : -1;
+                vv[u] = e + u < e1 ? __ldg(A.ka_val + e + u) : T(0);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                if (cc[u] < 0) { pc[u] = T(0); continue; }
+                pc[u] = pnew ? fmaT<T>(beta, __ldcg(py + cc[u]), __ldcg(zy + cc[u])) : __ldcg(py + cc[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) acc += vv[u] * pc[u];
+        }
+        for (int e = __ldg(A.cy_ptr + j); e < __ldg(A.cy_ptr + j + 1); e++) acc += __ldg(A.cy_val + e) * zs.XJ[__ldg(A.cy_col + e)];
+        const T qv = fixy[j] ? T(0) : A.scale * acc + A.shift * pj;
+        qy[j] = qv;
+        part += pj * qv;
+    }
+    {
+        const int lane = threadIdx.x & 31;
+        const int nwarps = stride >> 5;
+        const int gw = nwarps - 1 - (t0 >> 5);   // last warps of the grid
+        for (int s = gw; s < A.nJ; s += nwarps) {
+            T acc = T(0);
+            for (int e = A.cj_ptr[s] + lane; e < A.cj_ptr[s + 1]; e += 32) {
+                const int y = A.cj_col[e];
+                const T pv = pnew ? fmaT<T>(beta, __ldcg(py + y), __ldcg(zy + y)) : __ldcg(py + y);
+                acc += A.cj_val[e] * pv;
+            }
+            for (int t = lane; t < A.nJ; t += 32) acc += A.BJJ[(size_t)s * A.nJ + t] * zs.XJ[t];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) A.XoJ[s] = acc;
+        }
+    }
+    pq_part = part;
+    return true;
+}
+
 // E (replicated, after a barrier): qz = P_z (scale USmall^T XoJ + shift pz)
 template <typename T>
 __device__ void igm_apply_z(const IgmOp<T>& A, const ZProj<T>& P, const T* pz, T* qz, ZSmem<T>& zs) {
@@ -240,7 +321,8 @@ __global__ void __launch_bounds__(kBlock, 1) igm_pcg(IgmOp<T> A, ZProj<T> P, con
     __syncthreads();
     // r = P(b - K x): apply K to x (py = x_y)
     T pqp = T(0);
-    if (!igm_apply(A, P, fixy, x, zs.pz, q, zs.qz, zs, bar, pqp)) { status = 5; goto done; }
+    if (A.ka_ptr) igm_apply_asm(A, fixy, x, zs.pz, q, zs, pqp);
+    else if (!igm_apply(A, P, fixy, x, zs.pz, q, zs.qz, zs, bar, pqp)) { status = 5; goto done; }
     if (!grid_sync(bar)) { status = 5; goto done; }
     igm_apply_z(A, P, zs.pz, zs.qz, zs);
     part[0] = T(0);
@@ -288,7 +370,8 @@ __global__ void __launch_bounds__(kBlock, 1) igm_pcg(IgmOp<T> A, ZProj<T> P, con
             if (it >= maxit) { status = 3; break; }
             // q = K p, p = z + beta p_old formed on the fly and stored in pw
             T pq_part = T(0);
-            if (!igm_apply(A, P, fixy, pold, zs.pz, q, zs.qz, zs, bar, pq_part, z, beta, pw)) { status = 5; break; }
+            if (A.ka_ptr) igm_apply_asm(A, fixy, pold, zs.pz, q, zs, pq_part, z, beta, pw);
+            else if (!igm_apply(A, P, fixy, pold, zs.pz, q, zs.qz, zs, bar, pq_part, z, beta, pw)) { status = 5; break; }
             pq1[0] = pq_part;
             publish_partials<T, 1>(pq1, partials + 2 * gridDim.x);
             if (!grid_sync(bar)) { status = 5; break; }
@@ -750,6 +833,10 @@ struct Igm {
     DBuf<float> s_val32, w_val32, yt_val32, jt_val32, Us32, minvy32, Mz32, Qz32, U32, Qc32, XoJ32;
     DBuf<double> xs, bsys, r64, z64, p64, q64, prev, Xfull, XJ64, scratch;
     DBuf<float> r32, e32, z32, p32, q32, pb32;
+    // assembled operator of the FP32 inner solves
+    bool asm_ok = false;
+    DBuf<int> ka_ptr, ka_col, cy_ptr, cy_col, cj_ptr, cj_col;
+    DBuf<float> ka_val32, cy_val32, cj_val32, bjj32;
     DBuf<double> pb64;   // second direction buffers of the PCG (double-buffered p)
     DBuf<unsigned char> fixy;
     std::vector<unsigned char> h_fixy;
@@ -858,11 +945,15 @@ struct Igm {
 
     IgmOp<double> op64(double scale, double shift) {
         return {nCut, nY, nZ, nJ, w_ptr.p, w_tag.p, w_val.p, s_ptr.p, s_col.p, s_val.p, yt_ptr.p, yt_row.p, yt_val.p,
-                jt_ptr.p, jt_row.p, jt_val.p, Us.p, scale, shift, U.p, Qc.p, XoJ.p};
+                jt_ptr.p, jt_row.p, jt_val.p, Us.p, scale, shift, U.p, Qc.p, XoJ.p,
+                nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     }
     IgmOp<float> op32(double scale, double shift) {
+        const bool a = asm_ok;
         return {nCut, nY, nZ, nJ, w_ptr.p, w_tag.p, w_val32.p, s_ptr.p, s_col.p, s_val32.p, yt_ptr.p, yt_row.p, yt_val32.p,
-                jt_ptr.p, jt_row.p, jt_val32.p, Us32.p, (float)scale, (float)shift, U32.p, Qc32.p, XoJ32.p};
+                jt_ptr.p, jt_row.p, jt_val32.p, Us32.p, (float)scale, (float)shift, U32.p, Qc32.p, XoJ32.p,
+                a ? ka_ptr.p : nullptr, ka_col.p, ka_val32.p, cy_ptr.p, cy_col.p, cy_val32.p, cj_ptr.p, cj_col.p,
+                cj_val32.p, bjj32.p};
     }
 
     template <typename T>
@@ -1241,6 +1332,58 @@ int igm_run(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts_in, do
                 add(j, delta);
             },
             K.ptr, K.col, K.val);
+        // assembled operator of the FP32 inner solves: K_yy (without the multigrid's delta), the
+        // free-to-translation coupling C_yJ and its transpose
+        if (!getenv("MTK_NO_ASM")) {
+            std::vector<float> kv(K.val.size());
+#pragma omp parallel for schedule(static)
+            for (int j = 0; j < nY; j++)
+                for (int q = K.ptr[j]; q < K.ptr[j + 1]; q++)
+                    kv[q] = (float)(K.col[q] == j ? K.val[q] - delta : K.val[q]);
+            MTK_TRY(S.ka_ptr.upload(K.ptr.data(), K.ptr.size(), st));
+            MTK_TRY(S.ka_col.upload(K.col.data(), K.col.size(), st));
+            MTK_TRY(S.ka_val32.upload(kv.data(), kv.size(), st));
+            std::vector<int> cptr, ccol;
+            std::vector<double> cval;
+            build_rows_parallel<double>(
+                nY, std::max(nJ, 1),
+                [&](int j, auto add) {
+                    for (int e = yptr[j]; e < yptr[j + 1]; e++) {
+                        const int r = yrow[e], c2 = r >> 1, kk = r & 1;
+                        const double w1 = yval[e];
+                        for (int q = hs_ptr[c2]; q < hs_ptr[c2 + 1]; q++) {
+                            const int r2 = 2 * hs_col[q] + kk;
+                            const double sv = hs_val[q];
+                            for (int e2 = d->w_ptr[r2]; e2 < d->w_ptr[r2 + 1]; e2++)
+                                if (tag[e2] < 0) add(-1 - tag[e2], 2.0 * w1 * sv * d->w_val[e2]);
+                        }
+                    }
+                },
+                cptr, ccol, cval);
+            std::vector<float> cv32(cval.begin(), cval.end());
+            std::vector<int> tptr(std::max(nJ, 1) + 1, 0), tcol(ccol.size());
+            std::vector<float> tval(ccol.size());
+            for (int c2 : ccol) tptr[c2 + 1]++;
+            for (int a2 = 0; a2 < std::max(nJ, 1); a2++) tptr[a2 + 1] += tptr[a2];
+            {
+                std::vector<int> fill(tptr.begin(), tptr.end() - 1);
+                for (int j = 0; j < nY; j++)
+                    for (int q = cptr[j]; q < cptr[j + 1]; q++) {
+                        const int t = fill[ccol[q]]++;
+                        tcol[t] = j;
+                        tval[t] = (float)cval[q];
+                    }
+            }
+            if (ccol.empty()) { ccol.push_back(0); cv32.push_back(0.f); tcol.push_back(0); tval.push_back(0.f); }
+            MTK_TRY(S.cy_ptr.upload(cptr.data(), cptr.size(), st));
+            MTK_TRY(S.cy_col.upload(ccol.data(), ccol.size(), st));
+            MTK_TRY(S.cy_val32.upload(cv32.data(), cv32.size(), st));
+            MTK_TRY(S.cj_ptr.upload(tptr.data(), tptr.size(), st));
+            MTK_TRY(S.cj_col.upload(tcol.data(), tcol.size(), st));
+            MTK_TRY(S.cj_val32.upload(tval.data(), tval.size(), st));
+            MTK_CUDA_TRY(cudaStreamSynchronize(st));
+            S.asm_ok = true;   // BJJ is uploaded once it is built below
+        }
         std::vector<int> node(nY), comp(nY);
         for (int j = 0; j < nY; j++) { node[j] = y2full[j] / 2; comp[j] = y2full[j] % 2; }
         MTK_TRY(S.build_mg(std::move(K), std::move(node), std::move(comp), nFull / 2));
@@ -1271,6 +1414,11 @@ int igm_run(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts_in, do
                     }
                 }
         }
+    }
+    if (S.asm_ok) {
+        std::vector<float> b32(BJJ.begin(), BJJ.end());
+        if (b32.empty()) b32.push_back(0.f);
+        MTK_TRY(S.bjj32.upload(b32.data(), b32.size(), st));
     }
     auto build_zblock = [&](double scale, double shift, std::vector<double>& Kzz) {
         Kzz.assign((size_t)nZ * nZ, 0.0);
