@@ -1242,6 +1242,13 @@ int field_run(mtk_ctx* c, int32_t nF, int32_t nRosy, const int32_t* nbr_h, const
     double worst = 0.0;
     std::vector<double> Gr(kRing * kRing, 0.0), Gi(kRing * kRing, 0.0);
     const double tol = opts.tol;
+    // Attainable reduction of the FP32 solves, per refinement (first, second, later): the FP64
+    // residual after a correction exceeds the FP32 recursive one by the rounding of the FP32
+    // operator times the correction, which the near-null modes amplify (in the late power steps
+    // the first correction reaches only ~1/50 of its start residual however far FP32 iterates).
+    // Measured as sqrt(max(0, rr_fp64 - rr_fp32)) / |r_start| and used to stop the next step's
+    // solves at half of it instead of iterating below what FP64 will see.
+    double floor_rel[3] = {0.0, 0.0, 0.0};
     for (int k = 0; k < n_iter; k++) {
         double bnorm2 = 0, rr = 0;
         if (rhs) {   // plain solve: x = 0, r = b
@@ -1330,12 +1337,20 @@ int field_run(mtk_ctx* c, int32_t nF, int32_t nRosy, const int32_t* nbr_h, const
                 double itol = opts.inner_tol;
                 double need = std::sqrt(goal2 / rr) * 0.5;
                 if (need > itol) itol = need;
+                const int ki = std::min(outer, 3) - 1;
+                const double fl = std::min(0.5 * floor_rel[ki], 0.1);
+                if (fl > itol) itol = fl;
                 zero_f2<<<G, kStream, 0, st>>>(n, S.e32.p);
                 c->kernels++;
+                double frr = 0.0;
+                const long long it0 = iters;
                 int s = S.pcg<float, float2>(S.A32(), S.inv32.p, S.r32.p, S.e32.p, S.z32.p /*r*/, S.p32.p /*z*/,
                                              S.q32.p /*p*/, reinterpret_cast<float2*>(S.Lu.p) /*q*/, S.rb32.p, S.pb32.p,
                                              S.sv32.p, S.vv32.p, itol * itol * rr,
-                                             opts.max_iter, &iters, nullptr);
+                                             opts.max_iter, &iters, &frr);
+                if (debug)
+                    fprintf(stderr, "[field pcg] status %d iterations %lld rr %.3e target %.3e (from %.3e)\n", s,
+                            iters - it0, frr, itol * itol * rr, rr);
                 // an FP32 breakdown (p^H A p <= 0 in single precision) means the inner solve has
                 // stagnated: its last iterate is still a valid correction, and the FP64 refinement
                 // decides what comes next (bounded by max_refine, stopped when it makes no progress)
@@ -1350,6 +1365,7 @@ int field_run(mtk_ctx* c, int32_t nF, int32_t nRosy, const int32_t* nbr_h, const
                 refines++;
                 if (!(rr == rr)) return MTK_ERR_BREAKDOWN;
                 if (rr > goal2 && rr >= rr_prev) return MTK_ERR_NOT_CONVERGED;
+                if (s == MTK_OK && rr_prev > 0) floor_rel[ki] = std::sqrt(std::max(rr - frr, 0.0) / rr_prev);
             }
         }
         double rel = bnorm2 > 0 ? std::sqrt(rr / bnorm2) : 0.0;

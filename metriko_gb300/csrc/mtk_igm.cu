@@ -838,6 +838,9 @@ struct Igm {
     DBuf<int> ka_ptr, ka_col, cy_ptr, cy_col, cj_ptr, cj_col;
     DBuf<float> ka_val32, cy_val32, cj_val32, bjj32;
     DBuf<double> pb64;   // second direction buffers of the PCG (double-buffered p)
+    // attainable reduction of the FP32 solves per refinement (first, second, later), measured as
+    // sqrt(max(0, rr_fp64 - rr_fp32)) / |r_start|: the next solves stop at half of it
+    double floor_rel[3] = {0.0, 0.0, 0.0};
     DBuf<unsigned char> fixy;
     std::vector<unsigned char> h_fixy;
     int kq = 0;
@@ -1065,9 +1068,13 @@ struct Igm {
                 to_f32<<<grid(), kStream, 0, st>>>(nRed, r64.p, r32.p);
                 MTK_CUDA_TRY(cudaMemsetAsync(e32.p, 0, sizeof(float) * nRed, st));
                 c->kernels++;
+                const int ki = std::min(outer, 3) - 1;
+                const double fl = std::min(0.5 * floor_rel[ki], 0.1);
+                if (fl > itol) itol = fl;
+                double frr = 0.0;
                 int s = run_pcg<float>(op32(scale, shift), ZProj<float>{kq, Qz32.p, Mz32.p}, minvy32.p, r32.p, e32.p,
                                        z32.p /*r*/, p32.p /*z*/, q32.p /*p*/, reinterpret_cast<float*>(Xfull.p) /*q*/,
-                                       itol * itol * rr, o.max_iter, 0, smem32, &iters, nullptr);
+                                       itol * itol * rr, o.max_iter, 0, smem32, &iters, &frr);
                 // an FP32 breakdown (p^H A p <= 0 in single precision) means the inner solve has
                 // stagnated: its last iterate is still a valid correction, and the FP64 refinement
                 // decides what comes next (bounded by max_refine, stopped when it makes no progress)
@@ -1082,6 +1089,7 @@ struct Igm {
                 refines++;
                 if (!(rr == rr)) return MTK_ERR_BREAKDOWN;
                 if (rr > goal2 && rr >= rr_prev) return MTK_ERR_NOT_CONVERGED;
+                if (s == MTK_OK && rr_prev > 0) floor_rel[ki] = std::sqrt(std::max(rr - frr, 0.0) / rr_prev);
             }
         }
         double rel = bb > 0 ? std::sqrt(rr / bb) : 0.0;
