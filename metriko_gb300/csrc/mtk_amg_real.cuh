@@ -468,15 +468,22 @@ __device__ __forceinline__ T rcsr_row(const RDevCsr<T>& M, int row, int lane, in
 // spread over groups of M.group lanes (1..32) with a warp-uniform loop and fixed-order reduction.
 template <typename T>
 __device__ void rcsr_phase(const RDevCsr<T>& M, const T* x, const RDevCsr<T>* M2, const T* x2, T* out, T scale,
-                           const unsigned char* mask, T* xdot = nullptr) {
+                           const unsigned char* mask, T* xdot = nullptr, const float* phi = nullptr, int nphi = 0,
+                           const T* yc = nullptr) {
     const int stride = gridDim.x * blockDim.x;
     const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
     const int g = M.group;
+    // optional extra term out += sum_k phi[k n + row] yc[k] (phi column-major, yc replicated)
+    auto extra = [&](int row) {
+        T e = T(0);
+        for (int k = 0; k < nphi; k++) e += (T)__ldg(phi + (size_t)k * M.n + row) * yc[k];
+        return e;
+    };
     if (g == 1) {
         for (int row = t0; row < M.n; row += stride) {
             T s = rcsr_row(M, row, 0, 1, x);
             if (M2) s += rcsr_row(*M2, row, 0, 1, x2);
-            const T o = (mask && mask[row]) ? T(0) : scale * s;
+            const T o = (mask && mask[row]) ? T(0) : (phi ? scale * s + extra(row) : scale * s);
             out[row] = o;
             if (xdot) *xdot += __ldcg(x + row) * o;
         }
@@ -492,7 +499,7 @@ __device__ void rcsr_phase(const RDevCsr<T>& M, const T* x, const RDevCsr<T>* M2
         }
         for (int o = g >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
         if (sl == 0 && row < M.n) {
-            const T o = (mask && mask[row]) ? T(0) : scale * s;
+            const T o = (mask && mask[row]) ? T(0) : (phi ? scale * s + extra(row) : scale * s);
             out[row] = o;
             if (xdot) *xdot += __ldcg(x + row) * o;
         }
@@ -500,10 +507,11 @@ __device__ void rcsr_phase(const RDevCsr<T>& M, const T* x, const RDevCsr<T>* M2
 }
 
 // z = out_scale * B r on the hierarchy; level 0 reads H.L[0].r and writes H.L[0].y (masked);
-// rz (may be null) accumulates this thread's share of r . z.
+// rz (may be null) accumulates this thread's share of r . z.  With phi (column-major, nphi
+// columns) the level-0 output also gets phi * yc, in the same pass.
 template <typename T>
 __device__ bool rvcycle(const RDevHierarchy<T>& H, T out_scale, const unsigned char* mask0, const GridBarrier& bar,
-                        T* rz = nullptr) {
+                        T* rz = nullptr, const float* phi = nullptr, int nphi = 0, const T* yc = nullptr) {
     const int stride = gridDim.x * blockDim.x;
     const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
     for (int l = 0; l < H.nlev; l++) {
@@ -526,7 +534,7 @@ __device__ bool rvcycle(const RDevHierarchy<T>& H, T out_scale, const unsigned c
     for (int l = H.nlev - 1; l >= 0; l--) {
         const T* yn = (l + 1 < H.nlev) ? H.L[l + 1].y : H.yc;
         rcsr_phase<T>(H.L[l].S, H.L[l].r, &H.L[l].P, yn, H.L[l].y, l == 0 ? out_scale : T(1), l == 0 ? mask0 : nullptr,
-                      l == 0 ? rz : nullptr);
+                      l == 0 ? rz : nullptr, l == 0 ? phi : nullptr, nphi, yc);
         if (l > 0 && !grid_sync(bar)) return false;
     }
     return true;

@@ -69,15 +69,21 @@ struct IgmOp {
     const T* BJJ;       // 2 W_J^T S W_J, nJ x nJ (row-major)
 };
 
-// Shared-memory layout of the replicated z state.
+// Shared-memory layout of the replicated z state (cz, wsum: the Schur coarse space).
 template <typename T>
 struct ZSmem {
-    T *xz, *rz, *zz, *pz, *qz, *XJ, *tmpJ, *tz;
+    T *xz, *rz, *zz, *pz, *qz, *XJ, *tmpJ, *tz, *cz, *wsum;
     __device__ void bind(T* base, int nZ, int nJ) {
         xz = base; rz = xz + nZ; zz = rz + nZ; pz = zz + nZ; qz = pz + nZ; tz = qz + nZ;
-        XJ = tz + nZ; tmpJ = XJ + nJ;
+        XJ = tz + nZ; tmpJ = XJ + nJ; cz = tmpJ + nJ; wsum = cz + nZ;
     }
 };
+// bytes of ZSmem for nZ, nJ
+inline size_t zsmem_bytes(size_t elem, int nZ, int nJ) {
+    return elem * (7 * (size_t)nZ + 2 * (size_t)nJ + (size_t)kWarps * nZ + 8);
+}
+constexpr int kPhiSlot = 8;     // partials offset (in blocks) of the coarse-space dots
+constexpr int kMaxPhi = 64;     // largest z block that gets the Schur coarse space
 
 template <typename T>
 struct ZProj {
@@ -280,6 +286,54 @@ __device__ bool igm_apply_asm(const IgmOp<T>& A, const unsigned char* __restrict
     return true;
 }
 
+// Schur coarse space of the z block.  Phi (nY x nZ, column-major) holds approximations of
+// -K_yy^-1 K_yz, so the columns of Z = [Phi ; I] are the z directions extended into the free
+// block with (nearly) least energy; the preconditioner adds Z W Z^T r to the multigrid of the
+// free block, W = P (P G P + ridge)^-1 P with G = Z^T K Z (the P's keep it on the feasible z
+// directions; rows of fixed variables are zero in the input and masked in the output).  With
+// an exact Phi this is the block factorisation K^-1 = [K_yy^-1 0; 0 0] + Z S^-1 Z^T (S the Schur
+// complement of the z block), so the coupled system converges like the free block alone.
+//
+// Block partials of Phi^T r_y in fixed order: out[k * gridDim.x + blockIdx.x].
+template <typename T>
+__device__ void phi_dots_publish(const float* __restrict__ Phi, int nY, int nZ, const T* r, T* out, T* wsum) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int stride = gridDim.x * blockDim.x;
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int k = 0; k < nZ; k++) {
+        T a = T(0);
+        const float* col = Phi + (size_t)k * nY;
+        for (int j = t0; j < nY; j += stride) a += (T)__ldg(col + j) * __ldcg(r + j);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if (lane == 0) wsum[warp * nZ + k] = a;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < nZ; k += blockDim.x) {
+        T v = T(0);
+        for (int w = 0; w < nw; w++) v += wsum[w * nZ + k];
+        out[k * gridDim.x + blockIdx.x] = v;
+    }
+    __syncthreads();
+}
+
+// After a grid barrier: c = P (Phi^T r_y + r_z), zz = P Minv c (the coarse coefficients y_c).
+template <typename T>
+__device__ void phi_coarse(const ZProj<T>& P, int nZ, const T* parts, ZSmem<T>& zs) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int k = warp; k < nZ; k += nw) {
+        T v = T(0);
+        for (int b = lane; b < (int)gridDim.x; b += 32) v += __ldcg(parts + k * gridDim.x + b);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) zs.cz[k] = v + zs.rz[k];
+    }
+    __syncthreads();
+    project_z(P, nZ, zs.cz, zs.tz);
+    precond_z(P, nZ, zs.cz, zs.zz);
+    project_z(P, nZ, zs.zz, zs.tz);
+}
+
 // E (replicated, after a barrier): qz = P_z (scale USmall^T XoJ + shift pz)
 template <typename T>
 __device__ void igm_apply_z(const IgmOp<T>& A, const ZProj<T>& P, const T* pz, T* qz, ZSmem<T>& zs) {
@@ -302,7 +356,8 @@ __global__ void __launch_bounds__(kBlock, 1) igm_pcg(IgmOp<T> A, ZProj<T> P, con
                                                  const T* __restrict__ minvy, const T* __restrict__ b, T* x, T* r, T* z,
                                                  T* p, T* p2, T* q, T* partials, GridBarrier bar, double tol2,
                                                  int maxit, int mode, int* out,
-                                                 const RDevHierarchy<T>* __restrict__ Hp, T mg_scale) {
+                                                 const RDevHierarchy<T>* __restrict__ Hp, T mg_scale,
+                                                 const float* __restrict__ Phi) {
     extern __shared__ unsigned char smem_raw[];
     ZSmem<T> zs;
     zs.bind(reinterpret_cast<T*>(smem_raw), A.nZ, A.nJ);
@@ -313,6 +368,8 @@ __global__ void __launch_bounds__(kBlock, 1) igm_pcg(IgmOp<T> A, ZProj<T> P, con
     T rr = T(0);
     T part[2];
     T pq1[1];
+    const bool defl = Phi && Hp && mode == 0 && nZ > 0;   // Schur coarse space on (see phi_coarse)
+    T* phi_parts = partials + kPhiSlot * gridDim.x;
     // replicated z state
     for (int j = threadIdx.x; j < nZ; j += blockDim.x) {
         zs.xz[j] = x[nY + j];
@@ -337,16 +394,20 @@ __global__ void __launch_bounds__(kBlock, 1) igm_pcg(IgmOp<T> A, ZProj<T> P, con
             part[0] += rj * zj;
         }
     }
-    if (mode == 0 && Hp) {   // multigrid on the free block: z_y = mask (B r_y) / scale
-        if (!grid_sync(bar)) { status = 5; goto done; }
-        if (!rvcycle(*Hp, mg_scale, fixy, bar, &part[0])) { status = 5; goto done; }
-    }
     for (int j = threadIdx.x; j < nZ; j += blockDim.x) zs.rz[j] = __ldg(b + nY + j) - zs.qz[j];
     __syncthreads();
     project_z(P, nZ, zs.rz, zs.tz);
+    if (defl) phi_dots_publish(Phi, nY, nZ, r, phi_parts, zs.wsum);
+    if (mode == 0 && Hp) {   // multigrid on the free block: z_y = mask (B r_y) / scale (+ Phi y_c)
+        if (!grid_sync(bar)) { status = 5; goto done; }
+        if (defl) phi_coarse(P, nZ, phi_parts, zs);
+        if (!rvcycle(*Hp, mg_scale, fixy, bar, &part[0], defl ? Phi : nullptr, nZ, zs.zz)) { status = 5; goto done; }
+    }
     if (mode == 0) {
-        precond_z(P, nZ, zs.rz, zs.zz);
-        project_z(P, nZ, zs.zz, zs.tz);
+        if (!defl) {
+            precond_z(P, nZ, zs.rz, zs.zz);
+            project_z(P, nZ, zs.zz, zs.tz);
+        }
         for (int j = threadIdx.x; j < nZ; j += blockDim.x) zs.pz[j] = zs.zz[j];
         __syncthreads();
     }
@@ -401,17 +462,21 @@ __global__ void __launch_bounds__(kBlock, 1) igm_pcg(IgmOp<T> A, ZProj<T> P, con
                 }
                 part[1] += rj * rj;
             }
-            if (Hp) {
-                if (!grid_sync(bar)) { status = 5; break; }
-                if (!rvcycle(*Hp, mg_scale, fixy, bar, &part[0])) { status = 5; break; }
-            }
             for (int j = threadIdx.x; j < nZ; j += blockDim.x) {
                 zs.xz[j] += alpha * zs.pz[j];
                 zs.rz[j] -= alpha * zs.qz[j];
             }
             __syncthreads();
-            precond_z(P, nZ, zs.rz, zs.zz);
-            project_z(P, nZ, zs.zz, zs.tz);
+            if (defl) phi_dots_publish(Phi, nY, nZ, r, phi_parts, zs.wsum);
+            if (Hp) {
+                if (!grid_sync(bar)) { status = 5; break; }
+                if (defl) phi_coarse(P, nZ, phi_parts, zs);
+                if (!rvcycle(*Hp, mg_scale, fixy, bar, &part[0], defl ? Phi : nullptr, nZ, zs.zz)) { status = 5; break; }
+            }
+            if (!defl) {
+                precond_z(P, nZ, zs.rz, zs.zz);
+                project_z(P, nZ, zs.zz, zs.tz);
+            }
             publish_partials<T, 2>(part, partials + 3 * gridDim.x);
             if (!grid_sync(bar)) { status = 5; break; }
             gather_partials<T, 2>(partials + 3 * gridDim.x, part);
@@ -771,6 +836,28 @@ __global__ void face_residual(int nF, const int* __restrict__ cutF, const double
     publish_partials<double, 1>(red, partials);
 }
 
+// Block partials of Phi^T v (FP64 sums): partials[k * gridDim.x + blockIdx.x], k < nZ.
+__global__ void phi_tdot(int nY, int nZ, const float* __restrict__ Phi, const float* __restrict__ v, double* partials) {
+    for (int k = 0; k < nZ; k++) {
+        double a[1] = {0};
+        const float* col = Phi + (size_t)k * nY;
+        for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nY; j += gridDim.x * blockDim.x)
+            a[0] += (double)col[j] * (double)v[j];
+        block_sum<double, 1>(a);
+        if (threadIdx.x == 0) partials[k * gridDim.x + blockIdx.x] = a[0];
+    }
+}
+
+// out[k] = fixed-order sum of partials[k * nb + 0 .. nb), k < K (one block).
+__global__ void finalize_k(const double* partials, int nb, int K, double* out) {
+    for (int k = 0; k < K; k++) {
+        double v[1] = {0};
+        for (int i = threadIdx.x; i < nb; i += blockDim.x) v[0] += partials[k * nb + i];
+        block_sum<double, 1>(v);
+        if (threadIdx.x == 0) out[k] = v[0];
+    }
+}
+
 // Fixed-order sum of one partial per block (written by publish_partials over nb blocks).
 __global__ void finalize1(const double* partials, int nb, double* out) {
     double v[1] = {0};
@@ -836,6 +923,11 @@ struct Igm {
     // assembled operator of the FP32 inner solves
     bool asm_ok = false;
     DBuf<int> ka_ptr, ka_col, cy_ptr, cy_col, cj_ptr, cj_col;
+    // Schur coarse space of the z block (phi_coarse): Phi column-major nY x nZ, G0 = Z^T K0 Z and
+    // C0 = Z^T Z for Z = [Phi ; I] and the unscaled operator K0
+    bool phi_ok = false;
+    DBuf<float> phi, qid32;
+    std::vector<double> G0, C0;
     DBuf<float> ka_val32, cy_val32, cj_val32, bjj32;
     DBuf<double> pb64;   // second direction buffers of the PCG (double-buffered p)
     // attainable reduction of the FP32 solves per refinement (first, second, later), measured as
@@ -962,6 +1054,7 @@ struct Igm {
     template <typename T>
     int run_pcg(IgmOp<T> A, ZProj<T> P, const T* minv, const T* b, T* x, T* r, T* z, T* p, T* q, double tol2, int maxit,
                 int mode, size_t smem, long long* iters, double* rr_out) {
+        const float* phiP = (phi_ok && mg && mode == 0) ? phi.p : nullptr;
         auto kern = igm_pcg<T>;
         MTK_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         int per_sm = 0;
@@ -987,7 +1080,7 @@ struct Igm {
         T* p2 = sizeof(T) == 8 ? reinterpret_cast<T*>(pb64.p) : reinterpret_cast<T*>(pb32.p);
         void* params[] = {&A, &P, (void*)&fx, (void*)&minv, (void*)&b, (void*)&x, (void*)&r, (void*)&z, (void*)&p,
                           (void*)&p2, (void*)&q, (void*)&partials, &bar, &tol2, &maxit, &mode, (void*)&out,
-                          (void*)&Hp, (void*)&mg_scale};
+                          (void*)&Hp, (void*)&mg_scale, (void*)&phiP};
         MTK_TRY(reset_barrier(c));
         MTK_CUDA_TRY(cudaEventRecord(c->ev_k0, st));
         MTK_CUDA_TRY(cudaLaunchCooperativeKernel(reinterpret_cast<void*>(kern), dim3(grid), dim3(kBlock), params, smem, st));
@@ -999,7 +1092,8 @@ struct Igm {
         cudaEventElapsedTime(&kms, c->ev_k0, c->ev_k1);
         pcg_ms += kms;
         pcg_launches++;
-        pcg_bytes += (iter_bytes(sizeof(T)) + (Hp ? (sizeof(T) == 8 ? mg_bytes64 : mg_bytes32) : 0.0)) *
+        pcg_bytes += (iter_bytes(sizeof(T)) + (Hp ? (sizeof(T) == 8 ? mg_bytes64 : mg_bytes32) : 0.0) +
+                      (phiP ? 8.0 * nZ * (double)nY : 0.0)) *
                      (double)(c->h_int[1] + 1);
         if (iters) *iters += c->h_int[1];
         if (rr_out) *rr_out = reinterpret_cast<double*>(c->h_int + 4)[0];
@@ -1101,6 +1195,86 @@ struct Igm {
             stats->spmv_calls += iters + refines + 1;
             if (rel > stats->max_rel_residual) stats->max_rel_residual = rel;
         }
+        return MTK_OK;
+    }
+
+    // Schur coarse space (phi_coarse).  Column k of Phi: FP32 PCG on the free block with the z
+    // block frozen at e_k (projector Q = I, right-hand side 0, so the free block solves
+    // K_yy phi = -K_yz e_k), to 1e-2 of its start residual (a coarse-space basis needs no more:
+    // the Galerkin G below keeps the preconditioner exact on its span).  Then per column one
+    // operator application w = -K0 [phi_k ; e_k] (residual mode, no projection) and
+    // G0_lk = -(phi_l . w_y + w_z,l), C0_lk = phi_l . phi_k + delta_lk.  Leaves phi_ok false
+    // (block Jacobi) when the multigrid is off, the z block is empty or larger than kMaxPhi,
+    // or a column solve breaks down.
+    int build_phi(long long* iters) {
+        phi_ok = false;
+        if (!mg || nZ <= 0 || nZ > kMaxPhi) return MTK_OK;
+        MTK_TRY(phi.alloc((size_t)nY * nZ));
+        MTK_CUDA_TRY(cudaMemsetAsync(phi.p, 0, sizeof(float) * (size_t)nY * nZ, st));
+        std::vector<float> eye((size_t)nZ * nZ, 0.f);
+        for (int k = 0; k < nZ; k++) eye[(size_t)k * nZ + k] = 1.f;
+        MTK_TRY(qid32.upload(eye.data(), eye.size(), st));
+        const double save_scale = cur_scale;
+        cur_scale = 1.0;
+        const ZProj<float> frozen{nZ, qid32.p, Mz32.p};
+        const ZProj<float> open{0, qid32.p, Mz32.p};
+        float* xk = e32.p;
+        float* zero = r32.p;
+        float* qf = reinterpret_cast<float*>(Xfull.p);
+        MTK_CUDA_TRY(cudaMemsetAsync(zero, 0, sizeof(float) * nRed, st));
+        for (int k = 0; k < nZ; k++) {
+            MTK_CUDA_TRY(cudaMemsetAsync(xk, 0, sizeof(float) * nRed, st));
+            c->h_scalars[0] = 0.0;
+            reinterpret_cast<float*>(c->h_scalars)[0] = 1.f;
+            MTK_CUDA_TRY(cudaMemcpyAsync(xk + nY + k, c->h_scalars, sizeof(float), cudaMemcpyHostToDevice, st));
+            double rr0 = 0;
+            MTK_TRY(run_pcg<float>(op32(1.0, 0.0), frozen, minvy32.p, zero, xk, z32.p, p32.p, q32.p, qf, 0.0, 0, 1, smem32,
+                                   nullptr, &rr0));
+            if (!(rr0 > 0)) continue;   // z_k does not touch the free block: phi_k = 0
+            int s = run_pcg<float>(op32(1.0, 0.0), frozen, minvy32.p, zero, xk, z32.p, p32.p, q32.p, qf, 1e-4 * rr0, 200, 0,
+                                   smem32, iters, nullptr);
+            if (s == MTK_ERR_TIMEOUT) return s;
+            if (s != MTK_OK && s != MTK_ERR_NOT_CONVERGED) { cur_scale = save_scale; return MTK_OK; }
+            MTK_CUDA_TRY(cudaMemcpyAsync(phi.p + (size_t)k * nY, xk, sizeof(float) * nY, cudaMemcpyDeviceToDevice, st));
+        }
+        G0.assign((size_t)nZ * nZ, 0.0);
+        C0.assign((size_t)nZ * nZ, 0.0);
+        const int nb = stream_grid(c);
+        std::vector<float> wz(nZ);
+        std::vector<double> dw(nZ), dp(nZ);
+        for (int k = 0; k < nZ; k++) {
+            MTK_CUDA_TRY(cudaMemsetAsync(xk, 0, sizeof(float) * nRed, st));
+            MTK_CUDA_TRY(cudaMemcpyAsync(xk, phi.p + (size_t)k * nY, sizeof(float) * nY, cudaMemcpyDeviceToDevice, st));
+            reinterpret_cast<float*>(c->h_scalars)[0] = 1.f;
+            MTK_CUDA_TRY(cudaMemcpyAsync(xk + nY + k, c->h_scalars, sizeof(float), cudaMemcpyHostToDevice, st));
+            MTK_TRY(run_pcg<float>(op32(1.0, 0.0), open, minvy32.p, zero, xk, z32.p, p32.p, q32.p, qf, 0.0, 0, 1, smem32,
+                                   nullptr, nullptr));
+            // w = z32 (= -K0 Z_k): G0 column k; Phi^T phi_k: C0 column k
+            // (nb * nZ partials and nZ scalars fit the context buffers for nZ <= kMaxPhi)
+            phi_tdot<<<nb, kStream, 0, st>>>(nY, nZ, phi.p, z32.p, c->partials);
+            finalize_k<<<1, kStream, 0, st>>>(c->partials, nb, nZ, c->scalars);
+            MTK_CUDA_TRY(cudaMemcpyAsync(dw.data(), c->scalars, sizeof(double) * nZ, cudaMemcpyDeviceToHost, st));
+            phi_tdot<<<nb, kStream, 0, st>>>(nY, nZ, phi.p, phi.p + (size_t)k * nY, c->partials);
+            finalize_k<<<1, kStream, 0, st>>>(c->partials, nb, nZ, c->scalars);
+            MTK_CUDA_TRY(cudaMemcpyAsync(dp.data(), c->scalars, sizeof(double) * nZ, cudaMemcpyDeviceToHost, st));
+            c->kernels += 4;
+            MTK_CUDA_TRY(cudaGetLastError());
+            MTK_CUDA_TRY(cudaMemcpyAsync(wz.data(), z32.p + nY, sizeof(float) * nZ, cudaMemcpyDeviceToHost, st));
+            MTK_CUDA_TRY(cudaStreamSynchronize(st));
+            for (int l = 0; l < nZ; l++) {
+                G0[(size_t)l * nZ + k] = -(dw[l] + (double)wz[l]);
+                C0[(size_t)l * nZ + k] = dp[l] + (l == k ? 1.0 : 0.0);
+            }
+        }
+        for (int a = 0; a < nZ; a++)
+            for (int b = 0; b < a; b++) {
+                const double g = 0.5 * (G0[(size_t)a * nZ + b] + G0[(size_t)b * nZ + a]);
+                G0[(size_t)a * nZ + b] = G0[(size_t)b * nZ + a] = g;
+                const double h = 0.5 * (C0[(size_t)a * nZ + b] + C0[(size_t)b * nZ + a]);
+                C0[(size_t)a * nZ + b] = C0[(size_t)b * nZ + a] = h;
+            }
+        cur_scale = save_scale;
+        phi_ok = true;
         return MTK_OK;
     }
 };
@@ -1284,8 +1458,8 @@ int igm_run(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts_in, do
     const int nLeftCap = std::max(1, d->nSingular + d->nInteger);
     MTK_TRY(S.left.alloc(nLeftCap));
     // shared memory for the replicated z state: 6 nZ + 2 nJ values
-    S.smem64 = sizeof(double) * (6 * (size_t)nZ + 2 * (size_t)nJ + 8);
-    S.smem32 = sizeof(float) * (6 * (size_t)nZ + 2 * (size_t)nJ + 8);
+    S.smem64 = zsmem_bytes(sizeof(double), nZ, nJ);
+    S.smem32 = zsmem_bytes(sizeof(float), nZ, nJ);
     if (S.smem64 > 200 * 1024) { mtk_set_last_error("constrained block too large for shared memory", __FILE__, __LINE__); return MTK_ERR_BAD_INPUT; }
 
     const int G = S.grid();
@@ -1430,6 +1604,10 @@ int igm_run(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts_in, do
     }
     auto build_zblock = [&](double scale, double shift, std::vector<double>& Kzz) {
         Kzz.assign((size_t)nZ * nZ, 0.0);
+        if (S.phi_ok) {   // Galerkin block of the Schur coarse space
+            for (size_t i = 0; i < Kzz.size(); i++) Kzz[i] = scale * S.G0[i] + shift * S.C0[i];
+            return;
+        }
         std::vector<double> tmp((size_t)nJ * nZ, 0.0);   // BJJ * USmall
         for (int a = 0; a < nJ; a++)
             for (int b = 0; b < nJ; b++) {
@@ -1582,6 +1760,16 @@ int igm_run(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts_in, do
     MTK_CUDA_TRY(cudaMemsetAsync(S.xs.p, 0, sizeof(double) * nRed, st));
     for (int k = 0; k < d->nFixed; k++) MTK_TRY(add_constraint(d->fixedIdcs[k], d->fixedVals[k]));
     MTK_TRY(upload_constraints(length, 0.0));
+    if (!getenv("MTK_NO_PHI")) {
+        auto tp0 = std::chrono::steady_clock::now();
+        long long phi_iters = 0;
+        MTK_TRY(S.build_phi(&phi_iters));
+        stt->pcg_iters += phi_iters;
+        if (S.phi_ok) MTK_TRY(upload_constraints(length, 0.0));
+        if (Igm::debug())
+            fprintf(stderr, "[igm host] Schur coarse space %s: %lld PCG iterations, %.1f ms\n", S.phi_ok ? "on" : "off",
+                    phi_iters, std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tp0).count());
+    }
     std::vector<double> es;   // size-field job: exp(sbar_f) per face, target es_f * F2_f
     if (job) {
         es.resize(nF);
