@@ -380,7 +380,7 @@ inline bool build_hierarchy(int n, const std::vector<int>& nbr3, const std::vect
         {
             std::vector<cd> v(ln), w(ln);
 #pragma omp parallel for schedule(static)
-            for (int i = 0; i < ln; i++) v[i] = cd((i & 1) ? 1.0 : -1.0 + 0.25 * ((i * 7919) % 5), 0.1 * ((i * 104729) % 7));
+            for (int i = 0; i < ln; i++) v[i] = cd((i & 1) ? 1.0 : -1.0 + 0.25 * (double)(((unsigned)i * 7919u) % 5u), 0.1 * (double)(((unsigned)i * 104729u) % 7u));
             for (int it = 0; it < 12; it++) {
                 double red[3];   // v^H A v, v^H D v, |w|^2
                 det_row_sums<3>(

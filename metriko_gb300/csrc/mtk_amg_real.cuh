@@ -299,7 +299,7 @@ inline bool build_real_hierarchy(RCsr A0, std::vector<int> node, std::vector<int
         {
             std::vector<double> v(n), w(n);
 #pragma omp parallel for schedule(static)
-            for (int i = 0; i < n; i++) v[i] = (i & 1) ? 1.0 : -1.0 + 0.25 * ((i * 7919) % 5);
+            for (int i = 0; i < n; i++) v[i] = (i & 1) ? 1.0 : -1.0 + 0.25 * (double)(((unsigned)i * 7919u) % 5u);
             for (int it = 0; it < 12; it++) {
                 double red[3];   // v^T A v, v^T D v, |w|^2
                 det_row_sums<3>(

@@ -972,7 +972,14 @@ struct FieldSolver {
                 vals[(size_t)j * n + f] = std::complex<double>(-std::cos(ang), -std::sin(ang));
             }
         HostHierarchy HH;
+        const auto tb0 = std::chrono::steady_clock::now();
         if (!build_hierarchy(n, nbr3, vals, 3.0 + 1e-9, HH, 1)) return MTK_OK;   // keep Jacobi
+        {
+            const char* e = getenv("MTK_DEBUG");
+            if (e && e[0] == '1')
+                fprintf(stderr, "[field host]   (hierarchy build %.1f ms)\n",
+                        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tb0).count());
+        }
         const int nl = (int)HH.lv.size();
         if (nl == 0) return MTK_OK;
         const HostLevel& L0 = HH.lv[0];

@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "mtk_amg_real.cuh"
+#include "mtk_amg_real_gpu.cuh"
 #include "mtk_ctx.cuh"
 
 namespace mtk {
@@ -966,57 +967,105 @@ struct Igm {
     }
 
     int build_mg(RCsr K, std::vector<int> node, std::vector<int> comp, int nnode) {
+        // the Galerkin products run on the device (RDevBuilder, the same arrays as the host
+        // build); the host builds when the device build declines (a row beyond its capacity)
+        const auto tb0 = std::chrono::steady_clock::now();
+        std::vector<DevCycleOps> dops;
+        std::vector<double> Ainv;
+        int nc = 0;
+        bool dev_ok = false;
+        if (!getenv("MTK_MG_HOST")) {
+            RDevBuilder B(c, st);
+            MTK_TRY(B.build(K, node, comp, nnode, dops, nc, Ainv, dev_ok));
+        }
         RHierarchy HH;
-        if (!build_real_hierarchy(std::move(K), std::move(node), std::move(comp), nnode, HH)) return MTK_OK;
-        const int nl = (int)HH.lv.size();
+        if (!dev_ok) {
+            dops.clear();
+            if (!build_real_hierarchy(std::move(K), std::move(node), std::move(comp), nnode, HH)) return MTK_OK;
+            nc = HH.nc;
+            Ainv = HH.Ainv;
+        }
+        if (debug())
+            fprintf(stderr, "[igm host]   (hierarchy build %.1f ms, %s)\n",
+                    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tb0).count(),
+                    dev_ok ? "device Galerkin products" : "host");
+        const int nl = dev_ok ? (int)dops.size() : (int)HH.lv.size();
         if (nl == 0) return MTK_OK;
         // lanes per row of a CSR phase: fewest rounds x dependent loads (ptr, then batches of four
         // entries per lane, each a column load and a gather) over the persistent grid
         const double threads = (double)c->num_sms * kBlock;
-        auto grp = [&](const RCsr& M) {
-            const double avg = M.n > 0 ? (double)M.col.size() / M.n : 0.0;
+        auto grp = [&](int n, size_t nnz) {
+            const double avg = n > 0 ? (double)nnz / n : 0.0;
             int best = 1;
             double bc = 1e300;
             for (int g = 1; g <= 32; g <<= 1) {
-                const double cost = std::ceil(M.n * (double)g / threads) * (1.0 + 2.0 * std::ceil(avg / (4.0 * g)));
+                const double cost = std::ceil(n * (double)g / threads) * (1.0 + 2.0 * std::ceil(avg / (4.0 * g)));
                 if (cost < bc - 1e-9) { bc = cost; best = g; }
             }
             return best;
         };
+        // adopt a device CSR (FP64 values) and its FP32 copy
+        auto adopt = [&](DevCsr64& D, RCsrBufs& B, int group) -> int {
+            B.n = D.n;
+            B.group = group;
+            B.ptr = std::move(D.ptr);
+            B.col = std::move(D.col);
+            B.v64 = std::move(D.val);
+            MTK_TRY(B.v32.alloc(std::max<size_t>(D.nnz, 1)));
+            if (D.nnz)
+                rgpu::to_f32_vals<<<stream_grid(c), kStream, 0, st>>>(D.nnz, B.v64.p, B.v32.p);
+            MTK_CUDA_TRY(cudaGetLastError());
+            return MTK_OK;
+        };
+        std::vector<double> lvl_nnz(3 * nl), lvl_n(2 * nl);   // R, S, P entries; S rows, R rows
         for (int l = 0; l < nl; l++) {
-            const RCycleOps& O = HH.ops[l];
             RLevelBufs& B = rlv[l];
-            // level 0's up phase writes z with the thread-per-row mapping of the PCG vector loops,
-            // which read it with no grid barrier in between: keep it at one lane per row
-            const int up = l == 0 ? 1 : std::max(grp(O.S), grp(O.P));
-            MTK_TRY(upload_rcsr(O.R, B.R, grp(O.R)));
-            MTK_TRY(upload_rcsr(O.S, B.S, up));
-            MTK_TRY(upload_rcsr(O.P, B.P, up));
+            int nS, nR;
+            size_t zR, zS, zP;
+            if (dev_ok) {
+                DevCycleOps& O = dops[l];
+                nS = O.S.n; nR = O.R.n; zR = O.R.nnz; zS = O.S.nnz; zP = O.P.nnz;
+                // level 0's up phase writes z with the thread-per-row mapping of the PCG vector
+                // loops, which read it with no grid barrier in between: keep it at one lane per row
+                const int up = l == 0 ? 1 : std::max(grp(nS, zS), grp(O.P.n, zP));
+                MTK_TRY(adopt(O.R, B.R, grp(nR, zR)));
+                MTK_TRY(adopt(O.S, B.S, up));
+                MTK_TRY(adopt(O.P, B.P, up));
+            } else {
+                const RCycleOps& O = HH.ops[l];
+                nS = O.S.n; nR = O.R.n; zR = O.R.col.size(); zS = O.S.col.size(); zP = O.P.col.size();
+                const int up = l == 0 ? 1 : std::max(grp(nS, zS), grp(O.P.n, zP));
+                MTK_TRY(upload_rcsr(O.R, B.R, grp(nR, zR)));
+                MTK_TRY(upload_rcsr(O.S, B.S, up));
+                MTK_TRY(upload_rcsr(O.P, B.P, up));
+            }
+            lvl_nnz[3 * l] = (double)zR; lvl_nnz[3 * l + 1] = (double)zS; lvl_nnz[3 * l + 2] = (double)zP;
+            lvl_n[2 * l] = nS; lvl_n[2 * l + 1] = nR;
             if (l > 0) {
-                MTK_TRY(B.r64.alloc(O.S.n)); MTK_TRY(B.y64.alloc(O.S.n));
-                MTK_TRY(B.r32.alloc(O.S.n)); MTK_TRY(B.y32.alloc(O.S.n));
+                MTK_TRY(B.r64.alloc(nS)); MTK_TRY(B.y64.alloc(nS));
+                MTK_TRY(B.r32.alloc(nS)); MTK_TRY(B.y32.alloc(nS));
             }
             auto m64 = [](const RCsrBufs& C) { return RDevCsr<double>{C.n, C.group, C.ptr.p, C.col.p, C.v64.p}; };
             auto m32 = [](const RCsrBufs& C) { return RDevCsr<float>{C.n, C.group, C.ptr.p, C.col.p, C.v32.p}; };
             RH64.L[l] = RDevLevel<double>{m64(B.R), m64(B.S), m64(B.P), B.r64.p, B.y64.p};
             RH32.L[l] = RDevLevel<float>{m32(B.R), m32(B.S), m32(B.P), B.r32.p, B.y32.p};
         }
-        MTK_TRY(rAinv64.upload(HH.Ainv.data(), HH.Ainv.size(), st));
-        std::vector<float> a32(HH.Ainv.begin(), HH.Ainv.end());
+        MTK_TRY(rAinv64.upload(Ainv.data(), Ainv.size(), st));
+        std::vector<float> a32(Ainv.begin(), Ainv.end());
         MTK_TRY(rAinv32.upload(a32.data(), a32.size(), st));
-        MTK_TRY(rrc64.alloc(HH.nc)); MTK_TRY(ryc64.alloc(HH.nc));
-        MTK_TRY(rrc32.alloc(HH.nc)); MTK_TRY(ryc32.alloc(HH.nc));
-        RH64.nlev = nl; RH64.nc = HH.nc; RH64.Ainv = rAinv64.p; RH64.rc = rrc64.p; RH64.yc = ryc64.p;
-        RH32.nlev = nl; RH32.nc = HH.nc; RH32.Ainv = rAinv32.p; RH32.rc = rrc32.p; RH32.yc = ryc32.p;
+        MTK_TRY(rrc64.alloc(nc)); MTK_TRY(ryc64.alloc(nc));
+        MTK_TRY(rrc32.alloc(nc)); MTK_TRY(ryc32.alloc(nc));
+        RH64.nlev = nl; RH64.nc = nc; RH64.Ainv = rAinv64.p; RH64.rc = rrc64.p; RH64.yc = ryc64.p;
+        RH32.nlev = nl; RH32.nc = nc; RH32.Ainv = rAinv32.p; RH32.rc = rrc32.p; RH32.yc = ryc32.p;
         {
             auto cyc = [&](double T) {
                 double b = 0;
                 for (int l = 0; l < nl; l++) {
-                    const RCycleOps& O = HH.ops[l];
-                    const double nnz = (double)O.R.col.size() + O.S.col.size() + O.P.col.size();
-                    b += nnz * (T + 4) + 4.0 * (O.R.n + 2.0 * O.S.n) + T * (3.0 * O.S.n + 2.0 * O.R.n);
+                    const double nnz = lvl_nnz[3 * l] + lvl_nnz[3 * l + 1] + lvl_nnz[3 * l + 2];
+                    const double nS = lvl_n[2 * l], nR = lvl_n[2 * l + 1];
+                    b += nnz * (T + 4) + 4.0 * (nR + 2.0 * nS) + T * (3.0 * nS + 2.0 * nR);
                 }
-                return b + (double)HH.nc * HH.nc * T + 2.0 * HH.nc * T;
+                return b + (double)nc * nc * T + 2.0 * nc * T;
             };
             mg_bytes64 = cyc(8);
             mg_bytes32 = cyc(4);
@@ -1478,6 +1527,13 @@ int igm_run(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts_in, do
     // ---- multigrid for the free block: K_pre = 2 W_y^T S W_y + delta I, delta = 1e-4 / length^2
     //      (the seamless system is length^2 K_pre exactly; the naive one up to the shift)
     auto th0 = std::chrono::steady_clock::now();
+    auto tlap = th0;
+    auto lap = [&](const char* what) {   // set-up stage times (MTK_DEBUG=1)
+        if (!Igm::debug()) return;
+        const auto t = std::chrono::steady_clock::now();
+        fprintf(stderr, "[igm host]   %-28s %7.1f ms\n", what, std::chrono::duration<double, std::milli>(t - tlap).count());
+        tlap = t;
+    };
     if (nY > 0 && !getenv("MTK_NO_AMG")) {
         std::vector<int> hs_ptr, hs_col;
         std::vector<double> hs_val;
@@ -1493,6 +1549,7 @@ int igm_run(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts_in, do
                 }
             },
             hs_ptr, hs_col, hs_val);
+        lap("stiffness (cut vertices)");
         const double delta = 1e-4 / (d->length * d->length);
         RCsr K;
         K.n = nY;
@@ -1514,6 +1571,7 @@ int igm_run(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts_in, do
                 add(j, delta);
             },
             K.ptr, K.col, K.val);
+        lap("free block K");
         // assembled operator of the FP32 inner solves: K_yy (without the multigrid's delta), the
         // free-to-translation coupling C_yJ and its transpose
         if (!getenv("MTK_NO_ASM")) {
@@ -1565,10 +1623,12 @@ int igm_run(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts_in, do
             MTK_TRY(S.cj_val32.upload(tval.data(), tval.size(), st));
             MTK_CUDA_TRY(cudaStreamSynchronize(st));
             S.asm_ok = true;   // BJJ is uploaded once it is built below
+            lap("assembled operator + upload");
         }
         std::vector<int> node(nY), comp(nY);
         for (int j = 0; j < nY; j++) { node[j] = y2full[j] / 2; comp[j] = y2full[j] % 2; }
         MTK_TRY(S.build_mg(std::move(K), std::move(node), std::move(comp), nFull / 2));
+        lap("hierarchy + upload");
     }
     if (Igm::debug())
         fprintf(stderr, "[igm host] multigrid set-up %.1f ms (levels %d)\n",

@@ -61,6 +61,20 @@ def test_pipeline_deterministic(gpu_ctx):
     assert list(a["fix_order"]) == list(b["fix_order"])
 
 
+@pytest.mark.parametrize("name", ["ico4_noise", "ico6_sh8"])
+def test_igm_multigrid_device_build_matches_host(gpu_ctx, monkeypatch, name):
+    """The IGM multigrid's Galerkin products built on the device (the default) give the same
+    arrays as the host build, so the whole pipeline is bit-identical either way."""
+    V, F, ratio, rs = meshgen.workload(name)
+    opts = M.solve_opts("mixed", tol=1e-8)
+    a = M.pipeline(gpu_ctx, V, F, ratio=ratio, round_seams=rs, opts=opts)
+    monkeypatch.setenv("MTK_MG_HOST", "1")
+    b = M.pipeline(gpu_ctx, V, F, ratio=ratio, round_seams=rs, opts=opts)
+    assert np.array_equal(a["fullx"], b["fullx"])
+    assert list(a["fix_order"]) == list(b["fix_order"])
+    assert a["stats"]["pcg_iters"] == b["stats"]["pcg_iters"]
+
+
 # full-size workloads: level-7 sphere (327,680 faces), the 1024 x 512 torus (1,048,576 faces,
 # seams rounded), the level-9 sphere with degree-16 displacement (5,242,880 faces)
 @pytest.mark.parametrize("name,prec,chi", [("ico6_sh8", "mixed", 2), ("ico7_sh8", "mixed", 2), ("ico7_sh8", "fp64", 2),
