@@ -347,11 +347,10 @@ inline HostCsr hcsr_adjoint(const HostCsr& M, int m) {
 //   P = alpha (I - omega D^-1 A) P_sa = alpha R^H
 // are formed for levels >= first_ops (the device applies level 0 from the ELL rows, the
 // aggregates, T and w_p).
-inline bool build_hierarchy(int n, const std::vector<int>& nbr3, const std::vector<std::complex<double>>& vals,
-                            double diag, HostHierarchy& H, int first_ops = 0) {
+// Level-0 CSR from the ELL rows: the diagonal and the three neighbours, sorted by column.
+inline HostCsr ell_to_csr(int n, const std::vector<int>& nbr3, const std::vector<std::complex<double>>& vals,
+                          double diag) {
     using cd = std::complex<double>;
-    H.lv.clear();
-    H.ops.clear();
     HostCsr A0;
     A0.n = n;
     A0.ptr.resize(n + 1);
@@ -367,7 +366,15 @@ inline bool build_hierarchy(int n, const std::vector<int>& nbr3, const std::vect
         for (int k = 0; k < 4; k++) { A0.col[4 * (size_t)f + k] = e[k].c; A0.val[4 * (size_t)f + k] = e[k].v; }
     }
     A0.ptr[n] = 4 * n;
-    HostCsr cur = std::move(A0);
+    return A0;
+}
+
+inline bool build_hierarchy(int n, const std::vector<int>& nbr3, const std::vector<std::complex<double>>& vals,
+                            double diag, HostHierarchy& H, int first_ops = 0) {
+    using cd = std::complex<double>;
+    H.lv.clear();
+    H.ops.clear();
+    HostCsr cur = ell_to_csr(n, nbr3, vals, diag);
     const double omega = kOmega, alpha = kAlpha;
     while (cur.n > kCoarseMax && (int)H.lv.size() < kMaxLevels - 1) {
         HostLevel L;

@@ -42,7 +42,7 @@ constexpr int kScanBlock = 1024;
 
 // ---------------------------------------------------------------- exclusive scan of counts
 // out[0] = 0, out[i + 1] = out[i] + cnt[i]; bsum: per-block totals (nb = ceil(n / kScanBlock)).
-__global__ void scan_block_sums(int n, const int* __restrict__ cnt, long long* bsum) {
+static __global__ void scan_block_sums(int n, const int* __restrict__ cnt, long long* bsum) {
     __shared__ long long s[32];
     const int b = blockIdx.x;
     long long v = 0;
@@ -59,7 +59,7 @@ __global__ void scan_block_sums(int n, const int* __restrict__ cnt, long long* b
 }
 
 // one thread: exclusive scan of the block totals in place, total in *tot
-__global__ void scan_block_offsets(int nb, long long* bsum, long long* tot) {
+static __global__ void scan_block_offsets(int nb, long long* bsum, long long* tot) {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
     long long run = 0;
     for (int b = 0; b < nb; b++) {
@@ -71,7 +71,7 @@ __global__ void scan_block_offsets(int nb, long long* bsum, long long* tot) {
 }
 
 // per block: sequential scan by one warp over kScanBlock counts (32 lanes x 32 values)
-__global__ void scan_apply(int n, const int* __restrict__ cnt, const long long* __restrict__ boff, int* out) {
+static __global__ void scan_apply(int n, const int* __restrict__ cnt, const long long* __restrict__ boff, int* out) {
     if (threadIdx.x >= 32) return;
     const int lane = threadIdx.x;
     const int base = blockIdx.x * kScanBlock + lane * 32;
@@ -246,10 +246,10 @@ __global__ void rows_dense(int n, int ncols, Visit visit, double* scratch, unsig
 }
 
 // ---------------------------------------------------------------- transpose
-__global__ void col_counts(int nnz, const int* __restrict__ col, int* cnt) {
+static __global__ void col_counts(int nnz, const int* __restrict__ col, int* cnt) {
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < nnz; p += gridDim.x * blockDim.x) atomicAdd(cnt + col[p], 1);
 }
-__global__ void transpose_fill(int n, const int* __restrict__ Mp, const int* __restrict__ Mc, const double* __restrict__ Mv,
+static __global__ void transpose_fill(int n, const int* __restrict__ Mp, const int* __restrict__ Mc, const double* __restrict__ Mv,
                                int* fill, int* tcol, double* tval) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         for (int p = Mp[i]; p < Mp[i + 1]; p++) {
@@ -261,7 +261,7 @@ __global__ void transpose_fill(int n, const int* __restrict__ Mp, const int* __r
 // One warp per output row: each entry goes to its rank among the row's entries (input rows are
 // distinct within an output row), so rows come out ascending (the host transpose's order);
 // values / div (div != 1).
-__global__ void transpose_rank(int m, const int* __restrict__ tp, const int* __restrict__ ucol,
+static __global__ void transpose_rank(int m, const int* __restrict__ tp, const int* __restrict__ ucol,
                                const double* __restrict__ uval, int* tcol, double* tval, double div) {
     const int lane = threadIdx.x & 31;
     const int warps = (gridDim.x * blockDim.x) >> 5;
@@ -279,7 +279,7 @@ __global__ void transpose_rank(int m, const int* __restrict__ tp, const int* __r
 
 // ---------------------------------------------------------------- cycle operators
 // S = omega D^-1 (2 I - A omega D^-1) on the pattern of A
-__global__ void smoother_vals(int n, const int* __restrict__ Ap, const int* __restrict__ Ac, const double* __restrict__ Av,
+static __global__ void smoother_vals(int n, const int* __restrict__ Ap, const int* __restrict__ Ac, const double* __restrict__ Av,
                               const double* __restrict__ dinv, double omega, double* Sv) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const double di = __dmul_rn(omega, dinv[i]);
@@ -293,7 +293,7 @@ __global__ void smoother_vals(int n, const int* __restrict__ Ap, const int* __re
 }
 
 // P row i = alpha P_sa row + (-alpha omega dinv_i) (A P_sa) row, merged by column
-__global__ void prolong_rows(int n, const int* __restrict__ Pp, const int* __restrict__ Pc, const double* __restrict__ Pv,
+static __global__ void prolong_rows(int n, const int* __restrict__ Pp, const int* __restrict__ Pc, const double* __restrict__ Pv,
                              const int* __restrict__ Bp, const int* __restrict__ Bc, const double* __restrict__ Bv,
                              const double* __restrict__ dinv, double alpha, double omega, int* cnt_out,
                              const int* __restrict__ optr, int* ocol, double* oval) {
@@ -319,12 +319,12 @@ __global__ void prolong_rows(int n, const int* __restrict__ Pp, const int* __res
 }
 
 // ---------------------------------------------------------------- spectral radius of D^-1 A
-__global__ void rho_start(int n, double* v) {
+static __global__ void rho_start(int n, double* v) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         v[i] = (i & 1) ? 1.0 : __dadd_rn(-1.0, __dmul_rn(0.25, (double)(((unsigned)i * 7919u) % 5u)));
 }
 // per row: w = dinv (A v); terms v (A v), v v / dinv, w w
-__global__ void rho_rows(int n, const int* __restrict__ Ap, const int* __restrict__ Ac, const double* __restrict__ Av,
+static __global__ void rho_rows(int n, const int* __restrict__ Ap, const int* __restrict__ Ac, const double* __restrict__ Av,
                          const double* __restrict__ dinv, const double* __restrict__ v, double* w, double* t3) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         double av = 0.0;
@@ -339,7 +339,7 @@ __global__ void rho_rows(int n, const int* __restrict__ Ap, const int* __restric
 // One CTA per block of kRhoRows rows: the terms are staged through shared memory in chunks and
 // summed by one thread in row order (the host's per-block order).
 constexpr int kRhoChunk = 1024;
-__global__ void rho_block_sums(int n, const double* __restrict__ t3, double* part) {
+static __global__ void rho_block_sums(int n, const double* __restrict__ t3, double* part) {
     __shared__ double sh[3 * kRhoChunk];
     const int b = blockIdx.x;
     const int r0 = b * kRhoRows, r1 = min(n, r0 + kRhoRows);
@@ -363,7 +363,7 @@ __global__ void rho_block_sums(int n, const double* __restrict__ t3, double* par
     }
 }
 // one thread: block sums in order into out[0..3), and the normalisation 1 / sqrt(out[2]) in out[3]
-__global__ void rho_total(int nb, const double* __restrict__ part, double* out) {
+static __global__ void rho_total(int nb, const double* __restrict__ part, double* out) {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
     double o0 = 0.0, o1 = 0.0, o2 = 0.0;
     for (int b = 0; b < nb; b++) {
@@ -376,13 +376,13 @@ __global__ void rho_total(int nb, const double* __restrict__ part, double* out) 
     out[2] = o2;
     out[3] = o2 > 0 ? __ddiv_rn(1.0, __dsqrt_rn(o2)) : 0.0;
 }
-__global__ void scale_vec(int n, const double* __restrict__ w, const double* __restrict__ sc, double* v) {
+static __global__ void scale_vec(int n, const double* __restrict__ w, const double* __restrict__ sc, double* v) {
     const double s = *sc;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] = __dmul_rn(w[i], s);
 }
 
 // dinv_i = 1 / A_ii (1 where the diagonal is missing or not positive), as raggregate
-__global__ void diag_inv(int n, const int* __restrict__ Ap, const int* __restrict__ Ac, const double* __restrict__ Av,
+static __global__ void diag_inv(int n, const int* __restrict__ Ap, const int* __restrict__ Ac, const double* __restrict__ Av,
                          double* dinv) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         int lo = Ap[i], hi = Ap[i + 1];
@@ -395,7 +395,7 @@ __global__ void diag_inv(int n, const int* __restrict__ Ap, const int* __restric
     }
 }
 
-__global__ void to_f32_vals(size_t n, const double* __restrict__ a, float* b) {
+static __global__ void to_f32_vals(size_t n, const double* __restrict__ a, float* b) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) b[i] = (float)a[i];
 }
 
@@ -472,18 +472,21 @@ class RDevBuilder {
             const bool dense = na <= rgpu::kDenseCols;
             if (dense) MTK_TRY(dense_scratch(na));
             // P_sa = (I - wp D^-1 A) T
+            // rows of level 0 are short (the mesh stencil): sorted arrays; deeper levels: a table,
+            // or dense scratch rows when the next level is small
+            auto rows = [&](int nr, auto visit, int* cnt, const int* optr, int* oc, double* ov) {
+                if (dense)
+                    rgpu::rows_dense<<<rgpu::kDenseGrid, kStream, 0, st_>>>(nr, na, visit, dacc_.p, dmark_.p, cnt, optr, oc, ov);
+                else if (levels == 0)
+                    rgpu::rows_sorted<<<grid(nr), kStream, 0, st_>>>(nr, visit, cnt, optr, oc, ov, err_.p);
+                else
+                    rgpu::rows_hash<<<grid(nr), 128, 0, st_>>>(nr, visit, cnt, optr, oc, ov, err_.p);
+            };
             const rgpu::PsaVisit pv{dA.ptr.p, dA.col.p, dA.val.p, agg.p, T.p, dinv.p, wp};
-            MTK_TRY(two_pass(n, Psa, [&](int* cnt, const int* optr, int* oc, double* ov) {
-                rgpu::rows_sorted<<<grid(n), kStream, 0, st_>>>(n, pv, cnt, optr, oc, ov, err_.p);
-            }));
+            MTK_TRY(two_pass(n, Psa, [&](int* cnt, const int* optr, int* oc, double* ov) { rows(n, pv, cnt, optr, oc, ov); }));
             // A P_sa
             const rgpu::ProdVisit ap{dA.ptr.p, dA.col.p, dA.val.p, Psa.ptr.p, Psa.col.p, Psa.val.p};
-            MTK_TRY(two_pass(n, AP, [&](int* cnt, const int* optr, int* oc, double* ov) {
-                if (dense)
-                    rgpu::rows_dense<<<rgpu::kDenseGrid, kStream, 0, st_>>>(n, na, ap, dacc_.p, dmark_.p, cnt, optr, oc, ov);
-                else
-                    rgpu::rows_sorted<<<grid(n), kStream, 0, st_>>>(n, ap, cnt, optr, oc, ov, err_.p);
-            }));
+            MTK_TRY(two_pass(n, AP, [&](int* cnt, const int* optr, int* oc, double* ov) { rows(n, ap, cnt, optr, oc, ov); }));
             lap("Psa, A Psa", levels);
             // P_sa^T (A P_sa)
             MTK_TRY(transpose(Psa, na, Pt, 1.0));

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "mtk_amg.cuh"
+#include "mtk_amg_gpu.cuh"
 #include "mtk_ctx.cuh"
 
 namespace mtk {
@@ -971,18 +972,34 @@ struct FieldSolver {
                 double ang = (double)N * (theta_h[3 * f + j] + pi);
                 vals[(size_t)j * n + f] = std::complex<double>(-std::cos(ang), -std::sin(ang));
             }
+        // the Galerkin products run on the device (CDevBuilder, the same arrays as the host
+        // build); the host builds when the device build declines (a row beyond its capacity)
         HostHierarchy HH;
         const auto tb0 = std::chrono::steady_clock::now();
-        if (!build_hierarchy(n, nbr3, vals, 3.0 + 1e-9, HH, 1)) return MTK_OK;   // keep Jacobi
+        std::vector<DevCycleOpsC> dops;
+        HostLevel dL0;
+        bool dev_ok = false;
+        if (!getenv("MTK_MG_HOST")) {
+            CDevBuilder B(c, c->stream);
+            std::vector<std::complex<double>> dAinv;
+            int dnc = 0;
+            MTK_TRY(B.build(ell_to_csr(n, nbr3, vals, 3.0 + 1e-9), dL0, dops, dnc, dAinv, dev_ok));
+            if (dev_ok) { HH.nc = dnc; HH.Ainv = std::move(dAinv); }
+        }
+        if (!dev_ok) {
+            dops.clear();
+            if (!build_hierarchy(n, nbr3, vals, 3.0 + 1e-9, HH, 1)) return MTK_OK;   // keep Jacobi
+        }
         {
             const char* e = getenv("MTK_DEBUG");
             if (e && e[0] == '1')
-                fprintf(stderr, "[field host]   (hierarchy build %.1f ms)\n",
-                        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tb0).count());
+                fprintf(stderr, "[field host]   (hierarchy build %.1f ms, %s)\n",
+                        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tb0).count(),
+                        dev_ok ? "device Galerkin products" : "host");
         }
-        const int nl = (int)HH.lv.size();
+        const int nl = dev_ok ? (int)dops.size() : (int)HH.lv.size();
         if (nl == 0) return MTK_OK;
-        const HostLevel& L0 = HH.lv[0];
+        const HostLevel& L0 = dev_ok ? dL0 : HH.lv[0];
         const int nagg = (int)L0.mptr.size() - 1;
         // chunks of <= 32 rows holding whole aggregates
         std::vector<int> chunk{0};
@@ -1029,15 +1046,43 @@ struct FieldSolver {
             return best;
         };
         auto avg = [](const HostCsr& M) { return M.n > 0 ? (double)M.col.size() / M.n : 0.0; };
+        auto davg = [](const DevCsrC& M) { return M.n > 0 ? (double)M.nnz / M.n : 0.0; };
+        // adopt a device CSR (FP64 values) and its FP32 copy
+        auto adopt = [&](DevCsrC& D, CsrBufs& B, int group) -> int {
+            B.n = D.n;
+            B.group = group;
+            B.ptr = std::move(D.ptr);
+            B.col = std::move(D.col);
+            B.v64 = std::move(D.val);
+            MTK_TRY(B.v32.alloc(std::max<size_t>(D.nnz, 1)));
+            if (D.nnz) cgpu::to_f32_vals<<<stream_grid(c), kStream, 0, st>>>(D.nnz, B.v64.p, B.v32.p);
+            MTK_CUDA_TRY(cudaGetLastError());
+            return MTK_OK;
+        };
         const int ni = nl - 1;   // inner (CSR) levels
+        std::vector<double> lv_nnz(3 * (size_t)std::max(ni, 1)), lv_n(2 * (size_t)std::max(ni, 1));
         for (int i = 0; i < ni; i++) {
-            const HostCycleOps& O = HH.ops[i + 1];
             LevelBufs& B = lvb[i];
-            MTK_TRY(upload_csr(O.R, B.R, grp(O.R.n, avg(O.R))));
-            const int up = grp(O.S.n, std::max(avg(O.S), avg(O.P)));
-            MTK_TRY(upload_csr(O.S, B.S, up));
-            MTK_TRY(upload_csr(O.P, B.P, up));
-            const int ln = O.S.n;
+            int ln = 0;
+            if (dev_ok) {
+                DevCycleOpsC& O = dops[i + 1];
+                lv_nnz[3 * i] = (double)O.R.nnz; lv_nnz[3 * i + 1] = (double)O.S.nnz; lv_nnz[3 * i + 2] = (double)O.P.nnz;
+                lv_n[2 * i] = O.S.n; lv_n[2 * i + 1] = O.R.n;
+                const int up = grp(O.S.n, std::max(davg(O.S), davg(O.P)));
+                MTK_TRY(adopt(O.R, B.R, grp(O.R.n, davg(O.R))));
+                MTK_TRY(adopt(O.S, B.S, up));
+                MTK_TRY(adopt(O.P, B.P, up));
+                ln = B.S.n;
+            } else {
+                const HostCycleOps& O = HH.ops[i + 1];
+                lv_nnz[3 * i] = (double)O.R.col.size(); lv_nnz[3 * i + 1] = (double)O.S.col.size(); lv_nnz[3 * i + 2] = (double)O.P.col.size();
+                lv_n[2 * i] = O.S.n; lv_n[2 * i + 1] = O.R.n;
+                MTK_TRY(upload_csr(O.R, B.R, grp(O.R.n, avg(O.R))));
+                const int up = grp(O.S.n, std::max(avg(O.S), avg(O.P)));
+                MTK_TRY(upload_csr(O.S, B.S, up));
+                MTK_TRY(upload_csr(O.P, B.P, up));
+                ln = O.S.n;
+            }
             MTK_TRY(B.r64.alloc(ln)); MTK_TRY(B.r32.alloc(ln));
             MTK_TRY(B.y64.alloc(ln)); MTK_TRY(B.y32.alloc(ln));
             auto mk64 = [](const CsrBufs& C) { return DevCsr<double>{C.n, C.group, C.ptr.p, C.col.p, C.v64.p}; };
@@ -1064,10 +1109,10 @@ struct FieldSolver {
             auto cyc = [&](double T) {
                 double bt = 0;
                 for (int i = 0; i < ni; i++) {
-                    const HostCycleOps& O = HH.ops[i + 1];
-                    const double nnz = (double)O.R.col.size() + O.S.col.size() + O.P.col.size();
-                    bt += nnz * (2 * T + 4) + 4.0 * (O.R.n + 2.0 * O.S.n);
-                    bt += 2 * T * (2.0 * O.S.n + 2.0 * O.R.n + O.S.n);
+                    const double nnz = lv_nnz[3 * i] + lv_nnz[3 * i + 1] + lv_nnz[3 * i + 2];
+                    const double nS = lv_n[2 * i], nR = lv_n[2 * i + 1];
+                    bt += nnz * (2 * T + 4) + 4.0 * (nR + 2.0 * nS);
+                    bt += 2 * T * (2.0 * nS + 2.0 * nR + nS);
                 }
                 bt += (double)HH.nc * HH.nc * 2 * T + 4.0 * HH.nc * T;
                 bt += 2.0 * nagg * 2 * T;
