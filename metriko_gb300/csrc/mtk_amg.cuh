@@ -197,35 +197,41 @@ inline int aggregate_level(HostLevel& L) {
     // pass 3: singletons / new aggregates for what is left
     for (int i = 0; i < n; i++)
         if (L.agg[i] < 0) { L.agg[i] = na++; parent[i] = -1; }
-    // transported near-null vector along the parent tree (parents precede in pass order)
+    // transported near-null vector along the parent forest: t = 1 at a root, t_v = -(a / |a|) t_parent
+    // with a = A(v, parent).  Each value depends on its parent's only, so the forest is resolved
+    // in parallel rounds (round r computes the nodes whose parent was resolved before round r):
+    // the same values as any sequential order.
     std::vector<std::complex<double>> t(n, std::complex<double>(0, 0));
-    std::vector<int> order;
-    order.reserve(n);
-    std::vector<char> done(n, 0);
     std::vector<int> cnt(na, 0);
     for (int i = 0; i < n; i++) cnt[L.agg[i]]++;
-    // resolve in dependency order (a parent is a root or attached earlier)
-    std::vector<int> stack;
-    for (int i = 0; i < n; i++) {
-        if (done[i]) continue;
-        stack.clear();
-        int k = i;
-        while (k >= 0 && !done[k]) { stack.push_back(k); k = parent[k]; }
-        for (int s = (int)stack.size() - 1; s >= 0; s--) {
-            int v = stack[s];
-            int pv = parent[v];
-            if (pv < 0) {
-                t[v] = 1.0;
-            } else {
+    {
+        std::vector<int> rnd(n), rnd_next;   // round in which a node was resolved (-1: not yet)
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < n; i++) {
+            rnd[i] = parent[i] < 0 ? 0 : -1;
+            if (parent[i] < 0) t[i] = 1.0;
+        }
+        for (int r = 1;; r++) {
+            rnd_next = rnd;
+            int changed = 0;
+#pragma omp parallel for schedule(static) reduction(+ : changed)
+            for (int v = 0; v < n; v++) {
+                if (rnd[v] >= 0) continue;
+                const int pv = parent[v];
+                if (rnd[pv] < 0) continue;
                 std::complex<double> a(0, 0);
                 for (int p = A.ptr[v]; p < A.ptr[v + 1]; p++) if (A.col[p] == pv) { a = A.val[p]; break; }
-                double m = std::abs(a);
+                const double m = std::abs(a);
                 t[v] = m > 0 ? -(a / m) * t[pv] : t[pv];
+                rnd_next[v] = r;
+                changed++;
             }
-            done[v] = 1;
+            rnd.swap(rnd_next);
+            if (!changed) break;
         }
     }
     L.T.resize(n);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < n; i++) L.T[i] = t[i] / std::sqrt((double)cnt[L.agg[i]]);
     L.mptr.assign(na + 1, 0);
     for (int i = 0; i < n; i++) L.mptr[L.agg[i] + 1]++;
