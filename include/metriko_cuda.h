@@ -258,6 +258,31 @@ int mtk_pipeline_size_field_gradient(mtk_ctx* ctx, int32_t nV, int32_t nF, const
                                      mtk_stats* stats);
 
 /*
+ * Barrier of the local-injectivity option: InjectiveBarrier(N, nF, intrinsic_field) followed by
+ * update(field, update_j, fBarrier, gBarrier) of core/igm/iterative_rounding/injective_barrier.h:
+ * 18-106.  Layout of intrinsic_field and field: 2*N values per face (vector j of face i at
+ * 2*N*i + 2*j).  Per row k = N*i + j (vectors j and (j+1) mod N of face i):
+ *   f_barrier[k]  1/bar(r) - 1 with r the volume ratio of the two vectors (infinite for r <= 0,
+ *                 0 for r >= 1/2)
+ *   bar_der[k]    the diagonal of gBarrier (d f_barrier / d r), when update_j
+ *   s_rows[4*k]   the row of dr/d(v0.x, v0.y, v1.x, v1.y) (gen_image_filed), when update_j
+ * bar_der and s_rows may be NULL when update_j == 0.
+ */
+int mtk_injective_barrier(mtk_ctx* ctx, int32_t nF, int32_t N, const double* intrinsic_field, const double* field,
+                          int32_t update_j, double* f_barrier, double* bar_der, double* s_rows);
+
+/*
+ * locally_injectivity_check of core/igm/parameterization_integ.ipp:46-63: the orientation of
+ * every cut face in the parameterization.  cfn[nF*3*N]: the N function values at the three
+ * corners of each cut face (corner j of face f at 3*N*f + N*j; corners in the order of the
+ * face's halfedge, its next and its prev); functions 0 and 1 are the (u, v) of the map.
+ * *n_flipped = faces with cross(b - a, c - a) < 0 (the map is locally injective when 0),
+ * *first_flipped (may be NULL) = the lowest such face, nF when none.
+ */
+int mtk_local_injectivity(mtk_ctx* ctx, int32_t nF, int32_t N, const double* cfn, int32_t* n_flipped,
+                          int32_t* first_flipped);
+
+/*
  * The inputs of mtk_field_smoothest for a closed mesh (host only): nbr[3*nF] the face across
  * each face halfedge, theta[3*nF] = farg(h) - farg(twin h) (face_rosy_field.h:72-102), and
  * area[nF] (may be NULL).

@@ -22,6 +22,7 @@ EXPORTS = [
     "mtk_ctx_kernel_count", "mtk_field_smoothest", "mtk_iterative_rounding", "mtk_pipeline_run",
     "mtk_seeded_init", "mtk_topology_from_field", "mtk_field_smoothest_noalloc", "mtk_size_field_gradient",
     "mtk_pipeline_size_field_gradient", "mtk_field_solve", "mtk_field_inputs", "mtk_field_spmv_bench",
+    "mtk_injective_barrier", "mtk_local_injectivity",
 ]
 
 
@@ -91,6 +92,10 @@ def lib():
         L.mtk_field_spmv_bench.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
                                            C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                            C.POINTER(C.c_double)]
+        L.mtk_injective_barrier.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
+                                            C.c_void_p, C.c_void_p, C.c_void_p]
+        L.mtk_local_injectivity.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.POINTER(C.c_int32),
+                                            C.POINTER(C.c_int32)]
         L.mtk_field_solve.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.c_void_p, C.POINTER(SolveOpts), C.c_void_p, C.POINTER(Stats)]
         L.mtk_pipeline_size_field_gradient.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
@@ -221,6 +226,34 @@ def field_inputs(V, F):
     area = np.empty(nF)
     _check(lib().mtk_field_inputs(len(V), nF, _ptr(V), _ptr(F), _ptr(nbr), _ptr(theta), _ptr(area)), "mtk_field_inputs")
     return nbr.reshape(nF, 3), theta.reshape(nF, 3), area
+
+
+def injective_barrier(ctx: Context, intrinsic_field, field, N=4, update_j=True):
+    """mtk_injective_barrier: (f_barrier (nF*N), bar_der (nF*N), s_rows (nF*N x 4)) of
+    InjectiveBarrier(N, nF, intrinsic_field).update(field, update_j, ...)."""
+    F2 = np.ascontiguousarray(intrinsic_field, np.float64).reshape(-1)
+    fd = np.ascontiguousarray(field, np.float64).reshape(-1)
+    if F2.size != fd.size or F2.size % (2 * N):
+        raise ValueError("fields must have 2*N values per face")
+    nF = F2.size // (2 * N)
+    fB = np.empty(nF * N)
+    dB = np.empty(nF * N) if update_j else None
+    S = np.empty(4 * nF * N) if update_j else None
+    _check(lib().mtk_injective_barrier(ctx.handle, nF, N, _ptr(F2), _ptr(fd), int(bool(update_j)), _ptr(fB),
+                                       _ptr(dB) if update_j else None, _ptr(S) if update_j else None),
+           "mtk_injective_barrier")
+    return fB, dB, (S.reshape(-1, 4) if update_j else None)
+
+
+def local_injectivity(ctx: Context, cfn, N=4):
+    """mtk_local_injectivity: (flipped faces, first flipped face (nF when none)) of the map
+    given by cfn (nF x 3N: the N function values at each corner)."""
+    c = np.ascontiguousarray(cfn, np.float64).reshape(-1)
+    nF = c.size // (3 * N)
+    nf, first = C.c_int32(0), C.c_int32(0)
+    _check(lib().mtk_local_injectivity(ctx.handle, nF, N, _ptr(c), C.byref(nf), C.byref(first)),
+           "mtk_local_injectivity")
+    return nf.value, first.value
 
 
 def spmv_bench(ctx: Context, nbr, theta, precision="mixed", reps=20):

@@ -1043,6 +1043,48 @@ class SeamlessIntegration:
         return mx <= 10e-7
 
 
+def injective_barrier_update(intrinsic_field, field, N=4, update_j=True):
+    """InjectiveBarrier(N, nF, intrinsic_field).update(field, updateJ, fBarrier, gBarrier)
+    (injective_barrier.h:18-106).  Row k = N i + j pairs vectors j and (j+1) mod N of face i
+    (2 N values per face).  Returns fBarrier, the diagonal of gBarrier and the rows of S
+    (gen_image_filed), the last two None without update_j."""
+    s = 0.5
+    F2 = np.asarray(intrinsic_field, float).reshape(-1, N, 2)
+    fd = np.asarray(field, float).reshape(-1, N, 2)
+    V = (np.sqrt(F2[..., 0] ** 2 + F2[..., 1] ** 2) *
+         np.sqrt(np.roll(F2, -1, axis=1)[..., 0] ** 2 + np.roll(F2, -1, axis=1)[..., 1] ** 2)).ravel()
+    v0 = fd.reshape(-1, 2)
+    v1 = np.roll(fd, -1, axis=1).reshape(-1, 2)
+    with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+        r = (v0[:, 0] * v1[:, 1] - v0[:, 1] * v1[:, 0]) / V
+        bar = (r / s) ** 3 - 3 * (r / s) ** 2 + 3 * r / s
+        fB = 1.0 / bar - 1.0
+        fB = np.where(r <= 0, np.inf, fB)
+        fB = np.where(r >= s, 0.0, fB)
+        if not update_j:
+            return fB, None, None
+        d = 3.0 * (r * r / (s * s * s)) - 6.0 * (r / (s * s)) + 3.0 / s
+        d = np.where(r <= 0, np.inf, d)
+        d = np.where(r >= s, 0.0, d)
+        der = -d / (bar * bar)
+    der = np.where(np.abs(fB) < 10e-9, 0.0, np.where(fB == np.inf, np.inf, der))
+    S = np.stack([v1[:, 1] / V, -v1[:, 0] / V, -v0[:, 1] / V, v0[:, 0] / V], axis=1)
+    return fB, der, S
+
+
+def locally_injective(cfn, N=4):
+    """locally_injectivity_check (parameterization_integ.ipp:46-63): corners a, b, c of each cut
+    face are the tails of f.half(), its next and its prev -- with face2half on the edge
+    (F[f,0], F[f,1]) that is the corner order F[f,0], F[f,1], F[f,2] of cutF -- and the face is
+    flipped when cross(b - a, c - a) < 0 in functions 0 and 1.  Returns (flipped faces, first
+    flipped face or nF)."""
+    c = np.asarray(cfn, float).reshape(-1, 3, N)
+    d1 = c[:, 1, :2] - c[:, 0, :2]
+    d2 = c[:, 2, :2] - c[:, 0, :2]
+    flipped = np.flatnonzero(d1[:, 0] * d2[:, 1] - d1[:, 1] * d2[:, 0] < 0)
+    return len(flipped), (int(flipped[0]) if len(flipped) else len(c))
+
+
 def iterative_rounding(fixedIdcs, fixedVals, singularIdcs, integerIdcs, length, Cfull, G2,
                        N, n, nF, seamless, roundSeams, F2, stats=None):
     """iter_rounding.h:33-113 (localInjectivity = false).  Returns (success, fullx, info)."""
