@@ -10,6 +10,8 @@
 // V(1,1) cycle is written as R / S / P sparse operators per level:
 //   down r_{l+1} = R r_l,  up y_l = S r_l + P y_{l+1}.
 #pragma once
+#include <cuda_fp16.h>
+
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -468,7 +470,7 @@ __device__ __forceinline__ T rcsr_row(const RDevCsr<T>& M, int row, int lane, in
 // spread over groups of M.group lanes (1..32) with a warp-uniform loop and fixed-order reduction.
 template <typename T>
 __device__ void rcsr_phase(const RDevCsr<T>& M, const T* x, const RDevCsr<T>* M2, const T* x2, T* out, T scale,
-                           const unsigned char* mask, T* xdot = nullptr, const float* phi = nullptr, int nphi = 0,
+                           const unsigned char* mask, T* xdot = nullptr, const __half* phi = nullptr, int nphi = 0,
                            const T* yc = nullptr) {
     const int stride = gridDim.x * blockDim.x;
     const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
@@ -476,7 +478,7 @@ __device__ void rcsr_phase(const RDevCsr<T>& M, const T* x, const RDevCsr<T>* M2
     // optional extra term out += sum_k phi[k n + row] yc[k] (phi column-major, yc replicated)
     auto extra = [&](int row) {
         T e = T(0);
-        for (int k = 0; k < nphi; k++) e += (T)__ldg(phi + (size_t)k * M.n + row) * yc[k];
+        for (int k = 0; k < nphi; k++) e += (T)__half2float(__ldg(phi + (size_t)k * M.n + row)) * yc[k];
         return e;
     };
     if (g == 1) {
@@ -511,7 +513,7 @@ __device__ void rcsr_phase(const RDevCsr<T>& M, const T* x, const RDevCsr<T>* M2
 // columns) the level-0 output also gets phi * yc, in the same pass.
 template <typename T>
 __device__ bool rvcycle(const RDevHierarchy<T>& H, T out_scale, const unsigned char* mask0, const GridBarrier& bar,
-                        T* rz = nullptr, const float* phi = nullptr, int nphi = 0, const T* yc = nullptr) {
+                        T* rz = nullptr, const __half* phi = nullptr, int nphi = 0, const T* yc = nullptr) {
     const int stride = gridDim.x * blockDim.x;
     const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
     for (int l = 0; l < H.nlev; l++) {

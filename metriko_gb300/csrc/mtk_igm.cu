@@ -297,14 +297,14 @@ __device__ bool igm_apply_asm(const IgmOp<T>& A, const unsigned char* __restrict
 //
 // Block partials of Phi^T r_y in fixed order: out[k * gridDim.x + blockIdx.x].
 template <typename T>
-__device__ void phi_dots_publish(const float* __restrict__ Phi, int nY, int nZ, const T* r, T* out, T* wsum) {
+__device__ void phi_dots_publish(const __half* __restrict__ Phi, int nY, int nZ, const T* r, T* out, T* wsum) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int stride = gridDim.x * blockDim.x;
     const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
     for (int k = 0; k < nZ; k++) {
         T a = T(0);
-        const float* col = Phi + (size_t)k * nY;
-        for (int j = t0; j < nY; j += stride) a += (T)__ldg(col + j) * __ldcg(r + j);
+        const __half* col = Phi + (size_t)k * nY;
+        for (int j = t0; j < nY; j += stride) a += (T)__half2float(__ldg(col + j)) * __ldcg(r + j);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
         if (lane == 0) wsum[warp * nZ + k] = a;
@@ -358,7 +358,7 @@ __global__ void __launch_bounds__(kBlock, 1) igm_pcg(IgmOp<T> A, ZProj<T> P, con
                                                  T* p, T* p2, T* q, T* partials, GridBarrier bar, double tol2,
                                                  int maxit, int mode, int* out,
                                                  const RDevHierarchy<T>* __restrict__ Hp, T mg_scale,
-                                                 const float* __restrict__ Phi) {
+                                                 const __half* __restrict__ Phi) {
     extern __shared__ unsigned char smem_raw[];
     ZSmem<T> zs;
     zs.bind(reinterpret_cast<T*>(smem_raw), A.nZ, A.nJ);
@@ -837,6 +837,16 @@ __global__ void face_residual(int nF, const int* __restrict__ cutF, const double
     publish_partials<double, 1>(red, partials);
 }
 
+// Phi rounded to FP16 (the kernels' copy); the FP32 copy keeps the rounded values, so the
+// Galerkin block built from it belongs to the basis the kernels apply.
+__global__ void phi_round_half(size_t n, float* phi, __half* phih) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const __half h = __float2half_rn(phi[i]);
+        phih[i] = h;
+        phi[i] = __half2float(h);
+    }
+}
+
 // Block partials of Phi^T v (FP64 sums): partials[k * gridDim.x + blockIdx.x], k < nZ.
 __global__ void phi_tdot(int nY, int nZ, const float* __restrict__ Phi, const float* __restrict__ v, double* partials) {
     for (int k = 0; k < nZ; k++) {
@@ -927,7 +937,8 @@ struct Igm {
     // Schur coarse space of the z block (phi_coarse): Phi column-major nY x nZ, G0 = Z^T K0 Z and
     // C0 = Z^T Z for Z = [Phi ; I] and the unscaled operator K0
     bool phi_ok = false;
-    DBuf<float> phi, qid32;
+    DBuf<float> phi, qid32;   // Phi (FP32, its values FP16-representable) while it is built
+    DBuf<__half> phih;         // Phi as the kernels read it
     std::vector<double> G0, C0;
     DBuf<float> ka_val32, cy_val32, cj_val32, bjj32;
     DBuf<double> pb64;   // second direction buffers of the PCG (double-buffered p)
@@ -1103,7 +1114,7 @@ struct Igm {
     template <typename T>
     int run_pcg(IgmOp<T> A, ZProj<T> P, const T* minv, const T* b, T* x, T* r, T* z, T* p, T* q, double tol2, int maxit,
                 int mode, size_t smem, long long* iters, double* rr_out) {
-        const float* phiP = (phi_ok && mg && mode == 0) ? phi.p : nullptr;
+        const __half* phiP = (phi_ok && mg && mode == 0) ? phih.p : nullptr;
         auto kern = igm_pcg<T>;
         MTK_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         int per_sm = 0;
@@ -1142,7 +1153,7 @@ struct Igm {
         pcg_ms += kms;
         pcg_launches++;
         pcg_bytes += (iter_bytes(sizeof(T)) + (Hp ? (sizeof(T) == 8 ? mg_bytes64 : mg_bytes32) : 0.0) +
-                      (phiP ? 8.0 * nZ * (double)nY : 0.0)) *
+                      (phiP ? 4.0 * nZ * (double)nY : 0.0)) *
                      (double)(c->h_int[1] + 1);
         if (iters) *iters += c->h_int[1];
         if (rr_out) *rr_out = reinterpret_cast<double*>(c->h_int + 4)[0];
@@ -1286,6 +1297,10 @@ struct Igm {
             if (s != MTK_OK && s != MTK_ERR_NOT_CONVERGED) { cur_scale = save_scale; return MTK_OK; }
             MTK_CUDA_TRY(cudaMemcpyAsync(phi.p + (size_t)k * nY, xk, sizeof(float) * nY, cudaMemcpyDeviceToDevice, st));
         }
+        MTK_TRY(phih.alloc((size_t)nY * nZ));
+        phi_round_half<<<stream_grid(c), kStream, 0, st>>>((size_t)nY * nZ, phi.p, phih.p);
+        c->kernels++;
+        MTK_CUDA_TRY(cudaGetLastError());
         G0.assign((size_t)nZ * nZ, 0.0);
         C0.assign((size_t)nZ * nZ, 0.0);
         const int nb = stream_grid(c);
