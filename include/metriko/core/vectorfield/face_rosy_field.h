@@ -295,21 +295,21 @@ namespace metriko {
             const int nF = m.nF;
             MatXi seams(nF, 3, 1);
             std::vector<char> visited(nF, 0);
-            std::deque<int> dq;
+            std::vector<int> queue(nF);   // FIFO: every face enters once
             for (int f0 = 0; f0 < nF; f0++) {
                 if (visited[f0]) continue;
                 visited[f0] = 1;
-                dq.push_back(f0);
-                while (!dq.empty()) {
-                    int f = dq.front();
-                    dq.pop_front();
+                size_t head = 0, tail = 0;
+                queue[tail++] = f0;
+                while (head < tail) {
+                    const int f = queue[head++];
                     for (int s = 0; s < 3; s++) {
                         int g = TT(f, s), j = TTi(f, s);
                         if (!visited[g]) {
                             visited[g] = 1;
                             seams(f, s) = 0;
                             seams(g, j) = 0;
-                            dq.push_back(g);
+                            queue[tail++] = g;
                         }
                     }
                 }

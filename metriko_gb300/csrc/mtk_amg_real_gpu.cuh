@@ -138,6 +138,60 @@ struct ProdVisit {
     }
 };
 
+// Cut-vertex stiffness row c: for the faces around c (in vf order), (b, g_a . g_b) for the
+// face's corners b, a the corner of c (the IGM free block's S, as its host assembly).
+struct StiffVisit {
+    const int *vf_ptr, *vf_face, *cutF;
+    const double* grad;
+    template <class Add>
+    __device__ void operator()(int c, Add& add) const {
+        for (int k = vf_ptr[c]; k < vf_ptr[c + 1]; k++) {
+            const int f = vf_face[k];
+            const int a = cutF[3 * f] == c ? 0 : (cutF[3 * f + 1] == c ? 1 : 2);
+            const double ga0 = grad[6 * f + 2 * a], ga1 = grad[6 * f + 2 * a + 1];
+            for (int j = 0; j < 3; j++)
+                add(cutF[3 * f + j], __dadd_rn(__dmul_rn(ga0, grad[6 * f + 2 * j]), __dmul_rn(ga1, grad[6 * f + 2 * j + 1])));
+        }
+    }
+};
+
+// Row j of 2 W_y^T S W (free columns: K_yy + delta on the diagonal; translation columns: C_yJ):
+// for the W^T entries (r = 2c + k, w1) of y_j, the stiffness row of c, the W entries of
+// 2 c' + k: (y', 2 w1 s w2) for free y' (translations: the slot -1 - tag).
+struct FreeBlockVisit {
+    const int *yt_ptr, *yt_row;
+    const double* yt_val;
+    const int *hs_ptr, *hs_col;
+    const double* hs_val;
+    const int *w_ptr, *w_tag;
+    const double* w_val;
+    double delta;
+    bool translations;
+    template <class Add>
+    __device__ void operator()(int j, Add& add) const {
+        for (int e = yt_ptr[j]; e < yt_ptr[j + 1]; e++) {
+            const int r = yt_row[e], c2 = r >> 1, kk = r & 1;
+            const double w2 = __dmul_rn(2.0, yt_val[e]);
+            for (int p = hs_ptr[c2]; p < hs_ptr[c2 + 1]; p++) {
+                const int r2 = 2 * hs_col[p] + kk;
+                const double ws = __dmul_rn(w2, hs_val[p]);
+                for (int e2 = w_ptr[r2]; e2 < w_ptr[r2 + 1]; e2++) {
+                    const int y2 = w_tag[e2];
+                    if (translations ? y2 < 0 : y2 >= 0) add(translations ? -1 - y2 : y2, __dmul_rn(ws, w_val[e2]));
+                }
+            }
+        }
+        if (!translations) add(j, delta);
+    }
+};
+
+// FP32 values of a free block without its diagonal shift delta
+static __global__ void free_block_f32(int n, const int* __restrict__ Kp, const int* __restrict__ Kc,
+                                      const double* __restrict__ Kv, double delta, float* out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        for (int q = Kp[i]; q < Kp[i + 1]; q++) out[q] = (float)(Kc[q] == i ? __dsub_rn(Kv[q], delta) : Kv[q]);
+}
+
 struct SortedAcc {
     int cols[kCapRow];
     double vals[kCapRow];
@@ -409,8 +463,11 @@ class RDevBuilder {
     // ok = false (status MTK_OK) where build_real_hierarchy would fail or a row exceeds the
     // kernels' capacity; the caller then builds on the host from A0, node and comp, which are
     // handed back unchanged.
+    // dA0 (may be null): the device copy of A0 (moved in), else A0 is uploaded
     int build(RCsr& A0, std::vector<int>& node, std::vector<int>& comp, int nnode, std::vector<DevCycleOps>& ops,
-              int& nc, std::vector<double>& Ainv, bool& ok, double omega_cap = 1.0, double alpha = 1.0) {
+              int& nc, std::vector<double>& Ainv, bool& ok, DevCsr64* dA0 = nullptr, double omega_cap = 1.0,
+              double alpha = 1.0) {
+        dA0_ = dA0;
         RLevel cur;
         std::swap(cur.A, A0);
         std::swap(cur.node, node);
@@ -425,7 +482,22 @@ class RDevBuilder {
         return st;
     }
 
-   private:
+    // capacity flag and scan total of the row builders (the free-block assembly uses them before
+    // build); failed(): a row exceeded its accumulator
+    int prepare() {
+        MTK_TRY(err_.alloc(1));
+        MTK_TRY(err_.zero(st_));
+        MTK_TRY(tot_.alloc(1));
+        return MTK_OK;
+    }
+    int failed(bool& f) {
+        int h = 0;
+        MTK_CUDA_TRY(cudaMemcpyAsync(&h, err_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
+        MTK_CUDA_TRY(cudaStreamSynchronize(st_));
+        f = h != 0;
+        return MTK_OK;
+    }
+
     int run(RLevel& cur, RLevel& lv0, RLevel*& give_back, std::vector<DevCycleOps>& ops, int& nc,
             std::vector<double>& Ainv, bool& ok, double omega_cap, double alpha) {
         ok = false;
@@ -445,7 +517,8 @@ class RDevBuilder {
         MTK_TRY(err_.zero(st_));
         MTK_TRY(tot_.alloc(1));
         DevCsr64 dA;
-        MTK_TRY(upload(cur.A, dA));
+        if (dA0_) dA = std::move(*dA0_);
+        else MTK_TRY(upload(cur.A, dA));
         int levels = 0;
         lap("upload", 0);
         while (cur.A.n > kRCoarseMax && levels < kRMaxLevels - 1) {
@@ -555,6 +628,7 @@ class RDevBuilder {
 
     mtk_ctx* c_;
     cudaStream_t st_;
+    DevCsr64* dA0_ = nullptr;
     DBuf<int> err_, cnt_;
     DBuf<long long> bsum_, tot_;
     DBuf<double> rv_, rw_, rt_, rpart_;

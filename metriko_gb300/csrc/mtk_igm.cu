@@ -977,7 +977,7 @@ struct Igm {
         return MTK_OK;
     }
 
-    int build_mg(RCsr K, std::vector<int> node, std::vector<int> comp, int nnode) {
+    int build_mg(RCsr K, std::vector<int> node, std::vector<int> comp, int nnode, DevCsr64* dK = nullptr) {
         // the Galerkin products run on the device (RDevBuilder, the same arrays as the host
         // build); the host builds when the device build declines (a row beyond its capacity)
         const auto tb0 = std::chrono::steady_clock::now();
@@ -987,7 +987,7 @@ struct Igm {
         bool dev_ok = false;
         if (!getenv("MTK_MG_HOST")) {
             RDevBuilder B(c, st);
-            MTK_TRY(B.build(K, node, comp, nnode, dops, nc, Ainv, dev_ok));
+            MTK_TRY(B.build(K, node, comp, nnode, dops, nc, Ainv, dev_ok, dK));
         }
         RHierarchy HH;
         if (!dev_ok) {
@@ -1550,99 +1550,166 @@ int igm_run(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts_in, do
         tlap = t;
     };
     if (nY > 0 && !getenv("MTK_NO_AMG")) {
-        std::vector<int> hs_ptr, hs_col;
-        std::vector<double> hs_val;
-        build_rows_parallel<double>(
-            nCut, nCut,
-            [&](int c2, auto add) {
-                for (int k = vptr[c2]; k < vptr[c2 + 1]; k++) {
-                    const int f = vface[k];
-                    const int a = d->cutF[3 * f] == c2 ? 0 : (d->cutF[3 * f + 1] == c2 ? 1 : 2);
-                    for (int j = 0; j < 3; j++)
-                        add(d->cutF[3 * f + j], h_grad[6 * f + 2 * a] * h_grad[6 * f + 2 * j] +
-                                                    h_grad[6 * f + 2 * a + 1] * h_grad[6 * f + 2 * j + 1]);
-                }
-            },
-            hs_ptr, hs_col, hs_val);
-        lap("stiffness (cut vertices)");
         const double delta = 1e-4 / (d->length * d->length);
         RCsr K;
-        K.n = nY;
-        build_rows_parallel<double>(
-            nY, nY,
-            [&](int j, auto add) {
-                for (int e = yptr[j]; e < yptr[j + 1]; e++) {
-                    const int r = yrow[e], c2 = r >> 1, kk = r & 1;
-                    const double w1 = yval[e];
-                    for (int p = hs_ptr[c2]; p < hs_ptr[c2 + 1]; p++) {
-                        const int r2 = 2 * hs_col[p] + kk;
-                        const double sv = hs_val[p];
-                        for (int e2 = d->w_ptr[r2]; e2 < d->w_ptr[r2 + 1]; e2++) {
-                            const int y2 = tag[e2];
-                            if (y2 >= 0) add(y2, 2.0 * w1 * sv * d->w_val[e2]);
-                        }
-                    }
+        DevCsr64 dK;
+        bool dev_K = false;
+        if (!getenv("MTK_MG_HOST")) {
+            // K_yy + delta I, the FP32 operator arrays and C_yJ / C_Jy assembled on the device (the
+            // arrays of the host assembly below, same rounding and order); K comes back to the host
+            // for the aggregation
+            RDevBuilder B(c, st);
+            MTK_TRY(B.prepare());
+            DevCsr64 Hs, Cy, Cj;
+            const rgpu::StiffVisit sv{S.vf_ptr.p, S.vf_face.p, S.cutF.p, S.grad.p};
+            MTK_TRY(B.two_pass(nCut, Hs, [&](int* cnt, const int* optr, int* oc, double* ov) {
+                rgpu::rows_sorted<<<B.grid(nCut), kStream, 0, st>>>(nCut, sv, cnt, optr, oc, ov, B.err_.p);
+            }));
+            const rgpu::FreeBlockVisit kv{S.yt_ptr.p, S.yt_row.p, S.yt_val.p, Hs.ptr.p, Hs.col.p, Hs.val.p,
+                                          S.w_ptr.p, S.w_tag.p, S.w_val.p, delta, false};
+            MTK_TRY(B.two_pass(nY, dK, [&](int* cnt, const int* optr, int* oc, double* ov) {
+                rgpu::rows_sorted<<<B.grid(nY), kStream, 0, st>>>(nY, kv, cnt, optr, oc, ov, B.err_.p);
+            }));
+            if (!getenv("MTK_NO_ASM")) {
+                MTK_TRY(S.ka_ptr.alloc(nY + 1));
+                MTK_TRY(S.ka_col.alloc(std::max<size_t>(dK.nnz, 1)));
+                MTK_TRY(S.ka_val32.alloc(std::max<size_t>(dK.nnz, 1)));
+                MTK_CUDA_TRY(cudaMemcpyAsync(S.ka_ptr.p, dK.ptr.p, sizeof(int) * (nY + 1), cudaMemcpyDeviceToDevice, st));
+                MTK_CUDA_TRY(cudaMemcpyAsync(S.ka_col.p, dK.col.p, sizeof(int) * dK.nnz, cudaMemcpyDeviceToDevice, st));
+                rgpu::free_block_f32<<<B.grid(nY), kStream, 0, st>>>(nY, dK.ptr.p, dK.col.p, dK.val.p, delta, S.ka_val32.p);
+                const rgpu::FreeBlockVisit cv{S.yt_ptr.p, S.yt_row.p, S.yt_val.p, Hs.ptr.p, Hs.col.p, Hs.val.p,
+                                              S.w_ptr.p, S.w_tag.p, S.w_val.p, 0.0, true};
+                MTK_TRY(B.two_pass(nY, Cy, [&](int* cnt, const int* optr, int* oc, double* ov) {
+                    rgpu::rows_sorted<<<B.grid(nY), kStream, 0, st>>>(nY, cv, cnt, optr, oc, ov, B.err_.p);
+                }));
+                MTK_TRY(B.transpose(Cy, std::max(nJ, 1), Cj, 1.0));
+                auto to32 = [&](const DevCsr64& M, DBuf<int>& ptr, DBuf<int>& col, DBuf<float>& v32) -> int {
+                    ptr = std::move(const_cast<DevCsr64&>(M).ptr);
+                    col = std::move(const_cast<DevCsr64&>(M).col);
+                    MTK_TRY(v32.alloc(std::max<size_t>(M.nnz, 1)));
+                    if (M.nnz) rgpu::to_f32_vals<<<B.grid((long long)M.nnz), kStream, 0, st>>>(M.nnz, M.val.p, v32.p);
+                    else MTK_CUDA_TRY(cudaMemsetAsync(v32.p, 0, sizeof(float), st));
+                    return MTK_OK;
+                };
+                MTK_TRY(to32(Cy, S.cy_ptr, S.cy_col, S.cy_val32));
+                MTK_TRY(to32(Cj, S.cj_ptr, S.cj_col, S.cj_val32));
+                if (Cy.nnz == 0) {   // empty coupling: one harmless entry so every array exists
+                    const int z = 0;
+                    MTK_CUDA_TRY(cudaMemcpyAsync(S.cy_col.p, &z, sizeof(int), cudaMemcpyHostToDevice, st));
+                    MTK_CUDA_TRY(cudaMemcpyAsync(S.cj_col.p, &z, sizeof(int), cudaMemcpyHostToDevice, st));
                 }
-                add(j, delta);
-            },
-            K.ptr, K.col, K.val);
-        lap("free block K");
-        // assembled operator of the FP32 inner solves: K_yy (without the multigrid's delta), the
-        // free-to-translation coupling C_yJ and its transpose
-        if (!getenv("MTK_NO_ASM")) {
-            std::vector<float> kv(K.val.size());
-#pragma omp parallel for schedule(static)
-            for (int j = 0; j < nY; j++)
-                for (int q = K.ptr[j]; q < K.ptr[j + 1]; q++)
-                    kv[q] = (float)(K.col[q] == j ? K.val[q] - delta : K.val[q]);
-            MTK_TRY(S.ka_ptr.upload(K.ptr.data(), K.ptr.size(), st));
-            MTK_TRY(S.ka_col.upload(K.col.data(), K.col.size(), st));
-            MTK_TRY(S.ka_val32.upload(kv.data(), kv.size(), st));
-            std::vector<int> cptr, ccol;
-            std::vector<double> cval;
+            }
+            MTK_CUDA_TRY(cudaGetLastError());
+            bool over = false;
+            MTK_TRY(B.failed(over));
+            if (!over) {
+                K.n = nY;
+                K.ptr.resize(nY + 1);
+                K.col.resize(dK.nnz);
+                K.val.resize(dK.nnz);
+                MTK_CUDA_TRY(cudaMemcpyAsync(K.ptr.data(), dK.ptr.p, sizeof(int) * (nY + 1), cudaMemcpyDeviceToHost, st));
+                MTK_CUDA_TRY(cudaMemcpyAsync(K.col.data(), dK.col.p, sizeof(int) * dK.nnz, cudaMemcpyDeviceToHost, st));
+                MTK_CUDA_TRY(cudaMemcpyAsync(K.val.data(), dK.val.p, sizeof(double) * dK.nnz, cudaMemcpyDeviceToHost, st));
+                MTK_CUDA_TRY(cudaStreamSynchronize(st));
+                dev_K = true;
+                if (!getenv("MTK_NO_ASM")) S.asm_ok = true;   // BJJ is uploaded once it is built below
+                lap("free block K (device) + download");
+            }
+        }
+        if (!dev_K) {
+            std::vector<int> hs_ptr, hs_col;
+            std::vector<double> hs_val;
             build_rows_parallel<double>(
-                nY, std::max(nJ, 1),
+                nCut, nCut,
+                [&](int c2, auto add) {
+                    for (int k = vptr[c2]; k < vptr[c2 + 1]; k++) {
+                        const int f = vface[k];
+                        const int a = d->cutF[3 * f] == c2 ? 0 : (d->cutF[3 * f + 1] == c2 ? 1 : 2);
+                        for (int j = 0; j < 3; j++)
+                            add(d->cutF[3 * f + j], h_grad[6 * f + 2 * a] * h_grad[6 * f + 2 * j] +
+                                                        h_grad[6 * f + 2 * a + 1] * h_grad[6 * f + 2 * j + 1]);
+                    }
+                },
+                hs_ptr, hs_col, hs_val);
+            lap("stiffness (cut vertices)");
+            K = RCsr();
+            K.n = nY;
+            build_rows_parallel<double>(
+                nY, nY,
                 [&](int j, auto add) {
                     for (int e = yptr[j]; e < yptr[j + 1]; e++) {
                         const int r = yrow[e], c2 = r >> 1, kk = r & 1;
                         const double w1 = yval[e];
-                        for (int q = hs_ptr[c2]; q < hs_ptr[c2 + 1]; q++) {
-                            const int r2 = 2 * hs_col[q] + kk;
-                            const double sv = hs_val[q];
-                            for (int e2 = d->w_ptr[r2]; e2 < d->w_ptr[r2 + 1]; e2++)
-                                if (tag[e2] < 0) add(-1 - tag[e2], 2.0 * w1 * sv * d->w_val[e2]);
+                        for (int p = hs_ptr[c2]; p < hs_ptr[c2 + 1]; p++) {
+                            const int r2 = 2 * hs_col[p] + kk;
+                            const double sv = hs_val[p];
+                            for (int e2 = d->w_ptr[r2]; e2 < d->w_ptr[r2 + 1]; e2++) {
+                                const int y2 = tag[e2];
+                                if (y2 >= 0) add(y2, 2.0 * w1 * sv * d->w_val[e2]);
+                            }
                         }
                     }
+                    add(j, delta);
                 },
-                cptr, ccol, cval);
-            std::vector<float> cv32(cval.begin(), cval.end());
-            std::vector<int> tptr(std::max(nJ, 1) + 1, 0), tcol(ccol.size());
-            std::vector<float> tval(ccol.size());
-            for (int c2 : ccol) tptr[c2 + 1]++;
-            for (int a2 = 0; a2 < std::max(nJ, 1); a2++) tptr[a2 + 1] += tptr[a2];
-            {
-                std::vector<int> fill(tptr.begin(), tptr.end() - 1);
+                K.ptr, K.col, K.val);
+            lap("free block K");
+            // assembled operator of the FP32 inner solves: K_yy (without the multigrid's delta), the
+            // free-to-translation coupling C_yJ and its transpose
+            if (!getenv("MTK_NO_ASM")) {
+                std::vector<float> kv(K.val.size());
+    #pragma omp parallel for schedule(static)
                 for (int j = 0; j < nY; j++)
-                    for (int q = cptr[j]; q < cptr[j + 1]; q++) {
-                        const int t = fill[ccol[q]]++;
-                        tcol[t] = j;
-                        tval[t] = (float)cval[q];
-                    }
+                    for (int q = K.ptr[j]; q < K.ptr[j + 1]; q++)
+                        kv[q] = (float)(K.col[q] == j ? K.val[q] - delta : K.val[q]);
+                MTK_TRY(S.ka_ptr.upload(K.ptr.data(), K.ptr.size(), st));
+                MTK_TRY(S.ka_col.upload(K.col.data(), K.col.size(), st));
+                MTK_TRY(S.ka_val32.upload(kv.data(), kv.size(), st));
+                std::vector<int> cptr, ccol;
+                std::vector<double> cval;
+                build_rows_parallel<double>(
+                    nY, std::max(nJ, 1),
+                    [&](int j, auto add) {
+                        for (int e = yptr[j]; e < yptr[j + 1]; e++) {
+                            const int r = yrow[e], c2 = r >> 1, kk = r & 1;
+                            const double w1 = yval[e];
+                            for (int q = hs_ptr[c2]; q < hs_ptr[c2 + 1]; q++) {
+                                const int r2 = 2 * hs_col[q] + kk;
+                                const double sv = hs_val[q];
+                                for (int e2 = d->w_ptr[r2]; e2 < d->w_ptr[r2 + 1]; e2++)
+                                    if (tag[e2] < 0) add(-1 - tag[e2], 2.0 * w1 * sv * d->w_val[e2]);
+                            }
+                        }
+                    },
+                    cptr, ccol, cval);
+                std::vector<float> cv32(cval.begin(), cval.end());
+                std::vector<int> tptr(std::max(nJ, 1) + 1, 0), tcol(ccol.size());
+                std::vector<float> tval(ccol.size());
+                for (int c2 : ccol) tptr[c2 + 1]++;
+                for (int a2 = 0; a2 < std::max(nJ, 1); a2++) tptr[a2 + 1] += tptr[a2];
+                {
+                    std::vector<int> fill(tptr.begin(), tptr.end() - 1);
+                    for (int j = 0; j < nY; j++)
+                        for (int q = cptr[j]; q < cptr[j + 1]; q++) {
+                            const int t = fill[ccol[q]]++;
+                            tcol[t] = j;
+                            tval[t] = (float)cval[q];
+                        }
+                }
+                if (ccol.empty()) { ccol.push_back(0); cv32.push_back(0.f); tcol.push_back(0); tval.push_back(0.f); }
+                MTK_TRY(S.cy_ptr.upload(cptr.data(), cptr.size(), st));
+                MTK_TRY(S.cy_col.upload(ccol.data(), ccol.size(), st));
+                MTK_TRY(S.cy_val32.upload(cv32.data(), cv32.size(), st));
+                MTK_TRY(S.cj_ptr.upload(tptr.data(), tptr.size(), st));
+                MTK_TRY(S.cj_col.upload(tcol.data(), tcol.size(), st));
+                MTK_TRY(S.cj_val32.upload(tval.data(), tval.size(), st));
+                MTK_CUDA_TRY(cudaStreamSynchronize(st));
+                S.asm_ok = true;   // BJJ is uploaded once it is built below
+                lap("assembled operator + upload");
             }
-            if (ccol.empty()) { ccol.push_back(0); cv32.push_back(0.f); tcol.push_back(0); tval.push_back(0.f); }
-            MTK_TRY(S.cy_ptr.upload(cptr.data(), cptr.size(), st));
-            MTK_TRY(S.cy_col.upload(ccol.data(), ccol.size(), st));
-            MTK_TRY(S.cy_val32.upload(cv32.data(), cv32.size(), st));
-            MTK_TRY(S.cj_ptr.upload(tptr.data(), tptr.size(), st));
-            MTK_TRY(S.cj_col.upload(tcol.data(), tcol.size(), st));
-            MTK_TRY(S.cj_val32.upload(tval.data(), tval.size(), st));
-            MTK_CUDA_TRY(cudaStreamSynchronize(st));
-            S.asm_ok = true;   // BJJ is uploaded once it is built below
-            lap("assembled operator + upload");
         }
         std::vector<int> node(nY), comp(nY);
         for (int j = 0; j < nY; j++) { node[j] = y2full[j] / 2; comp[j] = y2full[j] % 2; }
-        MTK_TRY(S.build_mg(std::move(K), std::move(node), std::move(comp), nFull / 2));
+        MTK_TRY(S.build_mg(std::move(K), std::move(node), std::move(comp), nFull / 2, dev_K ? &dK : nullptr));
         lap("hierarchy + upload");
     }
     if (Igm::debug())
