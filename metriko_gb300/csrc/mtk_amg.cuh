@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <cmath>
 #include <complex>
+#include <memory>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -201,18 +202,22 @@ inline int aggregate_level(HostLevel& L) {
     // with a = A(v, parent).  Each value depends on its parent's only, so the forest is resolved
     // in parallel rounds (round r computes the nodes whose parent was resolved before round r):
     // the same values as any sequential order.
-    std::vector<std::complex<double>> t(n, std::complex<double>(0, 0));
+    // (every entry of t and of the round arrays is written before it is read: no serial zeroing)
+    std::unique_ptr<std::complex<double>[]> t(new std::complex<double>[n]);
     std::vector<int> cnt(na, 0);
     for (int i = 0; i < n; i++) cnt[L.agg[i]]++;
     {
-        std::vector<int> rnd(n), rnd_next;   // round in which a node was resolved (-1: not yet)
+        std::unique_ptr<int[]> rnd_a(new int[n]), rnd_b(new int[n]);   // resolving round (-1: not yet)
+        int* rnd = rnd_a.get();
+        int* rnd_next = rnd_b.get();
 #pragma omp parallel for schedule(static)
         for (int i = 0; i < n; i++) {
             rnd[i] = parent[i] < 0 ? 0 : -1;
             if (parent[i] < 0) t[i] = 1.0;
         }
         for (int r = 1;; r++) {
-            rnd_next = rnd;
+#pragma omp parallel for schedule(static)
+            for (int i = 0; i < n; i++) rnd_next[i] = rnd[i];
             int changed = 0;
 #pragma omp parallel for schedule(static) reduction(+ : changed)
             for (int v = 0; v < n; v++) {
@@ -226,7 +231,7 @@ inline int aggregate_level(HostLevel& L) {
                 rnd_next[v] = r;
                 changed++;
             }
-            rnd.swap(rnd_next);
+            std::swap(rnd, rnd_next);
             if (!changed) break;
         }
     }
