@@ -698,31 +698,21 @@ constexpr int kRing = 12;
 // partials for j < cnt: [Re, Im] of u^H (L V_j) and of V_j^H b
 struct RingPtrs { const double2* V[kRing]; const double2* LV[kRing]; int cnt; };
 
-// One pass over the rows for all ring vectors (u and b read once); per (j, thread) the sums run
-// over the thread's rows in grid-stride order, as one pass per vector would.
 __global__ void gram_row(int n, RingPtrs R, const double2* __restrict__ u, const double2* __restrict__ b,
                          double* partials) {
-    double red[4 * kRing];
-#pragma unroll
-    for (int k = 0; k < 4 * kRing; k++) red[k] = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const double2 ui = u[i], bi = b[i];
-#pragma unroll
-        for (int j = 0; j < kRing; j++) {
-            if (j < R.cnt) {
-                const double2 li = R.LV[j][i], vi = R.V[j][i];
-                red[4 * j] += ui.x * li.x + ui.y * li.y;   // conj(u) * Lv
-                red[4 * j + 1] += ui.x * li.y - ui.y * li.x;
-                red[4 * j + 2] += vi.x * bi.x + vi.y * bi.y;   // conj(v) * b
-                red[4 * j + 3] += vi.x * bi.y - vi.y * bi.x;
-            }
+    for (int j = 0; j < R.cnt; j++) {
+        double red[4] = {0, 0, 0, 0};
+        const double2* Vj = R.V[j];
+        const double2* Lj = R.LV[j];
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+            double2 ui = u[i], li = Lj[i], vi = Vj[i], bi = b[i];
+            red[0] += ui.x * li.x + ui.y * li.y;   // conj(u) * Lv
+            red[1] += ui.x * li.y - ui.y * li.x;
+            red[2] += vi.x * bi.x + vi.y * bi.y;   // conj(v) * b
+            red[3] += vi.x * bi.y - vi.y * bi.x;
         }
-    }
-    block_sum<double, 4 * kRing>(red);
-    if (threadIdx.x == 0) {
-#pragma unroll
-        for (int k = 0; k < 4 * kRing; k++)
-            if (k < 4 * R.cnt) partials[k * gridDim.x + blockIdx.x] = red[k];
+        double* pj = partials + 4 * j * gridDim.x;
+        publish_partials<double, 4>(red, pj);
     }
 }
 
