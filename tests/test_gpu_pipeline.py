@@ -61,10 +61,11 @@ def test_pipeline_deterministic(gpu_ctx):
     assert list(a["fix_order"]) == list(b["fix_order"])
 
 
-@pytest.mark.parametrize("name", ["ico4_noise", "ico6_sh8"])
+@pytest.mark.parametrize("name", ["ico4_noise", "ico6_sh8", "torus_64x32"])
 def test_igm_multigrid_device_build_matches_host(gpu_ctx, monkeypatch, name):
-    """The IGM multigrid's Galerkin products built on the device (the default) give the same
-    arrays as the host build, so the whole pipeline is bit-identical either way."""
+    """The multigrid set-up on the device (the default: the IGM free block, both hierarchies'
+    products) gives the same arrays as the host set-up, so the whole pipeline is bit-identical
+    either way."""
     V, F, ratio, rs = meshgen.workload(name)
     opts = M.solve_opts("mixed", tol=1e-8)
     a = M.pipeline(gpu_ctx, V, F, ratio=ratio, round_seams=rs, opts=opts)
