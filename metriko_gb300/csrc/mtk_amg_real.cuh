@@ -64,7 +64,8 @@ inline int raggregate(RLevel& L, std::vector<int>& cnode, std::vector<int>& ccom
     const RCsr& A = L.A;
     const int n = A.n, nn = L.nnode;
     std::vector<int> nd0(nn, -1), nd1(nn, -1);
-    for (int d = 0; d < n; d++) (L.comp[d] == 0 ? nd0 : nd1)[L.node[d]] = d;
+#pragma omp parallel for schedule(static)
+    for (int d = 0; d < n; d++) (L.comp[d] == 0 ? nd0 : nd1)[L.node[d]] = d;   // (node, comp) -> dof is one to one
     auto paired = [&](int v) { return nd0[v] >= 0 && nd1[v] >= 0; };
     // identity-coupled node neighbours (the 2x2 block between the two nodes is a multiple of I)
     std::vector<int> nptr(nn + 1, 0), nadj;
@@ -79,11 +80,14 @@ inline int raggregate(RLevel& L, std::vector<int>& cnode, std::vector<int>& ccom
             if (sm == 0) return false;
             return !(std::fabs(uv) + std::fabs(vu) > 1e-9 * sm || std::fabs(uu - vv) > 1e-9 * sm);
         };
+        // one test per entry of the comp-0 rows (flags), then counts and the list from the flags
+        std::vector<unsigned char> flag(A.col.size(), 0);
 #pragma omp parallel for schedule(static)
         for (int v = 0; v < nn; v++) {
             int cnt = 0;
             if (paired(v))
-                for (int p = A.ptr[nd0[v]]; p < A.ptr[nd0[v] + 1]; p++) cnt += coupled(v, p) ? 1 : 0;
+                for (int p = A.ptr[nd0[v]]; p < A.ptr[nd0[v] + 1]; p++)
+                    if (coupled(v, p)) { flag[p] = 1; cnt++; }
             nptr[v + 1] = cnt;
         }
         for (int v = 0; v < nn; v++) nptr[v + 1] += nptr[v];
@@ -93,7 +97,7 @@ inline int raggregate(RLevel& L, std::vector<int>& cnode, std::vector<int>& ccom
             if (!paired(v)) continue;
             int q = nptr[v];
             for (int p = A.ptr[nd0[v]]; p < A.ptr[nd0[v] + 1]; p++)
-                if (coupled(v, p)) nadj[q++] = L.node[A.col[p]];
+                if (flag[p]) nadj[q++] = L.node[A.col[p]];
         }
     }
     // visiting order: breadth-first over the identity-coupled graph, so that roots are packed

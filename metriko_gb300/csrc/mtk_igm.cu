@@ -1583,9 +1583,9 @@ int igm_run(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts_in, do
                     rgpu::rows_sorted<<<B.grid(nY), kStream, 0, st>>>(nY, cv, cnt, optr, oc, ov, B.err_.p);
                 }));
                 MTK_TRY(B.transpose(Cy, std::max(nJ, 1), Cj, 1.0));
-                auto to32 = [&](const DevCsr64& M, DBuf<int>& ptr, DBuf<int>& col, DBuf<float>& v32) -> int {
-                    ptr = std::move(const_cast<DevCsr64&>(M).ptr);
-                    col = std::move(const_cast<DevCsr64&>(M).col);
+                auto to32 = [&](DevCsr64& M, DBuf<int>& ptr, DBuf<int>& col, DBuf<float>& v32) -> int {
+                    ptr = std::move(M.ptr);
+                    col = std::move(M.col);
                     MTK_TRY(v32.alloc(std::max<size_t>(M.nnz, 1)));
                     if (M.nnz) rgpu::to_f32_vals<<<B.grid((long long)M.nnz), kStream, 0, st>>>(M.nnz, M.val.p, v32.p);
                     else MTK_CUDA_TRY(cudaMemsetAsync(v32.p, 0, sizeof(float), st));
