@@ -683,6 +683,21 @@ __device__ __forceinline__ double left_value(int i, const int* __restrict__ full
     return X;
 }
 
+// X(full) of the fixed variables (the post-rounding check): a free variable's value, or a
+// translation's USmall row times the z block (summed in the host's order).
+__global__ void fixed_values(int nfix, const int* __restrict__ fixed, const int* __restrict__ full2y,
+                             const int* __restrict__ full2j, int nY, int nZ, const double* __restrict__ Us,
+                             const double* __restrict__ xs, double* out) {
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nfix; q += gridDim.x * blockDim.x) {
+        const int full = fixed[q], y = full2y[full];
+        if (y >= 0) { out[q] = xs[y]; continue; }
+        const int sl = full2j[full];
+        double t = 0.0;
+        for (int j = 0; j < nZ; j++) t = __dadd_rn(t, __dmul_rn(Us[(size_t)sl * nZ + j], xs[nY + j]));
+        out[q] = t;
+    }
+}
+
 __global__ void round_argmin(int nLeft, const int* __restrict__ left, const int* __restrict__ full2y,
                              const int* __restrict__ full2j, int nY, int nZ, const double* __restrict__ Us,
                              const double* __restrict__ xs, double* out) {
@@ -1878,21 +1893,10 @@ int igm_run(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts_in, do
         MTK_CUDA_TRY(cudaStreamSynchronize(st));
         return MTK_OK;
     };
-    auto read_full = [&](int full) -> double {
-        int y = S.full2y[full];
-        std::vector<double> v(std::max(nZ, 1));
-        if (y >= 0) {
-            cudaMemcpyAsync(v.data(), S.xs.p + y, sizeof(double), cudaMemcpyDeviceToHost, st);
-            cudaStreamSynchronize(st);
-            return v[0];
-        }
-        cudaMemcpyAsync(v.data(), S.xs.p + S.nY, sizeof(double) * nZ, cudaMemcpyDeviceToHost, st);
-        cudaStreamSynchronize(st);
-        int s = S.full2j[full];
-        double t = 0;
-        for (int j = 0; j < nZ; j++) t += S.USmall[(size_t)s * nZ + j] * v[j];
-        return t;
-    };
+    DBuf<int> fixd;      // fixed full indices of the post-rounding check
+    DBuf<double> fixv;   // their values
+    MTK_TRY(fixd.alloc(nLeftCap));
+    MTK_TRY(fixv.alloc(nLeftCap));
 
     mtk_stats local{};
     mtk_stats* stt = stats ? stats : &local;
@@ -2090,10 +2094,16 @@ int igm_run(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts_in, do
         stt->ms_rounding += ms;
         // ---- post_checking: every fixed value within 1e-6 of an integer
         double worst = 0;
-        for (int q = 0; q < std::min(nfix, nLeftCap); q++) {
-            if (!fix_order) break;
-            double v = read_full(fix_order[q]);
-            worst = std::max(worst, std::fabs(v - std::round(v)));
+        const int nchk = fix_order ? std::min(nfix, nLeftCap) : 0;
+        if (nchk > 0) {   // all fixed values in one kernel and one copy
+            MTK_CUDA_TRY(cudaMemcpyAsync(fixd.p, fix_order, sizeof(int) * nchk, cudaMemcpyHostToDevice, st));
+            fixed_values<<<G, kStream, 0, st>>>(nchk, fixd.p, S.d_full2y.p, S.d_full2j.p, nY, nZ, S.Us.p, S.xs.p, fixv.p);
+            c->kernels++;
+            MTK_CUDA_TRY(cudaGetLastError());
+            std::vector<double> hv(nchk);
+            MTK_CUDA_TRY(cudaMemcpyAsync(hv.data(), fixv.p, sizeof(double) * nchk, cudaMemcpyDeviceToHost, st));
+            MTK_CUDA_TRY(cudaStreamSynchronize(st));
+            for (double v : hv) worst = std::max(worst, std::fabs(v - std::round(v)));
         }
         if (worst > 10e-7) { status = MTK_ERR_ROUNDING; break; }
     }
