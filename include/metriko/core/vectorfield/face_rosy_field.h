@@ -446,9 +446,10 @@ namespace metriko {
                 continue;
             }
             // unit-weight Dijkstra with pops ordered by (distance, id), run as a breadth-first
-            // search whose levels are visited in ascending id: the same pop order, and every vertex
-            // keeps as predecessor the first popped neighbour that reached it (the order in which
-            // a vertex lists its neighbours does not matter)
+            // search by levels: a vertex's predecessor is the first popped neighbour that reached
+            // it, i.e. its smallest-id neighbour in the previous level, and the search ends at the
+            // smallest-id cut vertex of the first level that holds one (the order in which a level
+            // is expanded does not matter, so levels are not sorted)
             for (int v : touched) { dist[v] = -1; prev[v] = -1; }
             touched.clear();
             dist[src] = 0;
@@ -456,19 +457,22 @@ namespace metriko {
             std::vector<int> level{src}, nlevel;
             int found = -1;
             for (int d = 0; !level.empty() && found < 0; d++) {
-                std::sort(level.begin(), level.end());
+                for (int u : level)
+                    if (in_cut[u] && (found < 0 || u < found)) found = u;
+                if (found >= 0) break;
                 nlevel.clear();
-                for (int u : level) {
-                    if (in_cut[u]) { found = u; break; }
+                for (int u : level)
                     for (int k = vptr[u]; k < vptr[u + 1]; k++) {
                         const int w = vv[k];
-                        if (dist[w] >= 0) continue;
-                        dist[w] = d + 1;
-                        prev[w] = u;
-                        touched.push_back(w);
-                        nlevel.push_back(w);
+                        if (dist[w] < 0) {
+                            dist[w] = d + 1;
+                            prev[w] = u;
+                            touched.push_back(w);
+                            nlevel.push_back(w);
+                        } else if (dist[w] == d + 1 && u < prev[w]) {
+                            prev[w] = u;
+                        }
                     }
-                }
                 level.swap(nlevel);
             }
             std::vector<int> path;
