@@ -235,25 +235,50 @@ namespace metriko {
             o.setFromTriplets(t.begin(), t.end());
             return o;
         }
+        // Rows formed independently (a count pass, then a fill pass): each entry is 0 plus its
+        // products in visit order, columns ascending -- the same arrays for any thread count.
         Sprs operator*(const Sprs& B) const {
             if (nc != B.nr) throw std::invalid_argument("sparse product: size mismatch");
             Sprs C(nr, B.nc);
-            std::vector<T> acc(B.nc, T(0));
-            std::vector<char> used(B.nc, 0);
-            std::vector<int> cols;
-            for (int i = 0; i < nr; i++) {
-                cols.clear();
+            auto row = [&](int i, std::vector<std::pair<int, T>>& e) {
+                e.clear();
                 for (int p = ptr[i]; p < ptr[i + 1]; p++) {
-                    int k = idx[p];
-                    for (int q = B.ptr[k]; q < B.ptr[k + 1]; q++) {
-                        int j = B.idx[q];
-                        if (!used[j]) { used[j] = 1; cols.push_back(j); acc[j] = T(0); }
-                        acc[j] += val[p] * B.val[q];
+                    const int k = idx[p];
+                    for (int q = B.ptr[k]; q < B.ptr[k + 1]; q++) e.emplace_back(B.idx[q], val[p] * B.val[q]);
+                }
+                for (size_t k = 1; k < e.size(); k++) {   // stable insertion sort (rows are short)
+                    const auto x = e[k];
+                    size_t j = k;
+                    while (j > 0 && e[j - 1].first > x.first) { e[j] = e[j - 1]; j--; }
+                    e[j] = x;
+                }
+            };
+#pragma omp parallel
+            {
+                std::vector<std::pair<int, T>> e;
+#pragma omp for schedule(static)
+                for (int i = 0; i < nr; i++) {
+                    row(i, e);
+                    int cnt = 0;
+                    for (size_t k = 0; k < e.size(); k++) cnt += (k == 0 || e[k].first != e[k - 1].first) ? 1 : 0;
+                    C.ptr[i + 1] = cnt;
+                }
+            }
+            for (int i = 0; i < nr; i++) C.ptr[i + 1] += C.ptr[i];
+            C.idx.resize(C.ptr[nr]);
+            C.val.resize(C.ptr[nr]);
+#pragma omp parallel
+            {
+                std::vector<std::pair<int, T>> e;
+#pragma omp for schedule(static)
+                for (int i = 0; i < nr; i++) {
+                    row(i, e);
+                    int o = C.ptr[i] - 1;
+                    for (size_t k = 0; k < e.size(); k++) {
+                        if (k == 0 || e[k].first != e[k - 1].first) { o++; C.idx[o] = e[k].first; C.val[o] = T(0); }
+                        C.val[o] += e[k].second;
                     }
                 }
-                std::sort(cols.begin(), cols.end());
-                for (int j : cols) { C.idx.push_back(j); C.val.push_back(acc[j]); used[j] = 0; }
-                C.ptr[i + 1] = static_cast<int>(C.idx.size());
             }
             return C;
         }

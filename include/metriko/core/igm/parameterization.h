@@ -393,16 +393,21 @@ namespace metriko {
         nZ = USmall.cols();
 
         // ---- target field (integ.ipp:30-43) and grid length (:70)
-        double norm = 0;
+        // the per-vector lengths in parallel, their sum in the serial order
+        std::vector<double> vlen(size_t(N) * cut.nF);
+        METRIKO_PARALLEL_FOR
         for (int f = 0; f < cut.nF; f++)
             for (int j = 0; j < N; j++) {
                 double s = 0;
                 for (int k = 0; k < 3; k++) s += ext(f, 3 * j + k) * ext(f, 3 * j + k);
-                norm += std::sqrt(s);
+                vlen[size_t(N) * f + j] = std::sqrt(s);
             }
+        double norm = 0;
+        for (double v : vlen) norm += v;
         norm /= double(N) * cut.nF;
         std::vector<double>& F2 = sys.F2;
         F2.assign(2 * size_t(N) * cut.nF, 0.0);
+        METRIKO_PARALLEL_FOR
         for (int f = 0; f < cut.nF; f++)
             for (int i = 0; i < N; i++) {
                 double sx = 0, sy = 0;
