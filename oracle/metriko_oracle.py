@@ -917,12 +917,101 @@ def lm_solve(st, max_iter=100, func_tol=1e-9, foo_tol=1e-9, stats=None):
             return False, x
 
 
+def _damped(J, lam):
+    """DiagonalDamping's dampJ (levenberg_marquardt.h:13-37): J with rows sqrt(lam sum_rows J^2)
+    on the diagonal, so dampJ^T dampJ = J^T J + lam diag(J^T J)."""
+    d = lam * np.asarray(J.multiply(J).sum(axis=0)).ravel()
+    return sp.vstack([J, sp.diags(np.sqrt(d))]).tocsr()
+
+
+def lm_solve_damped(st, lam, max_iter=100, func_tol=1e-9, foo_tol=1e-9, stats=None):
+    """levenberg_marquardt.h:140-231 with DiagonalDamping(lam) (levenberg_marquardt.h:13-76),
+    verbose = false: the normal matrix is dampJ^T dampJ; after each step the energies at prevx
+    and prevx + direction decide lam /= 10 (progress to a finite energy) or lam *= 10, and dampJ is
+    rebuilt from the Jacobian at the new iterate.  A factorisation failure (non-finite entries:
+    an infinite barrier derivative) ends the solve as in the reference ("Solver Failed to
+    factorize"); the iterate returned is then the last one.  Returns (flag, x, lam)."""
+    ls = _LLT()
+    prevx = st.initial_solution().copy()
+    E, J = st.objective_jacobian(prevx, True)
+    dampJ = _damped(J, lam)
+    x = prevx.copy()
+    it = 0
+
+    def energy(v):
+        e = st.objective_jacobian(v, False)[0]
+        with np.errstate(over="ignore", invalid="ignore"):
+            return float(e @ e)
+
+    while True:
+        with np.errstate(over="ignore", invalid="ignore"):
+            rhs = -(J.T @ E)
+        foo = np.abs(rhs).max() if rhs.size else 0.0
+        if foo < foo_tol:
+            x = prevx.copy()
+        N_ = (dampJ.T @ dampJ).tocsc()
+        if not np.all(np.isfinite(N_.data)):
+            return False, x, lam
+        try:
+            ls.factorize(N_)
+        except RuntimeError:
+            return False, x, lam
+        if stats is not None:
+            stats["factorizations"] = stats.get("factorizations", 0) + 1
+        d = ls.solve(rhs)
+        if np.linalg.norm(d) < func_tol:
+            return True, prevx.copy(), lam
+        e_prev, e_new = energy(prevx), energy(prevx + d)
+        if e_prev > e_new:
+            x = prevx + d
+            if abs(e_prev - e_new) < func_tol:
+                return False, x, lam
+        else:
+            x = prevx.copy()
+        E, J = st.objective_jacobian(x, True)
+        # DiagonalDamping::update: the energies at prevx and prevx + direction again
+        u_prev, u_new = energy(prevx), energy(prevx + d)
+        lam = lam / 10.0 if (u_prev > u_new and u_new != np.inf) else lam * 10.0
+        dampJ = _damped(J, lam)
+        if st.post_iteration(x):
+            return True, x, lam
+        it += 1
+        prevx = x.copy()
+        if it > max_iter:
+            return False, x, lam
+
+
+def _barrier_rows(intrinsic_field, field, N, update_j, wE, wJ, G):
+    """Barrier energy rows and Jacobian of Integration::compute_jacobian
+    (iter_rounding_common.h:63-88): E rows fBarrier * wE; J rows diag(barDer) image(field) G * wJ,
+    G mapping the unknowns to the field entries (2 N per face)."""
+    fB, der, S = injective_barrier_update(intrinsic_field, field, N, update_j)
+    Eb = fB * wE
+    if not update_j:
+        return Eb, None
+    nr = len(fB)
+    k = np.arange(nr)
+    i, j = k // N, k % N
+    cols = np.stack([2 * N * i + 2 * j, 2 * N * i + 2 * j + 1, 2 * N * i + 2 * ((j + 1) % N),
+                     2 * N * i + 2 * ((j + 1) % N) + 1], axis=1)
+    image = sp.csr_matrix((S.ravel(), (np.repeat(k, 4), cols.ravel())), shape=(nr, len(field)))
+    with np.errstate(invalid="ignore"):
+        Jb = (sp.diags(der) @ image @ G * wJ).tocsr()
+    return Eb, Jb
+
+
 class NaiveIntegration:
-    """iter_rounding_init.h:16-233 (localInjectivity = false)."""
+    """iter_rounding_init.h:16-233.  With local_injectivity the energy gets the barrier rows
+    (weight wBarrier = 1e-4) whose Jacobian the reference scales by wInteg * wClose instead
+    (iter_rounding_common.h:77-79), and the LM stops at the first locally injective map
+    (post_iteration = locally_injectivity_check on the parameterization, integ.ipp:46-63)."""
+    wBarrier = 1e-4
     wInteg, wConst, wClose = 10e3, 10e3, 1.0
 
-    def __init__(self, G2, Cfull, F2, fixedIdcs, fixedVals, length, nF, N, n):
+    def __init__(self, G2, Cfull, F2, fixedIdcs, fixedVals, length, nF, N, n, local_injectivity=False,
+                 fullx2N=None, cutF=None):
         self.G2, self.F2, self.length = G2, F2, length
+        self.N, self.local_inj, self.fullx2N, self.cutF = N, local_injectivity, fullx2N, cutF
         self.fixedIdcs, self.fixedVals = np.asarray(fixedIdcs), np.asarray(fixedVals, float)
         self.UFull, self.nonpart, self.uniqueJ, self.USmall = build_ufull(Cfull)
         UFull = self.UFull
@@ -950,12 +1039,18 @@ class NaiveIntegration:
                           shape=(len(self.fixedIdcs), nx + l1))
         self.J = sp.vstack([gI @ self.UExt * self.wInteg, gC @ self.UExt * self.wClose,
                             S @ self.UExt * self.wConst]).tocsr()
+        self.gClose = (gC @ self.UExt * self.wClose).tocsr()
 
     def initial_solution(self):
         return self.XF_Small
 
     def post_iteration(self, x):
-        return False
+        if not self.local_inj:
+            return False
+        X = (self.UExt @ x)[:self.nfull]
+        nfn = (self.fullx2N @ X).reshape(-1, self.N)
+        cfn = np.concatenate([nfn[self.cutF[:, j]] for j in range(3)], axis=1)
+        return locally_injective(cfn, self.N)[0] == 0
 
     def objective_jacobian(self, xf_, updateJ):
         xf = self.UExt @ xf_
@@ -965,7 +1060,10 @@ class NaiveIntegration:
         fC = f - self.F2
         fK = x[self.fixedIdcs] - self.fixedVals
         E = np.concatenate([fI * self.wInteg, fC * self.wClose, fK * self.wConst])
-        return E, self.J
+        if not self.local_inj:
+            return E, self.J
+        Eb, Jb = _barrier_rows(self.F2, f, self.N, updateJ, self.wBarrier, self.wInteg, self.gClose)
+        return np.concatenate([E, Eb]), (sp.vstack([self.J, Jb]).tocsr() if updateJ else self.J)
 
 
 class SeamlessIntegration:
@@ -973,6 +1071,7 @@ class SeamlessIntegration:
     wInteg, wConst, wClose = 1.0, 10e4, 0.01
 
     def __init__(self, ni: NaiveIntegration, xInit, F2, integerIdcs, singularIdcs, roundSeams):
+        self.N, self.local_inj, self.intrinsic, self.wBarrier = ni.N, ni.local_inj, ni.F2, ni.wBarrier
         self.UFull = ni.UFull
         self.F2 = F2
         self.X2F = (ni.G2 @ ni.UFull * ni.length).tocsr()
@@ -1031,7 +1130,13 @@ class SeamlessIntegration:
         fI = field - self.F2
         fC = xs - self.xPrev
         fK = X[self.fixedIdcs] - np.asarray(self.fixedVals, float)
-        return np.concatenate([fI * self.wInteg, fC * self.wClose, fK * self.wConst]), self.J
+        E = np.concatenate([fI * self.wInteg, fC * self.wClose, fK * self.wConst])
+        if not self.local_inj:
+            return E, self.J
+        # the barrier of the SI loop: intrinsic field of the NI (the InjectiveBarrier's V), on
+        # the current field X2F xs, Jacobian scaled by wBarrier (iter_rounding_common.h:77-78)
+        Eb, Jb = _barrier_rows(self.intrinsic, field, self.N, updateJ, self.wBarrier, self.wBarrier, self.X2F)
+        return np.concatenate([E, Eb]), (sp.vstack([self.J, Jb]).tocsr() if updateJ else self.J)
 
     def post_checking(self, x):
         X = self.UFull @ x
@@ -1086,18 +1191,26 @@ def locally_injective(cfn, N=4):
 
 
 def iterative_rounding(fixedIdcs, fixedVals, singularIdcs, integerIdcs, length, Cfull, G2,
-                       N, n, nF, seamless, roundSeams, F2, stats=None):
-    """iter_rounding.h:33-113 (localInjectivity = false).  Returns (success, fullx, info)."""
+                       N, n, nF, seamless, roundSeams, F2, stats=None, local_injectivity=False, fullx2N=None,
+                       cutF=None):
+    """iter_rounding.h:33-113.  Returns (success, fullx, info).  local_injectivity: the NI and
+    SI solves run with DiagonalDamping(0.01) and the barrier rows (needs fullx2N and cutF for
+    the NI stop)."""
     stats = {} if stats is None else stats
-    ni = NaiveIntegration(G2, Cfull, F2, fixedIdcs, fixedVals, length, nF, N, n)
+    ni = NaiveIntegration(G2, Cfull, F2, fixedIdcs, fixedVals, length, nF, N, n, local_injectivity, fullx2N, cutF)
     info = dict(ni=ni, x0=ni.x0.copy())
-    if not seamless:
+    if not seamless and not local_injectivity:
         return True, ni.x0.copy(), info
-    _, xlm = lm_solve(ni, stats=stats)
+    if local_injectivity:
+        _, xlm, _ = lm_solve_damped(ni, 0.01, stats=stats)
+    else:
+        _, xlm = lm_solve(ni, stats=stats)
     fullx = (ni.UExt @ xlm)[:ni.nfull]
     X_ = xlm[:ni.UFull.shape[1]]
     F2_ = (ni.UExt @ xlm)[ni.nfull:]
     info["x_ni_lm"] = fullx.copy()
+    if not seamless:
+        return True, fullx, info
     si = SeamlessIntegration(ni, X_, F2_, integerIdcs, singularIdcs, roundSeams)
     success, rounded = True, False
     resolves = 0
@@ -1106,7 +1219,10 @@ def iterative_rounding(fixedIdcs, fixedVals, singularIdcs, integerIdcs, length, 
         if not si.init_fixed_indices():
             continue
         rounded = True
-        _, xs = lm_solve(si, max_iter=100, func_tol=1e-7, foo_tol=1e-7, stats=stats)
+        if local_injectivity:
+            _, xs, _ = lm_solve_damped(si, 0.01, max_iter=100, func_tol=1e-7, foo_tol=1e-7, stats=stats)
+        else:
+            _, xs = lm_solve(si, max_iter=100, func_tol=1e-7, foo_tol=1e-7, stats=stats)
         resolves += 1
         if not si.post_checking(xs):
             success = False
@@ -1132,7 +1248,7 @@ def run_field(V, F, N=4, seed=0, n_iter=50, x0=None):
 
 
 def pipeline(V, F, ratio=0.02, N=4, seed=0, seamless=True, round_seams=False, n_iter=50,
-             x0=None, stop_after=None):
+             x0=None, stop_after=None, local_injectivity=False):
     out = {}
     m, L, M, c, field = run_field(V, F, N, seed, n_iter, x0)
     out.update(mesh=m, L=L, M=M, compressed=c, field=field)
@@ -1163,7 +1279,8 @@ def pipeline(V, F, ratio=0.02, N=4, seed=0, seamless=True, round_seams=False, n_
     stats = {}
     ok, fullx, info = iterative_rounding(st["fixedIdcs"], st["fixedVals"], st["singularIdcs"],
                                          st["integerIdcs"], length, Cfull, (G2 @ fullx2N).tocsr(),
-                                         N, n, m.nF, seamless, round_seams, F2, stats)
+                                         N, n, m.nF, seamless, round_seams, F2, stats,
+                                         local_injectivity, fullx2N, cutF)
     NF = fullx2N @ fullx
     nfn = NF.reshape(-1, N)
     cfn = np.concatenate([nfn[cutF[:, j]] for j in range(3)], axis=1)

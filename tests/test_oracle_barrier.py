@@ -53,3 +53,37 @@ def test_orientation_check_and_corner_order():
     cfn[7, 1, :2], cfn[7, 2, :2] = cfn[7, 2, :2].copy(), cfn[7, 1, :2].copy()   # plant one flip
     cfn[11, 1, :2], cfn[11, 2, :2] = cfn[11, 2, :2].copy(), cfn[11, 1, :2].copy()
     assert O.locally_injective(cfn) == (2, 7)
+
+
+def _si_barrier(out):
+    si = out["info"]["si"]
+    fB, _, _ = O.injective_barrier_update(out["F2"], si.X2F @ si.xCurr)
+    return fB
+
+
+def test_local_injectivity_path_matches_plain_when_inactive():
+    """localInjectivity = true with the barrier inactive everywhere: the damped LMs converge to the
+    undamped solutions (same fixes, the same map to round-off) and the map is locally injective."""
+    V, F, ratio, rs = meshgen.workload("ico2_noise")
+    a = O.pipeline(V, F, ratio=ratio, round_seams=rs)
+    b = O.pipeline(V, F, ratio=ratio, round_seams=rs, local_injectivity=True)
+    assert a["success"] and b["success"]
+    assert b["info"]["fix_order"] == a["info"]["fix_order"]
+    span = a["fullx"].max() - a["fullx"].min()
+    assert np.abs(b["fullx"] - a["fullx"]).max() <= 1e-6 * span
+    assert O.locally_injective(b["cfn"])[0] == 0
+    assert (_si_barrier(a) == 0).all()
+
+
+def test_local_injectivity_path_with_active_barrier():
+    """A coarse grid (ratio 0.15) compresses the map next to the singularities: barrier rows are
+    active (0 < r < 1/2) in the plain result; the local-injectivity path rounds successfully to a
+    locally injective map with a finite barrier."""
+    V, F, _, rs = meshgen.workload("ico3_noise")
+    a = O.pipeline(V, F, ratio=0.15, round_seams=rs)
+    fa = _si_barrier(a)
+    assert ((fa > 0) & np.isfinite(fa)).any()
+    b = O.pipeline(V, F, ratio=0.15, round_seams=rs, local_injectivity=True)
+    assert b["success"]
+    assert O.locally_injective(b["cfn"])[0] == 0
+    assert np.isfinite(_si_barrier(b)).all()
