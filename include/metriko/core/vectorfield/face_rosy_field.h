@@ -231,6 +231,17 @@ namespace metriko {
         F->singular = fld.singular;
         std::vector<int> turns(m.nF, 0);
         std::vector<char> visit(m.nF, 0);
+        // per face side: the neighbour across it (-1 across a seam) and the signed matching,
+        // gathered in parallel so that the sequential search touches one array
+        std::vector<int> nb(3 * size_t(m.nF)), nm(3 * size_t(m.nF));
+        METRIKO_PARALLEL_FOR
+        for (int i = 0; i < m.nF; i++)
+            for (int j = 0; j < 3; j++) {
+                const int e = m.edge[m.face2half3(i, j)];
+                const bool b = m.edge2face(e, 0) == i;
+                nb[3 * size_t(i) + j] = seam[e] ? -1 : (b ? m.edge2face(e, 1) : m.edge2face(e, 0));
+                nm[3 * size_t(i) + j] = (b ? 1 : -1) * fld.matching[e];
+            }
         std::deque<std::pair<int, int>> q;
         q.emplace_back(0, 0);
         while (!q.empty()) {
@@ -240,12 +251,8 @@ namespace metriko {
             visit[i] = 1;
             turns[i] = mm;
             for (int j = 0; j < 3; j++) {
-                int e = m.edge[m.face2half3(i, j)];
-                bool b = m.edge2face(e, 0) == i;
-                int fn = b ? m.edge2face(e, 1) : m.edge2face(e, 0);
-                int n = (b ? 1 : -1) * fld.matching[e];
-                n = (n + mm + 1000 * N) % N;
-                if (!visit[fn] && !seam[e]) q.emplace_back(fn, n);
+                const int fn = nb[3 * size_t(i) + j];
+                if (fn >= 0 && !visit[fn]) q.emplace_back(fn, (nm[3 * size_t(i) + j] + mm + 1000 * N) % N);
             }
         }
         METRIKO_PARALLEL_FOR
