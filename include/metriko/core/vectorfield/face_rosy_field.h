@@ -40,11 +40,13 @@ namespace metriko {
         // face_rosy_field.h:63-69: field(f,i) = pow(polar(1, arg c_f), 1/N) * pow(r, i)
         void set_field_from_compressed() {
             const complex r = std::polar(1., TwoPI / rosyN);
+            std::vector<complex> rpow(rosyN);   // pow(r, i), the same factor for every face
+            for (int i = 0; i < rosyN; i++) rpow[i] = i ? std::exp(double(i) * std::log(r)) : complex(1, 0);
             field = MatXc(mesh.nF, rosyN);
             METRIKO_PARALLEL_FOR
             for (int f = 0; f < mesh.nF; f++) {
                 complex root = std::exp(std::log(std::polar(1., std::arg(compressed[f]))) * (1. / rosyN));
-                for (int i = 0; i < rosyN; i++) field(f, i) = root * (i ? std::exp(double(i) * std::log(r)) : complex(1, 0));
+                for (int i = 0; i < rosyN; i++) field(f, i) = root * rpow[i];
             }
         }
 
