@@ -79,12 +79,12 @@ struct ZSmem {
         XJ = tz + nZ; tmpJ = XJ + nJ; cz = tmpJ + nJ; wsum = cz + nZ;
     }
 };
-// bytes of ZSmem for nZ, nJ
-inline size_t zsmem_bytes(size_t elem, int nZ, int nJ) {
-    return elem * (7 * (size_t)nZ + 2 * (size_t)nJ + (size_t)kWarps * nZ + 8);
-}
 constexpr int kPhiSlot = 8;     // partials offset (in blocks) of the coarse-space dots
 constexpr int kMaxPhi = 64;     // largest z block that gets the Schur coarse space
+// bytes of ZSmem for nZ, nJ (the per-warp coarse-space sums only where the coarse space can be on)
+inline size_t zsmem_bytes(size_t elem, int nZ, int nJ) {
+    return elem * (7 * (size_t)nZ + 2 * (size_t)nJ + (nZ <= kMaxPhi ? (size_t)kWarps * nZ : 0) + 8);
+}
 
 template <typename T>
 struct ZProj {
