@@ -419,27 +419,44 @@ namespace metriko {
         }
     }
 
-    // face_rosy_field.h:294-369 (cut_mesh_with_singularities)
-    inline void cut_mesh_with_singularities(const Hmesh& m, const VecXi& singularities, MatXi& cuts) {
-        const MatXi& F = m.idx;
-        MatXi TT, TTi;
-        detail::triangle_adjacency(m, TT, TTi);
-        cuts = detail::spanning_cut(m, TT, TTi);
-        // vertex -> neighbouring vertices (one per outgoing halfedge), built in parallel
-        std::vector<int> vptr(m.nV + 1, 0);
+    // The part of cut_mesh_with_singularities that depends on the mesh alone: the triangle
+    // adjacency, the spanning cut (libigl's cut with an all-zero matching) and the vertex
+    // adjacency that the singularity-path searches walk.  Depends on no field, so a caller may
+    // compute it while the field is solved (mtk_pipeline_run does, on a host thread).
+    struct SeamBase {
+        MatXi TT, TTi, cuts;
+        std::vector<int> vptr, vv;   // vertex -> neighbouring vertices (one per outgoing halfedge)
+    };
+
+    inline SeamBase seam_base(const Hmesh& m) {
+        SeamBase b;
+        detail::triangle_adjacency(m, b.TT, b.TTi);
+        b.cuts = detail::spanning_cut(m, b.TT, b.TTi);
+        b.vptr.assign(m.nV + 1, 0);
         METRIKO_PARALLEL_FOR
         for (int v = 0; v < m.nV; v++) {
             int cnt = 0, h = m.vert2half[v];
             do { cnt++; h = m.twin[m.prev[h]]; } while (h != m.vert2half[v]);
-            vptr[v + 1] = cnt;
+            b.vptr[v + 1] = cnt;
         }
-        for (int v = 0; v < m.nV; v++) vptr[v + 1] += vptr[v];
-        std::vector<int> vv(vptr[m.nV]);
+        for (int v = 0; v < m.nV; v++) b.vptr[v + 1] += b.vptr[v];
+        b.vv.resize(b.vptr[m.nV]);
         METRIKO_PARALLEL_FOR
         for (int v = 0; v < m.nV; v++) {
-            int q = vptr[v], h = m.vert2half[v];
-            do { vv[q++] = m.head[h]; h = m.twin[m.prev[h]]; } while (h != m.vert2half[v]);
+            int q = b.vptr[v], h = m.vert2half[v];
+            do { b.vv[q++] = m.head[h]; h = m.twin[m.prev[h]]; } while (h != m.vert2half[v]);
         }
+        return b;
+    }
+
+    // face_rosy_field.h:294-369 (cut_mesh_with_singularities), continuing from seam_base(m)
+    inline void cut_mesh_with_singularities(const Hmesh& m, const VecXi& singularities, SeamBase&& base, MatXi& cuts) {
+        const MatXi& F = m.idx;
+        const MatXi& TT = base.TT;
+        const MatXi& TTi = base.TTi;
+        const std::vector<int>& vptr = base.vptr;
+        const std::vector<int>& vv = base.vv;
+        cuts = std::move(base.cuts);
         std::vector<int> in_cut(m.nV, 0);
         for (int f = 0; f < m.nF; f++) for (int j = 0; j < 3; j++) if (cuts(f, j)) in_cut[F(f, j)] = 1;
         std::vector<int> dist(m.nV, -1), prev(m.nV, -1), touched;
@@ -503,17 +520,25 @@ namespace metriko {
         }
     }
 
-    // face_rosy_field.h:371-386
-    inline std::vector<bool> compute_seam(const FaceRosyField& f) {
+    // face_rosy_field.h:294-369 (cut_mesh_with_singularities)
+    inline void cut_mesh_with_singularities(const Hmesh& m, const VecXi& singularities, MatXi& cuts) {
+        cut_mesh_with_singularities(m, singularities, seam_base(m), cuts);
+    }
+
+    // face_rosy_field.h:371-386, with seam_base(f.mesh) computed beforehand
+    inline std::vector<bool> compute_seam(const FaceRosyField& f, SeamBase&& base) {
         std::vector<bool> seam(f.mesh.nE, false);
         std::vector<int> sv;
         for (int v = 0; v < f.mesh.nV; v++) if (f.singular[v] != 0) sv.push_back(v);
         MatXi cuts;
-        cut_mesh_with_singularities(f.mesh, VecXi(sv), cuts);
+        cut_mesh_with_singularities(f.mesh, VecXi(sv), std::move(base), cuts);
         for (int iF = 0; iF < f.mesh.nF; iF++)
             for (int j = 0; j < 3; j++) if (cuts(iF, j)) seam[f.mesh.face2edge(iF, j)] = true;
         return seam;
     }
+
+    // face_rosy_field.h:371-386
+    inline std::vector<bool> compute_seam(const FaceRosyField& f) { return compute_seam(f, seam_base(f.mesh)); }
 }
 
 #endif

@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <future>
 
 #include "metriko/core/igm/parameterization.h"
 #include "metriko/core/vectorfield/face_rosy_field.h"
@@ -51,6 +52,9 @@ extern "C" int mtk_pipeline_run(mtk_ctx* ctx, int32_t nV, int32_t nF, const doub
         auto mesh = std::make_unique<Hmesh>(V, F);
         lap(ts);
         stamp("hmesh", ts2);
+        // the field-independent part of the seam search runs on a host thread during the field solve
+        std::future<SeamBase> base;
+        if (popts->stop_after != 1) base = std::async(std::launch::async, [&m = *mesh] { return seam_base(m); });
         FaceRosyField rawf(*mesh, 4, popts->field_type == 1 ? FieldType::CurvatureAligned : FieldType::Smoothest);
         stamp("field (gpu)", ts2);
         ts = clk::now();
@@ -66,7 +70,7 @@ extern "C" int mtk_pipeline_run(mtk_ctx* ctx, int32_t nV, int32_t nF, const doub
             if (stats) { *stats = gpu::stats(); stats->ms_host = host_ms; stats->ms_total = std::chrono::duration<double, std::milli>(clk::now() - t0).count(); }
             return MTK_OK;
         }
-        auto seam = compute_seam(rawf);
+        auto seam = compute_seam(rawf, base.get());
         stamp("seam", ts2);
         auto cutm = compute_cut_mesh(*mesh, seam);
         stamp("cut mesh", ts2);
@@ -141,9 +145,10 @@ extern "C" int mtk_pipeline_size_field_gradient(mtk_ctx* ctx, int32_t nV, int32_
         std::memcpy(V.data(), Vb, sizeof(double) * 3 * size_t(nV));
         std::memcpy(F.data(), Fb, sizeof(int32_t) * 3 * size_t(nF));
         auto mesh = std::make_unique<Hmesh>(V, F);
+        auto base = std::async(std::launch::async, [&m = *mesh] { return seam_base(m); });   // during the field solve
         FaceRosyField rawf(*mesh, 4, popts->field_type == 1 ? FieldType::CurvatureAligned : FieldType::Smoothest);
         rawf.computeMatching(MatchingType::Curl);
-        auto seam = compute_seam(rawf);
+        auto seam = compute_seam(rawf, base.get());
         auto cutm = compute_cut_mesh(*mesh, seam);
         auto cmbf = compute_combbed_field(rawf, seam);
         MatXd extf = compute_extrinsic_field(*mesh, *cmbf, 4);
