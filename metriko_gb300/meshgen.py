@@ -12,6 +12,11 @@ dataset, so every workload here is generated from a seed:
 * ``torus(nu, nv, R, r, flip_p, jitter, seed)`` -- genus-1 parametric grid, each quad's
                                      diagonal flipped with probability ``flip_p`` and each vertex
                                      jittered tangentially by N(0, jitter * edge).
+* ``holed_slab(g, s, jitter, flip_p, seed)`` -- genus-g surface: the boundary of a one-voxel-thick
+                                     slab of (2g+1) x 3 voxels with g square holes, each voxel
+                                     split into s^3 cells, each boundary square cut into two
+                                     triangles (diagonal flipped with probability ``flip_p``),
+                                     vertices jittered by N(0, jitter / s).
 * ``workload(name)``               -- the named workloads (config sizes) used by tests/bench.
 
 Faces are consistently oriented with outward normals; vertex arrays are float64 (n x 3),
@@ -151,6 +156,43 @@ def torus(nu: int, nv: int, R: float = 1.0, r: float = 0.35, flip_p: float = 0.5
     return V, F.astype(np.int32)
 
 
+def holed_slab(g: int, s: int = 3, jitter: float = 0.05, flip_p: float = 0.5, seed: int = 0):
+    """Closed genus-g surface, the boundary of a polycube: a slab (2g+1) x 3 x 1 voxels with the
+    voxels (2k+1, 1), k < g, removed (g through-holes).  No two cells meet only along an edge or at
+    a corner, so the boundary is a 2-manifold; V - E + F = 2 - 2g.  Coordinates in voxel units."""
+    rng = np.random.default_rng(seed)
+    n = ((2 * g + 1) * s, 3 * s, s)
+    solid = np.ones(n, bool)
+    for k in range(g):
+        solid[(2 * k + 1) * s:(2 * k + 2) * s, s:2 * s, :] = False
+    pad = np.pad(solid, 1)
+    quads = []
+    for axis in range(3):
+        u, w = (axis + 1) % 3, (axis + 2) % 3
+        for sign in (1, -1):
+            cells = np.argwhere(pad & ~np.roll(pad, -sign, axis=axis)) - 1
+            base = cells.copy()
+            base[:, axis] += sign > 0
+            du = np.zeros(3, np.int64)
+            dw = np.zeros(3, np.int64)
+            du[u] = 1
+            dw[w] = 1
+            q = np.stack([base, base + du, base + du + dw, base + dw], axis=1)   # CCW about +axis
+            quads.append(q if sign > 0 else q[:, ::-1])
+    q = np.concatenate(quads)                                            # (nq, 4, 3) lattice points
+    key = (q[..., 0] * (n[1] + 1) + q[..., 1]) * (n[2] + 1) + q[..., 2]
+    uniq, inv = np.unique(key.ravel(), return_inverse=True)
+    inv = inv.reshape(-1, 4)
+    lat = np.stack([uniq // ((n[1] + 1) * (n[2] + 1)), (uniq // (n[2] + 1)) % (n[1] + 1), uniq % (n[2] + 1)], 1)
+    V = lat / s + rng.normal(0.0, jitter / s, size=lat.shape)
+    a, b, c, d = inv.T
+    flip = rng.random(len(a)) < flip_p
+    t0 = np.where(flip[:, None], np.stack([a, b, d], 1), np.stack([a, b, c], 1))
+    t1 = np.where(flip[:, None], np.stack([b, c, d], 1), np.stack([a, c, d], 1))
+    F = np.stack([t0, t1], axis=1).reshape(-1, 3)
+    return V.astype(np.float64), F.astype(np.int32)
+
+
 # Named workloads: (builder, grid ratio).  The ratio is RosyParameterization's `ratio`
 # argument (grid edge length = bbox diagonal * ratio / mean field norm).
 def workload(name: str, seed: int = 0):
@@ -177,6 +219,10 @@ def workload(name: str, seed: int = 0):
         nu, nv = (int(t) for t in name[6:].split("x"))
         v, f = torus(nu, nv, seed=seed)
         return v, f, 0.02, True
+    if name.startswith("genus"):    # e.g. genus2_s3: holed_slab(2, 3)
+        g, sub = name[5:].split("_s")
+        v, f = holed_slab(int(g), int(sub), seed=seed)
+        return v, f, 0.02, False
     raise KeyError(name)
 
 

@@ -47,7 +47,19 @@ def test_halfedge_invariants():
     assert abs(m.angleDefect.sum() - 4 * np.pi) < 1e-9
 
 
-@pytest.mark.parametrize("name,chi", [("ico2_noise", 2), ("ico3_noise", 2), ("ico4_noise", 2), ("torus_32x16", 0)])
+@pytest.mark.parametrize("g,s", [(1, 2), (2, 3), (3, 2)])
+def test_holed_slab_is_a_closed_oriented_genus_g_surface(g, s):
+    V, F = meshgen.holed_slab(g, s)
+    m = O.Hmesh(V, F)                        # raises on boundary or non-manifold edges
+    assert m.nV - m.nE + m.nF == 2 - 2 * g
+    assert abs(m.angleDefect.sum() - 2 * np.pi * (2 - 2 * g)) < 1e-9   # Gauss-Bonnet
+    a, b, c = V[F[:, 0]], V[F[:, 1]], V[F[:, 2]]
+    vol = np.einsum("ij,ij->i", a, np.cross(b, c)).sum() / 6
+    assert abs(vol - ((2 * g + 1) * 3 - g)) < 0.05 * ((2 * g + 1) * 3 - g)   # outward, voxel volume
+
+
+@pytest.mark.parametrize("name,chi", [("ico2_noise", 2), ("ico3_noise", 2), ("ico4_noise", 2), ("torus_32x16", 0),
+                                      ("genus2_s3", -2), ("genus3_s2", -4)])
 def test_singularity_index_sum(name, chi):
     """sum_v singular[v] = N * chi (face_rosy_field.h:126-133)."""
     V, F, ratio, rs = meshgen.workload(name)
@@ -103,7 +115,7 @@ def test_independent_rows():
     assert S.nnz == 1 and S.data[0] == 0.0   # cancelled entry kept as a structural zero
 
 
-@pytest.mark.parametrize("name", ["ico2_noise", "ico3_noise", "torus_32x16"])
+@pytest.mark.parametrize("name", ["ico2_noise", "ico3_noise", "torus_32x16", "genus2_s3"])
 def test_rounding_integrality_and_success(name):
     V, F, ratio, rs, out = oracle_run(name)
     assert out["success"]

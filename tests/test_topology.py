@@ -8,7 +8,8 @@ from metriko_gb300 import meshgen
 from oracle import metriko_oracle as O
 
 
-@pytest.mark.parametrize("name", ["ico2_noise", "ico3_noise", "ico4_noise", "torus_32x16", "torus_64x32"])
+@pytest.mark.parametrize("name", ["ico2_noise", "ico3_noise", "ico4_noise", "torus_32x16", "torus_64x32",
+                                  "genus2_s3", "genus3_s2", "genus2_s4"])
 def test_topology_matches_oracle(name):
     V, F, ratio, rs = meshgen.workload(name)
     ref = O.pipeline(V, F, ratio=ratio, round_seams=rs, stop_after="setup")
@@ -44,6 +45,21 @@ def test_seam_is_tree_through_singularities():
     verts = np.unique(E)
     assert len(E) == len(verts) - 1          # a tree
     assert set(np.flatnonzero(res["singular"])) <= set(verts.tolist())
+
+
+@pytest.mark.parametrize("name,genus", [("ico3_noise", 0), ("torus_32x16", 1), ("genus2_s3", 2), ("genus3_s2", 3)])
+def test_cut_mesh_is_a_disk(name, genus):
+    """The seam cuts every handle: the cut mesh is a topological disk (V - E + F = 1) and the seam
+    graph has first Betti number 2g (E_seam - V_seam + 1 independent cycles)."""
+    V, F, ratio, rs = meshgen.workload(name)
+    ref = O.pipeline(V, F, ratio=ratio, stop_after="field")
+    res = M.topology_from_field(V, F, ref["compressed"], ratio, rs)
+    cutF = res["cutF"]
+    e = np.unique(np.sort(np.concatenate([cutF[:, [0, 1]], cutF[:, [1, 2]], cutF[:, [2, 0]]]), axis=1), axis=0)
+    assert res["counts"]["nCut"] - len(e) + len(cutF) == 1
+    m = O.Hmesh(V, F)
+    E = m.edge2vert[res["seam"]]
+    assert len(E) - len(np.unique(E)) + 1 == 2 * genus
 
 
 def test_field_inputs_match_oracle():
