@@ -88,6 +88,12 @@ namespace metriko {
         VecXd faceArea, angleDefect, heArgOnFace;
 
         Hmesh(const MatXd& V, const MatXi& F);
+        // Two-phase construction: connectivity, face frames, normals, centres, areas and halfedge
+        // angles (all that a smoothest-field solve reads); finish() adds the element lists
+        // (halfs, verts, edges, faces) and the angle defects, which stay empty until then.
+        struct Deferred {};
+        Hmesh(const MatXd& V, const MatXi& F, Deferred);
+        void finish();
         Hmesh(const Hmesh&) = delete;
         Hmesh& operator=(const Hmesh&) = delete;
     };
@@ -201,7 +207,9 @@ namespace metriko {
         }
     }
 
-    inline Hmesh::Hmesh(const MatXd& V, const MatXi& F) {
+    inline Hmesh::Hmesh(const MatXd& V, const MatXi& F) : Hmesh(V, F, Deferred{}) { finish(); }
+
+    inline Hmesh::Hmesh(const MatXd& V, const MatXi& F, Deferred) {
         if (V.cols() != 3 || F.cols() != 3) throw std::invalid_argument("V and F must have 3 columns");
         pos = V;
         idx = F;
@@ -257,20 +265,9 @@ namespace metriko {
         }
         METRIKO_PARALLEL_FOR
         for (int h = 0; h < nH; h++) head[h] = tail[next[h]];
-        faces.resize(nF);
-        verts.resize(nV);
-        edges.resize(nE);
-        halfs.resize(nH);
-        METRIKO_PARALLEL_FOR
-        for (int i = 0; i < nH; i++) {
-            halfs[i] = Half{{i, this}};
-            if (i < nF) faces[i] = Face{{i, this}};
-            if (i < nV) verts[i] = Vert{{i, this}};
-            if (i < nE) edges[i] = Edge{{i, this}};
-        }
 
         faceBasisX = MatXd(nF, 3); faceBasisY = MatXd(nF, 3); faceNormal = MatXd(nF, 3); baryCenter = MatXd(nF, 3);
-        faceArea = VecXd(nF); heArgOnFace = VecXd(nH); angleDefect = VecXd(nV);
+        faceArea = VecXd(nF); heArgOnFace = VecXd(nH);
         METRIKO_PARALLEL_FOR
         for (int f = 0; f < nF; f++) {
             Row3d p0 = row3(pos, F(f, 0)), p1 = row3(pos, F(f, 1)), p2 = row3(pos, F(f, 2));
@@ -295,6 +292,21 @@ namespace metriko {
                 heArgOnFace[h.id] = sum;
             }
         }
+    }
+
+    inline void Hmesh::finish() {
+        faces.resize(nF);
+        verts.resize(nV);
+        edges.resize(nE);
+        halfs.resize(nH);
+        METRIKO_PARALLEL_FOR
+        for (int i = 0; i < nH; i++) {
+            halfs[i] = Half{{i, this}};
+            if (i < nF) faces[i] = Face{{i, this}};
+            if (i < nV) verts[i] = Vert{{i, this}};
+            if (i < nE) edges[i] = Edge{{i, this}};
+        }
+        angleDefect = VecXd(nV);
         METRIKO_PARALLEL_FOR
         for (int v = 0; v < nV; v++) {     // hmesh.h:599-610
             double sum = 0;

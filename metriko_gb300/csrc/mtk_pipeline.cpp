@@ -49,15 +49,21 @@ extern "C" int mtk_pipeline_run(mtk_ctx* ctx, int32_t nV, int32_t nF, const doub
         MatXi F(nF, 3);
         std::memcpy(V.data(), Vb, sizeof(double) * 3 * size_t(nV));
         std::memcpy(F.data(), Fb, sizeof(int32_t) * 3 * size_t(nF));
-        auto mesh = std::make_unique<Hmesh>(V, F);
+        auto mesh = std::make_unique<Hmesh>(V, F, Hmesh::Deferred{});
         lap(ts);
         stamp("hmesh", ts2);
-        // the field-independent part of the seam search runs on a host thread during the field solve
-        std::future<SeamBase> base;
-        if (popts->stop_after != 1) base = std::async(std::launch::async, [&m = *mesh] { return seam_base(m); });
+        // while the GPU solves the field, a host thread completes the mesh (element lists, angle
+        // defects: neither is read by the field solve) and computes the field-independent part of
+        // the seam search
+        const bool seams = popts->stop_after != 1;
+        auto pending = std::async(std::launch::async, [&m = *mesh, seams] {
+            m.finish();
+            return seams ? seam_base(m) : SeamBase{};
+        });
         FaceRosyField rawf(*mesh, 4, popts->field_type == 1 ? FieldType::CurvatureAligned : FieldType::Smoothest);
         stamp("field (gpu)", ts2);
         ts = clk::now();
+        SeamBase base = pending.get();
         rawf.computeMatching(MatchingType::Curl);
         stamp("matching+singular", ts2);
         if (compressed)
@@ -70,7 +76,7 @@ extern "C" int mtk_pipeline_run(mtk_ctx* ctx, int32_t nV, int32_t nF, const doub
             if (stats) { *stats = gpu::stats(); stats->ms_host = host_ms; stats->ms_total = std::chrono::duration<double, std::milli>(clk::now() - t0).count(); }
             return MTK_OK;
         }
-        auto seam = compute_seam(rawf, base.get());
+        auto seam = compute_seam(rawf, std::move(base));
         stamp("seam", ts2);
         auto cutm = compute_cut_mesh(*mesh, seam);
         stamp("cut mesh", ts2);
@@ -144,11 +150,12 @@ extern "C" int mtk_pipeline_size_field_gradient(mtk_ctx* ctx, int32_t nV, int32_
         MatXi F(nF, 3);
         std::memcpy(V.data(), Vb, sizeof(double) * 3 * size_t(nV));
         std::memcpy(F.data(), Fb, sizeof(int32_t) * 3 * size_t(nF));
-        auto mesh = std::make_unique<Hmesh>(V, F);
-        auto base = std::async(std::launch::async, [&m = *mesh] { return seam_base(m); });   // during the field solve
+        auto mesh = std::make_unique<Hmesh>(V, F, Hmesh::Deferred{});
+        auto pending = std::async(std::launch::async, [&m = *mesh] { m.finish(); return seam_base(m); });   // during the field solve
         FaceRosyField rawf(*mesh, 4, popts->field_type == 1 ? FieldType::CurvatureAligned : FieldType::Smoothest);
+        SeamBase base = pending.get();
         rawf.computeMatching(MatchingType::Curl);
-        auto seam = compute_seam(rawf, base.get());
+        auto seam = compute_seam(rawf, std::move(base));
         auto cutm = compute_cut_mesh(*mesh, seam);
         auto cmbf = compute_combbed_field(rawf, seam);
         MatXd extf = compute_extrinsic_field(*mesh, *cmbf, 4);
@@ -195,16 +202,20 @@ extern "C" int mtk_topology_from_field(int32_t nV, int32_t nF, const double* Vb,
         MatXi F(nF, 3);
         std::memcpy(V.data(), Vb, sizeof(double) * 3 * size_t(nV));
         std::memcpy(F.data(), Fb, sizeof(int32_t) * 3 * size_t(nF));
-        auto mesh = std::make_unique<Hmesh>(V, F);
+        // the same two-thread order as mtk_pipeline_run (the mesh completed and the seam base
+        // computed on a host thread while the field is set up)
+        auto mesh = std::make_unique<Hmesh>(V, F, Hmesh::Deferred{});
         stamp("hmesh");
+        auto pending = std::async(std::launch::async, [&m = *mesh] { m.finish(); return seam_base(m); });
         FaceRosyField rawf(*mesh, 4);
         rawf.compressed = VecXc(nF);
         for (int f = 0; f < nF; f++) rawf.compressed[f] = complex(compressed[2 * f], compressed[2 * f + 1]);
         rawf.set_field_from_compressed();
+        SeamBase base = pending.get();
         rawf.computeMatching(MatchingType::Curl);
         stamp("matching+singular");
         if (singular) std::memcpy(singular, rawf.singular.data(), sizeof(int32_t) * nV);
-        auto seam = compute_seam(rawf);
+        auto seam = compute_seam(rawf, std::move(base));
         stamp("seam");
         auto cutm = compute_cut_mesh(*mesh, seam);
         stamp("cut mesh");
