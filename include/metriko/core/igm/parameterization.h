@@ -16,6 +16,7 @@
 #ifndef METRIKO_PARAMETERIZATION_H
 #define METRIKO_PARAMETERIZATION_H
 #include <chrono>
+#include <future>
 #include <cstdio>
 #include <cstdlib>
 #include <map>
@@ -145,6 +146,7 @@ namespace metriko {
 
         void setup();
         void build_system(IntegSystem& sys);   // host part of integ()
+        void build_target(IntegSystem& sys) const;   // F2, length, cutV of build_system
         // Size-field gradient of the naive integration (mtk_size_field_gradient); no counterpart
         // in the reference.  s: log-size per raw vertex; T: per-face loss target (8 per face) or
         // nullptr for the integration target.  Fills fullx with x(s).
@@ -358,6 +360,9 @@ namespace metriko {
     }
 
     inline void RosyParameterization::build_system(IntegSystem& sys) {
+        // The target field, the grid length and the cut-vertex copy read only the cut mesh and
+        // the extrinsic field: computed on a host thread while the sparse products run.
+        auto target = std::async(std::launch::async, [this, &sys] { build_target(sys); });
         SprsD& fullx2Nfunc = sys.fullx2Nfunc;
         fullx2Nfunc = vtrans2cut * uncompress;
         SprsD Cfull = constraint * uncompress;     // structural zeros kept (Eigen product semantics)
@@ -392,6 +397,41 @@ namespace metriko {
         nJ = int(uniqueJ.size());
         nZ = USmall.cols();
 
+        // ---- W = rows k < n of fullx2Nfunc (rows k >= n are their negatives)
+        std::vector<int>& w_ptr = sys.w_ptr;
+        std::vector<int>& w_idx = sys.w_idx;
+        std::vector<double>& w_val = sys.w_val;
+        w_ptr.assign(n * size_t(cut.nV) + 1, 0);
+        w_idx.clear();
+        w_val.clear();
+        for (int c = 0; c < cut.nV; c++)
+            for (int k = 0; k < n; k++) {
+                int r = N * c + k;
+                for (int p = fullx2Nfunc.ptr[r]; p < fullx2Nfunc.ptr[r + 1]; p++) {
+                    if (fullx2Nfunc.val[p] == 0) continue;
+                    w_idx.push_back(fullx2Nfunc.idx[p]);
+                    w_val.push_back(fullx2Nfunc.val[p]);
+                }
+                w_ptr[n * c + k + 1] = int(w_idx.size());
+            }
+        target.get();
+
+        mtk_igm_desc& d = sys.desc;
+        d = mtk_igm_desc{};
+        d.nF = cut.nF; d.nCut = cut.nV; d.N = N; d.n = n;
+        d.cutF = cut.idx.data(); d.cutV = sys.cutV.data();
+        d.w_ptr = w_ptr.data(); d.w_idx = w_idx.data(); d.w_val = w_val.data();
+        d.nFull = nFull; d.full2y = full2y.data();
+        d.nJ = nJ; d.nZ = nZ; d.uniqueJ = uniqueJ.data(); d.USmall = USmall.data();
+        d.F2 = sys.F2.data(); d.length = sys.length;
+        d.nFixed = fixedIdcs.size(); d.fixedIdcs = fixedIdcs.data(); d.fixedVals = fixedVals.data();
+        d.nSingular = singularIdcs.size(); d.singularIdcs = singularIdcs.data();
+        d.nInteger = integerIdcs.size(); d.integerIdcs = integerIdcs.data();
+        d.seamless = seamless; d.roundSeams = roundSeams;
+        if (localInjectivity) throw std::invalid_argument("localInjectivity is not part of this build");
+    }
+
+    inline void RosyParameterization::build_target(IntegSystem& sys) const {
         // ---- target field (integ.ipp:30-43) and grid length (:70)
         // the per-vector lengths in parallel, their sum in the serial order
         std::vector<double> vlen(size_t(N) * cut.nF);
@@ -424,41 +464,9 @@ namespace metriko {
         double bb = std::sqrt((mx[0] - mn[0]) * (mx[0] - mn[0]) + (mx[1] - mn[1]) * (mx[1] - mn[1]) + (mx[2] - mn[2]) * (mx[2] - mn[2]));
         const double length = bb * gridscale / norm;
         sys.length = length;
-
-        // ---- W = rows k < n of fullx2Nfunc (rows k >= n are their negatives)
-        std::vector<int>& w_ptr = sys.w_ptr;
-        std::vector<int>& w_idx = sys.w_idx;
-        std::vector<double>& w_val = sys.w_val;
-        w_ptr.assign(n * size_t(cut.nV) + 1, 0);
-        w_idx.clear();
-        w_val.clear();
-        for (int c = 0; c < cut.nV; c++)
-            for (int k = 0; k < n; k++) {
-                int r = N * c + k;
-                for (int p = fullx2Nfunc.ptr[r]; p < fullx2Nfunc.ptr[r + 1]; p++) {
-                    if (fullx2Nfunc.val[p] == 0) continue;
-                    w_idx.push_back(fullx2Nfunc.idx[p]);
-                    w_val.push_back(fullx2Nfunc.val[p]);
-                }
-                w_ptr[n * c + k + 1] = int(w_idx.size());
-            }
         std::vector<double>& cutV = sys.cutV;
         cutV.assign(3 * size_t(cut.nV), 0.0);
         for (int i = 0; i < cut.nV; i++) for (int k = 0; k < 3; k++) cutV[3 * i + k] = cut.pos(i, k);
-
-        mtk_igm_desc& d = sys.desc;
-        d = mtk_igm_desc{};
-        d.nF = cut.nF; d.nCut = cut.nV; d.N = N; d.n = n;
-        d.cutF = cut.idx.data(); d.cutV = cutV.data();
-        d.w_ptr = w_ptr.data(); d.w_idx = w_idx.data(); d.w_val = w_val.data();
-        d.nFull = nFull; d.full2y = full2y.data();
-        d.nJ = nJ; d.nZ = nZ; d.uniqueJ = uniqueJ.data(); d.USmall = USmall.data();
-        d.F2 = F2.data(); d.length = length;
-        d.nFixed = fixedIdcs.size(); d.fixedIdcs = fixedIdcs.data(); d.fixedVals = fixedVals.data();
-        d.nSingular = singularIdcs.size(); d.singularIdcs = singularIdcs.data();
-        d.nInteger = integerIdcs.size(); d.integerIdcs = integerIdcs.data();
-        d.seamless = seamless; d.roundSeams = roundSeams;
-        if (localInjectivity) throw std::invalid_argument("localInjectivity is not part of this build");
     }
 
     inline double RosyParameterization::size_field_gradient(const VecXd& s, const VecXd* T, double mu, VecXd& grad_s) {
