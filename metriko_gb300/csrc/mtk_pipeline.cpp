@@ -78,11 +78,12 @@ extern "C" int mtk_pipeline_run(mtk_ctx* ctx, int32_t nV, int32_t nF, const doub
         }
         auto seam = compute_seam(rawf, std::move(base));
         stamp("seam", ts2);
-        auto cutm = compute_cut_mesh(*mesh, seam);
-        stamp("cut mesh", ts2);
+        // the cut mesh and the combing both read only the seam: the cut mesh on a host thread
+        auto cut_pending = std::async(std::launch::async, [&m = *mesh, &seam] { return compute_cut_mesh(m, seam); });
         auto cmbf = compute_combbed_field(rawf, seam);
         MatXd extf = compute_extrinsic_field(*mesh, *cmbf, 4);
-        stamp("combing+extrinsic", ts2);
+        auto cutm = cut_pending.get();
+        stamp("cut mesh+combing+extr", ts2);
         RosyParameterization rp(*mesh, *cutm, extf, cmbf->singular, cmbf->matching, seam, 4, popts->ratio);
         rp.seamless = popts->seamless != 0;
         rp.localInjectivity = false;
@@ -156,9 +157,10 @@ extern "C" int mtk_pipeline_size_field_gradient(mtk_ctx* ctx, int32_t nV, int32_
         SeamBase base = pending.get();
         rawf.computeMatching(MatchingType::Curl);
         auto seam = compute_seam(rawf, std::move(base));
-        auto cutm = compute_cut_mesh(*mesh, seam);
+        auto cut_pending = std::async(std::launch::async, [&m = *mesh, &seam] { return compute_cut_mesh(m, seam); });
         auto cmbf = compute_combbed_field(rawf, seam);
         MatXd extf = compute_extrinsic_field(*mesh, *cmbf, 4);
+        auto cutm = cut_pending.get();
         RosyParameterization rp(*mesh, *cutm, extf, cmbf->singular, cmbf->matching, seam, 4, popts->ratio);
         rp.seamless = false;
         rp.localInjectivity = false;
@@ -217,11 +219,11 @@ extern "C" int mtk_topology_from_field(int32_t nV, int32_t nF, const double* Vb,
         if (singular) std::memcpy(singular, rawf.singular.data(), sizeof(int32_t) * nV);
         auto seam = compute_seam(rawf, std::move(base));
         stamp("seam");
-        auto cutm = compute_cut_mesh(*mesh, seam);
-        stamp("cut mesh");
+        auto cut_pending = std::async(std::launch::async, [&m = *mesh, &seam] { return compute_cut_mesh(m, seam); });
         auto cmbf = compute_combbed_field(rawf, seam);
         MatXd extf = compute_extrinsic_field(*mesh, *cmbf, 4);
-        stamp("combing+extrinsic");
+        auto cutm = cut_pending.get();
+        stamp("cut mesh+combing+extr");
         RosyParameterization rp(*mesh, *cutm, extf, cmbf->singular, cmbf->matching, seam, 4, ratio);
         rp.seamless = true;
         rp.roundSeams = round_seams != 0;
