@@ -71,7 +71,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
                 print(r.stdout, r.stderr, file=sys.stderr)
     objs = [str(BUILD / (s + ".o")) for s in CU_SOURCES + CPP_SOURCES]
     if force or jobs or not OUT.exists():
-        _run([nvcc, *ARCH, "-shared", "-Xcompiler", "-fopenmp", "-o", str(OUT), *objs, "-lcudart", "-lgomp"])
+        _run([nvcc, *ARCH, "-shared", "-Xcompiler", "-fopenmp", "-o", str(OUT), *objs, "-lcudart", "-lgomp", "-lpthread"])
     return OUT
 
 
