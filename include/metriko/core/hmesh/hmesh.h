@@ -150,61 +150,75 @@ namespace metriko {
     inline AdjIter<AdjVH> Vert::adjHalfs(Half h, bool ccw) const { return {m, h.id, ccw}; }
 
     // libigl v2.5.0 edge_topology semantics (see file header).  EV: nE x 2, FE: nF x 3, EF: nE x 2.
+    // Built in parallel with the serial definition's result: entries are bucketed by their smaller
+    // vertex (atomic slots; each bucket is then sorted by (hi, face, corner), a total order, so the
+    // slot order does not matter), edge ids are the running count of distinct (lo, hi) pairs in
+    // that order, and the checks report the error the serial pass would meet first (a third face
+    // on any edge, else the first edge in order with one face or a repeated face).
     inline void edge_topology(const MatXi& F, int nV, MatXi& EV, MatXi& FE, MatXi& EF) {
         const int nF = F.rows();
+        const long long nEnt = 3LL * nF;
         struct Ent { int hi, f, i, a; };
         std::vector<int> cnt(nV + 1, 0);
-        for (int f = 0; f < nF; f++)
-            for (int i = 0; i < 3; i++) {
-                int a = F(f, i), b = F(f, (i + 1) % 3);
-                if (a < 0 || a >= nV || b < 0 || b >= nV || a == b) throw std::invalid_argument("bad face index");
-                cnt[std::min(a, b) + 1]++;
-            }
-        for (int v = 0; v < nV; v++) cnt[v + 1] += cnt[v];
-        std::vector<Ent> ent(size_t(3) * nF);
-        std::vector<int> fill(cnt.begin(), cnt.end() - 1);
-        for (int f = 0; f < nF; f++)
-            for (int i = 0; i < 3; i++) {
-                int a = F(f, i), b = F(f, (i + 1) % 3);
-                ent[fill[std::min(a, b)]++] = {std::max(a, b), f, i, a};
-            }
+        int bad = 0;
         METRIKO_PARALLEL_FOR
-        for (int v = 0; v < nV; v++)
+        for (int f = 0; f < nF; f++)
+            for (int i = 0; i < 3; i++) {
+                int a = F(f, i), b = F(f, (i + 1) % 3);
+                if (a < 0 || a >= nV || b < 0 || b >= nV || a == b) { __atomic_store_n(&bad, 1, __ATOMIC_RELAXED); continue; }
+                __atomic_fetch_add(&cnt[std::min(a, b) + 1], 1, __ATOMIC_RELAXED);
+            }
+        if (bad) throw std::invalid_argument("bad face index");
+        for (int v = 0; v < nV; v++) cnt[v + 1] += cnt[v];
+        std::vector<Ent> ent(nEnt);
+        std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+        METRIKO_PARALLEL_FOR
+        for (int f = 0; f < nF; f++)
+            for (int i = 0; i < 3; i++) {
+                int a = F(f, i), b = F(f, (i + 1) % 3);
+                ent[__atomic_fetch_add(&fill[std::min(a, b)], 1, __ATOMIC_RELAXED)] = {std::max(a, b), f, i, a};
+            }
+        std::vector<int> lo_of(nEnt);
+        METRIKO_PARALLEL_FOR
+        for (int v = 0; v < nV; v++) {
             std::sort(ent.begin() + cnt[v], ent.begin() + cnt[v + 1], [](const Ent& x, const Ent& y) {
                 if (x.hi != y.hi) return x.hi < y.hi;
                 if (x.f != y.f) return x.f < y.f;
                 return x.i < y.i;
             });
+            for (int p = cnt[v]; p < cnt[v + 1]; p++) lo_of[p] = v;
+        }
+        std::vector<int> eid(nEnt);    // 1 where an entry starts a new (lo, hi), then its edge id
+        METRIKO_PARALLEL_FOR
+        for (long long p = 0; p < nEnt; p++) eid[p] = p == 0 || lo_of[p] != lo_of[p - 1] || ent[p].hi != ent[p - 1].hi;
         int nE = 0;
-        std::vector<int> lo_of(ent.size());
-        for (int v = 0; v < nV; v++) for (int p = cnt[v]; p < cnt[v + 1]; p++) lo_of[p] = v;
-        for (size_t p = 0; p < ent.size(); p++)
-            if (p == 0 || lo_of[p] != lo_of[p - 1] || ent[p].hi != ent[p - 1].hi) nE++;
+        for (long long p = 0; p < nEnt; p++) { nE += eid[p]; eid[p] = nE - 1; }
+        std::vector<int> first(nE + 1);
+        METRIKO_PARALLEL_FOR
+        for (long long p = 0; p < nEnt; p++) if (p == 0 || eid[p] != eid[p - 1]) first[eid[p]] = int(p);
+        first[nE] = int(nEnt);
         EV = MatXi(nE, 2, -1);
         EF = MatXi(nE, 2, -1);
         FE = MatXi(nF, 3, -1);
-        int e = -1;
-        std::vector<int> dir0(nE, 0), count(nE, 0);
-        for (size_t p = 0; p < ent.size(); p++) {
-            bool fresh = p == 0 || lo_of[p] != lo_of[p - 1] || ent[p].hi != ent[p - 1].hi;
-            if (fresh) {
-                e++;
-                EV(e, 0) = lo_of[p];
-                EV(e, 1) = ent[p].hi;
-                EF(e, 0) = ent[p].f;
-                dir0[e] = ent[p].a == lo_of[p];
-            } else {
-                if (count[e] >= 2) throw std::invalid_argument("mesh is not edge-manifold");
-                EF(e, 1) = ent[p].f;
-            }
-            count[e]++;
-            FE(ent[p].f, ent[p].i) = e;
+        int over = 0;
+        std::vector<char> err(nE, 0);  // 1: one face (boundary), 2: the same face twice
+        METRIKO_PARALLEL_FOR
+        for (int e = 0; e < nE; e++) {
+            const int p0 = first[e], c = first[e + 1] - p0;
+            EV(e, 0) = lo_of[p0];
+            EV(e, 1) = ent[p0].hi;
+            EF(e, 0) = ent[p0].f;
+            if (c >= 2) EF(e, 1) = ent[p0 + 1].f;
+            if (c > 2) __atomic_store_n(&over, 1, __ATOMIC_RELAXED);
+            for (int p = p0; p < p0 + c; p++) FE(ent[p].f, ent[p].i) = e;
+            if (c != 2) { err[e] = 1; continue; }
+            if (ent[p0].a != lo_of[p0]) std::swap(EF(e, 0), EF(e, 1));
+            if (EF(e, 0) == EF(e, 1)) err[e] = 2;
         }
-        for (int k = 0; k < nE; k++) {
-            if (count[k] != 2) throw std::invalid_argument(count[k] > 2 ? "mesh is not edge-manifold" : "mesh has boundary edges (closed meshes only)");
-            if (!dir0[k]) std::swap(EF(k, 0), EF(k, 1));
-            if (EF(k, 0) == EF(k, 1)) throw std::invalid_argument("degenerate edge");
-        }
+        if (over) throw std::invalid_argument("mesh is not edge-manifold");
+        auto it = std::find_if(err.begin(), err.end(), [](char x) { return x != 0; });
+        if (it != err.end())
+            throw std::invalid_argument(*it == 1 ? "mesh has boundary edges (closed meshes only)" : "degenerate edge");
     }
 
     inline Hmesh::Hmesh(const MatXd& V, const MatXi& F) : Hmesh(V, F, Deferred{}) { finish(); }
@@ -237,9 +251,14 @@ namespace metriko {
             edge[2 * e] = edge[2 * e + 1] = e;
             edge2half[e] = 2 * e;
         }
-        for (int e = 0; e < nE; e++) {                // last write wins (dcel, hmesh.h:314-323)
-            vert2half[edge2vert(e, 0)] = 2 * e;
-            vert2half[edge2vert(e, 1)] = 2 * e + 1;
+        // last write wins in edge order (dcel, hmesh.h:314-323): halfedge 2e + s is written for
+        // edge2vert(e, s), so the survivor is the largest halfedge id starting at the vertex
+        METRIKO_PARALLEL_FOR
+        for (int h = 0; h < nH; h++) {
+            int* slot = &vert2half[tail[h]];
+            int cur = __atomic_load_n(slot, __ATOMIC_RELAXED);
+            while (h > cur && !__atomic_compare_exchange_n(slot, &cur, h, true, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) {
+            }
         }
         for (int v = 0; v < nV; v++) if (vert2half[v] < 0) throw std::invalid_argument("isolated vertex");
         face2half3 = MatXi(nF, 3);
