@@ -67,6 +67,23 @@ def test_topology_rejects_bad_index():
         M.topology_from_field(V, F, np.ones(len(F), complex))
 
 
+@pytest.mark.parametrize("case", ["non_manifold", "isolated_vertex", "repeated_vertex"])
+def test_topology_rejects_invalid_meshes(case):
+    """Closed, edge-manifold meshes only: a third face on an edge, a vertex in no face and a face
+    with a repeated vertex are rejected with MTK_ERR_BAD_INPUT and a message."""
+    V = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1], [1, 1, 1]], float)
+    tet = [[0, 2, 1], [0, 3, 2], [0, 1, 3], [1, 2, 3]]
+    F = {"non_manifold": tet + [[0, 1, 4]], "isolated_vertex": tet,
+         "repeated_vertex": [[0, 2, 2], [0, 3, 2], [0, 1, 3], [1, 2, 3]]}[case]
+    F = np.array(F, np.int32)
+    with pytest.raises(M.MetrikoError) as e:
+        M.topology_from_field(V, F, np.ones(len(F), complex))
+    assert e.value.status == _lib.BAD_INPUT
+    msg = str(e.value)      # carries mtk_last_error()
+    assert {"non_manifold": "edge-manifold", "isolated_vertex": "isolated vertex",
+            "repeated_vertex": "bad face index"}[case] in msg
+
+
 def test_ctx_create_without_gpu():
     import torch
     if torch.cuda.is_available():
