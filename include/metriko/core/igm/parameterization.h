@@ -117,6 +117,7 @@ namespace metriko {
         VecXd naivex;        // naive Poisson solution (ni.x0), for diagnostics
         MatXd nfn;
         MatXd cfn;
+        double deviation = 0;   // map_deviation of the result (computed by integ())
         std::vector<int> fixOrder, fixVals;   // greedy rounding order (diagnostics)
         bool verbose = false;
         bool seamless = false;
@@ -359,6 +360,40 @@ namespace metriko {
             if (is_inside_singular(v)) for (int j = 0; j < n; j++) singularIdcs[c++] = n * v + j;
     }
 
+    // The check at the end of the reference's integ() (parameterization_integ.ipp:100-117): on
+    // every face the 3D gradient of each of the N functions -- the corner hat-function gradients
+    // n x (next(h) vector) / (2 area) of G3 (:11-27), corners in the order of the face's
+    // halfedges, F(f,0), F(f,1), F(f,2) -- against the extrinsic field; returns the mean over
+    // faces and functions of |normalized(ext_k) - normalized(grad_k)|.  cfn: nF x 3N, the value
+    // of function k at corner j in column N j + k.  Per-face sums in parallel, their total in
+    // face order.
+    inline double map_deviation(const MatXd& cutV, const MatXi& cutF, const MatXd& cfn, const MatXd& ext, int N) {
+        const int nF = cutF.rows();
+        if (nF == 0 || N <= 0) return 0;
+        std::vector<double> part(nF);
+        METRIKO_PARALLEL_FOR
+        for (int f = 0; f < nF; f++) {
+            const Row3d p[3] = {row3(cutV, cutF(f, 0)), row3(cutV, cutF(f, 1)), row3(cutV, cutF(f, 2))};
+            const Row3d n = (p[1] - p[0]).cross(p[2] - p[0]);
+            const double a2 = n.norm();
+            const Row3d nu = n.normalized();
+            Row3d g[3];
+            for (int j = 0; j < 3; j++) g[j] = nu.cross(p[(j + 2) % 3] - p[(j + 1) % 3]) / a2;
+            double s = 0;
+            for (int k = 0; k < N; k++) {
+                Row3d grad = g[0] * cfn(f, k);
+                grad = grad + g[1] * cfn(f, N + k);
+                grad = grad + g[2] * cfn(f, 2 * N + k);
+                const Row3d e{ext(f, 3 * k), ext(f, 3 * k + 1), ext(f, 3 * k + 2)};
+                s += (e.normalized() - grad.normalized()).norm();
+            }
+            part[f] = s;
+        }
+        double sum = 0;
+        for (double v : part) sum += v;
+        return sum / (double(nF) * N);
+    }
+
     inline void RosyParameterization::build_system(IntegSystem& sys) {
         // The target field, the grid length and the cut-vertex copy read only the cut mesh and
         // the extrinsic field: computed on a host thread while the sparse products run.
@@ -496,11 +531,17 @@ namespace metriko {
         // ---- nfn (cut vertex x N) and cfn (face x 3N)  (integ.ipp:88-98)
         std::vector<double> NF = fullx2Nfunc * fullx.d;
         nfn = MatXd(cut.nV, N);
+        METRIKO_PARALLEL_FOR
         for (int i = 0; i < cut.nV; i++) for (int k = 0; k < N; k++) nfn(i, k) = NF[N * size_t(i) + k];
         cfn = MatXd(raw.nF, 3 * N);
+        METRIKO_PARALLEL_FOR
         for (int f = 0; f < raw.nF; f++)
             for (int j = 0; j < 3; j++)
                 for (int k = 0; k < N; k++) cfn(f, N * j + k) = nfn(cut.idx(f, j), k);
+        // ---- how close the map's gradients are to the field (integ.ipp:100-117)
+        deviation = map_deviation(cut.pos, cut.idx, cfn, ext, N);
+        if (verbose || (getenv("MTK_DEBUG") && getenv("MTK_DEBUG")[0] == '1'))
+            fprintf(stderr, "Deviation of the recovered tf from the original : %.9g\n", deviation);
         return success;
     }
 }

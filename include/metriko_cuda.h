@@ -291,6 +291,18 @@ int mtk_field_inputs(int32_t nV, int32_t nF, const double* V, const int32_t* F, 
                      double* area);
 
 /*
+ * Host only (no GPU): the check at the end of RosyParameterization::integ()
+ * (parameterization_integ.ipp:100-117, with G3 of :11-27) -- the mean over faces and functions
+ * of |normalized(ext_k) - normalized(grad_k)|, grad_k the 3D gradient on the face of function k
+ * of the map.  cutV[3*nCut], cutF[3*nF] (cut mesh), cfn[nF*3N] (function k at corner j in
+ * column N*j + k, as mtk_pipeline_run returns it), ext[nF*3N] (the combed extrinsic field,
+ * vector k in columns 3k..3k+2).  RosyParameterization::integ() stores the same value in its
+ * member `deviation`.
+ */
+int mtk_map_deviation(int32_t nF, int32_t N, int32_t nCut, const int32_t* cutF, const double* cutV,
+                      const double* cfn, const double* ext, double* deviation);
+
+/*
  * SpMV roofline measurement (no counterpart in the reference): assembles the field operator
  * of mtk_field_smoothest and times `reps` stand-alone SpMVs y = L x (FP32 or FP64), each after
  * an L2 flush and with its own CUDA events.  *bytes_per_spmv: algorithmic bytes per SpMV

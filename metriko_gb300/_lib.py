@@ -22,7 +22,7 @@ EXPORTS = [
     "mtk_ctx_kernel_count", "mtk_field_smoothest", "mtk_iterative_rounding", "mtk_pipeline_run",
     "mtk_seeded_init", "mtk_topology_from_field", "mtk_field_smoothest_noalloc", "mtk_size_field_gradient",
     "mtk_pipeline_size_field_gradient", "mtk_field_solve", "mtk_field_inputs", "mtk_field_spmv_bench",
-    "mtk_injective_barrier", "mtk_local_injectivity",
+    "mtk_injective_barrier", "mtk_local_injectivity", "mtk_map_deviation",
 ]
 
 
@@ -96,6 +96,8 @@ def lib():
                                             C.c_void_p, C.c_void_p, C.c_void_p]
         L.mtk_local_injectivity.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.POINTER(C.c_int32),
                                             C.POINTER(C.c_int32)]
+        L.mtk_map_deviation.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.POINTER(C.c_double)]
         L.mtk_field_solve.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.c_void_p, C.POINTER(SolveOpts), C.c_void_p, C.POINTER(Stats)]
         L.mtk_pipeline_size_field_gradient.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
@@ -243,6 +245,22 @@ def injective_barrier(ctx: Context, intrinsic_field, field, N=4, update_j=True):
                                        _ptr(dB) if update_j else None, _ptr(S) if update_j else None),
            "mtk_injective_barrier")
     return fB, dB, (S.reshape(-1, 4) if update_j else None)
+
+
+def map_deviation(cutV, cutF, cfn, ext, N=4):
+    """mtk_map_deviation (host only): the check at the end of the reference's integ() -- mean over
+    faces and functions of |normalized(ext_k) - normalized(3D gradient of function k)|."""
+    V = np.ascontiguousarray(cutV, np.float64)
+    F = np.ascontiguousarray(cutF, np.int32)
+    c = np.ascontiguousarray(cfn, np.float64)
+    e = np.ascontiguousarray(ext, np.float64)
+    nF = len(F)
+    if c.size != 3 * N * nF or e.size != 3 * N * nF:
+        raise ValueError("cfn and ext need 3N values per face")
+    out = C.c_double(0)
+    _check(lib().mtk_map_deviation(nF, N, len(V), _ptr(F), _ptr(V), _ptr(c), _ptr(e), C.byref(out)),
+           "mtk_map_deviation")
+    return out.value
 
 
 def local_injectivity(ctx: Context, cfn, N=4):

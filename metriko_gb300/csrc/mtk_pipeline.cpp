@@ -273,3 +273,19 @@ extern "C" int mtk_field_inputs(int32_t nV, int32_t nF, const double* Vb, const 
         return MTK_ERR_BAD_INPUT;
     }
 }
+
+extern "C" int mtk_map_deviation(int32_t nF, int32_t N, int32_t nCut, const int32_t* cutF, const double* cutV,
+                                 const double* cfn, const double* ext, double* deviation) {
+    if (nF < 0 || N <= 0 || nCut < 0 || !deviation || (nF > 0 && (!cutF || !cutV || !cfn || !ext)))
+        return MTK_ERR_BAD_INPUT;
+    for (size_t i = 0; i < 3 * size_t(nF); i++)
+        if (cutF[i] < 0 || cutF[i] >= nCut) return MTK_ERR_BAD_INPUT;
+    MatXd V(nCut, 3), C(nF, 3 * N), E(nF, 3 * N);
+    MatXi F(nF, 3);
+    std::memcpy(V.data(), cutV, sizeof(double) * 3 * size_t(nCut));
+    std::memcpy(F.data(), cutF, sizeof(int32_t) * 3 * size_t(nF));
+    std::memcpy(C.data(), cfn, sizeof(double) * 3 * size_t(N) * nF);
+    std::memcpy(E.data(), ext, sizeof(double) * 3 * size_t(N) * nF);
+    *deviation = map_deviation(V, F, C, E, N);
+    return MTK_OK;
+}

@@ -1177,6 +1177,31 @@ def injective_barrier_update(intrinsic_field, field, N=4, update_j=True):
     return fB, der, S
 
 
+def map_deviation(cutV, cutF, cfn, ext, N=4):
+    """The check at the end of integ() (parameterization_integ.ipp:100-117): vf = G3 * NF, G3 the
+    per-face 3D gradient operator of :11-27 -- for the halfedge h of face f starting at corner j
+    (corners in the order F[f,0], F[f,1], F[f,2] of f's halfedges), the row block
+    normal x next(h).vec / (2 area), next(h) running from corner j+1 to corner j+2 -- and the
+    result is the mean over faces and functions of |normalized(ext_k) - normalized(vf_k)|
+    (normalized leaves a zero vector unchanged)."""
+    p = np.asarray(cutV, float)[np.asarray(cutF)]
+    n = np.cross(p[:, 1] - p[:, 0], p[:, 2] - p[:, 0])
+    a2 = np.linalg.norm(n, axis=1)
+    nu = n / a2[:, None]
+    c = np.asarray(cfn, float).reshape(-1, 3, N)
+    vf = np.zeros((len(p), N, 3))
+    for j in range(3):
+        g = np.cross(nu, p[:, (j + 2) % 3] - p[:, (j + 1) % 3]) / a2[:, None]
+        vf += c[:, j, :, None] * g[:, None, :]
+    ev = np.asarray(ext, float).reshape(-1, N, 3)
+
+    def unit(v):
+        nrm = np.linalg.norm(v, axis=-1, keepdims=True)
+        return np.where(nrm > 0, v / np.where(nrm > 0, nrm, 1.0), v)
+
+    return float(np.linalg.norm(unit(ev) - unit(vf), axis=-1).sum() / (len(p) * N))
+
+
 def locally_injective(cfn, N=4):
     """locally_injectivity_check (parameterization_integ.ipp:46-63): corners a, b, c of each cut
     face are the tails of f.half(), its next and its prev -- with face2half on the edge
