@@ -19,7 +19,7 @@
 
 namespace metriko {
     struct Hmesh;
-    struct Half; struct Vert; struct Edge; struct Face;
+    struct Half; struct Vert; struct Edge; struct Face; struct Crnr;
 
     struct Elem {
         int id;
@@ -38,6 +38,7 @@ namespace metriko {
         Row3d center() const;
         double area() const;
         AdjIter<AdjFH> adjHalfs(bool ccw = true) const;
+        AdjIter<AdjFH> adjHalfs(Half h, bool ccw = true) const;
     };
     struct Edge : Elem {
         Half half() const;
@@ -45,15 +46,28 @@ namespace metriko {
         Vert vert1() const;
         Face face0() const;
         Face face1() const;
+        double len() const;
+        double cot() const;
         bool isBoundary() const { return false; }
     };
     struct Vert : Elem {
         Half half() const;
         Row3d pos() const;
+        Row3d basisX() const;
+        Row3d basisY() const;
+        Row3d normal() const;
+        double baryArea() const;
+        double circArea() const;
         bool isBoundary() const { return false; }
         bool isInterior() const { return true; }
         AdjIter<AdjVH> adjHalfs(bool ccw = true) const;
         AdjIter<AdjVH> adjHalfs(Half h, bool ccw = true) const;
+    };
+    // corner c of face f sits at F(f, c - 3f); its halfedge is the one opposite that vertex
+    struct Crnr : Elem {
+        Half half() const;
+        Vert vert() const;
+        Face face() const;
     };
     struct Half : Elem {
         Half next() const;
@@ -63,7 +77,11 @@ namespace metriko {
         Vert head() const;
         Edge edge() const;
         Face face() const;
+        Crnr crnr() const;
         double farg() const;
+        double varg() const;
+        double darg() const;
+        double cot() const;
         double len() const { return vec().norm(); }
         bool isBoundary() const { return false; }
         bool isCanonical() const;
@@ -86,11 +104,20 @@ namespace metriko {
         MatXi face2half3;  // nF x 3, halfedge of face f on face2edge(f,j)
         MatXd faceBasisX, faceBasisY, faceNormal, baryCenter;
         VecXd faceArea, angleDefect, heArgOnFace;
+        // filled by finish() (hmesh.h:452-611 of the reference): vertex frames, dual areas,
+        // cotangents, dihedral angles, halfedge angles around vertices, corner handles;
+        // closed meshes only, so there are no boundary loops and no boundary vertices
+        MatXd vertBasisX, vertBasisY, vertNormal;
+        VecXd baryDualArea, circDualArea, halfCotan, edgeCotan, dihedralArg, heArgOnVert;
+        std::vector<Crnr> crnrs;
+        std::vector<int> loop2half;
+        std::vector<bool> isBV;
 
         Hmesh(const MatXd& V, const MatXi& F);
         // Two-phase construction: connectivity, face frames, normals, centres, areas and halfedge
         // angles (all that a smoothest-field solve reads); finish() adds the element lists
-        // (halfs, verts, edges, faces) and the angle defects, which stay empty until then.
+        // (halfs, verts, edges, faces, crnrs), the angle defects and the vertex and edge
+        // geometry below, which stay empty until then.
         struct Deferred {};
         Hmesh(const MatXd& V, const MatXi& F, Deferred);
         void finish();
@@ -129,7 +156,21 @@ namespace metriko {
     inline Vert Half::head() const { return {{m->head[id], m}}; }
     inline Edge Half::edge() const { return {{m->edge[id], m}}; }
     inline Face Half::face() const { return {{m->face[id], m}}; }
+    inline Crnr Half::crnr() const { return {{m->crnr[id], m}}; }
     inline double Half::farg() const { return m->heArgOnFace[id]; }
+    inline double Half::varg() const { return m->heArgOnVert[id]; }
+    inline double Half::darg() const { return m->dihedralArg[id]; }
+    inline double Half::cot() const { return m->halfCotan[id]; }
+    inline double Edge::len() const { return Half{{m->edge2half[id], m}}.len(); }
+    inline double Edge::cot() const { return m->edgeCotan[id]; }
+    inline Row3d Vert::basisX() const { return row3(m->vertBasisX, id); }
+    inline Row3d Vert::basisY() const { return row3(m->vertBasisY, id); }
+    inline Row3d Vert::normal() const { return row3(m->vertNormal, id); }
+    inline double Vert::baryArea() const { return m->baryDualArea[id]; }
+    inline double Vert::circArea() const { return m->circDualArea[id]; }
+    inline Half Crnr::half() const { return {{m->crnr2half[id], m}}; }
+    inline Vert Crnr::vert() const { return half().prev().tail(); }
+    inline Face Crnr::face() const { return half().face(); }
     inline bool Half::isCanonical() const { return m->edge2half[m->edge[id]] == id; }
     inline Row3d Half::vec() const { return row3(m->pos, m->head[id]) - row3(m->pos, m->tail[id]); }
     inline Half Vert::half() const { return {{m->vert2half[id], m}}; }
@@ -146,6 +187,7 @@ namespace metriko {
     inline Row3d Face::center() const { return row3(m->baryCenter, id); }
     inline double Face::area() const { return m->faceArea[id]; }
     inline AdjIter<AdjFH> Face::adjHalfs(bool ccw) const { return {m, m->face2half[id], ccw}; }
+    inline AdjIter<AdjFH> Face::adjHalfs(Half h, bool ccw) const { return {m, h.id, ccw}; }
     inline AdjIter<AdjVH> Vert::adjHalfs(bool ccw) const { return {m, m->vert2half[id], ccw}; }
     inline AdjIter<AdjVH> Vert::adjHalfs(Half h, bool ccw) const { return {m, h.id, ccw}; }
 
@@ -318,23 +360,99 @@ namespace metriko {
         verts.resize(nV);
         edges.resize(nE);
         halfs.resize(nH);
+        crnrs.resize(nC);
         METRIKO_PARALLEL_FOR
         for (int i = 0; i < nH; i++) {
             halfs[i] = Half{{i, this}};
             if (i < nF) faces[i] = Face{{i, this}};
             if (i < nV) verts[i] = Vert{{i, this}};
             if (i < nE) edges[i] = Edge{{i, this}};
+            if (i < nC) crnrs[i] = Crnr{{i, this}};
         }
+        loop2half.clear();
+        nL = 0;
+        isBV.assign(nV, false);
+        // halfedge angles around each vertex and the angle defect (hmesh.h:599-610): the angle
+        // sum in ring order from vert2half, each halfedge's running sum rescaled to 2 pi
         angleDefect = VecXd(nV);
+        heArgOnVert = VecXd(nH);
         METRIKO_PARALLEL_FOR
-        for (int v = 0; v < nV; v++) {     // hmesh.h:599-610
+        for (int v = 0; v < nV; v++) {
             double sum = 0;
             for (Half h : verts[v].adjHalfs()) {
+                heArgOnVert[h.id] = sum;
                 Row3d v1 = h.vec().normalized();
                 Row3d v2 = h.prev().twin().vec().normalized();
                 sum += std::acos(v1.dot(v2));
             }
             angleDefect[v] = TwoPI - sum;
+            for (Half h : verts[v].adjHalfs()) heArgOnVert[h.id] *= TwoPI / sum;
+        }
+        // vertex normals: area-weighted face normals summed in face order (hmesh.h:535-541), so
+        // each vertex adds its faces by ascending id; then the vertex frame (:543-549)
+        vertNormal = MatXd(nV, 3);
+        vertBasisX = MatXd(nV, 3);
+        vertBasisY = MatXd(nV, 3);
+        METRIKO_PARALLEL_FOR
+        for (int v = 0; v < nV; v++) {
+            int fs[64], k = 0;
+            bool small = true;
+            for (Half h : verts[v].adjHalfs()) {
+                if (k == 64) { small = false; break; }
+                fs[k++] = h.face().id;
+            }
+            std::vector<int> big;
+            const int* list = fs;
+            if (!small) {
+                for (Half h : verts[v].adjHalfs()) big.push_back(h.face().id);
+                std::sort(big.begin(), big.end());
+                list = big.data();
+                k = int(big.size());
+            } else {
+                std::sort(fs, fs + k);
+            }
+            Row3d n(0, 0, 0);
+            for (int q = 0; q < k; q++) {
+                const int f = list[q];
+                const double a = faceArea[f];
+                n = Row3d(n[0] + faceNormal(f, 0) * a, n[1] + faceNormal(f, 1) * a, n[2] + faceNormal(f, 2) * a);
+            }
+            n = n.normalized();
+            set_row3(vertNormal, v, n);
+            const Row3d d = row3(pos, head[vert2half[v]]) - row3(pos, v);
+            const Row3d x = (d - n * d.dot(n)).normalized();
+            set_row3(vertBasisX, v, x);
+            set_row3(vertBasisY, v, n.cross(x));
+        }
+        // dihedral angle and cotangent of each halfedge (hmesh.h:551-572), edge cotangents
+        dihedralArg = VecXd(nH);
+        halfCotan = VecXd(nH);
+        METRIKO_PARALLEL_FOR
+        for (int i = 0; i < nH; i++) {
+            const Half h{{i, this}};
+            const Row3d n1 = row3(faceNormal, face[i]), n2 = row3(faceNormal, face[twin[i]]);
+            const Row3d v = h.vec() / h.len();
+            dihedralArg[i] = std::atan2(v.dot(n1.cross(n2)), n1.dot(n2));
+            const Row3d vn = h.next().vec();
+            const Row3d vp = h.prev().vec() * -1;
+            halfCotan[i] = vp.dot(vn) / vp.cross(vn).norm();
+        }
+        edgeCotan = VecXd(nE);
+        METRIKO_PARALLEL_FOR
+        for (int e = 0; e < nE; e++) edgeCotan[e] = (halfCotan[edge2half[e]] + halfCotan[twin[edge2half[e]]]) * 0.5;
+        // dual areas (hmesh.h:574-585): barycentric and circumcentric, summed in ring order
+        baryDualArea = VecXd(nV);
+        circDualArea = VecXd(nV);
+        METRIKO_PARALLEL_FOR
+        for (int v = 0; v < nV; v++) {
+            double a1 = 0, a2 = 0;
+            for (Half h : verts[v].adjHalfs()) {
+                a1 += faceArea[h.face().id];
+                a2 += h.cot() * h.vec().squaredNorm();
+                a2 += h.prev().cot() * h.prev().vec().squaredNorm();
+            }
+            baryDualArea[v] = a1 / 3.;
+            circDualArea[v] = a2 * 0.125;
         }
     }
 }

@@ -291,6 +291,19 @@ int mtk_field_inputs(int32_t nV, int32_t nF, const double* V, const int32_t* F, 
                      double* area);
 
 /*
+ * Host only (no GPU): the vertex and edge geometry of Hmesh (hmesh.h:452-611 of the reference:
+ * the members vertNormal, vertBasisX, vertBasisY, baryDualArea, circDualArea, halfCotan,
+ * edgeCotan, dihedralArg, heArgOnVert, angleDefect) for a closed mesh, in the reference's
+ * halfedge / edge numbering (nE = 3 nF / 2, nH = 2 nE).  Every output may be NULL:
+ * vert_normal, vert_basis_x, vert_basis_y [3 nV]; bary_area, circ_area, angle_defect [nV];
+ * half_cotan, dihedral, he_arg_on_vert [nH]; edge_cotan [nE].
+ */
+int mtk_mesh_geometry(int32_t nV, int32_t nF, const double* V, const int32_t* F, double* vert_normal,
+                      double* vert_basis_x, double* vert_basis_y, double* bary_area, double* circ_area,
+                      double* half_cotan, double* edge_cotan, double* dihedral, double* he_arg_on_vert,
+                      double* angle_defect);
+
+/*
  * Host only (no GPU): the check at the end of RosyParameterization::integ()
  * (parameterization_integ.ipp:100-117, with G3 of :11-27) -- the mean over faces and functions
  * of |normalized(ext_k) - normalized(grad_k)|, grad_k the 3D gradient on the face of function k

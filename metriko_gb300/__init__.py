@@ -5,6 +5,6 @@ rounding (the numerical core of komietty/metriko), as hand-written sm_103a CUDA 
 Python here is plumbing for tests and benchmarks: `Context`, `pipeline`, `field_smoothest`.
 """
 from ._lib import (Context, MetrikoError, PREC_FP64, PREC_MIXED, field_smoothest, lib,  # noqa: F401
-                   field_inputs, field_solve, injective_barrier, local_injectivity, map_deviation, pipeline, seeded_init,
+                   field_inputs, field_solve, injective_barrier, local_injectivity, map_deviation, mesh_geometry, pipeline, seeded_init,
                    size_field_gradient, solve_opts, spmv_bench, topology_from_field)
 from . import meshgen  # noqa: F401

@@ -23,6 +23,7 @@ EXPORTS = [
     "mtk_seeded_init", "mtk_topology_from_field", "mtk_field_smoothest_noalloc", "mtk_size_field_gradient",
     "mtk_pipeline_size_field_gradient", "mtk_field_solve", "mtk_field_inputs", "mtk_field_spmv_bench",
     "mtk_injective_barrier", "mtk_local_injectivity", "mtk_map_deviation",
+    "mtk_mesh_geometry",
 ]
 
 
@@ -96,6 +97,7 @@ def lib():
                                             C.c_void_p, C.c_void_p, C.c_void_p]
         L.mtk_local_injectivity.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.POINTER(C.c_int32),
                                             C.POINTER(C.c_int32)]
+        L.mtk_mesh_geometry.argtypes = [C.c_int32, C.c_int32] + [C.c_void_p] * 12
         L.mtk_map_deviation.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_void_p, C.POINTER(C.c_double)]
         L.mtk_field_solve.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -245,6 +247,22 @@ def injective_barrier(ctx: Context, intrinsic_field, field, N=4, update_j=True):
                                        _ptr(dB) if update_j else None, _ptr(S) if update_j else None),
            "mtk_injective_barrier")
     return fB, dB, (S.reshape(-1, 4) if update_j else None)
+
+
+def mesh_geometry(V, F):
+    """mtk_mesh_geometry (host only): the vertex and edge geometry of the C++ Hmesh as a dict
+    (vertNormal, vertBasisX, vertBasisY, baryDualArea, circDualArea, halfCotan, edgeCotan,
+    dihedralArg, heArgOnVert, angleDefect)."""
+    V = np.ascontiguousarray(V, np.float64)
+    F = np.ascontiguousarray(F, np.int32)
+    nV, nF = len(V), len(F)
+    nE = 3 * nF // 2
+    out = dict(vertNormal=np.zeros((nV, 3)), vertBasisX=np.zeros((nV, 3)), vertBasisY=np.zeros((nV, 3)),
+               baryDualArea=np.zeros(nV), circDualArea=np.zeros(nV), halfCotan=np.zeros(2 * nE),
+               edgeCotan=np.zeros(nE), dihedralArg=np.zeros(2 * nE), heArgOnVert=np.zeros(2 * nE),
+               angleDefect=np.zeros(nV))
+    _check(lib().mtk_mesh_geometry(nV, nF, _ptr(V), _ptr(F), *[_ptr(out[k]) for k in out]), "mtk_mesh_geometry")
+    return out
 
 
 def map_deviation(cutV, cutF, cfn, ext, N=4):

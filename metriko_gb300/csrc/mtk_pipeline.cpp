@@ -6,6 +6,9 @@
 #include <cstdlib>
 #include <cstring>
 #include <future>
+#if defined(_OPENMP)
+#include <omp.h>
+#endif
 
 #include "metriko/core/igm/parameterization.h"
 #include "metriko/core/vectorfield/face_rosy_field.h"
@@ -13,6 +16,16 @@
 void mtk_set_last_error(const char* msg, const char* file, int line);
 
 using namespace metriko;
+
+namespace {
+// Host work that runs beside the GPU field solve uses a quarter of the cores for its parallel
+// loops, so that the field's own host steps keep most of them (per-thread OpenMP setting).
+void side_thread_cores() {
+#if defined(_OPENMP)
+    omp_set_num_threads(std::max(1, omp_get_num_procs() / 4));
+#endif
+}
+}
 
 extern "C" int mtk_pipeline_run(mtk_ctx* ctx, int32_t nV, int32_t nF, const double* Vb, const int32_t* Fb,
                                 const mtk_pipeline_opts* popts, const mtk_solve_opts* sopts, int32_t* singular,
@@ -57,6 +70,7 @@ extern "C" int mtk_pipeline_run(mtk_ctx* ctx, int32_t nV, int32_t nF, const doub
         // the seam search
         const bool seams = popts->stop_after != 1;
         auto pending = std::async(std::launch::async, [&m = *mesh, seams] {
+            side_thread_cores();
             m.finish();
             return seams ? seam_base(m) : SeamBase{};
         });
@@ -152,7 +166,7 @@ extern "C" int mtk_pipeline_size_field_gradient(mtk_ctx* ctx, int32_t nV, int32_
         std::memcpy(V.data(), Vb, sizeof(double) * 3 * size_t(nV));
         std::memcpy(F.data(), Fb, sizeof(int32_t) * 3 * size_t(nF));
         auto mesh = std::make_unique<Hmesh>(V, F, Hmesh::Deferred{});
-        auto pending = std::async(std::launch::async, [&m = *mesh] { m.finish(); return seam_base(m); });   // during the field solve
+        auto pending = std::async(std::launch::async, [&m = *mesh] { side_thread_cores(); m.finish(); return seam_base(m); });   // during the field solve
         FaceRosyField rawf(*mesh, 4, popts->field_type == 1 ? FieldType::CurvatureAligned : FieldType::Smoothest);
         SeamBase base = pending.get();
         rawf.computeMatching(MatchingType::Curl);
@@ -208,7 +222,7 @@ extern "C" int mtk_topology_from_field(int32_t nV, int32_t nF, const double* Vb,
         // computed on a host thread while the field is set up)
         auto mesh = std::make_unique<Hmesh>(V, F, Hmesh::Deferred{});
         stamp("hmesh");
-        auto pending = std::async(std::launch::async, [&m = *mesh] { m.finish(); return seam_base(m); });
+        auto pending = std::async(std::launch::async, [&m = *mesh] { side_thread_cores(); m.finish(); return seam_base(m); });
         FaceRosyField rawf(*mesh, 4);
         rawf.compressed = VecXc(nF);
         for (int f = 0; f < nF; f++) rawf.compressed[f] = complex(compressed[2 * f], compressed[2 * f + 1]);
@@ -288,4 +302,33 @@ extern "C" int mtk_map_deviation(int32_t nF, int32_t N, int32_t nCut, const int3
     std::memcpy(E.data(), ext, sizeof(double) * 3 * size_t(N) * nF);
     *deviation = map_deviation(V, F, C, E, N);
     return MTK_OK;
+}
+
+extern "C" int mtk_mesh_geometry(int32_t nV, int32_t nF, const double* Vb, const int32_t* Fb, double* vert_normal,
+                                 double* vert_basis_x, double* vert_basis_y, double* bary_area, double* circ_area,
+                                 double* half_cotan, double* edge_cotan, double* dihedral, double* he_arg_on_vert,
+                                 double* angle_defect) {
+    if (nV <= 0 || nF <= 0 || !Vb || !Fb) return MTK_ERR_BAD_INPUT;
+    try {
+        MatXd V(nV, 3);
+        MatXi F(nF, 3);
+        std::memcpy(V.data(), Vb, sizeof(double) * 3 * size_t(nV));
+        std::memcpy(F.data(), Fb, sizeof(int32_t) * 3 * size_t(nF));
+        Hmesh m(V, F);
+        auto put = [](double* dst, const double* src, size_t n) { if (dst) std::memcpy(dst, src, sizeof(double) * n); };
+        put(vert_normal, m.vertNormal.data(), 3 * size_t(nV));
+        put(vert_basis_x, m.vertBasisX.data(), 3 * size_t(nV));
+        put(vert_basis_y, m.vertBasisY.data(), 3 * size_t(nV));
+        put(bary_area, m.baryDualArea.data(), nV);
+        put(circ_area, m.circDualArea.data(), nV);
+        put(half_cotan, m.halfCotan.data(), m.nH);
+        put(edge_cotan, m.edgeCotan.data(), m.nE);
+        put(dihedral, m.dihedralArg.data(), m.nH);
+        put(he_arg_on_vert, m.heArgOnVert.data(), m.nH);
+        put(angle_defect, m.angleDefect.data(), nV);
+        return MTK_OK;
+    } catch (const std::exception& e) {
+        mtk_set_last_error(e.what(), __FILE__, __LINE__);
+        return MTK_ERR_BAD_INPUT;
+    }
 }

@@ -195,6 +195,50 @@ class Hmesh:
     def is_canonical(self, h):
         return self.edge2half[self.edge[h]] == h
 
+    def vertex_geometry(self):
+        """The rest of the reference's Hmesh constructor (hmesh.h:535-611) for a closed mesh:
+        vertex normals (area-weighted face normals accumulated face by face, then normalized),
+        vertex frames (x: the first outgoing edge projected to the tangent plane), dihedral angle
+        and cotangent per halfedge, edge cotangents, barycentric and circumcentric dual areas and
+        the halfedge angles around each vertex (running angle sum in ring order, rescaled to 2 pi).
+        Returns a dict with the reference's member names."""
+        V, F = self.pos, self.idx
+        nV, nH = self.nV, self.nH
+        vn = np.zeros((nV, 3))
+        fa = self.faceNormal * self.faceArea[:, None]
+        for f in range(self.nF):                 # face order, as the reference accumulates
+            for j in range(3):
+                vn[F[f, j]] = vn[F[f, j]] + fa[f]
+        vn = vn / _norm3(vn)[:, None]
+        d = V[self.head[self.vert2half]] - V
+        x = _normalized(d - _dot3(d, vn)[:, None] * vn)
+        vec = self.hvec
+        n1, n2 = self.faceNormal[self.face], self.faceNormal[self.face[self.twin]]
+        v = vec / _norm3(vec)[:, None]
+        dih = np.arctan2(_dot3(v, np.cross(n1, n2)), _dot3(n1, n2))
+        vnx = vec[self.next]
+        vpr = -vec[self.prev]
+        cot = _dot3(vpr, vnx) / _norm3(np.cross(vpr, vnx))
+        ecot = (cot[self.edge2half] + cot[self.twin[self.edge2half]]) * 0.5
+        bary, circ, varg = np.zeros(nV), np.zeros(nV), np.zeros(nH)
+        sq = _dot3(vec, vec)
+        ang = np.arccos(_dot3(_normalized(vec), _normalized(vec[self.twin[self.prev]])))
+        for u in range(nV):
+            a1 = a2 = s = 0.0
+            ring = self.ccw(self.vert2half[u])
+            for h in ring:
+                a1 += self.faceArea[self.face[h]]
+                a2 += cot[h] * sq[h]
+                a2 += cot[self.prev[h]] * sq[self.prev[h]]
+                varg[h] = s
+                s += ang[h]
+            bary[u], circ[u] = a1 / 3.0, a2 * 0.125
+            for h in ring:
+                varg[h] *= TWO_PI / s
+        return dict(vertNormal=vn, vertBasisX=x, vertBasisY=np.cross(vn, x), baryDualArea=bary,
+                    circDualArea=circ, halfCotan=cot, edgeCotan=ecot, dihedralArg=dih, heArgOnVert=varg,
+                    angleDefect=self.angleDefect)
+
     def ccw(self, h0):
         """Outgoing halfedges around tail(h0), ccw (AdjVH with ccw=true)."""
         out, h = [], h0

@@ -70,3 +70,25 @@ def test_field_inputs_match_oracle():
     assert np.array_equal(nbr, m.face[m.twin[m.FH]])
     assert np.abs(theta - (m.farg[m.FH] - m.farg[m.twin[m.FH]])).max() < 1e-12
     assert np.array_equal(area, m.faceArea)
+
+
+@pytest.mark.parametrize("name", ["ico3_noise", "torus_32x16", "genus2_s3"])
+def test_mesh_vertex_and_edge_geometry_matches_oracle(name):
+    """Hmesh's vertex frames, dual areas, cotangents, dihedral angles and vertex halfedge angles
+    (mtk_mesh_geometry) against the oracle: the algebraic ones bit for bit, the ones through
+    acos / atan2 to a few ulp (numpy's and the C library's functions may round differently)."""
+    V, F, _, _ = meshgen.workload(name)
+    g = M.mesh_geometry(V, F)
+    m = O.Hmesh(V, F)
+    o = m.vertex_geometry()
+    for k in ["vertNormal", "vertBasisX", "vertBasisY", "baryDualArea", "circDualArea", "halfCotan", "edgeCotan"]:
+        assert np.array_equal(g[k], o[k]), k
+    for k in ["dihedralArg", "heArgOnVert", "angleDefect"]:
+        assert np.abs(g[k] - o[k]).max() <= 1e-14, k
+    area = m.faceArea.sum()
+    assert abs(g["baryDualArea"].sum() - area) <= 1e-12 * area
+    assert abs(g["circDualArea"].sum() - area) <= 1e-12 * area      # cotangent identity, closed mesh
+    assert abs(g["angleDefect"].sum() - 2 * np.pi * (m.nV - m.nE + m.nF)) < 1e-9
+    X, Y, Nn = g["vertBasisX"], g["vertBasisY"], g["vertNormal"]
+    assert np.abs(np.einsum("ij,ij->i", X, Nn)).max() < 1e-12 and np.abs(np.einsum("ij,ij->i", X, Y)).max() < 1e-12
+    assert np.abs(np.linalg.norm(Y, axis=1) - 1).max() < 1e-12
