@@ -3,7 +3,7 @@
 //
 // The reference spells its host API with Eigen types (include/metriko/core/common/typedef.h:13-40
 // in metriko): complex, Row3d, VecXi/VecXd/VecXc, MatXi/MatXd/MatXc, SprsD/SprsC, TripD/TripC.
-// Eigen is not part of this build, so the same names are provided here with only the
+// Eigen is not a dependency of this library, so the same names are provided here with only the
 // operations the field + integration + IGM path needs.  Dense matrices are row-major.
 //
 #ifndef METRIKO_TYPEDEF_H

@@ -130,7 +130,7 @@ namespace metriko {
                              const double ratio = 0.02)
             : raw(raw_), cut(cut_), ext(ext_), singlars(sing_), matching(matching_), seam(seam_), gridscale(ratio) {
             N = degree;
-            if (N % 2 != 0) throw std::invalid_argument("odd N is not part of this build");
+            if (N % 2 != 0) throw std::invalid_argument("odd N is not supported (N = 4 and other even N only)");
             n = N / 2;
             lreductor = MatXi(N, n, 0);
             for (int i = 0; i < n; i++) { lreductor(i, i) = 1; lreductor(n + i, i) = -1; }
@@ -463,7 +463,7 @@ namespace metriko {
         d.nSingular = singularIdcs.size(); d.singularIdcs = singularIdcs.data();
         d.nInteger = integerIdcs.size(); d.integerIdcs = integerIdcs.data();
         d.seamless = seamless; d.roundSeams = roundSeams;
-        if (localInjectivity) throw std::invalid_argument("localInjectivity is not part of this build");
+        if (localInjectivity) throw std::invalid_argument("localInjectivity has no GPU solver (its barrier pieces are mtk_injective_barrier / mtk_local_injectivity)");
     }
 
     inline void RosyParameterization::build_target(IntegSystem& sys) const {

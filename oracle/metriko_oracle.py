@@ -1,7 +1,7 @@
 """FP64 CPU ORACLE for metriko's field + seamless-integration + IGM path.
 
-TEST INFRASTRUCTURE ONLY.  This module is the checker for the CUDA path and the timed CPU
-baseline.  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference arm
+TEST INFRASTRUCTURE ONLY.  This module is the reference result the CUDA path is compared
+against and the timed CPU baseline.  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference arm
 may import it.  Nothing in the product (metriko_gb300/, include/) imports it.
 
 What it restates (reference paths are relative to the metriko project root):
