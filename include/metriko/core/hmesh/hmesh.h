@@ -63,6 +63,10 @@ namespace metriko {
         AdjIter<AdjVH> adjHalfs(bool ccw = true) const;
         AdjIter<AdjVH> adjHalfs(Half h, bool ccw = true) const;
     };
+    // boundary loop (closed meshes have none: Hmesh::loops stays empty)
+    struct Loop : Elem {
+        Half half() const;
+    };
     // corner c of face f sits at F(f, c - 3f); its halfedge is the one opposite that vertex
     struct Crnr : Elem {
         Half half() const;
@@ -110,6 +114,7 @@ namespace metriko {
         MatXd vertBasisX, vertBasisY, vertNormal;
         VecXd baryDualArea, circDualArea, halfCotan, edgeCotan, dihedralArg, heArgOnVert;
         std::vector<Crnr> crnrs;
+        std::vector<Loop> loops;
         std::vector<int> loop2half;
         std::vector<bool> isBV;
 
@@ -168,6 +173,7 @@ namespace metriko {
     inline Row3d Vert::normal() const { return row3(m->vertNormal, id); }
     inline double Vert::baryArea() const { return m->baryDualArea[id]; }
     inline double Vert::circArea() const { return m->circDualArea[id]; }
+    inline Half Loop::half() const { return {{m->loop2half[id], m}}; }
     inline Half Crnr::half() const { return {{m->crnr2half[id], m}}; }
     inline Vert Crnr::vert() const { return half().prev().tail(); }
     inline Face Crnr::face() const { return half().face(); }
@@ -370,6 +376,7 @@ namespace metriko {
             if (i < nC) crnrs[i] = Crnr{{i, this}};
         }
         loop2half.clear();
+        loops.clear();
         nL = 0;
         isBV.assign(nV, false);
         // halfedge angles around each vertex and the angle defect (hmesh.h:599-610): the angle
