@@ -18,8 +18,14 @@
 #include "metriko/core/common/typedef.h"
 
 namespace metriko {
+    // Rows in order, each kept when its part orthogonal to the rows kept before (modified
+    // Gram-Schmidt, two passes) keeps more than tol of its norm.  Each basis vector is walked over
+    // its nonzero columns only: the skipped terms are exact zeros, so every nonzero value (and
+    // every decision) is the one of the dense loops; constraint rows have a handful of nonzeros
+    // and the basis vectors stay sparse.
     inline std::vector<int> independent_rows(const MatXd& C, double tol = 1e-9) {
         std::vector<std::vector<double>> basis;
+        std::vector<std::vector<int>> support;
         std::vector<int> keep;
         for (int i = 0; i < C.rows(); i++) {
             std::vector<double> r(C.row(i), C.row(i) + C.cols());
@@ -28,17 +34,24 @@ namespace metriko {
             n0 = std::sqrt(n0);
             if (n0 == 0) continue;
             for (int pass = 0; pass < 2; pass++)
-                for (auto& q : basis) {
+                for (size_t b = 0; b < basis.size(); b++) {
+                    const std::vector<double>& q = basis[b];
+                    const std::vector<int>& nz = support[b];
                     double d = 0;
-                    for (size_t j = 0; j < r.size(); j++) d += q[j] * r[j];
-                    for (size_t j = 0; j < r.size(); j++) r[j] -= d * q[j];
+                    for (int j : nz) d += q[j] * r[j];
+                    for (int j : nz) r[j] -= d * q[j];
                 }
             double n = 0;
             for (double v : r) n += v * v;
             n = std::sqrt(n);
             if (n > tol * n0) {
-                for (double& v : r) v /= n;
+                std::vector<int> nz;
+                for (size_t j = 0; j < r.size(); j++) {
+                    r[j] /= n;
+                    if (r[j] != 0) nz.push_back(int(j));
+                }
                 basis.push_back(std::move(r));
+                support.push_back(std::move(nz));
                 keep.push_back(i);
             }
         }
@@ -71,24 +84,52 @@ namespace metriko {
         std::iota(colq.begin(), colq.end(), 0);
         double maxpivot = 0;
         int nzp = size;
+        // The pivot is the first maximum of |a_ij| over the trailing block in column-major order,
+        // i.e. the maximum with the smallest (column, row).  Rows are scanned in parallel (each
+        // thread keeps its best under that order, the bests are merged under it too) and the
+        // trailing rows are eliminated in parallel; every entry gets the arithmetic of the serial
+        // loops, so the factors do not depend on the thread count.
+        struct Piv { double a; int i, j; };
+        auto better = [](const Piv& x, const Piv& y) {   // x before y
+            if (x.a != y.a) return x.a > y.a;
+            if (x.j != y.j) return x.j < y.j;
+            return x.i < y.i;
+        };
         for (int k = 0; k < size; k++) {
-            double best = -1;
-            int pr = k, pc = k;
-            for (int j = k; j < cols; j++)
-                for (int i = k; i < rows; i++) {
-                    double a = std::fabs(A(i, j));
-                    if (a > best) { best = a; pr = i; pc = j; }
+            Piv best{-1.0, k, k};
+#if defined(_OPENMP)
+            #pragma omp parallel if ((long long)(rows - k) * (cols - k) > 65536)
+            {
+                Piv mine{-1.0, k, k};
+                #pragma omp for schedule(static) nowait
+                for (int i = k; i < rows; i++)
+                    for (int j = k; j < cols; j++) {
+                        const Piv c{std::fabs(A(i, j)), i, j};
+                        if (better(c, mine)) mine = c;
+                    }
+                #pragma omp critical(metriko_fullpiv)
+                if (better(mine, best)) best = mine;
+            }
+#else
+            for (int i = k; i < rows; i++)
+                for (int j = k; j < cols; j++) {
+                    const Piv c{std::fabs(A(i, j)), i, j};
+                    if (better(c, best)) best = c;
                 }
-            if (best == 0.0) { nzp = k; break; }
-            maxpivot = std::max(maxpivot, best);
+#endif
+            const int pr = best.i, pc = best.j;
+            if (best.a == 0.0) { nzp = k; break; }
+            maxpivot = std::max(maxpivot, best.a);
             if (pr != k) for (int j = 0; j < cols; j++) std::swap(A(k, j), A(pr, j));
             if (pc != k) { for (int i = 0; i < rows; i++) std::swap(A(i, k), A(i, pc)); std::swap(colq[k], colq[pc]); }
             if (k < rows - 1) for (int i = k + 1; i < rows; i++) A(i, k) /= A(k, k);
-            if (k < size - 1)
+            if (k < size - 1) {
+                #pragma omp parallel for schedule(static) if ((long long)(rows - k) * (cols - k) > 65536)
                 for (int i = k + 1; i < rows; i++) {
-                    double l = A(i, k);
+                    const double l = A(i, k);
                     for (int j = k + 1; j < cols; j++) A(i, j) -= l * A(k, j);
                 }
+            }
         }
         const double thr = std::numeric_limits<double>::epsilon() * size * maxpivot;
         std::vector<int> piv;
@@ -99,9 +140,10 @@ namespace metriko {
         MatXd U(rank, cols, 0.0);
         for (int i = 0; i < rank; i++) for (int j = i; j < cols; j++) U(i, j) = A(piv[i], j);
         for (int i = 0; i < rank; i++) if (piv[i] != i) for (int r = 0; r < rank; r++) std::swap(U(r, i), U(r, piv[i]));
-        // back substitution U11 X = U12, stored in the trailing columns of U
-        for (int i = rank - 1; i >= 0; i--)
-            for (int j = 0; j < dimker; j++) {
+        // back substitution U11 X = U12, stored in the trailing columns of U (columns independent)
+        METRIKO_PARALLEL_FOR
+        for (int j = 0; j < dimker; j++)
+            for (int i = rank - 1; i >= 0; i--) {
                 double s = U(i, rank + j);
                 for (int k = i + 1; k < rank; k++) s -= U(i, k) * U(k, rank + j);
                 U(i, rank + j) = s / U(i, i);
