@@ -92,3 +92,19 @@ def test_mesh_vertex_and_edge_geometry_matches_oracle(name):
     X, Y, Nn = g["vertBasisX"], g["vertBasisY"], g["vertNormal"]
     assert np.abs(np.einsum("ij,ij->i", X, Nn)).max() < 1e-12 and np.abs(np.einsum("ij,ij->i", X, Y)).max() < 1e-12
     assert np.abs(np.linalg.norm(Y, axis=1) - 1).max() < 1e-12
+
+
+def test_constraint_reduction_with_many_singularities():
+    """A noisy level-5 sphere (338 singularities, 1,652 constraint rows): the host's sparse
+    Gram-Schmidt row selection and parallel full-pivot kernel give the oracle's dense results
+    (constrained variables nJ and kernel dimension nZ)."""
+    V, F, ratio, rs = meshgen.workload("ico5_noise")
+    ref = O.pipeline(V, F, ratio=ratio, round_seams=rs, stop_after="setup")
+    st = ref["setup"]
+    Cfull = O.structural_product(st["constraint"], st["uncompress"])
+    Cr = Cfull[O.independent_rows(Cfull)].tocsr()
+    uj = np.unique(Cr.indices)
+    K = O.fullpiv_kernel(Cr[:, uj].toarray())
+    res = M.topology_from_field(V, F, ref["compressed"], ratio, rs)
+    assert res["counts"]["nS"] > 300
+    assert res["counts"]["nJ"] == len(uj) and res["counts"]["nZ"] == K.shape[1]
