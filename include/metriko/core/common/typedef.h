@@ -219,6 +219,7 @@ namespace metriko {
         }
         std::vector<T> operator*(const std::vector<T>& x) const {
             std::vector<T> y(nr, T(0));
+            METRIKO_PARALLEL_FOR
             for (int i = 0; i < nr; i++) {
                 T s(0);
                 for (int p = ptr[i]; p < ptr[i + 1]; p++) s += val[p] * x[idx[p]];
