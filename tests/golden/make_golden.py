@@ -3,7 +3,7 @@
 The reference (komietty/metriko) cannot be built here and ships no tests or golden data, so
 these fixtures pin the FP64 CPU oracle's outputs on small seeded meshes; the GPU tests check
 the CUDA path against them and the CPU tests check that the oracle still reproduces them.
-Run:  python tests/golden/make_golden.py
+Run:  python tests/golden/make_golden.py [name ...]   (all fixtures when no name is given)
 """
 import sys
 from pathlib import Path
@@ -16,11 +16,11 @@ sys.path.insert(0, str(ROOT))
 from metriko_gb300 import meshgen  # noqa: E402
 from oracle import metriko_oracle as O  # noqa: E402
 
-NAMES = ["ico2_noise", "ico3_noise", "torus_32x16"]
+NAMES = ["ico2_noise", "ico3_noise", "torus_32x16", "genus2_s3"]
 
 
-def main():
-    for name in NAMES:
+def main(names):
+    for name in names:
         V, F, ratio, rs = meshgen.workload(name)
         out = O.pipeline(V, F, ratio=ratio, round_seams=rs)
         info = out["info"]
@@ -35,4 +35,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:] or NAMES)
