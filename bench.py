@@ -246,7 +246,10 @@ def run_ours(args):
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1) if achieved else None,
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
-                     "peak_kind": peak_kind, "traffic": None},
+                     "peak_kind": peak_kind, "traffic": None,
+                     "traffic_ncu": ("igm_pcg<float> at 1.3M faces: 429 MB DRAM read+write per PCG iteration "
+                                     "(one 78-iteration launch: 33.9 GB in 19.1 ms), against about 460 MB of "
+                                     "algorithmic bytes per iteration: profiles/igm_pcg_f32_ico8_sh8.md")},
         "spmv": spmv,
         "clocks": clocks,
         "cpu_baseline": cpu,
