@@ -108,3 +108,40 @@ def test_constraint_reduction_with_many_singularities():
     res = M.topology_from_field(V, F, ref["compressed"], ratio, rs)
     assert res["counts"]["nS"] > 300
     assert res["counts"]["nJ"] == len(uj) and res["counts"]["nZ"] == K.shape[1]
+
+
+def _projected_field(V, F, a=(0.3, -0.2, 1.0)):
+    """Compressed 4-RoSy field (unit, 4th power) of the tangential projection of the direction a,
+    in each face's frame (x along F[f,1] - F[f,0])."""
+    p0, p1, p2 = V[F[:, 0]], V[F[:, 1]], V[F[:, 2]]
+    bx = p1 - p0
+    bx /= np.linalg.norm(bx, axis=1, keepdims=True)
+    n = np.cross(p1 - p0, p2 - p0)
+    n /= np.linalg.norm(n, axis=1, keepdims=True)
+    by = np.cross(n, bx)
+    a = np.asarray(a, float) / np.linalg.norm(a)
+    d = a - (n @ a)[:, None] * n
+    z = np.einsum("ij,ij->i", d, bx) + 1j * np.einsum("ij,ij->i", d, by)
+    return (z / np.abs(z)) ** 4
+
+
+def test_host_topology_at_the_benchmark_size():
+    """The host stages on the 1.3M-face benchmark mesh (two host threads, parallel edge topology)
+    through size-independent properties: the singular indices sum to 4 chi, the seam is a tree
+    that reaches every singular vertex, the cut mesh is a disk and the counts are consistent."""
+    V, F, ratio, rs = meshgen.workload("ico8_sh8")
+    res = M.topology_from_field(V, F, _projected_field(V, F), ratio, rs)
+    c = res["counts"]
+    assert c["nV"] == 655362 and c["nE"] == 1966080
+    assert res["singular"].sum() == 8
+    m_edges = np.sort(np.concatenate([F[:, [0, 1]], F[:, [1, 2]], F[:, [2, 0]]]), axis=1)
+    ev = np.unique(m_edges, axis=0)                     # edge_topology numbering: sorted (lo, hi)
+    E = ev[res["seam"]]
+    verts = np.unique(E)
+    assert len(E) == len(verts) - 1                     # a tree
+    assert set(np.flatnonzero(res["singular"])) <= set(verts.tolist())
+    assert c["nCut"] == c["nV"] + len(E) - 1            # each tree edge opens into two boundary edges
+    cutF = res["cutF"]
+    ce = np.unique(np.sort(np.concatenate([cutF[:, [0, 1]], cutF[:, [1, 2]], cutF[:, [2, 0]]]), axis=1), axis=0)
+    assert c["nCut"] - len(ce) + len(cutF) == 1         # a disk
+    assert c["nS"] == int((res["singular"] != 0).sum()) and c["nFull"] == 2 * (c["nV"] + c["nT"])
