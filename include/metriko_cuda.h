@@ -27,6 +27,15 @@
  *   mtk_pipeline_run      <- the example_igm.cpp:13-31 call sequence (Hmesh -> field ->
  *                            matching -> seam -> cut -> combing -> RosyParameterization
  *                            setup()/integ()) as one call with host buffers
+ *   mtk_mesh_geometry     <- the vertex and edge geometry of the Hmesh constructor
+ *                            (include/metriko/core/hmesh/hmesh.h:535-611), host only
+ *   mtk_map_deviation     <- the closing check of RosyParameterization::integ()
+ *                            (parameterization_integ.ipp:100-117), host only
+ *   mtk_injective_barrier, mtk_local_injectivity <- InjectiveBarrier
+ *                            (iterative_rounding/injective_barrier.h:10-110) and
+ *                            locally_injectivity_check (parameterization_integ.ipp:46-63)
+ * The direct caller of iterative_rounding passes the descriptor mtk_igm_desc that
+ * RosyParameterization::build_system fills, not an assembled Cfull / G2.
  */
 #ifndef METRIKO_CUDA_H
 #define METRIKO_CUDA_H
