@@ -1,7 +1,12 @@
 //
+// Restates parts of metriko (https://github.com/komietty/metriko),
+// Copyright (C) 2025 Saki Komikado <komietty@gmail.com>.
+// This Source Code Form is subject to the terms of the Mozilla Public License v.2.0
+// (https://mozilla.org/MPL/2.0/).
+//
 // metriko-gb300: halfedge mesh (DCEL) with the reference's numbering.
 //
-// Replaces metriko include/metriko/core/hmesh/hmesh.h:24-611 (struct Hmesh, handles, dcel()).
+// Replaces metriko include/metriko/core/hmesh/hmesh.h:24-569 (struct Hmesh, handles, dcel()).
 // Only closed, consistently oriented, edge-manifold triangle meshes are accepted (the
 // workloads of this path); anything else throws std::invalid_argument.
 //
@@ -10,8 +15,8 @@
 //    lexicographically, one edge per distinct (min, max); edge2face(e,0) is the face in which
 //    the edge runs min->max (restated from libigl's documented behaviour);
 //  * halfedge 2e starts at edge2vert(e,0) inside edge2face(e,0), 2e+1 is its twin;
-//  * vert2half[v] is the last halfedge written for v in edge order (hmesh.h:313-323);
-//  * face2half[f] runs F(f,0)->F(f,1) (hmesh.h:421).
+//  * vert2half[v] is the last halfedge written for v in edge order (hmesh.h:240-311, :377);
+//  * face2half[f] runs F(f,0)->F(f,1) (hmesh.h:379).
 //
 #ifndef METRIKO_HMESH_H
 #define METRIKO_HMESH_H
@@ -108,7 +113,7 @@ namespace metriko {
         MatXi face2half3;  // nF x 3, halfedge of face f on face2edge(f,j)
         MatXd faceBasisX, faceBasisY, faceNormal, baryCenter;
         VecXd faceArea, angleDefect, heArgOnFace;
-        // filled by finish() (hmesh.h:452-611 of the reference): vertex frames, dual areas,
+        // filled by finish() (hmesh.h:444-568 of the reference): vertex frames, dual areas,
         // cotangents, dihedral angles, halfedge angles around vertices, corner handles;
         // closed meshes only, so there are no boundary loops and no boundary vertices
         MatXd vertBasisX, vertBasisY, vertNormal;
@@ -299,7 +304,7 @@ namespace metriko {
             edge[2 * e] = edge[2 * e + 1] = e;
             edge2half[e] = 2 * e;
         }
-        // last write wins in edge order (dcel, hmesh.h:314-323): halfedge 2e + s is written for
+        // last write wins in edge order (dcel, hmesh.h:240-311, :377): halfedge 2e + s is written for
         // edge2vert(e, s), so the survivor is the largest halfedge id starting at the vertex
         METRIKO_PARALLEL_FOR
         for (int h = 0; h < nH; h++) {
@@ -323,7 +328,7 @@ namespace metriko {
                 prev[face2half3(f, (j + 1) % 3)] = face2half3(f, j);
             }
             face2half[f] = face2half3(f, 0);
-            // corner 3f+it is the halfedge opposite F(f,it) (hmesh.h:471-484)
+            // corner 3f+it is the halfedge opposite F(f,it) (hmesh.h:429-442)
             for (int it = 0; it < 3; it++) {
                 int h = face2half3(f, (it + 1) % 3);
                 crnr2half[3 * f + it] = h;
@@ -348,7 +353,7 @@ namespace metriko {
             faceArea[f] = n.norm() * 0.5;
         }
         METRIKO_PARALLEL_FOR
-        for (int f = 0; f < nF; f++) {     // hmesh.h:522-531
+        for (int f = 0; f < nF; f++) {     // hmesh.h:480-489
             double sum = 0;
             Row3d bx = row3(faceBasisX, f);
             for (int j = 0; j < 3; j++) {
@@ -379,7 +384,7 @@ namespace metriko {
         loops.clear();
         nL = 0;
         isBV.assign(nV, false);
-        // halfedge angles around each vertex and the angle defect (hmesh.h:599-610): the angle
+        // halfedge angles around each vertex and the angle defect (hmesh.h:557-568): the angle
         // sum in ring order from vert2half, each halfedge's running sum rescaled to 2 pi
         angleDefect = VecXd(nV);
         heArgOnVert = VecXd(nH);
@@ -395,8 +400,8 @@ namespace metriko {
             angleDefect[v] = TwoPI - sum;
             for (Half h : verts[v].adjHalfs()) heArgOnVert[h.id] *= TwoPI / sum;
         }
-        // vertex normals: area-weighted face normals summed in face order (hmesh.h:535-541), so
-        // each vertex adds its faces by ascending id; then the vertex frame (:543-549)
+        // vertex normals: area-weighted face normals summed in face order (hmesh.h:491-498), so
+        // each vertex adds its faces by ascending id; then the vertex frame (:500-506)
         vertNormal = MatXd(nV, 3);
         vertBasisX = MatXd(nV, 3);
         vertBasisY = MatXd(nV, 3);
@@ -431,7 +436,7 @@ namespace metriko {
             set_row3(vertBasisX, v, x);
             set_row3(vertBasisY, v, n.cross(x));
         }
-        // dihedral angle and cotangent of each halfedge (hmesh.h:551-572), edge cotangents
+        // dihedral angle and cotangent of each halfedge (hmesh.h:508-533), edge cotangents
         dihedralArg = VecXd(nH);
         halfCotan = VecXd(nH);
         METRIKO_PARALLEL_FOR
@@ -447,7 +452,7 @@ namespace metriko {
         edgeCotan = VecXd(nE);
         METRIKO_PARALLEL_FOR
         for (int e = 0; e < nE; e++) edgeCotan[e] = (halfCotan[edge2half[e]] + halfCotan[twin[edge2half[e]]]) * 0.5;
-        // dual areas (hmesh.h:574-585): barycentric and circumcentric, summed in ring order
+        // dual areas (hmesh.h:535-546): barycentric and circumcentric, summed in ring order
         baryDualArea = VecXd(nV);
         circDualArea = VecXd(nV);
         METRIKO_PARALLEL_FOR

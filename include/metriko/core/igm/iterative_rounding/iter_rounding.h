@@ -1,4 +1,9 @@
 //
+// Restates parts of metriko (https://github.com/komietty/metriko),
+// Copyright (C) 2025 Saki Komikado <komietty@gmail.com>.
+// This Source Code Form is subject to the terms of the Mozilla Public License v.2.0
+// (https://mozilla.org/MPL/2.0/).
+//
 // metriko-gb300: iterative rounding entry point.
 //
 // Replaces metriko include/metriko/core/igm/iterative_rounding/iter_rounding.h:33-113 (and the

@@ -1,4 +1,9 @@
 //
+// Restates parts of metriko (https://github.com/komietty/metriko),
+// Copyright (C) 2025 Saki Komikado <komietty@gmail.com>.
+// This Source Code Form is subject to the terms of the Mozilla Public License v.2.0
+// (https://mozilla.org/MPL/2.0/).
+//
 // metriko-gb300: seamless parameterization front-end (RosyParameterization).
 //
 // Replaces metriko include/metriko/core/igm/parameterization.h:11-152,
@@ -165,7 +170,7 @@ namespace metriko {
             return h0;
         }
 
-        // parameterization_setup.ipp:3-8
+        // parameterization_setup.ipp:3-9
         void compute_he2matching() {
             he2matching = VecXi(raw.nH);
             for (int h = 0; h < raw.nH; h++) {
@@ -174,7 +179,7 @@ namespace metriko {
             }
         }
 
-        // parameterization_setup.ipp:10-49
+        // parameterization_setup.ipp:11-50
         void compute_he2transidx() {
             he2transidx = VecXi(raw.nH, 32767);
             std::vector<int> valence(raw.nV, 0);
@@ -404,7 +409,7 @@ namespace metriko {
         reduce_to_linearly_independent(Cfull);
         const int nFull = n * nR;
 
-        // ---- UFull = permutation * blockdiag(I, kernel(CSmall))  (iter_rounding_init.h:195-251)
+        // ---- UFull = permutation * blockdiag(I, kernel(CSmall))  (iter_rounding_init.h:98-154)
         std::vector<int>& uniqueJ = sys.uniqueJ;
         uniqueJ.clear();
         {

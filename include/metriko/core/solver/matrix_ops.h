@@ -7,7 +7,7 @@
 // Both span the same row space, so the constraint null space is identical.
 //
 // fullpiv_kernel restates Eigen FullPivLU::kernel() as used by NaiveIntegration
-// (iter_rounding_init.h:226-228): LU with complete pivoting (pivot = first maximum |a_ij| of the
+// (iter_rounding_init.h:129-130): LU with complete pivoting (pivot = first maximum |a_ij| of the
 // trailing block in column-major order), rank threshold eps * min(rows, cols) * max pivot,
 // kernel basis = identity on the free columns and -U11^-1 U12 on the pivot columns.
 //

@@ -1,7 +1,12 @@
 //
+// Restates parts of metriko (https://github.com/komietty/metriko),
+// Copyright (C) 2025 Saki Komikado <komietty@gmail.com>.
+// This Source Code Form is subject to the terms of the Mozilla Public License v.2.0
+// (https://mozilla.org/MPL/2.0/).
+//
 // metriko-gb300: face-based N-RoSy field, matching, singularities, seams, combing.
 //
-// Replaces metriko include/metriko/core/vectorfield/face_rosy_field.h:16-386.
+// Replaces metriko include/metriko/core/vectorfield/face_rosy_field.h:16-360.
 //  * The smoothest field (connectionLaplacian + galerkinMassMatrix + solveSmallestEig, :43-110)
 //    is computed on the GPU by mtk_field_smoothest (assembly, PCG inverse iteration).
 //  * Matching, singularities, seams, combing and the extrinsic field are host algorithms with
@@ -37,7 +42,7 @@ namespace metriko {
             if (compressed.size() == m.nF) set_field_from_compressed();
         }
 
-        // face_rosy_field.h:63-69: field(f,i) = pow(polar(1, arg c_f), 1/N) * pow(r, i)
+        // face_rosy_field.h:37-43: field(f,i) = pow(polar(1, arg c_f), 1/N) * pow(r, i)
         void set_field_from_compressed() {
             const complex r = std::polar(1., TwoPI / rosyN);
             std::vector<complex> rpow(rosyN);   // pow(r, i), the same factor for every face
@@ -51,7 +56,7 @@ namespace metriko {
         }
 
         // Inputs of the device assembly: neighbour across each face halfedge and
-        // theta = farg(h) - farg(twin h); L(f, nbr) = -(-e^{i theta})^N (face_rosy_field.h:78-96).
+        // theta = farg(h) - farg(twin h); L(f, nbr) = -(-e^{i theta})^N (face_rosy_field.h:52-75).
         void assembly_inputs(std::vector<int>& nbr, std::vector<double>& theta) const {
             nbr.resize(3 * size_t(mesh.nF));
             theta.resize(3 * size_t(mesh.nF));
@@ -109,7 +114,7 @@ namespace metriko {
             return D;
         }
 
-        // face_rosy_field.h:23-32 (lambda = 0): D (squared for N = 4), rhs = M D / sqrt|D^H M D|,
+        // face_rosy_field.h:25-33 (lambda = 0): D (squared for N = 4), rhs = M D / sqrt|D^H M D|,
         // compressed = L^-1 rhs by one device solve (mtk_field_solve).
         VecXc solveCurvatureAligned() {
             if (rosyN != 2 && rosyN != 4) throw std::invalid_argument("CurvatureAligned needs N = 2 or 4");
@@ -136,7 +141,7 @@ namespace metriko {
             return c;
         }
 
-        void computeConnection() {      // face_rosy_field.h:135-143
+        void computeConnection() {      // face_rosy_field.h:109-117
             connection = VecXc(mesh.nE, complex(0, 0));
             METRIKO_PARALLEL_FOR
             for (int e = 0; e < mesh.nE; e++) {
@@ -148,7 +153,7 @@ namespace metriko {
             }
         }
 
-        void computeSingular(const VecXd& effort) {   // face_rosy_field.h:126-133
+        void computeSingular(const VecXd& effort) {   // face_rosy_field.h:100-107
             singular = VecXi(mesh.nV, 1);
             METRIKO_PARALLEL_FOR
             for (int v = 0; v < mesh.nV; v++) {
@@ -162,7 +167,7 @@ namespace metriko {
             }
         }
 
-        void computeMatching(const MatchingType type) {   // face_rosy_field.h:145-161
+        void computeMatching(const MatchingType type) {   // face_rosy_field.h:119-135
             computeConnection();
             matching = VecXi(mesh.nE, -1);
             VecXd effort = VecXd::Zero(mesh.nE);
@@ -172,7 +177,7 @@ namespace metriko {
         }
 
     private:
-        void pMatching(VecXd& effort) {    // face_rosy_field.h:164-193
+        void pMatching(VecXd& effort) {    // face_rosy_field.h:138-167
             METRIKO_PARALLEL_FOR
             for (int e = 0; e < mesh.nE; e++) {
                 int f0 = mesh.edge2face(e, 0), f1 = mesh.edge2face(e, 1);
@@ -194,7 +199,7 @@ namespace metriko {
             }
         }
 
-        void cMatching(VecXd& effort) {    // face_rosy_field.h:195-228
+        void cMatching(VecXd& effort) {    // face_rosy_field.h:169-202
             METRIKO_PARALLEL_FOR
             for (int e = 0; e < mesh.nE; e++) {
                 int iM = 0;
@@ -222,7 +227,7 @@ namespace metriko {
         }
     };
 
-    // face_rosy_field.h:233-275
+    // face_rosy_field.h:207-249
     inline std::unique_ptr<FaceRosyField> compute_combbed_field(const FaceRosyField& fld, const std::vector<bool>& seam) {
         const Hmesh& m = fld.mesh;
         const int N = fld.rosyN;
@@ -268,7 +273,7 @@ namespace metriko {
         return F;
     }
 
-    // face_rosy_field.h:277-290 (N = 4)
+    // face_rosy_field.h:251-264 (N = 4)
     inline MatXd compute_extrinsic_field(const Hmesh& mesh, const FaceRosyField& fld, int rosyN) {
         MatXd ext(mesh.nF, 3 * rosyN);
         METRIKO_PARALLEL_FOR
@@ -449,7 +454,7 @@ namespace metriko {
         return b;
     }
 
-    // face_rosy_field.h:294-369 (cut_mesh_with_singularities), continuing from seam_base(m)
+    // face_rosy_field.h:268-343 (cut_mesh_with_singularities), continuing from seam_base(m)
     inline void cut_mesh_with_singularities(const Hmesh& m, const VecXi& singularities, SeamBase&& base, MatXi& cuts) {
         const MatXi& F = m.idx;
         const MatXi& TT = base.TT;
@@ -520,12 +525,12 @@ namespace metriko {
         }
     }
 
-    // face_rosy_field.h:294-369 (cut_mesh_with_singularities)
+    // face_rosy_field.h:268-343 (cut_mesh_with_singularities)
     inline void cut_mesh_with_singularities(const Hmesh& m, const VecXi& singularities, MatXi& cuts) {
         cut_mesh_with_singularities(m, singularities, seam_base(m), cuts);
     }
 
-    // face_rosy_field.h:371-386, with seam_base(f.mesh) computed beforehand
+    // face_rosy_field.h:345-360, with seam_base(f.mesh) computed beforehand
     inline std::vector<bool> compute_seam(const FaceRosyField& f, SeamBase&& base) {
         std::vector<bool> seam(f.mesh.nE, false);
         std::vector<int> sv;
@@ -537,7 +542,7 @@ namespace metriko {
         return seam;
     }
 
-    // face_rosy_field.h:371-386
+    // face_rosy_field.h:345-360
     inline std::vector<bool> compute_seam(const FaceRosyField& f) { return compute_seam(f, seam_base(f.mesh)); }
 }
 

@@ -21,7 +21,7 @@ namespace metriko::gpu {
     struct Options {
         mtk_solve_opts solve{};
         int seed = 0;           // start vector of the power iteration
-        int n_iter = 50;        // power iterations (sparse_linear_solver.h:452, nIter = 50)
+        int n_iter = 50;        // power iterations (sparse_linear_solver.h:29, nIter = 50)
         int device = 0;
         Options() { mtk_default_opts(&solve); }
     };

@@ -8,10 +8,10 @@
  *
  * Reference interfaces replaced (paths inside the metriko project):
  *   mtk_field_smoothest   <- FaceRosyField(const Hmesh&, int, FieldType::Smoothest)
- *                            (include/metriko/core/vectorfield/face_rosy_field.h:43-49) with
- *                            connectionLaplacian (:72-102), galerkinMassMatrix (:104-110) and
+ *                            (include/metriko/core/vectorfield/face_rosy_field.h:17-23) with
+ *                            connectionLaplacian (:46-76), galerkinMassMatrix (:78-84) and
  *                            solveSmallestEig(SprsC&, SprsC&, int nIter = 50)
- *                            (include/metriko/core/solver/sparse_linear_solver.h:452-477)
+ *                            (include/metriko/core/solver/sparse_linear_solver.h:29-54)
  *   mtk_iterative_rounding <- iterative_rounding(fixedIdcs, fixedVals, singularIdcs,
  *                            integerIdcs, length, Cfull, G2, N, n, nF, seamless, roundSeams,
  *                            localInjectivity, verbose, intrinsicField, iter_cb, fullx)
@@ -22,13 +22,13 @@
  *                            (include/metriko/core/solver/levenberg_marquardt.h:140-231,
  *                            iter_rounding.h:14-31)
  *   mtk_topology_from_field <- the host stages of the same sequence for a given field
- *                            (face_rosy_field.h:126-386, parameterization.h:43-152,
+ *                            (face_rosy_field.h:100-360, parameterization.h:43-152,
  *                            parameterization_setup.ipp:3-170, parameterization_integ.ipp:3-70)
  *   mtk_pipeline_run      <- the example_igm.cpp:13-31 call sequence (Hmesh -> field ->
  *                            matching -> seam -> cut -> combing -> RosyParameterization
  *                            setup()/integ()) as one call with host buffers
  *   mtk_mesh_geometry     <- the vertex and edge geometry of the Hmesh constructor
- *                            (include/metriko/core/hmesh/hmesh.h:535-611), host only
+ *                            (include/metriko/core/hmesh/hmesh.h:491-568), host only
  *   mtk_map_deviation     <- the closing check of RosyParameterization::integ()
  *                            (parameterization_integ.ipp:100-117), host only
  *   mtk_injective_barrier, mtk_local_injectivity <- InjectiveBarrier
@@ -94,6 +94,11 @@ typedef struct {
     int64_t igm_pcg_launches;
     double igm_pcg_ms;
     double igm_pcg_bytes;
+    /* greedy rounding: steps whose pick (first position among the candidates within 1e-8 of
+       the smallest distance to an integer) is not the strict '<' pick of the reference, and the
+       largest distance gap between the two picks over those steps                           */
+    int64_t strict_order_differs;
+    double strict_order_gap;
 } mtk_stats;
 
 const char* mtk_status_string(int status);
@@ -104,6 +109,14 @@ int mtk_ctx_create(int device, mtk_ctx** out);
 int mtk_ctx_destroy(mtk_ctx* ctx);
 /* Number of library kernels launched on this context so far (instrumentation). */
 int64_t mtk_ctx_kernel_count(const mtk_ctx* ctx);
+/*
+ * Polls a waiting CTA makes at a grid barrier of the persistent solver kernels before it gives
+ * up: the kernel then leaves its loops and the call returns MTK_ERR_TIMEOUT, with the context
+ * still usable.  Default 2^24 (about a second).  No counterpart in the reference (which has no
+ * device code); small values exist to exercise the timeout path (0 = give up at the first poll
+ * that finds the barrier still closed).  polls < 0 -> MTK_ERR_BAD_INPUT.
+ */
+int mtk_ctx_set_wait_limit(mtk_ctx* ctx, int64_t polls);
 
 /*
  * Smoothest N-RoSy field: assemble the connection Laplacian L (face graph, 3 neighbours per
@@ -196,7 +209,7 @@ int mtk_pipeline_run(mtk_ctx* ctx, int32_t nV, int32_t nF, const double* V, cons
  * Host-only topology stages for a caller-supplied field (no device work): Hmesh, Curl
  * matching and singularities, seams, cut mesh, combing, RosyParameterization::setup() and the
  * host part of integ() (constraint reduction, UFull kernel block, target field, grid length).
- * Replaces the face_rosy_field.h:126-386 and parameterization*.{h,ipp} host code.
+ * Replaces the face_rosy_field.h:100-360 and parameterization*.{h,ipp} host code.
  *   compressed[2*nF]  field eigenvector (re, im) -- e.g. the output of mtk_field_smoothest
  *   singular[nV], matching[nE] (combed), seam[nE], cutF[nF*3]
  *   counts[8]         nV, nE, nCut, nT, nS, nJ, nZ, nFull;   *length: grid edge length
@@ -213,11 +226,17 @@ int mtk_topology_from_field(int32_t nV, int32_t nF, const double* V, const int32
  * (which has no GPU code); it allocates nothing and needs no mtk_ctx.
  *   All pointers are DEVICE pointers owned by the caller: nbr[3*nF], theta[3*nF], area[nF],
  *   x0[2*nF] (re, im), out[2*nF].  stream: a cudaStream_t (NULL = default stream).
+ *   Closed meshes: every nbr entry must lie in [0, nF) (the diagonal is 3 + 1e-9); an entry
+ *   outside (e.g. -1 for a boundary edge) -> MTK_ERR_BAD_INPUT, detected on the device, with
+ *   no solve.  n_iter = 0 copies x0 to out.  max_iter caps every inner PCG solve
+ *   (MTK_ERR_NOT_CONVERGED when reached).
  *   Working memory is a 64 MiB static device array inside the library (held by every GPU that
  *   loads the library until exit), which limits nF to 409600; larger nF -> MTK_ERR_BAD_INPUT.
- *   The first call on a device looks the array up (cudaGetSymbolAddress): make that first
- *   call before any stream capture.  All calls share the array: calls that overlap on the GPU
- *   race.  *iterations (may be NULL) receives the total PCG iterations.  Returns when done.
+ *   The first call on a device looks the array up (cudaGetSymbolAddress) and keeps its address
+ *   for the life of the process: make that first call before any stream capture, and make no
+ *   call on a device after cudaDeviceReset().  All calls share the array: calls that overlap on
+ *   the GPU race.  *iterations (may be NULL) receives the total PCG iterations.  The call reads
+ *   its status back and waits for `stream` before it returns.
  */
 int mtk_field_smoothest_noalloc(int32_t nF, int32_t nRosy, const int32_t* nbr, const double* theta,
                                 const double* area, const double* x0, int32_t n_iter, double tol,
@@ -226,7 +245,7 @@ int mtk_field_smoothest_noalloc(int32_t nF, int32_t nRosy, const int32_t* nbr, c
 /*
  * One solve L x = rhs with the connection Laplacian of mtk_field_smoothest (same inputs, same
  * assembly, preconditioner and precision options).  Replaces solveSquare(lhs, rhs) of
- * face_rosy_field.h:23-32 / sparse_linear_solver.h:16-27 for FieldType::CurvatureAligned
+ * face_rosy_field.h:25-33 / sparse_linear_solver.h:16-27 for FieldType::CurvatureAligned
  * (lambda = 0, so lhs = L).  rhs[2*nF] and out[2*nF] are (re, im) per face.
  */
 int mtk_field_solve(mtk_ctx* ctx, int32_t nF, int32_t nRosy, const int32_t* nbr, const double* theta,
@@ -293,14 +312,14 @@ int mtk_local_injectivity(mtk_ctx* ctx, int32_t nF, int32_t N, const double* cfn
 
 /*
  * The inputs of mtk_field_smoothest for a closed mesh (host only): nbr[3*nF] the face across
- * each face halfedge, theta[3*nF] = farg(h) - farg(twin h) (face_rosy_field.h:72-102), and
+ * each face halfedge, theta[3*nF] = farg(h) - farg(twin h) (face_rosy_field.h:46-76), and
  * area[nF] (may be NULL).
  */
 int mtk_field_inputs(int32_t nV, int32_t nF, const double* V, const int32_t* F, int32_t* nbr, double* theta,
                      double* area);
 
 /*
- * Host only (no GPU): the vertex and edge geometry of Hmesh (hmesh.h:452-611 of the reference:
+ * Host only (no GPU): the vertex and edge geometry of Hmesh (hmesh.h:444-568 of the reference:
  * the members vertNormal, vertBasisX, vertBasisY, baryDualArea, circDualArea, halfCotan,
  * edgeCotan, dihedralArg, heArgOnVert, angleDefect) for a closed mesh, in the reference's
  * halfedge / edge numbering (nE = 3 nF / 2, nH = 2 nE).  Every output may be NULL:

@@ -23,7 +23,7 @@ EXPORTS = [
     "mtk_seeded_init", "mtk_topology_from_field", "mtk_field_smoothest_noalloc", "mtk_size_field_gradient",
     "mtk_pipeline_size_field_gradient", "mtk_field_solve", "mtk_field_inputs", "mtk_field_spmv_bench",
     "mtk_injective_barrier", "mtk_local_injectivity", "mtk_map_deviation",
-    "mtk_mesh_geometry",
+    "mtk_mesh_geometry", "mtk_ctx_set_wait_limit",
 ]
 
 
@@ -46,7 +46,8 @@ class Stats(C.Structure):
                 ("ms_total", C.c_double), ("resolves", C.c_int64), ("lm_iterations", C.c_int64),
                 ("min_order_margin", C.c_double), ("field_pcg_launches", C.c_int64),
                 ("field_pcg_ms", C.c_double), ("field_pcg_bytes", C.c_double), ("igm_pcg_launches", C.c_int64),
-                ("igm_pcg_ms", C.c_double), ("igm_pcg_bytes", C.c_double)]
+                ("igm_pcg_ms", C.c_double), ("igm_pcg_bytes", C.c_double),
+                ("strict_order_differs", C.c_int64), ("strict_order_gap", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -75,6 +76,7 @@ def lib():
         L.mtk_ctx_destroy.argtypes = [C.c_void_p]
         L.mtk_ctx_kernel_count.argtypes = [C.c_void_p]
         L.mtk_ctx_kernel_count.restype = C.c_int64
+        L.mtk_ctx_set_wait_limit.argtypes = [C.c_void_p, C.c_int64]
         L.mtk_seeded_init.argtypes = [C.c_int32, C.c_int32, C.c_void_p]
         L.mtk_field_smoothest.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.c_void_p, C.c_int32, C.POINTER(SolveOpts), C.c_void_p,
@@ -143,6 +145,10 @@ class Context:
 
     def kernel_count(self):
         return int(lib().mtk_ctx_kernel_count(self.handle))
+
+    def set_wait_limit(self, polls: int):
+        """Polls of a grid-barrier wait before the call gives up with TIMEOUT (default 2**24)."""
+        _check(lib().mtk_ctx_set_wait_limit(self.handle, int(polls)), "mtk_ctx_set_wait_limit")
 
     def __enter__(self):
         return self

@@ -42,6 +42,7 @@ struct GridBarrier {
     unsigned int* count;       // arrivals in the current generation
     unsigned int* gen;         // generation counter
     int* err;                  // sticky error flag (MTK_ERR_TIMEOUT)
+    long long limit = kSpinLimit;   // polls before a waiting CTA gives up
 };
 
 __device__ __forceinline__ unsigned int ld_acquire(const unsigned int* p) {
@@ -68,7 +69,8 @@ __device__ __forceinline__ void st_relaxed(unsigned int* p, unsigned int v) {
 // Grid-wide barrier for a cooperative launch (one CTA per SM).  Thread 0 of every CTA
 // arrives with an acq_rel atomic; the last arrival resets the counter and publishes the next
 // generation with a release store; the others poll it with acquire loads (tight spin first,
-// then nanosleep backoff) for at most kSpinLimit polls, after which MTK_ERR_TIMEOUT is
+// then nanosleep backoff) for at most `limit` polls (kSpinLimit unless the context sets a
+// smaller wait limit), after which MTK_ERR_TIMEOUT is
 // recorded and every CTA leaves.  Returns false (in every thread) on timeout or a recorded
 // error; callers then leave their loop.
 __device__ __forceinline__ bool grid_sync(const GridBarrier& b) {
@@ -85,7 +87,7 @@ __device__ __forceinline__ bool grid_sync(const GridBarrier& b) {
             } else {
                 long long spins = 0;
                 while (ld_acquire(b.gen) == g) {
-                    if (++spins > kSpinLimit) { atomicExch(b.err, (int)MTK_ERR_TIMEOUT); ok = 0; break; }
+                    if (++spins > b.limit) { atomicExch(b.err, (int)MTK_ERR_TIMEOUT); ok = 0; break; }
                     if ((spins & 255) == 0 && ld_volatile(b.err) != 0) { ok = 0; break; }
                     if (spins > 2048) __nanosleep(100);
                 }

@@ -97,8 +97,14 @@ extern "C" int mtk_ctx_destroy(mtk_ctx* c) {
 
 extern "C" int64_t mtk_ctx_kernel_count(const mtk_ctx* c) { return c ? c->kernels : 0; }
 
+extern "C" int mtk_ctx_set_wait_limit(mtk_ctx* c, int64_t polls) {
+    if (!c || polls < 0) return MTK_ERR_BAD_INPUT;
+    c->wait_limit = polls > 0 ? (long long)polls : 0;
+    return MTK_OK;
+}
+
 // splitmix64 over (seed, 2f) and (seed, 2f+1), mapped to [-1, 1).  Replaces the
-// std::rand-based VecXc::Random start of solveSmallestEig (sparse_linear_solver.h:455) with a
+// std::rand-based VecXc::Random start of solveSmallestEig (sparse_linear_solver.h:32) with a
 // reproducible vector that the CPU oracle regenerates bit-for-bit.
 extern "C" void mtk_seeded_init(int32_t n, int32_t seed, double* out) {
     const uint64_t G = 0x9E3779B97F4A7C15ULL;

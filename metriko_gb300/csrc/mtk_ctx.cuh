@@ -23,6 +23,7 @@ struct mtk_ctx {
     int* dev_int = nullptr;        // device ints (iteration counts, status)
     int partial_blocks = 0;        // capacity in blocks
     long long kernels = 0;
+    long long wait_limit = mtk::kSpinLimit;   // polls of a grid-barrier wait before MTK_ERR_TIMEOUT
 };
 
 namespace mtk {
@@ -66,7 +67,7 @@ struct DBuf {
     }
 };
 
-inline GridBarrier barrier_of(mtk_ctx* c) { return GridBarrier{c->bar, c->bar + 1, c->dev_err}; }
+inline GridBarrier barrier_of(mtk_ctx* c) { return GridBarrier{c->bar, c->bar + 1, c->dev_err, c->wait_limit}; }
 
 // Resets the barrier words and the error flag before a cooperative launch.
 inline int reset_barrier(mtk_ctx* c) {

@@ -2,7 +2,7 @@
 // SpMV, persistent PCG (FP32 or FP64) and the inverse power iteration with FP64 residuals,
 // Rayleigh quotient and normalisation.
 //
-// Replaces (metriko) face_rosy_field.h:43-49 + :72-110 and sparse_linear_solver.h:452-477.
+// Replaces (metriko) face_rosy_field.h:17-23 + :72-110 and sparse_linear_solver.h:29-54.
 // The reference factorises L once (CHOLMOD simplicial LDL^T or Eigen SparseLU) and runs 50
 // triangular-solve pairs; here every inverse-iteration step is a preconditioned CG solve of
 // L x = M u to a relative residual `tol`, warm-started from the Galerkin guess
@@ -59,7 +59,7 @@ struct ComplexEll {
 
 // ---------------------------------------------------------------------------- assembly
 // One thread per face: off-diagonals -(-e^{i theta})^N = -e^{i N (theta + pi)}, diagonal
-// count + 1e-9 (face_rosy_field.h:88-101).  No atomics: every row is written by its owner.
+// count + 1e-9 (face_rosy_field.h:52-75).  No atomics: every row is written by its owner.
 __global__ void field_assemble(int n, int N, const int* __restrict__ nbr_in, const double* __restrict__ theta,
                                const double* __restrict__ area, int* nbr, double2* v64, float2* v32,
                                double* d64, float* d32, double* inv64, float* inv32, float* area32) {
@@ -1362,6 +1362,10 @@ int field_run(mtk_ctx* c, int32_t nF, int32_t nRosy, const int32_t* nbr_h, const
             MTK_CUDA_TRY(cudaStreamSynchronize(st));
             bnorm2 = c->h_scalars[2];
             rr = c->h_scalars[3];
+        }
+        if (!(bnorm2 == bnorm2) || !(rr == rr)) {   // a NaN in the inputs reached the right-hand side
+            mtk_set_last_error("field solve: NaN in the right-hand side or the start residual", __FILE__, __LINE__);
+            return MTK_ERR_BREAKDOWN;
         }
         const double goal2 = tol * tol * bnorm2;
         const double start_rel = bnorm2 > 0 ? std::sqrt(rr / bnorm2) : 0.0;

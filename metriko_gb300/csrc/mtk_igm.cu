@@ -668,11 +668,8 @@ __global__ void expand_full(int nFull, const int* __restrict__ full2y, const int
     }
 }
 
-// Greedy rounding choice (iter_rounding_loop.h:29-43), one block: d_i = |X - round X| over the
-// left indices (d <= 1e-6 counts as 0, the reference's integrality threshold); the pick is the
-// first position whose d is within 1e-6 of the minimum -- the reference's strict '<' among
-// values that close is decided by round-off (constraint-linked variables share their
-// fractional part).  out = [position, d, X, smallest d outside the tie group].
+// Value X of full variable i from the reduced coordinates: a free variable is its y entry, a
+// constrained one the USmall row times z (same order of additions as the host).
 __device__ __forceinline__ double left_value(int i, const int* __restrict__ full2y, const int* __restrict__ full2j,
                                              int nY, int nZ, const double* __restrict__ Us, const double* __restrict__ xs) {
     int y = full2y[i];
@@ -698,26 +695,44 @@ __global__ void fixed_values(int nfix, const int* __restrict__ fixed, const int*
     }
 }
 
+// Greedy pick of SeamlessIntegration::initFixedIndices (iter_rounding_loop.h:34-38) over the left
+// indices, one CTA.  The reference keeps the first position with the smallest |X - round X|
+// under a strict '<'; candidates within kTieWindow of the smallest distance are equal in exact
+// arithmetic (variables tied by a constraint, already-integral values), so among them the first
+// position is taken and round-off cannot reorder them.
+// out: [0] pick position, [1] its distance, [2] its X, [3] smallest distance outside the tie
+// group (1e300 when none), [4] the strict '<' pick position, [5] its distance.
+constexpr double kTieWindow = 1e-8;
+
 __global__ void round_argmin(int nLeft, const int* __restrict__ left, const int* __restrict__ full2y,
                              const int* __restrict__ full2j, int nY, int nZ, const double* __restrict__ Us,
                              const double* __restrict__ xs, double* out) {
     __shared__ double sd[kStream];
     __shared__ int si[kStream];
-    // pass 1: minimum distance
+    // pass 1: smallest distance and the first position holding it
     double bd = 1e300;
+    int bk = 0x7fffffff;
     for (int t = threadIdx.x; t < nLeft; t += blockDim.x) {
         double X = left_value(left[t], full2y, full2j, nY, nZ, Us, xs);
         double d = fabs(X - round(X));
-        if (d <= 10e-7) d = 0.0;
-        bd = fmin(bd, d);
+        if (d < bd) { bd = d; bk = t; }
     }
     sd[threadIdx.x] = bd;
+    si[threadIdx.x] = bk;
     __syncthreads();
     for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w) sd[threadIdx.x] = fmin(sd[threadIdx.x], sd[threadIdx.x + w]);
+        if (threadIdx.x < w) {
+            const double od = sd[threadIdx.x + w];
+            const int ok = si[threadIdx.x + w];
+            if (od < sd[threadIdx.x] || (od == sd[threadIdx.x] && ok < si[threadIdx.x])) {
+                sd[threadIdx.x] = od;
+                si[threadIdx.x] = ok;
+            }
+        }
         __syncthreads();
     }
     const double dmin = sd[0];
+    const int kstrict = si[0];
     __syncthreads();
     // pass 2: first position inside the tie group, and the best distance outside it
     int bi = 0x7fffffff;
@@ -725,8 +740,7 @@ __global__ void round_argmin(int nLeft, const int* __restrict__ left, const int*
     for (int t = threadIdx.x; t < nLeft; t += blockDim.x) {
         double X = left_value(left[t], full2y, full2j, nY, nZ, Us, xs);
         double d = fabs(X - round(X));
-        if (d <= 10e-7) d = 0.0;
-        if (d <= dmin + 10e-7) {
+        if (d <= dmin + kTieWindow) {
             if (t < bi) { bi = t; bX = X; bdist = d; }
         } else {
             other = fmin(other, d);
@@ -744,7 +758,10 @@ __global__ void round_argmin(int nLeft, const int* __restrict__ left, const int*
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0) { out[0] = (double)si[0]; out[1] = sdd[0]; out[2] = sX[0]; out[3] = so[0]; }
+    if (threadIdx.x == 0) {
+        out[0] = (double)si[0]; out[1] = sdd[0]; out[2] = sX[0]; out[3] = so[0];
+        out[4] = (double)kstrict; out[5] = dmin;
+    }
 }
 
 // NI-LM field block (Gauss-Newton with the diagonal field block eliminated exactly):
@@ -2050,7 +2067,7 @@ int igm_run(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts_in, do
     else leftv.assign(d->singularIdcs, d->singularIdcs + d->nSingular);
     bool rounded = false;
     double min_margin = 1e300;
-    std::vector<double> h_arg(4);
+    std::vector<double> h_arg(6);
     bool constraints_dirty = true;
     while (!leftv.empty()) {
         // ---- initFixedIndices: argmin |X - round X| over leftIdcs (FP64 on the device)
@@ -2058,12 +2075,16 @@ int igm_run(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts_in, do
         round_argmin<<<1, kStream, 0, st>>>((int)leftv.size(), S.left.p, S.d_full2y.p, S.d_full2j.p, nY, nZ, S.Us.p, S.xs.p,
                                            c->scalars);
         c->kernels++;
-        MTK_CUDA_TRY(cudaMemcpyAsync(h_arg.data(), c->scalars, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        MTK_CUDA_TRY(cudaMemcpyAsync(h_arg.data(), c->scalars, 6 * sizeof(double), cudaMemcpyDeviceToHost, st));
         MTK_CUDA_TRY(cudaStreamSynchronize(st));
         const int k = (int)h_arg[0];
         const double mind = h_arg[1];
         if (Igm::debug()) fprintf(stderr, "[round] left=%zu pick=%d full=%d X=%.9f d=%.3e second=%.3e\n", leftv.size(), k, leftv[k], h_arg[2], mind, h_arg[3]);
-        if (h_arg[3] < 1e299) min_margin = std::min(min_margin, h_arg[3] - mind);
+        if (h_arg[3] < 1e299) min_margin = std::min(min_margin, h_arg[3] - h_arg[5]);
+        if ((int)h_arg[4] != k) {   // a tie resolved by position, not by the strict '<'
+            stt->strict_order_differs++;
+            stt->strict_order_gap = std::max(stt->strict_order_gap, mind - h_arg[5]);
+        }
         const int idx = leftv[k];
         const int ival = (int)std::round(h_arg[2]);
         if (fix_order && nfix < nLeftCap) { fix_order[nfix] = idx; if (fix_vals) fix_vals[nfix] = ival; }

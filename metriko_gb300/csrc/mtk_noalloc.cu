@@ -10,9 +10,17 @@
 // library holds it until the process exits.  It bounds the problem size to kMaxFaces faces.
 // The first call on a device looks the array's device address up with cudaGetSymbolAddress
 // (host code cannot use the symbol itself: in host code it names a host-side stand-in), so
-// that first call should come before any stream capture.  Every call shares the array, which
-// keeps the last call's contents: the barrier words and the status word are cleared at the
-// start of each call, and calls that overlap on the GPU (two streams, two threads) race.
+// that first call should come before any stream capture.  The address is kept for the life of
+// the process; a cudaDeviceReset() unloads the module, and the entry point must not be called
+// on that device after one.  Every call shares the array, which keeps the last call's
+// contents: the barrier words, the error flag and the status word are cleared at the start of
+// each call, and calls that overlap on the GPU (two streams, two threads) race.  Each call
+// reads its status back and waits for its stream before it returns.
+//
+// Meshes are closed: every face has three neighbours, so the diagonal of L is 3 + 1e-9 in
+// every row (the reference's count of neighbours plus its shift).  A neighbour index outside
+// [0, nF) -- including -1, a boundary edge -- is found during assembly, the solve is skipped
+// and the call returns MTK_ERR_BAD_INPUT, as the regular entry point does.
 //
 // Algorithm: the same inverse power iteration as mtk_field_smoothest with the FP64 path
 // (assembly of the connection Laplacian, then n_iter steps of x = L^-1 M u solved by PCG to
@@ -35,11 +43,13 @@ constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
-// header layout (bytes): [0,16) barrier count/gen, [16,20) error flag, [32,48) status +
-// iterations, [256, 512) scalars, [4096, 65536) reduction partials (<= 7 slots per CTA)
+// header layout (bytes): [0,16) barrier count/gen, [16,20) error flag, [20,24) bad-neighbour
+// flag, [32,48) status + iterations, [256, 512) scalars, [4096, 65536) reduction partials
+// (<= 7 slots per CTA)
 struct Layout {
     unsigned int* bar;
     int* err;
+    int* bad_nbr;
     int* status;
     double* scal;
     double* partials;
@@ -52,6 +62,7 @@ __host__ __device__ inline Layout layout_of(unsigned char* base, int n) {
     Layout L{};
     L.bar = reinterpret_cast<unsigned int*>(base);
     L.err = reinterpret_cast<int*>(base + 16);
+    L.bad_nbr = reinterpret_cast<int*>(base + 20);
     L.status = reinterpret_cast<int*>(base + 32);
     L.scal = reinterpret_cast<double*>(base + 256);
     L.partials = reinterpret_cast<double*>(base + 4096);
@@ -68,14 +79,16 @@ __host__ __device__ inline Layout layout_of(unsigned char* base, int n) {
     return L;
 }
 
-__device__ __forceinline__ double2 row_apply(int i, int n, const int* __restrict__ nbr, const double2* __restrict__ val,
-                                             double diag, const double2* __restrict__ x) {
+// val and x are written earlier in the same kernel, so they are read through L2 (__ldcg), not
+// the read-only path.  nbr has been range-checked by the assembly before any call.
+__device__ __forceinline__ double2 row_apply(int i, int n, const int* __restrict__ nbr, const double2* val,
+                                             double diag, const double2* x) {
     double2 xi = __ldcg(x + i);
     double re = diag * xi.x, im = diag * xi.y;
 #pragma unroll
     for (int j = 0; j < 3; j++) {
         int c = nbr[3 * i + j];
-        double2 a = val[j * n + i];
+        double2 a = __ldcg(val + j * n + i);
         double2 xc = __ldcg(x + c);
         re += a.x * xc.x - a.y * xc.y;
         im += a.x * xc.y + a.y * xc.x;
@@ -91,13 +104,15 @@ __global__ void __launch_bounds__(kBlock) noalloc_power(unsigned char* base, int
     GridBarrier bar{L.bar, L.bar + 1, L.err};
     const int stride = gridDim.x * blockDim.x;
     const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
-    const double diag = 3.0 + 1e-9;
+    const double diag = 3.0 + 1e-9;   // three neighbours per face (closed mesh) + the 1e-9 shift
     const int G = gridDim.x;
     int status = 0;
     long long total_it = 0;
-    // assembly (face_rosy_field.h:88-101) and the start vector
+    // assembly (face_rosy_field.h:52-75), the neighbour range check and the start vector
     for (int f = t0; f < n; f += stride) {
         for (int j = 0; j < 3; j++) {
+            const int g = nbr[3 * f + j];
+            if (g < 0 || g >= n) atomicExch(L.bad_nbr, 1);
             double s, c;
             sincos((double)N * (theta[3 * f + j] + 3.14159265358979323846), &s, &c);
             L.val[j * n + f] = make_double2(-c, -s);
@@ -105,6 +120,7 @@ __global__ void __launch_bounds__(kBlock) noalloc_power(unsigned char* base, int
         L.u[f] = make_double2(x0[2 * f], x0[2 * f + 1]);
     }
     if (!grid_sync(bar)) { status = MTK_ERR_TIMEOUT; goto done; }
+    if (ld_volatile(L.bad_nbr) != 0) { status = MTK_ERR_BAD_INPUT; goto done; }   // same value in every CTA
     for (int k = 0; k < n_iter; k++) {
         // b = M u; Galerkin factor g = (u^H M u) / (u^H L u); |b|^2
         double red3[3] = {0, 0, 0};
@@ -254,12 +270,19 @@ extern "C" int mtk_field_smoothest_noalloc(int32_t nF, int32_t nRosy, const int3
     int sms = 0, coop = 0, per_sm = 0;
     MTK_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     MTK_CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device));
-    if (!coop) return MTK_ERR_CUDA;
+    if (!coop) {
+        mtk_set_last_error("mtk_field_smoothest_noalloc: the device does not support cooperative launches", __FILE__,
+                           __LINE__);
+        return MTK_ERR_CUDA;
+    }
     MTK_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, noalloc_power, kBlock, 0));
-    if (per_sm < 1) return MTK_ERR_CUDA;
+    if (per_sm < 1) {
+        mtk_set_last_error("mtk_field_smoothest_noalloc: the solver kernel does not fit on an SM", __FILE__, __LINE__);
+        return MTK_ERR_CUDA;
+    }
     const int grid = sms < 512 ? sms : 512;   // one CTA per SM; partials hold 7 slots x 512 CTAs
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    // what must start at zero: barrier words, error flag, status
+    // what must start at zero: barrier words, error flag, bad-neighbour flag, status
     MTK_CUDA_TRY(cudaMemsetAsync(base, 0, 64, st));
     int n = nF, N = nRosy, it = n_iter, mi = max_iter;
     double t = tol;
@@ -269,5 +292,7 @@ extern "C" int mtk_field_smoothest_noalloc(int32_t nF, int32_t nRosy, const int3
     MTK_CUDA_TRY(cudaMemcpyAsync(h_status, base + 32, sizeof(h_status), cudaMemcpyDeviceToHost, st));
     MTK_CUDA_TRY(cudaStreamSynchronize(st));
     if (iterations) *iterations = h_status[1];
+    if (h_status[0] == MTK_ERR_BAD_INPUT)
+        mtk_set_last_error("mtk_field_smoothest_noalloc: a neighbour index is outside [0, nF)", __FILE__, __LINE__);
     return h_status[0];
 }

@@ -1,26 +1,30 @@
 """FP64 CPU ORACLE for metriko's field + seamless-integration + IGM path.
 
+Restates the algorithms of metriko (https://github.com/komietty/metriko), Copyright (C) 2025
+Saki Komikado <komietty@gmail.com>, subject to the terms of the Mozilla Public License v.2.0
+(https://mozilla.org/MPL/2.0/).
+
 TEST INFRASTRUCTURE ONLY.  This module is the reference result the CUDA path is compared
 against and the timed CPU baseline.  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference arm
 may import it.  Nothing in the product (metriko_gb300/, include/) imports it.
 
 What it restates (reference paths are relative to the metriko project root):
 
-  a1  Hmesh construction              include/metriko/core/hmesh/hmesh.h:282-611
+  a1  Hmesh construction              include/metriko/core/hmesh/hmesh.h:313-569
       (libigl v2.5.0 edge_topology restated from its documented behaviour)
-  a2  connectionLaplacian             include/metriko/core/vectorfield/face_rosy_field.h:72-102
-  a3  galerkinMassMatrix              face_rosy_field.h:104-110
-  a4  solveSmallestEig (50 iters)     include/metriko/core/solver/sparse_linear_solver.h:452-477
+  a2  connectionLaplacian             include/metriko/core/vectorfield/face_rosy_field.h:46-76
+  a3  galerkinMassMatrix              face_rosy_field.h:78-84
+  a4  solveSmallestEig (50 iters)     include/metriko/core/solver/sparse_linear_solver.h:29-54
       direct sparse LU (scipy SuperLU), the reference's non-SuiteSparse branch
-  a5  N-th root field                 face_rosy_field.h:63-69
-  a6  computeConnection / cMatching / computeSingular   face_rosy_field.h:126-143,195-228
-  a7  compute_seam / cut_mesh_with_singularities        face_rosy_field.h:294-386
+  a5  N-th root field                 face_rosy_field.h:37-43
+  a6  computeConnection / cMatching / computeSingular   face_rosy_field.h:100-117,169-202
+  a7  compute_seam / cut_mesh_with_singularities        face_rosy_field.h:268-360
       (libigl v2.5.0 cut_mesh_from_singularities, dijkstra, adjacency_list,
        vertex_triangle_adjacency, triangle_triangle_adjacency restated)
-  a8  compute_combbed_field / compute_extrinsic_field   face_rosy_field.h:233-290
+  a8  compute_combbed_field / compute_extrinsic_field   face_rosy_field.h:207-264
   a9  compute_cut_mesh                include/metriko/core/igm/parameterization.h:126-152
-  a10 compute_he2transidx / he2matching   include/metriko/core/igm/parameterization_setup.ipp:3-49
-  a11 setup                           parameterization_setup.ipp:51-170
+  a10 compute_he2transidx / he2matching   include/metriko/core/igm/parameterization_setup.ipp:3-50
+  a11 setup                           parameterization_setup.ipp:52-170
   a12 integ                           include/metriko/core/igm/parameterization_integ.ipp:3-120
   a13 reduce_to_linearly_independent  include/metriko/core/solver/matrix_ops.h:12-28
   a14 NaiveIntegration                include/metriko/core/igm/iterative_rounding/iter_rounding_init.h:16-233
@@ -30,16 +34,17 @@ What it restates (reference paths are relative to the metriko project root):
 
 Deliberate, documented choices (identical in the product path):
   * the power iteration starts from a caller-supplied seeded vector instead of
-    Eigen's std::rand-based VecXc::Random (sparse_linear_solver.h:455);
+    Eigen's std::rand-based VecXc::Random (sparse_linear_solver.h:32);
   * reduce_to_linearly_independent keeps the greedy (first-in-row-order) maximal independent
     row set instead of Eigen SparseQR<COLAMD>'s column-pivot order; the constraint null space
     is the same;
   * the constraint kernel basis restates Eigen's FullPivLU::kernel (complete pivoting, first
     maximum in column-major order, identity on the free columns);
   * greedy rounding (iter_rounding_loop.h:34-38) picks the first position among candidates
-    whose distance to an integer is within 1e-6 of the minimum (distances <= 1e-6 count as 0,
-    the reference's own integrality threshold): the reference's strict '<' there is decided
-    by round-off (structural ties between constraint-linked variables, already-integral values).
+    whose distance to an integer is within TIE_WINDOW = 1e-8 of the minimum; the reference's
+    strict '<' among such candidates is decided by round-off (structural ties between
+    constraint-linked variables, already-integral values).  Every step where this pick differs
+    from the strict '<' pick is recorded (info["strict_differs"]: step, distance gap).
 Closed, consistently oriented, edge-manifold triangle meshes only.
 
 Parity status: the reference cannot be compiled here (Eigen, libigl, SuiteSparse absent) and
@@ -58,6 +63,8 @@ import scipy.sparse as sp
 import scipy.sparse.linalg as spla
 
 TWO_PI = 2.0 * math.pi
+# greedy rounding: distances to an integer within this of the smallest count as tied
+TIE_WINDOW = 1e-8
 
 
 def cround(x):
@@ -114,7 +121,7 @@ def edge_topology(F):
 
 
 class Hmesh:
-    """Halfedge mesh with the reference's numbering (hmesh.h:282-611) for closed meshes."""
+    """Halfedge mesh with the reference's numbering (hmesh.h:313-569) for closed meshes."""
 
     def __init__(self, V, F):
         V = np.asarray(V, np.float64)
@@ -154,7 +161,7 @@ class Hmesh:
         self.face2half = FH[:, 0]
         self.edge2half = 2 * ar
         self.vert2half = vert2half
-        # face frames (hmesh.h:503-520)
+        # face frames (hmesh.h:461-478)
         P0, P1, P2 = V[F[:, 0]], V[F[:, 1]], V[F[:, 2]]
         x = P1 - P0
         t = -(P0 - P2)
@@ -163,7 +170,7 @@ class Hmesh:
         self.faceBasisY = _normalized(-np.cross(x, n))
         self.faceNormal = _normalized(n)
         self.faceArea = _norm3(n) * 0.5
-        # heArgOnFace (hmesh.h:522-531)
+        # heArgOnFace (hmesh.h:480-489)
         vec = V[self.head] - V[self.tail]
         self.hvec = vec
         farg = np.zeros(2 * nE)
@@ -176,7 +183,7 @@ class Hmesh:
             s = s + np.where(far, np.arccos(_dot3(v1, v2)), 0.0)
             farg[h] = s
         self.farg = farg
-        # angleDefect (hmesh.h:599-610): interior angle at tail(h) inside face(h)
+        # angleDefect (hmesh.h:557-568): interior angle at tail(h) inside face(h)
         h = np.arange(2 * nE)
         ang = np.arccos(_dot3(_normalized(vec[h]), _normalized(vec[twin[prv[h]]])))
         ssum = np.zeros(nV)
@@ -196,7 +203,7 @@ class Hmesh:
         return self.edge2half[self.edge[h]] == h
 
     def vertex_geometry(self):
-        """The rest of the reference's Hmesh constructor (hmesh.h:535-611) for a closed mesh:
+        """The rest of the reference's Hmesh constructor (hmesh.h:491-568) for a closed mesh:
         vertex normals (area-weighted face normals accumulated face by face, then normalized),
         vertex frames (x: the first outgoing edge projected to the tangent plane), dihedral angle
         and cotangent per halfedge, edge cotangents, barycentric and circumcentric dual areas and
@@ -261,7 +268,7 @@ class Hmesh:
 # a2-a5  smoothest N-RoSy field
 # --------------------------------------------------------------------------------------------
 def connection_laplacian(m: Hmesh, N: int):
-    """face_rosy_field.h:72-102: L_ff = #interior neighbours + 1e-9, L_fg = -r_twin^N."""
+    """face_rosy_field.h:46-76: L_ff = #interior neighbours + 1e-9, L_fg = -r_twin^N."""
     h1 = m.edge2half
     h2 = m.twin[h1]
     v1 = np.exp(1j * m.farg[h1])
@@ -304,9 +311,18 @@ def seeded_init(n: int, seed: int):
     return u[0::2] + 1j * u[1::2]
 
 
+def spd_factor(A):
+    """Direct factorisation of a symmetric / Hermitian positive-definite matrix, the role of
+    CHOLMOD's simplicial LDL^T (suitesparse_pdefinite.h:26-40) and Eigen's SimplicialLLT
+    (iter_rounding.h:14-31): a fill-reducing symmetric ordering (minimum degree on A + A^T) and
+    no pivoting, which a positive-definite matrix does not need (SuperLU in symmetric mode)."""
+    return spla.splu(sp.csc_matrix(A), permc_spec="MMD_AT_PLUS_A", diag_pivot_thresh=0.0,
+                     options=dict(SymmetricMode=True))
+
+
 def smallest_eig(L, M, x0, n_iter=50):
-    """sparse_linear_solver.h:452-477: x = L^-1 M u; x /= sqrt|x^H M x|; u = x (n_iter times)."""
-    lu = spla.splu(L.tocsc())
+    """sparse_linear_solver.h:29-54: x = L^-1 M u; x /= sqrt|x^H M x|; u = x (n_iter times)."""
+    lu = spd_factor(L)
     u = x0.copy()
     x = u
     for _ in range(n_iter):
@@ -318,7 +334,7 @@ def smallest_eig(L, M, x0, n_iter=50):
 
 
 def rosy_from_compressed(c, N):
-    """face_rosy_field.h:63-69: field(f,i) = pow(polar(1, arg c_f), 1/N) * pow(r, i)."""
+    """face_rosy_field.h:37-43: field(f,i) = pow(polar(1, arg c_f), 1/N) * pow(r, i)."""
     z = np.exp(1j * np.angle(c))
     root = np.exp(np.log(z) * (1.0 / N))
     r = np.exp(1j * TWO_PI / N)
@@ -339,7 +355,7 @@ def compute_connection(m: Hmesh):
 
 
 def c_matching(m: Hmesh, field, conn, N):
-    """face_rosy_field.h:195-228 (MatchingType::Curl)."""
+    """face_rosy_field.h:169-202 (MatchingType::Curl)."""
     h = m.edge2half
     v = _normalized(m.hvec[h])
     f0, f1 = m.edge2face[:, 0], m.edge2face[:, 1]
@@ -368,7 +384,7 @@ def c_matching(m: Hmesh, field, conn, N):
 
 
 def compute_singular(m: Hmesh, effort, N):
-    """face_rosy_field.h:126-133."""
+    """face_rosy_field.h:100-107."""
     h = np.arange(m.nH)
     sgn = np.where(m.is_canonical(h), -1.0, 1.0)
     contrib = sgn * effort[m.edge[h]]
@@ -500,7 +516,7 @@ def dijkstra_unit(source, targets, VV):
 
 
 def compute_seam(m: Hmesh, singular):
-    """face_rosy_field.h:294-386."""
+    """face_rosy_field.h:268-360."""
     F = m.idx
     TT, TTi = triangle_triangle_adjacency(m)
     cuts = cut_mesh_from_singularities_zero(m, TT, TTi)
@@ -547,7 +563,7 @@ def compute_seam(m: Hmesh, singular):
 # a8  combing and extrinsic field
 # --------------------------------------------------------------------------------------------
 def combed_field(m: Hmesh, field, matching, seam, N):
-    """face_rosy_field.h:233-275."""
+    """face_rosy_field.h:207-249."""
     nF = m.nF
     out = np.zeros_like(field)
     turns = np.zeros(nF, np.int64)
@@ -576,7 +592,7 @@ def combed_field(m: Hmesh, field, matching, seam, N):
 
 
 def extrinsic_field(m: Hmesh, field):
-    """face_rosy_field.h:277-290 (N = 4)."""
+    """face_rosy_field.h:251-264 (N = 4)."""
     ext = np.empty((m.nF, 12))
     for i in range(4):
         c = field[:, i]
@@ -616,7 +632,7 @@ def cut_mesh(m: Hmesh, seam):
 # a10-a11  transitions, matchings, setup
 # --------------------------------------------------------------------------------------------
 def he2transidx(m: Hmesh, seam, singular):
-    """parameterization_setup.ipp:10-49 (closed meshes)."""
+    """parameterization_setup.ipp:11-50 (closed meshes)."""
     valence = np.zeros(m.nV, np.int64)
     np.add.at(valence, m.edge2vert[seam, 0], 1)
     np.add.at(valence, m.edge2vert[seam, 1], 1)
@@ -656,7 +672,7 @@ def he2matching(m: Hmesh, matching, N):
 
 
 def setup(m: Hmesh, cutF, n_cut, seam, singular, matching, N=4):
-    """parameterization_setup.ipp:51-170.  Returns a dict of the setup products."""
+    """parameterization_setup.ipp:52-170.  Returns a dict of the setup products."""
     n = N // 2
     lred = np.vstack([np.eye(n), -np.eye(n)])
     hti, nT = he2transidx(m, seam, singular)
@@ -854,7 +870,7 @@ def fullpiv_kernel(A):
 
 
 def build_ufull(Cfull):
-    """iter_rounding_init.h:195-251: UFull = permutation * blockdiag(I, kernel(CSmall))."""
+    """iter_rounding_init.h:98-154: UFull = permutation * blockdiag(I, kernel(CSmall))."""
     Cfull = sp.csr_matrix(Cfull)
     ncols = Cfull.shape[1]
     uniqueJ = np.unique(Cfull.indices) if Cfull.nnz else np.zeros(0, np.int64)
@@ -918,7 +934,7 @@ class _LLT:
     """CholeskyWrapper stand-in (iter_rounding.h:14-31): direct factorisation per call."""
 
     def factorize(self, A):
-        self.lu = spla.splu(sp.csc_matrix(A))
+        self.lu = spd_factor(A)
         return True
 
     def solve(self, rhs):
@@ -969,7 +985,7 @@ def _damped(J, lam):
 
 
 def lm_solve_damped(st, lam, max_iter=100, func_tol=1e-9, foo_tol=1e-9, stats=None):
-    """levenberg_marquardt.h:140-231 with DiagonalDamping(lam) (levenberg_marquardt.h:13-76),
+    """levenberg_marquardt.h:140-231 with DiagonalDamping(lam) (levenberg_marquardt.h:13-88),
     verbose = false: the normal matrix is dampJ^T dampJ; after each step the energies at prevx
     and prevx + direction decide lam /= 10 (progress to a finite energy) or lam *= 10, and dampJ is
     rebuilt from the Jacobian at the new iterate.  A factorisation failure (non-finite entries:
@@ -1114,7 +1130,7 @@ class SeamlessIntegration:
     """iter_rounding_loop.h:10-125 (frac = 1, localInjectivity = false)."""
     wInteg, wConst, wClose = 1.0, 10e4, 0.01
 
-    def __init__(self, ni: NaiveIntegration, xInit, F2, integerIdcs, singularIdcs, roundSeams):
+    def __init__(self, ni: NaiveIntegration, xInit, F2, integerIdcs, singularIdcs, roundSeams, tie_window=None):
         self.N, self.local_inj, self.intrinsic, self.wBarrier = ni.N, ni.local_inj, ni.F2, ni.wBarrier
         self.UFull = ni.UFull
         self.F2 = F2
@@ -1129,24 +1145,31 @@ class SeamlessIntegration:
         self.roundedSingulars = False
         self.leftIdcs = list(self.integerIdcs if roundSeams else self.singularIdcs)
         self.fixedIdcs, self.fixedVals = [], []
+        self.tie_window = TIE_WINDOW if tie_window is None else tie_window
         self.order_margin = []
+        self.strict_differs = []   # (step, d_pick - d_strict, d_pick) where the pick is not strict '<'
 
     def init_fixed_indices(self):
         self.xPrev = self.xCurr.copy()
         X = self.UFull @ self.xCurr
         vals = X[self.leftIdcs]
         d = np.abs(vals - cround(vals))
-        d = np.where(d <= 10e-7, 0.0, d)          # integral values (order = round-off): by position
-        # argmin with ties within 1e-6 resolved by position (the reference's strict '<' keeps
-        # the first minimum; values this close differ only by round-off, e.g. two variables
-        # tied by a constraint)
+        # the reference's pick (iter_rounding_loop.h:34-38): the first position with the
+        # smallest distance under a strict '<'
+        k_strict = int(np.argmin(d))
+        # this restatement: the first position among the candidates within TIE_WINDOW of the
+        # minimum.  Distances this close are equal in exact arithmetic (variables tied by a
+        # constraint, already-integral values), so the reference's choice among them is decided
+        # by round-off; the window only needs to exceed that round-off.
         dmin = d.min()
-        tied = d <= dmin + 10e-7
+        tied = d <= dmin + self.tie_window
         k = int(np.flatnonzero(tied)[0])
         mind = d[k]
         rest = d[~tied]
         if len(rest):
             self.order_margin.append(float(rest.min() - dmin))
+        if k != k_strict:
+            self.strict_differs.append((len(self.fixedIdcs), float(d[k] - d[k_strict]), float(d[k])))
         idx = self.leftIdcs[k]
         self.fixedIdcs.append(idx)
         self.fixedVals.append(int(cround(X[idx])))
@@ -1261,7 +1284,7 @@ def locally_injective(cfn, N=4):
 
 def iterative_rounding(fixedIdcs, fixedVals, singularIdcs, integerIdcs, length, Cfull, G2,
                        N, n, nF, seamless, roundSeams, F2, stats=None, local_injectivity=False, fullx2N=None,
-                       cutF=None):
+                       cutF=None, tie_window=None):
     """iter_rounding.h:33-113.  Returns (success, fullx, info).  local_injectivity: the NI and
     SI solves run with DiagonalDamping(0.01) and the barrier rows (needs fullx2N and cutF for
     the NI stop)."""
@@ -1280,7 +1303,7 @@ def iterative_rounding(fixedIdcs, fixedVals, singularIdcs, integerIdcs, length, 
     info["x_ni_lm"] = fullx.copy()
     if not seamless:
         return True, fullx, info
-    si = SeamlessIntegration(ni, X_, F2_, integerIdcs, singularIdcs, roundSeams)
+    si = SeamlessIntegration(ni, X_, F2_, integerIdcs, singularIdcs, roundSeams, tie_window)
     success, rounded = True, False
     resolves = 0
     xs = None
@@ -1298,7 +1321,7 @@ def iterative_rounding(fixedIdcs, fixedVals, singularIdcs, integerIdcs, length, 
             break
     fullx = (ni.UFull @ xs) if rounded else ni.x0.copy()
     info.update(si=si, fix_order=list(si.fixedIdcs), fix_vals=list(si.fixedVals),
-                resolves=resolves, margins=si.order_margin)
+                resolves=resolves, margins=si.order_margin, strict_differs=si.strict_differs)
     return success, fullx, info
 
 
@@ -1317,7 +1340,9 @@ def run_field(V, F, N=4, seed=0, n_iter=50, x0=None):
 
 
 def pipeline(V, F, ratio=0.02, N=4, seed=0, seamless=True, round_seams=False, n_iter=50,
-             x0=None, stop_after=None, local_injectivity=False):
+             x0=None, stop_after=None, local_injectivity=False, tie_window=None):
+    """example_igm.cpp:13-31.  tie_window: the greedy rounding's tie window (TIE_WINDOW when
+    None; 0 gives the reference's strict '<' pick)."""
     out = {}
     m, L, M, c, field = run_field(V, F, N, seed, n_iter, x0)
     out.update(mesh=m, L=L, M=M, compressed=c, field=field)
@@ -1349,7 +1374,7 @@ def pipeline(V, F, ratio=0.02, N=4, seed=0, seamless=True, round_seams=False, n_
     ok, fullx, info = iterative_rounding(st["fixedIdcs"], st["fixedVals"], st["singularIdcs"],
                                          st["integerIdcs"], length, Cfull, (G2 @ fullx2N).tocsr(),
                                          N, n, m.nF, seamless, round_seams, F2, stats,
-                                         local_injectivity, fullx2N, cutF)
+                                         local_injectivity, fullx2N, cutF, tie_window)
     NF = fullx2N @ fullx
     nfn = NF.reshape(-1, N)
     cfn = np.concatenate([nfn[cutF[:, j]] for j in range(3)], axis=1)
@@ -1410,7 +1435,7 @@ def size_field_gradient(out, F, s, T=None, mu=0.0):
 
 
 # --------------------------------------------------------------------------------------------
-# CurvatureAligned field (face_rosy_field.h:23-32, principalCurvatureDir :86-98, the dihedral
+# CurvatureAligned field (face_rosy_field.h:25-33, principalCurvatureDir :86-98, the dihedral
 # angle of hmesh.h:508-519, solveSquare sparse_linear_solver.h:16-27 with lambda = 0).
 # --------------------------------------------------------------------------------------------
 def principal_curvature_dir(m: Hmesh):
@@ -1436,4 +1461,4 @@ def curvature_aligned(m: Hmesh, N: int = 4):
     L = connection_laplacian(m, N)
     Mm = mass_matrix(m)
     rhs = (Mm @ D) / np.sqrt(abs(np.vdot(D, Mm @ D)))
-    return spla.splu(L.tocsc()).solve(rhs), rhs
+    return spd_factor(L).solve(rhs), rhs

@@ -22,9 +22,11 @@ def _uv_diag(x):
     return max(np.ptp(x), 1.0) * np.sqrt(2.0)
 
 
-@pytest.mark.parametrize("name", ["ico2_noise", "ico3_noise", "torus_32x16"])
+@pytest.mark.parametrize("name", ["ico2_noise", "ico3_noise", "torus_32x16", "genus2_s3", "icosphere_obj"])
 @pytest.mark.parametrize("prec", ["mixed", "fp64"])
 def test_pipeline_matches_golden(gpu_ctx, name, prec):
+    """icosphere_obj is the reference's own model (example/models/icosphere.obj, the level-4
+    workload's mesh) with the workload's radial noise; the others are seeded meshes."""
     g = np.load(GOLDEN / f"{name}.npz")
     r = M.pipeline(gpu_ctx, g["V"], g["F"], ratio=float(g["ratio"]), round_seams=bool(g["round_seams"]),
                    opts=M.solve_opts(prec, tol=TOL))
@@ -76,9 +78,42 @@ def test_igm_multigrid_device_build_matches_host(gpu_ctx, monkeypatch, name):
     assert a["stats"]["pcg_iters"] == b["stats"]["pcg_iters"]
 
 
-# full-size workloads: level-7 sphere (327,680 faces), the 1024 x 512 torus (1,048,576 faces,
-# seams rounded), the level-9 sphere with degree-16 displacement (5,242,880 faces)
+def _wrap(a):
+    return np.abs((a + np.pi) % (2.0 * np.pi) - np.pi)
+
+
+@pytest.mark.parametrize("name", ["ico5_sh8", "ico6_sh8", "ico7_sh8"])
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+def test_pipeline_matches_large_golden(gpu_ctx, name, prec):
+    """The oracle's outputs on the level-5/6/7 spheres with the level-7 workload's displacement
+    (20,480 / 81,920 / 327,680 faces; level 7 is the workload itself): singular indices, seams,
+    combed matching, the fixing order and the rounded values identical; the field within 1e-5
+    rad per face and the map within 1e-6 of its bounding-box diagonal on the stored samples."""
+    g = np.load(GOLDEN / f"{name}.npz")
+    V, F, ratio, rs = meshgen.workload(name)
+    assert len(V) == int(g["nV"]) and len(F) == int(g["nF"])
+    assert np.abs(V[g["v_sample_idx"]] - g["v_sample"]).max() <= 1e-12
+    r = M.pipeline(gpu_ctx, V, F, ratio=ratio, round_seams=rs, opts=M.solve_opts(prec, tol=TOL))
+    assert r["status"] == 0
+    assert np.array_equal(r["singular"], g["singular"].astype(np.int32))
+    assert np.array_equal(r["seam"], np.unpackbits(g["seam"])[: int(g["n_edges"])].astype(bool))
+    assert np.array_equal(r["matching"], g["combed_matching"].astype(np.int32))
+    assert r["counts"]["nT"] == int(g["nT"]) and r["counts"]["nS"] == int(g["nS"])
+    assert list(r["fix_order"]) == list(g["fix_order"])
+    assert list(r["fix_vals"]) == list(g["fix_vals"])
+    diag = max(float(g["uv_ptp"]), 1.0) * np.sqrt(2.0)
+    assert len(r["fullx"]) == int(g["n_full"])
+    assert np.abs(r["fullx"][g["fix_order"]] - g["fullx_fixed"]).max() <= 1e-6 * diag
+    assert np.abs(r["fullx"][g["x_sample_idx"]] - g["fullx_sample"]).max() <= 1e-6 * diag
+    assert np.abs(r["x_naive"][g["x_sample_idx"]] - g["x_naive_sample"]).max() <= 1e-6 * diag
+    assert _wrap(np.angle(r["compressed"][g["face_sample"]]) - g["field_angle"]).max() / 4 < 1e-5
+
+
+# full-size workloads: level-7 sphere (327,680 faces), the level-8 benchmark sphere (1,310,720
+# faces), the 1024 x 512 torus (1,048,576 faces, seams rounded), the level-9 sphere with
+# degree-16 displacement (5,242,880 faces)
 @pytest.mark.parametrize("name,prec,chi", [("ico6_sh8", "mixed", 2), ("ico7_sh8", "mixed", 2), ("ico7_sh8", "fp64", 2),
+                                           ("ico8_sh8", "mixed", 2), ("ico8_sh8", "fp64", 2),
                                            ("torus_1024x512", "mixed", 0), ("ico9_sh16", "mixed", 2)])
 def test_pipeline_size_independent_properties(gpu_ctx, name, prec, chi):
     """At sizes beyond the oracle: sum of indices = 4 chi (Poincare-Hopf), every rounded value

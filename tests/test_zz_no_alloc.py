@@ -4,8 +4,8 @@ It serves callers that cannot call cudaMalloc -- code inside a framework that ow
 memory, or code that must not allocate after start-up: they pass their own device buffers and
 the library works in a static device array.  This test calls it through the C ABI on device
 buffers (allocated here by torch, standing in for the caller's allocator) and checks it against
-mtk_field_smoothest, the regular entry point, on two calls in a row: the second call reuses the
-scratch array left by the first.  Tolerance as for the field parity tests: per-face field angle
+mtk_field_smoothest, the regular entry point, and against the oracle's direct-solve inverse
+iteration, on two calls in a row: the second call reuses the scratch array left by the first.  Tolerance as for the field parity tests: per-face field angle
 within 1e-5 rad and the Dirichlet energy within 1e-6 relative.  The file is named so pytest
 collects it last.
 """
@@ -56,12 +56,46 @@ def test_noalloc_matches_regular_entry_point_twice():
     with M.Context(0) as ctx:
         ref, _ = M.field_smoothest(ctx, nbr, theta, m.faceArea, x0, opts=M.solve_opts("fp64", tol=1e-10))
     e_ref = np.vdot(ref, L @ ref).real
+    # the oracle: 50 inverse power steps with direct solves from the same start vector
+    orc = O.smallest_eig(L, O.mass_matrix(m), x0, 50)
+    e_orc = np.vdot(orc, L @ orc).real
     for _ in range(2):
         status, c, iters = _noalloc(torch, nbr, theta, m.faceArea, x0, 50, 1e-10, 50000)
         assert status == 0, M.lib().mtk_last_error().decode()
         assert iters > 0
         assert np.abs(np.angle(c / ref)).max() / 4 < 1e-5
         assert abs(np.vdot(c, L @ c).real - e_ref) / e_ref < 1e-6
+        assert np.abs(np.angle(c / orc)).max() / 4 < 1e-5
+        assert abs(np.vdot(c, L @ c).real - e_orc) / e_orc < 1e-6
+
+
+def test_noalloc_failure_statuses():
+    """An inner solve capped at one iteration reports NOT_CONVERGED; a neighbour index outside
+    [0, nF) (here -1, as a boundary edge would give) is rejected on the device with BAD_INPUT and
+    no solve; n_iter = 0 returns the start vector.  A good call afterwards still succeeds, so no
+    state from the failed calls is left in the shared scratch array."""
+    torch = pytest.importorskip("torch")
+    m, nbr, theta = _inputs("ico3_noise")
+    x0 = O.seeded_init(m.nF, 1)
+    status, _, iters = _noalloc(torch, nbr, theta, m.faceArea, x0, 50, 1e-12, 1)
+    assert status == M._lib.NOT_CONVERGED
+    assert iters == 1
+    bad = nbr.copy()
+    bad[7, 1] = -1
+    status, _, iters = _noalloc(torch, bad, theta, m.faceArea, x0, 50, 1e-10, 50000)
+    assert status == M._lib.BAD_INPUT
+    assert iters == 0
+    assert "neighbour" in M.lib().mtk_last_error().decode()
+    bad[7, 1] = m.nF
+    status, _, _ = _noalloc(torch, bad, theta, m.faceArea, x0, 50, 1e-10, 50000)
+    assert status == M._lib.BAD_INPUT
+    status, c, iters = _noalloc(torch, nbr, theta, m.faceArea, x0, 0, 1e-10, 50000)
+    assert status == 0 and iters == 0
+    assert np.array_equal(c, x0)
+    status, c, iters = _noalloc(torch, nbr, theta, m.faceArea, x0, 50, 1e-10, 50000)
+    assert status == 0 and iters > 0
+    orc = O.smallest_eig(O.connection_laplacian(m, 4), O.mass_matrix(m), x0, 50)
+    assert np.abs(np.angle(c / orc)).max() / 4 < 1e-5
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch():
