@@ -10,13 +10,18 @@ matching, seams, cut, combing, setup and integ.  Reported:
   value  device milliseconds of the solver stages (field + naive/LM integration + rounding
          loop, CUDA events inside the library), mixed precision, median over the K steps
   e2e    wall milliseconds of the whole call with host buffers in and out (H2D/D2H inside)
-  fp64   the same device stages with the plain FP64 GPU path (timed once per run)
+  fp64   the same device stages with the plain FP64 GPU path (median over K steps after the
+         timed region)
 The L2 is flushed (256 MiB write) before every step.
 
 --impl reference: the FP64 CPU oracle (the reference algorithm restated with direct sparse
-solvers: SuperLU factorisation of L once + 50 solves, LU of the naive KKT system, one
-factorisation per LM iteration) timed on the host cores on a bounded sample of the same
-workload, extrapolated to the full solve by the operation counts (see cpu_baseline.sample).
+solves: one factorisation of L + 50 inverse-iteration solves, LU of the naive KKT system, one
+SPD factorisation per LM iteration), single-threaded on the host.  The full 1.3M-face path takes
+a quarter of an hour there, so each step runs the whole path on a seeded sample of the same
+family (the level-5 sphere, 20,480 faces) and the value is extrapolated to the workload's face
+count by the growth exponent fitted in the same run over a ladder of sizes (levels 3, 4, 5); the
+line says so (cpu_baseline.value_kind).  The GPU arm reports its own times on the sample mesh
+too, so one ratio is measured on the same configuration.
 """
 from __future__ import annotations
 
@@ -145,11 +150,12 @@ def run_ours(args):
     opts_mixed = M.solve_opts("mixed", tol=args.tol)
     opts_fp64 = M.solve_opts("fp64", tol=args.tol)
 
-    def step(opts):
+    def step(opts, mesh=None):
+        Vs, Fs, rat, rsm = mesh or (V, F, ratio, rs)
         flush_l2(flush)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        r = M.pipeline(ctx, V, F, ratio=ratio, round_seams=rs, opts=opts)
+        r = M.pipeline(ctx, Vs, Fs, ratio=rat, round_seams=rsm, opts=opts)
         wall = (time.perf_counter() - t0) * 1e3
         if r["status"] != 0:
             raise RuntimeError(f"pipeline status {r['status']}")
@@ -180,12 +186,25 @@ def run_ours(args):
     rdev = torch.device("cuda", dev) if world > 1 else None
     job = replica_job(dev_ms, walls, t_total, args.steps, world, device=rdev)
     launches = rank_sum(launches, world, device=rdev)
-    # plain FP64 GPU path, same workload (after the timed region)
+    # plain FP64 GPU path, same workload and step count (after the timed region), median
     if args.no_fp64:
         st64, fp64_ms = {"pcg_iters": None}, None
     else:
-        r64, st64, wall64 = step(opts_fp64)
-        fp64_ms = st64["ms_field"] + st64["ms_integrate"] + st64["ms_rounding"]
+        runs64 = [step(opts_fp64) for _ in range(args.steps)]
+        ms64 = [x[1]["ms_field"] + x[1]["ms_integrate"] + x[1]["ms_rounding"] for x in runs64]
+        fp64_ms = statistics.median(ms64)
+        st64 = runs64[len(runs64) // 2][1]
+    # the same pipeline on the CPU baseline's sample mesh (the top rung of its ladder), so that
+    # one GPU/CPU ratio is measured on the same configuration
+    same = None
+    if not args.no_cpu:
+        sm = meshgen.workload(LADDER[-1], seed=rank)
+        step(opts_mixed, sm)
+        runs_s = [step(opts_mixed, sm) for _ in range(max(3, min(args.steps, 5)))]
+        same = {"workload": LADDER[-1], "faces": len(sm[1]),
+                "value": round(statistics.median([x[1]["ms_field"] + x[1]["ms_integrate"] + x[1]["ms_rounding"]
+                                                  for x in runs_s]), 3),
+                "e2e": round(statistics.median([x[2] for x in runs_s]), 3), "unit": "ms", "steps": len(runs_s)}
     # stand-alone SpMV of the field operator (after the timed region): FP32 and FP64, each SpMV
     # after an L2 flush, CUDA events around the kernel alone
     spmv = None
@@ -223,6 +242,10 @@ def run_ours(args):
     h2d = world * (V.nbytes + F.nbytes)      # every rank copies a mesh of the same size
     d2h = world * (r["cfn"].nbytes + r["fullx"].nbytes + r["singular"].nbytes + r["compressed"].nbytes)
     cpu = cpu_baseline(args) if (rank == 0 and not args.no_cpu) else None
+    if same is not None and cpu is not None:
+        same["cpu_ms"] = cpu["measured"]["ms"]
+        same["cpu_over_gpu_e2e"] = round(cpu["measured"]["ms"] / same["e2e"], 2)
+        same["cpu_over_gpu_value"] = round(cpu["measured"]["ms"] / same["value"], 2)
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "ms", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(job["ms_per_step"], 3), "higher_is_better": False,
@@ -237,12 +260,20 @@ def run_ours(args):
         "e2e": {"value": round(job["e2e"], 3), "unit": "ms", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "fp64_gpu_ms": round(fp64_ms, 3) if fp64_ms else None,
+        "fp64_gpu_steps": None if args.no_fp64 else args.steps,
         "mixed_vs_fp64_speedup": (round(fp64_ms / statistics.median(dev_ms), 3)     # this rank's own runs
                                   if (fp64_ms and statistics.median(dev_ms) > 0) else None),
         "stages_ms": {"field": round(st["ms_field"], 3), "integrate": round(st["ms_integrate"], 3),
                       "rounding": round(st["ms_rounding"], 3), "host": round(st["ms_host"], 3)},
         "solver": {"pcg_iters": st["pcg_iters"], "solves": st["solves"], "resolves": st["resolves"],
                    "max_rel_residual": st["max_rel_residual"], "fp64_pcg_iters": st64["pcg_iters"]},
+        "rounding_order": {"min_order_margin": st.get("min_order_margin"),
+                           "strict_order_differs": st.get("strict_order_differs"),
+                           "strict_order_gap": st.get("strict_order_gap"),
+                           "note": ("greedy picks tied within 1e-8 are taken by position; strict_order_differs "
+                                    "counts the steps whose pick is not the strict '<' pick, strict_order_gap the "
+                                    "largest distance gap between the two")},
+        "same_config": same,
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1) if achieved else None,
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
@@ -264,45 +295,116 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
-SAMPLE_ALPHA = 1.34   # growth of the sparse LU factorisation time with faces (20K -> 80K faces)
+LADDER = ["ico3_sh8", "ico4_sh8", "ico5_sh8"]   # CPU sample sizes: 1,280 / 5,120 / 20,480 faces
+
+
+def cpu_info():
+    """Host CPU model and core count (lscpu, else /proc/cpuinfo)."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    if model is None:
+        try:
+            for line in Path("/proc/cpuinfo").read_text().splitlines():
+                if line.lower().startswith(("model name", "cpu model")):
+                    model = line.split(":", 1)[1].strip()
+                    break
+        except Exception:
+            pass
+    return {"cpu_model": model, "host_cores": os.cpu_count()}
+
+
+def time_oracle(name):
+    """The whole oracle path on one seeded workload, single-threaded: (ms, faces, re-solves,
+    factorisations)."""
+    from metriko_gb300 import meshgen
+    from oracle import metriko_oracle as O
+
+    V, F, ratio, rs = meshgen.workload(name)
+    t0 = time.perf_counter()
+    out = O.pipeline(V, F, ratio=ratio, round_seams=rs)
+    ms = (time.perf_counter() - t0) * 1e3
+    return ms, len(F), out["info"].get("resolves"), out["stats"].get("factorizations")
+
+
+def fit_growth(points):
+    """Least-squares fit of log(ms) = a + b log(faces): (b, rms of the log residuals)."""
+    x = np.log([p[0] for p in points])
+    y = np.log([p[1] for p in points])
+    b, a = np.polyfit(x, y, 1)
+    rms = float(np.sqrt(np.mean((y - (a + b * x)) ** 2)))
+    return float(b), rms
+
+
+def extrapolation(points, faces_target):
+    """(ms at faces_target, exponent, rms): the largest measured point scaled by the fitted
+    growth exponent."""
+    b, rms = fit_growth(points)
+    f_top, t_top = max(points)
+    return t_top * (faces_target / f_top) ** b, b, rms
+
+
+def workload_faces(name):
+    from metriko_gb300 import meshgen
+    return len(meshgen.workload(name)[1])
 
 
 def cpu_baseline(args):
     """FP64 CPU oracle (the reference algorithm with direct sparse solves) timed on a bounded
-    sample: the full path on a smaller mesh of the same family, single thread, then scaled to
-    the workload's face count by (F / F_sample)^SAMPLE_ALPHA."""
-    from metriko_gb300 import meshgen
-    from oracle import metriko_oracle as O
-
-    V, F, ratio, rs = meshgen.workload(args.sample_workload)
-    Vw, Fw, _, _ = meshgen.workload(args.workload) if args.workload != args.sample_workload else (V, F, 0, 0)
-    t0 = time.perf_counter()
-    out = O.pipeline(V, F, ratio=ratio, round_seams=rs)
-    t = (time.perf_counter() - t0) * 1e3
-    nF, nFw = len(F), len(Fw)
-    scaled = t * (nFw / nF) ** SAMPLE_ALPHA
-    return {"value": round(scaled, 1), "unit": "ms", "cores": 1, "kind": "port",
-            "sample": (f"full oracle path (SuperLU field factorisation + 50 solves, KKT LU, one factorisation "
-                       f"per LM iteration) on {args.sample_workload} ({nF} faces) = {t:.0f} ms single-threaded, "
-                       f"scaled to {nFw} faces by (F/F_sample)^{SAMPLE_ALPHA}"),
-            "measured_ms": round(t, 1), "sample_faces": nF, "resolves": out["info"].get("resolves"),
-            "factorizations": out["stats"].get("factorizations")}
+    sample: the whole path once on each rung of LADDER, single-threaded; the value is the top
+    rung's time extrapolated to the workload's face count by the exponent fitted over the
+    ladder (labelled value_kind "extrapolated"); the top rung's measured time is the
+    same-configuration number (`measured`)."""
+    ladder = []
+    for name in LADDER:
+        ms, nf, rsv, fac = time_oracle(name)
+        ladder.append({"workload": name, "faces": nf, "ms": round(ms, 1), "resolves": rsv, "factorizations": fac})
+    nFw = workload_faces(args.workload)
+    v, b, rms = extrapolation([(r["faces"], r["ms"]) for r in ladder], nFw)
+    top = ladder[-1]
+    return {"value": round(v, 1), "unit": "ms", "cores": 1, "kind": "port", "value_kind": "extrapolated",
+            "sample": (f"whole oracle path (field: one SPD factorisation + 50 solves; naive KKT LU; one SPD "
+                       f"factorisation per LM iteration) single-threaded on {', '.join(LADDER)}; "
+                       f"{top['workload']} ({top['faces']} faces) = {top['ms']:.0f} ms measured, extrapolated to "
+                       f"{nFw} faces by the fitted exponent {b:.3f}"),
+            "exponent": round(b, 4), "fit_rms_log": round(rms, 4), "ladder": ladder,
+            "measured": {"workload": top["workload"], "faces": top["faces"], "ms": top["ms"]}, **cpu_info()}
 
 
 def run_reference(args):
+    """The reference arm: every step runs the whole oracle path on the sample mesh (the top rung
+    of LADDER); the lower rungs run once before the timed steps (with the warm-up) to fit the
+    growth exponent, which the steps' median also enters."""
     rank, world = env_rank()
     if rank != 0:
         return
-    for _ in range(max(0, min(args.warmup, 1))):
-        cpu_baseline(args)
-    vals = [cpu_baseline(args) for _ in range(max(1, args.steps))]
-    cpu = vals[len(vals) // 2]
-    v = statistics.median([c["value"] for c in vals])
-    cpu["value"] = v
+    for _ in range(max(0, min(args.warmup, 2))):
+        time_oracle(LADDER[0])
+    low = [time_oracle(name) for name in LADDER[:-1]]
+    steps = [time_oracle(LADDER[-1]) for _ in range(max(1, args.steps))]
+    t_med = statistics.median([s[0] for s in steps])
+    pts = [(f, ms) for ms, f, _, _ in low] + [(steps[0][1], t_med)]
+    nFw = workload_faces(args.workload)
+    v, b, rms = extrapolation(pts, nFw)
+    v = round(v, 1)
+    cpu = {"value": v, "unit": "ms", "cores": 1, "kind": "port", "value_kind": "extrapolated",
+           "sample": (f"whole oracle path single-threaded on {LADDER[-1]} ({steps[0][1]} faces) every step, median "
+                      f"{t_med:.0f} ms; extrapolated to {nFw} faces by the exponent {b:.3f} fitted over "
+                      f"{', '.join(LADDER)} (rms of log residuals {rms:.3f})"),
+           "exponent": round(b, 4), "fit_rms_log": round(rms, 4),
+           "ladder": [{"faces": f, "ms": round(ms, 1)} for f, ms in pts],
+           "measured": {"workload": LADDER[-1], "faces": steps[0][1], "ms": round(t_med, 1),
+                        "resolves": steps[0][2], "factorizations": steps[0][3]}, **cpu_info()}
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "ms", "n_gpus": world,
-            "steps": len(vals), "warmup": args.warmup, "higher_is_better": False, "dtype": "f64",
+            "steps": len(steps), "warmup": args.warmup, "higher_is_better": False, "dtype": "f64",
             "data": "synthetic (seeded mesh generator)", "vs_baseline": None,
-            "config": {"workload": args.workload, "sample_workload": args.sample_workload},
+            "config": {"workload": args.workload, "sample_workload": LADDER[-1]},
             "cpu_baseline": cpu,
             "e2e": {"value": v, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -315,7 +417,6 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ico8_sh8")
-    ap.add_argument("--sample-workload", default="ico4_sh8")
     ap.add_argument("--tol", type=float, default=1e-8)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 GPU comparison run (profiling runs)")

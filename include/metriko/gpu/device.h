@@ -12,9 +12,16 @@
 #include "metriko_cuda.h"
 
 namespace metriko::gpu {
+    // A failed library call: carries the mtk_status, so callers above the C++ API (the C ABI
+    // pipeline entry points) can hand the same status on.
+    struct status_error : std::runtime_error {
+        int status;
+        status_error(int s, const std::string& msg) : std::runtime_error(msg), status(s) {}
+    };
+
     inline void check(int status, const char* what) {
         if (status != MTK_OK)
-            throw std::runtime_error(std::string(what) + ": " + mtk_status_string(status) + " " + mtk_last_error());
+            throw status_error(status, std::string(what) + ": " + mtk_status_string(status) + " " + mtk_last_error());
     }
 
     // Solver options shared by the header-only entry points (FaceRosyField, integ()).

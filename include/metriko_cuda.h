@@ -94,11 +94,13 @@ typedef struct {
     int64_t igm_pcg_launches;
     double igm_pcg_ms;
     double igm_pcg_bytes;
-    /* greedy rounding: steps whose pick (first position among the candidates within 1e-8 of
-       the smallest distance to an integer) is not the strict '<' pick of the reference, and the
-       largest distance gap between the two picks over those steps                           */
+    /* greedy rounding: steps whose pick (distances <= 1e-6 count as 0; first position among
+       the candidates within 1e-8 of the smallest distance) is not the strict '<' pick of the
+       reference -- among fractional candidates (with the largest distance gap between the two
+       picks), and among already-integral ones (no re-solve follows such a pick)              */
     int64_t strict_order_differs;
     double strict_order_gap;
+    int64_t integral_order_differs;
 } mtk_stats;
 
 const char* mtk_status_string(int status);

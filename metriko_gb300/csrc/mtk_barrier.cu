@@ -78,6 +78,7 @@ extern "C" int mtk_injective_barrier(mtk_ctx* c, int32_t nF, int32_t N, const do
         return MTK_ERR_BAD_INPUT;
     if (nF == 0) return MTK_OK;
     MTK_CUDA_TRY(cudaSetDevice(c->device));
+    AllocStreamScope alloc_scope(c->stream);
     cudaStream_t st = c->stream;
     const size_t nv = 2 * (size_t)N * nF, nr = (size_t)N * nF;
     DBuf<double> dF2, dfield, dfB, ddB, dS;
@@ -105,6 +106,7 @@ extern "C" int mtk_local_injectivity(mtk_ctx* c, int32_t nF, int32_t N, const do
     if (first_flipped) *first_flipped = nF;
     if (nF == 0) return MTK_OK;
     MTK_CUDA_TRY(cudaSetDevice(c->device));
+    AllocStreamScope alloc_scope(c->stream);
     cudaStream_t st = c->stream;
     DBuf<double> dc;
     MTK_TRY(dc.upload(cfn, 3 * (size_t)N * nF, st));

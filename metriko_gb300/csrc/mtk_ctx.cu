@@ -66,6 +66,14 @@ extern "C" int mtk_ctx_create(int device, mtk_ctx** out) {
     if (e == cudaSuccess) e = cudaMallocHost(&c->h_int, sizeof(int) * 16);
     if (e == cudaSuccess) e = cudaMemset(c->bar, 0, 4 * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMemset(c->dev_err, 0, sizeof(int));
+    // the device's default memory pool serves the stream-ordered buffers of every call; keep
+    // what it has allocated between calls (released by mtk_ctx_destroy)
+    if (e == cudaSuccess) {
+        cudaMemPool_t pool;
+        e = cudaDeviceGetDefaultMemPool(&pool, device);
+        uint64_t keep = UINT64_MAX;
+        if (e == cudaSuccess) e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
     if (e != cudaSuccess) {
         mtk_set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
         mtk_ctx_destroy(c);
@@ -79,6 +87,10 @@ extern "C" int mtk_ctx_destroy(mtk_ctx* c) {
     if (!c) return MTK_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    {
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, c->device) == cudaSuccess) cudaMemPoolTrimTo(pool, 0);
+    }
     if (c->bar) cudaFree(c->bar);
     if (c->dev_err) cudaFree(c->dev_err);
     if (c->partials) cudaFree(c->partials);

@@ -28,31 +28,63 @@ struct mtk_ctx {
 
 namespace mtk {
 
-// RAII device buffer (allocation happens once per solve set-up, never inside the loops).
+// Stream of the context call running on this host thread (set by AllocStreamScope at the entry
+// points): device buffers are then allocated and freed in that stream's order from the device's
+// memory pool, whose release threshold the context raises, so a repeated call reuses the pool's
+// blocks instead of calling cudaMalloc / cudaFree (and the device-wide synchronisation of
+// cudaFree).  Every use of such a buffer is on the same stream.
+inline cudaStream_t& alloc_stream() {
+    static thread_local cudaStream_t s = nullptr;
+    return s;
+}
+struct AllocStreamScope {
+    cudaStream_t prev;
+    explicit AllocStreamScope(cudaStream_t s) : prev(alloc_stream()) { alloc_stream() = s; }
+    ~AllocStreamScope() { alloc_stream() = prev; }
+    AllocStreamScope(const AllocStreamScope&) = delete;
+    AllocStreamScope& operator=(const AllocStreamScope&) = delete;
+};
+
+// RAII device buffer (allocation happens once per solve set-up, never inside the loops):
+// stream-ordered inside a context call, plain cudaMalloc outside one.
 template <typename T>
 struct DBuf {
     T* p = nullptr;
     size_t n = 0;
+    cudaStream_t s = nullptr;   // stream of a stream-ordered allocation
+    bool async = false;
     DBuf() = default;
     DBuf(const DBuf&) = delete;
     DBuf& operator=(const DBuf&) = delete;
-    DBuf(DBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    DBuf(DBuf&& o) noexcept : p(o.p), n(o.n), s(o.s), async(o.async) { o.p = nullptr; o.n = 0; }
     DBuf& operator=(DBuf&& o) noexcept {
         if (this != &o) {
-            if (p) cudaFree(p);
+            release();
             p = o.p;
             n = o.n;
+            s = o.s;
+            async = o.async;
             o.p = nullptr;
             o.n = 0;
         }
         return *this;
     }
-    ~DBuf() { if (p) cudaFree(p); }
+    ~DBuf() { release(); }
+    void release() {
+        if (p) {
+            if (async) cudaFreeAsync(p, s);
+            else cudaFree(p);
+        }
+        p = nullptr;
+    }
     int alloc(size_t count) {
-        if (p) { cudaFree(p); p = nullptr; }
+        release();
         n = count;
         if (count == 0) return MTK_OK;
-        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        s = alloc_stream();
+        async = s != nullptr;
+        cudaError_t e = async ? cudaMallocAsync(reinterpret_cast<void**>(&p), count * sizeof(T), s)
+                              : cudaMalloc(&p, count * sizeof(T));
         if (e != cudaSuccess) { mtk_set_last_error(cudaGetErrorString(e), __FILE__, __LINE__); p = nullptr; return MTK_ERR_CUDA; }
         return MTK_OK;
     }

@@ -1216,6 +1216,7 @@ int field_run(mtk_ctx* c, int32_t nF, int32_t nRosy, const int32_t* nbr_h, const
     mtk_default_opts(&opts);
     if (opts_in) opts = *opts_in;
     MTK_CUDA_TRY(cudaSetDevice(c->device));
+    AllocStreamScope alloc_scope(c->stream);
     FieldSolver S;
     S.c = c;
     S.n = nF;
@@ -1496,6 +1497,7 @@ extern "C" int mtk_field_spmv_bench(mtk_ctx* c, int32_t nF, int32_t nRosy, const
     for (int64_t i = 0; i < 3 * (int64_t)nF; i++)
         if (nbr_h[i] < 0 || nbr_h[i] >= nF) return MTK_ERR_BAD_INPUT;
     MTK_CUDA_TRY(cudaSetDevice(c->device));
+    AllocStreamScope alloc_scope(c->stream);
     cudaStream_t st = c->stream;
     const int n = nF;
     DBuf<int> nbr_in, nbr;

@@ -697,11 +697,12 @@ __global__ void fixed_values(int nfix, const int* __restrict__ fixed, const int*
 
 // Greedy pick of SeamlessIntegration::initFixedIndices (iter_rounding_loop.h:34-38) over the left
 // indices, one CTA.  The reference keeps the first position with the smallest |X - round X|
-// under a strict '<'; candidates within kTieWindow of the smallest distance are equal in exact
-// arithmetic (variables tied by a constraint, already-integral values), so among them the first
-// position is taken and round-off cannot reorder them.
+// under a strict '<'.  Here distances within its integrality threshold (1e-6, :73: no re-solve
+// follows) count as 0, and candidates within kTieWindow of the smallest distance are taken by
+// position: they are equal in exact arithmetic (variables tied by a constraint, already-integral
+// values), so round-off and the reference's O(1 / penalty) residuals cannot reorder them.
 // out: [0] pick position, [1] its distance, [2] its X, [3] smallest distance outside the tie
-// group (1e300 when none), [4] the strict '<' pick position, [5] its distance.
+// group (1e300 when none), [4] the strict '<' pick position (raw distances), [5] its distance.
 constexpr double kTieWindow = 1e-8;
 
 __global__ void round_argmin(int nLeft, const int* __restrict__ left, const int* __restrict__ full2y,
@@ -709,7 +710,7 @@ __global__ void round_argmin(int nLeft, const int* __restrict__ left, const int*
                              const double* __restrict__ xs, double* out) {
     __shared__ double sd[kStream];
     __shared__ int si[kStream];
-    // pass 1: smallest distance and the first position holding it
+    // pass 1: smallest raw distance and the first position holding it (the strict '<' pick)
     double bd = 1e300;
     int bk = 0x7fffffff;
     for (int t = threadIdx.x; t < nLeft; t += blockDim.x) {
@@ -731,8 +732,9 @@ __global__ void round_argmin(int nLeft, const int* __restrict__ left, const int*
         }
         __syncthreads();
     }
-    const double dmin = sd[0];
+    const double draw_min = sd[0];
     const int kstrict = si[0];
+    const double dmin = draw_min <= 10e-7 ? 0.0 : draw_min;
     __syncthreads();
     // pass 2: first position inside the tie group, and the best distance outside it
     int bi = 0x7fffffff;
@@ -740,6 +742,7 @@ __global__ void round_argmin(int nLeft, const int* __restrict__ left, const int*
     for (int t = threadIdx.x; t < nLeft; t += blockDim.x) {
         double X = left_value(left[t], full2y, full2j, nY, nZ, Us, xs);
         double d = fabs(X - round(X));
+        if (d <= 10e-7) d = 0.0;
         if (d <= dmin + kTieWindow) {
             if (t < bi) { bi = t; bX = X; bdist = d; }
         } else {
@@ -760,7 +763,7 @@ __global__ void round_argmin(int nLeft, const int* __restrict__ left, const int*
     }
     if (threadIdx.x == 0) {
         out[0] = (double)si[0]; out[1] = sdd[0]; out[2] = sX[0]; out[3] = so[0];
-        out[4] = (double)kstrict; out[5] = dmin;
+        out[4] = (double)kstrict; out[5] = draw_min;
     }
 }
 
@@ -1445,6 +1448,7 @@ int igm_run(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts_in, do
     mtk_default_opts(&o);
     if (opts_in) o = *opts_in;
     MTK_CUDA_TRY(cudaSetDevice(c->device));
+    AllocStreamScope alloc_scope(c->stream);
     auto t_start = std::chrono::steady_clock::now();
     Igm S;
     S.c = c;
@@ -2080,10 +2084,14 @@ int igm_run(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts_in, do
         const int k = (int)h_arg[0];
         const double mind = h_arg[1];
         if (Igm::debug()) fprintf(stderr, "[round] left=%zu pick=%d full=%d X=%.9f d=%.3e second=%.3e\n", leftv.size(), k, leftv[k], h_arg[2], mind, h_arg[3]);
-        if (h_arg[3] < 1e299) min_margin = std::min(min_margin, h_arg[3] - h_arg[5]);
+        if (h_arg[3] < 1e299) min_margin = std::min(min_margin, h_arg[3] - mind);
         if ((int)h_arg[4] != k) {   // a tie resolved by position, not by the strict '<'
-            stt->strict_order_differs++;
-            stt->strict_order_gap = std::max(stt->strict_order_gap, mind - h_arg[5]);
+            if (mind > 10e-7) {     // among fractional candidates
+                stt->strict_order_differs++;
+                stt->strict_order_gap = std::max(stt->strict_order_gap, std::fabs(h_arg[2] - std::round(h_arg[2])) - h_arg[5]);
+            } else {                // among already-integral candidates (no re-solve follows)
+                stt->integral_order_differs++;
+            }
         }
         const int idx = leftv[k];
         const int ival = (int)std::round(h_arg[2]);

@@ -141,6 +141,9 @@ extern "C" int mtk_pipeline_run(mtk_ctx* ctx, int32_t nV, int32_t nF, const doub
     } catch (const std::invalid_argument& e) {
         mtk_set_last_error(e.what(), __FILE__, __LINE__);
         return MTK_ERR_BAD_INPUT;
+    } catch (const metriko::gpu::status_error& e) {
+        mtk_set_last_error(e.what(), __FILE__, __LINE__);
+        return e.status;
     } catch (const std::exception& e) {
         mtk_set_last_error(e.what(), __FILE__, __LINE__);
         return MTK_ERR_CUDA;
@@ -194,6 +197,9 @@ extern "C" int mtk_pipeline_size_field_gradient(mtk_ctx* ctx, int32_t nV, int32_
     } catch (const std::invalid_argument& e) {
         mtk_set_last_error(e.what(), __FILE__, __LINE__);
         return MTK_ERR_BAD_INPUT;
+    } catch (const metriko::gpu::status_error& e) {
+        mtk_set_last_error(e.what(), __FILE__, __LINE__);
+        return e.status;
     } catch (const std::exception& e) {
         mtk_set_last_error(e.what(), __FILE__, __LINE__);
         return MTK_ERR_CUDA;
@@ -259,6 +265,9 @@ extern "C" int mtk_topology_from_field(int32_t nV, int32_t nF, const double* Vb,
     } catch (const std::invalid_argument& e) {
         mtk_set_last_error(e.what(), __FILE__, __LINE__);
         return MTK_ERR_BAD_INPUT;
+    } catch (const metriko::gpu::status_error& e) {
+        mtk_set_last_error(e.what(), __FILE__, __LINE__);
+        return e.status;
     } catch (const std::exception& e) {
         mtk_set_last_error(e.what(), __FILE__, __LINE__);
         return MTK_ERR_BAD_INPUT;

@@ -40,11 +40,13 @@ Deliberate, documented choices (identical in the product path):
     is the same;
   * the constraint kernel basis restates Eigen's FullPivLU::kernel (complete pivoting, first
     maximum in column-major order, identity on the free columns);
-  * greedy rounding (iter_rounding_loop.h:34-38) picks the first position among candidates
-    whose distance to an integer is within TIE_WINDOW = 1e-8 of the minimum; the reference's
-    strict '<' among such candidates is decided by round-off (structural ties between
-    constraint-linked variables, already-integral values).  Every step where this pick differs
-    from the strict '<' pick is recorded (info["strict_differs"]: step, distance gap).
+  * greedy rounding (iter_rounding_loop.h:34-38): distances within the reference's own
+    integrality threshold (1e-6, :73) count as 0, and the pick is the first position among the
+    candidates within TIE_WINDOW = 1e-8 of the minimum; the reference's strict '<' among such
+    candidates is decided by round-off (structural ties between constraint-linked variables)
+    and by the O(1 / penalty) residuals of already-integral values.  Every step where this pick
+    differs from the strict '<' pick is recorded (info["strict_differs"]: step, distance gap,
+    distance of the pick).
 Closed, consistently oriented, edge-manifold triangle meshes only.
 
 Parity status: the reference cannot be compiled here (Eigen, libigl, SuiteSparse absent) and
@@ -1157,10 +1159,14 @@ class SeamlessIntegration:
         # the reference's pick (iter_rounding_loop.h:34-38): the first position with the
         # smallest distance under a strict '<'
         k_strict = int(np.argmin(d))
-        # this restatement: the first position among the candidates within TIE_WINDOW of the
-        # minimum.  Distances this close are equal in exact arithmetic (variables tied by a
-        # constraint, already-integral values), so the reference's choice among them is decided
-        # by round-off; the window only needs to exceed that round-off.
+        # this restatement: distances within the reference's integrality threshold (1e-6, the
+        # test of iter_rounding_loop.h:73, below which no re-solve follows) count as 0, and the
+        # pick is the first position among the candidates within TIE_WINDOW of the minimum.
+        # Distances this close are equal in exact arithmetic (variables tied by a constraint,
+        # already-integral values whose residual is O(1 / penalty)), so the reference's choice
+        # among them is decided by round-off and penalty residuals.
+        if self.tie_window > 0:
+            d = np.where(d <= 10e-7, 0.0, d)
         dmin = d.min()
         tied = d <= dmin + self.tie_window
         k = int(np.flatnonzero(tied)[0])
@@ -1169,7 +1175,8 @@ class SeamlessIntegration:
         if len(rest):
             self.order_margin.append(float(rest.min() - dmin))
         if k != k_strict:
-            self.strict_differs.append((len(self.fixedIdcs), float(d[k] - d[k_strict]), float(d[k])))
+            draw = np.abs(vals - cround(vals))
+            self.strict_differs.append((len(self.fixedIdcs), float(draw[k] - draw[k_strict]), float(draw[k])))
         idx = self.leftIdcs[k]
         self.fixedIdcs.append(idx)
         self.fixedVals.append(int(cround(X[idx])))

@@ -14,7 +14,8 @@ matching, the fixing order and values, the counts -- and the floating-point outp
 seeded sample (the field angle per face and the map's values at every fixed variable and at a
 sample of the others); their meshes are regenerated by metriko_gb300.meshgen, checked against
 stored sample positions.  Each fixture also records the oracle's tie statistics (steps where
-the greedy pick differs from the strict '<' pick, the smallest margin) and its run time.
+the greedy pick differs from the strict '<' pick among fractional and among already-integral
+candidates, the smallest margin) and its run time.
 
 Run:  python tests/golden/make_golden.py [name ...]   (all fixtures when no name is given)
 """
@@ -39,8 +40,9 @@ SAMPLE = 32768
 
 def _tie_stats(info):
     sd = info["strict_differs"]
-    return dict(strict_differs=np.int32(len(sd)),
-                strict_gap_max=np.float64(max((g for _, g, _ in sd), default=0.0)),
+    frac = [g for _, g, dp in sd if dp > 10e-7]
+    return dict(strict_differs=np.int32(len(frac)), integral_differs=np.int32(len(sd) - len(frac)),
+                strict_gap_max=np.float64(max(frac, default=0.0)),
                 min_margin=np.float64(min(info["margins"]) if info["margins"] else np.inf),
                 resolves=np.int32(info["resolves"]))
 
@@ -92,7 +94,8 @@ def main(names):
         np.savez_compressed(Path(__file__).parent / f"{name}.npz", **data)
         info = out["info"]
         print(f"{name}: {len(F)} faces, {len(info['fix_order'])} fixings, {info['resolves']} re-solves, "
-              f"{len(info['strict_differs'])} steps differ from strict '<', oracle {seconds:.1f} s", flush=True)
+              f"{int(data['strict_differs'])} fractional / {int(data['integral_differs'])} integral steps differ "
+              f"from strict '<', oracle {seconds:.1f} s", flush=True)
 
 
 if __name__ == "__main__":

@@ -54,7 +54,7 @@ def fake_bench(monkeypatch):
     monkeypatch.setattr(meshgen, "workload", lambda name, seed=0: small)
     monkeypatch.setattr(meshgen, "icosphere", lambda lvl: small[:2])
     monkeypatch.setattr(bench, "cpu_baseline", lambda args: {"value": 1.0, "unit": "ms", "cores": 1, "kind": "port",
-                                                             "sample": "fake"})
+                                                             "sample": "fake", "measured": {"ms": 5000.0}})
     monkeypatch.setenv("RANK", "0")
     monkeypatch.setenv("WORLD_SIZE", "1")
     return bench, small
@@ -65,7 +65,7 @@ def test_bench_line_carries_the_contract_keys(fake_bench, capsys):
 
     class A:
         gpus, steps, warmup, impl = 1, 3, 3, "ours"
-        workload, sample_workload, tol = "ico8_sh8", "ico4_sh8", 1e-8
+        workload, tol = "ico8_sh8", 1e-8
         no_cpu = no_fp64 = no_spmv = False
 
     bench.run_ours(A())
@@ -86,3 +86,17 @@ def test_bench_line_carries_the_contract_keys(fake_bench, capsys):
     assert r["frac"] == pytest.approx(r["achieved"] / r["peak"], rel=1e-3)
     assert line["spmv"]["level9"]["kernel"] == "spmv_ell<float>"
     assert "l2" in line["config"] and line["config"]["workload"] == "ico8_sh8"
+    same = line["same_config"]          # the GPU on the CPU baseline's sample mesh
+    assert same["workload"] == bench.LADDER[-1] and same["value"] == 1000.0
+    assert same["cpu_ms"] == 5000.0 and same["cpu_over_gpu_value"] == 5.0
+    assert line["fp64_gpu_steps"] == 3
+
+
+def test_growth_fit_and_extrapolation():
+    sys.path.insert(0, str(ROOT))
+    import bench
+    pts = [(1280, 2.0 * 1280 ** 1.3), (5120, 2.0 * 5120 ** 1.3), (20480, 2.0 * 20480 ** 1.3)]
+    b, rms = bench.fit_growth(pts)
+    assert b == pytest.approx(1.3, abs=1e-9) and rms < 1e-9
+    v, b2, _ = bench.extrapolation(pts, 1310720)
+    assert v == pytest.approx(2.0 * 1310720 ** 1.3, rel=1e-9) and b2 == pytest.approx(1.3)

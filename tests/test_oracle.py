@@ -144,9 +144,9 @@ def test_oracle_reproduces_golden(name):
 
 @pytest.mark.parametrize("name", ["ico2_noise", "ico3_noise", "torus_32x16", "genus2_s3"])
 def test_tie_window_matches_strict_order_up_to_roundoff_ties(name):
-    """The greedy rounding takes the first position among candidates within TIE_WINDOW (1e-8) of
-    the smallest distance; the reference keeps the first strict '<' minimum
-    (iter_rounding_loop.h:34-38).  Run both ways, the two give the same fixed (index, value)
+    """The greedy rounding counts distances <= 1e-6 as 0 and takes the first position among
+    candidates within TIE_WINDOW (1e-8) of the smallest distance; the reference keeps the first
+    strict '<' minimum (iter_rounding_loop.h:34-38).  Run both ways, the two give the same fixed (index, value)
     pairs, the same number of re-solves and the same map; every step whose pick differs is a
     tie of a few 1e-9 at most (round-off between constraint-linked or already-integral values)."""
     V, F, ratio, rs, out = oracle_run(name)
@@ -156,7 +156,10 @@ def test_tie_window_matches_strict_order_up_to_roundoff_ties(name):
     assert a["resolves"] == b["resolves"]
     diag = np.ptp(out["fullx"]) * np.sqrt(2.0)
     assert np.abs(out["fullx"] - strict["fullx"]).max() <= 1e-9 * diag
-    assert all(gap <= 5e-9 for _, gap, _ in a["strict_differs"])
+    # fractional ties: round-off between constraint-linked values; already-integral picks
+    # (distance <= 1e-6, no re-solve) differ by the O(1 / penalty) residuals
+    assert all(gap <= 5e-9 for _, gap, dp in a["strict_differs"] if dp > 1e-6)
+    assert all(dp <= 1e-6 + 5e-9 for _, gap, dp in a["strict_differs"] if gap > 5e-9)
     assert b["strict_differs"] == []
     # the margin to the best candidate outside a tie group is far above the window
     assert min(a["margins"]) > 1e-5

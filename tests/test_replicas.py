@@ -69,7 +69,7 @@ def test_reference_arm_prints_only_on_rank_zero(monkeypatch, capsys):
     monkeypatch.setenv("WORLD_SIZE", "2")
 
     class A:
-        warmup, steps, workload, sample_workload = 3, 2, "ico8_sh8", "ico4_sh8"
+        warmup, steps, workload = 3, 2, "ico8_sh8"
 
     bench.run_reference(A())          # rank 1 returns at once: no work, no line
     assert capsys.readouterr().out == ""
