@@ -512,6 +512,10 @@ struct DevCsr {
     const int* ptr;
     const int* col;
     const V2* val;
+    // SELL-32 copy (mtk_sell.cuh), used by one-lane-per-row phases when present
+    const int* sptr = nullptr;
+    const int* scol = nullptr;
+    const V2* sval = nullptr;
 };
 
 template <typename T>

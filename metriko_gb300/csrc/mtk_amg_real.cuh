@@ -429,6 +429,10 @@ struct RDevCsr {
     const int* ptr;
     const int* col;
     const T* val;
+    // SELL-32 copy (mtk_sell.cuh), used by the one-lane-per-row phases when present
+    const int* sptr = nullptr;
+    const int* scol = nullptr;
+    const T* sval = nullptr;
 };
 
 template <typename T>
@@ -470,6 +474,36 @@ __device__ __forceinline__ T rcsr_row(const RDevCsr<T>& M, int row, int lane, in
     return s;
 }
 
+// Row sum of the SELL-32 copy: the lane of `row` within its slice walks the row's entries in
+// CSR order, four loads in flight, each load coalesced across the slice's 32 lanes.
+template <typename T>
+__device__ __forceinline__ T rsell_row(const RDevCsr<T>& M, int row, const T* __restrict__ x) {
+    T s = T(0);
+    const int sl = row >> 5;
+    const int e = __ldg(M.sptr + sl + 1);
+    for (int p = __ldg(M.sptr + sl) + (row & 31); p < e; p += 4 * 32) {
+        int c[4];
+        T v[4], xv[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int pu = p + u * 32;
+            c[u] = pu < e ? __ldg(M.scol + pu) : -1;
+            v[u] = pu < e ? __ldg(M.sval + pu) : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) xv[u] = c[u] >= 0 ? __ldcg(x + c[u]) : T(0);
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            if (c[u] >= 0) s += v[u] * xv[u];
+    }
+    return s;
+}
+
+template <typename T>
+__device__ __forceinline__ T rrow1(const RDevCsr<T>& M, int row, const T* __restrict__ x) {
+    return M.sptr ? rsell_row(M, row, x) : rcsr_row(M, row, 0, 1, x);
+}
+
 // out[row] = scale * (M x + M2 x2); mask (may be null) zeroes rows where mask != 0.  Rows are
 // spread over groups of M.group lanes (1..32) with a warp-uniform loop and fixed-order reduction.
 template <typename T>
@@ -487,8 +521,8 @@ __device__ void rcsr_phase(const RDevCsr<T>& M, const T* x, const RDevCsr<T>* M2
     };
     if (g == 1) {
         for (int row = t0; row < M.n; row += stride) {
-            T s = rcsr_row(M, row, 0, 1, x);
-            if (M2) s += rcsr_row(*M2, row, 0, 1, x2);
+            T s = rrow1(M, row, x);
+            if (M2) s += rrow1(*M2, row, x2);
             const T o = (mask && mask[row]) ? T(0) : (phi ? scale * s + extra(row) : scale * s);
             out[row] = o;
             if (xdot) *xdot += __ldcg(x + row) * o;

@@ -24,6 +24,7 @@
 #include "mtk_amg.cuh"
 #include "mtk_amg_gpu.cuh"
 #include "mtk_ctx.cuh"
+#include "mtk_sell.cuh"
 
 namespace mtk {
 
@@ -231,6 +232,41 @@ __device__ __forceinline__ void csr_row_acc(const DevCsr<T>& M, int row, int lan
     }
 }
 
+// The same row sum from the SELL-32 copy: the row's lane walks its entries in CSR order, 32
+// apart in the slice (each load coalesced across the slice's 32 lanes).
+template <typename T>
+__device__ __forceinline__ void sell_row_acc(const DevCsr<T>& M, int row, const typename V2of<T>::type* __restrict__ x,
+                                             T& re, T& im) {
+    using V2 = typename V2of<T>::type;
+    const int sl = row >> 5;
+    const int e = __ldg(M.sptr + sl + 1);
+    for (int p = __ldg(M.sptr + sl) + (row & 31); p < e; p += 4 * 32) {
+        int c[4];
+        V2 v[4], xv[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int pu = p + u * 32;
+            c[u] = pu < e ? __ldg(M.scol + pu) : -1;
+            v[u] = pu < e ? __ldg(M.sval + pu) : V2{};
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) xv[u] = c[u] >= 0 ? __ldcg(x + c[u]) : V2{};
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            if (c[u] >= 0) {
+                re += v[u].x * xv[u].x - v[u].y * xv[u].y;
+                im += v[u].x * xv[u].y + v[u].y * xv[u].x;
+            }
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void row1_acc(const DevCsr<T>& M, int row, const typename V2of<T>::type* __restrict__ x, T& re,
+                                         T& im) {
+    if (M.sptr) sell_row_acc(M, row, x, re, im);
+    else csr_row_acc(M, row, 0, 1, x, re, im);
+}
+
 // One CSR phase over all rows: out[row] = M x (+ M2 x2), each row on a group of M.group lanes
 // (1, 2, ..., 32; lanes stride the row, then a fixed-order butterfly reduction) across the grid.
 template <typename T>
@@ -243,8 +279,8 @@ __device__ void csr_phase(const DevCsr<T>& M, const typename V2of<T>::type* x, c
     if (g == 1) {
         for (int row = t0; row < M.n; row += stride) {
             T re = T(0), im = T(0);
-            csr_row_acc(M, row, 0, 1, x, re, im);
-            if (M2) csr_row_acc(*M2, row, 0, 1, x2, re, im);
+            row1_acc(M, row, x, re, im);
+            if (M2) row1_acc(*M2, row, x2, re, im);
             V2 o;
             o.x = re;
             o.y = im;
@@ -919,6 +955,10 @@ struct FieldSolver {
         DBuf<double2> v64;
         DBuf<float2> v32;
         int n = 0, group = 1;
+        size_t nnz = 0;
+        SellIdx sell;              // SELL-32 copy (mtk_sell.cuh) where sell_worth holds
+        DBuf<double2> s64;
+        DBuf<float2> s32;
     };
     struct LevelBufs {
         CsrBufs R, S, P;
@@ -945,6 +985,7 @@ struct FieldSolver {
         cudaStream_t st = c->stream;
         B.n = M.n;
         B.group = group;
+        B.nnz = M.col.size();
         MTK_TRY(B.ptr.upload(M.ptr.data(), M.ptr.size(), st));
         MTK_TRY(B.col.upload(M.col.data(), M.col.size(), st));
         std::vector<double2> v64(M.val.size());
@@ -1047,10 +1088,16 @@ struct FieldSolver {
         };
         auto avg = [](const HostCsr& M) { return M.n > 0 ? (double)M.col.size() / M.n : 0.0; };
         auto davg = [](const DevCsrC& M) { return M.n > 0 ? (double)M.nnz / M.n : 0.0; };
+        // a matrix for which the cost model picks several lanes per row, with enough rows to fill
+        // the grid with one lane per row and short rows, gets a SELL-32 copy and one lane per row
+        const bool use_sell = !getenv("MTK_NO_SELL");
+        auto worth = [&](int rows, double a) { return use_sell && sell_worth(rows, a * rows, grp(rows, a)); };
+        auto sgrp = [&](int rows, double a) { return worth(rows, a) ? 1 : grp(rows, a); };
         // adopt a device CSR (FP64 values) and its FP32 copy
         auto adopt = [&](DevCsrC& D, CsrBufs& B, int group) -> int {
             B.n = D.n;
             B.group = group;
+            B.nnz = D.nnz;
             B.ptr = std::move(D.ptr);
             B.col = std::move(D.col);
             B.v64 = std::move(D.val);
@@ -1068,8 +1115,8 @@ struct FieldSolver {
                 DevCycleOpsC& O = dops[i + 1];
                 lv_nnz[3 * i] = (double)O.R.nnz; lv_nnz[3 * i + 1] = (double)O.S.nnz; lv_nnz[3 * i + 2] = (double)O.P.nnz;
                 lv_n[2 * i] = O.S.n; lv_n[2 * i + 1] = O.R.n;
-                const int up = grp(O.S.n, std::max(davg(O.S), davg(O.P)));
-                MTK_TRY(adopt(O.R, B.R, grp(O.R.n, davg(O.R))));
+                const int up = sgrp(O.S.n, std::max(davg(O.S), davg(O.P)));
+                MTK_TRY(adopt(O.R, B.R, sgrp(O.R.n, davg(O.R))));
                 MTK_TRY(adopt(O.S, B.S, up));
                 MTK_TRY(adopt(O.P, B.P, up));
                 ln = B.S.n;
@@ -1077,16 +1124,31 @@ struct FieldSolver {
                 const HostCycleOps& O = HH.ops[i + 1];
                 lv_nnz[3 * i] = (double)O.R.col.size(); lv_nnz[3 * i + 1] = (double)O.S.col.size(); lv_nnz[3 * i + 2] = (double)O.P.col.size();
                 lv_n[2 * i] = O.S.n; lv_n[2 * i + 1] = O.R.n;
-                MTK_TRY(upload_csr(O.R, B.R, grp(O.R.n, avg(O.R))));
-                const int up = grp(O.S.n, std::max(avg(O.S), avg(O.P)));
+                MTK_TRY(upload_csr(O.R, B.R, sgrp(O.R.n, avg(O.R))));
+                const int up = sgrp(O.S.n, std::max(avg(O.S), avg(O.P)));
                 MTK_TRY(upload_csr(O.S, B.S, up));
                 MTK_TRY(upload_csr(O.P, B.P, up));
                 ln = O.S.n;
             }
             MTK_TRY(B.r64.alloc(ln)); MTK_TRY(B.r32.alloc(ln));
             MTK_TRY(B.y64.alloc(ln)); MTK_TRY(B.y32.alloc(ln));
-            auto mk64 = [](const CsrBufs& C) { return DevCsr<double>{C.n, C.group, C.ptr.p, C.col.p, C.v64.p}; };
-            auto mk32 = [](const CsrBufs& C) { return DevCsr<float>{C.n, C.group, C.ptr.p, C.col.p, C.v32.p}; };
+            if (use_sell)
+                for (CsrBufs* C : {&B.R, &B.S, &B.P})
+                    if (C->group == 1 && C->n > 0 && worth(C->n, (double)C->nnz / C->n)) {
+                        MTK_TRY(sell_build_index(c, st, C->n, C->ptr.p, C->col.p, C->sell));
+                        MTK_TRY(sell_fill_values<double2>(c, st, C->n, C->ptr.p, C->col.p, C->v64.p, C->sell, C->s64));
+                        MTK_TRY(sell_fill_values<float2>(c, st, C->n, C->ptr.p, C->col.p, C->v32.p, C->sell, C->s32));
+                    }
+            auto mk64 = [](const CsrBufs& C) {
+                DevCsr<double> M{C.n, C.group, C.ptr.p, C.col.p, C.v64.p};
+                if (C.sell.sptr.p) { M.sptr = C.sell.sptr.p; M.scol = C.sell.scol.p; M.sval = C.s64.p; }
+                return M;
+            };
+            auto mk32 = [](const CsrBufs& C) {
+                DevCsr<float> M{C.n, C.group, C.ptr.p, C.col.p, C.v32.p};
+                if (C.sell.sptr.p) { M.sptr = C.sell.sptr.p; M.scol = C.sell.scol.p; M.sval = C.s32.p; }
+                return M;
+            };
             H64.L[i] = DevLevel<double>{mk64(B.R), mk64(B.S), mk64(B.P), B.r64.p, B.y64.p};
             H32.L[i] = DevLevel<float>{mk32(B.R), mk32(B.S), mk32(B.P), B.r32.p, B.y32.p};
         }

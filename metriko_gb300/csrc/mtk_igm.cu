@@ -32,6 +32,7 @@
 #include "mtk_amg_real.cuh"
 #include "mtk_amg_real_gpu.cuh"
 #include "mtk_ctx.cuh"
+#include "mtk_sell.cuh"
 
 namespace mtk {
 
@@ -68,7 +69,42 @@ struct IgmOp {
     const int* cj_col;
     const T* cj_val;
     const T* BJJ;       // 2 W_J^T S W_J, nJ x nJ (row-major)
+    // translation rows (the long lists of W_J^T / C_Jy: every cut copy along a seam segment
+    // references its translation) cut into chunks of at most kJChunk entries, one warp each,
+    // spread over the grid; chunk c of row jc_row[c] starts at entry jc_beg[c] of that row's list
+    // and writes its partial sum to XoJp[c]; row s owns the chunks [jc_first[s], jc_first[s + 1]),
+    // which the reader adds in order.  jc_n = 0: one warp per row.
+    int jc_n = 0;
+    const int* jc_row = nullptr;
+    const int* jc_beg = nullptr;
+    const int* jc_first = nullptr;
+    T* XoJp = nullptr;
 };
+constexpr int kJChunk = 256;
+
+// chunks of the translation rows given their CSR row pointer (host)
+inline void translation_chunks(const std::vector<int>& ptr, std::vector<int>& row, std::vector<int>& beg,
+                               std::vector<int>& first) {
+    const int nJ = (int)ptr.size() - 1;
+    row.clear(); beg.clear(); first.assign(nJ + 1, 0);
+    for (int s = 0; s < nJ; s++) {
+        first[s] = (int)row.size();
+        int e = ptr[s];
+        do {
+            row.push_back(s);
+            beg.push_back(e);
+            e += kJChunk;
+        } while (e < ptr[s + 1]);
+    }
+    first[nJ] = (int)row.size();
+}
+// the end of chunk c: kJChunk entries on, or its row's end
+__device__ __forceinline__ int jchunk_end(const int* __restrict__ ptr, const int* __restrict__ jc_row,
+                                          const int* __restrict__ jc_beg, int c) {
+    const int e = jc_beg[c] + kJChunk;
+    const int re = ptr[jc_row[c] + 1];
+    return e < re ? e : re;
+}
 
 // Shared-memory layout of the replicated z state (cz, wsum: the Schur coarse space).
 template <typename T>
@@ -204,12 +240,23 @@ __device__ bool igm_apply(const IgmOp<T>& A, const ZProj<T>& P, const unsigned c
         const int lane = threadIdx.x & 31;
         const int nwarps = stride >> 5;
         const int gw = nwarps - 1 - (t0 >> 5);   // last warps of the grid
-        for (int s = gw; s < A.nJ; s += nwarps) {
-            T acc = T(0);
-            for (int e = A.jt_ptr[s] + lane; e < A.jt_ptr[s + 1]; e += 32) acc += A.jt_val[e] * __ldcg(A.Qc + A.jt_row[e]);
+        if (A.jc_n > 0) {
+            for (int ch = gw; ch < A.jc_n; ch += nwarps) {
+                T acc = T(0);
+                const int e1 = jchunk_end(A.jt_ptr, A.jc_row, A.jc_beg, ch);
+                for (int e = A.jc_beg[ch] + lane; e < e1; e += 32) acc += A.jt_val[e] * __ldcg(A.Qc + A.jt_row[e]);
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) A.XoJ[s] = T(2) * acc;
+                for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                if (lane == 0) A.XoJp[ch] = T(2) * acc;
+            }
+        } else {
+            for (int s = gw; s < A.nJ; s += nwarps) {
+                T acc = T(0);
+                for (int e = A.jt_ptr[s] + lane; e < A.jt_ptr[s + 1]; e += 32) acc += A.jt_val[e] * __ldcg(A.Qc + A.jt_row[e]);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                if (lane == 0) A.XoJ[s] = T(2) * acc;
+            }
         }
     }
     pq_part = part;
@@ -270,17 +317,35 @@ __device__ bool igm_apply_asm(const IgmOp<T>& A, const unsigned char* __restrict
         const int lane = threadIdx.x & 31;
         const int nwarps = stride >> 5;
         const int gw = nwarps - 1 - (t0 >> 5);   // last warps of the grid
-        for (int s = gw; s < A.nJ; s += nwarps) {
-            T acc = T(0);
-            for (int e = A.cj_ptr[s] + lane; e < A.cj_ptr[s + 1]; e += 32) {
-                const int y = A.cj_col[e];
-                const T pv = pnew ? fmaT<T>(beta, __ldcg(py + y), __ldcg(zy + y)) : __ldcg(py + y);
-                acc += A.cj_val[e] * pv;
-            }
-            for (int t = lane; t < A.nJ; t += 32) acc += A.BJJ[(size_t)s * A.nJ + t] * zs.XJ[t];
+        if (A.jc_n > 0) {
+            for (int ch = gw; ch < A.jc_n; ch += nwarps) {
+                const int s = A.jc_row[ch];
+                T acc = T(0);
+                const int e1 = jchunk_end(A.cj_ptr, A.jc_row, A.jc_beg, ch);
+                for (int e = A.jc_beg[ch] + lane; e < e1; e += 32) {
+                    const int y = A.cj_col[e];
+                    const T pv = pnew ? fmaT<T>(beta, __ldcg(py + y), __ldcg(zy + y)) : __ldcg(py + y);
+                    acc += A.cj_val[e] * pv;
+                }
+                if (ch == A.jc_first[s])   // the row's first chunk also takes the dense J block
+                    for (int t = lane; t < A.nJ; t += 32) acc += A.BJJ[(size_t)s * A.nJ + t] * zs.XJ[t];
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) A.XoJ[s] = acc;
+                for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                if (lane == 0) A.XoJp[ch] = acc;
+            }
+        } else {
+            for (int s = gw; s < A.nJ; s += nwarps) {
+                T acc = T(0);
+                for (int e = A.cj_ptr[s] + lane; e < A.cj_ptr[s + 1]; e += 32) {
+                    const int y = A.cj_col[e];
+                    const T pv = pnew ? fmaT<T>(beta, __ldcg(py + y), __ldcg(zy + y)) : __ldcg(py + y);
+                    acc += A.cj_val[e] * pv;
+                }
+                for (int t = lane; t < A.nJ; t += 32) acc += A.BJJ[(size_t)s * A.nJ + t] * zs.XJ[t];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                if (lane == 0) A.XoJ[s] = acc;
+            }
         }
     }
     pq_part = part;
@@ -295,19 +360,33 @@ __device__ bool igm_apply_asm(const IgmOp<T>& A, const unsigned char* __restrict
 // an exact Phi this is the block factorisation K^-1 = [K_yy^-1 0; 0 0] + Z S^-1 Z^T (S the Schur
 // complement of the z block), so the coupled system converges like the free block alone.
 //
-// Block partials of Phi^T r_y in fixed order: out[k * gridDim.x + blockIdx.x].
+// Block partials of Phi^T r_y in fixed order: out[k * gridDim.x + blockIdx.x].  The columns are
+// taken kPhiChunk at a time in one pass over r (each thread keeps one sum per column of the
+// chunk, over the same rows in the same order as a pass per column would).
+constexpr int kPhiChunk = 8;
 template <typename T>
 __device__ void phi_dots_publish(const __half* __restrict__ Phi, int nY, int nZ, const T* r, T* out, T* wsum) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int stride = gridDim.x * blockDim.x;
     const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
-    for (int k = 0; k < nZ; k++) {
-        T a = T(0);
-        const __half* col = Phi + (size_t)k * nY;
-        for (int j = t0; j < nY; j += stride) a += (T)__half2float(__ldg(col + j)) * __ldcg(r + j);
+    for (int k0 = 0; k0 < nZ; k0 += kPhiChunk) {
+        const int kc = nZ - k0 < kPhiChunk ? nZ - k0 : kPhiChunk;
+        T a[kPhiChunk];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-        if (lane == 0) wsum[warp * nZ + k] = a;
+        for (int u = 0; u < kPhiChunk; u++) a[u] = T(0);
+        for (int j = t0; j < nY; j += stride) {
+            const T rj = __ldcg(r + j);
+#pragma unroll
+            for (int u = 0; u < kPhiChunk; u++)
+                if (u < kc) a[u] += (T)__half2float(__ldg(Phi + (size_t)(k0 + u) * nY + j)) * rj;
+        }
+#pragma unroll
+        for (int u = 0; u < kPhiChunk; u++) {
+            T v = a[u];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0 && u < kc) wsum[warp * nZ + k0 + u] = v;
+        }
     }
     __syncthreads();
     for (int k = threadIdx.x; k < nZ; k += blockDim.x) {
@@ -338,7 +417,15 @@ __device__ void phi_coarse(const ZProj<T>& P, int nZ, const T* parts, ZSmem<T>& 
 // E (replicated, after a barrier): qz = P_z (scale USmall^T XoJ + shift pz)
 template <typename T>
 __device__ void igm_apply_z(const IgmOp<T>& A, const ZProj<T>& P, const T* pz, T* qz, ZSmem<T>& zs) {
-    for (int s = threadIdx.x; s < A.nJ; s += blockDim.x) zs.tmpJ[s] = __ldcg(A.XoJ + s);
+    for (int s = threadIdx.x; s < A.nJ; s += blockDim.x) {
+        if (A.jc_n > 0) {   // the row's chunk partials in chunk order
+            T v = T(0);
+            for (int ch = A.jc_first[s]; ch < A.jc_first[s + 1]; ch++) v += __ldcg(A.XoJp + ch);
+            zs.tmpJ[s] = v;
+        } else {
+            zs.tmpJ[s] = __ldcg(A.XoJ + s);
+        }
+    }
     __syncthreads();
     for (int j = threadIdx.x; j < A.nZ; j += blockDim.x) {
         T acc = T(0);
@@ -976,6 +1063,11 @@ struct Igm {
     DBuf<__half> phih;         // Phi as the kernels read it
     std::vector<double> G0, C0;
     DBuf<float> ka_val32, cy_val32, cj_val32, bjj32;
+    // translation-row chunks of the matrix-free (jt) and the assembled (cj) operator
+    DBuf<int> jtc_row, jtc_beg, jtc_first, cjc_row, cjc_beg, cjc_first;
+    int jtc_n = 0, cjc_n = 0;
+    DBuf<double> XoJp;
+    DBuf<float> XoJp32;
     DBuf<double> pb64;   // second direction buffers of the PCG (double-buffered p)
     // attainable reduction of the FP32 solves per refinement (first, second, later), measured as
     // sqrt(max(0, rr_fp64 - rr_fp32)) / |r_start|: the next solves stop at half of it
@@ -988,7 +1080,16 @@ struct Igm {
     long long pcg_launches = 0;
     long long nnzW = 0, nnzS = 0, nnzYT = 0;
     // multigrid on the free block (host-built)
-    struct RCsrBufs { DBuf<int> ptr, col; DBuf<double> v64; DBuf<float> v32; int n = 0, group = 1; };
+    struct RCsrBufs {
+        DBuf<int> ptr, col;
+        DBuf<double> v64;
+        DBuf<float> v32;
+        int n = 0, group = 1;
+        size_t nnz = 0;
+        SellIdx sell;                 // SELL-32 copy (mtk_sell.cuh) where sell_worth holds
+        DBuf<double> s64;
+        DBuf<float> s32;
+    };
     struct RLevelBufs { RCsrBufs R, S, P; DBuf<double> r64, y64; DBuf<float> r32, y32; } rlv[kRMaxLevels];
     DBuf<double> rAinv64, rrc64, ryc64;
     DBuf<float> rAinv32, rrc32, ryc32;
@@ -1004,6 +1105,7 @@ struct Igm {
     int upload_rcsr(const RCsr& M, RCsrBufs& B, int group) {
         B.n = M.n;
         B.group = group;
+        B.nnz = M.col.size();
         MTK_TRY(B.ptr.upload(M.ptr.data(), M.ptr.size(), st));
         MTK_TRY(B.col.upload(M.col.data(), M.col.size(), st));
         MTK_TRY(B.v64.upload(M.val.data(), M.val.size(), st));
@@ -1050,10 +1152,15 @@ struct Igm {
             }
             return best;
         };
+        // a matrix for which the cost model picks several lanes per row, with enough rows to fill
+        // the grid with one lane per row and short rows, gets a SELL-32 copy and one lane per row
+        const bool use_sell = !getenv("MTK_NO_SELL");
+        auto sell_rows = [&](int n, size_t nnz) { return use_sell && sell_worth(n, (double)nnz, grp(n, nnz)); };
         // adopt a device CSR (FP64 values) and its FP32 copy
         auto adopt = [&](DevCsr64& D, RCsrBufs& B, int group) -> int {
             B.n = D.n;
             B.group = group;
+            B.nnz = D.nnz;
             B.ptr = std::move(D.ptr);
             B.col = std::move(D.col);
             B.v64 = std::move(D.val);
@@ -1073,15 +1180,17 @@ struct Igm {
                 nS = O.S.n; nR = O.R.n; zR = O.R.nnz; zS = O.S.nnz; zP = O.P.nnz;
                 // level 0's up phase writes z with the thread-per-row mapping of the PCG vector
                 // loops, which read it with no grid barrier in between: keep it at one lane per row
-                const int up = l == 0 ? 1 : std::max(grp(nS, zS), grp(O.P.n, zP));
-                MTK_TRY(adopt(O.R, B.R, grp(nR, zR)));
+                const int up = l == 0 || (sell_rows(nS, zS) && sell_rows(O.P.n, zP)) ? 1
+                                                                                       : std::max(grp(nS, zS), grp(O.P.n, zP));
+                MTK_TRY(adopt(O.R, B.R, sell_rows(nR, zR) ? 1 : grp(nR, zR)));
                 MTK_TRY(adopt(O.S, B.S, up));
                 MTK_TRY(adopt(O.P, B.P, up));
             } else {
                 const RCycleOps& O = HH.ops[l];
                 nS = O.S.n; nR = O.R.n; zR = O.R.col.size(); zS = O.S.col.size(); zP = O.P.col.size();
-                const int up = l == 0 ? 1 : std::max(grp(nS, zS), grp(O.P.n, zP));
-                MTK_TRY(upload_rcsr(O.R, B.R, grp(nR, zR)));
+                const int up = l == 0 || (sell_rows(nS, zS) && sell_rows(O.P.n, zP)) ? 1
+                                                                                       : std::max(grp(nS, zS), grp(O.P.n, zP));
+                MTK_TRY(upload_rcsr(O.R, B.R, sell_rows(nR, zR) ? 1 : grp(nR, zR)));
                 MTK_TRY(upload_rcsr(O.S, B.S, up));
                 MTK_TRY(upload_rcsr(O.P, B.P, up));
             }
@@ -1091,8 +1200,23 @@ struct Igm {
                 MTK_TRY(B.r64.alloc(nS)); MTK_TRY(B.y64.alloc(nS));
                 MTK_TRY(B.r32.alloc(nS)); MTK_TRY(B.y32.alloc(nS));
             }
-            auto m64 = [](const RCsrBufs& C) { return RDevCsr<double>{C.n, C.group, C.ptr.p, C.col.p, C.v64.p}; };
-            auto m32 = [](const RCsrBufs& C) { return RDevCsr<float>{C.n, C.group, C.ptr.p, C.col.p, C.v32.p}; };
+            if (use_sell)
+                for (RCsrBufs* C : {&B.R, &B.S, &B.P})
+                    if (C->group == 1 && C->n > 0 && sell_rows(C->n, C->nnz)) {
+                        MTK_TRY(sell_build_index(c, st, C->n, C->ptr.p, C->col.p, C->sell));
+                        MTK_TRY(sell_fill_values<double>(c, st, C->n, C->ptr.p, C->col.p, C->v64.p, C->sell, C->s64));
+                        MTK_TRY(sell_fill_values<float>(c, st, C->n, C->ptr.p, C->col.p, C->v32.p, C->sell, C->s32));
+                    }
+            auto m64 = [](const RCsrBufs& C) {
+                RDevCsr<double> M{C.n, C.group, C.ptr.p, C.col.p, C.v64.p};
+                if (C.sell.sptr.p) { M.sptr = C.sell.sptr.p; M.scol = C.sell.scol.p; M.sval = C.s64.p; }
+                return M;
+            };
+            auto m32 = [](const RCsrBufs& C) {
+                RDevCsr<float> M{C.n, C.group, C.ptr.p, C.col.p, C.v32.p};
+                if (C.sell.sptr.p) { M.sptr = C.sell.sptr.p; M.scol = C.sell.scol.p; M.sval = C.s32.p; }
+                return M;
+            };
             RH64.L[l] = RDevLevel<double>{m64(B.R), m64(B.S), m64(B.P), B.r64.p, B.y64.p};
             RH32.L[l] = RDevLevel<float>{m32(B.R), m32(B.S), m32(B.P), B.r32.p, B.y32.p};
         }
@@ -1134,16 +1258,38 @@ struct Igm {
     }
 
     IgmOp<double> op64(double scale, double shift) {
-        return {nCut, nY, nZ, nJ, w_ptr.p, w_tag.p, w_val.p, s_ptr.p, s_col.p, s_val.p, yt_ptr.p, yt_row.p, yt_val.p,
-                jt_ptr.p, jt_row.p, jt_val.p, Us.p, scale, shift, U.p, Qc.p, XoJ.p,
-                nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+        IgmOp<double> A{nCut, nY, nZ, nJ, w_ptr.p, w_tag.p, w_val.p, s_ptr.p, s_col.p, s_val.p, yt_ptr.p, yt_row.p,
+                        yt_val.p, jt_ptr.p, jt_row.p, jt_val.p, Us.p, scale, shift, U.p, Qc.p, XoJ.p,
+                        nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+        if (jtc_n > 0) { A.jc_n = jtc_n; A.jc_row = jtc_row.p; A.jc_beg = jtc_beg.p; A.jc_first = jtc_first.p; A.XoJp = XoJp.p; }
+        return A;
     }
     IgmOp<float> op32(double scale, double shift) {
         const bool a = asm_ok;
-        return {nCut, nY, nZ, nJ, w_ptr.p, w_tag.p, w_val32.p, s_ptr.p, s_col.p, s_val32.p, yt_ptr.p, yt_row.p, yt_val32.p,
-                jt_ptr.p, jt_row.p, jt_val32.p, Us32.p, (float)scale, (float)shift, U32.p, Qc32.p, XoJ32.p,
-                a ? ka_ptr.p : nullptr, ka_col.p, ka_val32.p, cy_ptr.p, cy_col.p, cy_val32.p, cj_ptr.p, cj_col.p,
-                cj_val32.p, bjj32.p};
+        IgmOp<float> A{nCut, nY, nZ, nJ, w_ptr.p, w_tag.p, w_val32.p, s_ptr.p, s_col.p, s_val32.p, yt_ptr.p, yt_row.p,
+                       yt_val32.p, jt_ptr.p, jt_row.p, jt_val32.p, Us32.p, (float)scale, (float)shift, U32.p, Qc32.p,
+                       XoJ32.p, a ? ka_ptr.p : nullptr, ka_col.p, ka_val32.p, cy_ptr.p, cy_col.p, cy_val32.p, cj_ptr.p,
+                       cj_col.p, cj_val32.p, bjj32.p};
+        if (a && cjc_n > 0) {
+            A.jc_n = cjc_n; A.jc_row = cjc_row.p; A.jc_beg = cjc_beg.p; A.jc_first = cjc_first.p; A.XoJp = XoJp32.p;
+        } else if (!a && jtc_n > 0) {
+            A.jc_n = jtc_n; A.jc_row = jtc_row.p; A.jc_beg = jtc_beg.p; A.jc_first = jtc_first.p; A.XoJp = XoJp32.p;
+        }
+        return A;
+    }
+
+    // chunk lists of the translation rows of a CSR row pointer held on the host
+    int upload_chunks(const std::vector<int>& ptr, DBuf<int>& row, DBuf<int>& beg, DBuf<int>& first, int& n) {
+        std::vector<int> r, b, f;
+        translation_chunks(ptr, r, b, f);
+        n = (int)r.size();
+        if (n == 0) return MTK_OK;
+        MTK_TRY(row.upload(r.data(), r.size(), st));
+        MTK_TRY(beg.upload(b.data(), b.size(), st));
+        MTK_TRY(first.upload(f.data(), f.size(), st));
+        const size_t need = std::max<size_t>(n, std::max(jtc_n, cjc_n));
+        if (XoJp.n < need) { MTK_TRY(XoJp.alloc(need)); MTK_TRY(XoJp32.alloc(need)); }
+        return MTK_OK;
     }
 
     template <typename T>
@@ -1531,6 +1677,7 @@ int igm_run(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts_in, do
     MTK_TRY(S.yt_val.upload(yval.data(), yval.size(), st));
     MTK_TRY(S.yt_val32.upload(yv32.data(), yv32.size(), st));
     MTK_TRY(S.jt_ptr.upload(jptr.data(), jptr.size(), st));
+    if (!getenv("MTK_NO_JCHUNK")) MTK_TRY(S.upload_chunks(jptr, S.jtc_row, S.jtc_beg, S.jtc_first, S.jtc_n));
     MTK_TRY(S.jt_row.upload(jrow.data(), jrow.size(), st));
     MTK_TRY(S.jt_val.upload(jval.data(), jval.size(), st));
     MTK_TRY(S.jt_val32.upload(jv32.data(), jv32.size(), st));
@@ -1779,6 +1926,12 @@ int igm_run(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts_in, do
         std::vector<float> b32(BJJ.begin(), BJJ.end());
         if (b32.empty()) b32.push_back(0.f);
         MTK_TRY(S.bjj32.upload(b32.data(), b32.size(), st));
+        if (!getenv("MTK_NO_JCHUNK") && nJ > 0) {   // chunks of the translation rows of C_Jy
+            std::vector<int> cptr(nJ + 1);
+            MTK_CUDA_TRY(cudaMemcpyAsync(cptr.data(), S.cj_ptr.p, sizeof(int) * (nJ + 1), cudaMemcpyDeviceToHost, st));
+            MTK_CUDA_TRY(cudaStreamSynchronize(st));
+            MTK_TRY(S.upload_chunks(cptr, S.cjc_row, S.cjc_beg, S.cjc_first, S.cjc_n));
+        }
     }
     auto build_zblock = [&](double scale, double shift, std::vector<double>& Kzz) {
         Kzz.assign((size_t)nZ * nZ, 0.0);

@@ -932,11 +932,24 @@ def target_field(m: Hmesh, ext, N):
 # --------------------------------------------------------------------------------------------
 # a14-a21  iterative rounding
 # --------------------------------------------------------------------------------------------
+# The reference refactorises J^T J on every LM iteration even when it has not changed (the
+# linear SI problems).  With this flag set (golden-fixture generation only) a bit-identical
+# matrix reuses the previous factorisation, which gives bit-identical solves; the timed CPU
+# baseline keeps the reference's behaviour (flag off).
+REUSE_IDENTICAL_FACTORIZATION = False
+
+
 class _LLT:
     """CholeskyWrapper stand-in (iter_rounding.h:14-31): direct factorisation per call."""
 
     def factorize(self, A):
+        A = sp.csc_matrix(A)
+        if (REUSE_IDENTICAL_FACTORIZATION and getattr(self, "key", None) is not None
+                and self.key[0].shape == A.shape and np.array_equal(self.key[1], A.indptr)
+                and np.array_equal(self.key[2], A.indices) and np.array_equal(self.key[3], A.data)):
+            return True
         self.lu = spd_factor(A)
+        self.key = (A, A.indptr.copy(), A.indices.copy(), A.data.copy())
         return True
 
     def solve(self, rhs):
@@ -1469,3 +1482,149 @@ def curvature_aligned(m: Hmesh, N: int = 4):
     Mm = mass_matrix(m)
     rhs = (Mm @ D) / np.sqrt(abs(np.vdot(D, Mm @ D)))
     return spd_factor(L).solve(rhs), rhs
+
+
+# --------------------------------------------------------------------------------------------
+# Vertex-position gradient of the size-field loss (differentiation; no counterpart in the
+# reference).  The loss of size_field_gradient,
+#   l(V, s) = sum_f |length X2F_f x - exp(sbar_f) F2_f|^2 + mu sum_edges (s_i - s_j)^2,
+# with the integration target F2 itself (T = F2), is differentiated with respect to the vertex
+# positions with every integer decision frozen (matching, seams, cut, combing turns, anchors).
+# x minimises the first term under the constraints, so dl/dV is the partial derivative at fixed
+# x (envelope theorem).  V enters through
+#   * the per-face gradient operator G2 (the cut face's shape in its own frame) and the grid
+#     length (bounding-box diagonal * ratio / mean field norm, the norm being 1);
+#   * the target F2_f = (cos a_fk, sin a_fk), a_fk = arg(c_f) / N + 2 pi (k + turn_f) / N, with
+#     c the 50-step inverse power iteration of (L(V), M(V)) from the seeded start: L through
+#     theta_h = farg(h) - farg(twin h), M = diag(face area).
+# The power iteration is differentiated step by step in reverse (one solve with L per step;
+# the iterates are kept).  Per-face geometric derivatives (area, farg, G2 entries) are taken by
+# complex-step differentiation of the same per-face formulas (exact to round-off).
+# --------------------------------------------------------------------------------------------
+def _face_geom(P0, P1, P2):
+    """Per face: area, farg of the second and third halfedges (hmesh.h:480-489; the first is 0)
+    and the G2 entries (gx, gy) of the three corners (parameterization_integ.ipp:11-24).
+    Written with operations that continue analytically (complex-step differentiation)."""
+    x = P1 - P0
+    t = P2 - P0
+    n = np.cross(x, t)
+    nn = _norm3(n)
+    A = nn * 0.5
+    bX = x / _norm3(x)[..., None]
+    nh = n / nn[..., None]
+    bY = -np.cross(x, n)
+    bY = bY / _norm3(bY)[..., None]
+    e1 = (P2 - P1) / _norm3(P2 - P1)[..., None]
+    e2 = (P0 - P2) / _norm3(P0 - P2)[..., None]
+    f1 = np.arccos(_dot3(e1, bX))
+    f2 = f1 + np.arccos(_dot3(e2, e1))
+    P = [P0, P1, P2]
+    gx, gy = [], []
+    for j in range(3):
+        nxt = P[(j + 2) % 3] - P[(j + 1) % 3]
+        g = np.cross(nh, nxt) / (A * 2)[..., None]
+        gx.append(_dot3(g, bX))
+        gy.append(_dot3(g, bY))
+    return A, f1, f2, np.stack(gx, -1), np.stack(gy, -1)
+
+
+def _face_geom_jacobian(V, F):
+    """Complex-step derivatives of _face_geom with respect to the face's nine coordinates:
+    returns (values, d) with d[name] of shape (nF, 9[, 3]) (corner-major, x y z)."""
+    P = [V[F[:, j]].astype(np.complex128) for j in range(3)]
+    base = _face_geom(*[p.real for p in P])
+    h = 1e-30
+    nF = len(F)
+    dA, df1, df2 = np.empty((nF, 9)), np.empty((nF, 9)), np.empty((nF, 9))
+    dgx, dgy = np.empty((nF, 9, 3)), np.empty((nF, 9, 3))
+    for c in range(3):
+        for k in range(3):
+            Q = [p.copy() for p in P]
+            Q[c][:, k] += 1j * h
+            A, f1, f2, gx, gy = _face_geom(*Q)
+            q = 3 * c + k
+            dA[:, q], df1[:, q], df2[:, q] = A.imag / h, f1.imag / h, f2.imag / h
+            dgx[:, q], dgy[:, q] = gx.imag / h, gy.imag / h
+    return base, dict(A=dA, f1=df1, f2=df2, gx=dgx, gy=dgy)
+
+
+def _power_iterates(L, M, x0, n_iter):
+    """smallest_eig keeping every iterate u_k and scale s_k (u_k = x_k / s_k)."""
+    lu = spd_factor(L)
+    us, ss = [x0.copy()], [1.0]
+    u = x0.copy()
+    for _ in range(n_iter):
+        x = lu.solve(M @ u)
+        s_ = math.sqrt(abs(np.vdot(x, M @ x)))
+        u = x / s_
+        us.append(u)
+        ss.append(s_)
+    return lu, us, ss
+
+
+def position_gradient(V, F, s, mu=0.0, ratio=0.02, seed=0, round_seams=False, n_iter=50, N=4):
+    """Loss and gradient with respect to s and V of the size-field loss with the integration
+    target (T = F2), integer decisions frozen at V.  Returns (loss, grad_s, grad_V (nV x 3),
+    fullx, aux) with aux holding the frozen decisions."""
+    V = np.asarray(V, np.float64)
+    F = np.asarray(F)
+    out = pipeline(V, F, ratio=ratio, seamless=False, round_seams=round_seams, n_iter=n_iter, seed=seed)
+    loss, grad_s, fullx = size_field_gradient(out, F, s, None, mu)
+    m = out["mesh"]
+    nF, nV = m.nF, m.nV
+    cutF = out["cutF"]
+    NF = (out["fullx2N"] @ fullx).reshape(-1, N)          # function values at the cut vertices
+    length = out["length"]
+    es = np.exp(s[F].mean(axis=1))
+    F2 = out["F2"].reshape(nF, N, 2)
+    (A, f1, f2, gx, gy), J = _face_geom_jacobian(V, F)
+    # residuals r_fk = length sum_a g_a NF[c_a, k] - e_f F2_fk
+    grad_u = np.stack([np.einsum("fa,fak->fk", gx, NF[cutF]), np.einsum("fa,fak->fk", gy, NF[cutF])], -1)
+    r = length * grad_u - es[:, None, None] * F2
+    # d/d g_a, d/d length, d/d F2
+    dgx = 2.0 * length * np.einsum("fk,fak->fa", r[..., 0], NF[cutF])
+    dgy = 2.0 * length * np.einsum("fk,fak->fa", r[..., 1], NF[cutF])
+    dlength = 2.0 * float(np.sum(r * grad_u))
+    dF2 = -2.0 * es[:, None, None] * r
+    # F2_fk = (cos a_fk, sin a_fk) -> d/d phi_f (a_fk = phi_f + const, phi_f = arg(c_f) / N)
+    dphi = np.sum(dF2[..., 0] * -F2[..., 1] + dF2[..., 1] * F2[..., 0], axis=1)
+    # reverse power iteration
+    L, Mm = out["L"], out["M"]
+    area = m.faceArea
+    lu, us, ss = _power_iterates(L, Mm, seeded_init(nF, seed), n_iter)
+    c = us[-1]
+    gu = 1j * dphi * c / (N * np.abs(c) ** 2)
+    g_area = np.zeros(nF)
+    g_theta = np.zeros((nF, 3))
+    nb = m.face[m.twin[m.FH]]                               # neighbour across FH[f, j]
+    Lfg = np.stack([np.asarray(L[np.arange(nF), nb[:, j]]).ravel() for j in range(3)], 1)
+    for k in range(n_iter, 0, -1):
+        u, s_, up = us[k], ss[k], us[k - 1]
+        x = u * s_
+        a = float(np.real(np.vdot(gu, x)))
+        gx_ = gu / s_ - a * (area * x) / s_ ** 3
+        g_area += -a / s_ ** 3 * 0.5 * np.abs(x) ** 2
+        mu_ = lu.solve(gx_)
+        g_area += np.real(np.conj(mu_) * up)
+        g_theta += -np.real(np.conj(mu_)[:, None] * 1j * N * Lfg * x[nb])
+        gu = area * mu_
+    # theta_fj = farg(FH[f, j]) - farg(twin FH[f, j]) -> d/d farg of every halfedge
+    g_farg = np.zeros(m.nH)
+    np.add.at(g_farg, m.FH.ravel(), g_theta.ravel())
+    np.add.at(g_farg, m.twin[m.FH].ravel(), -g_theta.ravel())
+    # halfedges FH[f, 1], FH[f, 2] carry farg f1, f2 (FH[f, 0] has farg 0)
+    d1, d2 = g_farg[m.FH[:, 1]], g_farg[m.FH[:, 2]]
+    gface = (g_area[:, None] * J["A"] + d1[:, None] * J["f1"] + d2[:, None] * J["f2"]
+             + np.einsum("fa,fqa->fq", dgx, J["gx"]) + np.einsum("fa,fqa->fq", dgy, J["gy"]))
+    grad_V = np.zeros((nV, 3))
+    for cidx in range(3):
+        np.add.at(grad_V, F[:, cidx], gface[:, 3 * cidx:3 * cidx + 3])
+    # length = ratio |D| / norm, D the bounding-box diagonal: d length / d D = ratio D / (|D| norm)
+    D = V.max(0) - V.min(0)
+    norm = ratio * float(np.linalg.norm(D)) / length
+    dl_dD = dlength * ratio * D / (float(np.linalg.norm(D)) * norm)
+    for k in range(3):
+        grad_V[int(np.argmax(V[:, k])), k] += dl_dD[k]
+        grad_V[int(np.argmin(V[:, k])), k] -= dl_dD[k]
+    aux = dict(singular=out["singular"], seam=out["seam"], combed_matching=out["combed_matching"], length=length)
+    return loss, grad_s, grad_V, fullx, aux
