@@ -157,6 +157,12 @@ namespace metriko {
         // in the reference.  s: log-size per raw vertex; T: per-face loss target (8 per face) or
         // nullptr for the integration target.  Fills fullx with x(s).
         double size_field_gradient(const VecXd& s, const VecXd* T, double mu, VecXd& grad_s);
+        // The same loss with the integration target, plus its partial derivatives at fixed x
+        // (mtk_size_field_position_partials): per face the G2 entries (dgx, dgy: 3 per face), the
+        // field angle (dphi), and the grid length (*dlength, *length_out = the grid length).
+        double size_field_position_partials(const VecXd& s, double mu, VecXd& grad_s, std::vector<double>& dgx,
+                                            std::vector<double>& dgy, std::vector<double>& dphi, double* dlength,
+                                            double* length_out);
         bool integ();
 
     private:
@@ -520,6 +526,27 @@ namespace metriko {
                                            s.data(), T ? T->data() : nullptr, mu, &loss, grad_s.data(), fullx.data(),
                                            &gpu::stats()),
                    "mtk_size_field_gradient");
+        return loss;
+    }
+
+    inline double RosyParameterization::size_field_position_partials(const VecXd& s, double mu, VecXd& grad_s,
+                                                                     std::vector<double>& dgx, std::vector<double>& dgy,
+                                                                     std::vector<double>& dphi, double* dlength,
+                                                                     double* length_out) {
+        IntegSystem sys;
+        build_system(sys);
+        if (s.size() != raw.nV) throw std::invalid_argument("size field: bad sizes");
+        grad_s = VecXd(raw.nV);
+        fullx = VecXd(sys.desc.nFull);
+        dgx.assign(3 * size_t(raw.nF), 0.0);
+        dgy.assign(3 * size_t(raw.nF), 0.0);
+        dphi.assign(raw.nF, 0.0);
+        double loss = 0;
+        gpu::check(mtk_size_field_position_partials(gpu::context(), &sys.desc, &gpu::options().solve, raw.nV,
+                                                    raw.idx.data(), s.data(), mu, &loss, grad_s.data(), fullx.data(),
+                                                    dgx.data(), dgy.data(), dphi.data(), dlength, &gpu::stats()),
+                   "mtk_size_field_position_partials");
+        if (length_out) *length_out = sys.length;
         return loss;
     }
 

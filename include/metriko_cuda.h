@@ -288,6 +288,60 @@ int mtk_pipeline_size_field_gradient(mtk_ctx* ctx, int32_t nV, int32_t nF, const
                                      mtk_stats* stats);
 
 /*
+ * Gradient of the size-field loss of mtk_size_field_gradient with respect to the VERTEX
+ * POSITIONS as well (differentiation; no counterpart in the reference).  The loss uses the
+ * integration target (T = F2, the combed field in each face frame); every integer decision
+ * (matching, seams, cut, combing, anchors) is held at its value for V.  Because x minimises the
+ * loss's first term under the constraints, dl/dV is the partial derivative at fixed x; V enters
+ * through the per-face gradient operator G2, the grid length (bounding-box diagonal), and the
+ * field angle phi_f = arg(c_f) / 4 of the target, where c is the 50-step inverse power iteration
+ * of (L(V), M(V)).  That dependence is carried by mtk_field_power_adjoint (one Hermitian solve
+ * per power step, in reverse) and mtk_face_geometry_backward (per-face derivatives of the area,
+ * the halfedge angles and G2).  Whole path with host buffers, as mtk_pipeline_size_field_gradient:
+ *   s[nV], mu >= 0; loss, grad_s[nV], grad_V[3 nV]; fullx (capacity fullx_cap, *n_full).
+ */
+int mtk_pipeline_position_gradient(mtk_ctx* ctx, int32_t nV, int32_t nF, const double* V, const int32_t* F,
+                                   const mtk_pipeline_opts* popts, const mtk_solve_opts* sopts, const double* s,
+                                   double mu, double* loss, double* grad_s, double* grad_V, double* fullx,
+                                   int32_t fullx_cap, int32_t* n_full, mtk_stats* stats);
+
+/*
+ * mtk_size_field_gradient with the integration target, also returning the loss's partial
+ * derivatives at fixed x (no counterpart in the reference): per face the derivative with
+ * respect to the G2 entries of its corners (dgx[3 nF], dgy[3 nF], corner a of face f at 3 f + a,
+ * the entries (g . bX, g . bY) of the corner's gradient), to the field angle phi_f (dphi[nF]),
+ * and to the grid length (*dlength).
+ */
+int mtk_size_field_position_partials(mtk_ctx* ctx, const mtk_igm_desc* desc, const mtk_solve_opts* opts, int32_t nV,
+                                     const int32_t* F, const double* s, double mu, double* loss, double* grad_s,
+                                     double* fullx, double* dgx, double* dgy, double* dphi, double* dlength,
+                                     mtk_stats* stats);
+
+/*
+ * Reverse pass of the smoothest field's inverse power iteration (no counterpart in the
+ * reference).  Runs mtk_field_smoothest (same inputs; out[2 nF] = the field c) keeping the n_iter
+ * iterates, then, for the loss derivative dphi[nF] with respect to the field angle
+ * phi_f = arg(c_f) / nRosy, one solve with L per step in reverse order, giving the derivatives
+ * with respect to theta (g_theta[3 nF], the transport angle of halfedge j of face f) and to the
+ * face areas (g_area[nF]).  The solves use the same multigrid, precision and tolerance.
+ */
+int mtk_field_power_adjoint(mtk_ctx* ctx, int32_t nF, int32_t nRosy, const int32_t* nbr, const double* theta,
+                            const double* area, const double* x0, int32_t n_iter, const mtk_solve_opts* opts,
+                            const double* dphi, double* out, double* g_theta, double* g_area, mtk_stats* stats);
+
+/*
+ * Assembly backward of the per-face geometry (no counterpart in the reference): from the loss's
+ * derivatives with respect to each face's area (g_area[nF]), the halfedge angles heArgOnFace of
+ * its second and third halfedges (g_farg1, g_farg2 [nF]; the first is 0 by construction) and its
+ * G2 entries (g_gx, g_gy [3 nF]), the gradient with respect to the vertex positions
+ * grad_V[3 nV] (hmesh.h:461-489, parameterization_integ.ipp:11-24; forward-mode dual numbers per
+ * face on the device, vertices summing their faces in ascending order).
+ */
+int mtk_face_geometry_backward(mtk_ctx* ctx, int32_t nV, int32_t nF, const double* V, const int32_t* F,
+                               const double* g_area, const double* g_farg1, const double* g_farg2, const double* g_gx,
+                               const double* g_gy, double* grad_V);
+
+/*
  * Barrier of the local-injectivity option: InjectiveBarrier(N, nF, intrinsic_field) followed by
  * update(field, update_j, fBarrier, gBarrier) of core/igm/iterative_rounding/injective_barrier.h:
  * 18-106.  Layout of intrinsic_field and field: 2*N values per face (vector j of face i at

@@ -23,7 +23,8 @@ EXPORTS = [
     "mtk_seeded_init", "mtk_topology_from_field", "mtk_field_smoothest_noalloc", "mtk_size_field_gradient",
     "mtk_pipeline_size_field_gradient", "mtk_field_solve", "mtk_field_inputs", "mtk_field_spmv_bench",
     "mtk_injective_barrier", "mtk_local_injectivity", "mtk_map_deviation",
-    "mtk_mesh_geometry", "mtk_ctx_set_wait_limit",
+    "mtk_mesh_geometry", "mtk_ctx_set_wait_limit", "mtk_pipeline_position_gradient", "mtk_size_field_position_partials",
+    "mtk_field_power_adjoint", "mtk_face_geometry_backward",
 ]
 
 
@@ -109,6 +110,14 @@ def lib():
                                                        C.POINTER(PipelineOpts), C.POINTER(SolveOpts), C.c_void_p,
                                                        C.c_void_p, C.c_double, C.POINTER(C.c_double), C.c_void_p,
                                                        C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(Stats)]
+        L.mtk_pipeline_position_gradient.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
+                                                     C.POINTER(PipelineOpts), C.POINTER(SolveOpts), C.c_void_p,
+                                                     C.c_double, C.POINTER(C.c_double), C.c_void_p, C.c_void_p,
+                                                     C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(Stats)]
+        L.mtk_field_power_adjoint.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                              C.c_void_p, C.c_int32, C.POINTER(SolveOpts), C.c_void_p, C.c_void_p,
+                                              C.c_void_p, C.c_void_p, C.POINTER(Stats)]
+        L.mtk_face_geometry_backward.argtypes = [C.c_void_p, C.c_int32, C.c_int32] + [C.c_void_p] * 8
         _lib = L
     return _lib
 
@@ -359,6 +368,44 @@ def size_field_gradient(ctx: Context, V, F, s, T=None, mu=0.0, ratio=0.02, seed=
                                                   C.byref(n_full), C.byref(st)),
            "mtk_pipeline_size_field_gradient")
     return dict(loss=loss.value, grad=grad, fullx=fullx[:n_full.value].copy(), stats=st.as_dict())
+
+
+def position_gradient(ctx: Context, V, F, s, mu=0.0, ratio=0.02, seed=0, round_seams=False, n_iter=50, opts=None):
+    """mtk_pipeline_position_gradient: the size-field loss with the integration target, its
+    gradient with respect to s and to the vertex positions (integer decisions held fixed)."""
+    V = np.ascontiguousarray(V, np.float64)
+    F = np.ascontiguousarray(F, np.int32)
+    nV, nF = len(V), len(F)
+    s = np.ascontiguousarray(s, np.float64)
+    if s.shape != (nV,):
+        raise ValueError("s must have one value per vertex")
+    nE = 3 * nF // 2
+    cap = 2 * (nV + 4 * nE) + 16
+    fullx = np.zeros(cap)
+    grad_s = np.zeros(nV)
+    grad_V = np.zeros((nV, 3))
+    loss = C.c_double(0)
+    n_full = C.c_int32(0)
+    p = PipelineOpts(seed, n_iter, ratio, int(round_seams), 0, 0, 0)
+    o = opts or solve_opts()
+    st = Stats()
+    _check(lib().mtk_pipeline_position_gradient(ctx.handle, nV, nF, _ptr(V), _ptr(F), C.byref(p), C.byref(o), _ptr(s),
+                                                float(mu), C.byref(loss), _ptr(grad_s), _ptr(grad_V), _ptr(fullx), cap,
+                                                C.byref(n_full), C.byref(st)),
+           "mtk_pipeline_position_gradient")
+    return dict(loss=loss.value, grad_s=grad_s, grad_V=grad_V, fullx=fullx[:n_full.value].copy(), stats=st.as_dict())
+
+
+def face_geometry_backward(ctx: Context, V, F, g_area, g_farg1, g_farg2, g_gx, g_gy):
+    """mtk_face_geometry_backward: vertex-position gradient from per-face derivatives."""
+    V = np.ascontiguousarray(V, np.float64)
+    F = np.ascontiguousarray(F, np.int32)
+    arrs = [np.ascontiguousarray(a, np.float64).reshape(-1) for a in (g_area, g_farg1, g_farg2, g_gx, g_gy)]
+    out = np.zeros((len(V), 3))
+    _check(lib().mtk_face_geometry_backward(ctx.handle, len(V), len(F), _ptr(V), _ptr(F), *[_ptr(a) for a in arrs],
+                                            _ptr(out)),
+           "mtk_face_geometry_backward")
+    return out
 
 
 def topology_from_field(V, F, compressed, ratio=0.02, round_seams=False):

@@ -866,6 +866,69 @@ __global__ void start_from_rhs(int n, const double2* __restrict__ b, double2* x,
     publish_partials<double, 1>(red, partials);
 }
 
+// ---------------------------------------------------------------- reverse power iteration
+// Adjoint of u_{k+1} = x / s, x = L^-1 M u_k, s = sqrt(x^H M x) (the field's inverse power
+// iteration), for a loss seeded through the field angle phi_f = arg(c_f) / N of the last iterate
+// c.  With the real inner product <a, b> = Re(a^H b):
+//   seed       gu = i dphi c / (N |c|^2)                (dl = <gu, dc>)
+//   per step   a = <gu, u_{k+1}>, gx = (gu - a M u_{k+1}) / s_{k+1}, d area -= a |u_{k+1}|^2 / 2;
+//              L mu = gx (the same Hermitian solve as the forward step);
+//              d area_f += Re(conj(mu_f) u_k,f), d theta_fj += N Im(conj(mu_f) L_fj x_g)
+//              (dL_fj / dtheta = i N L_fj, x = s u_{k+1}), gu = M mu.
+__global__ void adj_seed(int n, int N, const double* __restrict__ dphi, const double2* __restrict__ c, double2* gu) {
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < n; f += gridDim.x * blockDim.x) {
+        const double2 cf = c[f];
+        const double w = dphi[f] / ((double)N * (cf.x * cf.x + cf.y * cf.y));
+        gu[f] = make_double2(-w * cf.y, w * cf.x);
+    }
+}
+
+// block partials of Re(gu^H u)
+__global__ void adj_dot(int n, const double2* __restrict__ gu, const double2* __restrict__ u, double* partials) {
+    double v[1] = {0.0};
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < n; f += gridDim.x * blockDim.x) {
+        const double2 g = gu[f], w = u[f];
+        v[0] += g.x * w.x + g.y * w.y;
+    }
+    block_sum<double, 1>(v);
+    if (threadIdx.x == 0) partials[blockIdx.x] = v[0];
+}
+
+// gx = (gu - a area u) / s into b; g_area -= a |u|^2 / 2.  scal[0] = a, s2[0] = s^2.
+__global__ void adj_rhs(int n, const double2* __restrict__ gu, const double2* __restrict__ u,
+                        const double* __restrict__ area, const double* __restrict__ scal, const double* __restrict__ s2,
+                        double2* b, double* g_area) {
+    const double a = scal[0], s = sqrt(fabs(s2[0]));
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < n; f += gridDim.x * blockDim.x) {
+        const double2 g = gu[f], w = u[f];
+        const double m = area[f];
+        b[f] = make_double2((g.x - a * m * w.x) / s, (g.y - a * m * w.y) / s);
+        g_area[f] -= 0.5 * a * (w.x * w.x + w.y * w.y);
+    }
+}
+
+// after L mu = gx: the area and transport-angle terms of this step and gu = M mu
+__global__ void adj_accumulate(ComplexEll<double> A, int N, const double2* __restrict__ mu, const double2* __restrict__ u,
+                               const double2* __restrict__ uprev, const double* __restrict__ s2,
+                               const double* __restrict__ area, double* g_area, double* g_theta, double2* gu) {
+    const int n = A.n;
+    const double s = sqrt(fabs(s2[0]));
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < n; f += gridDim.x * blockDim.x) {
+        const double2 m = mu[f], up = uprev[f];
+        g_area[f] += m.x * up.x + m.y * up.y;
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            const int g = A.nbr[j * n + f];
+            const double2 l = A.val[j * n + f], w = u[g];
+            const double xr = s * w.x, xi = s * w.y;
+            const double lr = l.x * xr - l.y * xi, li = l.x * xi + l.y * xr;   // L_fj x_g
+            g_theta[j * n + f] += (double)N * (m.x * li - m.y * lr);            // N Im(conj(mu) L x)
+        }
+        const double a = area[f];
+        gu[f] = make_double2(a * m.x, a * m.y);
+    }
+}
+
 __global__ void zero_f2(int n, float2* e) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) e[i] = make_float2(0.f, 0.f);
 }
@@ -1266,9 +1329,18 @@ template <> DevHierarchy<float> FieldSolver::hier<float>() const { return H32; }
 namespace {
 // The field solves: with rhs == nullptr the inverse power iteration from x0 (n_iter steps,
 // M-normalised), otherwise one solve L x = rhs from x = 0 (x0 and n_iter unused).
+// Reverse pass of the power iteration (mtk_field_power_adjoint): dphi[nF] in, per face the
+// derivatives with respect to theta (3 nF, [3 f + j] for the halfedge F(f,j) -> F(f,j+1)) and
+// to the face area (nF) out.
+struct FieldAdjoint {
+    const double* dphi;
+    double* g_theta;
+    double* g_area;
+};
+
 int field_run(mtk_ctx* c, int32_t nF, int32_t nRosy, const int32_t* nbr_h, const double* theta_h, const double* area_h,
               const double* x0, int32_t n_iter, const mtk_solve_opts* opts_in, double* out, mtk_stats* stats,
-              const double* rhs) {
+              const double* rhs, const FieldAdjoint* adj = nullptr) {
     if (rhs) n_iter = 1;
     if (!c || nF <= 0 || nRosy <= 0 || !nbr_h || !theta_h || !area_h || (!x0 && !rhs) || !out || n_iter < 0)
         return MTK_ERR_BAD_INPUT;
@@ -1364,6 +1436,75 @@ int field_run(mtk_ctx* c, int32_t nF, int32_t nRosy, const int32_t* nbr_h, const
     // Measured as sqrt(max(0, rr_fp64 - rr_fp32)) / |r_start| and used to stop the next step's
     // solves at half of it instead of iterating below what FP64 will see.
     double floor_rel[3] = {0.0, 0.0, 0.0};
+    DBuf<double2> Uall;   // the iterates u_0 .. u_n (reverse pass only)
+    DBuf<double> sall;    // s_k^2 = x_k^H M x_k
+    if (adj) {
+        MTK_TRY(Uall.alloc((size_t)(n_iter + 1) * n));
+        MTK_TRY(sall.alloc((size_t)n_iter + 1));
+        MTK_CUDA_TRY(cudaMemcpyAsync(Uall.p, S.ringU[0].p, sizeof(double2) * n, cudaMemcpyDeviceToDevice, st));
+    }
+    // one solve L x = b from the current x / r (S.b, S.x, S.r, and S.r32 when MIXED) to the
+    // relative residual tol: FP64 PCG, or FP32 PCG inside FP64 refinement; rr in: the start
+    // residual |r|^2, out: the final one
+    auto solve_to_goal = [&](double bnorm2, double& rr) -> int {
+        const double goal2 = tol * tol * bnorm2;
+        solves++;
+        refines++;
+        if (!mixed) {
+            double frr = 0;
+            int s = S.pcg<double, double2>(S.A64(), S.inv64.p, S.b.p, S.x.p, S.r.p, S.z64.p, S.p64.p, S.q64.p, S.rb64.p,
+                                           S.pb64.p, S.sv64.p, S.vv64.p, goal2,
+                                           opts.max_iter, &iters, &frr);
+            if (s != MTK_OK) return s;
+            // true FP64 residual of the result
+            residual64<<<G, kStream, 0, st>>>(S.A64(), S.b.p, S.x.p, S.r.p, nullptr, c->partials);
+            c->kernels++;
+            MTK_TRY(S.finalize(G, 1));
+            MTK_TRY(S.read_scalars(1));
+            rr = c->h_scalars[0];
+            refines++;
+        } else {
+            int outer = 0;
+            while (rr > goal2) {
+                if (outer >= opts.max_refine) return MTK_ERR_NOT_CONVERGED;
+                outer++;
+                // inner FP32 solve L e = r to inner_tol relative (at least the outer goal)
+                double itol = opts.inner_tol;
+                double need = std::sqrt(goal2 / rr) * 0.5;
+                if (need > itol) itol = need;
+                const int ki = std::min(outer, 3) - 1;
+                const double fl = std::min(0.5 * floor_rel[ki], 0.1);
+                if (fl > itol) itol = fl;
+                zero_f2<<<G, kStream, 0, st>>>(n, S.e32.p);
+                c->kernels++;
+                double frr = 0.0;
+                const long long it0 = iters;
+                int s = S.pcg<float, float2>(S.A32(), S.inv32.p, S.r32.p, S.e32.p, S.z32.p /*r*/, S.p32.p /*z*/,
+                                             S.q32.p /*p*/, reinterpret_cast<float2*>(S.Lu.p) /*q*/, S.rb32.p, S.pb32.p,
+                                             S.sv32.p, S.vv32.p, itol * itol * rr,
+                                             opts.max_iter, &iters, &frr);
+                if (debug)
+                    fprintf(stderr, "[field pcg] status %d iterations %lld rr %.3e target %.3e (from %.3e)\n", s,
+                            iters - it0, frr, itol * itol * rr, rr);
+                // an FP32 breakdown (p^H A p <= 0 in single precision) means the inner solve has
+                // stagnated: its last iterate is still a valid correction, and the FP64 refinement
+                // decides what comes next (bounded by max_refine, stopped when it makes no progress)
+                if (s == MTK_ERR_TIMEOUT) return s;
+                const double rr_prev = rr;
+                add_correction<<<G, kStream, 0, st>>>(n, S.e32.p, S.x.p);
+                residual64<<<G, kStream, 0, st>>>(S.A64(), S.b.p, S.x.p, S.r.p, S.r32.p, c->partials);
+                c->kernels += 2;
+                MTK_TRY(S.finalize(G, 1));
+                MTK_TRY(S.read_scalars(1));
+                rr = c->h_scalars[0];
+                refines++;
+                if (!(rr == rr)) return MTK_ERR_BREAKDOWN;
+                if (rr > goal2 && rr >= rr_prev) return MTK_ERR_NOT_CONVERGED;
+                if (s == MTK_OK && rr_prev > 0) floor_rel[ki] = std::sqrt(std::max(rr - frr, 0.0) / rr_prev);
+            }
+        }
+        return MTK_OK;
+    };
     for (int k = 0; k < n_iter; k++) {
         double bnorm2 = 0, rr = 0;
         if (rhs) {   // plain solve: x = 0, r = b
@@ -1430,63 +1571,8 @@ int field_run(mtk_ctx* c, int32_t nF, int32_t nRosy, const int32_t* nbr_h, const
             mtk_set_last_error("field solve: NaN in the right-hand side or the start residual", __FILE__, __LINE__);
             return MTK_ERR_BREAKDOWN;
         }
-        const double goal2 = tol * tol * bnorm2;
         const double start_rel = bnorm2 > 0 ? std::sqrt(rr / bnorm2) : 0.0;
-        solves++;
-        refines++;
-        if (!mixed) {
-            double frr = 0;
-            int s = S.pcg<double, double2>(S.A64(), S.inv64.p, S.b.p, S.x.p, S.r.p, S.z64.p, S.p64.p, S.q64.p, S.rb64.p,
-                                           S.pb64.p, S.sv64.p, S.vv64.p, goal2,
-                                           opts.max_iter, &iters, &frr);
-            if (s != MTK_OK) return s;
-            // true FP64 residual of the result
-            residual64<<<G, kStream, 0, st>>>(S.A64(), S.b.p, S.x.p, S.r.p, nullptr, c->partials);
-            c->kernels++;
-            MTK_TRY(S.finalize(G, 1));
-            MTK_TRY(S.read_scalars(1));
-            rr = c->h_scalars[0];
-            refines++;
-        } else {
-            int outer = 0;
-            while (rr > goal2) {
-                if (outer >= opts.max_refine) return MTK_ERR_NOT_CONVERGED;
-                outer++;
-                // inner FP32 solve L e = r to inner_tol relative (at least the outer goal)
-                double itol = opts.inner_tol;
-                double need = std::sqrt(goal2 / rr) * 0.5;
-                if (need > itol) itol = need;
-                const int ki = std::min(outer, 3) - 1;
-                const double fl = std::min(0.5 * floor_rel[ki], 0.1);
-                if (fl > itol) itol = fl;
-                zero_f2<<<G, kStream, 0, st>>>(n, S.e32.p);
-                c->kernels++;
-                double frr = 0.0;
-                const long long it0 = iters;
-                int s = S.pcg<float, float2>(S.A32(), S.inv32.p, S.r32.p, S.e32.p, S.z32.p /*r*/, S.p32.p /*z*/,
-                                             S.q32.p /*p*/, reinterpret_cast<float2*>(S.Lu.p) /*q*/, S.rb32.p, S.pb32.p,
-                                             S.sv32.p, S.vv32.p, itol * itol * rr,
-                                             opts.max_iter, &iters, &frr);
-                if (debug)
-                    fprintf(stderr, "[field pcg] status %d iterations %lld rr %.3e target %.3e (from %.3e)\n", s,
-                            iters - it0, frr, itol * itol * rr, rr);
-                // an FP32 breakdown (p^H A p <= 0 in single precision) means the inner solve has
-                // stagnated: its last iterate is still a valid correction, and the FP64 refinement
-                // decides what comes next (bounded by max_refine, stopped when it makes no progress)
-                if (s == MTK_ERR_TIMEOUT) return s;
-                const double rr_prev = rr;
-                add_correction<<<G, kStream, 0, st>>>(n, S.e32.p, S.x.p);
-                residual64<<<G, kStream, 0, st>>>(S.A64(), S.b.p, S.x.p, S.r.p, S.r32.p, c->partials);
-                c->kernels += 2;
-                MTK_TRY(S.finalize(G, 1));
-                MTK_TRY(S.read_scalars(1));
-                rr = c->h_scalars[0];
-                refines++;
-                if (!(rr == rr)) return MTK_ERR_BREAKDOWN;
-                if (rr > goal2 && rr >= rr_prev) return MTK_ERR_NOT_CONVERGED;
-                if (s == MTK_OK && rr_prev > 0) floor_rel[ki] = std::sqrt(std::max(rr - frr, 0.0) / rr_prev);
-            }
-        }
+        MTK_TRY(solve_to_goal(bnorm2, rr));
         double rel = bnorm2 > 0 ? std::sqrt(rr / bnorm2) : 0.0;
         if (rel > worst) worst = rel;
         if (debug)
@@ -1500,6 +1586,58 @@ int field_run(mtk_ctx* c, int32_t nF, int32_t nRosy, const int32_t* nbr_h, const
         normalize_to<<<G, kStream, 0, st>>>(n, c->scalars, S.x.p, S.ringU[(k + 1) % ring].p);
         c->kernels++;
         MTK_CUDA_TRY(cudaGetLastError());
+        if (adj) {   // keep u_{k+1} and s_{k+1}^2 for the reverse pass
+            MTK_CUDA_TRY(cudaMemcpyAsync(Uall.p + (size_t)(k + 1) * n, S.ringU[(k + 1) % ring].p, sizeof(double2) * n,
+                                         cudaMemcpyDeviceToDevice, st));
+            MTK_CUDA_TRY(cudaMemcpyAsync(sall.p + k + 1, c->scalars, sizeof(double), cudaMemcpyDeviceToDevice, st));
+        }
+    }
+    if (adj) {
+        // reverse pass over the stored iterates (faces in the solver's order)
+        std::vector<double> dphi_p(n);
+        for (int k = 0; k < n; k++) dphi_p[k] = adj->dphi[S.amg ? S.perm[k] : k];
+        DBuf<double> d_dphi, g_area, g_theta;
+        DBuf<double2> gu;
+        MTK_TRY(d_dphi.upload(dphi_p.data(), n, st));
+        MTK_TRY(g_area.alloc(n)); MTK_TRY(g_area.zero(st));
+        MTK_TRY(g_theta.alloc(3 * (size_t)n)); MTK_TRY(g_theta.zero(st));
+        MTK_TRY(gu.alloc(n));
+        adj_seed<<<G, kStream, 0, st>>>(n, nRosy, d_dphi.p, Uall.p + (size_t)n_iter * n, gu.p);
+        c->kernels++;
+        for (int k = n_iter; k >= 1; k--) {
+            const double2* uk = Uall.p + (size_t)k * n;
+            const double2* up = Uall.p + (size_t)(k - 1) * n;
+            adj_dot<<<G, kStream, 0, st>>>(n, gu.p, uk, c->partials);
+            c->kernels++;
+            MTK_TRY(S.finalize(G, 1));
+            adj_rhs<<<G, kStream, 0, st>>>(n, gu.p, uk, S.area.p, c->scalars, sall.p + k, S.b.p, g_area.p);
+            start_from_rhs<<<G, kStream, 0, st>>>(n, S.b.p, S.x.p, S.r.p, mixed ? S.r32.p : nullptr, c->partials);
+            c->kernels += 2;
+            MTK_TRY(S.finalize(G, 1));
+            MTK_TRY(S.read_scalars(1));
+            double rr = c->h_scalars[0];
+            if (!(rr == rr)) {
+                mtk_set_last_error("field adjoint: NaN in the reverse pass", __FILE__, __LINE__);
+                return MTK_ERR_BREAKDOWN;
+            }
+            const double bnorm2 = rr;
+            MTK_TRY(solve_to_goal(bnorm2, rr));
+            const double rel = bnorm2 > 0 ? std::sqrt(rr / bnorm2) : 0.0;
+            if (rel > worst) worst = rel;
+            adj_accumulate<<<G, kStream, 0, st>>>(S.A64(), nRosy, S.x.p, uk, up, sall.p + k, S.area.p, g_area.p,
+                                                  g_theta.p, gu.p);
+            c->kernels++;
+            MTK_CUDA_TRY(cudaGetLastError());
+        }
+        std::vector<double> ha(n), ht(3 * (size_t)n);
+        MTK_CUDA_TRY(cudaMemcpyAsync(ha.data(), g_area.p, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+        MTK_CUDA_TRY(cudaMemcpyAsync(ht.data(), g_theta.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
+        MTK_CUDA_TRY(cudaStreamSynchronize(st));
+        for (int k = 0; k < n; k++) {
+            const int f = S.amg ? S.perm[k] : k;
+            adj->g_area[f] = ha[k];
+            for (int j = 0; j < 3; j++) adj->g_theta[3 * (size_t)f + j] = ht[(size_t)j * n + k];
+        }
     }
     std::vector<double> out_p;
     double* out_u = out;
@@ -1541,6 +1679,14 @@ extern "C" int mtk_field_smoothest(mtk_ctx* c, int32_t nF, int32_t nRosy, const 
                                    int32_t n_iter, const mtk_solve_opts* opts_in, double* out, mtk_stats* stats) {
     if (!x0) return MTK_ERR_BAD_INPUT;
     return field_run(c, nF, nRosy, nbr_h, theta_h, area_h, x0, n_iter, opts_in, out, stats, nullptr);
+}
+
+extern "C" int mtk_field_power_adjoint(mtk_ctx* c, int32_t nF, int32_t nRosy, const int32_t* nbr_h, const double* theta_h,
+                                       const double* area_h, const double* x0, int32_t n_iter, const mtk_solve_opts* opts_in,
+                                       const double* dphi, double* out, double* g_theta, double* g_area, mtk_stats* stats) {
+    if (!x0 || !dphi || !g_theta || !g_area || n_iter < 1) return MTK_ERR_BAD_INPUT;
+    const FieldAdjoint adj{dphi, g_theta, g_area};
+    return field_run(c, nF, nRosy, nbr_h, theta_h, area_h, x0, n_iter, opts_in, out, stats, nullptr, &adj);
 }
 
 extern "C" int mtk_field_solve(mtk_ctx* c, int32_t nF, int32_t nRosy, const int32_t* nbr_h, const double* theta_h,

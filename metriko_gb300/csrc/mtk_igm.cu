@@ -931,6 +931,54 @@ __global__ void add_z_projected(int nY, int nZ, int kq, const double* __restrict
 // Size-field loss, per face (functions k = 0..3 with k >= 2 the negatives of k - 2): the
 // gradient g of the parameterization U, r = length g - es_f T_f (8 values), rT_f = r . T_f, and
 // the partial sum of |r|^2.
+// Partial derivatives of the size-field loss with the integration target (T = F2) at fixed x,
+// for the vertex-position gradient (x minimises the loss's first term, so dl/dV is the partial
+// at fixed x): per face, with r_fk = length grad(u_k)_f - e_f F2_fk and NF[c, k] the function
+// values at the cut corners (sign symmetry: NF[c, k + 2] = -NF[c, k]),
+//   dgx[3 f + a] = 2 length sum_k r_fk,x NF[c_a, k],   dgy likewise with the y components,
+//   dphi[f] = sum_k (-2 e_f r_fk) . (-F2_fk,y, F2_fk,x)   (F2_fk = (cos, sin) of the field angle),
+// and the block partials of dl/dlength = sum_f sum_k 2 r_fk . grad(u_k)_f.
+__global__ void face_position_partials(int nF, const int* __restrict__ cutF, const double* __restrict__ grad,
+                                       const double* __restrict__ U, double length, const double* __restrict__ es,
+                                       const double* __restrict__ F2, double* dgx, double* dgy, double* dphi,
+                                       double* partials) {
+    double red[1] = {0};
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nF; f += gridDim.x * blockDim.x) {
+        double g[2][2] = {{0, 0}, {0, 0}};
+        for (int a = 0; a < 3; a++) {
+            const int c = cutF[3 * f + a];
+            const double gx = grad[6 * f + 2 * a], gy = grad[6 * f + 2 * a + 1];
+            for (int k = 0; k < 2; k++) { g[k][0] += gx * U[2 * c + k]; g[k][1] += gy * U[2 * c + k]; }
+        }
+        double r[4][2];
+        double dl = 0, dp = 0;
+        for (int k = 0; k < 4; k++) {
+            const double sgn = k < 2 ? 1.0 : -1.0;
+            for (int comp = 0; comp < 2; comp++) {
+                const double gu = sgn * g[k & 1][comp];
+                r[k][comp] = length * gu - es[f] * F2[8 * f + 2 * k + comp];
+                dl += 2.0 * r[k][comp] * gu;
+            }
+            const double tx = F2[8 * f + 2 * k], ty = F2[8 * f + 2 * k + 1];
+            dp += -2.0 * es[f] * (r[k][0] * -ty + r[k][1] * tx);
+        }
+        for (int a = 0; a < 3; a++) {
+            const int c = cutF[3 * f + a];
+            double sx = 0, sy = 0;
+            for (int k = 0; k < 4; k++) {
+                const double nf = (k < 2 ? 1.0 : -1.0) * U[2 * c + (k & 1)];
+                sx += r[k][0] * nf;
+                sy += r[k][1] * nf;
+            }
+            dgx[3 * f + a] = 2.0 * length * sx;
+            dgy[3 * f + a] = 2.0 * length * sy;
+        }
+        dphi[f] = dp;
+        red[0] += dl;
+    }
+    publish_partials<double, 1>(red, partials);
+}
+
 __global__ void face_residual(int nF, const int* __restrict__ cutF, const double* __restrict__ grad,
                               const double* __restrict__ U, double length, const double* __restrict__ es,
                               const double* __restrict__ T, double* r, double* rT, double* partials) {
@@ -1037,6 +1085,11 @@ struct SizeFieldJob {
     double mu;
     double* loss;
     double* grad_s;     // nV
+    // position partials (face_position_partials; T must be null), all null when not wanted
+    double* dgx = nullptr;      // 3 nF
+    double* dgy = nullptr;      // 3 nF
+    double* dphi = nullptr;     // nF
+    double* dlength = nullptr;  // 1
 };
 
 struct Igm {
@@ -2119,6 +2172,20 @@ int igm_run(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts_in, do
         MTK_CUDA_TRY(cudaGetLastError());
         double lsum = 0;
         MTK_CUDA_TRY(cudaMemcpyAsync(&lsum, c->scalars, sizeof(double), cudaMemcpyDeviceToHost, st));
+        if (job->dgx) {   // position partials at the forward x (U still holds W x)
+            DBuf<double> pgx, pgy, pph;
+            MTK_TRY(pgx.alloc(3 * (size_t)nF)); MTK_TRY(pgy.alloc(3 * (size_t)nF)); MTK_TRY(pph.alloc(nF));
+            face_position_partials<<<G, kStream, 0, st>>>(nF, S.cutF.p, S.grad.p, S.U.p, length, d_es.p, S.F2.p, pgx.p,
+                                                          pgy.p, pph.p, c->partials);
+            finalize1<<<1, kStream, 0, st>>>(c->partials, G, c->scalars + 1);
+            c->kernels += 2;
+            MTK_CUDA_TRY(cudaGetLastError());
+            MTK_CUDA_TRY(cudaMemcpyAsync(job->dgx, pgx.p, sizeof(double) * 3 * nF, cudaMemcpyDeviceToHost, st));
+            MTK_CUDA_TRY(cudaMemcpyAsync(job->dgy, pgy.p, sizeof(double) * 3 * nF, cudaMemcpyDeviceToHost, st));
+            MTK_CUDA_TRY(cudaMemcpyAsync(job->dphi, pph.p, sizeof(double) * nF, cudaMemcpyDeviceToHost, st));
+            MTK_CUDA_TRY(cudaMemcpyAsync(job->dlength, c->scalars + 1, sizeof(double), cudaMemcpyDeviceToHost, st));
+            MTK_CUDA_TRY(cudaStreamSynchronize(st));
+        }
         MTK_TRY(S.build_rhs(r8.p, 2.0 * length, 0.0, nullptr, S.bsys.p));
         MTK_CUDA_TRY(cudaMemsetAsync(lam.p, 0, sizeof(double) * nRed, st));   // feasible: fixed entries 0
         double rel2 = 0;
@@ -2299,6 +2366,18 @@ extern "C" int mtk_iterative_rounding(mtk_ctx* c, const mtk_igm_desc* d, const m
                                       int32_t* fix_order, int32_t* fix_vals, int32_t* n_fixed, double* x_naive,
                                       mtk_stats* stats) {
     return igm_run(c, d, opts_in, fullx, fix_order, fix_vals, n_fixed, x_naive, stats, nullptr);
+}
+
+extern "C" int mtk_size_field_position_partials(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts,
+                                                int32_t nV, const int32_t* F, const double* s, double mu, double* loss,
+                                                double* grad_s, double* fullx, double* dgx, double* dgy, double* dphi,
+                                                double* dlength, mtk_stats* stats) {
+    if (!c || !d || !F || !s || !loss || !grad_s || !fullx || !dgx || !dgy || !dphi || !dlength || nV <= 0 || !(mu >= 0))
+        return MTK_ERR_BAD_INPUT;
+    for (int64_t i = 0; i < 3 * (int64_t)d->nF; i++)
+        if (F[i] < 0 || F[i] >= nV) return MTK_ERR_BAD_INPUT;
+    SizeFieldJob job{nV, F, s, nullptr, mu, loss, grad_s, dgx, dgy, dphi, dlength};
+    return igm_run(c, d, opts, fullx, nullptr, nullptr, nullptr, nullptr, stats, &job);
 }
 
 extern "C" int mtk_size_field_gradient(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts, int32_t nV,

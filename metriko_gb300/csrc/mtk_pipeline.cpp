@@ -206,6 +206,108 @@ extern "C" int mtk_pipeline_size_field_gradient(mtk_ctx* ctx, int32_t nV, int32_
     }
 }
 
+extern "C" int mtk_pipeline_position_gradient(mtk_ctx* ctx, int32_t nV, int32_t nF, const double* Vb, const int32_t* Fb,
+                                              const mtk_pipeline_opts* popts, const mtk_solve_opts* sopts,
+                                              const double* s, double mu, double* loss, double* grad_s, double* grad_V,
+                                              double* fullx_out, int32_t fullx_cap, int32_t* n_full, mtk_stats* stats) {
+    if (!ctx || nV <= 0 || nF <= 0 || !Vb || !Fb || !popts || !s || !loss || !grad_s || !grad_V || !(mu >= 0))
+        return MTK_ERR_BAD_INPUT;
+    gpu::bound_context() = ctx;
+    struct Unbind { ~Unbind() { gpu::bound_context() = nullptr; } } unbind;
+    gpu::stats() = mtk_stats{};
+    if (sopts) gpu::options().solve = *sopts;
+    else mtk_default_opts(&gpu::options().solve);
+    gpu::options().seed = popts->seed;
+    gpu::options().n_iter = popts->n_iter > 0 ? popts->n_iter : 50;
+    try {
+        MatXd V(nV, 3);
+        MatXi F(nF, 3);
+        std::memcpy(V.data(), Vb, sizeof(double) * 3 * size_t(nV));
+        std::memcpy(F.data(), Fb, sizeof(int32_t) * 3 * size_t(nF));
+        auto mesh = std::make_unique<Hmesh>(V, F, Hmesh::Deferred{});
+        auto pending = std::async(std::launch::async, [&m = *mesh] { side_thread_cores(); m.finish(); return seam_base(m); });
+        FaceRosyField rawf(*mesh, 4, FieldType::Smoothest);
+        SeamBase base = pending.get();
+        rawf.computeMatching(MatchingType::Curl);
+        auto seam = compute_seam(rawf, std::move(base));
+        auto cut_pending = std::async(std::launch::async, [&m = *mesh, &seam] { return compute_cut_mesh(m, seam); });
+        auto cmbf = compute_combbed_field(rawf, seam);
+        MatXd extf = compute_extrinsic_field(*mesh, *cmbf, 4);
+        auto cutm = cut_pending.get();
+        RosyParameterization rp(*mesh, *cutm, extf, cmbf->singular, cmbf->matching, seam, 4, popts->ratio);
+        rp.seamless = false;
+        rp.localInjectivity = false;
+        rp.roundSeams = popts->round_seams != 0;
+        rp.verbose = false;
+        rp.setup();
+        // 1. the loss, its s gradient and its partials at fixed x (G2 entries, field angle, length)
+        VecXd sv(std::vector<double>(s, s + nV)), gs;
+        std::vector<double> dgx, dgy, dphi;
+        double dlength = 0, length = 0;
+        *loss = rp.size_field_position_partials(sv, mu, gs, dgx, dgy, dphi, &dlength, &length);
+        std::memcpy(grad_s, gs.data(), sizeof(double) * nV);
+        // 2. the field angle through the power iteration: derivatives of theta and of the areas
+        std::vector<int> nb;
+        std::vector<double> th;
+        rawf.assembly_inputs(nb, th);
+        std::vector<double> x0(2 * size_t(nF)), cfield(2 * size_t(nF)), gth(3 * size_t(nF)), gar(nF);
+        mtk_seeded_init(nF, gpu::options().seed, x0.data());
+        gpu::check(mtk_field_power_adjoint(ctx, nF, 4, nb.data(), th.data(), mesh->faceArea.data(), x0.data(),
+                                           gpu::options().n_iter, &gpu::options().solve, dphi.data(), cfield.data(),
+                                           gth.data(), gar.data(), &gpu::stats()),
+                   "mtk_field_power_adjoint");
+        // theta_fj = farg(h) - farg(twin h) for the halfedge h of f on edge j
+        const Hmesh& m = *mesh;
+        std::vector<double> gfarg(m.nH, 0.0), gf1(nF), gf2(nF);
+        for (int f = 0; f < nF; f++)
+            for (int j = 0; j < 3; j++) {
+                const int h = m.face2half3(f, j);
+                gfarg[h] += gth[3 * size_t(f) + j];
+                gfarg[m.twin[h]] -= gth[3 * size_t(f) + j];
+            }
+        for (int f = 0; f < nF; f++) {
+            gf1[f] = gfarg[m.face2half3(f, 1)];
+            gf2[f] = gfarg[m.face2half3(f, 2)];
+        }
+        // 3. per-face geometry backward and the vertex gather
+        gpu::check(mtk_face_geometry_backward(ctx, nV, nF, Vb, Fb, gar.data(), gf1.data(), gf2.data(), dgx.data(),
+                                              dgy.data(), grad_V),
+                   "mtk_face_geometry_backward");
+        // 4. length = ratio |D| / norm, D the bounding-box diagonal: its extreme vertices (the
+        //    first vertex holding each extreme coordinate)
+        double D[3];
+        int imax[3] = {0, 0, 0}, imin[3] = {0, 0, 0};
+        for (int k = 0; k < 3; k++) {
+            for (int v = 1; v < nV; v++) {
+                if (Vb[3 * size_t(v) + k] > Vb[3 * size_t(imax[k]) + k]) imax[k] = v;
+                if (Vb[3 * size_t(v) + k] < Vb[3 * size_t(imin[k]) + k]) imin[k] = v;
+            }
+            D[k] = Vb[3 * size_t(imax[k]) + k] - Vb[3 * size_t(imin[k]) + k];
+        }
+        const double dn = std::sqrt(D[0] * D[0] + D[1] * D[1] + D[2] * D[2]);
+        const double norm = popts->ratio * dn / length;
+        for (int k = 0; k < 3; k++) {
+            const double g = dlength * popts->ratio * D[k] / (dn * norm);
+            grad_V[3 * size_t(imax[k]) + k] += g;
+            grad_V[3 * size_t(imin[k]) + k] -= g;
+        }
+        const int nFull = rp.fullx.size();
+        if (n_full) *n_full = nFull;
+        if (fullx_out && fullx_cap >= nFull) std::memcpy(fullx_out, rp.fullx.data(), sizeof(double) * nFull);
+        if (stats) *stats = gpu::stats();
+        return MTK_OK;
+    } catch (const std::invalid_argument& e) {
+        mtk_set_last_error(e.what(), __FILE__, __LINE__);
+        return MTK_ERR_BAD_INPUT;
+    } catch (const metriko::gpu::status_error& e) {
+        mtk_set_last_error(e.what(), __FILE__, __LINE__);
+        return e.status;
+    } catch (const std::exception& e) {
+        mtk_set_last_error(e.what(), __FILE__, __LINE__);
+        return MTK_ERR_CUDA;
+    }
+}
+
 extern "C" int mtk_topology_from_field(int32_t nV, int32_t nF, const double* Vb, const int32_t* Fb,
                                        const double* compressed, double ratio, int32_t round_seams,
                                        int32_t* singular, int32_t* matching, uint8_t* seam_out, int32_t* cutF,
