@@ -1154,8 +1154,9 @@ struct FieldSolver {
         // a matrix for which the cost model picks several lanes per row, with enough rows to fill
         // the grid with one lane per row and short rows, gets a SELL-32 copy and one lane per row
         const bool use_sell = !getenv("MTK_NO_SELL");
-        auto worth = [&](int rows, double a) { return use_sell && sell_worth(rows, a * rows, grp(rows, a)); };
+        auto worth = [&](int rows, double a) { return use_sell && sell_worth(rows, a); };
         auto sgrp = [&](int rows, double a) { return worth(rows, a) ? 1 : grp(rows, a); };
+        bool up_sell = false, r_sell = false;
         // adopt a device CSR (FP64 values) and its FP32 copy
         auto adopt = [&](DevCsrC& D, CsrBufs& B, int group) -> int {
             B.n = D.n;
@@ -1178,6 +1179,8 @@ struct FieldSolver {
                 DevCycleOpsC& O = dops[i + 1];
                 lv_nnz[3 * i] = (double)O.R.nnz; lv_nnz[3 * i + 1] = (double)O.S.nnz; lv_nnz[3 * i + 2] = (double)O.P.nnz;
                 lv_n[2 * i] = O.S.n; lv_n[2 * i + 1] = O.R.n;
+                up_sell = worth(O.S.n, std::max(davg(O.S), davg(O.P)));
+                r_sell = worth(O.R.n, davg(O.R));
                 const int up = sgrp(O.S.n, std::max(davg(O.S), davg(O.P)));
                 MTK_TRY(adopt(O.R, B.R, sgrp(O.R.n, davg(O.R))));
                 MTK_TRY(adopt(O.S, B.S, up));
@@ -1187,6 +1190,8 @@ struct FieldSolver {
                 const HostCycleOps& O = HH.ops[i + 1];
                 lv_nnz[3 * i] = (double)O.R.col.size(); lv_nnz[3 * i + 1] = (double)O.S.col.size(); lv_nnz[3 * i + 2] = (double)O.P.col.size();
                 lv_n[2 * i] = O.S.n; lv_n[2 * i + 1] = O.R.n;
+                up_sell = worth(O.S.n, std::max(avg(O.S), avg(O.P)));
+                r_sell = worth(O.R.n, avg(O.R));
                 MTK_TRY(upload_csr(O.R, B.R, sgrp(O.R.n, avg(O.R))));
                 const int up = sgrp(O.S.n, std::max(avg(O.S), avg(O.P)));
                 MTK_TRY(upload_csr(O.S, B.S, up));
@@ -1195,13 +1200,12 @@ struct FieldSolver {
             }
             MTK_TRY(B.r64.alloc(ln)); MTK_TRY(B.r32.alloc(ln));
             MTK_TRY(B.y64.alloc(ln)); MTK_TRY(B.y32.alloc(ln));
-            if (use_sell)
-                for (CsrBufs* C : {&B.R, &B.S, &B.P})
-                    if (C->group == 1 && C->n > 0 && worth(C->n, (double)C->nnz / C->n)) {
-                        MTK_TRY(sell_build_index(c, st, C->n, C->ptr.p, C->col.p, C->sell));
-                        MTK_TRY(sell_fill_values<double2>(c, st, C->n, C->ptr.p, C->col.p, C->v64.p, C->sell, C->s64));
-                        MTK_TRY(sell_fill_values<float2>(c, st, C->n, C->ptr.p, C->col.p, C->v32.p, C->sell, C->s32));
-                    }
+            for (CsrBufs* C : {&B.R, &B.S, &B.P})
+                if (C->n > 0 && (C == &B.R ? r_sell : up_sell)) {
+                    MTK_TRY(sell_build_index(c, st, C->n, C->ptr.p, C->col.p, C->sell));
+                    MTK_TRY(sell_fill_values<double2>(c, st, C->n, C->ptr.p, C->col.p, C->v64.p, C->sell, C->s64));
+                    MTK_TRY(sell_fill_values<float2>(c, st, C->n, C->ptr.p, C->col.p, C->v32.p, C->sell, C->s32));
+                }
             auto mk64 = [](const CsrBufs& C) {
                 DevCsr<double> M{C.n, C.group, C.ptr.p, C.col.p, C.v64.p};
                 if (C.sell.sptr.p) { M.sptr = C.sell.sptr.p; M.scol = C.sell.scol.p; M.sval = C.s64.p; }

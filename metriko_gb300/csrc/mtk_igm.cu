@@ -1208,7 +1208,8 @@ struct Igm {
         // a matrix for which the cost model picks several lanes per row, with enough rows to fill
         // the grid with one lane per row and short rows, gets a SELL-32 copy and one lane per row
         const bool use_sell = !getenv("MTK_NO_SELL");
-        auto sell_rows = [&](int n, size_t nnz) { return use_sell && sell_worth(n, (double)nnz, grp(n, nnz)); };
+        auto sell_rows = [&](int n, double avg) { return use_sell && sell_worth(n, avg); };
+        auto avg_of = [](int n, size_t nnz) { return n > 0 ? (double)nnz / n : 0.0; };
         // adopt a device CSR (FP64 values) and its FP32 copy
         auto adopt = [&](DevCsr64& D, RCsrBufs& B, int group) -> int {
             B.n = D.n;
@@ -1224,6 +1225,7 @@ struct Igm {
             return MTK_OK;
         };
         std::vector<double> lvl_nnz(3 * nl), lvl_n(2 * nl);   // R, S, P entries; S rows, R rows
+        std::vector<char> up_sell(nl, 0), r_sell(nl, 0);       // phases given SELL-32 copies
         for (int l = 0; l < nl; l++) {
             RLevelBufs& B = rlv[l];
             int nS, nR;
@@ -1233,17 +1235,20 @@ struct Igm {
                 nS = O.S.n; nR = O.R.n; zR = O.R.nnz; zS = O.S.nnz; zP = O.P.nnz;
                 // level 0's up phase writes z with the thread-per-row mapping of the PCG vector
                 // loops, which read it with no grid barrier in between: keep it at one lane per row
-                const int up = l == 0 || (sell_rows(nS, zS) && sell_rows(O.P.n, zP)) ? 1
-                                                                                       : std::max(grp(nS, zS), grp(O.P.n, zP));
-                MTK_TRY(adopt(O.R, B.R, sell_rows(nR, zR) ? 1 : grp(nR, zR)));
+                // level 0's up phase stays CSR, one lane per row (short rows; see sell_worth)
+                up_sell[l] = l > 0 && sell_rows(nS, std::max(avg_of(nS, zS), avg_of(O.P.n, zP)));
+                r_sell[l] = sell_rows(nR, avg_of(nR, zR));
+                const int up = l == 0 || up_sell[l] ? 1 : std::max(grp(nS, zS), grp(O.P.n, zP));
+                MTK_TRY(adopt(O.R, B.R, r_sell[l] ? 1 : grp(nR, zR)));
                 MTK_TRY(adopt(O.S, B.S, up));
                 MTK_TRY(adopt(O.P, B.P, up));
             } else {
                 const RCycleOps& O = HH.ops[l];
                 nS = O.S.n; nR = O.R.n; zR = O.R.col.size(); zS = O.S.col.size(); zP = O.P.col.size();
-                const int up = l == 0 || (sell_rows(nS, zS) && sell_rows(O.P.n, zP)) ? 1
-                                                                                       : std::max(grp(nS, zS), grp(O.P.n, zP));
-                MTK_TRY(upload_rcsr(O.R, B.R, sell_rows(nR, zR) ? 1 : grp(nR, zR)));
+                up_sell[l] = l > 0 && sell_rows(nS, std::max(avg_of(nS, zS), avg_of(O.P.n, zP)));
+                r_sell[l] = sell_rows(nR, avg_of(nR, zR));
+                const int up = l == 0 || up_sell[l] ? 1 : std::max(grp(nS, zS), grp(O.P.n, zP));
+                MTK_TRY(upload_rcsr(O.R, B.R, r_sell[l] ? 1 : grp(nR, zR)));
                 MTK_TRY(upload_rcsr(O.S, B.S, up));
                 MTK_TRY(upload_rcsr(O.P, B.P, up));
             }
@@ -1253,13 +1258,12 @@ struct Igm {
                 MTK_TRY(B.r64.alloc(nS)); MTK_TRY(B.y64.alloc(nS));
                 MTK_TRY(B.r32.alloc(nS)); MTK_TRY(B.y32.alloc(nS));
             }
-            if (use_sell)
-                for (RCsrBufs* C : {&B.R, &B.S, &B.P})
-                    if (C->group == 1 && C->n > 0 && sell_rows(C->n, C->nnz)) {
-                        MTK_TRY(sell_build_index(c, st, C->n, C->ptr.p, C->col.p, C->sell));
-                        MTK_TRY(sell_fill_values<double>(c, st, C->n, C->ptr.p, C->col.p, C->v64.p, C->sell, C->s64));
-                        MTK_TRY(sell_fill_values<float>(c, st, C->n, C->ptr.p, C->col.p, C->v32.p, C->sell, C->s32));
-                    }
+            for (RCsrBufs* C : {&B.R, &B.S, &B.P})
+                if (C->n > 0 && (C == &B.R ? r_sell[l] : up_sell[l])) {
+                    MTK_TRY(sell_build_index(c, st, C->n, C->ptr.p, C->col.p, C->sell));
+                    MTK_TRY(sell_fill_values<double>(c, st, C->n, C->ptr.p, C->col.p, C->v64.p, C->sell, C->s64));
+                    MTK_TRY(sell_fill_values<float>(c, st, C->n, C->ptr.p, C->col.p, C->v32.p, C->sell, C->s32));
+                }
             auto m64 = [](const RCsrBufs& C) {
                 RDevCsr<double> M{C.n, C.group, C.ptr.p, C.col.p, C.v64.p};
                 if (C.sell.sptr.p) { M.sptr = C.sell.sptr.p; M.scol = C.sell.scol.p; M.sval = C.s64.p; }
