@@ -342,6 +342,33 @@ int mtk_face_geometry_backward(mtk_ctx* ctx, int32_t nV, int32_t nF, const doubl
                                const double* g_gy, double* grad_V);
 
 /*
+ * Assembled sparse systems (the general linear-solver seam).  Replaces, for symmetric / Hermitian
+ * positive-definite matrices, the direct solvers behind solveSquare(SprsC&, VecXc&) and
+ * solveSmallestEig(SprsC&, SprsC&, int) (include/metriko/core/solver/sparse_linear_solver.h:16-54)
+ * and the LMSolver's linear-solver template parameter CholeskyWrapper::factorize / solve
+ * (include/metriko/core/igm/iterative_rounding/iter_rounding.h:14-31).
+ *   mtk_csr_create   n x n CSR (ptr[n+1] with ptr[0] = 0, col[nnz], val[nnz] or, when
+ *                    complex_values, val[2 nnz] as (re, im)); copied to the device once (FP64 and
+ *                    FP32) with its Jacobi inverse.  A diagonal entry <= 0 -> MTK_ERR_BAD_INPUT.
+ *   mtk_csr_pcg      A X = B for nrhs columns (column-major: column c at c * n (real) or
+ *                    c * 2 n (complex, (re, im) pairs)); x in: start, out: solution.  Jacobi PCG,
+ *                    up to four columns per launch (the matrix read once per iteration for all),
+ *                    FP64 or FP32 inside FP64 refinement (opts->precision), each column to the
+ *                    relative residual opts->tol.
+ *   mtk_csr_smallest_eig  n_iter steps of x = L^-1 M u, x /= sqrt|x^H M x|, u = x from x0 (complex
+ *                    (re, im) vectors; L and M complex Hermitian, e.g. M diagonal), the reference's
+ *                    solveSmallestEig with iterative solves; out[2 n].
+ */
+typedef struct mtk_csr mtk_csr;
+int mtk_csr_create(mtk_ctx* ctx, int32_t n, const int32_t* ptr, const int32_t* col, const double* val,
+                   int32_t complex_values, mtk_csr** out);
+int mtk_csr_destroy(mtk_csr* A);
+int mtk_csr_pcg(mtk_ctx* ctx, const mtk_csr* A, int32_t nrhs, const double* b, double* x, const mtk_solve_opts* opts,
+                mtk_stats* stats);
+int mtk_csr_smallest_eig(mtk_ctx* ctx, const mtk_csr* L, const mtk_csr* M, const double* x0, int32_t n_iter,
+                         const mtk_solve_opts* opts, double* out, mtk_stats* stats);
+
+/*
  * Barrier of the local-injectivity option: InjectiveBarrier(N, nF, intrinsic_field) followed by
  * update(field, update_j, fBarrier, gBarrier) of core/igm/iterative_rounding/injective_barrier.h:
  * 18-106.  Layout of intrinsic_field and field: 2*N values per face (vector j of face i at

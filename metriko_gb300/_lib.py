@@ -24,7 +24,8 @@ EXPORTS = [
     "mtk_pipeline_size_field_gradient", "mtk_field_solve", "mtk_field_inputs", "mtk_field_spmv_bench",
     "mtk_injective_barrier", "mtk_local_injectivity", "mtk_map_deviation",
     "mtk_mesh_geometry", "mtk_ctx_set_wait_limit", "mtk_pipeline_position_gradient", "mtk_size_field_position_partials",
-    "mtk_field_power_adjoint", "mtk_face_geometry_backward",
+    "mtk_field_power_adjoint", "mtk_face_geometry_backward", "mtk_csr_create", "mtk_csr_destroy", "mtk_csr_pcg",
+    "mtk_csr_smallest_eig",
 ]
 
 
@@ -118,6 +119,13 @@ def lib():
                                               C.c_void_p, C.c_int32, C.POINTER(SolveOpts), C.c_void_p, C.c_void_p,
                                               C.c_void_p, C.c_void_p, C.POINTER(Stats)]
         L.mtk_face_geometry_backward.argtypes = [C.c_void_p, C.c_int32, C.c_int32] + [C.c_void_p] * 8
+        L.mtk_csr_create.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                     C.POINTER(C.c_void_p)]
+        L.mtk_csr_destroy.argtypes = [C.c_void_p]
+        L.mtk_csr_pcg.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.POINTER(SolveOpts),
+                                  C.POINTER(Stats)]
+        L.mtk_csr_smallest_eig.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                           C.POINTER(SolveOpts), C.c_void_p, C.POINTER(Stats)]
         _lib = L
     return _lib
 
@@ -406,6 +414,76 @@ def face_geometry_backward(ctx: Context, V, F, g_area, g_farg1, g_farg2, g_gx, g
                                             _ptr(out)),
            "mtk_face_geometry_backward")
     return out
+
+
+class CsrMatrix:
+    """A device-resident assembled sparse matrix (mtk_csr): symmetric / Hermitian positive
+    definite, real or complex; built from a scipy.sparse matrix."""
+
+    def __init__(self, ctx: Context, A):
+        import scipy.sparse as sp
+        A = sp.csr_matrix(A)
+        A.sort_indices()
+        self.n = A.shape[0]
+        self.complex = np.iscomplexobj(A.data)
+        ptr = np.ascontiguousarray(A.indptr, np.int32)
+        col = np.ascontiguousarray(A.indices, np.int32)
+        if self.complex:
+            val = np.empty(2 * A.nnz)
+            val[0::2], val[1::2] = A.data.real, A.data.imag
+        else:
+            val = np.ascontiguousarray(A.data, np.float64)
+        h = C.c_void_p()
+        _check(lib().mtk_csr_create(ctx.handle, self.n, _ptr(ptr), _ptr(col), _ptr(val), int(self.complex), C.byref(h)),
+               "mtk_csr_create")
+        self.handle, self.ctx = h, ctx
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().mtk_csr_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _pack(self, v):
+        v = np.asarray(v)
+        v2 = v.reshape(self.n, -1, order="F")
+        if self.complex:
+            out = np.empty((2 * self.n, v2.shape[1]), order="F")
+            out[0::2], out[1::2] = v2.real, v2.imag
+            return out, v2.shape[1]
+        return np.asfortranarray(v2, np.float64), v2.shape[1]
+
+    def _unpack(self, w, shape):
+        if self.complex:
+            w = w[0::2] + 1j * w[1::2]
+        return w.reshape(shape, order="F")
+
+    def solve(self, b, x0=None, opts=None):
+        """mtk_csr_pcg: A X = B (b: n or n x k); returns (x, stats)."""
+        B, k = self._pack(b)
+        X, _ = self._pack(np.zeros_like(np.asarray(b)) if x0 is None else x0)
+        st = Stats()
+        o = opts or solve_opts()
+        _check(lib().mtk_csr_pcg(self.ctx.handle, self.handle, k, _ptr(B), _ptr(X), C.byref(o), C.byref(st)),
+               "mtk_csr_pcg")
+        return self._unpack(X, np.asarray(b).shape), st.as_dict()
+
+
+def csr_smallest_eig(ctx: Context, L: CsrMatrix, M: CsrMatrix, x0, n_iter=50, opts=None):
+    """mtk_csr_smallest_eig: the reference's solveSmallestEig on assembled (L, M)."""
+    x = np.empty(2 * L.n)
+    x[0::2], x[1::2] = np.real(x0), np.imag(x0)
+    out = np.empty(2 * L.n)
+    st = Stats()
+    o = opts or solve_opts()
+    _check(lib().mtk_csr_smallest_eig(ctx.handle, L.handle, M.handle, _ptr(x), n_iter, C.byref(o), _ptr(out), C.byref(st)),
+           "mtk_csr_smallest_eig")
+    return out[0::2] + 1j * out[1::2], st.as_dict()
 
 
 def topology_from_field(V, F, compressed, ratio=0.02, round_seams=False):

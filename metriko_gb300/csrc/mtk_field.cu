@@ -1331,8 +1331,6 @@ template <> DevHierarchy<float> FieldSolver::hier<float>() const { return H32; }
 }  // namespace
 
 namespace {
-// The field solves: with rhs == nullptr the inverse power iteration from x0 (n_iter steps,
-// M-normalised), otherwise one solve L x = rhs from x = 0 (x0 and n_iter unused).
 // Reverse pass of the power iteration (mtk_field_power_adjoint): dphi[nF] in, per face the
 // derivatives with respect to theta (3 nF, [3 f + j] for the halfedge F(f,j) -> F(f,j+1)) and
 // to the face area (nF) out.
@@ -1341,6 +1339,10 @@ struct FieldAdjoint {
     double* g_theta;
     double* g_area;
 };
+
+// The field solves: with rhs == nullptr the inverse power iteration from x0 (n_iter steps,
+// M-normalised), otherwise one solve L x = rhs from x = 0 (x0 and n_iter unused); with adj the
+// iterates are kept and the reverse pass follows the forward one.
 
 int field_run(mtk_ctx* c, int32_t nF, int32_t nRosy, const int32_t* nbr_h, const double* theta_h, const double* area_h,
               const double* x0, int32_t n_iter, const mtk_solve_opts* opts_in, double* out, mtk_stats* stats,

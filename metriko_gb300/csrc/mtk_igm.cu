@@ -1240,6 +1240,10 @@ struct Igm {
                 r_sell[l] = sell_rows(nR, avg_of(nR, zR));
                 const int up = l == 0 || up_sell[l] ? 1 : std::max(grp(nS, zS), grp(O.P.n, zP));
                 MTK_TRY(adopt(O.R, B.R, r_sell[l] ? 1 : grp(nR, zR)));
+                if (debug())
+                    fprintf(stderr, "[igm host]   level %d: %d rows (S %.1f, P %.1f per row), R %d rows (%.1f per row)%s%s\n",
+                            l, nS, avg_of(nS, zS), avg_of(O.P.n, zP), nR, avg_of(nR, zR), up_sell[l] ? ", up SELL" : "",
+                            r_sell[l] ? ", R SELL" : "");
                 MTK_TRY(adopt(O.S, B.S, up));
                 MTK_TRY(adopt(O.P, B.P, up));
             } else {

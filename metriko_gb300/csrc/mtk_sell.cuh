@@ -21,15 +21,16 @@
 namespace mtk {
 
 // When a SELL-32 copy pays (measured on the GB300 with the persistent solvers' phase timers, at
-// 1.3M faces): on the phases of large levels whose rows hold 10 to 24 entries on average -- the
-// restriction of the IGM free block's first level (38.8 -> 28.0 us per application) and the
-// up-phase of the field's first inner level (28.4 -> 22.3 us), where one lane per row with
-// coalesced entry loads beats the scattered per-thread row walks.  On the short rows of the
-// finest IGM level (about 7 entries: 63 -> 70 us) and on small levels (fewer rows than the grid
-// has threads) the padding and the lost lane parallelism made it slower.
-constexpr double kSellMinAvg = 10.0, kSellMaxAvg = 24.0;
+// 1.3M faces): on the phases of levels with at least 100K rows and at most 24 entries per row on
+// average -- the restriction of the IGM free block's first level (38.8 -> 28.0 us per
+// application) and the up-phase of the field's first inner level (28.4 -> 22.3 us), where one
+// lane per row with coalesced entry loads beats the scattered per-thread row walks.  Small levels
+// (fewer rows than the grid has threads) lose lane parallelism and keep CSR; so does the finest
+// IGM level's up-phase (about 7 entries per row: 63 -> 70 us with SELL), which the caller leaves
+// out.
+constexpr double kSellMaxAvg = 24.0;
 constexpr int kSellMinRows = 100000;
-inline bool sell_worth(int n, double avg) { return n >= kSellMinRows && avg >= kSellMinAvg && avg <= kSellMaxAvg; }
+inline bool sell_worth(int n, double avg) { return n >= kSellMinRows && avg <= kSellMaxAvg; }
 
 namespace sellk {
 // w[s] = longest row of slice s

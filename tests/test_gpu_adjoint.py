@@ -158,9 +158,14 @@ def _position_fd_check(gpu_ctx, name, ndir, h, rtol, seed):
         Vp, Vm = V + h * d, V - h * d
         if not all(np.array_equal(a, b) for W in (Vp, Vm) for a, b in zip(_topology(gpu_ctx, W, F, ratio), base)):
             continue
-        lp = M.size_field_gradient(gpu_ctx, Vp, F, s, mu=0.1, ratio=ratio, opts=_opts())["loss"]
-        lm = M.size_field_gradient(gpu_ctx, Vm, F, s, mu=0.1, ratio=ratio, opts=_opts())["loss"]
-        fd = (lp - lm) / (2 * h)
+        # central differences at h and h/2, Richardson-combined (the field's near-degenerate
+        # eigenvalue cluster makes the loss strongly curved in V)
+        def central(t):
+            lp = M.size_field_gradient(gpu_ctx, V + t * d, F, s, mu=0.1, ratio=ratio, opts=_opts())["loss"]
+            lm = M.size_field_gradient(gpu_ctx, V - t * d, F, s, mu=0.1, ratio=ratio, opts=_opts())["loss"]
+            return (lp - lm) / (2 * t)
+        f1, f2 = central(h), central(h / 2)
+        fd = f2 + (f2 - f1) / 3.0
         an = float(np.sum(g * d))
         assert abs(fd - an) <= rtol * max(abs(fd), abs(an), 1e-3 * np.linalg.norm(g)), (fd, an)
         checked += 1
@@ -175,4 +180,4 @@ def test_position_autograd_finite_differences_small(gpu_ctx):
 def test_position_autograd_finite_differences_level7(gpu_ctx):
     """Differentiation workload: level-7 displaced sphere (327,680 faces), s ~ N(0, 0.2), 16 random
     directions that keep every integer decision."""
-    _position_fd_check(gpu_ctx, "ico7_sh8", 16, 1e-4, 1e-4, 32)
+    _position_fd_check(gpu_ctx, "ico7_sh8", 16, 4e-5, 1e-4, 32)
