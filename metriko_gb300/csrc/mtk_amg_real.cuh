@@ -513,10 +513,21 @@ __device__ void rcsr_phase(const RDevCsr<T>& M, const T* x, const RDevCsr<T>* M2
     const int stride = gridDim.x * blockDim.x;
     const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
     const int g = M.group;
-    // optional extra term out += sum_k phi[k n + row] yc[k] (phi column-major, yc replicated)
+    // optional extra term out += sum_k phi[row kp + k] yc[k] (phi row-major FP16, each row padded
+    // to kp = nphi rounded up to 8 entries: one 16-byte load per 8 columns; yc replicated)
+    const int kp = (nphi + 7) & ~7;
     auto extra = [&](int row) {
         T e = T(0);
-        for (int k = 0; k < nphi; k++) e += (T)__half2float(__ldg(phi + (size_t)k * M.n + row)) * yc[k];
+        for (int k0 = 0; k0 < nphi; k0 += 8) {
+            const uint4 v = __ldg(reinterpret_cast<const uint4*>(phi + (size_t)row * kp + k0));
+            const __half2* h2 = reinterpret_cast<const __half2*>(&v);
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const float2 f = __half22float2(h2[q]);
+                if (k0 + 2 * q < nphi) e += (T)f.x * yc[k0 + 2 * q];
+                if (k0 + 2 * q + 1 < nphi) e += (T)f.y * yc[k0 + 2 * q + 1];
+            }
+        }
         return e;
     };
     if (g == 1) {
@@ -547,8 +558,9 @@ __device__ void rcsr_phase(const RDevCsr<T>& M, const T* x, const RDevCsr<T>* M2
 }
 
 // z = out_scale * B r on the hierarchy; level 0 reads H.L[0].r and writes H.L[0].y (masked);
-// rz (may be null) accumulates this thread's share of r . z.  With phi (column-major, nphi
-// columns) the level-0 output also gets phi * yc, in the same pass.
+// rz (may be null) accumulates this thread's share of r . z.  With phi (row-major FP16, nphi
+// columns, rows padded to a multiple of 8) the level-0 output also gets phi * yc, in the same
+// pass.
 template <typename T>
 __device__ bool rvcycle(const RDevHierarchy<T>& H, T out_scale, const unsigned char* mask0, const GridBarrier& bar,
                         T* rz = nullptr, const __half* phi = nullptr, int nphi = 0, const T* yc = nullptr) {

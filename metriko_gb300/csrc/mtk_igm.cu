@@ -352,7 +352,7 @@ __device__ bool igm_apply_asm(const IgmOp<T>& A, const unsigned char* __restrict
     return true;
 }
 
-// Schur coarse space of the z block.  Phi (nY x nZ, column-major) holds approximations of
+// Schur coarse space of the z block.  Phi (nY x nZ; the kernels read an FP16 row-major copy) holds approximations of
 // -K_yy^-1 K_yz, so the columns of Z = [Phi ; I] are the z directions extended into the free
 // block with (nearly) least energy; the preconditioner adds Z W Z^T r to the multigrid of the
 // free block, W = P (P G P + ridge)^-1 P with G = Z^T K Z (the P's keep it on the feasible z
@@ -360,15 +360,17 @@ __device__ bool igm_apply_asm(const IgmOp<T>& A, const unsigned char* __restrict
 // an exact Phi this is the block factorisation K^-1 = [K_yy^-1 0; 0 0] + Z S^-1 Z^T (S the Schur
 // complement of the z block), so the coupled system converges like the free block alone.
 //
-// Block partials of Phi^T r_y in fixed order: out[k * gridDim.x + blockIdx.x].  The columns are
-// taken kPhiChunk at a time in one pass over r (each thread keeps one sum per column of the
-// chunk, over the same rows in the same order as a pass per column would).
-constexpr int kPhiChunk = 8;
+// Block partials of Phi^T r_y in fixed order: out[k * gridDim.x + blockIdx.x].  Phi is row-major
+// FP16 with rows padded to kp = nZ rounded up to 8 (16-byte loads); the columns are taken
+// kPhiChunk at a time in one pass over r (each thread keeps one sum per column of the chunk, over
+// the same rows in the same order as a pass per column would).
+constexpr int kPhiChunk = 16;
 template <typename T>
 __device__ void phi_dots_publish(const __half* __restrict__ Phi, int nY, int nZ, const T* r, T* out, T* wsum) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int stride = gridDim.x * blockDim.x;
     const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    const int kp = (nZ + 7) & ~7;
     for (int k0 = 0; k0 < nZ; k0 += kPhiChunk) {
         const int kc = nZ - k0 < kPhiChunk ? nZ - k0 : kPhiChunk;
         T a[kPhiChunk];
@@ -377,8 +379,17 @@ __device__ void phi_dots_publish(const __half* __restrict__ Phi, int nY, int nZ,
         for (int j = t0; j < nY; j += stride) {
             const T rj = __ldcg(r + j);
 #pragma unroll
-            for (int u = 0; u < kPhiChunk; u++)
-                if (u < kc) a[u] += (T)__half2float(__ldg(Phi + (size_t)(k0 + u) * nY + j)) * rj;
+            for (int g = 0; g < kPhiChunk / 8; g++) {
+                if (8 * g >= kc) break;
+                const uint4 v = __ldg(reinterpret_cast<const uint4*>(Phi + (size_t)j * kp + k0 + 8 * g));
+                const __half2* h2 = reinterpret_cast<const __half2*>(&v);
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const float2 f = __half22float2(h2[q]);
+                    a[8 * g + 2 * q] += (T)f.x * rj;
+                    a[8 * g + 2 * q + 1] += (T)f.y * rj;
+                }
+            }
         }
 #pragma unroll
         for (int u = 0; u < kPhiChunk; u++) {
@@ -1007,12 +1018,15 @@ __global__ void face_residual(int nF, const int* __restrict__ cutF, const double
     publish_partials<double, 1>(red, partials);
 }
 
-// Phi rounded to FP16 (the kernels' copy); the FP32 copy keeps the rounded values, so the
-// Galerkin block built from it belongs to the basis the kernels apply.
-__global__ void phi_round_half(size_t n, float* phi, __half* phih) {
+// Phi rounded to FP16 (the kernels' copy, row-major with rows padded to kp entries, the padding
+// zeroed beforehand); the FP32 copy (column-major) keeps the rounded values, so the Galerkin
+// block built from it belongs to the basis the kernels apply.
+__global__ void phi_round_half(int nY, int nZ, int kp, float* phi, __half* phih) {
+    const size_t n = (size_t)nY * nZ;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t j = i % nY, k = i / nY;
         const __half h = __float2half_rn(phi[i]);
-        phih[i] = h;
+        phih[j * kp + k] = h;
         phi[i] = __half2float(h);
     }
 }
@@ -1539,8 +1553,10 @@ struct Igm {
             if (s != MTK_OK && s != MTK_ERR_NOT_CONVERGED) { cur_scale = save_scale; return MTK_OK; }
             MTK_CUDA_TRY(cudaMemcpyAsync(phi.p + (size_t)k * nY, xk, sizeof(float) * nY, cudaMemcpyDeviceToDevice, st));
         }
-        MTK_TRY(phih.alloc((size_t)nY * nZ));
-        phi_round_half<<<stream_grid(c), kStream, 0, st>>>((size_t)nY * nZ, phi.p, phih.p);
+        const int kp = (nZ + 7) & ~7;
+        MTK_TRY(phih.alloc((size_t)nY * kp));
+        MTK_CUDA_TRY(cudaMemsetAsync(phih.p, 0, sizeof(__half) * (size_t)nY * kp, st));
+        phi_round_half<<<stream_grid(c), kStream, 0, st>>>(nY, nZ, kp, phi.p, phih.p);
         c->kernels++;
         MTK_CUDA_TRY(cudaGetLastError());
         G0.assign((size_t)nZ * nZ, 0.0);
