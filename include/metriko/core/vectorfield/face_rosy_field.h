@@ -167,7 +167,23 @@ namespace metriko {
             }
         }
 
-        void computeMatching(const MatchingType type) {   // face_rosy_field.h:119-135
+        // face_rosy_field.h:119-135.  Inside a device pipeline call (a context bound to the host
+        // thread) the Curl matching and the singular indices come from mtk_curl_matching, one
+        // thread per edge and per vertex, with the same integer results; `connection` is then left
+        // empty (nothing downstream of the matching reads it).
+        void computeMatching(const MatchingType type) {
+            if (type == MatchingType::Curl && gpu::bound_context() && rosyN <= 8) {
+                matching = VecXi(mesh.nE, -1);
+                singular = VecXi(mesh.nV, 0);
+                connection = VecXc();
+                gpu::check(mtk_curl_matching(gpu::bound_context(), mesh.nV, mesh.nF, mesh.nE, rosyN, mesh.pos.data(),
+                                             mesh.idx.data(), mesh.edge2vert.data(), mesh.edge2face.data(),
+                                             mesh.vert2half.data(), mesh.prev.data(), mesh.angleDefect.data(),
+                                             reinterpret_cast<const double*>(compressed.data()), matching.data(),
+                                             singular.data()),
+                           "mtk_curl_matching");
+                return;
+            }
             computeConnection();
             matching = VecXi(mesh.nE, -1);
             VecXd effort = VecXd::Zero(mesh.nE);

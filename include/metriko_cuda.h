@@ -342,6 +342,22 @@ int mtk_face_geometry_backward(mtk_ctx* ctx, int32_t nV, int32_t nF, const doubl
                                const double* g_gy, double* grad_V);
 
 /*
+ * Curl matching and singular indices on the device, for a closed mesh: computeConnection,
+ * cMatching and computeSingular of FaceRosyField::computeMatching(MatchingType::Curl)
+ * (include/metriko/core/vectorfield/face_rosy_field.h:100-135, :169-202), one thread per edge and
+ * one per vertex.  Mesh arrays in the Hmesh numbering (halfedge 2e of edge e runs from
+ * edge_vert[2e] to edge_vert[2e+1] inside face edge_face[2e]; 2e+1 is its twin, in
+ * edge_face[2e+1]):  V[3 nV], F[3 nF], edge_vert[2 nE], edge_face[2 nE], vert_half[nV],
+ * prev_half[2 nE], angle_defect[nV]; compressed[2 nF] the field (re, im); N <= 8.
+ * Out: matching[nE], singular[nV].  The integer outputs equal the host loops' (the arithmetic is
+ * the same, up to the last bit of the device's cos / sin / atan2 / sqrt).
+ */
+int mtk_curl_matching(mtk_ctx* ctx, int32_t nV, int32_t nF, int32_t nE, int32_t N, const double* V, const int32_t* F,
+                      const int32_t* edge_vert, const int32_t* edge_face, const int32_t* vert_half,
+                      const int32_t* prev_half, const double* angle_defect, const double* compressed,
+                      int32_t* matching, int32_t* singular);
+
+/*
  * Assembled sparse systems (the general linear-solver seam).  Replaces, for symmetric / Hermitian
  * positive-definite matrices, the direct solvers behind solveSquare(SprsC&, VecXc&) and
  * solveSmallestEig(SprsC&, SprsC&, int) (include/metriko/core/solver/sparse_linear_solver.h:16-54)

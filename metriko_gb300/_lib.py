@@ -25,7 +25,7 @@ EXPORTS = [
     "mtk_injective_barrier", "mtk_local_injectivity", "mtk_map_deviation",
     "mtk_mesh_geometry", "mtk_ctx_set_wait_limit", "mtk_pipeline_position_gradient", "mtk_size_field_position_partials",
     "mtk_field_power_adjoint", "mtk_face_geometry_backward", "mtk_csr_create", "mtk_csr_destroy", "mtk_csr_pcg",
-    "mtk_csr_smallest_eig",
+    "mtk_csr_smallest_eig", "mtk_curl_matching",
 ]
 
 
@@ -126,6 +126,7 @@ def lib():
                                   C.POINTER(Stats)]
         L.mtk_csr_smallest_eig.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
                                            C.POINTER(SolveOpts), C.c_void_p, C.POINTER(Stats)]
+        L.mtk_curl_matching.argtypes = [C.c_void_p] + [C.c_int32] * 4 + [C.c_void_p] * 10
         _lib = L
     return _lib
 
@@ -414,6 +415,26 @@ def face_geometry_backward(ctx: Context, V, F, g_area, g_farg1, g_farg2, g_gx, g
                                             _ptr(out)),
            "mtk_face_geometry_backward")
     return out
+
+
+def curl_matching(ctx: Context, V, F, edge_vert, edge_face, vert_half, prev_half, angle_defect, compressed, N=4):
+    """mtk_curl_matching: Curl matching[nE] and singular indices[nV] on the device, from the mesh
+    arrays in the Hmesh numbering and the compressed field (complex[nF])."""
+    V = np.ascontiguousarray(V, np.float64)
+    F = np.ascontiguousarray(F, np.int32)
+    ev = np.ascontiguousarray(edge_vert, np.int32)
+    ef = np.ascontiguousarray(edge_face, np.int32)
+    vh = np.ascontiguousarray(vert_half, np.int32)
+    pv = np.ascontiguousarray(prev_half, np.int32)
+    ad = np.ascontiguousarray(angle_defect, np.float64)
+    c = np.ascontiguousarray(np.asarray(compressed, np.complex128).view(np.float64))
+    nE = len(ev)
+    matching = np.zeros(nE, np.int32)
+    singular = np.zeros(len(V), np.int32)
+    _check(lib().mtk_curl_matching(ctx.handle, len(V), len(F), nE, N, _ptr(V), _ptr(F), _ptr(ev), _ptr(ef), _ptr(vh),
+                                   _ptr(pv), _ptr(ad), _ptr(c), _ptr(matching), _ptr(singular)),
+           "mtk_curl_matching")
+    return matching, singular
 
 
 class CsrMatrix:

@@ -20,7 +20,8 @@ CSRC = HERE / "csrc"
 OUT = HERE / "libmetriko_cuda.so"
 BUILD = HERE / "_build"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["mtk_ctx.cu", "mtk_field.cu", "mtk_igm.cu", "mtk_noalloc.cu", "mtk_barrier.cu", "mtk_adjoint.cu", "mtk_csr.cu"]
+CU_SOURCES = ["mtk_ctx.cu", "mtk_field.cu", "mtk_igm.cu", "mtk_noalloc.cu", "mtk_barrier.cu", "mtk_adjoint.cu", "mtk_csr.cu",
+              "mtk_topology.cu"]
 CPP_SOURCES = ["mtk_pipeline.cpp"]
 
 

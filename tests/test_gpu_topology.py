@@ -1,0 +1,93 @@
+"""Curl matching and singular indices on the device (mtk_curl_matching) against the oracle's
+computeConnection / cMatching / computeSingular (face_rosy_field.h:100-202): integer outputs,
+identical.  On the golden fixtures (their stored field), on seeded fields, and at the 1.3M-face
+benchmark size on the field the GPU solves, where the host C++ path of mtk_topology_from_field
+gives the singular indices to compare."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import metriko_gb300 as M
+from metriko_gb300 import meshgen
+from oracle import metriko_oracle as O
+
+pytestmark = pytest.mark.gpu
+GOLDEN = Path(__file__).parent / "golden"
+
+
+def _oracle(m, c, N=4):
+    fld = O.rosy_from_compressed(c, N)
+    conn = O.compute_connection(m)
+    iM, effort = O.c_matching(m, fld, conn, N)
+    return iM, O.compute_singular(m, effort, N)
+
+
+def _device(ctx, m, c, N=4):
+    return M.curl_matching(ctx, m.pos, m.idx, m.edge2vert, m.edge2face, m.vert2half, m.prev, m.angleDefect, c, N=N)
+
+
+@pytest.mark.parametrize("name", ["ico2_noise", "ico3_noise", "torus_32x16", "genus2_s3", "icosphere_obj"])
+def test_curl_matching_golden_field(gpu_ctx, name):
+    g = np.load(GOLDEN / f"{name}.npz")
+    m = O.Hmesh(g["V"], g["F"])
+    c = g["compressed"]
+    match, sing = _device(gpu_ctx, m, c)
+    ref_match, ref_sing = _oracle(m, c)
+    assert np.array_equal(match, ref_match)
+    assert np.array_equal(sing, ref_sing)
+    assert np.array_equal(sing, g["singular"])
+
+
+@pytest.mark.parametrize("N", [1, 2, 3, 4, 6])
+@pytest.mark.parametrize("seed", [0, 1])
+def test_curl_matching_seeded_field(gpu_ctx, N, seed):
+    """A rough field (seeded, not smooth): many edges with large efforts and every matching
+    value; N other than 4 goes through the generic kernel."""
+    V, F, _, _ = meshgen.workload("ico3_noise")
+    m = O.Hmesh(V, F)
+    c = O.seeded_init(m.nF, seed)
+    match, sing = _device(gpu_ctx, m, c, N)
+    ref_match, ref_sing = _oracle(m, c, N)
+    assert np.array_equal(match, ref_match)
+    assert np.array_equal(sing, ref_sing)
+
+
+def test_curl_matching_sums_to_euler_characteristic(gpu_ctx):
+    """Sum of singular indices = N * chi on a smooth field: 8 on the sphere, 0 on the torus."""
+    for name, want in [("ico4_noise", 8), ("torus_64x32", 0)]:
+        V, F, _, _ = meshgen.workload(name)
+        m = O.Hmesh(V, F)
+        nbr = m.face[m.twin[m.FH]].astype(np.int32)
+        theta = m.farg[m.FH] - m.farg[m.twin[m.FH]]
+        c, _ = M.field_smoothest(gpu_ctx, nbr, theta, m.faceArea, O.seeded_init(m.nF, 0))
+        _, sing = _device(gpu_ctx, m, c)
+        assert int(sing.sum()) == want
+
+
+def test_curl_matching_benchmark_size(gpu_ctx):
+    """1,310,720 faces / 1,966,080 edges: the device matching equals the oracle's on every edge
+    and the device singular indices equal the host C++ loops' (mtk_topology_from_field)."""
+    V, F, ratio, rs = meshgen.workload("ico8_sh8")
+    m = O.Hmesh(V, F)
+    nbr = m.face[m.twin[m.FH]].astype(np.int32)
+    theta = m.farg[m.FH] - m.farg[m.twin[m.FH]]
+    c, _ = M.field_smoothest(gpu_ctx, nbr, theta, m.faceArea, O.seeded_init(m.nF, 0))
+    match, sing = _device(gpu_ctx, m, c)
+    fld = O.rosy_from_compressed(c, 4)
+    ref_match, _ = O.c_matching(m, fld, O.compute_connection(m), 4)
+    assert np.array_equal(match, ref_match)
+    host = M.topology_from_field(V, F, c, ratio=ratio, round_seams=rs)
+    assert np.array_equal(sing, host["singular"])
+    assert int(sing.sum()) == 8
+
+
+def test_curl_matching_rejects_open_mesh(gpu_ctx):
+    V, F, _, _ = meshgen.workload("ico2_noise")
+    m = O.Hmesh(V, F)
+    ef = m.edge2face.copy()
+    ef[5, 1] = -1
+    with pytest.raises(M.MetrikoError) as e:
+        M.curl_matching(gpu_ctx, m.pos, m.idx, m.edge2vert, ef, m.vert2half, m.prev, m.angleDefect,
+                        O.seeded_init(m.nF, 0))
+    assert e.value.status == M._lib.BAD_INPUT
