@@ -734,33 +734,39 @@ constexpr int kRing = 12;
 // partials for j < cnt: [Re, Im] of u^H (L V_j) and of V_j^H b
 struct RingPtrs { const double2* V[kRing]; const double2* LV[kRing]; int cnt; };
 
+// One pass over the rows for all C ring vectors (u and b read once); per j the same row order
+// and the same fixed-order block and grid reductions as one pass per vector.
+template <int C>
 __global__ void gram_row(int n, RingPtrs R, const double2* __restrict__ u, const double2* __restrict__ b,
                          double* partials) {
-    for (int j = 0; j < R.cnt; j++) {
-        double red[4] = {0, 0, 0, 0};
-        const double2* Vj = R.V[j];
-        const double2* Lj = R.LV[j];
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-            double2 ui = u[i], li = Lj[i], vi = Vj[i], bi = b[i];
-            red[0] += ui.x * li.x + ui.y * li.y;   // conj(u) * Lv
-            red[1] += ui.x * li.y - ui.y * li.x;
-            red[2] += vi.x * bi.x + vi.y * bi.y;   // conj(v) * b
-            red[3] += vi.x * bi.y - vi.y * bi.x;
+    double red[4 * C];
+#pragma unroll
+    for (int k = 0; k < 4 * C; k++) red[k] = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double2 ui = u[i], bi = b[i];
+#pragma unroll
+        for (int j = 0; j < C; j++) {
+            const double2 li = R.LV[j][i], vi = R.V[j][i];
+            red[4 * j + 0] += ui.x * li.x + ui.y * li.y;   // conj(u) * Lv
+            red[4 * j + 1] += ui.x * li.y - ui.y * li.x;
+            red[4 * j + 2] += vi.x * bi.x + vi.y * bi.y;   // conj(v) * b
+            red[4 * j + 3] += vi.x * bi.y - vi.y * bi.x;
         }
-        double* pj = partials + 4 * j * gridDim.x;
-        publish_partials<double, 4>(red, pj);
     }
+    publish_partials<double, 4 * C>(red, partials);
 }
 
 struct StartCoef { double re[kRing], im[kRing]; const double2* V[kRing]; const double2* LV[kRing]; int cnt; };
 
-// x = V y, r = b - (L V) y, r32 = r, partial |r|^2
+// x = V y, r = b - (L V) y, r32 = r, partial |r|^2 (C ring vectors, unrolled)
+template <int C>
 __global__ void combine_start(int n, StartCoef c, const double2* __restrict__ b, double2* x, double2* r, float2* r32,
                               double* partials) {
     double red[1] = {0};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         double xr = 0, xi = 0, lr = 0, li = 0;
-        for (int j = 0; j < c.cnt; j++) {
+#pragma unroll
+        for (int j = 0; j < C; j++) {
             double2 v = c.V[j][i], l = c.LV[j][i];
             xr += c.re[j] * v.x - c.im[j] * v.y;
             xi += c.re[j] * v.y + c.im[j] * v.x;
@@ -775,6 +781,24 @@ __global__ void combine_start(int n, StartCoef c, const double2* __restrict__ b,
         red[0] += ri.x * ri.x + ri.y * ri.y;
     }
     publish_partials<double, 1>(red, partials);
+}
+
+// the kernels above for a ring count known only at run time (1 .. kRing)
+template <int C = 1>
+void launch_gram(int cnt, int G, cudaStream_t st, int n, const RingPtrs& R, const double2* u, const double2* b,
+                 double* partials) {
+    if constexpr (C < kRing) {
+        if (cnt != C) return launch_gram<C + 1>(cnt, G, st, n, R, u, b, partials);
+    }
+    gram_row<C><<<G, kStream, 0, st>>>(n, R, u, b, partials);
+}
+template <int C = 1>
+void launch_combine(int cnt, int G, cudaStream_t st, int n, const StartCoef& sc, const double2* b, double2* x,
+                    double2* r, float2* r32, double* partials) {
+    if constexpr (C < kRing) {
+        if (cnt != C) return launch_combine<C + 1>(cnt, G, st, n, sc, b, x, r, r32, partials);
+    }
+    combine_start<C><<<G, kStream, 0, st>>>(n, sc, b, x, r, r32, partials);
 }
 
 // K3: x += e (FP32 correction), r = b - L x in FP64, r32 = r, partial |r|^2.
@@ -1537,7 +1561,7 @@ int field_run(mtk_ctx* c, int32_t nF, int32_t nRosy, const int32_t* nbr_h, const
                 R.LV[j] = S.ringL[sj].p;
             }
             R.cnt = cnt;
-            gram_row<<<G, kStream, 0, st>>>(n, R, uk, S.b.p, c->partials);
+            launch_gram(cnt, G, st, n, R, uk, S.b.p, c->partials);
             c->kernels++;
             MTK_TRY(S.finalize(G, 4 * cnt));
             MTK_CUDA_TRY(cudaMemcpyAsync(c->h_scalars + 8, c->scalars, 4 * cnt * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -1565,7 +1589,7 @@ int field_run(mtk_ctx* c, int32_t nF, int32_t nRosy, const int32_t* nbr_h, const
             StartCoef sc{};
             for (int j = 0; j < cnt; j++) { sc.re[j] = yr[j]; sc.im[j] = yi[j]; sc.V[j] = R.V[j]; sc.LV[j] = R.LV[j]; }
             sc.cnt = cnt;
-            combine_start<<<G, kStream, 0, st>>>(n, sc, S.b.p, S.x.p, S.r.p, mixed ? S.r32.p : nullptr, c->partials);
+            launch_combine(cnt, G, st, n, sc, S.b.p, S.x.p, S.r.p, mixed ? S.r32.p : nullptr, c->partials);
             c->kernels++;
             MTK_TRY(S.finalize(G, 1));
             MTK_CUDA_TRY(cudaMemcpyAsync(c->h_scalars + 3, c->scalars, sizeof(double), cudaMemcpyDeviceToHost, st));

@@ -21,14 +21,14 @@
 namespace mtk {
 
 // When a SELL-32 copy pays (measured on the GB300 with the persistent solvers' phase timers, at
-// 1.3M faces): on the phases of levels with at least 100K rows and at most 24 entries per row on
-// average -- the restriction of the IGM free block's first level (38.8 -> 28.0 us per
-// application) and the up-phase of the field's first inner level (28.4 -> 22.3 us), where one
-// lane per row with coalesced entry loads beats the scattered per-thread row walks.  Small levels
-// (fewer rows than the grid has threads) lose lane parallelism and keep CSR; so does the finest
-// IGM level's up-phase (about 7 entries per row: 63 -> 70 us with SELL), which the caller leaves
-// out.
-constexpr double kSellMaxAvg = 24.0;
+// 1.3M faces): on the phases of levels with at least 100K rows and at most 48 entries per row on
+// average -- the restriction of the IGM free block's first level (about 43 entries per row:
+// 39.1 -> 28.1 us per application) and the up-phase of the field's first inner level
+// (28.4 -> 22.3 us), where one lane per row with coalesced entry loads beats the scattered
+// per-thread row walks.  Small levels (fewer rows than the grid has threads) lose lane
+// parallelism and keep CSR; so does the finest IGM level's up-phase (about 7 entries per row:
+// 63 -> 70 us with SELL), which the caller leaves out.
+constexpr double kSellMaxAvg = 48.0;
 constexpr int kSellMinRows = 100000;
 inline bool sell_worth(int n, double avg) { return n >= kSellMinRows && avg <= kSellMaxAvg; }
 
