@@ -124,6 +124,16 @@ def flush_l2(buf):
     buf.add_(1.0)
 
 
+# ncu --set full captures at 1.3M faces (ico8_sh8): DRAM read + write per pass of the FP32 inner
+# solve (iterations + 1 passes per launch)
+NCU_DRAM_PER_PASS = {
+    "igm_pcg": {"bytes": 35.91e9 / 79, "source": "igm_pcg<float>, one 78-iteration launch: 35.91 GB DRAM "
+                                                 "in 14.87 ms (profiles/igm_pcg_f32_ico8_sh8.md)"},
+    "field_pcg": {"bytes": 12.49e9 / 33, "source": "pcg_complex_mg<float>, one 32-iteration launch: 12.49 GB "
+                                                   "DRAM in 6.12 ms (profiles/pcg_complex_mg_f32_ico8_sh8.md)"},
+}
+
+
 def load_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -237,7 +247,13 @@ def run_ours(args):
     d_ms = st.get(f"{dominant}_ms", 0.0)
     d_bytes = st.get(f"{dominant}_bytes", 0.0)
     d_launch = max(1, st.get(f"{dominant}_launches", 1))
+    d_passes = st.get(f"{dominant}_passes", 0)
     achieved = (d_bytes / d_launch) / (d_ms / d_launch * 1e-3) / 1e9 if d_ms > 0 else None
+    # DRAM bytes per pass (one PCG iteration or the start pass) of one ncu --set full capture of
+    # the kernel at 1.3M faces (dram__bytes_read.sum + dram__bytes_write.sum over iterations + 1),
+    # scaled to this run's average launch; measured on the FP32 inner solves
+    ncu_pass = NCU_DRAM_PER_PASS.get(dominant) if args.workload == "ico8_sh8" else None
+    traffic = ncu_pass["bytes"] * d_passes / d_launch if (ncu_pass and d_passes) else None
     nV, nF = len(V), len(F)
     h2d = world * (V.nbytes + F.nbytes)      # every rank copies a mesh of the same size
     d2h = world * (r["cfn"].nbytes + r["fullx"].nbytes + r["singular"].nbytes + r["compressed"].nbytes)
@@ -277,10 +293,10 @@ def run_ours(args):
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1) if achieved else None,
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
-                     "peak_kind": peak_kind, "traffic": None,
-                     "traffic_ncu": ("igm_pcg<float> at 1.3M faces: 429 MB DRAM read+write per PCG iteration "
-                                     "(one 78-iteration launch: 33.9 GB in 19.1 ms), against about 460 MB of "
-                                     "algorithmic bytes per iteration: profiles/igm_pcg_f32_ico8_sh8.md")},
+                     "peak_kind": peak_kind,
+                     "bytes_per_launch": round(d_bytes / d_launch, 1),
+                     "traffic": round(traffic, 1) if traffic else None,
+                     "traffic_source": ncu_pass["source"] if ncu_pass else None},
         "spmv": spmv,
         "clocks": clocks,
         "cpu_baseline": cpu,

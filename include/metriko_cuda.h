@@ -101,6 +101,9 @@ typedef struct {
     int64_t strict_order_differs;
     double strict_order_gap;
     int64_t integral_order_differs;
+    /* passes of the persistent PCG kernels: iterations + 1 per launch (the start pass)      */
+    int64_t field_pcg_passes;
+    int64_t igm_pcg_passes;
 } mtk_stats;
 
 const char* mtk_status_string(int status);

@@ -50,7 +50,8 @@ class Stats(C.Structure):
                 ("field_pcg_ms", C.c_double), ("field_pcg_bytes", C.c_double), ("igm_pcg_launches", C.c_int64),
                 ("igm_pcg_ms", C.c_double), ("igm_pcg_bytes", C.c_double),
                 ("strict_order_differs", C.c_int64), ("strict_order_gap", C.c_double),
-                ("integral_order_differs", C.c_int64)]
+                ("integral_order_differs", C.c_int64), ("field_pcg_passes", C.c_int64),
+                ("igm_pcg_passes", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -182,7 +182,8 @@ inline int aggregate_level(HostLevel& L) {
         }
         na++;
     }
-    // pass 2: attach to the strongest aggregated neighbour
+    // pass 2: attach to the strongest aggregated neighbour (|a|^2 = re^2 + im^2, the first
+    // largest in row order)
     for (int i = 0; i < n; i++) {
         if (L.agg[i] >= 0) continue;
         int best = -1;
@@ -190,7 +191,7 @@ inline int aggregate_level(HostLevel& L) {
         for (int p = A.ptr[i]; p < A.ptr[i + 1]; p++) {
             int j = A.col[p];
             if (j == i || L.agg[j] < 0) continue;
-            double w = std::abs(A.val[p]);
+            double w = std::norm(A.val[p]);
             if (w > bw) { bw = w; best = j; }
         }
         if (best >= 0) { L.agg[i] = L.agg[best]; parent[i] = best; }
@@ -226,7 +227,7 @@ inline int aggregate_level(HostLevel& L) {
                 if (rnd[pv] < 0) continue;
                 std::complex<double> a(0, 0);
                 for (int p = A.ptr[v]; p < A.ptr[v + 1]; p++) if (A.col[p] == pv) { a = A.val[p]; break; }
-                const double m = std::abs(a);
+                const double m = std::sqrt(std::norm(a));
                 t[v] = m > 0 ? -(a / m) * t[pv] : t[pv];
                 rnd_next[v] = r;
                 changed++;

@@ -3,10 +3,12 @@
 //
 // CDevBuilder produces the same level-0 data (aggregates, T, w_p), inner-level cycle operators
 // (R, S, P) and coarse inverse as build_hierarchy(..., first_ops = 1), bit for bit: the
-// aggregation stays on the host; the spectral-radius estimate, P_sa, A P_sa, the Galerkin
-// product and the cycle operators run on the device with explicit round-to-nearest operations
-// in the order of the host's std::complex<double> arithmetic (a * b = (ac - bd, ad + bc), a real
-// factor scales both components, sums start from 0 and follow the host's visit order).
+// aggregation (the greedy passes as rounds of a distance-2 independent-set test, the transport
+// along the parent forest), the spectral-radius estimate, P_sa, A P_sa, the Galerkin product
+// and the cycle operators run on the device with explicit round-to-nearest operations in the
+// order of the host's std::complex<double> arithmetic (a * b = (ac - bd, ad + bc), a real factor
+// scales both components, sums start from 0 and follow the host's visit order); only the
+// coarsest operator comes back to the host, for its dense inverse.
 #pragma once
 #include <chrono>
 #include <complex>
@@ -290,6 +292,131 @@ static __global__ void to_f32_vals(size_t n, const double2* __restrict__ a, floa
         b[i] = make_float2((float)a[i].x, (float)a[i].y);
 }
 
+// ---------------------------------------------------------------- aggregation (aggregate_level)
+// Pass 1 of aggregate_level (rows in index order; a row whose neighbours are all free roots an
+// aggregate with them) is the lexicographically first distance-2 independent set of the row
+// graph.  It is found in rounds: a node whose closed distance-2 neighbourhood holds no root and
+// no lower undecided node becomes a root, a node with a root within distance 2 is covered.  Each
+// round is two passes (distance 1, then distance 2) reading the previous pass's arrays only.
+// state: 0 undecided, 1 root, 2 covered.
+static __global__ void mis_near(int n, const int* __restrict__ Ap, const int* __restrict__ Ac,
+                                const signed char* __restrict__ state, int* low1, unsigned char* root1) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const signed char si = state[i];
+        int lo = si == 0 ? i : 0x7fffffff;
+        unsigned char rt = si == 1;
+        for (int p = Ap[i]; p < Ap[i + 1]; p++) {
+            const int j = Ac[p];
+            if (j == i) continue;
+            const signed char sj = state[j];
+            if (sj == 0 && j < lo) lo = j;
+            if (sj == 1) rt = 1;
+        }
+        low1[i] = lo;
+        root1[i] = rt;
+    }
+}
+static __global__ void mis_decide(int n, const int* __restrict__ Ap, const int* __restrict__ Ac,
+                                  const int* __restrict__ low1, const unsigned char* __restrict__ root1,
+                                  signed char* state, int* undecided) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (state[i] != 0) continue;
+        int lo = low1[i];
+        unsigned char rt = root1[i];
+        for (int p = Ap[i]; p < Ap[i + 1]; p++) {
+            const int j = Ac[p];
+            if (j == i) continue;
+            lo = min(lo, low1[j]);
+            rt |= root1[j];
+        }
+        if (rt) state[i] = 2;
+        else if (lo == i) state[i] = 1;
+        else *undecided = 1;
+    }
+}
+static __global__ void root_flags(int n, const signed char* __restrict__ state, int* flag) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) flag[i] = state[i] == 1;
+}
+// pass 1 assignment: a root and its neighbours (a node has at most one root neighbour)
+static __global__ void agg_pass1(int n, const int* __restrict__ Ap, const int* __restrict__ Ac,
+                                 const signed char* __restrict__ state, const int* __restrict__ rid, int* agg, int* parent) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int a = -1, pa = -1;
+        if (state[i] == 1) {
+            a = rid[i];
+        } else {
+            for (int p = Ap[i]; p < Ap[i + 1]; p++) {
+                const int j = Ac[p];
+                if (j != i && state[j] == 1) { a = rid[j]; pa = j; break; }
+            }
+        }
+        agg[i] = a;
+        parent[i] = pa;
+    }
+}
+// pass 2: a node left over attaches to its strongest neighbour among those aggregated at its
+// turn in index order (pass-1 nodes, and pass-2 nodes of lower index); *err when there is none
+static __global__ void agg_pass2(int n, const int* __restrict__ Ap, const int* __restrict__ Ac,
+                                 const double2* __restrict__ Av, const int* __restrict__ agg1, int* parent, int* err) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (agg1[i] >= 0) continue;
+        int best = -1;
+        double bw = -1.0;
+        for (int p = Ap[i]; p < Ap[i + 1]; p++) {
+            const int j = Ac[p];
+            if (j == i || (agg1[j] < 0 && j > i)) continue;
+            const double2 a = Av[p];
+            const double w = __dadd_rn(__dmul_rn(a.x, a.x), __dmul_rn(a.y, a.y));
+            if (w > bw) { bw = w; best = j; }
+        }
+        parent[i] = best;
+        if (best < 0) *err = 1;
+    }
+}
+// pass-2 aggregates along the parent chains (each step to a lower index or a pass-1 node)
+static __global__ void agg_resolve(int n, const int* __restrict__ parent, const int* __restrict__ prev, int* agg,
+                                   int* changed) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (prev[i] >= 0) continue;
+        const int a = prev[parent[i]];
+        if (a >= 0) { agg[i] = a; *changed = 1; }
+    }
+}
+// transported near-null vector, in rounds of the parent forest: t = 1 at a root,
+// t_v = -(a / |a|) t_parent with a the first entry of row v in the parent's column
+static __global__ void transport_round(int n, int round, const int* __restrict__ Ap, const int* __restrict__ Ac,
+                                       const double2* __restrict__ Av, const int* __restrict__ parent, int* stage,
+                                       double2* t, int* changed) {
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        if (stage[v] >= 0) continue;
+        const int pv = parent[v];
+        if (pv < 0) {
+            t[v] = make_double2(1.0, 0.0);
+            stage[v] = round;
+            *changed = 1;
+            continue;
+        }
+        const int sp = stage[pv];
+        if (sp < 0 || sp >= round) continue;
+        double2 a = make_double2(0.0, 0.0);
+        for (int p = Ap[v]; p < Ap[v + 1]; p++)
+            if (Ac[p] == pv) { a = Av[p]; break; }
+        const double m = __dsqrt_rn(__dadd_rn(__dmul_rn(a.x, a.x), __dmul_rn(a.y, a.y)));
+        t[v] = m > 0 ? cmul_rn(make_double2(-__ddiv_rn(a.x, m), -__ddiv_rn(a.y, m)), t[pv]) : t[pv];
+        stage[v] = round;
+        *changed = 1;
+    }
+}
+static __global__ void agg_count(int n, const int* __restrict__ agg, int* cnt) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) atomicAdd(cnt + agg[i], 1);
+}
+static __global__ void t_scale(int n, const int* __restrict__ agg, const int* __restrict__ cnt, double2* t) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double s = __dsqrt_rn((double)cnt[agg[i]]);
+        t[i] = make_double2(__ddiv_rn(t[i].x, s), __ddiv_rn(t[i].y, s));
+    }
+}
+
 }  // namespace cgpu
 
 // Host driver of the complex device build.  Outputs: level 0 (host: aggregates, members, T, w_p),
@@ -317,29 +444,29 @@ class CDevBuilder {
         MTK_TRY(err_.alloc(1));
         MTK_TRY(err_.zero(st_));
         MTK_TRY(tot_.alloc(1));
-        HostCsr cur = std::move(A0);
         DevCsrC dA;
-        MTK_TRY(upload(cur, dA));
+        MTK_TRY(upload(A0, dA));
+        int cur_n = A0.n;
+        A0 = HostCsr();
         const double omega = kOmega, alpha = kAlpha;
         int levels = 0;
-        while (cur.n > kCoarseMax && levels < kMaxLevels - 1) {
+        while (cur_n > kCoarseMax && levels < kMaxLevels - 1) {
             HostLevel L;
-            L.A = std::move(cur);
-            const int ln = L.A.n;
+            const int ln = cur_n;
             DBuf<double> dinv;
             MTK_TRY(dinv.alloc(ln));
             cgpu::diag_inv<<<grid(ln), kStream, 0, st_>>>(ln, dA.ptr.p, dA.col.p, dA.val.p, dinv.p);
             MTK_TRY(spectral_radius_launch(dA, dinv.p));
-            const int na = aggregate_level(L);   // host, while the power steps run
-            if (na >= L.A.n) return MTK_OK;
             DBuf<int> agg;
             DBuf<double2> T;
-            MTK_TRY(agg.upload(L.agg.data(), ln, st_));
-            MTK_TRY(T.upload(reinterpret_cast<const double2*>(L.T.data()), ln, st_));
+            int na = 0;
+            bool agg_ok = false;
+            MTK_TRY(aggregate_device(dA, agg, T, na, agg_ok));
+            if (!agg_ok || na >= ln) return MTK_OK;
             double rho = 0;
             MTK_TRY(spectral_radius_finish(ln, rho));
             L.wp = rho > 0 ? (4.0 / 3.0) / rho : 0.0;
-            lap("aggregate (host) + rho", levels);
+            lap("aggregate + rho", levels);
             const bool dense = na <= rgpu::kDenseCols;
             if (dense) MTK_TRY(dense_scratch(na));
             DevCsrC Psa, AP, Ph, Ac;
@@ -388,22 +515,30 @@ class CDevBuilder {
             MTK_CUDA_TRY(cudaStreamSynchronize(st_));
             if (herr) return MTK_OK;
             ops.push_back(std::move(O));
-            HostCsr next;
-            MTK_TRY(download(Ac, next));
-            if (levels == 0) {   // level 0 data for the caller
-                L0.agg = std::move(L.agg);
-                L0.T = std::move(L.T);
-                L0.mptr = std::move(L.mptr);
-                L0.mem = std::move(L.mem);
+            if (levels == 0) {   // level 0 data for the caller: aggregates, T, members in row order
+                L0.agg.resize(ln);
+                L0.T.resize(ln);
+                MTK_CUDA_TRY(cudaMemcpyAsync(L0.agg.data(), agg.p, sizeof(int) * ln, cudaMemcpyDeviceToHost, st_));
+                MTK_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<double2*>(L0.T.data()), T.p, sizeof(double2) * ln,
+                                             cudaMemcpyDeviceToHost, st_));
+                MTK_CUDA_TRY(cudaStreamSynchronize(st_));
+                L0.mptr.assign(na + 1, 0);
+                for (int i = 0; i < ln; i++) L0.mptr[L0.agg[i] + 1]++;
+                for (int a = 0; a < na; a++) L0.mptr[a + 1] += L0.mptr[a];
+                L0.mem.resize(ln);
+                std::vector<int> fill(L0.mptr.begin(), L0.mptr.end() - 1);
+                for (int i = 0; i < ln; i++) L0.mem[fill[L0.agg[i]]++] = i;
                 L0.wp = L.wp;
-                L0.A.n = L.A.n;
+                L0.A.n = ln;
             }
             levels++;
-            cur = std::move(next);
+            cur_n = na;
             dA = std::move(Ac);
-            lap("download", levels - 1);
+            lap("level data", levels - 1);
         }
-        if (cur.n > kCoarseMax) return MTK_OK;
+        if (cur_n > kCoarseMax) return MTK_OK;
+        HostCsr cur;
+        MTK_TRY(download(dA, cur));
         nc = cur.n;
         Ainv.assign((size_t)nc * nc, cd(0.0));
         for (int i = 0; i < nc; i++)
@@ -431,6 +566,82 @@ class CDevBuilder {
     int grid(long long n) const {
         const long long g = (n + kStream - 1) / kStream;
         return (int)std::max(1LL, std::min(g, (long long)c_->num_sms * 16));
+    }
+    // aggregate_level on the device (the same aggregates and T): the pass-1 roots by rounds of
+    // the distance-2 independent-set test, pass 2 and the transport by rounds over the parent
+    // forest.  ok = false (the host build takes over) if a row is left without an aggregate.
+    int aggregate_device(const DevCsrC& dA, DBuf<int>& agg, DBuf<double2>& T, int& na, bool& ok) {
+        ok = false;
+        const int n = dA.n;
+        const int g = grid(n);
+        DBuf<signed char> state;
+        DBuf<unsigned char> root1;
+        DBuf<int> low1, flag, rid, parent, prev, stage, cnt, word;
+        MTK_TRY(state.alloc(n));
+        MTK_TRY(root1.alloc(n));
+        MTK_TRY(low1.alloc(n));
+        MTK_TRY(flag.alloc(n));
+        MTK_TRY(rid.alloc(n + 1));
+        MTK_TRY(parent.alloc(n));
+        MTK_TRY(prev.alloc(n));
+        MTK_TRY(stage.alloc(n));
+        MTK_TRY(agg.alloc(n));
+        MTK_TRY(T.alloc(n));
+        MTK_TRY(word.alloc(2));
+        MTK_TRY(state.zero(st_));
+        int h = 0;
+        auto read_word = [&](int& out) -> int {
+            MTK_CUDA_TRY(cudaMemcpyAsync(&out, word.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
+            MTK_CUDA_TRY(cudaStreamSynchronize(st_));
+            return MTK_OK;
+        };
+        // every loop below settles at least one node per round: n + 1 rounds bound them
+        for (int round = 0;; round++) {
+            if (round > n) return MTK_OK;
+            MTK_CUDA_TRY(cudaMemsetAsync(word.p, 0, sizeof(int), st_));
+            cgpu::mis_near<<<g, kStream, 0, st_>>>(n, dA.ptr.p, dA.col.p, state.p, low1.p, root1.p);
+            cgpu::mis_decide<<<g, kStream, 0, st_>>>(n, dA.ptr.p, dA.col.p, low1.p, root1.p, state.p, word.p);
+            c_->kernels += 2;
+            MTK_TRY(read_word(h));
+            if (!h) break;
+        }
+        cgpu::root_flags<<<g, kStream, 0, st_>>>(n, state.p, flag.p);
+        size_t total = 0;
+        MTK_TRY(scan(n, flag.p, rid.p, total));
+        na = (int)total;
+        cgpu::agg_pass1<<<g, kStream, 0, st_>>>(n, dA.ptr.p, dA.col.p, state.p, rid.p, agg.p, parent.p);
+        MTK_CUDA_TRY(cudaMemsetAsync(word.p, 0, sizeof(int), st_));
+        cgpu::agg_pass2<<<g, kStream, 0, st_>>>(n, dA.ptr.p, dA.col.p, dA.val.p, agg.p, parent.p, word.p);
+        c_->kernels += 3;
+        MTK_TRY(read_word(h));
+        if (h) return MTK_OK;
+        for (int round = 0;; round++) {
+            if (round > n) return MTK_OK;
+            MTK_CUDA_TRY(cudaMemcpyAsync(prev.p, agg.p, sizeof(int) * n, cudaMemcpyDeviceToDevice, st_));
+            MTK_CUDA_TRY(cudaMemsetAsync(word.p, 0, sizeof(int), st_));
+            cgpu::agg_resolve<<<g, kStream, 0, st_>>>(n, parent.p, prev.p, agg.p, word.p);
+            c_->kernels++;
+            MTK_TRY(read_word(h));
+            if (!h) break;
+        }
+        MTK_CUDA_TRY(cudaMemsetAsync(stage.p, 0xff, sizeof(int) * n, st_));
+        for (int round = 0;; round++) {
+            if (round > n) return MTK_OK;
+            MTK_CUDA_TRY(cudaMemsetAsync(word.p, 0, sizeof(int), st_));
+            cgpu::transport_round<<<g, kStream, 0, st_>>>(n, round, dA.ptr.p, dA.col.p, dA.val.p, parent.p, stage.p, T.p,
+                                                          word.p);
+            c_->kernels++;
+            MTK_TRY(read_word(h));
+            if (!h) break;
+        }
+        MTK_TRY(cnt.alloc(std::max(na, 1)));
+        MTK_TRY(cnt.zero(st_));
+        cgpu::agg_count<<<g, kStream, 0, st_>>>(n, agg.p, cnt.p);
+        cgpu::t_scale<<<g, kStream, 0, st_>>>(n, agg.p, cnt.p, T.p);
+        c_->kernels += 2;
+        MTK_CUDA_TRY(cudaGetLastError());
+        ok = true;
+        return MTK_OK;
     }
     int dense_scratch(int ncols) {
         if (ncols <= dense_cols_) return MTK_OK;

@@ -1035,7 +1035,7 @@ struct FieldSolver {
     DBuf<float2> v32, r32, e32, z32, p32, q32;
     int grid = 0;
     double pcg_ms = 0, pcg_bytes = 0;
-    long long pcg_launches = 0;
+    long long pcg_launches = 0, pcg_passes = 0;
     // multigrid hierarchy (host-built, device-resident), both precisions
     struct CsrBufs {
         DBuf<int> ptr, col;
@@ -1336,6 +1336,7 @@ struct FieldSolver {
                                    : ell + T_ + 4.0 * T_ + 18.0 * T_ + 3.0 * T_;
         const double cyc = amg ? (sizeof(T) == 8 ? vcycle_bytes64 : vcycle_bytes32) : 0.0;
         pcg_bytes += (per_row * (double)n + cyc) * (double)(c->h_int[1] + 1);
+        pcg_passes += c->h_int[1] + 1;
         *iters += c->h_int[1];
         if (final_rr) *final_rr = reinterpret_cast<double*>(c->h_int + 4)[0];
         int st = c->h_int[0];
@@ -1696,6 +1697,7 @@ int field_run(mtk_ctx* c, int32_t nF, int32_t nRosy, const int32_t* nbr_h, const
         if (worst > stats->max_rel_residual) stats->max_rel_residual = worst;
         stats->ms_field += ms;
         stats->field_pcg_launches += S.pcg_launches;
+        stats->field_pcg_passes += S.pcg_passes;
         stats->field_pcg_ms += S.pcg_ms;
         stats->field_pcg_bytes += S.pcg_bytes;
         stats->kernel_launches = c->kernels;

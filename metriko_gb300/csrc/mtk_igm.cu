@@ -1144,7 +1144,7 @@ struct Igm {
     int kq = 0;
     size_t smem64 = 0, smem32 = 0;
     double pcg_ms = 0, pcg_bytes = 0;
-    long long pcg_launches = 0;
+    long long pcg_launches = 0, pcg_passes = 0;
     long long nnzW = 0, nnzS = 0, nnzYT = 0;
     // multigrid on the free block (host-built)
     struct RCsrBufs {
@@ -1411,6 +1411,7 @@ struct Igm {
         pcg_bytes += (iter_bytes(sizeof(T)) + (Hp ? (sizeof(T) == 8 ? mg_bytes64 : mg_bytes32) : 0.0) +
                       (phiP ? 4.0 * nZ * (double)nY : 0.0)) *
                      (double)(c->h_int[1] + 1);
+        pcg_passes += c->h_int[1] + 1;
         if (iters) *iters += c->h_int[1];
         if (rr_out) *rr_out = reinterpret_cast<double*>(c->h_int + 4)[0];
         int s = c->h_int[0];
@@ -2246,6 +2247,7 @@ int igm_run(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts_in, do
         cudaEventElapsedTime(&msj, c->ev_a, c->ev_b);
         stt->ms_integrate += msj;
         stt->igm_pcg_launches += S.pcg_launches;
+        stt->igm_pcg_passes += S.pcg_passes;
         stt->igm_pcg_ms += S.pcg_ms;
         stt->igm_pcg_bytes += S.pcg_bytes;
         expand_full<<<G, kStream, 0, st>>>(nFull, S.d_full2y.p, S.d_full2j.p, nY, nZ, S.Us.p, S.xs.p, S.Xfull.p);
@@ -2273,6 +2275,7 @@ int igm_run(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts_in, do
     int nfix = 0;
     auto finish = [&](const double* xsrc) -> int {
         stt->igm_pcg_launches += S.pcg_launches;
+        stt->igm_pcg_passes += S.pcg_passes;
         stt->igm_pcg_ms += S.pcg_ms;
         stt->igm_pcg_bytes += S.pcg_bytes;
         expand_full<<<G, kStream, 0, st>>>(nFull, S.d_full2y.p, S.d_full2j.p, nY, nZ, S.Us.p, xsrc, S.Xfull.p);
