@@ -345,6 +345,22 @@ int mtk_face_geometry_backward(mtk_ctx* ctx, int32_t nV, int32_t nF, const doubl
                                const double* g_gy, double* grad_V);
 
 /*
+ * The inputs of mtk_field_smoothest computed on the device from the raw closed mesh (V[3 nV],
+ * F[3 nF]) without the halfedge mesh: nbr[3 nF] the face across side j of face f (the side from
+ * F(f, j) to F(f, j+1)), theta[3 nF] = heArgOnFace(h) - heArgOnFace(twin h) and area[nF]
+ * (include/metriko/core/hmesh/hmesh.h:313-489 of the reference: the constructor's pairing, face
+ * frames and halfedge angles).  The same values as mtk_field_inputs (the halfedge mesh on the
+ * host), theta up to the last-bit rounding of acos.  A boundary or non-manifold edge, faces of
+ * opposite orientation or a side with equal end points -> MTK_ERR_BAD_INPUT.
+ */
+int mtk_mesh_field_inputs(mtk_ctx* ctx, int32_t nV, int32_t nF, const double* V, const int32_t* F, int32_t* nbr,
+                          double* theta, double* area);
+/* mtk_mesh_field_inputs followed by mtk_field_smoothest (same remaining arguments and outputs). */
+int mtk_field_smoothest_mesh(mtk_ctx* ctx, int32_t nV, int32_t nF, const double* V, const int32_t* F, int32_t nRosy,
+                             const double* x0, int32_t n_iter, const mtk_solve_opts* opts, double* out,
+                             mtk_stats* stats);
+
+/*
  * Curl matching and singular indices on the device, for a closed mesh: computeConnection,
  * cMatching and computeSingular of FaceRosyField::computeMatching(MatchingType::Curl)
  * (include/metriko/core/vectorfield/face_rosy_field.h:100-135, :169-202), one thread per edge and

@@ -7,5 +7,6 @@ Python here is plumbing for tests and benchmarks: `Context`, `pipeline`, `field_
 from ._lib import (Context, MetrikoError, PREC_FP64, PREC_MIXED, field_smoothest, lib,  # noqa: F401
                    field_inputs, field_solve, injective_barrier, local_injectivity, map_deviation, mesh_geometry, pipeline, seeded_init,
                    size_field_gradient, solve_opts, spmv_bench, topology_from_field, position_gradient,
-                   face_geometry_backward, CsrMatrix, csr_smallest_eig, curl_matching)
+                   face_geometry_backward, CsrMatrix, csr_smallest_eig, curl_matching, mesh_field_inputs,
+                   field_smoothest_mesh)
 from . import meshgen  # noqa: F401

@@ -25,7 +25,7 @@ EXPORTS = [
     "mtk_injective_barrier", "mtk_local_injectivity", "mtk_map_deviation",
     "mtk_mesh_geometry", "mtk_ctx_set_wait_limit", "mtk_pipeline_position_gradient", "mtk_size_field_position_partials",
     "mtk_field_power_adjoint", "mtk_face_geometry_backward", "mtk_csr_create", "mtk_csr_destroy", "mtk_csr_pcg",
-    "mtk_csr_smallest_eig", "mtk_curl_matching",
+    "mtk_csr_smallest_eig", "mtk_curl_matching", "mtk_mesh_field_inputs", "mtk_field_smoothest_mesh",
 ]
 
 
@@ -128,6 +128,10 @@ def lib():
         L.mtk_csr_smallest_eig.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
                                            C.POINTER(SolveOpts), C.c_void_p, C.POINTER(Stats)]
         L.mtk_curl_matching.argtypes = [C.c_void_p] + [C.c_int32] * 4 + [C.c_void_p] * 10
+        L.mtk_mesh_field_inputs.argtypes = [C.c_void_p, C.c_int32, C.c_int32] + [C.c_void_p] * 5
+        L.mtk_field_smoothest_mesh.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
+                                               C.c_void_p, C.c_int32, C.POINTER(SolveOpts), C.c_void_p,
+                                               C.POINTER(Stats)]
         _lib = L
     return _lib
 
@@ -416,6 +420,34 @@ def face_geometry_backward(ctx: Context, V, F, g_area, g_farg1, g_farg2, g_gx, g
                                             _ptr(out)),
            "mtk_face_geometry_backward")
     return out
+
+
+def mesh_field_inputs(ctx: Context, V, F):
+    """mtk_mesh_field_inputs: (nbr[nF, 3], theta[nF, 3], area[nF]) computed on the device."""
+    V = np.ascontiguousarray(V, np.float64)
+    F = np.ascontiguousarray(F, np.int32)
+    nF = len(F)
+    nbr = np.zeros((nF, 3), np.int32)
+    theta = np.zeros((nF, 3))
+    area = np.zeros(nF)
+    _check(lib().mtk_mesh_field_inputs(ctx.handle, len(V), nF, _ptr(V), _ptr(F), _ptr(nbr), _ptr(theta), _ptr(area)),
+           "mtk_mesh_field_inputs")
+    return nbr, theta, area
+
+
+def field_smoothest_mesh(ctx: Context, V, F, x0, n_rosy=4, n_iter=50, opts=None):
+    """mtk_field_smoothest_mesh: the smoothest field from the raw mesh (inputs on the device)."""
+    V = np.ascontiguousarray(V, np.float64)
+    F = np.ascontiguousarray(F, np.int32)
+    nF = len(F)
+    x = np.empty(2 * nF)
+    x[0::2], x[1::2] = np.real(x0), np.imag(x0)
+    out = np.empty(2 * nF)
+    st = Stats()
+    o = opts if opts is not None else solve_opts()
+    _check(lib().mtk_field_smoothest_mesh(ctx.handle, len(V), nF, _ptr(V), _ptr(F), n_rosy, _ptr(x), n_iter, C.byref(o),
+                                          _ptr(out), C.byref(st)), "mtk_field_smoothest_mesh")
+    return out[0::2] + 1j * out[1::2], st.as_dict()
 
 
 def curl_matching(ctx: Context, V, F, edge_vert, edge_face, vert_half, prev_half, angle_defect, compressed, N=4):

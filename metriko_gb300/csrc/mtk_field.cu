@@ -728,8 +728,11 @@ __global__ void finalize_partials(const double* partials, int nb, int K, double*
 // Subspace warm start.  The inverse iterates on a sphere stay inside a nearly degenerate
 // cluster of eigenvectors, so the previous m iterates span the solution well: the start of
 // each solve is the Galerkin solution of L x = b on V = [u_k, ..., u_{k-m+1}] (L V is kept
-// from power_prepare, so no extra operator applications).
-constexpr int kRing = 12;
+// from power_prepare, so no extra operator applications).  m = 6: at 1.3M faces the field stage
+// took 535 / 505 / 502 / 496 ms with m = 12 / 8 / 6 / 4 (2284 / 2235 / 2257 / 2287 PCG passes):
+// the Gram row and the start combination cost 4 complex FP64 multiply-adds per vector and row,
+// which the GB300's FP64 rate makes the larger term beyond six vectors.
+constexpr int kRing = 6;
 
 // partials for j < cnt: [Re, Im] of u^H (L V_j) and of V_j^H b
 struct RingPtrs { const double2* V[kRing]; const double2* LV[kRing]; int cnt; };

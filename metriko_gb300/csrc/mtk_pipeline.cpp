@@ -20,9 +20,9 @@ using namespace metriko;
 namespace {
 // Host work that runs beside the GPU field solve uses a quarter of the cores for its parallel
 // loops, so that the field's own host steps keep most of them (per-thread OpenMP setting).
-void side_thread_cores() {
+void side_thread_cores(int share = 4) {
 #if defined(_OPENMP)
-    omp_set_num_threads(std::max(1, omp_get_num_procs() / 4));
+    omp_set_num_threads(std::max(1, omp_get_num_procs() / share));
 #endif
 }
 }
@@ -62,22 +62,56 @@ extern "C" int mtk_pipeline_run(mtk_ctx* ctx, int32_t nV, int32_t nF, const doub
         MatXi F(nF, 3);
         std::memcpy(V.data(), Vb, sizeof(double) * 3 * size_t(nV));
         std::memcpy(F.data(), Fb, sizeof(int32_t) * 3 * size_t(nF));
-        auto mesh = std::make_unique<Hmesh>(V, F, Hmesh::Deferred{});
-        lap(ts);
-        stamp("hmesh", ts2);
-        // while the GPU solves the field, a host thread completes the mesh (element lists, angle
-        // defects: neither is read by the field solve) and computes the field-independent part of
-        // the seam search
         const bool seams = popts->stop_after != 1;
-        auto pending = std::async(std::launch::async, [&m = *mesh, seams] {
-            side_thread_cores();
-            m.finish();
-            return seams ? seam_base(m) : SeamBase{};
-        });
-        FaceRosyField rawf(*mesh, 4, popts->field_type == 1 ? FieldType::CurvatureAligned : FieldType::Smoothest);
-        stamp("field (gpu)", ts2);
-        ts = clk::now();
-        SeamBase base = pending.get();
+        std::unique_ptr<Hmesh> mesh;
+        std::unique_ptr<FaceRosyField> rawfp;
+        SeamBase base;
+        if (popts->field_type != 1) {
+            // the smoothest field needs only the face pairing, the halfedge angles and the areas:
+            // computed on the device from V and F (mtk_field_smoothest_mesh), so a host thread
+            // builds the whole halfedge mesh and the field-independent part of the seam search
+            // while the GPU solves
+            auto built = std::async(std::launch::async, [&V, &F, seams] {
+                side_thread_cores(2);
+                auto m = std::make_unique<Hmesh>(V, F, Hmesh::Deferred{});
+                m->finish();
+                SeamBase b = seams ? seam_base(*m) : SeamBase{};
+                return std::make_pair(std::move(m), std::move(b));
+            });
+            std::vector<double> x0(2 * size_t(nF)), cfield(2 * size_t(nF));
+            mtk_seeded_init(nF, gpu::options().seed, x0.data());
+            const int fs = mtk_field_smoothest_mesh(ctx, nV, nF, Vb, Fb, 4, x0.data(), gpu::options().n_iter,
+                                                    &gpu::options().solve, cfield.data(), &gpu::stats());
+            ts = clk::now();
+            auto pr = built.get();   // a wait here (the mesh outlasting the field) is host time
+            lap(ts);
+            gpu::check(fs, "mtk_field_smoothest_mesh");
+            mesh = std::move(pr.first);
+            base = std::move(pr.second);
+            rawfp = std::make_unique<FaceRosyField>(*mesh, 4);
+            rawfp->compressed = VecXc(nF);
+            for (int f = 0; f < nF; f++) rawfp->compressed[f] = complex(cfield[2 * f], cfield[2 * f + 1]);
+            rawfp->set_field_from_compressed();
+            lap(ts);
+            stamp("field (gpu) + hmesh", ts2);
+        } else {
+            mesh = std::make_unique<Hmesh>(V, F, Hmesh::Deferred{});
+            lap(ts);
+            stamp("hmesh", ts2);
+            // while the GPU solves the field, a host thread completes the mesh (element lists,
+            // angle defects: neither is read by the field solve) and computes the field-independent
+            // part of the seam search
+            auto pending = std::async(std::launch::async, [&m = *mesh, seams] {
+                side_thread_cores();
+                m.finish();
+                return seams ? seam_base(m) : SeamBase{};
+            });
+            rawfp = std::make_unique<FaceRosyField>(*mesh, 4, FieldType::CurvatureAligned);
+            stamp("field (gpu)", ts2);
+            ts = clk::now();
+            base = pending.get();
+        }
+        FaceRosyField& rawf = *rawfp;
         rawf.computeMatching(MatchingType::Curl);
         stamp("matching+singular", ts2);
         if (compressed)

@@ -17,6 +17,15 @@
 // cos/sin/atan2/sqrt; the integer decisions are the host's (tested on every fixture and at the
 // 1.3M-face benchmark size).  A ring that does not close within kMaxRing halfedges sets the error
 // word and leaves that vertex's index at 0 (the call then fails with MTK_ERR_BAD_INPUT).
+//
+// Field inputs from the raw mesh on the device (mtk_mesh_field_inputs, mtk_field_smoothest_mesh):
+// the face across each face side, theta = heArgOnFace(h) - heArgOnFace(twin h) and the face
+// areas of the Hmesh constructor (hmesh.h:313-489) without building the halfedge mesh.  The face
+// sides are paired through a hash table keyed by their sorted vertex pair; the face frames and
+// halfedge angles repeat the host's arithmetic in its order (no contraction into fused
+// multiply-adds), so area and the pairing are the host's bit for bit and theta differs from it
+// only by the last-bit rounding of acos.  The pipeline entry point starts the field solve from
+// these while a host thread builds the halfedge mesh.
 #include <cmath>
 #include <vector>
 
@@ -133,7 +142,171 @@ __global__ void singular_index(int nV, int N, const int* __restrict__ vert_half,
     }
 }
 
+// ------------------------------------------------------------------ field inputs from V, F
+constexpr unsigned long long kEmpty = ~0ull;
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long k) {
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdull;
+    k ^= k >> 33;
+    k *= 0xc4ceb9fe1a85ec53ull;
+    k ^= k >> 33;
+    return k;
+}
+
+// each face side (f, j) from F(f, j) to F(f, j+1) into the table keyed by its sorted vertex pair;
+// the first two sides of a key fill its two slots, a third sets err bit 1 (non-manifold edge)
+__global__ void sides_insert(int nF, const int* __restrict__ F, unsigned long long mask, unsigned long long* keys,
+                             int* s0, int* s1, int* err) {
+    const int ns = 3 * nF;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
+        const int f = s / 3, j = s - 3 * f;
+        const int a = F[3 * (size_t)f + j], b = F[3 * (size_t)f + (j + 1) % 3];
+        if (a == b) { atomicOr(err, 8); continue; }
+        const unsigned long long key = ((unsigned long long)min(a, b) << 32) | (unsigned long long)max(a, b);
+        unsigned long long h = mix64(key) & mask;
+        for (unsigned long long probe = 0; probe <= mask; probe++) {
+            const unsigned long long prev = atomicCAS(keys + h, kEmpty, key);
+            if (prev == kEmpty || prev == key) {
+                if (atomicCAS(s0 + h, -1, s) != -1 && atomicCAS(s1 + h, -1, s) != -1) atomicOr(err, 1);
+                break;
+            }
+            h = (h + 1) & mask;
+        }
+    }
+}
+
+// partner side of every side; err bit 2: an edge with one side (boundary), bit 4: two sides
+// running the same way (inconsistent orientation)
+__global__ void sides_pair(unsigned long long nslot, const int* __restrict__ F, const unsigned long long* __restrict__ keys,
+                           const int* __restrict__ s0, const int* __restrict__ s1, int* partner, int* err) {
+    for (unsigned long long h = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; h < nslot;
+         h += (unsigned long long)gridDim.x * blockDim.x) {
+        if (keys[h] == kEmpty) continue;
+        const int a = s0[h], b = s1[h];
+        if (b < 0) { atomicOr(err, 2); continue; }
+        const int fa = a / 3, ja = a - 3 * fa, fb = b / 3, jb = b - 3 * fb;
+        const int ta = F[3 * (size_t)fa + ja], tb = F[3 * (size_t)fb + jb];
+        if (ta == tb) atomicOr(err, 4);
+        partner[a] = b;
+        partner[b] = a;
+    }
+}
+
+__device__ __forceinline__ double sq_rn(V3 a) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(a.x, a.x), __dmul_rn(a.y, a.y)), __dmul_rn(a.z, a.z));
+}
+__device__ __forceinline__ double dot_rn(V3 a, V3 b) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(a.x, b.x), __dmul_rn(a.y, b.y)), __dmul_rn(a.z, b.z));
+}
+__device__ __forceinline__ V3 sub_rn(V3 a, V3 b) { return {__dsub_rn(a.x, b.x), __dsub_rn(a.y, b.y), __dsub_rn(a.z, b.z)}; }
+__device__ __forceinline__ V3 unit_rn(V3 a) {   // Row3d::normalized
+    const double n = sq_rn(a);
+    if (!(n > 0)) return a;
+    const double r = __dsqrt_rn(n);
+    return {__ddiv_rn(a.x, r), __ddiv_rn(a.y, r), __ddiv_rn(a.z, r)};
+}
+
+// per face: heArgOnFace of its three sides (hmesh.h:480-489) and its area (hmesh.h:461-474)
+__global__ void face_angles(int nF, const double* __restrict__ P, const int* __restrict__ F, double* farg, double* area) {
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nF; f += gridDim.x * blockDim.x) {
+        const V3 p0 = vload(P, F[3 * (size_t)f]), p1 = vload(P, F[3 * (size_t)f + 1]), p2 = vload(P, F[3 * (size_t)f + 2]);
+        const V3 x = sub_rn(p1, p0);
+        const V3 dm = sub_rn(p0, p2);
+        const V3 t{__dmul_rn(dm.x, -1.0), __dmul_rn(dm.y, -1.0), __dmul_rn(dm.z, -1.0)};
+        const V3 n{__dsub_rn(__dmul_rn(x.y, t.z), __dmul_rn(x.z, t.y)), __dsub_rn(__dmul_rn(x.z, t.x), __dmul_rn(x.x, t.z)),
+                   __dsub_rn(__dmul_rn(x.x, t.y), __dmul_rn(x.y, t.x))};
+        area[f] = __dmul_rn(__dsqrt_rn(sq_rn(n)), 0.5);
+        const V3 bx = unit_rn(x);
+        const V3 e[3] = {unit_rn(sub_rn(p1, p0)), unit_rn(sub_rn(p2, p1)), unit_rn(sub_rn(p0, p2))};
+        double sum = 0.0;
+        for (int j = 0; j < 3; j++) {
+            const V3 v1 = e[j], v2 = e[(j + 2) % 3];
+            if (__dsqrt_rn(sq_rn(sub_rn(v1, bx))) > 1e-10) sum = __dadd_rn(sum, acos(dot_rn(v1, v2)));
+            farg[3 * (size_t)f + j] = sum;
+        }
+    }
+}
+
+__global__ void side_outputs(int nF, const int* __restrict__ partner, const double* __restrict__ farg, int* nbr,
+                             double* theta) {
+    const int ns = 3 * nF;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
+        const int t = partner[s];
+        nbr[s] = t / 3;
+        theta[s] = __dsub_rn(farg[s], farg[t]);
+    }
+}
+
 }  // namespace
+
+extern "C" int mtk_mesh_field_inputs(mtk_ctx* c, int32_t nV, int32_t nF, const double* V, const int32_t* F, int32_t* nbr,
+                                     double* theta, double* area) {
+    if (!c || nV <= 0 || nF <= 0 || !V || !F || !nbr || !theta || !area) return MTK_ERR_BAD_INPUT;
+    if (nF > (1 << 29)) return MTK_ERR_BAD_INPUT;
+    for (int64_t i = 0; i < 3 * (int64_t)nF; i++)
+        if (F[i] < 0 || F[i] >= nV) {
+            mtk_set_last_error("mtk_mesh_field_inputs: face corner out of range", __FILE__, __LINE__);
+            return MTK_ERR_BAD_INPUT;
+        }
+    MTK_CUDA_TRY(cudaSetDevice(c->device));
+    AllocStreamScope alloc_scope(c->stream);
+    cudaStream_t st = c->stream;
+    const size_t ns = 3 * (size_t)nF;
+    size_t nslot = 1;
+    while (nslot < ns) nslot <<= 1;   // at most half full: a key takes one slot for two sides
+    DBuf<double> dV, dfarg, darea, dtheta;
+    DBuf<int> dF, ds0, ds1, dpart, dnbr;
+    DBuf<unsigned long long> dkeys;
+    MTK_TRY(dV.upload(V, 3 * (size_t)nV, st));
+    MTK_TRY(dF.upload(F, ns, st));
+    MTK_TRY(dkeys.alloc(nslot));
+    MTK_TRY(ds0.alloc(nslot));
+    MTK_TRY(ds1.alloc(nslot));
+    MTK_TRY(dpart.alloc(ns));
+    MTK_TRY(dfarg.alloc(ns));
+    MTK_TRY(darea.alloc(nF));
+    MTK_TRY(dnbr.alloc(ns));
+    MTK_TRY(dtheta.alloc(ns));
+    MTK_CUDA_TRY(cudaMemsetAsync(dkeys.p, 0xff, sizeof(unsigned long long) * nslot, st));
+    MTK_CUDA_TRY(cudaMemsetAsync(ds0.p, 0xff, sizeof(int) * nslot, st));
+    MTK_CUDA_TRY(cudaMemsetAsync(ds1.p, 0xff, sizeof(int) * nslot, st));
+    MTK_CUDA_TRY(cudaMemsetAsync(dpart.p, 0xff, sizeof(int) * ns, st));
+    MTK_CUDA_TRY(cudaMemsetAsync(c->dev_err, 0, sizeof(int), st));
+    const int G = stream_grid(c) * 4;
+    sides_insert<<<G, kStream, 0, st>>>(nF, dF.p, (unsigned long long)(nslot - 1), dkeys.p, ds0.p, ds1.p, c->dev_err);
+    sides_pair<<<G, kStream, 0, st>>>((unsigned long long)nslot, dF.p, dkeys.p, ds0.p, ds1.p, dpart.p, c->dev_err);
+    face_angles<<<G, kStream, 0, st>>>(nF, dV.p, dF.p, dfarg.p, darea.p);
+    MTK_CUDA_TRY(cudaMemcpyAsync(c->h_int, c->dev_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    MTK_CUDA_TRY(cudaStreamSynchronize(st));
+    c->kernels += 3;
+    if (const int e = c->h_int[0]) {
+        mtk_set_last_error(e & 2   ? "mtk_mesh_field_inputs: boundary edge (closed meshes only)"
+                           : e & 1 ? "mtk_mesh_field_inputs: non-manifold edge (three or more faces)"
+                           : e & 4 ? "mtk_mesh_field_inputs: inconsistently oriented faces"
+                                   : "mtk_mesh_field_inputs: degenerate face side",
+                           __FILE__, __LINE__);
+        return MTK_ERR_BAD_INPUT;
+    }
+    side_outputs<<<G, kStream, 0, st>>>(nF, dpart.p, dfarg.p, dnbr.p, dtheta.p);
+    c->kernels++;
+    MTK_CUDA_TRY(cudaGetLastError());
+    MTK_CUDA_TRY(cudaMemcpyAsync(nbr, dnbr.p, sizeof(int) * ns, cudaMemcpyDeviceToHost, st));
+    MTK_CUDA_TRY(cudaMemcpyAsync(theta, dtheta.p, sizeof(double) * ns, cudaMemcpyDeviceToHost, st));
+    MTK_CUDA_TRY(cudaMemcpyAsync(area, darea.p, sizeof(double) * nF, cudaMemcpyDeviceToHost, st));
+    MTK_CUDA_TRY(cudaStreamSynchronize(st));
+    return MTK_OK;
+}
+
+extern "C" int mtk_field_smoothest_mesh(mtk_ctx* c, int32_t nV, int32_t nF, const double* V, const int32_t* F,
+                                        int32_t nRosy, const double* x0, int32_t n_iter, const mtk_solve_opts* opts,
+                                        double* out, mtk_stats* stats) {
+    if (!c || nF <= 0 || !x0 || !out) return MTK_ERR_BAD_INPUT;
+    std::vector<int32_t> nbr(3 * (size_t)nF);
+    std::vector<double> theta(3 * (size_t)nF), area(nF);
+    MTK_TRY(mtk_mesh_field_inputs(c, nV, nF, V, F, nbr.data(), theta.data(), area.data()));
+    return mtk_field_smoothest(c, nF, nRosy, nbr.data(), theta.data(), area.data(), x0, n_iter, opts, out, stats);
+}
 
 extern "C" int mtk_curl_matching(mtk_ctx* c, int32_t nV, int32_t nF, int32_t nE, int32_t N, const double* V,
                                  const int32_t* F, const int32_t* edge_vert, const int32_t* edge_face,

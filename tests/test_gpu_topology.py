@@ -91,3 +91,42 @@ def test_curl_matching_rejects_open_mesh(gpu_ctx):
         M.curl_matching(gpu_ctx, m.pos, m.idx, m.edge2vert, ef, m.vert2half, m.prev, m.angleDefect,
                         O.seeded_init(m.nF, 0))
     assert e.value.status == M._lib.BAD_INPUT
+
+
+@pytest.mark.parametrize("name", ["ico3_noise", "torus_64x32", "ico6_sh8"])
+def test_mesh_field_inputs_match_host(gpu_ctx, name):
+    """Face pairing, halfedge-angle differences and areas from the raw mesh on the device equal
+    the halfedge mesh's on the host: pairing and areas bit for bit, theta to the rounding of acos."""
+    V, F, _, _ = meshgen.workload(name)
+    nbr_h, theta_h, area_h = M.field_inputs(V, F)
+    nbr_d, theta_d, area_d = M.mesh_field_inputs(gpu_ctx, V, F)
+    assert np.array_equal(nbr_d.reshape(-1), np.asarray(nbr_h).reshape(-1))
+    assert np.array_equal(area_d, np.asarray(area_h))
+    assert np.abs(theta_d.reshape(-1) - np.asarray(theta_h).reshape(-1)).max() <= 1e-13
+
+
+def test_field_smoothest_mesh_matches_face_graph_entry(gpu_ctx):
+    V, F, _, _ = meshgen.workload("ico4_noise")
+    nbr, theta, area = M.field_inputs(V, F)
+    x0 = O.seeded_init(len(F), 0)
+    opts = M.solve_opts("mixed", tol=1e-10)
+    a, _ = M.field_smoothest(gpu_ctx, nbr, theta, area, x0, opts=opts)
+    b, _ = M.field_smoothest_mesh(gpu_ctx, V, F, x0, opts=opts)
+    assert np.abs(np.angle(a / b)).max() / 4 < 1e-7
+
+
+@pytest.mark.parametrize("case", ["boundary", "flipped", "duplicate", "degenerate"])
+def test_mesh_field_inputs_rejects(gpu_ctx, case):
+    V, F, _, _ = meshgen.workload("ico2_noise")
+    F = np.array(F, np.int32)
+    if case == "boundary":
+        F = F[1:]
+    elif case == "flipped":
+        F[3] = F[3, ::-1]
+    elif case == "duplicate":
+        F = np.vstack([F, F[:1]])
+    else:
+        F[5, 1] = F[5, 0]
+    with pytest.raises(M.MetrikoError) as e:
+        M.mesh_field_inputs(gpu_ctx, V, F)
+    assert e.value.status == M._lib.BAD_INPUT
