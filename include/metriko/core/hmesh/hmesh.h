@@ -7,15 +7,23 @@
 // metriko-gb300: halfedge mesh (DCEL) with the reference's numbering.
 //
 // Replaces metriko include/metriko/core/hmesh/hmesh.h:24-569 (struct Hmesh, handles, dcel()).
-// Only closed, consistently oriented, edge-manifold triangle meshes are accepted (the
-// workloads of this path); anything else throws std::invalid_argument.
+// Consistently oriented, edge-manifold triangle meshes, closed or with boundary loops, are
+// accepted; anything else throws std::invalid_argument.
 //
 // Numbering follows the reference exactly, because every later integer decision depends on it:
 //  * edges: libigl v2.5.0 edge_topology -- entries (min v, max v, face, corner) sorted
 //    lexicographically, one edge per distinct (min, max); edge2face(e,0) is the face in which
-//    the edge runs min->max (restated from libigl's documented behaviour);
-//  * halfedge 2e starts at edge2vert(e,0) inside edge2face(e,0), 2e+1 is its twin;
-//  * vert2half[v] is the last halfedge written for v in edge order (hmesh.h:240-311, :377);
+//    the edge runs min->max, -1 on the side of a boundary edge that has no face (restated from
+//    libigl's documented behaviour);
+//  * interior halfedges are numbered in edge order, slot 0 (tail edge2vert(e,0), face
+//    edge2face(e,0)) before slot 1, skipping a slot without a face (dcel, hmesh.h:254-258): a
+//    closed mesh has 2e and its twin 2e+1;
+//  * boundary halfedges (face -1) follow from 3 nF on, loop by loop (hmesh.h:393-418): loops in
+//    the order of their first interior halfedge without a twin, each walked backwards along the
+//    interior halfedges it borders; loop2half[l] is the loop's first boundary halfedge;
+//  * vert2half[v] is the last interior halfedge written for v in edge order (hmesh.h:268-279,
+//    :377); edge2half[e] is the slot-0 halfedge, or the boundary halfedge when slot 0 has no face
+//    (:420-421);
 //  * face2half[f] runs F(f,0)->F(f,1) (hmesh.h:379).
 //
 #ifndef METRIKO_HMESH_H
@@ -53,7 +61,7 @@ namespace metriko {
         Face face1() const;
         double len() const;
         double cot() const;
-        bool isBoundary() const { return false; }
+        bool isBoundary() const;
     };
     struct Vert : Elem {
         Half half() const;
@@ -63,8 +71,8 @@ namespace metriko {
         Row3d normal() const;
         double baryArea() const;
         double circArea() const;
-        bool isBoundary() const { return false; }
-        bool isInterior() const { return true; }
+        bool isBoundary() const;
+        bool isInterior() const;
         AdjIter<AdjVH> adjHalfs(bool ccw = true) const;
         AdjIter<AdjVH> adjHalfs(Half h, bool ccw = true) const;
     };
@@ -92,7 +100,7 @@ namespace metriko {
         double darg() const;
         double cot() const;
         double len() const { return vec().norm(); }
-        bool isBoundary() const { return false; }
+        bool isBoundary() const;
         bool isCanonical() const;
         Row3d vec() const;
     };
@@ -112,16 +120,17 @@ namespace metriko {
         MatXi face2edge;   // nF x 3, edge of (F(f,j), F(f,j+1))
         MatXi face2half3;  // nF x 3, halfedge of face f on face2edge(f,j)
         MatXd faceBasisX, faceBasisY, faceNormal, baryCenter;
-        VecXd faceArea, angleDefect, heArgOnFace;
+        VecXd faceArea, angleDefect, heArgOnFace;   // heArgOnFace: 0 on boundary halfedges
+        std::vector<int> loop2half;   // first boundary halfedge of each boundary loop
+        std::vector<bool> isBV;       // vertex on a boundary edge
+        std::vector<char> isBE;       // edge with one face
+        bool hasBoundary = false;
         // filled by finish() (hmesh.h:444-568 of the reference): vertex frames, dual areas,
-        // cotangents, dihedral angles, halfedge angles around vertices, corner handles;
-        // closed meshes only, so there are no boundary loops and no boundary vertices
+        // cotangents, dihedral angles, halfedge angles around vertices, corner handles
         MatXd vertBasisX, vertBasisY, vertNormal;
         VecXd baryDualArea, circDualArea, halfCotan, edgeCotan, dihedralArg, heArgOnVert;
         std::vector<Crnr> crnrs;
         std::vector<Loop> loops;
-        std::vector<int> loop2half;
-        std::vector<bool> isBV;
 
         Hmesh(const MatXd& V, const MatXi& F);
         // Two-phase construction: connectivity, face frames, normals, centres, areas and halfedge
@@ -183,6 +192,10 @@ namespace metriko {
     inline Vert Crnr::vert() const { return half().prev().tail(); }
     inline Face Crnr::face() const { return half().face(); }
     inline bool Half::isCanonical() const { return m->edge2half[m->edge[id]] == id; }
+    inline bool Half::isBoundary() const { return m->face[id] == -1; }
+    inline bool Edge::isBoundary() const { return m->isBE[id] != 0; }
+    inline bool Vert::isBoundary() const { return m->isBV[id]; }
+    inline bool Vert::isInterior() const { return !m->isBV[id]; }
     inline Row3d Half::vec() const { return row3(m->pos, m->head[id]) - row3(m->pos, m->tail[id]); }
     inline Half Vert::half() const { return {{m->vert2half[id], m}}; }
     inline Row3d Vert::pos() const { return row3(m->pos, id); }
@@ -264,14 +277,17 @@ namespace metriko {
             if (c >= 2) EF(e, 1) = ent[p0 + 1].f;
             if (c > 2) __atomic_store_n(&over, 1, __ATOMIC_RELAXED);
             for (int p = p0; p < p0 + c; p++) FE(ent[p].f, ent[p].i) = e;
-            if (c != 2) { err[e] = 1; continue; }
+            if (c > 2) continue;
+            // slot 0 holds the face in which the edge runs lo -> hi (-1 when a boundary edge's
+            // one face runs hi -> lo)
             if (ent[p0].a != lo_of[p0]) std::swap(EF(e, 0), EF(e, 1));
-            if (EF(e, 0) == EF(e, 1)) err[e] = 2;
+            if (c == 2 && EF(e, 0) == EF(e, 1)) err[e] = 2;
+            else if (c == 2 && ent[p0].a == ent[p0 + 1].a) err[e] = 3;   // both faces run the same way
         }
         if (over) throw std::invalid_argument("mesh is not edge-manifold");
         auto it = std::find_if(err.begin(), err.end(), [](char x) { return x != 0; });
         if (it != err.end())
-            throw std::invalid_argument(*it == 1 ? "mesh has boundary edges (closed meshes only)" : "degenerate edge");
+            throw std::invalid_argument(*it == 2 ? "degenerate edge" : "inconsistently oriented faces");
     }
 
     inline Hmesh::Hmesh(const MatXd& V, const MatXi& F) : Hmesh(V, F, Deferred{}) { finish(); }
@@ -287,27 +303,45 @@ namespace metriko {
         nH = 2 * nE;
         nC = 3 * nF;
         nEularChars = nV - nE + nF;
+        const int nI = 3 * nF;   // interior halfedges (one per face corner)
         vert2half.assign(nV, -1);
         edge2half.resize(nE);
         face2half.resize(nF);
         crnr2half.assign(nC, -1);
-        next.assign(nH, -1); prev.assign(nH, -1); twin.resize(nH); tail.resize(nH);
-        head.resize(nH); edge.resize(nH); face.resize(nH); crnr.assign(nH, -1);
-        METRIKO_PARALLEL_FOR
-        for (int e = 0; e < nE; e++) {
-            tail[2 * e] = edge2vert(e, 0);
-            tail[2 * e + 1] = edge2vert(e, 1);
-            face[2 * e] = edge2face(e, 0);
-            face[2 * e + 1] = edge2face(e, 1);
-            twin[2 * e] = 2 * e + 1;
-            twin[2 * e + 1] = 2 * e;
-            edge[2 * e] = edge[2 * e + 1] = e;
-            edge2half[e] = 2 * e;
+        next.assign(nH, -1); prev.assign(nH, -1); twin.assign(nH, -1); tail.assign(nH, -1);
+        head.assign(nH, -1); edge.assign(nH, -1); face.assign(nH, -1); crnr.assign(nH, -1);
+        isBE.assign(nE, 0);
+        // EH(e, s): the interior halfedge of edge e in slot s (-1 when the slot has no face), the
+        // running count of faced slots in (edge, slot) order
+        MatXi EH(nE, 2, -1);
+        {
+            std::vector<int> cnt(nE + 1, 0);
+            METRIKO_PARALLEL_FOR
+            for (int e = 0; e < nE; e++) {
+                const int c = (edge2face(e, 0) >= 0) + (edge2face(e, 1) >= 0);
+                cnt[e + 1] = c;
+                isBE[e] = c == 1;
+            }
+            for (int e = 0; e < nE; e++) cnt[e + 1] += cnt[e];
+            if (cnt[nE] != nI) throw std::invalid_argument("mesh is not edge-manifold");
+            METRIKO_PARALLEL_FOR
+            for (int e = 0; e < nE; e++) {
+                int h = cnt[e];
+                for (int k = 0; k < 2; k++) {
+                    if (edge2face(e, k) < 0) continue;
+                    EH(e, k) = h;
+                    tail[h] = edge2vert(e, k);
+                    face[h] = edge2face(e, k);
+                    edge[h] = e;
+                    h++;
+                }
+                if (EH(e, 0) >= 0 && EH(e, 1) >= 0) { twin[EH(e, 0)] = EH(e, 1); twin[EH(e, 1)] = EH(e, 0); }
+            }
         }
-        // last write wins in edge order (dcel, hmesh.h:240-311, :377): halfedge 2e + s is written for
-        // edge2vert(e, s), so the survivor is the largest halfedge id starting at the vertex
+        // last write wins in (edge, slot) order (dcel, hmesh.h:268-279, :377): the survivor is
+        // the largest interior halfedge id starting at the vertex
         METRIKO_PARALLEL_FOR
-        for (int h = 0; h < nH; h++) {
+        for (int h = 0; h < nI; h++) {
             int* slot = &vert2half[tail[h]];
             int cur = __atomic_load_n(slot, __ATOMIC_RELAXED);
             while (h > cur && !__atomic_compare_exchange_n(slot, &cur, h, true, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) {
@@ -319,7 +353,7 @@ namespace metriko {
         for (int f = 0; f < nF; f++)
             for (int j = 0; j < 3; j++) {
                 int e = face2edge(f, j);
-                face2half3(f, j) = 2 * e + (edge2face(e, 0) == f ? 0 : 1);
+                face2half3(f, j) = EH(e, edge2face(e, 0) == f ? 0 : 1);
             }
         METRIKO_PARALLEL_FOR
         for (int f = 0; f < nF; f++) {
@@ -336,10 +370,55 @@ namespace metriko {
             }
         }
         METRIKO_PARALLEL_FOR
-        for (int h = 0; h < nH; h++) head[h] = tail[next[h]];
+        for (int h = 0; h < nI; h++) head[h] = tail[next[h]];
+        // boundary loops (hmesh.h:393-418): each interior halfedge without a twin, in id order,
+        // starts a new loop unless an earlier loop took it; the loop's boundary halfedges are
+        // numbered on from 3 nF, each the reverse of the interior halfedge it borders, walking
+        // to the previous interior halfedge without a twin around the shared vertex
+        loop2half.clear();
+        {
+            int iB = nI;
+            for (int iH = 0; iH < nI; iH++) {
+                if (twin[iH] != -1) continue;
+                int jH = iH;
+                const int jB = iB;
+                bool done = false;
+                while (true) {
+                    if (iB >= nH) throw std::invalid_argument("mesh is not edge-manifold");
+                    tail[iB] = head[jH];
+                    head[iB] = tail[jH];
+                    edge[iB] = edge[jH];
+                    prev[iB] = iB - 1;
+                    next[iB] = iB + 1;
+                    twin[jH] = iB;
+                    twin[iB] = jH;
+                    jH = prev[jH];
+                    long long guard = 0;
+                    while (twin[jH] != -1) {
+                        if (jH == iH) { done = true; break; }
+                        jH = prev[twin[jH]];
+                        if (++guard > nH) throw std::invalid_argument("mesh is not edge-manifold");
+                    }
+                    if (done) break;
+                    iB++;
+                }
+                prev[jB] = iB;
+                next[iB] = jB;
+                loop2half.push_back(jB);
+                iB++;
+            }
+            if (iB != nH) throw std::invalid_argument("mesh is not edge-manifold");
+        }
+        nL = int(loop2half.size());
+        hasBoundary = nL > 0;
+        isBV.assign(nV, false);
+        METRIKO_PARALLEL_FOR
+        for (int e = 0; e < nE; e++) edge2half[e] = EH(e, 0) >= 0 ? EH(e, 0) : twin[EH(e, 1)];
+        for (int e = 0; e < nE; e++)
+            if (isBE[e]) { isBV[edge2vert(e, 0)] = true; isBV[edge2vert(e, 1)] = true; }
 
         faceBasisX = MatXd(nF, 3); faceBasisY = MatXd(nF, 3); faceNormal = MatXd(nF, 3); baryCenter = MatXd(nF, 3);
-        faceArea = VecXd(nF); heArgOnFace = VecXd(nH);
+        faceArea = VecXd(nF); heArgOnFace = VecXd(nH, 0.0);
         METRIKO_PARALLEL_FOR
         for (int f = 0; f < nF; f++) {
             Row3d p0 = row3(pos, F(f, 0)), p1 = row3(pos, F(f, 1)), p2 = row3(pos, F(f, 2));
@@ -380,12 +459,12 @@ namespace metriko {
             if (i < nE) edges[i] = Edge{{i, this}};
             if (i < nC) crnrs[i] = Crnr{{i, this}};
         }
-        loop2half.clear();
-        loops.clear();
-        nL = 0;
-        isBV.assign(nV, false);
+        loops.resize(nL);
+        for (int l = 0; l < nL; l++) loops[l] = Loop{{l, this}};
         // halfedge angles around each vertex and the angle defect (hmesh.h:557-568): the angle
-        // sum in ring order from vert2half, each halfedge's running sum rescaled to 2 pi
+        // sum in ring order from vert2half, each halfedge's running sum rescaled to 2 pi; at a
+        // boundary vertex the ring includes its boundary halfedge, whose angle is the one between
+        // the vertex's two boundary edges, and the defect is pi - sum
         angleDefect = VecXd(nV);
         heArgOnVert = VecXd(nH);
         METRIKO_PARALLEL_FOR
@@ -397,7 +476,7 @@ namespace metriko {
                 Row3d v2 = h.prev().twin().vec().normalized();
                 sum += std::acos(v1.dot(v2));
             }
-            angleDefect[v] = TwoPI - sum;
+            angleDefect[v] = isBV[v] ? PI - sum : TwoPI - sum;
             for (Half h : verts[v].adjHalfs()) heArgOnVert[h.id] *= TwoPI / sum;
         }
         // vertex normals: area-weighted face normals summed in face order (hmesh.h:491-498), so
@@ -410,13 +489,14 @@ namespace metriko {
             int fs[64], k = 0;
             bool small = true;
             for (Half h : verts[v].adjHalfs()) {
+                if (h.face().id < 0) continue;
                 if (k == 64) { small = false; break; }
                 fs[k++] = h.face().id;
             }
             std::vector<int> big;
             const int* list = fs;
             if (!small) {
-                for (Half h : verts[v].adjHalfs()) big.push_back(h.face().id);
+                for (Half h : verts[v].adjHalfs()) if (h.face().id >= 0) big.push_back(h.face().id);
                 std::sort(big.begin(), big.end());
                 list = big.data();
                 k = int(big.size());
@@ -436,15 +516,22 @@ namespace metriko {
             set_row3(vertBasisX, v, x);
             set_row3(vertBasisY, v, n.cross(x));
         }
-        // dihedral angle and cotangent of each halfedge (hmesh.h:508-533), edge cotangents
+        // dihedral angle and cotangent of each halfedge (hmesh.h:508-533), edge cotangents; the
+        // dihedral angle is 0 on both halfedges of a boundary edge, the cotangent 0 on a boundary
+        // halfedge
         dihedralArg = VecXd(nH);
         halfCotan = VecXd(nH);
         METRIKO_PARALLEL_FOR
         for (int i = 0; i < nH; i++) {
             const Half h{{i, this}};
-            const Row3d n1 = row3(faceNormal, face[i]), n2 = row3(faceNormal, face[twin[i]]);
-            const Row3d v = h.vec() / h.len();
-            dihedralArg[i] = std::atan2(v.dot(n1.cross(n2)), n1.dot(n2));
+            if (isBE[edge[i]]) {
+                dihedralArg[i] = 0;
+            } else {
+                const Row3d n1 = row3(faceNormal, face[i]), n2 = row3(faceNormal, face[twin[i]]);
+                const Row3d v = h.vec() / h.len();
+                dihedralArg[i] = std::atan2(v.dot(n1.cross(n2)), n1.dot(n2));
+            }
+            if (face[i] < 0) { halfCotan[i] = 0.; continue; }
             const Row3d vn = h.next().vec();
             const Row3d vp = h.prev().vec() * -1;
             halfCotan[i] = vp.dot(vn) / vp.cross(vn).norm();
@@ -459,7 +546,7 @@ namespace metriko {
         for (int v = 0; v < nV; v++) {
             double a1 = 0, a2 = 0;
             for (Half h : verts[v].adjHalfs()) {
-                a1 += faceArea[h.face().id];
+                if (h.face().id != -1) a1 += faceArea[h.face().id];
                 a2 += h.cot() * h.vec().squaredNorm();
                 a2 += h.prev().cot() * h.prev().vec().squaredNorm();
             }

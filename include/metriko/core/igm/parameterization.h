@@ -39,7 +39,20 @@ namespace metriko {
         MatXi idx;
     };
 
-    // parameterization.h:126-152: duplicate every vertex once per seam sector.
+    // First halfedge in cw order from v.half() on a boundary edge (parameterization.h:82,136), or
+    // on a seam edge (:81,137); v.half() when there is none.
+    inline int first_cw_half(const Hmesh& m, int v, const std::vector<bool>* seam) {
+        const int h0 = m.vert2half[v];
+        int h = h0;
+        do {
+            if (seam ? bool((*seam)[m.edge[h]]) : m.isBE[m.edge[h]] != 0) return h;
+            h = m.next[m.twin[h]];
+        } while (h != h0);
+        return h0;
+    }
+
+    // parameterization.h:126-152: duplicate every vertex once per seam sector.  A boundary vertex
+    // starts at its first boundary-edge halfedge and skips its boundary halfedge.
     inline std::unique_ptr<CutMesh> compute_cut_mesh(const Hmesh& m, const std::vector<bool>& seam) {
         auto cm = std::make_unique<CutMesh>();
         cm->nF = m.nF;
@@ -49,18 +62,11 @@ namespace metriko {
         std::vector<int> bgn(m.nV), base(m.nV + 1, 0);
         METRIKO_PARALLEL_FOR
         for (int v = 0; v < m.nV; v++) {
-            int b = m.vert2half[v];
-            {   // first seam halfedge in cw order from v.half()
-                int h0 = b, h = h0;
-                do {
-                    if (seam[m.edge[h]]) { b = h; break; }
-                    h = m.next[m.twin[h]];
-                } while (h != h0);
-            }
+            const int b = first_cw_half(m, v, m.isBV[v] ? nullptr : &seam);
             bgn[v] = b;
             int cnt = 0, h = b;
             do {
-                if (seam[m.edge[h]] || h == b) cnt++;
+                if (m.face[h] >= 0 && (seam[m.edge[h]] || h == b)) cnt++;
                 h = m.twin[m.prev[h]];
             } while (h != b);
             base[v + 1] = cnt;
@@ -72,6 +78,7 @@ namespace metriko {
         for (int v = 0; v < m.nV; v++) {
             int c = base[v] - 1, h = bgn[v];
             do {
+                if (m.face[h] < 0) { h = m.twin[m.prev[h]]; continue; }
                 if (seam[m.edge[h]] || h == bgn[v]) {
                     c++;
                     for (int k = 0; k < 3; k++) cm->pos(c, k) = m.pos(v, k);
@@ -166,15 +173,10 @@ namespace metriko {
         bool integ();
 
     private:
-        bool is_inside_singular(int v) const { return singlars[v] != 0; }
-        int first_seam_he(int v) const {
-            int h0 = raw.vert2half[v], h = h0;
-            do {
-                if (seam[raw.edge[h]]) return h;
-                h = raw.next[raw.twin[h]];
-            } while (h != h0);
-            return h0;
-        }
+        // parameterization.h:80-82
+        bool is_inside_singular(int v) const { return !raw.isBV[v] && singlars[v] != 0; }
+        int first_seam_he(int v) const { return first_cw_half(raw, v, &seam); }
+        int first_bndr_he(int v) const { return first_cw_half(raw, v, nullptr); }
 
         // parameterization_setup.ipp:3-9
         void compute_he2matching() {
@@ -195,15 +197,16 @@ namespace metriko {
             int tid = 1;
             for (int v = 0; v < raw.nV; v++) {
                 if ((valence[v] == 2 && !is_inside_singular(v)) || valence[v] == 0) continue;
-                int h0 = raw.vert2half[v], cH = h0;
+                int h0 = first_bndr_he(v), cH = h0;
                 do {
                     int cE = raw.edge[cH];
-                    if (seam[cE] && !claimed[cE]) {
+                    if (!raw.isBE[cE] && seam[cE] && !claimed[cE]) {
                         he2transidx[cH] = tid;
                         he2transidx[raw.twin[cH]] = -tid;
                         claimed[cE] = 1;
                         int jv = raw.head[cH];
-                        while (valence[jv] == 2 && !is_inside_singular(jv)) {
+                        // traces the seam until a singular or boundary vertex
+                        while (valence[jv] == 2 && !is_inside_singular(jv) && !raw.isBV[jv]) {
                             int nh = -1, g0 = raw.vert2half[jv], g = g0;
                             do {
                                 if (seam[raw.edge[g]] && !claimed[raw.edge[g]]) { nh = g; break; }
@@ -244,6 +247,7 @@ namespace metriko {
         std::vector<int> plainCut(raw.nV, -1);
         METRIKO_PARALLEL_FOR
         for (int v = 0; v < raw.nV; v++) {
+            if (raw.isBV[v]) continue;
             const int g0 = raw.vert2half[v];
             int g = g0;
             bool onSeam = false;
@@ -255,14 +259,16 @@ namespace metriko {
             const int f = raw.face[g0];
             for (int j = 0; j < 3; j++) if (raw.idx(f, j) == v) plainCut[v] = cut.idx(f, j);
         }
-        for (int v = 0; v < raw.nV; v++) {       // setup.ipp:66-124, vertices on the seam
+        for (int v = 0; v < raw.nV; v++) {       // setup.ipp:66-124, vertices on the seam or boundary
             if (plainCut[v] >= 0) continue;
+            const bool bv = raw.isBV[v];
             std::vector<MatXi> pm{I};
             std::vector<int> pidx{v};
             int iVcut = -1;
-            const int h0 = first_seam_he(v);
+            const int h0 = bv ? first_bndr_he(v) : first_seam_he(v);
             int h = h0;
             do {
+                if (raw.face[h] < 0) break;   // the boundary halfedge ends the fan (setup.ipp:77)
                 int f = raw.face[h];
                 int jVcut = -1;
                 for (int j = 0; j < 3; j++) if (raw.idx(f, j) == v) jVcut = cut.idx(f, j);
@@ -271,7 +277,7 @@ namespace metriko {
                     for (size_t i = 0; i < pidx.size(); i++) block(vT, pm[i], N * iVcut, N * pidx[i]);
                 }
                 int hn = raw.twin[raw.prev[h]];
-                if (seam[raw.edge[hn]]) {
+                if (raw.face[hn] >= 0 && seam[raw.edge[hn]]) {
                     const MatXi& p = perms[he2matching[hn]];
                     int t = he2transidx[hn];
                     if (t > 0) {
@@ -286,6 +292,7 @@ namespace metriko {
                 }
                 h = hn;
             } while (h != h0);
+            if (bv) continue;                  // no constraint on a boundary vertex (setup.ipp:105)
             std::set<int> uniq(pidx.begin(), pidx.end());
             std::vector<int> idcs(uniq.begin(), uniq.end());
             std::vector<MatXi> mats(idcs.size());

@@ -57,6 +57,7 @@ namespace metriko {
 
         // Inputs of the device assembly: neighbour across each face halfedge and
         // theta = farg(h) - farg(twin h); L(f, nbr) = -(-e^{i theta})^N (face_rosy_field.h:52-75).
+        // A boundary side has no neighbour (-1, theta 0) and adds nothing to L (:64).
         void assembly_inputs(std::vector<int>& nbr, std::vector<double>& theta) const {
             nbr.resize(3 * size_t(mesh.nF));
             theta.resize(3 * size_t(mesh.nF));
@@ -65,7 +66,7 @@ namespace metriko {
                 for (int j = 0; j < 3; j++) {
                     int h = mesh.face2half3(f, j), t = mesh.twin[h];
                     nbr[3 * f + j] = mesh.face[t];
-                    theta[3 * f + j] = mesh.heArgOnFace[h] - mesh.heArgOnFace[t];
+                    theta[3 * f + j] = mesh.face[t] < 0 ? 0.0 : mesh.heArgOnFace[h] - mesh.heArgOnFace[t];
                 }
         }
 
@@ -104,8 +105,12 @@ namespace metriko {
                     const Half hh{{h, &mesh}};
                     const Row3d vec = hh.vec();
                     const double l = vec.norm();
-                    const Row3d n1 = row3(mesh.faceNormal, f), n2 = row3(mesh.faceNormal, mesh.face[mesh.twin[h]]);
-                    const double darg = std::atan2((vec / l).dot(n1.cross(n2)), n1.dot(n2));
+                    const int g = mesh.face[mesh.twin[h]];
+                    double darg = 0;   // 0 on a boundary edge (hmesh.h:510-513)
+                    if (g >= 0) {
+                        const Row3d n1 = row3(mesh.faceNormal, f), n2 = row3(mesh.faceNormal, g);
+                        darg = std::atan2((vec / l).dot(n1.cross(n2)), n1.dot(n2));
+                    }
                     const complex c = std::polar(1., mesh.heArgOnFace[h]) * l;
                     dir += -c * c / l * darg;
                 }
@@ -141,10 +146,11 @@ namespace metriko {
             return c;
         }
 
-        void computeConnection() {      // face_rosy_field.h:109-117
+        void computeConnection() {      // face_rosy_field.h:109-117 (interior edges; 0 on the boundary)
             connection = VecXc(mesh.nE, complex(0, 0));
             METRIKO_PARALLEL_FOR
             for (int e = 0; e < mesh.nE; e++) {
+                if (mesh.isBE[e]) continue;
                 Row3d v = Half{{mesh.edge2half[e], &mesh}}.vec().normalized();
                 int f0 = mesh.edge2face(e, 0), f1 = mesh.edge2face(e, 1);
                 complex ef(v.dot(row3(mesh.faceBasisX, f0)), v.dot(row3(mesh.faceBasisY, f0)));
@@ -153,10 +159,12 @@ namespace metriko {
             }
         }
 
-        void computeSingular(const VecXd& effort) {   // face_rosy_field.h:100-107
+        // face_rosy_field.h:100-107: boundary vertices keep the initial 1
+        void computeSingular(const VecXd& effort) {
             singular = VecXi(mesh.nV, 1);
             METRIKO_PARALLEL_FOR
             for (int v = 0; v < mesh.nV; v++) {
+                if (mesh.isBV[v]) continue;
                 double sum = mesh.angleDefect[v] * rosyN;
                 int h0 = mesh.vert2half[v], h = h0;
                 do {
@@ -176,11 +184,14 @@ namespace metriko {
                 matching = VecXi(mesh.nE, -1);
                 singular = VecXi(mesh.nV, 0);
                 connection = VecXc();
+                // a closed mesh's halfedges are 2e / 2e + 1, so the twin and edge arrays stay here
+                const bool b = mesh.hasBoundary;
                 gpu::check(mtk_curl_matching(gpu::bound_context(), mesh.nV, mesh.nF, mesh.nE, rosyN, mesh.pos.data(),
                                              mesh.idx.data(), mesh.edge2vert.data(), mesh.edge2face.data(),
-                                             mesh.vert2half.data(), mesh.prev.data(), mesh.angleDefect.data(),
-                                             reinterpret_cast<const double*>(compressed.data()), matching.data(),
-                                             singular.data()),
+                                             mesh.vert2half.data(), mesh.prev.data(), b ? mesh.twin.data() : nullptr,
+                                             b ? mesh.edge.data() : nullptr, b ? mesh.edge2half.data() : nullptr,
+                                             mesh.angleDefect.data(), reinterpret_cast<const double*>(compressed.data()),
+                                             matching.data(), singular.data()),
                            "mtk_curl_matching");
                 return;
             }
@@ -193,9 +204,10 @@ namespace metriko {
         }
 
     private:
-        void pMatching(VecXd& effort) {    // face_rosy_field.h:138-167
+        void pMatching(VecXd& effort) {    // face_rosy_field.h:138-167 (interior edges)
             METRIKO_PARALLEL_FOR
             for (int e = 0; e < mesh.nE; e++) {
+                if (mesh.isBE[e]) continue;
                 int f0 = mesh.edge2face(e, 0), f1 = mesh.edge2face(e, 1);
                 complex conn = connection[e];
                 double minRot = 1000.;
@@ -215,9 +227,10 @@ namespace metriko {
             }
         }
 
-        void cMatching(VecXd& effort) {    // face_rosy_field.h:169-202
+        void cMatching(VecXd& effort) {    // face_rosy_field.h:169-202 (interior edges)
             METRIKO_PARALLEL_FOR
             for (int e = 0; e < mesh.nE; e++) {
+                if (mesh.isBE[e]) continue;
                 int iM = 0;
                 double mn = 32767000.;
                 Row3d v = Half{{mesh.edge2half[e], &mesh}}.vec().normalized();
@@ -243,7 +256,7 @@ namespace metriko {
         }
     };
 
-    // face_rosy_field.h:207-249
+    // face_rosy_field.h:207-249 (the search crosses no boundary edge; they keep matching -1)
     inline std::unique_ptr<FaceRosyField> compute_combbed_field(const FaceRosyField& fld, const std::vector<bool>& seam) {
         const Hmesh& m = fld.mesh;
         const int N = fld.rosyN;
@@ -262,7 +275,7 @@ namespace metriko {
             for (int j = 0; j < 3; j++) {
                 const int e = m.edge[m.face2half3(i, j)];
                 const bool b = m.edge2face(e, 0) == i;
-                nb[3 * size_t(i) + j] = seam[e] ? -1 : (b ? m.edge2face(e, 1) : m.edge2face(e, 0));
+                nb[3 * size_t(i) + j] = (seam[e] || m.isBE[e]) ? -1 : (b ? m.edge2face(e, 1) : m.edge2face(e, 0));
                 nm[3 * size_t(i) + j] = (b ? 1 : -1) * fld.matching[e];
             }
         std::deque<std::pair<int, int>> q;
@@ -285,7 +298,8 @@ namespace metriko {
         F->matching = VecXi(m.nE, -1);
         METRIKO_PARALLEL_FOR
         for (int e = 0; e < m.nE; e++)
-            F->matching[e] = (turns[m.edge2face(e, 0)] - turns[m.edge2face(e, 1)] + fld.matching[e] + 1000 * N) % N;
+            if (!m.isBE[e])
+                F->matching[e] = (turns[m.edge2face(e, 0)] - turns[m.edge2face(e, 1)] + fld.matching[e] + 1000 * N) % N;
         return F;
     }
 
@@ -305,7 +319,8 @@ namespace metriko {
     }
 
     namespace detail {
-        // TT(f,s): face across edge s = (F(f,s), F(f,s+1)); TTi(f,s): that edge's slot in TT(f,s).
+        // TT(f,s): face across edge s = (F(f,s), F(f,s+1)); TTi(f,s): that edge's slot in TT(f,s);
+        // both -1 on a boundary side.
         inline void triangle_adjacency(const Hmesh& m, MatXi& TT, MatXi& TTi) {
             TT = MatXi(m.nF, 3);
             TTi = MatXi(m.nF, 3);
@@ -315,11 +330,13 @@ namespace metriko {
                     int t = m.twin[m.face2half3(f, s)];
                     int g = m.face[t];
                     TT(f, s) = g;
-                    TTi(f, s) = m.face2half3(g, 0) == t ? 0 : (m.face2half3(g, 1) == t ? 1 : 2);
+                    TTi(f, s) = g < 0 ? -1 : (m.face2half3(g, 0) == t ? 0 : (m.face2half3(g, 1) == t ? 1 : 2));
                 }
         }
 
-        // libigl cut_mesh_from_singularities with an all-zero matching (see file header).
+        // libigl cut_mesh_from_singularities with an all-zero matching (see file header).  A
+        // boundary side is never crossed by the flood fill, so it stays a seam, and the retraction
+        // counts it once (TT = -1 <= f); boundary loops are cycles and are never retracted.
         inline MatXi spanning_cut(const Hmesh& m, const MatXi& TT, const MatXi& TTi) {
             const MatXi& F = m.idx;
             const int nF = m.nF;
@@ -335,7 +352,7 @@ namespace metriko {
                     const int f = queue[head++];
                     for (int s = 0; s < 3; s++) {
                         int g = TT(f, s), j = TTi(f, s);
-                        if (!visited[g]) {
+                        if (g >= 0 && !visited[g]) {
                             visited[g] = 1;
                             seams(f, s) = 0;
                             seams(g, j) = 0;
@@ -383,7 +400,7 @@ namespace metriko {
                             if (!pruned(f, s2)) continue;
                             const int a = F(f, s2), b = F(f, (s2 + 1) % 3), w = a == v ? b : a;
                             pruned(f, s2) = 0;
-                            pruned(TT(f, s2), TTi(f, s2)) = 0;
+                            if (TT(f, s2) >= 0) pruned(TT(f, s2), TTi(f, s2)) = 0;
                             deg[v]--;
                             deg[w]--;
                             if (deg[w] == 1) next_layer.push_back(w);
@@ -414,7 +431,7 @@ namespace metriko {
                     int a = F(f, s), b = F(f, (s + 1) % 3);
                     if (e[a] == 1 || e[b] == 1) {
                         seams(f, s) = 0;
-                        seams(TT(f, s), TTi(f, s)) = 0;
+                        if (TT(f, s) >= 0) seams(TT(f, s), TTi(f, s)) = 0;
                         e[a]--;
                         e[b]--;
                         removed = true;
@@ -536,7 +553,9 @@ namespace metriko {
                 for (int z = 0; z < 3; z++)
                     if ((F(fi, z) == v0 && F(fi, (z + 1) % 3) == v1) || (F(fi, z) == v1 && F(fi, (z + 1) % 3) == v0)) j = z;
                 cuts(fi, j) = 1;
-                cuts(TT(fi, j), TTi(fi, j)) = 1;
+                // never a boundary edge: every boundary vertex is on the cut, and a search stops at
+                // the first cut vertex it reaches
+                if (TT(fi, j) >= 0) cuts(TT(fi, j), TTi(fi, j)) = 1;
             }
         }
     }

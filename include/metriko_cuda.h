@@ -124,10 +124,12 @@ int64_t mtk_ctx_kernel_count(const mtk_ctx* ctx);
 int mtk_ctx_set_wait_limit(mtk_ctx* ctx, int64_t polls);
 
 /*
- * Smoothest N-RoSy field: assemble the connection Laplacian L (face graph, 3 neighbours per
- * face) and the lumped mass M = diag(area) on the device, then run n_iter steps of inverse
+ * Smoothest N-RoSy field: assemble the connection Laplacian L (face graph, up to 3 neighbours
+ * per face) and the lumped mass M = diag(area) on the device, then run n_iter steps of inverse
  * power iteration  x = L^-1 M u,  x /= sqrt|x^H M x|,  u = x.
- *   nbr[3*f+j]   face across the j-th halfedge of face f (halfedge F(f,j) -> F(f,j+1))
+ *   nbr[3*f+j]   face across the j-th halfedge of face f (halfedge F(f,j) -> F(f,j+1)), or -1
+ *                when that halfedge lies on the boundary (no entry, face_rosy_field.h:64); any
+ *                other value outside [0, nF), or f itself -> MTK_ERR_BAD_INPUT
  *   theta[3*f+j] heArgOnFace(h) - heArgOnFace(twin(h)) for that halfedge; the off-diagonal
  *                entry is  L(f, nbr) = -(-exp(i theta))^nRosy,  the diagonal #nbr + 1e-9
  *   area[f]      face area;  x0[2*f], x0[2*f+1]  start vector (re, im)
@@ -231,9 +233,9 @@ int mtk_topology_from_field(int32_t nV, int32_t nF, const double* V, const int32
  * (which has no GPU code); it allocates nothing and needs no mtk_ctx.
  *   All pointers are DEVICE pointers owned by the caller: nbr[3*nF], theta[3*nF], area[nF],
  *   x0[2*nF] (re, im), out[2*nF].  stream: a cudaStream_t (NULL = default stream).
- *   Closed meshes: every nbr entry must lie in [0, nF) (the diagonal is 3 + 1e-9); an entry
- *   outside (e.g. -1 for a boundary edge) -> MTK_ERR_BAD_INPUT, detected on the device, with
- *   no solve.  n_iter = 0 copies x0 to out.  max_iter caps every inner PCG solve
+ *   nbr as for mtk_field_smoothest: -1 marks a boundary side (the row's diagonal is then its
+ *   count of neighbours + 1e-9); any other entry outside [0, nF) -> MTK_ERR_BAD_INPUT, detected
+ *   on the device, with no solve.  n_iter = 0 copies x0 to out.  max_iter caps every inner PCG solve
  *   (MTK_ERR_NOT_CONVERGED when reached).
  *   Working memory is a 64 MiB static device array inside the library (held by every GPU that
  *   loads the library until exit), which limits nF to 409600; larger nF -> MTK_ERR_BAD_INPUT.
@@ -271,7 +273,8 @@ int mtk_field_solve(mtk_ctx* ctx, int32_t nF, int32_t nRosy, const int32_t* nbr,
  *   F[3*nF]      raw mesh faces (corner vertex ids < nV; the rows of the cut faces)
  *   s[nV]        log-size per raw vertex
  *   T[8*nF]      loss target per face in the F2 layout, or NULL for the integration target F2
- *   mu >= 0      edge smoothness weight (every edge of a closed mesh lies in two faces)
+ *   mu >= 0      edge smoothness weight: the term sums (s_i - s_j)^2 / 2 over face sides, i.e.
+ *                every interior edge once and a boundary edge at half weight
  *   loss, grad_s[nV], fullx[nFull] (the integration result x(s) in full variables)
  * desc->seamless and the rounding fields are not used.
  */
@@ -345,13 +348,14 @@ int mtk_face_geometry_backward(mtk_ctx* ctx, int32_t nV, int32_t nF, const doubl
                                const double* g_gy, double* grad_V);
 
 /*
- * The inputs of mtk_field_smoothest computed on the device from the raw closed mesh (V[3 nV],
- * F[3 nF]) without the halfedge mesh: nbr[3 nF] the face across side j of face f (the side from
- * F(f, j) to F(f, j+1)), theta[3 nF] = heArgOnFace(h) - heArgOnFace(twin h) and area[nF]
- * (include/metriko/core/hmesh/hmesh.h:313-489 of the reference: the constructor's pairing, face
- * frames and halfedge angles).  The same values as mtk_field_inputs (the halfedge mesh on the
- * host), theta up to the last-bit rounding of acos.  A boundary or non-manifold edge, faces of
- * opposite orientation or a side with equal end points -> MTK_ERR_BAD_INPUT.
+ * The inputs of mtk_field_smoothest computed on the device from the raw mesh (V[3 nV], F[3 nF])
+ * without the halfedge mesh: nbr[3 nF] the face across side j of face f (the side from F(f, j)
+ * to F(f, j+1); -1 on a boundary side, with theta 0), theta[3 nF] = heArgOnFace(h) -
+ * heArgOnFace(twin h) and area[nF] (include/metriko/core/hmesh/hmesh.h:313-489 of the reference:
+ * the constructor's pairing, face frames and halfedge angles).  The same values as
+ * mtk_field_inputs (the halfedge mesh on the host), theta up to the last-bit rounding of acos.
+ * A non-manifold edge, faces of opposite orientation or a side with equal end points ->
+ * MTK_ERR_BAD_INPUT.
  */
 int mtk_mesh_field_inputs(mtk_ctx* ctx, int32_t nV, int32_t nF, const double* V, const int32_t* F, int32_t* nbr,
                           double* theta, double* area);
@@ -361,19 +365,23 @@ int mtk_field_smoothest_mesh(mtk_ctx* ctx, int32_t nV, int32_t nF, const double*
                              mtk_stats* stats);
 
 /*
- * Curl matching and singular indices on the device, for a closed mesh: computeConnection,
- * cMatching and computeSingular of FaceRosyField::computeMatching(MatchingType::Curl)
+ * Curl matching and singular indices on the device: computeConnection, cMatching and
+ * computeSingular of FaceRosyField::computeMatching(MatchingType::Curl)
  * (include/metriko/core/vectorfield/face_rosy_field.h:100-135, :169-202), one thread per edge and
- * one per vertex.  Mesh arrays in the Hmesh numbering (halfedge 2e of edge e runs from
- * edge_vert[2e] to edge_vert[2e+1] inside face edge_face[2e]; 2e+1 is its twin, in
- * edge_face[2e+1]):  V[3 nV], F[3 nF], edge_vert[2 nE], edge_face[2 nE], vert_half[nV],
- * prev_half[2 nE], angle_defect[nV]; compressed[2 nF] the field (re, im); N <= 8.
- * Out: matching[nE], singular[nV].  The integer outputs equal the host loops' (the arithmetic is
- * the same, up to the last bit of the device's cos / sin / atan2 / sqrt).
+ * one per vertex.  Mesh arrays in the Hmesh numbering: V[3 nV], F[3 nF], edge_vert[2 nE] (edge e
+ * runs from edge_vert[2e] to edge_vert[2e+1] inside face edge_face[2e]; edge_face[2e+1] is the
+ * other face, -1 on a boundary edge's faceless side), vert_half[nV], prev_half[2 nE],
+ * angle_defect[nV]; compressed[2 nF] the field (re, im); N <= 8.  twin_half[2 nE],
+ * half_edge[2 nE], edge_half[nE] (Hmesh twin, edge, edge2half): required for a mesh with
+ * boundary, NULL (all three) for a closed mesh, whose halfedges 2e / 2e+1 give them.
+ * Out: matching[nE] (-1 on boundary edges), singular[nV] (1 on boundary vertices, as the
+ * reference leaves them).  The integer outputs equal the host loops' (the arithmetic is the same,
+ * up to the last bit of the device's cos / sin / atan2 / sqrt).
  */
 int mtk_curl_matching(mtk_ctx* ctx, int32_t nV, int32_t nF, int32_t nE, int32_t N, const double* V, const int32_t* F,
                       const int32_t* edge_vert, const int32_t* edge_face, const int32_t* vert_half,
-                      const int32_t* prev_half, const double* angle_defect, const double* compressed,
+                      const int32_t* prev_half, const int32_t* twin_half, const int32_t* half_edge,
+                      const int32_t* edge_half, const double* angle_defect, const double* compressed,
                       int32_t* matching, int32_t* singular);
 
 /*
@@ -429,9 +437,9 @@ int mtk_local_injectivity(mtk_ctx* ctx, int32_t nF, int32_t N, const double* cfn
                           int32_t* first_flipped);
 
 /*
- * The inputs of mtk_field_smoothest for a closed mesh (host only): nbr[3*nF] the face across
- * each face halfedge, theta[3*nF] = farg(h) - farg(twin h) (face_rosy_field.h:46-76), and
- * area[nF] (may be NULL).
+ * The inputs of mtk_field_smoothest (host only): nbr[3*nF] the face across each face halfedge
+ * (-1 on the boundary, theta 0 there), theta[3*nF] = farg(h) - farg(twin h)
+ * (face_rosy_field.h:46-76), and area[nF] (may be NULL).
  */
 int mtk_field_inputs(int32_t nV, int32_t nF, const double* V, const int32_t* F, int32_t* nbr, double* theta,
                      double* area);
@@ -439,8 +447,9 @@ int mtk_field_inputs(int32_t nV, int32_t nF, const double* V, const int32_t* F, 
 /*
  * Host only (no GPU): the vertex and edge geometry of Hmesh (hmesh.h:444-568 of the reference:
  * the members vertNormal, vertBasisX, vertBasisY, baryDualArea, circDualArea, halfCotan,
- * edgeCotan, dihedralArg, heArgOnVert, angleDefect) for a closed mesh, in the reference's
- * halfedge / edge numbering (nE = 3 nF / 2, nH = 2 nE).  Every output may be NULL:
+ * edgeCotan, dihedralArg, heArgOnVert, angleDefect), in the reference's halfedge / edge
+ * numbering (interior halfedges first, then the boundary loops; nH = 2 nE, nE from
+ * mtk_topology_from_field's counts or 3 nF / 2 for a closed mesh).  Every output may be NULL:
  * vert_normal, vert_basis_x, vert_basis_y [3 nV]; bary_area, circ_area, angle_defect [nV];
  * half_cotan, dihedral, he_arg_on_vert [nH]; edge_cotan [nE].
  */

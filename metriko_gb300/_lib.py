@@ -127,7 +127,7 @@ def lib():
                                   C.POINTER(Stats)]
         L.mtk_csr_smallest_eig.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
                                            C.POINTER(SolveOpts), C.c_void_p, C.POINTER(Stats)]
-        L.mtk_curl_matching.argtypes = [C.c_void_p] + [C.c_int32] * 4 + [C.c_void_p] * 10
+        L.mtk_curl_matching.argtypes = [C.c_void_p] + [C.c_int32] * 4 + [C.c_void_p] * 13
         L.mtk_mesh_field_inputs.argtypes = [C.c_void_p, C.c_int32, C.c_int32] + [C.c_void_p] * 5
         L.mtk_field_smoothest_mesh.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
                                                C.c_void_p, C.c_int32, C.POINTER(SolveOpts), C.c_void_p,
@@ -144,6 +144,13 @@ def _check(status, what):
 
 def _ptr(a):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def num_edges(F):
+    """Number of distinct undirected edges of a triangle mesh (3 nF / 2 when it is closed)."""
+    F = np.asarray(F, np.int64)
+    e = np.sort(np.concatenate([F[:, [0, 1]], F[:, [1, 2]], F[:, [2, 0]]]), axis=1)
+    return int(len(np.unique(e[:, 0] * (int(F.max()) + 1) + e[:, 1]))) if len(F) else 0
 
 
 def solve_opts(precision="mixed", tol=1e-8, max_iter=50000, max_refine=12, inner_tol=3e-6):
@@ -216,7 +223,7 @@ def pipeline(ctx: Context, V, F, ratio=0.02, seed=0, round_seams=False, seamless
     V = np.ascontiguousarray(V, np.float64)
     F = np.ascontiguousarray(F, np.int32)
     nV, nF = len(V), len(F)
-    nE = 3 * nF // 2
+    nE = num_edges(F)
     singular = np.zeros(nV, np.int32)
     matching = np.zeros(nE, np.int32)
     seam = np.zeros(nE, np.uint8)
@@ -286,7 +293,7 @@ def mesh_geometry(V, F):
     V = np.ascontiguousarray(V, np.float64)
     F = np.ascontiguousarray(F, np.int32)
     nV, nF = len(V), len(F)
-    nE = 3 * nF // 2
+    nE = num_edges(F)
     out = dict(vertNormal=np.zeros((nV, 3)), vertBasisX=np.zeros((nV, 3)), vertBasisY=np.zeros((nV, 3)),
                baryDualArea=np.zeros(nV), circDualArea=np.zeros(nV), halfCotan=np.zeros(2 * nE),
                edgeCotan=np.zeros(nE), dihedralArg=np.zeros(2 * nE), heArgOnVert=np.zeros(2 * nE),
@@ -368,7 +375,7 @@ def size_field_gradient(ctx: Context, V, F, s, T=None, mu=0.0, ratio=0.02, seed=
         if T.size != 8 * nF:
             raise ValueError("T must have 8 values per face")
         Tp = _ptr(T)
-    nE = 3 * nF // 2
+    nE = num_edges(F)
     cap = 2 * (nV + 4 * nE) + 16
     fullx = np.zeros(cap)
     grad = np.zeros(nV)
@@ -393,7 +400,7 @@ def position_gradient(ctx: Context, V, F, s, mu=0.0, ratio=0.02, seed=0, round_s
     s = np.ascontiguousarray(s, np.float64)
     if s.shape != (nV,):
         raise ValueError("s must have one value per vertex")
-    nE = 3 * nF // 2
+    nE = num_edges(F)
     cap = 2 * (nV + 4 * nE) + 16
     fullx = np.zeros(cap)
     grad_s = np.zeros(nV)
@@ -450,9 +457,11 @@ def field_smoothest_mesh(ctx: Context, V, F, x0, n_rosy=4, n_iter=50, opts=None)
     return out[0::2] + 1j * out[1::2], st.as_dict()
 
 
-def curl_matching(ctx: Context, V, F, edge_vert, edge_face, vert_half, prev_half, angle_defect, compressed, N=4):
+def curl_matching(ctx: Context, V, F, edge_vert, edge_face, vert_half, prev_half, angle_defect, compressed, N=4,
+                  twin=None, half_edge=None, edge_half=None):
     """mtk_curl_matching: Curl matching[nE] and singular indices[nV] on the device, from the mesh
-    arrays in the Hmesh numbering and the compressed field (complex[nF])."""
+    arrays in the Hmesh numbering and the compressed field (complex[nF]).  twin / half_edge /
+    edge_half: the halfedge arrays of a mesh with boundary (None for a closed mesh)."""
     V = np.ascontiguousarray(V, np.float64)
     F = np.ascontiguousarray(F, np.int32)
     ev = np.ascontiguousarray(edge_vert, np.int32)
@@ -464,8 +473,12 @@ def curl_matching(ctx: Context, V, F, edge_vert, edge_face, vert_half, prev_half
     nE = len(ev)
     matching = np.zeros(nE, np.int32)
     singular = np.zeros(len(V), np.int32)
+    extra = [None, None, None]
+    if twin is not None:
+        extra = [np.ascontiguousarray(a, np.int32) for a in (twin, half_edge, edge_half)]
     _check(lib().mtk_curl_matching(ctx.handle, len(V), len(F), nE, N, _ptr(V), _ptr(F), _ptr(ev), _ptr(ef), _ptr(vh),
-                                   _ptr(pv), _ptr(ad), _ptr(c), _ptr(matching), _ptr(singular)),
+                                   _ptr(pv), *(_ptr(a) for a in extra), _ptr(ad), _ptr(c), _ptr(matching),
+                                   _ptr(singular)),
            "mtk_curl_matching")
     return matching, singular
 
@@ -546,7 +559,7 @@ def topology_from_field(V, F, compressed, ratio=0.02, round_seams=False):
     V = np.ascontiguousarray(V, np.float64)
     F = np.ascontiguousarray(F, np.int32)
     nV, nF = len(V), len(F)
-    nE = 3 * nF // 2
+    nE = num_edges(F)
     c = np.empty(2 * nF)
     c[0::2], c[1::2] = np.real(compressed), np.imag(compressed)
     singular = np.zeros(nV, np.int32)

@@ -359,25 +359,35 @@ inline HostCsr hcsr_adjoint(const HostCsr& M, int m) {
 //   P = alpha (I - omega D^-1 A) P_sa = alpha R^H
 // are formed for levels >= first_ops (the device applies level 0 from the ELL rows, the
 // aggregates, T and w_p).
-// Level-0 CSR from the ELL rows: the diagonal and the three neighbours, sorted by column.
+// Level-0 CSR from the ELL rows: the diagonal and the neighbours, sorted by column.  A boundary
+// side (nbr -1) has no entry and lowers the diagonal by 1 (diag is that of a face with three
+// neighbours), which gives the reference's #neighbours + 1e-9.
 inline HostCsr ell_to_csr(int n, const std::vector<int>& nbr3, const std::vector<std::complex<double>>& vals,
                           double diag) {
     using cd = std::complex<double>;
     HostCsr A0;
     A0.n = n;
-    A0.ptr.resize(n + 1);
-    A0.col.resize(4 * (size_t)n);
-    A0.val.resize(4 * (size_t)n);
+    A0.ptr.assign(n + 1, 0);
+    for (int f = 0; f < n; f++) {
+        int k = 1;
+        for (int j = 0; j < 3; j++) k += nbr3[3 * (size_t)f + j] >= 0;
+        A0.ptr[f + 1] = A0.ptr[f] + k;
+    }
+    A0.col.resize(A0.ptr[n]);
+    A0.val.resize(A0.ptr[n]);
 #pragma omp parallel for schedule(static)
     for (int f = 0; f < n; f++) {
-        A0.ptr[f] = 4 * f;
         struct E { int c; cd v; } e[4];
-        e[0] = {f, cd(diag, 0)};
-        for (int j = 0; j < 3; j++) e[1 + j] = {nbr3[3 * f + j], vals[(size_t)j * n + f]};
-        std::sort(e, e + 4, [](const E& a, const E& b) { return a.c < b.c; });
-        for (int k = 0; k < 4; k++) { A0.col[4 * (size_t)f + k] = e[k].c; A0.val[4 * (size_t)f + k] = e[k].v; }
+        int k = 1, missing = 0;
+        for (int j = 0; j < 3; j++) {
+            const int g = nbr3[3 * (size_t)f + j];
+            if (g < 0) { missing++; continue; }
+            e[k++] = {g, vals[(size_t)j * n + f]};
+        }
+        e[0] = {f, cd(missing ? diag - (double)missing : diag, 0)};
+        std::sort(e, e + k, [](const E& a, const E& b) { return a.c < b.c; });
+        for (int q = 0; q < k; q++) { A0.col[A0.ptr[f] + q] = e[q].c; A0.val[A0.ptr[f] + q] = e[q].v; }
     }
-    A0.ptr[n] = 4 * n;
     return A0;
 }
 

@@ -60,23 +60,31 @@ struct ComplexEll {
 
 // ---------------------------------------------------------------------------- assembly
 // One thread per face: off-diagonals -(-e^{i theta})^N = -e^{i N (theta + pi)}, diagonal
-// count + 1e-9 (face_rosy_field.h:52-75).  No atomics: every row is written by its owner.
+// #neighbours + 1e-9 (face_rosy_field.h:52-75).  No atomics: every row is written by its owner.
+// Every row keeps the uniform diagonal 3 + 1e-9 of a closed mesh; a boundary side (nbr_in -1:
+// no neighbour, nothing in L, :64) becomes the entry -1 on the row's own column, so the row
+// applies (3 - #boundary sides + 1e-9) to its own value, the reference's diagonal.  The kernels
+// and the multigrid passes that factor A = d I + (ELL entries) then need no per-row diagonal.
 __global__ void field_assemble(int n, int N, const int* __restrict__ nbr_in, const double* __restrict__ theta,
                                const double* __restrict__ area, int* nbr, double2* v64, float2* v32,
                                double* d64, float* d32, double* inv64, float* inv32, float* area32) {
     for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < n; f += gridDim.x * blockDim.x) {
-        int cnt = 0;
         for (int j = 0; j < 3; j++) {
             int g = nbr_in[3 * f + j];
-            double s, c;
-            sincos((double)N * (theta[3 * f + j] + 3.14159265358979323846), &s, &c);
-            double2 a = make_double2(-c, -s);
+            double2 a;
+            if (g < 0) {
+                g = f;
+                a = make_double2(-1.0, 0.0);
+            } else {
+                double s, c;
+                sincos((double)N * (theta[3 * f + j] + 3.14159265358979323846), &s, &c);
+                a = make_double2(-c, -s);
+            }
             nbr[j * n + f] = g;
             v64[j * n + f] = a;
             v32[j * n + f] = make_float2((float)a.x, (float)a.y);
-            cnt++;
         }
-        double d = (double)cnt + 1e-9;
+        double d = 3.0 + 1e-9;
         d64[f] = d;
         d32[f] = (float)d;
         inv64[f] = 1.0 / d;
@@ -946,6 +954,7 @@ __global__ void adj_accumulate(ComplexEll<double> A, int N, const double2* __res
 #pragma unroll
         for (int j = 0; j < 3; j++) {
             const int g = A.nbr[j * n + f];
+            if (g == f) continue;   // a boundary side: no transport angle
             const double2 l = A.val[j * n + f], w = u[g];
             const double xr = s * w.x, xi = s * w.y;
             const double lr = l.x * xr - l.y * xi, li = l.x * xi + l.y * xr;   // L_fj x_g
@@ -1379,7 +1388,11 @@ int field_run(mtk_ctx* c, int32_t nF, int32_t nRosy, const int32_t* nbr_h, const
     if (!c || nF <= 0 || nRosy <= 0 || !nbr_h || !theta_h || !area_h || (!x0 && !rhs) || !out || n_iter < 0)
         return MTK_ERR_BAD_INPUT;
     for (int64_t i = 0; i < 3 * (int64_t)nF; i++)
-        if (nbr_h[i] < 0 || nbr_h[i] >= nF) { mtk_set_last_error("face neighbour out of range (closed meshes only)", __FILE__, __LINE__); return MTK_ERR_BAD_INPUT; }
+        if (nbr_h[i] < -1 || nbr_h[i] >= nF || nbr_h[i] == i / 3) {
+            mtk_set_last_error("face neighbour out of range (a face index other than its own, or -1 for a boundary side)",
+                               __FILE__, __LINE__);
+            return MTK_ERR_BAD_INPUT;
+        }
     mtk_solve_opts opts;
     mtk_default_opts(&opts);
     if (opts_in) opts = *opts_in;
@@ -1417,7 +1430,8 @@ int field_run(mtk_ctx* c, int32_t nF, int32_t nRosy, const int32_t* nbr_h, const
         for (int k = 0; k < n; k++) {
             const int f = S.perm[k];
             for (int j = 0; j < 3; j++) {
-                nbr_p[3 * (size_t)k + j] = inv[nbr_h[3 * (size_t)f + j]];
+                const int g = nbr_h[3 * (size_t)f + j];
+                nbr_p[3 * (size_t)k + j] = g < 0 ? -1 : inv[g];
                 theta_p[3 * (size_t)k + j] = theta_h[3 * (size_t)f + j];
             }
             area_p[k] = area_h[f];
@@ -1738,7 +1752,7 @@ extern "C" int mtk_field_spmv_bench(mtk_ctx* c, int32_t nF, int32_t nRosy, const
                                     double* ms_copy_same_bytes) {
     if (!c || nF <= 0 || !nbr_h || !theta_h || reps <= 0 || !ms_per_spmv || !bytes_per_spmv) return MTK_ERR_BAD_INPUT;
     for (int64_t i = 0; i < 3 * (int64_t)nF; i++)
-        if (nbr_h[i] < 0 || nbr_h[i] >= nF) return MTK_ERR_BAD_INPUT;
+        if (nbr_h[i] < -1 || nbr_h[i] >= nF || nbr_h[i] == i / 3) return MTK_ERR_BAD_INPUT;
     MTK_CUDA_TRY(cudaSetDevice(c->device));
     AllocStreamScope alloc_scope(c->stream);
     cudaStream_t st = c->stream;

@@ -17,10 +17,11 @@
 // each call, and calls that overlap on the GPU (two streams, two threads) race.  Each call
 // reads its status back and waits for its stream before it returns.
 //
-// Meshes are closed: every face has three neighbours, so the diagonal of L is 3 + 1e-9 in
-// every row (the reference's count of neighbours plus its shift).  A neighbour index outside
-// [0, nF) -- including -1, a boundary edge -- is found during assembly, the solve is skipped
-// and the call returns MTK_ERR_BAD_INPUT, as the regular entry point does.
+// A neighbour of -1 marks a boundary side (no entry in L).  As in the regular entry point every
+// row keeps the diagonal 3 + 1e-9 and a boundary side acts as the entry -1 on the row's own
+// column, so a row applies its count of neighbours + 1e-9 to its own value (the reference's
+// diagonal).  Any other neighbour index outside [0, nF), or a face's own index, is found during
+// assembly, the solve is skipped and the call returns MTK_ERR_BAD_INPUT.
 //
 // Algorithm: the same inverse power iteration as mtk_field_smoothest with the FP64 path
 // (assembly of the connection Laplacian, then n_iter steps of x = L^-1 M u solved by PCG to
@@ -80,7 +81,8 @@ __host__ __device__ inline Layout layout_of(unsigned char* base, int n) {
 }
 
 // val and x are written earlier in the same kernel, so they are read through L2 (__ldcg), not
-// the read-only path.  nbr has been range-checked by the assembly before any call.
+// the read-only path.  nbr has been range-checked by the assembly before any call; a boundary
+// side (-1) reads the row's own value with the entry -1 stored for it.
 __device__ __forceinline__ double2 row_apply(int i, int n, const int* __restrict__ nbr, const double2* val,
                                              double diag, const double2* x) {
     double2 xi = __ldcg(x + i);
@@ -88,6 +90,7 @@ __device__ __forceinline__ double2 row_apply(int i, int n, const int* __restrict
 #pragma unroll
     for (int j = 0; j < 3; j++) {
         int c = nbr[3 * i + j];
+        if (c < 0) c = i;
         double2 a = __ldcg(val + j * n + i);
         double2 xc = __ldcg(x + c);
         re += a.x * xc.x - a.y * xc.y;
@@ -104,7 +107,7 @@ __global__ void __launch_bounds__(kBlock) noalloc_power(unsigned char* base, int
     GridBarrier bar{L.bar, L.bar + 1, L.err};
     const int stride = gridDim.x * blockDim.x;
     const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
-    const double diag = 3.0 + 1e-9;   // three neighbours per face (closed mesh) + the 1e-9 shift
+    const double diag = 3.0 + 1e-9;   // three sides per face + the 1e-9 shift (boundary sides: entry -1)
     const int G = gridDim.x;
     int status = 0;
     long long total_it = 0;
@@ -112,7 +115,11 @@ __global__ void __launch_bounds__(kBlock) noalloc_power(unsigned char* base, int
     for (int f = t0; f < n; f += stride) {
         for (int j = 0; j < 3; j++) {
             const int g = nbr[3 * f + j];
-            if (g < 0 || g >= n) atomicExch(L.bad_nbr, 1);
+            if (g < -1 || g >= n || g == f) atomicExch(L.bad_nbr, 1);
+            if (g < 0) {
+                L.val[j * n + f] = make_double2(-1.0, 0.0);
+                continue;
+            }
             double s, c;
             sincos((double)N * (theta[3 * f + j] + 3.14159265358979323846), &s, &c);
             L.val[j * n + f] = make_double2(-c, -s);
@@ -293,6 +300,7 @@ extern "C" int mtk_field_smoothest_noalloc(int32_t nF, int32_t nRosy, const int3
     MTK_CUDA_TRY(cudaStreamSynchronize(st));
     if (iterations) *iterations = h_status[1];
     if (h_status[0] == MTK_ERR_BAD_INPUT)
-        mtk_set_last_error("mtk_field_smoothest_noalloc: a neighbour index is outside [0, nF)", __FILE__, __LINE__);
+        mtk_set_last_error("mtk_field_smoothest_noalloc: a neighbour index is outside [0, nF) (other than -1) or a "
+                           "face's own index", __FILE__, __LINE__);
     return h_status[0];
 }

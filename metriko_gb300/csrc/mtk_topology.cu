@@ -2,7 +2,8 @@
 //
 // Replaces the host loops of FaceRosyField::computeMatching(MatchingType::Curl):
 // computeConnection (face_rosy_field.h:109-117), cMatching (:169-202) and computeSingular
-// (:100-107), with one thread per edge and one per vertex, closed meshes.
+// (:100-107), with one thread per edge and one per vertex.  Boundary edges (a face slot of -1)
+// keep matching -1 and effort 0 (:121-122, :170); boundary vertices keep the index 1 (:101-102).
 //  * The face frame of f is rebuilt from its corners as in the Hmesh constructor (hmesh.h:461-474):
 //    bX = dir(p1 - p0), bY = dir(-(p1 - p0) x n), n = (p1 - p0) x (p2 - p0).
 //  * The field vectors are field(f, i) = e^{i arg(c_f) / N} e^{2 pi i i / N} (face_rosy_field.h:37-43).
@@ -10,17 +11,20 @@
 //    v = dir(edge vector), connection = (v.bX1 + i v.bY1) / (v.bX0 + i v.bY0);
 //    matching = the first i of least sum_j (v . (v1_{(i+j)%N} - v0_j))^2 (strict '<');
 //    effort = arg(prod_j field(f1, (j + i) % N) / (field(f0, j) connection)).
-//  * Per vertex: the ring from vert_half[v] by h <- twin(prev h) (twin h = h ^ 1), each
-//    halfedge adding -effort (the edge's canonical halfedge 2e) or +effort (its twin 2e + 1),
-//    singular = round((N angleDefect + sum) / 2 pi).
+//  * Per vertex: the ring from vert_half[v] by h <- twin(prev h), each halfedge adding -effort
+//    (the edge's canonical halfedge edge2half[e]) or +effort (its twin),
+//    singular = round((N angleDefect + sum) / 2 pi); a ring that meets a boundary halfedge (id
+//    >= 3 nF: boundary halfedges are numbered after the interior ones) marks a boundary vertex.
+//    A closed mesh may pass no halfedge arrays: its halfedges are 2e and 2e + 1 (twin h = h ^ 1).
 // The arithmetic is the host's, in the same order, up to the last-bit rounding of the device's
 // cos/sin/atan2/sqrt; the integer decisions are the host's (tested on every fixture and at the
 // 1.3M-face benchmark size).  A ring that does not close within kMaxRing halfedges sets the error
 // word and leaves that vertex's index at 0 (the call then fails with MTK_ERR_BAD_INPUT).
 //
 // Field inputs from the raw mesh on the device (mtk_mesh_field_inputs, mtk_field_smoothest_mesh):
-// the face across each face side, theta = heArgOnFace(h) - heArgOnFace(twin h) and the face
-// areas of the Hmesh constructor (hmesh.h:313-489) without building the halfedge mesh.  The face
+// the face across each face side (-1 on a boundary side, with theta 0), theta = heArgOnFace(h) -
+// heArgOnFace(twin h) and the face areas of the Hmesh constructor (hmesh.h:313-489) without
+// building the halfedge mesh.  The face
 // sides are paired through a hash table keyed by their sorted vertex pair; the face frames and
 // halfedge angles repeat the host's arithmetic in its order (no contraction into fused
 // multiply-adds), so area and the pairing are the host's bit for bit and theta differs from it
@@ -88,6 +92,11 @@ __global__ void curl_matching(int nE, int Nrt, const double* __restrict__ P, con
     const int N = NT > 0 ? NT : Nrt;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nE; e += gridDim.x * blockDim.x) {
         const int f0 = ef[2 * (size_t)e], f1 = ef[2 * (size_t)e + 1];
+        if (f0 < 0 || f1 < 0) {   // boundary edge
+            matching[e] = -1;
+            effort[e] = 0.0;
+            continue;
+        }
         const V3 v = vunit(vsub(vload(P, ev[2 * (size_t)e + 1]), vload(P, ev[2 * (size_t)e])));
         V3 bx0, by0, bx1, by1;
         face_frame(P, F, f0, bx0, by0);
@@ -122,23 +131,34 @@ __global__ void curl_matching(int nE, int Nrt, const double* __restrict__ P, con
     }
 }
 
-__global__ void singular_index(int nV, int N, const int* __restrict__ vert_half, const int* __restrict__ prev,
+// twin/hedge/e2h: the halfedge arrays of a mesh with boundary, or all null for the closed
+// numbering (halfedges 2e, 2e + 1); nI = 3 nF, the first boundary halfedge id
+__global__ void singular_index(int nV, int N, int nI, const int* __restrict__ vert_half, const int* __restrict__ prev,
+                               const int* __restrict__ twin, const int* __restrict__ hedge, const int* __restrict__ e2h,
                                const double* __restrict__ defect, const double* __restrict__ effort,
                                int* __restrict__ singular, int* err) {
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nV; v += gridDim.x * blockDim.x) {
         double sum = defect[v] * N;
         const int h0 = vert_half[v];
         int h = h0, steps = 0;
+        bool boundary = false;
         do {
-            sum += ((h & 1) ? 1.0 : -1.0) * effort[h >> 1];
-            h = prev[h] ^ 1;
+            if (twin) {
+                if (h >= nI) boundary = true;
+                const int e = hedge[h];
+                sum += (e2h[e] == h ? -1.0 : 1.0) * effort[e];
+                h = twin[prev[h]];
+            } else {
+                sum += ((h & 1) ? 1.0 : -1.0) * effort[h >> 1];
+                h = prev[h] ^ 1;
+            }
         } while (h != h0 && ++steps < kMaxRing);
         if (h != h0) {
             atomicExch(err, 1);
             singular[v] = 0;
             continue;
         }
-        singular[v] = (int)round(sum / kTwoPi);   // std::round: halves away from zero
+        singular[v] = boundary ? 1 : (int)round(sum / kTwoPi);   // std::round: halves away from zero
     }
 }
 
@@ -176,7 +196,7 @@ __global__ void sides_insert(int nF, const int* __restrict__ F, unsigned long lo
     }
 }
 
-// partner side of every side; err bit 2: an edge with one side (boundary), bit 4: two sides
+// partner side of every side (stays -1 for the one side of a boundary edge); err bit 4: two sides
 // running the same way (inconsistent orientation)
 __global__ void sides_pair(unsigned long long nslot, const int* __restrict__ F, const unsigned long long* __restrict__ keys,
                            const int* __restrict__ s0, const int* __restrict__ s1, int* partner, int* err) {
@@ -184,7 +204,7 @@ __global__ void sides_pair(unsigned long long nslot, const int* __restrict__ F, 
          h += (unsigned long long)gridDim.x * blockDim.x) {
         if (keys[h] == kEmpty) continue;
         const int a = s0[h], b = s1[h];
-        if (b < 0) { atomicOr(err, 2); continue; }
+        if (b < 0) continue;   // boundary edge
         const int fa = a / 3, ja = a - 3 * fa, fb = b / 3, jb = b - 3 * fb;
         const int ta = F[3 * (size_t)fa + ja], tb = F[3 * (size_t)fb + jb];
         if (ta == tb) atomicOr(err, 4);
@@ -233,6 +253,11 @@ __global__ void side_outputs(int nF, const int* __restrict__ partner, const doub
     const int ns = 3 * nF;
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
         const int t = partner[s];
+        if (t < 0) {   // boundary side: no neighbour (face_rosy_field.h:64)
+            nbr[s] = -1;
+            theta[s] = 0.0;
+            continue;
+        }
         nbr[s] = t / 3;
         theta[s] = __dsub_rn(farg[s], farg[t]);
     }
@@ -281,8 +306,7 @@ extern "C" int mtk_mesh_field_inputs(mtk_ctx* c, int32_t nV, int32_t nF, const d
     MTK_CUDA_TRY(cudaStreamSynchronize(st));
     c->kernels += 3;
     if (const int e = c->h_int[0]) {
-        mtk_set_last_error(e & 2   ? "mtk_mesh_field_inputs: boundary edge (closed meshes only)"
-                           : e & 1 ? "mtk_mesh_field_inputs: non-manifold edge (three or more faces)"
+        mtk_set_last_error(e & 1   ? "mtk_mesh_field_inputs: non-manifold edge (three or more faces)"
                            : e & 4 ? "mtk_mesh_field_inputs: inconsistently oriented faces"
                                    : "mtk_mesh_field_inputs: degenerate face side",
                            __FILE__, __LINE__);
@@ -310,7 +334,8 @@ extern "C" int mtk_field_smoothest_mesh(mtk_ctx* c, int32_t nV, int32_t nF, cons
 
 extern "C" int mtk_curl_matching(mtk_ctx* c, int32_t nV, int32_t nF, int32_t nE, int32_t N, const double* V,
                                  const int32_t* F, const int32_t* edge_vert, const int32_t* edge_face,
-                                 const int32_t* vert_half, const int32_t* prev_half, const double* angle_defect,
+                                 const int32_t* vert_half, const int32_t* prev_half, const int32_t* twin_half,
+                                 const int32_t* half_edge, const int32_t* edge_half, const double* angle_defect,
                                  const double* compressed, int32_t* matching, int32_t* singular) {
     if (!c || nV <= 0 || nF <= 0 || nE <= 0 || N < 1 || N > 8 || !V || !F || !edge_vert || !edge_face || !vert_half ||
         !prev_half || !angle_defect || !compressed || !matching || !singular)
@@ -320,20 +345,35 @@ extern "C" int mtk_curl_matching(mtk_ctx* c, int32_t nV, int32_t nF, int32_t nE,
         mtk_set_last_error(what, __FILE__, __LINE__);
         return MTK_ERR_BAD_INPUT;
     };
+    const bool general = twin_half != nullptr;
+    if (general != (half_edge != nullptr) || general != (edge_half != nullptr))
+        return bad("mtk_curl_matching: twin_half, half_edge and edge_half are given together or not at all");
+    if (3 * (int64_t)nF > nH) return bad("mtk_curl_matching: more face corners than halfedges");
     for (int64_t i = 0; i < 3 * (int64_t)nF; i++)
         if (F[i] < 0 || F[i] >= nV) return bad("mtk_curl_matching: face corner out of range");
     for (int64_t i = 0; i < nH; i++) {
         if (edge_vert[i] < 0 || edge_vert[i] >= nV) return bad("mtk_curl_matching: edge vertex out of range");
-        if (edge_face[i] < 0 || edge_face[i] >= nF) return bad("mtk_curl_matching: edge face out of range (closed meshes only)");
+        if (edge_face[i] < -1 || edge_face[i] >= nF || (!general && edge_face[i] < 0))
+            return bad("mtk_curl_matching: edge face out of range (-1 on a boundary edge needs the halfedge arrays)");
         if (prev_half[i] < 0 || prev_half[i] >= nH) return bad("mtk_curl_matching: prev halfedge out of range");
+        if (general && (twin_half[i] < 0 || twin_half[i] >= nH || half_edge[i] < 0 || half_edge[i] >= nE))
+            return bad("mtk_curl_matching: twin or edge of a halfedge out of range");
     }
+    if (general)
+        for (int i = 0; i < nE; i++)
+            if (edge_half[i] < 0 || edge_half[i] >= nH) return bad("mtk_curl_matching: edge halfedge out of range");
     for (int i = 0; i < nV; i++)
         if (vert_half[i] < 0 || vert_half[i] >= nH) return bad("mtk_curl_matching: vertex halfedge out of range");
     MTK_CUDA_TRY(cudaSetDevice(c->device));
     AllocStreamScope alloc_scope(c->stream);
     cudaStream_t st = c->stream;
     DBuf<double> dV, dc, ddef, deff;
-    DBuf<int> dF, dev, def, dvh, dprev, dm, ds;
+    DBuf<int> dF, dev, def, dvh, dprev, dm, ds, dtwin, dhe, de2h;
+    if (general) {
+        MTK_TRY(dtwin.upload(twin_half, (size_t)nH, st));
+        MTK_TRY(dhe.upload(half_edge, (size_t)nH, st));
+        MTK_TRY(de2h.upload(edge_half, (size_t)nE, st));
+    }
     MTK_TRY(dV.upload(V, 3 * (size_t)nV, st));
     MTK_TRY(dF.upload(F, 3 * (size_t)nF, st));
     MTK_TRY(dev.upload(edge_vert, (size_t)nH, st));
@@ -349,7 +389,9 @@ extern "C" int mtk_curl_matching(mtk_ctx* c, int32_t nV, int32_t nF, int32_t nE,
     const int G = stream_grid(c) * 4;
     auto kernel = N == 4 ? curl_matching<4> : curl_matching<0>;
     kernel<<<G, kStream, 0, st>>>(nE, N, dV.p, dF.p, dev.p, def.p, dc.p, dm.p, deff.p);
-    singular_index<<<G, kStream, 0, st>>>(nV, N, dvh.p, dprev.p, ddef.p, deff.p, ds.p, c->dev_err);
+    singular_index<<<G, kStream, 0, st>>>(nV, N, 3 * nF, dvh.p, dprev.p, general ? dtwin.p : nullptr,
+                                          general ? dhe.p : nullptr, general ? de2h.p : nullptr, ddef.p, deff.p, ds.p,
+                                          c->dev_err);
     c->kernels += 2;
     MTK_CUDA_TRY(cudaGetLastError());
     MTK_CUDA_TRY(cudaMemcpyAsync(matching, dm.p, sizeof(int) * nE, cudaMemcpyDeviceToHost, st));

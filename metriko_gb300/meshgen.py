@@ -17,6 +17,10 @@ dataset, so every workload here is generated from a seed:
                                      split into s^3 cells, each boundary square cut into two
                                      triangles (diagonal flipped with probability ``flip_p``),
                                      vertices jittered by N(0, jitter / s).
+* ``cap(level, zcut, sigma, seed)`` -- open disk: the faces of a level-k icosphere above
+                                     z = zcut, radial noise N(0, sigma) (one boundary loop).
+* ``cylinder(nu, nv, ...)``       -- open cylinder on a periodic-by-open grid (two boundary
+                                     loops), diagonals flipped at random, jittered.
 * ``workload(name)``               -- the named workloads (config sizes) used by tests/bench.
 
 Faces are consistently oriented with outward normals; vertex arrays are float64 (n x 3),
@@ -193,6 +197,66 @@ def holed_slab(g: int, s: int = 3, jitter: float = 0.05, flip_p: float = 0.5, se
     return V.astype(np.float64), F.astype(np.int32)
 
 
+def _compact(V, F):
+    """Drops the vertices no face uses and renumbers the rest in their original order."""
+    used = np.zeros(len(V), bool)
+    used[F.ravel()] = True
+    new = np.cumsum(used) - 1
+    return V[used], new[F].astype(np.int32)
+
+
+def _check_manifold_boundary(F):
+    """Every boundary vertex must lie on exactly two boundary edges (no two boundary loops
+    touching at a vertex), and every edge on at most two faces."""
+    e = np.concatenate([F[:, [0, 1]], F[:, [1, 2]], F[:, [2, 0]]])
+    key = np.sort(e, axis=1)
+    u, cnt = np.unique(key, axis=0, return_counts=True)
+    if cnt.max() > 2:
+        raise ValueError("edge on more than two faces")
+    bv = u[cnt == 1].ravel()
+    if len(bv):
+        vc = np.bincount(bv)
+        if vc[vc > 0].max() != 2 or vc[vc > 0].min() != 2:
+            raise ValueError("boundary loops touch at a vertex")
+
+
+def cap(level: int, zcut: float = -0.3, sigma: float = 0.01, seed: int = 0):
+    """Open surface with one boundary loop (a disk): the faces of a level-``level`` icosphere
+    whose three vertices lie above z = ``zcut``, each vertex displaced radially by N(0, sigma)."""
+    v, f = icosphere(level)
+    keep = (v[f][:, :, 2] > zcut).all(axis=1)
+    V, F = _compact(v, f[keep])
+    _check_manifold_boundary(F)
+    return radial_noise(V, sigma, seed), F
+
+
+def cylinder(nu: int, nv: int, r: float = 0.5, h: float = 1.0, flip_p: float = 0.5, jitter: float = 0.1,
+             seed: int = 0):
+    """Open cylinder (an annulus: two boundary loops) on an nu x nv grid, u around the axis
+    (periodic), v along it (nv + 1 rows of vertices); each quad's diagonal flipped with probability
+    ``flip_p``, interior vertices jittered by N(0, jitter * edge) in u and v."""
+    rng = np.random.default_rng(seed)
+    i, j = np.meshgrid(np.arange(nu), np.arange(nv + 1), indexing="ij")
+    ju = rng.normal(0.0, jitter, size=i.shape)
+    jv = rng.normal(0.0, jitter, size=j.shape)
+    jv[:, 0] = 0.0
+    jv[:, nv] = 0.0
+    u = 2.0 * np.pi * (i + ju) / nu
+    z = h * (j + jv) / nv
+    V = np.stack([r * np.cos(u), r * np.sin(u), z], axis=-1).reshape(-1, 3)
+    ii, jj = np.meshgrid(np.arange(nu), np.arange(nv), indexing="ij")
+    idx = lambda a, b: (a % nu) * (nv + 1) + b  # noqa: E731
+    a = idx(ii, jj).ravel()
+    b = idx(ii + 1, jj).ravel()
+    c = idx(ii + 1, jj + 1).ravel()
+    d = idx(ii, jj + 1).ravel()
+    flip = rng.random(a.shape) < flip_p
+    t0 = np.where(flip[:, None], np.stack([a, b, d], 1), np.stack([a, b, c], 1))
+    t1 = np.where(flip[:, None], np.stack([b, c, d], 1), np.stack([a, c, d], 1))
+    F = np.stack([t0, t1], axis=1).reshape(-1, 3)
+    return V, F.astype(np.int32)
+
+
 # Named workloads: (builder, grid ratio).  The ratio is RosyParameterization's `ratio`
 # argument (grid edge length = bbox diagonal * ratio / mean field norm).
 def workload(name: str, seed: int = 0):
@@ -219,6 +283,13 @@ def workload(name: str, seed: int = 0):
         nu, nv = (int(t) for t in name[6:].split("x"))
         v, f = torus(nu, nv, seed=seed)
         return v, f, 0.02, True
+    if name.startswith("cap") and name.endswith("_noise"):   # e.g. cap4_noise: open disk
+        v, f = cap(int(name[3:-6]), seed=seed)
+        return v, f, 0.03, False
+    if name.startswith("cyl_"):     # e.g. cyl_32x12: open cylinder (two boundary loops)
+        nu, nv = (int(t) for t in name[4:].split("x"))
+        v, f = cylinder(nu, nv, seed=seed)
+        return v, f, 0.03, True
     if name.startswith("genus"):    # e.g. genus2_s3: holed_slab(2, 3)
         g, sub = name[5:].split("_s")
         v, f = holed_slab(int(g), int(sub), seed=seed)

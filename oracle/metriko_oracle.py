@@ -47,7 +47,7 @@ Deliberate, documented choices (identical in the product path):
     and by the O(1 / penalty) residuals of already-integral values.  Every step where this pick
     differs from the strict '<' pick is recorded (info["strict_differs"]: step, distance gap,
     distance of the pick).
-Closed, consistently oriented, edge-manifold triangle meshes only.
+Consistently oriented, edge-manifold triangle meshes, closed or with boundary.
 
 Parity status: the reference cannot be compiled here (Eigen, libigl, SuiteSparse absent) and
 holds no tests or golden vectors, so this restatement is pinned only by the reference's own
@@ -90,8 +90,8 @@ def _normalized(a):
 # a1  mesh
 # --------------------------------------------------------------------------------------------
 def edge_topology(F):
-    """libigl v2.5.0 edge_topology: edges sorted by (min v, max v, face, corner);
-    EF[e,0] is the face in which the edge runs min->max."""
+    """libigl v2.5.0 edge_topology: edges sorted by (min v, max v, face, corner); EF[e,0] is the
+    face in which the edge runs min->max, -1 on the side of a boundary edge that has no face."""
     F = np.asarray(F, np.int64)
     nF = len(F)
     a = F.ravel()
@@ -108,22 +108,32 @@ def edge_topology(F):
     cnt = np.bincount(eid, minlength=nE)
     if cnt.max() > 2:
         raise ValueError("mesh is not edge-manifold")
-    if cnt.min() < 2:
-        raise ValueError("mesh has boundary edges (closed meshes only)")
     first = np.flatnonzero(new)
     FE = np.empty((nF, 3), np.int64)
     FE[f_s, l_s] = eid
     EV = np.stack([lo_s[first], hi_s[first]], 1)
-    EF = np.stack([f_s[first], f_s[first + 1]], 1)
-    # flip so that EF[e,0] holds the directed edge lo->hi
-    dir0 = a_s[first] == lo_s[first]
-    flip = ~dir0
+    two = cnt == 2
+    second = np.where(two, first + 1, first)
+    EF = np.stack([f_s[first], np.where(two, f_s[second], -1)], 1)
+    # flip so that EF[e,0] holds the directed edge lo->hi (a boundary edge whose only face runs
+    # hi->lo keeps that face in slot 1 and -1 in slot 0)
+    flip = a_s[first] != lo_s[first]
     EF[flip] = EF[flip][:, ::-1]
+    if (two & (EF[:, 0] == EF[:, 1])).any():
+        raise ValueError("degenerate edge")
+    if (two & (a_s[first] == a_s[second])).any():
+        raise ValueError("inconsistently oriented faces")
     return EV, FE, EF
 
 
 class Hmesh:
-    """Halfedge mesh with the reference's numbering (hmesh.h:313-569) for closed meshes."""
+    """Halfedge mesh with the reference's numbering (hmesh.h:240-311 dcel, :313-569), for
+    edge-manifold, consistently oriented meshes with or without boundary:
+      * interior halfedges are numbered in edge order, slot 0 before slot 1, each slot that has
+        a face (dcel, hmesh.h:254-258), so a closed mesh has 2e / 2e+1;
+      * boundary halfedges (face -1) follow from 3 nF on, loop by loop (hmesh.h:393-418): the
+        loops are found in the order of their first interior halfedge without a twin, and each
+        loop is walked backwards along the interior halfedges it borders."""
 
     def __init__(self, V, F):
         V = np.asarray(V, np.float64)
@@ -133,36 +143,87 @@ class Hmesh:
         nV, nF, nE = len(V), len(F), len(EV)
         self.nV, self.nF, self.nE, self.nH = nV, nF, nE, 2 * nE
         self.edge2vert, self.face2edge, self.edge2face = EV, FE, EF
-        ar = np.arange(nE)
-        # halfedge 2e: tail EV[e,0], face EF[e,0]; 2e+1: tail EV[e,1], face EF[e,1]
-        tail = np.empty(2 * nE, np.int64)
-        tail[0::2], tail[1::2] = EV[:, 0], EV[:, 1]
-        face = np.empty(2 * nE, np.int64)
-        face[0::2], face[1::2] = EF[:, 0], EF[:, 1]
-        twin = np.empty(2 * nE, np.int64)
-        twin[0::2], twin[1::2] = 2 * ar + 1, 2 * ar
-        edge = np.repeat(ar, 2)
+        nH, nI = 2 * nE, 3 * nF
+        valid = EF >= 0                               # (nE, 2)
+        EH = np.full((nE, 2), -1, np.int64)
+        EH[valid] = np.arange(int(valid.sum()))       # row-major: edge order, slot 0 first
+        if int(valid.sum()) != nI:
+            raise ValueError("mesh is not edge-manifold")
+        tail = np.full(nH, -1, np.int64)
+        face = np.full(nH, -1, np.int64)
+        edge = np.full(nH, -1, np.int64)
+        twin = np.full(nH, -1, np.int64)
+        for k in range(2):
+            ok = valid[:, k]
+            tail[EH[ok, k]] = EV[ok, k]
+            face[EH[ok, k]] = EF[ok, k]
+            edge[EH[ok, k]] = np.flatnonzero(ok)
+        both = valid[:, 0] & valid[:, 1]
+        twin[EH[both, 0]] = EH[both, 1]
+        twin[EH[both, 1]] = EH[both, 0]
         # FH[f,j]: the halfedge of face f on edge FE[f,j]
-        FH = 2 * FE + (EF[FE, 0] != np.arange(nF)[:, None])
-        nxt = np.empty(2 * nE, np.int64)
-        prv = np.empty(2 * nE, np.int64)
+        slot = (EF[FE, 0] != np.arange(nF)[:, None]).astype(np.int64)
+        FH = EH[FE, slot]
+        nxt = np.full(nH, -1, np.int64)
+        prv = np.full(nH, -1, np.int64)
         for j in range(3):
             nxt[FH[:, j]] = FH[:, (j + 1) % 3]
             prv[FH[:, (j + 1) % 3]] = FH[:, j]
-        # vert2half: dcel() writes in edge order, last write wins
-        emax = np.full(nV, -1, np.int64)
-        np.maximum.at(emax, EV[:, 0], ar)
-        np.maximum.at(emax, EV[:, 1], ar)
-        if (emax < 0).any():
+        # vert2half: dcel() writes in (edge, slot) order, last write wins = the largest interior
+        # halfedge id starting at the vertex
+        v2h = np.full(nV, -1, np.int64)
+        np.maximum.at(v2h, tail[:nI], np.arange(nI))
+        if (v2h < 0).any():
             raise ValueError("isolated vertex")
-        vert2half = 2 * emax + (EV[emax, 1] == np.arange(nV))
+        head = np.full(nH, -1, np.int64)
+        head[:nI] = tail[nxt[:nI]]
+        # boundary loops (hmesh.h:393-418)
+        loop2half = []
+        iB = nI
+        for iH in range(nI):
+            if twin[iH] != -1:
+                continue
+            jH, jB = iH, iB
+            done = False
+            while True:
+                tail[iB] = head[jH]
+                head[iB] = tail[jH]
+                edge[iB] = edge[jH]
+                prv[iB] = iB - 1
+                nxt[iB] = iB + 1
+                twin[jH], twin[iB] = iB, jH
+                jH = prv[jH]
+                while twin[jH] != -1:
+                    if jH == iH:
+                        done = True
+                        break
+                    jH = prv[twin[jH]]
+                if done:
+                    break
+                iB += 1
+            prv[jB] = iB
+            nxt[iB] = jB
+            loop2half.append(jB)
+            iB += 1
+        if iB != nH:
+            raise ValueError("mesh is not edge-manifold")
         self.tail, self.face, self.twin, self.edge = tail, face, twin, edge
-        self.next, self.prev = nxt, prv
-        self.head = tail[nxt]
+        self.next, self.prev, self.head = nxt, prv, head
         self.FH = FH
         self.face2half = FH[:, 0]
-        self.edge2half = 2 * ar
-        self.vert2half = vert2half
+        e2h = EH[:, 0].copy()
+        e2h[e2h < 0] = twin[EH[e2h < 0, 1]]
+        self.edge2half = e2h
+        self.vert2half = v2h
+        self.loop2half = np.asarray(loop2half, np.int64)
+        self.nL = len(loop2half)
+        isBE = (EF < 0).any(axis=1)
+        self.isBE = isBE
+        isBV = np.zeros(nV, bool)
+        isBV[EV[isBE, 0]] = True
+        isBV[EV[isBE, 1]] = True
+        self.isBV = isBV
+        self.is_boundary = bool(isBE.any())
         # face frames (hmesh.h:461-478)
         P0, P1, P2 = V[F[:, 0]], V[F[:, 1]], V[F[:, 2]]
         x = P1 - P0
@@ -172,10 +233,10 @@ class Hmesh:
         self.faceBasisY = _normalized(-np.cross(x, n))
         self.faceNormal = _normalized(n)
         self.faceArea = _norm3(n) * 0.5
-        # heArgOnFace (hmesh.h:480-489)
-        vec = V[self.head] - V[self.tail]
+        # heArgOnFace (hmesh.h:480-489); boundary halfedges are never written there (0 here)
+        vec = V[head] - V[tail]
         self.hvec = vec
-        farg = np.zeros(2 * nE)
+        farg = np.zeros(nH)
         s = np.zeros(nF)
         for j in range(3):
             h = FH[:, j]
@@ -185,12 +246,15 @@ class Hmesh:
             s = s + np.where(far, np.arccos(_dot3(v1, v2)), 0.0)
             farg[h] = s
         self.farg = farg
-        # angleDefect (hmesh.h:557-568): interior angle at tail(h) inside face(h)
-        h = np.arange(2 * nE)
+        # angleDefect (hmesh.h:557-568): the angle between each outgoing halfedge and the next one
+        # in ring order, summed in ccw order from vert2half (at a boundary vertex this includes
+        # the angle between its two boundary edges); 2 pi - sum inside, pi - sum on the boundary
+        h = np.arange(nH)
         ang = np.arccos(_dot3(_normalized(vec[h]), _normalized(vec[twin[prv[h]]])))
+        self.ring_angle = ang
         ssum = np.zeros(nV)
-        for v in range(nV):  # ccw order from vert2half, as the reference sums
-            h0 = vert2half[v]
+        for v in range(nV):
+            h0 = v2h[v]
             hh = h0
             acc = 0.0
             while True:
@@ -199,18 +263,18 @@ class Hmesh:
                 if hh == h0:
                     break
             ssum[v] = acc
-        self.angleDefect = TWO_PI - ssum
+        self.angleDefect = np.where(isBV, math.pi, TWO_PI) - ssum
 
     def is_canonical(self, h):
         return self.edge2half[self.edge[h]] == h
 
     def vertex_geometry(self):
-        """The rest of the reference's Hmesh constructor (hmesh.h:491-568) for a closed mesh:
-        vertex normals (area-weighted face normals accumulated face by face, then normalized),
-        vertex frames (x: the first outgoing edge projected to the tangent plane), dihedral angle
-        and cotangent per halfedge, edge cotangents, barycentric and circumcentric dual areas and
-        the halfedge angles around each vertex (running angle sum in ring order, rescaled to 2 pi).
-        Returns a dict with the reference's member names."""
+        """The rest of the reference's Hmesh constructor (hmesh.h:491-568): vertex normals
+        (area-weighted face normals accumulated face by face, then normalized), vertex frames (x:
+        the first outgoing edge projected to the tangent plane), dihedral angle (0 on boundary
+        edges) and cotangent per halfedge (0 on boundary halfedges), edge cotangents, barycentric
+        and circumcentric dual areas and the halfedge angles around each vertex (running angle sum
+        in ring order, rescaled to 2 pi).  Returns a dict with the reference's member names."""
         V, F = self.pos, self.idx
         nV, nH = self.nV, self.nH
         vn = np.zeros((nV, 3))
@@ -222,21 +286,27 @@ class Hmesh:
         d = V[self.head[self.vert2half]] - V
         x = _normalized(d - _dot3(d, vn)[:, None] * vn)
         vec = self.hvec
-        n1, n2 = self.faceNormal[self.face], self.faceNormal[self.face[self.twin]]
+        bnd_h = self.face < 0
+        bnd_e = self.isBE[self.edge]
+        fh = np.where(bnd_h, 0, self.face)
+        ft = np.where(bnd_h[self.twin], 0, self.face[self.twin])
+        n1, n2 = self.faceNormal[fh], self.faceNormal[ft]
         v = vec / _norm3(vec)[:, None]
-        dih = np.arctan2(_dot3(v, np.cross(n1, n2)), _dot3(n1, n2))
+        dih = np.where(bnd_e, 0.0, np.arctan2(_dot3(v, np.cross(n1, n2)), _dot3(n1, n2)))
         vnx = vec[self.next]
         vpr = -vec[self.prev]
-        cot = _dot3(vpr, vnx) / _norm3(np.cross(vpr, vnx))
+        with np.errstate(invalid="ignore", divide="ignore"):
+            cot = np.where(bnd_h, 0.0, _dot3(vpr, vnx) / _norm3(np.cross(vpr, vnx)))
         ecot = (cot[self.edge2half] + cot[self.twin[self.edge2half]]) * 0.5
         bary, circ, varg = np.zeros(nV), np.zeros(nV), np.zeros(nH)
         sq = _dot3(vec, vec)
-        ang = np.arccos(_dot3(_normalized(vec), _normalized(vec[self.twin[self.prev]])))
+        ang = self.ring_angle
         for u in range(nV):
             a1 = a2 = s = 0.0
             ring = self.ccw(self.vert2half[u])
             for h in ring:
-                a1 += self.faceArea[self.face[h]]
+                if self.face[h] >= 0:
+                    a1 += self.faceArea[self.face[h]]
                 a2 += cot[h] * sq[h]
                 a2 += cot[self.prev[h]] * sq[self.prev[h]]
                 varg[h] = s
@@ -249,7 +319,8 @@ class Hmesh:
                     angleDefect=self.angleDefect)
 
     def ccw(self, h0):
-        """Outgoing halfedges around tail(h0), ccw (AdjVH with ccw=true)."""
+        """Outgoing halfedges around tail(h0), ccw (AdjVH with ccw=true); includes the boundary
+        halfedge of a boundary vertex."""
         out, h = [], h0
         while True:
             out.append(h)
@@ -270,7 +341,8 @@ class Hmesh:
 # a2-a5  smoothest N-RoSy field
 # --------------------------------------------------------------------------------------------
 def connection_laplacian(m: Hmesh, N: int):
-    """face_rosy_field.h:46-76: L_ff = #interior neighbours + 1e-9, L_fg = -r_twin^N."""
+    """face_rosy_field.h:46-76: L_ff = #interior neighbours + 1e-9, L_fg = -r_twin^N; a face side
+    on the boundary adds nothing (:64)."""
     h1 = m.edge2half
     h2 = m.twin[h1]
     v1 = np.exp(1j * m.farg[h1])
@@ -283,10 +355,12 @@ def connection_laplacian(m: Hmesh, N: int):
     for j in range(3):
         h = m.FH[:, j]
         t = m.twin[h]
-        rr = transport[t]
-        rows += [np.arange(m.nF), np.arange(m.nF)]
-        cols += [np.arange(m.nF), m.face[t]]
-        vals += [np.ones(m.nF, np.complex128), -np.exp(N * np.log(rr))]
+        inner = m.face[t] >= 0
+        fi = np.flatnonzero(inner)
+        rr = transport[t[inner]]
+        rows += [fi, fi]
+        cols += [fi, m.face[t[inner]]]
+        vals += [np.ones(len(fi), np.complex128), -np.exp(N * np.log(rr))]
     L = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
                       shape=(m.nF, m.nF))
     L = L + 1e-9 * sp.identity(m.nF, dtype=np.complex128, format="csr")
@@ -347,20 +421,30 @@ def rosy_from_compressed(c, N):
 # --------------------------------------------------------------------------------------------
 # a6  matching and singularities
 # --------------------------------------------------------------------------------------------
+def _interior_faces(m: Hmesh):
+    """edge2face with the -1 of boundary edges replaced by 0 (their values are discarded)."""
+    f0, f1 = m.edge2face[:, 0].copy(), m.edge2face[:, 1].copy()
+    f0[f0 < 0] = 0
+    f1[f1 < 0] = 0
+    return f0, f1
+
+
 def compute_connection(m: Hmesh):
+    """face_rosy_field.h:109-117; 0 on boundary edges."""
     h = m.edge2half
     v = _normalized(m.hvec[h])
-    f0, f1 = m.edge2face[:, 0], m.edge2face[:, 1]
+    f0, f1 = _interior_faces(m)
     ef = _dot3(v, m.faceBasisX[f0]) + 1j * _dot3(v, m.faceBasisY[f0])
     eg = _dot3(v, m.faceBasisX[f1]) + 1j * _dot3(v, m.faceBasisY[f1])
-    return eg / ef
+    return np.where(m.isBE, 0.0, eg / ef)
 
 
 def c_matching(m: Hmesh, field, conn, N):
-    """face_rosy_field.h:169-202 (MatchingType::Curl)."""
+    """face_rosy_field.h:169-202 (MatchingType::Curl), interior edges only: a boundary edge keeps
+    matching -1 (:121) and effort 0 (:122)."""
     h = m.edge2half
     v = _normalized(m.hvec[h])
-    f0, f1 = m.edge2face[:, 0], m.edge2face[:, 1]
+    f0, f1 = _interior_faces(m)
     bx0, by0, bx1, by1 = m.faceBasisX[f0], m.faceBasisY[f0], m.faceBasisX[f1], m.faceBasisY[f1]
     best = np.full(m.nE, 32767000.0)
     iM = np.zeros(m.nE, np.int64)
@@ -380,13 +464,15 @@ def c_matching(m: Hmesh, field, conn, N):
     for i in range(N):
         a0 = field[f0, i]
         a1 = field[f1, (i + iM) % N]
-        coef = coef * (a1 / (a0 * conn))
-    effort = np.angle(coef)
+        with np.errstate(invalid="ignore", divide="ignore"):
+            coef = coef * (a1 / (a0 * conn))
+    effort = np.where(m.isBE, 0.0, np.angle(coef))
+    iM = np.where(m.isBE, -1, iM)
     return iM, effort
 
 
 def compute_singular(m: Hmesh, effort, N):
-    """face_rosy_field.h:100-107."""
+    """face_rosy_field.h:100-107: boundary vertices keep the initial 1 (:101-102)."""
     h = np.arange(m.nH)
     sgn = np.where(m.is_canonical(h), -1.0, 1.0)
     contrib = sgn * effort[m.edge[h]]
@@ -397,14 +483,15 @@ def compute_singular(m: Hmesh, effort, N):
         for hh in m.ccw(m.vert2half[v]):
             t += contrib[hh]
         acc[v] = t
-    return cround(acc / TWO_PI).astype(np.int64)
+    return np.where(m.isBV, 1, cround(acc / TWO_PI)).astype(np.int64)
 
 
 # --------------------------------------------------------------------------------------------
 # a7  seams: libigl cut_mesh_from_singularities + dijkstra, then singularity paths
 # --------------------------------------------------------------------------------------------
 def triangle_triangle_adjacency(m: Hmesh):
-    F = m.idx
+    """libigl triangle_triangle_adjacency: TT(f,s) the face across side s, TTi(f,s) that side's
+    slot in TT(f,s); both -1 on a boundary side."""
     TT = np.empty((m.nF, 3), np.int64)
     TTi = np.empty((m.nF, 3), np.int64)
     for j in range(3):
@@ -413,15 +500,17 @@ def triangle_triangle_adjacency(m: Hmesh):
         g = m.face[t]
         TT[:, j] = g
         # local index of twin halfedge inside g
-        loc = np.argmax(m.FH[g] == t[:, None], axis=1)
-        TTi[:, j] = loc
+        loc = np.argmax(m.FH[np.maximum(g, 0)] == t[:, None], axis=1)
+        TTi[:, j] = np.where(g < 0, -1, loc)
     return TT, TTi
 
 
 def cut_mesh_from_singularities_zero(m: Hmesh, TT, TTi):
     """libigl MeshCutter with an all-zero matching: BFS flood fill from face 0 marks the dual
-    spanning tree; Retract() dissolves seam edges with a degree-1 endpoint, scanning faces in
-    order, pass after pass, at most 10001 passes (guard > 10000)."""
+    spanning tree (a boundary side stays a seam); Retract() counts each seam edge once (from the
+    face with the larger id, boundary sides from their one face) and dissolves seam edges with a
+    degree-1 endpoint, scanning faces in order, pass after pass, at most 10001 passes
+    (guard > 10000)."""
     F = m.idx
     nF = m.nF
     seams = np.ones((nF, 3), bool)
@@ -554,6 +643,10 @@ def compute_seam(m: Hmesh, singular):
                 if (a == v0 and b == v1) or (a == v1 and b == v0):
                     jj = z
             cuts[fi, jj] = True
+            # a path never runs along a boundary edge: every boundary vertex is on the cut
+            # (boundary sides stay seams in the spanning cut) and the search stops at the first
+            # cut vertex it reaches
+            assert TT[fi, jj] >= 0
             cuts[TT[fi, jj], TTi[fi, jj]] = True
     seam = np.zeros(m.nE, bool)
     fs, js = np.nonzero(cuts)
@@ -565,7 +658,7 @@ def compute_seam(m: Hmesh, singular):
 # a8  combing and extrinsic field
 # --------------------------------------------------------------------------------------------
 def combed_field(m: Hmesh, field, matching, seam, N):
-    """face_rosy_field.h:207-249."""
+    """face_rosy_field.h:207-249 (boundary edges are not crossed, and keep matching -1)."""
     nF = m.nF
     out = np.zeros_like(field)
     turns = np.zeros(nF, np.int64)
@@ -587,9 +680,10 @@ def combed_field(m: Hmesh, field, matching, seam, N):
             fn = m.edge2face[e, 1] if b else m.edge2face[e, 0]
             n = (1 if b else -1) * matching[e]
             n = (n + mm + 1000 * N) % N
-            if not visit[fn] and not seam[e]:
+            if not m.isBE[e] and not visit[fn] and not seam[e]:
                 q.append((fn, n))
-    newm = (turns[m.edge2face[:, 0]] - turns[m.edge2face[:, 1]] + matching + 1000 * N) % N
+    f0, f1 = _interior_faces(m)
+    newm = np.where(m.isBE, -1, (turns[f0] - turns[f1] + matching + 1000 * N) % N)
     return out, newm
 
 
@@ -607,8 +701,18 @@ def extrinsic_field(m: Hmesh, field):
 # a9  cut mesh
 # --------------------------------------------------------------------------------------------
 def first_seam_he(m: Hmesh, seam, v):
+    """parameterization.h:81 (find_first_seam_he)."""
     for h in m.cw(m.vert2half[v]):
         if seam[m.edge[h]]:
+            return h
+    return m.vert2half[v]
+
+
+def first_bndr_he(m: Hmesh, v):
+    """parameterization.h:82 (find_first_bndr_he): the first halfedge in cw order from
+    vert2half on a boundary edge, else vert2half."""
+    for h in m.cw(m.vert2half[v]):
+        if m.isBE[m.edge[h]]:
             return h
     return m.vert2half[v]
 
@@ -619,8 +723,10 @@ def cut_mesh(m: Hmesh, seam):
     cutF = np.empty_like(F)
     cut2pos = []
     for v in range(m.nV):
-        bgn = first_seam_he(m, seam, v)
+        bgn = first_bndr_he(m, v) if m.isBV[v] else first_seam_he(m, seam, v)
         for h in m.ccw(bgn):
+            if m.face[h] < 0:
+                continue
             if seam[m.edge[h]] or h == bgn:
                 cut2pos.append(v)
             f = m.face[h]
@@ -634,26 +740,26 @@ def cut_mesh(m: Hmesh, seam):
 # a10-a11  transitions, matchings, setup
 # --------------------------------------------------------------------------------------------
 def he2transidx(m: Hmesh, seam, singular):
-    """parameterization_setup.ipp:11-50 (closed meshes)."""
+    """parameterization_setup.ipp:11-50."""
     valence = np.zeros(m.nV, np.int64)
     np.add.at(valence, m.edge2vert[seam, 0], 1)
     np.add.at(valence, m.edge2vert[seam, 1], 1)
-    inside_sing = singular != 0
+    inside_sing = (singular != 0) & ~m.isBV          # is_inside_singular (parameterization.h:80)
     hti = np.full(m.nH, 32767, np.int64)
     claimed = np.zeros(m.nE, bool)
     tid = 1
     for v in range(m.nV):
         if (valence[v] == 2 and not inside_sing[v]) or valence[v] == 0:
             continue
-        for cH in m.ccw(m.vert2half[v]):
+        for cH in m.ccw(first_bndr_he(m, v)):
             cE = m.edge[cH]
-            if not seam[cE] or claimed[cE]:
+            if m.isBE[cE] or not seam[cE] or claimed[cE]:
                 continue
             hti[cH] = tid
             hti[m.twin[cH]] = -tid
             claimed[cE] = True
             jv = m.head[cH]
-            while valence[jv] == 2 and not inside_sing[jv]:
+            while valence[jv] == 2 and not inside_sing[jv] and not m.isBV[jv]:
                 nh = None
                 for h in m.ccw(m.vert2half[jv]):
                     if seam[m.edge[h]] and not claimed[m.edge[h]]:
@@ -681,7 +787,7 @@ def setup(m: Hmesh, cutF, n_cut, seam, singular, matching, N=4):
     hem = he2matching(m, matching, N)
     nV = m.nV
     nR = nV + nT
-    inside_sing = singular != 0
+    inside_sing = (singular != 0) & ~m.isBV
     nS = int(inside_sing.sum())
     unit = np.zeros((N, N), np.int64)
     for i in range(N):
@@ -705,7 +811,10 @@ def setup(m: Hmesh, cutF, n_cut, seam, singular, matching, N=4):
         pm = [I.copy()]
         pidx = [v]
         iv = -1
-        for h in m.ccw(first_seam_he(m, seam, v)):
+        bgn = first_bndr_he(m, v) if m.isBV[v] else first_seam_he(m, seam, v)
+        for h in m.ccw(bgn):
+            if m.face[h] < 0:
+                break                      # the boundary halfedge ends the fan (setup.ipp:77)
             f = m.face[h]
             jv = -1
             for j in range(3):
@@ -716,7 +825,7 @@ def setup(m: Hmesh, cutF, n_cut, seam, singular, matching, N=4):
                 for k in range(len(pidx)):
                     block(vr, vc, vv, pm[k], N * iv, N * pidx[k])
             hn = m.twin[m.prev[h]]
-            if seam[m.edge[hn]]:
+            if m.face[hn] >= 0 and seam[m.edge[hn]]:
                 p = perms[hem[hn]]
                 t = hti[hn]
                 if t > 0:
@@ -727,6 +836,8 @@ def setup(m: Hmesh, cutF, n_cut, seam, singular, matching, N=4):
                     pm.append(-I)
                     pidx.append(nV - t - 1)
                     pm = [p @ x for x in pm]
+        if m.isBV[v]:
+            continue                       # no constraint on a boundary vertex (setup.ipp:105)
         idcs = sorted(set(pidx))
         mats = []
         for j in idcs:

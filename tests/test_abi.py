@@ -51,12 +51,18 @@ def test_seeded_init_matches_oracle(seed):
     assert np.abs(a.real).max() <= 1 and np.abs(a.imag).max() <= 1
 
 
-def test_topology_rejects_open_mesh():
-    V = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], float)
-    F = np.array([[0, 1, 2]], np.int32)
+def test_topology_rejects_inconsistent_orientation():
+    """Two faces that run along their shared edge the same way (one face flipped) cannot be given
+    the reference's halfedge numbering: MTK_ERR_BAD_INPUT with a message.  A single triangle, all
+    boundary, is a valid open mesh."""
+    V = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [1, 1, 0]], float)
+    F = np.array([[0, 1, 2], [1, 2, 3]], np.int32)
     with pytest.raises(M.MetrikoError) as e:
-        M.topology_from_field(V, F, np.ones(1, complex))
+        M.topology_from_field(V, F, np.ones(2, complex))
     assert e.value.status == _lib.BAD_INPUT
+    assert "oriented" in str(e.value)
+    res = M.topology_from_field(V[:3], F[:1], np.ones(1, complex))
+    assert list(res["singular"]) == [1, 1, 1] and res["seam"].all() and res["counts"]["nCut"] == 3
 
 
 def test_topology_rejects_bad_index():
