@@ -223,13 +223,13 @@ def pipeline(ctx: Context, V, F, ratio=0.02, seed=0, round_seams=False, seamless
     V = np.ascontiguousarray(V, np.float64)
     F = np.ascontiguousarray(F, np.int32)
     nV, nF = len(V), len(F)
-    nE = num_edges(F)
+    nE = 3 * nF          # bound on the edge count; the outputs are cut to counts["nE"]
     singular = np.zeros(nV, np.int32)
     matching = np.zeros(nE, np.int32)
     seam = np.zeros(nE, np.uint8)
     compressed = np.zeros(2 * nF)
     cfn = np.zeros(nF * 12)
-    cap = 2 * (nV + 4 * nE) + 16
+    cap = 2 * (nV + nE) + 16                      # n (nV + nT) full variables, nT <= nE
     fullx = np.zeros(cap)
     xnaive = np.zeros(cap)
     fix_cap = 2 * (nV + nE) + 16
@@ -249,7 +249,8 @@ def pipeline(ctx: Context, V, F, ratio=0.02, seed=0, round_seams=False, seamless
     if check and status not in (OK, ROUNDING):
         _check(status, "mtk_pipeline_run")
     nfull, nfix = n_full.value, n_fixed.value
-    return dict(status=status, singular=singular, matching=matching, seam=seam.astype(bool),
+    ne = int(counts[1])
+    return dict(status=status, singular=singular, matching=matching[:ne].copy(), seam=seam[:ne].astype(bool),
                 compressed=compressed[0::2] + 1j * compressed[1::2], cfn=cfn.reshape(nF, 12),
                 fullx=fullx[:nfull].copy(), x_naive=xnaive[:nfull].copy(),
                 fix_order=fix_order[:nfix].copy(), fix_vals=fix_vals[:nfix].copy(),
@@ -375,8 +376,7 @@ def size_field_gradient(ctx: Context, V, F, s, T=None, mu=0.0, ratio=0.02, seed=
         if T.size != 8 * nF:
             raise ValueError("T must have 8 values per face")
         Tp = _ptr(T)
-    nE = num_edges(F)
-    cap = 2 * (nV + 4 * nE) + 16
+    cap = 2 * (nV + 3 * nF) + 16                  # n (nV + nT) full variables, nT <= nE <= 3 nF
     fullx = np.zeros(cap)
     grad = np.zeros(nV)
     loss = C.c_double(0)
@@ -400,8 +400,7 @@ def position_gradient(ctx: Context, V, F, s, mu=0.0, ratio=0.02, seed=0, round_s
     s = np.ascontiguousarray(s, np.float64)
     if s.shape != (nV,):
         raise ValueError("s must have one value per vertex")
-    nE = num_edges(F)
-    cap = 2 * (nV + 4 * nE) + 16
+    cap = 2 * (nV + 3 * nF) + 16                  # n (nV + nT) full variables, nT <= nE <= 3 nF
     fullx = np.zeros(cap)
     grad_s = np.zeros(nV)
     grad_V = np.zeros((nV, 3))
@@ -559,7 +558,7 @@ def topology_from_field(V, F, compressed, ratio=0.02, round_seams=False):
     V = np.ascontiguousarray(V, np.float64)
     F = np.ascontiguousarray(F, np.int32)
     nV, nF = len(V), len(F)
-    nE = num_edges(F)
+    nE = 3 * nF          # bound on the edge count; the outputs are cut to counts["nE"]
     c = np.empty(2 * nF)
     c[0::2], c[1::2] = np.real(compressed), np.imag(compressed)
     singular = np.zeros(nV, np.int32)
@@ -571,6 +570,7 @@ def topology_from_field(V, F, compressed, ratio=0.02, round_seams=False):
     _check(lib().mtk_topology_from_field(nV, nF, _ptr(V), _ptr(F), _ptr(c), ratio, int(round_seams),
                                          _ptr(singular), _ptr(matching), _ptr(seam), _ptr(cutF), _ptr(counts),
                                          C.byref(length)), "mtk_topology_from_field")
-    return dict(singular=singular, matching=matching, seam=seam.astype(bool), cutF=cutF.reshape(nF, 3),
+    ne = int(counts[1])
+    return dict(singular=singular, matching=matching[:ne].copy(), seam=seam[:ne].astype(bool), cutF=cutF.reshape(nF, 3),
                 counts=dict(zip(["nV", "nE", "nCut", "nT", "nS", "nJ", "nZ", "nFull"], counts.tolist())),
                 length=length.value)

@@ -1491,6 +1491,19 @@ int field_run(mtk_ctx* c, int32_t nF, int32_t nRosy, const int32_t* nbr_h, const
         MTK_TRY(sall.alloc((size_t)n_iter + 1));
         MTK_CUDA_TRY(cudaMemcpyAsync(Uall.p, S.ringU[0].p, sizeof(double2) * n, cudaMemcpyDeviceToDevice, st));
     }
+    // FP32 refinement cannot converge on a near-singular operator: on a flat or developable open
+    // patch a parallel field has zero Dirichlet energy, so L's smallest eigenvalue is the 1e-9
+    // shift (condition ~6e9, which FP32 drops from the operator entirely).  A solve whose FP32
+    // refinement stops reducing the FP64 residual (or runs out of refinements) continues in
+    // FP64 PCG from its current iterate, and the rest of the run stays in FP64.  There the solve
+    // stops on the recursive residual; the true residual is bounded by about cond(L) * eps.
+    bool fallback64 = false;
+    auto alloc64 = [&]() -> int {
+        if (S.z64.p) return MTK_OK;
+        MTK_TRY(S.z64.alloc(n)); MTK_TRY(S.p64.alloc(n)); MTK_TRY(S.q64.alloc(n));
+        if (S.amg) { MTK_TRY(S.rb64.alloc(n)); MTK_TRY(S.pb64.alloc(n)); MTK_TRY(S.sv64.alloc(n)); MTK_TRY(S.vv64.alloc(n)); }
+        return MTK_OK;
+    };
     // one solve L x = b from the current x / r (S.b, S.x, S.r, and S.r32 when MIXED) to the
     // relative residual tol: FP64 PCG, or FP32 PCG inside FP64 refinement; rr in: the start
     // residual |r|^2, out: the final one
@@ -1498,23 +1511,11 @@ int field_run(mtk_ctx* c, int32_t nF, int32_t nRosy, const int32_t* nbr_h, const
         const double goal2 = tol * tol * bnorm2;
         solves++;
         refines++;
-        if (!mixed) {
-            double frr = 0;
-            int s = S.pcg<double, double2>(S.A64(), S.inv64.p, S.b.p, S.x.p, S.r.p, S.z64.p, S.p64.p, S.q64.p, S.rb64.p,
-                                           S.pb64.p, S.sv64.p, S.vv64.p, goal2,
-                                           opts.max_iter, &iters, &frr);
-            if (s != MTK_OK) return s;
-            // true FP64 residual of the result
-            residual64<<<G, kStream, 0, st>>>(S.A64(), S.b.p, S.x.p, S.r.p, nullptr, c->partials);
-            c->kernels++;
-            MTK_TRY(S.finalize(G, 1));
-            MTK_TRY(S.read_scalars(1));
-            rr = c->h_scalars[0];
-            refines++;
-        } else {
+        if (mixed && !fallback64) {
             int outer = 0;
+            bool stalled = false;
             while (rr > goal2) {
-                if (outer >= opts.max_refine) return MTK_ERR_NOT_CONVERGED;
+                if (outer >= opts.max_refine) { stalled = true; break; }
                 outer++;
                 // inner FP32 solve L e = r to inner_tol relative (at least the outer goal)
                 double itol = opts.inner_tol;
@@ -1536,7 +1537,7 @@ int field_run(mtk_ctx* c, int32_t nF, int32_t nRosy, const int32_t* nbr_h, const
                             iters - it0, frr, itol * itol * rr, rr);
                 // an FP32 breakdown (p^H A p <= 0 in single precision) means the inner solve has
                 // stagnated: its last iterate is still a valid correction, and the FP64 refinement
-                // decides what comes next (bounded by max_refine, stopped when it makes no progress)
+                // decides what comes next
                 if (s == MTK_ERR_TIMEOUT) return s;
                 const double rr_prev = rr;
                 add_correction<<<G, kStream, 0, st>>>(n, S.e32.p, S.x.p);
@@ -1547,9 +1548,27 @@ int field_run(mtk_ctx* c, int32_t nF, int32_t nRosy, const int32_t* nbr_h, const
                 rr = c->h_scalars[0];
                 refines++;
                 if (!(rr == rr)) return MTK_ERR_BREAKDOWN;
-                if (rr > goal2 && rr >= rr_prev) return MTK_ERR_NOT_CONVERGED;
+                if (rr > goal2 && rr >= rr_prev) { stalled = true; break; }
                 if (s == MTK_OK && rr_prev > 0) floor_rel[ki] = std::sqrt(std::max(rr - frr, 0.0) / rr_prev);
             }
+            if (!stalled) return MTK_OK;
+            fallback64 = true;
+            if (debug) fprintf(stderr, "[field] FP32 refinement stalled at %.3e: FP64 PCG from here on\n", std::sqrt(rr / bnorm2));
+            MTK_TRY(alloc64());
+        }
+        {
+            double frr = 0;
+            int s = S.pcg<double, double2>(S.A64(), S.inv64.p, S.b.p, S.x.p, S.r.p, S.z64.p, S.p64.p, S.q64.p, S.rb64.p,
+                                           S.pb64.p, S.sv64.p, S.vv64.p, goal2,
+                                           opts.max_iter, &iters, &frr);
+            if (s != MTK_OK) return s;
+            // true FP64 residual of the result
+            residual64<<<G, kStream, 0, st>>>(S.A64(), S.b.p, S.x.p, S.r.p, nullptr, c->partials);
+            c->kernels++;
+            MTK_TRY(S.finalize(G, 1));
+            MTK_TRY(S.read_scalars(1));
+            rr = c->h_scalars[0];
+            refines++;
         }
         return MTK_OK;
     };
@@ -1620,7 +1639,13 @@ int field_run(mtk_ctx* c, int32_t nF, int32_t nRosy, const int32_t* nbr_h, const
             return MTK_ERR_BREAKDOWN;
         }
         const double start_rel = bnorm2 > 0 ? std::sqrt(rr / bnorm2) : 0.0;
-        MTK_TRY(solve_to_goal(bnorm2, rr));
+        if (const int s2 = solve_to_goal(bnorm2, rr); s2 != MTK_OK) {
+            if (s2 == MTK_ERR_NOT_CONVERGED)
+                mtk_set_last_error("field solve: PCG reached its iteration cap (max_iter)", __FILE__, __LINE__);
+            else if (s2 == MTK_ERR_BREAKDOWN)
+                mtk_set_last_error("field solve: PCG breakdown (p^H L p <= 0 or NaN)", __FILE__, __LINE__);
+            return s2;
+        }
         double rel = bnorm2 > 0 ? std::sqrt(rr / bnorm2) : 0.0;
         if (rel > worst) worst = rel;
         if (debug)

@@ -17,8 +17,9 @@ dataset, so every workload here is generated from a seed:
                                      split into s^3 cells, each boundary square cut into two
                                      triangles (diagonal flipped with probability ``flip_p``),
                                      vertices jittered by N(0, jitter / s).
-* ``cap(level, zcut, sigma, seed)`` -- open disk: the faces of a level-k icosphere above
-                                     z = zcut, radial noise N(0, sigma) (one boundary loop).
+* ``cap(level, zcut, sigma, seed, sh)`` -- open disk: the faces of a level-k icosphere above
+                                     z = zcut, radial noise N(0, sigma) or the degree-8
+                                     spherical-harmonic radius (one boundary loop).
 * ``cylinder(nu, nv, ...)``       -- open cylinder on a periodic-by-open grid (two boundary
                                      loops), diagonals flipped at random, jittered.
 * ``workload(name)``               -- the named workloads (config sizes) used by tests/bench.
@@ -220,13 +221,16 @@ def _check_manifold_boundary(F):
             raise ValueError("boundary loops touch at a vertex")
 
 
-def cap(level: int, zcut: float = -0.3, sigma: float = 0.01, seed: int = 0):
+def cap(level: int, zcut: float = -0.3, sigma: float = 0.01, seed: int = 0, sh: bool = False):
     """Open surface with one boundary loop (a disk): the faces of a level-``level`` icosphere
-    whose three vertices lie above z = ``zcut``, each vertex displaced radially by N(0, sigma)."""
+    whose three vertices lie above z = ``zcut``, each vertex displaced radially by N(0, sigma), or
+    with ``sh`` by the degree-8 spherical-harmonic radius of ``sh_displace`` (scale 0.05)."""
     v, f = icosphere(level)
     keep = (v[f][:, :, 2] > zcut).all(axis=1)
     V, F = _compact(v, f[keep])
     _check_manifold_boundary(F)
+    if sh:
+        return sh_displace(V, 8, 0.05, seed), F
     return radial_noise(V, sigma, seed), F
 
 
@@ -286,6 +290,9 @@ def workload(name: str, seed: int = 0):
     if name.startswith("cap") and name.endswith("_noise"):   # e.g. cap4_noise: open disk
         v, f = cap(int(name[3:-6]), seed=seed)
         return v, f, 0.03, False
+    if name.startswith("cap") and name.endswith("_sh8"):     # e.g. cap7_sh8: smooth open disk
+        v, f = cap(int(name[3:-4]), seed=seed, sh=True)
+        return v, f, 0.01, False
     if name.startswith("cyl_"):     # e.g. cyl_32x12: open cylinder (two boundary loops)
         nu, nv = (int(t) for t in name[4:].split("x"))
         v, f = cylinder(nu, nv, seed=seed)

@@ -4,12 +4,13 @@ The reference (komietty/metriko) cannot be built here and ships no tests or gold
 these fixtures pin the FP64 CPU oracle's outputs on seeded meshes; the GPU tests check the CUDA
 path against them and the CPU tests check that the oracle still reproduces them.
 
-Small fixtures (ico2_noise, ico3_noise, torus_32x16, genus2_s3) store the mesh and every output
+Small fixtures (ico2_noise, ico3_noise, torus_32x16, genus2_s3, and the open meshes cap3_noise,
+cap4_sh8 -- disks -- and cyl_32x12 -- an annulus, seams rounded) store the mesh and every output
 in full.  `icosphere_obj` is the reference's own model, example/models/icosphere.obj (a Blender
 level-4 icosphere, 2562 vertices / 5120 faces), with the level-4 workload's radial N(0, 0.01)
 displacement (seed 0) and grid ratio 0.03; it stores the displaced mesh, so the GPU side needs
 no copy of the reference.  The large fixtures (ico5_sh8, ico6_sh8, ico7_sh8: up to 327,680
-faces) store the integer outputs in full -- singular indices, seams (packed bits), the combed
+faces; cap6_sh8: an open disk of 52,982 faces) store the integer outputs in full -- singular indices, seams (packed bits), the combed
 matching, the fixing order and values, the counts -- and the floating-point outputs on a
 seeded sample (the field angle per face and the map's values at every fixed variable and at a
 sample of the others); their meshes are regenerated by metriko_gb300.meshgen, checked against
@@ -32,8 +33,8 @@ sys.path.insert(0, str(ROOT))
 from metriko_gb300 import meshgen  # noqa: E402
 from oracle import metriko_oracle as O  # noqa: E402
 
-SMALL = ["ico2_noise", "ico3_noise", "torus_32x16", "genus2_s3"]
-LARGE = ["ico5_sh8", "ico6_sh8", "ico7_sh8"]
+SMALL = ["ico2_noise", "ico3_noise", "torus_32x16", "genus2_s3", "cap3_noise", "cap4_sh8", "cyl_32x12"]
+LARGE = ["ico5_sh8", "ico6_sh8", "ico7_sh8", "cap6_sh8"]
 REFERENCE_OBJ = Path("/root/reference/example/models/icosphere.obj")
 SAMPLE = 32768
 

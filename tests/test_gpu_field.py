@@ -56,10 +56,12 @@ def test_field_iteration_cap_reports_not_converged(gpu_ctx):
     assert e.value.status == M._lib.NOT_CONVERGED
 
 
-def test_field_rejects_bad_neighbour(gpu_ctx):
+@pytest.mark.parametrize("bad", ["past_end", "minus_two", "own_face"])
+def test_field_rejects_bad_neighbour(gpu_ctx, bad):
+    """-1 marks a boundary side; any other index outside [0, nF), or the face's own, is rejected."""
     m, nbr, theta = _inputs("ico3_noise")
     nbr = nbr.copy()
-    nbr[5, 1] = m.nF + 7
+    nbr[5, 1] = {"past_end": m.nF + 7, "minus_two": -2, "own_face": 5}[bad]
     with pytest.raises(M.MetrikoError) as e:
         M.field_smoothest(gpu_ctx, nbr, theta, m.faceArea, O.seeded_init(m.nF, 0))
     assert e.value.status == M._lib.BAD_INPUT

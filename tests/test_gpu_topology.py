@@ -115,13 +115,13 @@ def test_field_smoothest_mesh_matches_face_graph_entry(gpu_ctx):
     assert np.abs(np.angle(a / b)).max() / 4 < 1e-7
 
 
-@pytest.mark.parametrize("case", ["boundary", "flipped", "duplicate", "degenerate"])
+@pytest.mark.parametrize("case", ["flipped", "duplicate", "degenerate"])
 def test_mesh_field_inputs_rejects(gpu_ctx, case):
+    """Faces of opposite orientation, an edge with a third face and a side with equal end points
+    are rejected (an edge with one face is a boundary side: tests/test_gpu_open_mesh.py)."""
     V, F, _, _ = meshgen.workload("ico2_noise")
     F = np.array(F, np.int32)
-    if case == "boundary":
-        F = F[1:]
-    elif case == "flipped":
+    if case == "flipped":
         F[3] = F[3, ::-1]
     elif case == "duplicate":
         F = np.vstack([F, F[:1]])

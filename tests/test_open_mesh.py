@@ -11,6 +11,8 @@ boundary edge as a seam; the cut mesh, the transition ids and setup() start a bo
 fan at its first boundary-edge halfedge and stop at its boundary halfedge
 (parameterization.h:80-82,136-140, parameterization_setup.ipp:26-36,76-105).
 """
+from pathlib import Path
+
 import numpy as np
 import pytest
 
@@ -122,3 +124,15 @@ def test_oracle_rounds_open_meshes(name):
     cnt = (m.face[m.twin[m.FH]] >= 0).sum(axis=1)
     assert np.abs(out["L"].diagonal().real - (cnt + 1e-9)).max() < 1e-15
     assert (cnt < 3).any()
+
+
+def test_open_large_golden_mesh_regenerates():
+    """The open-disk fixture of 52,982 faces keeps no mesh: the seeded generator must still
+    produce it, and its stored rounded values are integral."""
+    g = np.load(Path(__file__).parent / "golden" / "cap6_sh8.npz")
+    V, F, ratio, rs = meshgen.workload("cap6_sh8")
+    assert len(V) == int(g["nV"]) and len(F) == int(g["nF"])
+    assert np.abs(V[g["v_sample_idx"]] - g["v_sample"]).max() <= 1e-12
+    X = g["fullx_fixed"]
+    assert np.abs(X - np.round(X)).max() <= 1e-6
+    assert np.array_equal(np.round(X).astype(int), g["fix_vals"])

@@ -127,7 +127,8 @@ def test_rounding_integrality_and_success(name):
     assert np.array_equal(O.cround(X[fixed]).astype(int), np.asarray(info["fix_vals"]))
 
 
-@pytest.mark.parametrize("name", ["ico2_noise", "ico3_noise", "torus_32x16", "genus2_s3"])
+@pytest.mark.parametrize("name", ["ico2_noise", "ico3_noise", "torus_32x16", "genus2_s3", "cap3_noise", "cap4_sh8",
+                                  "cyl_32x12"])
 def test_oracle_reproduces_golden(name):
     g = np.load(GOLDEN / f"{name}.npz")
     V, F, ratio, rs, out = oracle_run(name)

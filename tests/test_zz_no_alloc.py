@@ -24,8 +24,8 @@ pytestmark = pytest.mark.gpu
 def _inputs(name):
     V, F, _, _ = meshgen.workload(name)
     m = O.Hmesh(V, F)
-    nbr = m.face[m.twin[m.FH]].astype(np.int32)
-    theta = m.farg[m.FH] - m.farg[m.twin[m.FH]]
+    nbr = m.face[m.twin[m.FH]].astype(np.int32)        # -1 on a boundary side
+    theta = np.where(nbr >= 0, m.farg[m.FH] - m.farg[m.twin[m.FH]], 0.0)
     return m, nbr, theta
 
 
@@ -69,11 +69,32 @@ def test_noalloc_matches_regular_entry_point_twice():
         assert abs(np.vdot(c, L @ c).real - e_orc) / e_orc < 1e-6
 
 
+def test_noalloc_open_mesh_matches_regular_entry_point():
+    """A disk-shaped mesh: boundary sides (nbr -1) give rows with fewer neighbours, the same
+    operator as the regular entry point and the oracle."""
+    torch = pytest.importorskip("torch")
+    m, nbr, theta = _inputs("cap4_sh8")
+    assert (nbr == -1).any()
+    x0 = O.seeded_init(m.nF, 2)
+    L = O.connection_laplacian(m, 4)
+    with M.Context(0) as ctx:
+        ref, _ = M.field_smoothest(ctx, nbr, theta, m.faceArea, x0, opts=M.solve_opts("fp64", tol=1e-10))
+    orc = O.smallest_eig(L, O.mass_matrix(m), x0, 50)
+    for _ in range(2):
+        status, c, iters = _noalloc(torch, nbr, theta, m.faceArea, x0, 50, 1e-10, 50000)
+        assert status == 0, M.lib().mtk_last_error().decode()
+        assert np.abs(np.angle(c / ref)).max() / 4 < 1e-5
+        assert np.abs(np.angle(c / orc)).max() / 4 < 1e-5
+        e, e_orc = np.vdot(c, L @ c).real, np.vdot(orc, L @ orc).real
+        assert abs(e - e_orc) / e_orc < 1e-6
+
+
 def test_noalloc_failure_statuses():
     """An inner solve capped at one iteration reports NOT_CONVERGED; a neighbour index outside
-    [0, nF) (here -1, as a boundary edge would give) is rejected on the device with BAD_INPUT and
-    no solve; n_iter = 0 returns the start vector.  A good call afterwards still succeeds, so no
-    state from the failed calls is left in the shared scratch array."""
+    [0, nF) other than -1 (-1 marks a boundary side), or a face's own index, is rejected on the
+    device with BAD_INPUT and no solve; n_iter = 0 returns the start vector.  A good call
+    afterwards still succeeds, so no state from the failed calls is left in the shared scratch
+    array."""
     torch = pytest.importorskip("torch")
     m, nbr, theta = _inputs("ico3_noise")
     x0 = O.seeded_init(m.nF, 1)
@@ -81,14 +102,15 @@ def test_noalloc_failure_statuses():
     assert status == M._lib.NOT_CONVERGED
     assert iters == 1
     bad = nbr.copy()
-    bad[7, 1] = -1
+    bad[7, 1] = -2
     status, _, iters = _noalloc(torch, bad, theta, m.faceArea, x0, 50, 1e-10, 50000)
     assert status == M._lib.BAD_INPUT
     assert iters == 0
     assert "neighbour" in M.lib().mtk_last_error().decode()
-    bad[7, 1] = m.nF
-    status, _, _ = _noalloc(torch, bad, theta, m.faceArea, x0, 50, 1e-10, 50000)
-    assert status == M._lib.BAD_INPUT
+    for v in (m.nF, 7):
+        bad[7, 1] = v
+        status, _, _ = _noalloc(torch, bad, theta, m.faceArea, x0, 50, 1e-10, 50000)
+        assert status == M._lib.BAD_INPUT
     status, c, iters = _noalloc(torch, nbr, theta, m.faceArea, x0, 0, 1e-10, 50000)
     assert status == 0 and iters == 0
     assert np.array_equal(c, x0)
