@@ -558,7 +558,7 @@ struct DevLevel0 {
     const int* agg;      // aggregate (level-1 row) of each row
     const V2* t;         // T(k, agg k): transported near-null coefficient / sqrt|aggregate|
     const int* chunk;    // chunk starts, nchunk + 1 entries
-    T dinv;              // 1 / diagonal (every row of a closed mesh has three neighbours)
+    T dinv;              // 1 / (3 + 1e-9): the uniform ELL diagonal (boundary sides are entries -1)
     T omega, alpha, wp;  // smoothing weight, coarse-correction scale, prolongation smoothing
 };
 

@@ -2225,7 +2225,7 @@ int igm_run(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts_in, do
         MTK_CUDA_TRY(cudaMemcpyAsync(h_q.data(), q.p, sizeof(double) * nF, cudaMemcpyDeviceToHost, st));
         MTK_CUDA_TRY(cudaStreamSynchronize(st));
         // assembly backward: dsbar_f / ds_v = 1/3 for the corners of f; smoothness over edges
-        // (every edge of a closed mesh lies in two faces, each contributing half)
+        // (half of (s_a - s_b)^2 per face side: an interior edge once, a boundary edge at half weight)
         const double* sv = job->s;
         double smooth = 0;
         std::fill(job->grad_s, job->grad_s + job->nV, 0.0);

@@ -1554,7 +1554,8 @@ def size_field_gradient(out, F, s, T=None, mu=0.0):
     grad = np.zeros(len(s))
     for j in range(3):
         np.add.at(grad, F[:, j], gf)
-    # smoothness: each edge of a closed mesh lies in two faces, each contributing half
+    # smoothness: half of (s_a - s_b)^2 per face side (an interior edge once, a boundary edge at
+    # half weight)
     smooth = 0.0
     for j in range(3):
         a, b = F[:, j], F[:, (j + 1) % 3]
@@ -1707,8 +1708,10 @@ def position_gradient(V, F, s, mu=0.0, ratio=0.02, seed=0, round_seams=False, n_
     gu = 1j * dphi * c / (N * np.abs(c) ** 2)
     g_area = np.zeros(nF)
     g_theta = np.zeros((nF, 3))
-    nb = m.face[m.twin[m.FH]]                               # neighbour across FH[f, j]
-    Lfg = np.stack([np.asarray(L[np.arange(nF), nb[:, j]]).ravel() for j in range(3)], 1)
+    nb = m.face[m.twin[m.FH]]                               # neighbour across FH[f, j] (-1: boundary)
+    inner = nb >= 0
+    nb = np.where(inner, nb, 0)
+    Lfg = np.stack([np.asarray(L[np.arange(nF), nb[:, j]]).ravel() for j in range(3)], 1) * inner
     for k in range(n_iter, 0, -1):
         u, s_, up = us[k], ss[k], us[k - 1]
         x = u * s_

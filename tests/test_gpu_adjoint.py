@@ -19,7 +19,7 @@ def _opts():
     return M.solve_opts(TIGHT["prec"], tol=TIGHT["tol"])
 
 
-@pytest.mark.parametrize("name", ["ico3_noise", "torus_32x16"])
+@pytest.mark.parametrize("name", ["ico3_noise", "torus_32x16", "cap3_noise"])
 @pytest.mark.parametrize("target", ["integration", "perturbed"])
 def test_size_field_gradient_matches_oracle(gpu_ctx, name, target):
     V, F, ratio, rs = meshgen.workload(name)
@@ -107,10 +107,11 @@ def test_face_geometry_backward_matches_complex_step(gpu_ctx):
     assert np.abs(got - ref).max() <= 1e-9 * np.abs(ref).max()
 
 
-@pytest.mark.parametrize("name", ["ico3_noise", "torus_32x16"])
+@pytest.mark.parametrize("name", ["ico3_noise", "torus_32x16", "cap3_noise"])
 def test_position_gradient_matches_oracle(gpu_ctx, name):
     """dl/dV (integration target, integer decisions frozen): GPU reverse power iteration, face
-    partials and geometry backward against the oracle (direct solves, complex-step geometry)."""
+    partials and geometry backward against the oracle (direct solves, complex-step geometry).
+    cap3_noise is an open disk: a boundary side carries no transport angle."""
     V, F, ratio, rs = meshgen.workload(name)
     rng = np.random.default_rng(4)
     s = rng.normal(0, 0.2, len(V))

@@ -31,7 +31,7 @@ def test_oracle_size_field_zero_field_reproduces_naive_integration():
     assert np.allclose(x, out["info"]["x0"], rtol=1e-9, atol=1e-9 * np.abs(x).max())
 
 
-@pytest.mark.parametrize("name", ["ico2_noise", "torus_32x16"])
+@pytest.mark.parametrize("name", ["ico2_noise", "torus_32x16", "cap2_noise"])
 def test_oracle_position_gradient_matches_finite_differences(name):
     """The oracle's vertex-position gradient (envelope of the naive integration, reverse pass of
     the 50-step inverse power iteration, complex-step face geometry) against FP64 central
