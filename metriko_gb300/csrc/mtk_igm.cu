@@ -118,7 +118,7 @@ struct ZSmem {
 constexpr int kPhiSlot = 8;     // partials offset (in blocks) of the coarse-space dots
 constexpr int kMaxPhi = 64;     // largest z block that gets the Schur coarse space
 // bytes of ZSmem for nZ, nJ (the per-warp coarse-space sums only where the coarse space can be on)
-inline size_t zsmem_bytes(size_t elem, int nZ, int nJ) {
+__host__ __device__ inline size_t zsmem_bytes(size_t elem, int nZ, int nJ) {
     return elem * (7 * (size_t)nZ + 2 * (size_t)nJ + (nZ <= kMaxPhi ? (size_t)kWarps * nZ : 0) + 8);
 }
 
@@ -450,16 +450,19 @@ __device__ void igm_apply_z(const IgmOp<T>& A, const ZProj<T>& P, const T* pz, T
 // Persistent projected PCG.  mode 0: solve K x = b from a feasible x (x, b: [y ; z] global).
 // mode 1: residual only, r = P(b - K x) written to r, |r|^2 in out.
 // out[0] status, out[1] iterations, (double*)(out+4): final |r|^2.
-template <typename T>
+// ZG: the replicated z state of each CTA lives in its own slice of zglob (zstride values) instead
+// of shared memory, for constraint kernels too large for an SM's shared memory (a mesh with
+// many singularities); the arithmetic is the same.
+template <typename T, bool ZG>
 __global__ void __launch_bounds__(kBlock, 1) igm_pcg(IgmOp<T> A, ZProj<T> P, const unsigned char* __restrict__ fixy,
                                                  const T* __restrict__ minvy, const T* __restrict__ b, T* x, T* r, T* z,
                                                  T* p, T* p2, T* q, T* partials, GridBarrier bar, double tol2,
                                                  int maxit, int mode, int* out,
                                                  const RDevHierarchy<T>* __restrict__ Hp, T mg_scale,
-                                                 const __half* __restrict__ Phi) {
+                                                 const __half* __restrict__ Phi, T* zglob, long long zstride) {
     extern __shared__ unsigned char smem_raw[];
     ZSmem<T> zs;
-    zs.bind(reinterpret_cast<T*>(smem_raw), A.nZ, A.nJ);
+    zs.bind(ZG ? zglob + (size_t)blockIdx.x * (size_t)zstride : reinterpret_cast<T*>(smem_raw), A.nZ, A.nJ);
     const int nY = A.nY, nZ = A.nZ;
     const int stride = gridDim.x * blockDim.x;
     const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
@@ -919,11 +922,12 @@ __global__ void add_f32(int n, const float* __restrict__ e, double* x) {
 // x_z += P_z e_z with the FP64 projector (one block).  The FP32 solve's own projector leaves
 // O(1e-7) components along the constraint rows; the FP64 residual cannot see components in
 // the null space of K, so they are removed here before the correction is accumulated.
+// scratch: 2 nZ doubles of global memory when they do not fit in shared memory, else null
 __global__ void add_z_projected(int nY, int nZ, int kq, const double* __restrict__ Q, const float* __restrict__ e,
-                                double* x) {
+                                double* x, double* scratch) {
     extern __shared__ double sz[];
-    double* ez = sz;
-    double* t = sz + nZ;
+    double* ez = scratch ? scratch : sz;
+    double* t = ez + nZ;
     for (int j = threadIdx.x; j < nZ; j += blockDim.x) ez[j] = (double)e[nY + j];
     __syncthreads();
     for (int a = threadIdx.x; a < kq; a += blockDim.x) {
@@ -1143,6 +1147,12 @@ struct Igm {
     std::vector<unsigned char> h_fixy;
     int kq = 0;
     size_t smem64 = 0, smem32 = 0;
+    // z state of the PCG kernel in global memory when it needs more than kZSmemMax bytes
+    static constexpr size_t kZSmemMax = 200 * 1024;
+    int nZ_ = 0, nJ_ = 0;
+    bool z_global_forced = false;
+    DBuf<unsigned char> zstate_global;
+    DBuf<double> zproj_scratch;
     double pcg_ms = 0, pcg_bytes = 0;
     long long pcg_launches = 0, pcg_passes = 0;
     long long nnzW = 0, nnzS = 0, nnzYT = 0;
@@ -1371,13 +1381,26 @@ struct Igm {
     int run_pcg(IgmOp<T> A, ZProj<T> P, const T* minv, const T* b, T* x, T* r, T* z, T* p, T* q, double tol2, int maxit,
                 int mode, size_t smem, long long* iters, double* rr_out) {
         const __half* phiP = (phi_ok && mg && mode == 0) ? phih.p : nullptr;
-        auto kern = igm_pcg<T>;
+        // the replicated z state in shared memory, or (a constraint kernel too large for it, or
+        // MTK_Z_GLOBAL=1) in one global slice per CTA
+        const bool zg = smem > kZSmemMax || z_global_forced;
+        auto kern = zg ? igm_pcg<T, true> : igm_pcg<T, false>;
+        if (zg) smem = 0;
         MTK_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         int per_sm = 0;
         MTK_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, smem));
         if (per_sm < 1) { mtk_set_last_error("IGM solver does not fit on an SM", __FILE__, __LINE__); return MTK_ERR_CUDA; }
         per_sm = 1;   // one CTA per SM
         int grid = std::min(c->num_sms * per_sm, c->partial_blocks);
+        T* zglob = nullptr;
+        long long zstride = 0;
+        if (zg) {
+            zstride = (long long)((zsmem_bytes(sizeof(T), nZ_, nJ_) + sizeof(double) - 1) / sizeof(T));
+            zstride = (zstride + 31) & ~31LL;   // 256-byte aligned slices (FP64) / 128-byte (FP32)
+            const size_t need = (size_t)grid * (size_t)zstride * sizeof(T);
+            if (zstate_global.n < need) MTK_TRY(zstate_global.alloc(need));
+            zglob = reinterpret_cast<T*>(zstate_global.p);
+        }
         const unsigned char* fx = fixy.p;
         T* partials = reinterpret_cast<T*>(c->partials);
         GridBarrier bar = barrier_of(c);
@@ -1396,7 +1419,7 @@ struct Igm {
         T* p2 = sizeof(T) == 8 ? reinterpret_cast<T*>(pb64.p) : reinterpret_cast<T*>(pb32.p);
         void* params[] = {&A, &P, (void*)&fx, (void*)&minv, (void*)&b, (void*)&x, (void*)&r, (void*)&z, (void*)&p,
                           (void*)&p2, (void*)&q, (void*)&partials, &bar, &tol2, &maxit, &mode, (void*)&out,
-                          (void*)&Hp, (void*)&mg_scale, (void*)&phiP};
+                          (void*)&Hp, (void*)&mg_scale, (void*)&phiP, (void*)&zglob, (void*)&zstride};
         MTK_TRY(reset_barrier(c));
         MTK_CUDA_TRY(cudaEventRecord(c->ev_k0, st));
         MTK_CUDA_TRY(cudaLaunchCooperativeKernel(reinterpret_cast<void*>(kern), dim3(grid), dim3(kBlock), params, smem, st));
@@ -1492,8 +1515,13 @@ struct Igm {
                 if (s == MTK_ERR_TIMEOUT) return s;
                 const double rr_prev = rr;
                 add_f32<<<grid(), kStream, 0, st>>>(nY, e32.p, x);
-                if (nZ > 0)
-                    add_z_projected<<<1, kStream, sizeof(double) * 2 * (size_t)nZ, st>>>(nY, nZ, kq, Qz.p, e32.p, x);
+                if (nZ > 0) {
+                    const size_t zb = sizeof(double) * 2 * (size_t)nZ;
+                    const bool zgl = zb > 48 * 1024;   // default dynamic shared-memory limit
+                    if (zgl && zproj_scratch.n < 2 * (size_t)nZ) MTK_TRY(zproj_scratch.alloc(2 * (size_t)nZ));
+                    add_z_projected<<<1, kStream, zgl ? 0 : zb, st>>>(nY, nZ, kq, Qz.p, e32.p, x,
+                                                                     zgl ? zproj_scratch.p : nullptr);
+                }
                 c->kernels += 2;
                 MTK_TRY(run_pcg<double>(op64(scale, shift), ZProj<double>{kq, Qz.p, Mz.p}, minvy.p, b, x, r64.p, z64.p,
                                         p64.p, q64.p, 0.0, 0, 1, smem64, nullptr, &rr));
@@ -1785,7 +1813,9 @@ int igm_run(mtk_ctx* c, const mtk_igm_desc* d, const mtk_solve_opts* opts_in, do
     // shared memory for the replicated z state: 6 nZ + 2 nJ values
     S.smem64 = zsmem_bytes(sizeof(double), nZ, nJ);
     S.smem32 = zsmem_bytes(sizeof(float), nZ, nJ);
-    if (S.smem64 > 200 * 1024) { mtk_set_last_error("constrained block too large for shared memory", __FILE__, __LINE__); return MTK_ERR_BAD_INPUT; }
+    S.nZ_ = nZ;
+    S.nJ_ = nJ;
+    S.z_global_forced = getenv("MTK_Z_GLOBAL") && getenv("MTK_Z_GLOBAL")[0] == '1';
 
     const int G = S.grid();
     MTK_CUDA_TRY(cudaEventRecord(c->ev_a, st));

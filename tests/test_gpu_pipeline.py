@@ -63,6 +63,23 @@ def test_pipeline_deterministic(gpu_ctx):
     assert list(a["fix_order"]) == list(b["fix_order"])
 
 
+@pytest.mark.parametrize("case", ["ico4_noise", "torus_32x16"])
+def test_igm_z_state_in_global_memory_matches_shared(gpu_ctx, monkeypatch, case):
+    """The IGM kernel keeps the replicated z state (constraint-kernel coordinates) of each CTA in
+    shared memory, or in a global slice per CTA when it does not fit (meshes with many
+    singularities; MTK_Z_GLOBAL=1 forces it).  Both give the same arithmetic: bit-identical maps,
+    fixing order and iteration counts."""
+    V, F, ratio, rs = meshgen.workload(case)
+    opts = M.solve_opts("mixed", tol=1e-8)
+    a = M.pipeline(gpu_ctx, V, F, ratio=ratio, round_seams=rs, opts=opts)
+    monkeypatch.setenv("MTK_Z_GLOBAL", "1")
+    b = M.pipeline(gpu_ctx, V, F, ratio=ratio, round_seams=rs, opts=opts)
+    assert a["status"] == 0 and b["status"] == 0
+    assert np.array_equal(a["fullx"], b["fullx"])
+    assert list(a["fix_order"]) == list(b["fix_order"]) and list(a["fix_vals"]) == list(b["fix_vals"])
+    assert a["stats"]["pcg_iters"] == b["stats"]["pcg_iters"]
+
+
 @pytest.mark.parametrize("name", ["ico4_noise", "ico6_sh8", "torus_64x32"])
 def test_igm_multigrid_device_build_matches_host(gpu_ctx, monkeypatch, name):
     """The multigrid set-up on the device (the default: the IGM free block, both hierarchies'
