@@ -464,6 +464,7 @@ namespace metriko {
     struct SeamBase {
         MatXi TT, TTi, cuts;
         std::vector<int> vptr, vv;   // vertex -> neighbouring vertices (one per outgoing halfedge)
+        std::vector<int> ve;         // the edge of each (vertex, neighbour) entry
     };
 
     inline SeamBase seam_base(const Hmesh& m) {
@@ -479,10 +480,11 @@ namespace metriko {
         }
         for (int v = 0; v < m.nV; v++) b.vptr[v + 1] += b.vptr[v];
         b.vv.resize(b.vptr[m.nV]);
+        b.ve.resize(b.vptr[m.nV]);
         METRIKO_PARALLEL_FOR
         for (int v = 0; v < m.nV; v++) {
             int q = b.vptr[v], h = m.vert2half[v];
-            do { b.vv[q++] = m.head[h]; h = m.twin[m.prev[h]]; } while (h != m.vert2half[v]);
+            do { b.ve[q] = m.edge[h]; b.vv[q++] = m.head[h]; h = m.twin[m.prev[h]]; } while (h != m.vert2half[v]);
         }
         return b;
     }
@@ -565,11 +567,26 @@ namespace metriko {
         cut_mesh_with_singularities(m, singularities, seam_base(m), cuts);
     }
 
-    // face_rosy_field.h:345-360, with seam_base(f.mesh) computed beforehand
+    // face_rosy_field.h:345-360, with seam_base(f.mesh) computed beforehand.  Inside a device
+    // pipeline call (a context bound to the host thread) the singularity-path searches run on the
+    // device (mtk_seam_paths: the same searches, the same paths, one launch for all of them); the
+    // seam is the spanning cut's edges plus the paths' edges either way.
     inline std::vector<bool> compute_seam(const FaceRosyField& f, SeamBase&& base) {
         std::vector<bool> seam(f.mesh.nE, false);
         std::vector<int> sv;
         for (int v = 0; v < f.mesh.nV; v++) if (f.singular[v] != 0) sv.push_back(v);
+        if (gpu::bound_context() && !base.ve.empty()) {
+            const Hmesh& m = f.mesh;
+            std::vector<uint8_t> in_cut(m.nV, 0), flag(m.nE, 0);
+            for (int iF = 0; iF < m.nF; iF++)
+                for (int j = 0; j < 3; j++)
+                    if (base.cuts(iF, j)) { in_cut[m.idx(iF, j)] = 1; flag[m.face2edge(iF, j)] = 1; }
+            gpu::check(mtk_seam_paths(gpu::bound_context(), m.nV, m.nE, base.vptr.data(), base.vv.data(), base.ve.data(),
+                                      int(sv.size()), sv.data(), in_cut.data(), flag.data()),
+                       "mtk_seam_paths");
+            for (int e = 0; e < m.nE; e++) seam[e] = flag[e] != 0;
+            return seam;
+        }
         MatXi cuts;
         cut_mesh_with_singularities(f.mesh, VecXi(sv), std::move(base), cuts);
         for (int iF = 0; iF < f.mesh.nF; iF++)

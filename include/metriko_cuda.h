@@ -385,6 +385,21 @@ int mtk_curl_matching(mtk_ctx* ctx, int32_t nV, int32_t nF, int32_t nE, int32_t 
                       int32_t* matching, int32_t* singular);
 
 /*
+ * The singularity-path searches of cut_mesh_with_singularities on the device
+ * (include/metriko/core/vectorfield/face_rosy_field.h:287-326 of the reference, libigl's
+ * unit-weight dijkstra): for each source in order, a breadth-first search until a level holds a
+ * vertex of the cut; the path from the smallest-id such vertex back along the predecessors (each
+ * vertex's smallest-id neighbour in the previous level) joins the cut.  The same paths as the
+ * host search (compute_seam), found in one cooperative launch with one grid barrier per level.
+ *   vptr[nV+1], vv[vptr[nV]]   each vertex's neighbours, ve[vptr[nV]] the edge of each entry
+ *   src[n_src]                 the sources (the singular vertices, in vertex order)
+ *   in_cut[nV] (in/out)        1 for vertices of the cut (the spanning cut's, then the paths')
+ *   seam[nE] (in/out)          edge flags: set for every edge of a path (entries already set stay)
+ */
+int mtk_seam_paths(mtk_ctx* ctx, int32_t nV, int32_t nE, const int32_t* vptr, const int32_t* vv, const int32_t* ve,
+                   int32_t n_src, const int32_t* src, uint8_t* in_cut, uint8_t* seam);
+
+/*
  * Assembled sparse systems (the general linear-solver seam).  Replaces, for symmetric / Hermitian
  * positive-definite matrices, the direct solvers behind solveSquare(SprsC&, VecXc&) and
  * solveSmallestEig(SprsC&, SprsC&, int) (include/metriko/core/solver/sparse_linear_solver.h:16-54)

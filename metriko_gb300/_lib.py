@@ -26,6 +26,7 @@ EXPORTS = [
     "mtk_mesh_geometry", "mtk_ctx_set_wait_limit", "mtk_pipeline_position_gradient", "mtk_size_field_position_partials",
     "mtk_field_power_adjoint", "mtk_face_geometry_backward", "mtk_csr_create", "mtk_csr_destroy", "mtk_csr_pcg",
     "mtk_csr_smallest_eig", "mtk_curl_matching", "mtk_mesh_field_inputs", "mtk_field_smoothest_mesh",
+    "mtk_seam_paths",
 ]
 
 
@@ -129,6 +130,7 @@ def lib():
                                            C.POINTER(SolveOpts), C.c_void_p, C.POINTER(Stats)]
         L.mtk_curl_matching.argtypes = [C.c_void_p] + [C.c_int32] * 4 + [C.c_void_p] * 13
         L.mtk_mesh_field_inputs.argtypes = [C.c_void_p, C.c_int32, C.c_int32] + [C.c_void_p] * 5
+        L.mtk_seam_paths.argtypes = [C.c_void_p, C.c_int32, C.c_int32] + [C.c_void_p] * 3 + [C.c_int32] + [C.c_void_p] * 3
         L.mtk_field_smoothest_mesh.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
                                                C.c_void_p, C.c_int32, C.POINTER(SolveOpts), C.c_void_p,
                                                C.POINTER(Stats)]
@@ -480,6 +482,20 @@ def curl_matching(ctx: Context, V, F, edge_vert, edge_face, vert_half, prev_half
                                    _ptr(singular)),
            "mtk_curl_matching")
     return matching, singular
+
+
+def seam_paths(ctx: Context, nV, nE, vptr, vv, ve, sources, in_cut, seam):
+    """mtk_seam_paths: the singularity-path searches on the device.  Returns (in_cut, seam) after
+    every path joined the cut (copies of the inputs updated)."""
+    vptr = np.ascontiguousarray(vptr, np.int32)
+    vv = np.ascontiguousarray(vv, np.int32)
+    ve = np.ascontiguousarray(ve, np.int32)
+    src = np.ascontiguousarray(sources, np.int32)
+    cut = np.ascontiguousarray(in_cut, np.uint8).copy()
+    sm = np.ascontiguousarray(seam, np.uint8).copy()
+    _check(lib().mtk_seam_paths(ctx.handle, nV, nE, _ptr(vptr), _ptr(vv), _ptr(ve), len(src), _ptr(src), _ptr(cut),
+                                _ptr(sm)), "mtk_seam_paths")
+    return cut.astype(bool), sm.astype(bool)
 
 
 class CsrMatrix:

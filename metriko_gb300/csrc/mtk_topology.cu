@@ -263,7 +263,166 @@ __global__ void side_outputs(int nF, const int* __restrict__ partner, const doub
     }
 }
 
+// ------------------------------------------------------------------ singularity paths (seams)
+// cut_mesh_with_singularities' searches (face_rosy_field.h:287-326, libigl's unit-weight
+// dijkstra): for each source in order, a breadth-first search by levels from the source until a
+// level holds a vertex of the cut; the path runs from the smallest-id such vertex back along the
+// predecessors (each vertex's predecessor: its smallest-id neighbour in the previous level) and
+// joins the cut.  One cooperative launch runs every search, one grid barrier per level:
+//  * sd[v] = (search << 32) | level marks the vertices reached by the current search (claimed by
+//    compare-and-swap, so each vertex enters one level once); pred[v] keeps, per search, the
+//    smallest neighbour id of the previous level by a 64-bit atomicMin on
+//    ((~search) << 32) | neighbour -- both are independent of the order of the expansion;
+//  * a vertex is checked against the cut when it is claimed, and the smallest cut vertex of the
+//    new level (atomicMin) ends the search after the barrier;
+//  * counts and minima rotate over three slots (level d reads slot d % 3, fills (d + 1) % 3 and
+//    clears (d + 2) % 3), so no slot is cleared while another CTA may still read it;
+//  * one thread walks the path back, adds its vertices to the cut and flags its edges.
+// Every loop is bounded (levels <= nV, path <= nV steps) and every wait is the bounded grid
+// barrier; a timeout leaves the error flag set and the call returns MTK_ERR_TIMEOUT.
+constexpr int kNone = 0x7fffffff;
+
+__global__ void __launch_bounds__(kBlock, 1) seam_paths(int nV, int ns, const int* __restrict__ vptr,
+                                                       const int* __restrict__ vv, const int* __restrict__ ve,
+                                                       const int* __restrict__ src, int* in_cut, unsigned long long* sd,
+                                                       unsigned long long* pred, int* fr, int* ctl,
+                                                       unsigned char* seam_edge, GridBarrier bar) {
+    // ctl: [0] vertices on the cut, [1..3] frontier counts, [4..6] smallest cut vertex per slot
+    const int stride = gridDim.x * blockDim.x;
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
+    for (int si = 0; si < ns; si++) {
+        const int s = src[si];
+        const unsigned int iter = (unsigned int)si + 1u;
+        if (ld_volatile(ctl) == 0) {
+            // no cut vertex anywhere: the search would exhaust the mesh, the path is the source alone
+            if (lead) { in_cut[s] = 1; ctl[0] = 1; }
+            if (!grid_sync(bar)) return;
+            continue;
+        }
+        if (ld_volatile(in_cut + s)) continue;   // found at level 0: the path is the source alone
+        if (lead) {
+            fr[0] = s;
+            ctl[1] = 1; ctl[2] = 0; ctl[3] = 0;
+            ctl[4] = kNone; ctl[5] = kNone; ctl[6] = kNone;
+            sd[s] = ((unsigned long long)iter << 32);
+            pred[s] = ~0ull;
+        }
+        if (!grid_sync(bar)) return;
+        int found = -1;
+        for (int d = 0; d < nV; d++) {
+            const int p = d % 3, q = (d + 1) % 3, r = (d + 2) % 3;
+            const int n = ld_volatile(ctl + 1 + p);
+            const int* cur = fr + (size_t)p * nV;
+            int* nxt = fr + (size_t)q * nV;
+            if (lead) { ctl[1 + r] = 0; ctl[4 + r] = kNone; }
+            const unsigned long long lvl = ((unsigned long long)iter << 32) | (unsigned int)(d + 1);
+            const unsigned long long pk_hi = (unsigned long long)(~iter) << 32;
+            for (int i = t0; i < n; i += stride) {
+                const int u = __ldcg(cur + i);
+                const unsigned long long pk = pk_hi | (unsigned int)u;
+                const int e1 = vptr[u + 1];
+                for (int k = vptr[u]; k < e1; k++) {
+                    const int w = vv[k];
+                    unsigned long long old = atomicAdd(sd + w, 0ull);
+                    bool join = false;
+                    for (int tries = 0; tries < 64; tries++) {
+                        if ((old >> 32) == iter) { join = old == lvl; break; }
+                        const unsigned long long prev = atomicCAS(sd + w, old, lvl);
+                        if (prev == old) {   // claimed: w enters level d + 1
+                            const int idx = atomicAdd(ctl + 1 + q, 1);
+                            nxt[idx] = w;
+                            if (ld_volatile(in_cut + w)) atomicMin(ctl + 4 + q, w);
+                            join = true;
+                            break;
+                        }
+                        old = prev;
+                    }
+                    if (join) atomicMin(pred + w, pk);
+                }
+            }
+            if (!grid_sync(bar)) return;
+            const int f = ld_volatile(ctl + 4 + q);
+            if (f != kNone) { found = f; break; }
+            if (ld_volatile(ctl + 1 + q) == 0) break;   // the search exhausted its component
+        }
+        if (lead) {
+            int ncut = ctl[0];
+            if (found >= 0) {
+                int v = found;
+                for (int step = 0; v != s && step < nV; step++) {
+                    if (!in_cut[v]) { in_cut[v] = 1; ncut++; }
+                    const int u = (int)(unsigned int)(pred[v] & 0xffffffffull);
+                    for (int k = vptr[v]; k < vptr[v + 1]; k++)
+                        if (vv[k] == u) { seam_edge[ve[k]] = 1; break; }
+                    v = u;
+                }
+            }
+            if (!in_cut[s]) { in_cut[s] = 1; ncut++; }
+            ctl[0] = ncut;
+        }
+        if (!grid_sync(bar)) return;
+    }
+}
+
 }  // namespace
+
+extern "C" int mtk_seam_paths(mtk_ctx* c, int32_t nV, int32_t nE, const int32_t* vptr, const int32_t* vv,
+                              const int32_t* ve, int32_t n_src, const int32_t* src, uint8_t* in_cut, uint8_t* seam) {
+    if (!c || nV <= 0 || nE <= 0 || n_src < 0 || !vptr || !vv || !ve || (n_src > 0 && !src) || !in_cut || !seam)
+        return MTK_ERR_BAD_INPUT;
+    auto bad = [](const char* what) {
+        mtk_set_last_error(what, __FILE__, __LINE__);
+        return MTK_ERR_BAD_INPUT;
+    };
+    if (vptr[0] != 0) return bad("mtk_seam_paths: vptr[0] must be 0");
+    for (int v = 0; v < nV; v++)
+        if (vptr[v + 1] < vptr[v]) return bad("mtk_seam_paths: vptr must not decrease");
+    const int64_t nadj = vptr[nV];
+    for (int64_t k = 0; k < nadj; k++) {
+        if (vv[k] < 0 || vv[k] >= nV) return bad("mtk_seam_paths: neighbour out of range");
+        if (ve[k] < 0 || ve[k] >= nE) return bad("mtk_seam_paths: edge out of range");
+    }
+    for (int i = 0; i < n_src; i++)
+        if (src[i] < 0 || src[i] >= nV) return bad("mtk_seam_paths: source out of range");
+    if (n_src == 0) return MTK_OK;
+    MTK_CUDA_TRY(cudaSetDevice(c->device));
+    AllocStreamScope alloc_scope(c->stream);
+    cudaStream_t st = c->stream;
+    std::vector<int> cut_i(nV);
+    int ncut = 0;
+    for (int v = 0; v < nV; v++) { cut_i[v] = in_cut[v] ? 1 : 0; ncut += cut_i[v]; }
+    DBuf<int> dptr, dvv, dve, dsrc, dcut, dfr, dctl;
+    DBuf<unsigned long long> dsd, dpred;
+    DBuf<unsigned char> dseam;
+    MTK_TRY(dptr.upload(vptr, (size_t)nV + 1, st));
+    MTK_TRY(dvv.upload(vv, (size_t)nadj, st));
+    MTK_TRY(dve.upload(ve, (size_t)nadj, st));
+    MTK_TRY(dsrc.upload(src, (size_t)n_src, st));
+    MTK_TRY(dcut.upload(cut_i.data(), (size_t)nV, st));
+    MTK_TRY(dseam.upload(seam, (size_t)nE, st));
+    MTK_TRY(dfr.alloc(3 * (size_t)nV));
+    MTK_TRY(dsd.alloc(nV));
+    MTK_TRY(dpred.alloc(nV));
+    int h_ctl[8] = {ncut, 0, 0, 0, kNone, kNone, kNone, 0};
+    MTK_TRY(dctl.upload(h_ctl, 8, st));
+    MTK_CUDA_TRY(cudaMemsetAsync(dsd.p, 0, sizeof(unsigned long long) * nV, st));
+    int grid = 0;
+    MTK_TRY(launch_persistent(c, seam_paths, &grid, (int)nV, (int)n_src, (const int*)dptr.p, (const int*)dvv.p,
+                              (const int*)dve.p, (const int*)dsrc.p, dcut.p, dsd.p, dpred.p, dfr.p, dctl.p, dseam.p,
+                              barrier_of(c)));
+    MTK_CUDA_TRY(cudaGetLastError());
+    MTK_CUDA_TRY(cudaMemcpyAsync(cut_i.data(), dcut.p, sizeof(int) * nV, cudaMemcpyDeviceToHost, st));
+    MTK_CUDA_TRY(cudaMemcpyAsync(seam, dseam.p, (size_t)nE, cudaMemcpyDeviceToHost, st));
+    MTK_CUDA_TRY(cudaMemcpyAsync(c->h_int, c->dev_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    MTK_CUDA_TRY(cudaStreamSynchronize(st));
+    if (c->h_int[0]) {
+        mtk_set_last_error("mtk_seam_paths: a grid barrier wait ran out", __FILE__, __LINE__);
+        return MTK_ERR_TIMEOUT;
+    }
+    for (int v = 0; v < nV; v++) in_cut[v] = (uint8_t)cut_i[v];
+    return MTK_OK;
+}
 
 extern "C" int mtk_mesh_field_inputs(mtk_ctx* c, int32_t nV, int32_t nF, const double* V, const int32_t* F, int32_t* nbr,
                                      double* theta, double* area) {

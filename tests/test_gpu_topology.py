@@ -130,3 +130,49 @@ def test_mesh_field_inputs_rejects(gpu_ctx, case):
     with pytest.raises(M.MetrikoError) as e:
         M.mesh_field_inputs(gpu_ctx, V, F)
     assert e.value.status == M._lib.BAD_INPUT
+
+
+def _seam_inputs(m):
+    """The spanning cut (libigl's cut with an all-zero matching) and the vertex rings of the
+    oracle's mesh: what mtk_seam_paths starts from."""
+    TT, TTi = O.triangle_triangle_adjacency(m)
+    cuts = O.cut_mesh_from_singularities_zero(m, TT, TTi)
+    in_cut = np.zeros(m.nV, np.uint8)
+    in_cut[m.idx[cuts]] = 1
+    seam0 = np.zeros(m.nE, np.uint8)
+    seam0[m.face2edge[cuts]] = 1
+    vptr, vv, ve = [0], [], []
+    for v in range(m.nV):
+        ring = m.ccw(m.vert2half[v])
+        vv += [int(m.head[h]) for h in ring]
+        ve += [int(m.edge[h]) for h in ring]
+        vptr.append(len(vv))
+    return in_cut, seam0, np.array(vptr), np.array(vv), np.array(ve)
+
+
+@pytest.mark.parametrize("name", ["ico3_noise", "torus_32x16", "genus2_s3", "cap4_sh8", "cyl_32x12", "ico5_sh8"])
+def test_seam_paths_match_oracle(gpu_ctx, name):
+    """The singularity-path searches on the device (one cooperative launch, one grid barrier per
+    level) give the oracle's seam bit for bit: spheres, a torus, a genus-2 surface, an open disk
+    and an open cylinder (whose boundary vertices, index 1, are sources already on the cut)."""
+    V, F, ratio, rs = meshgen.workload(name)
+    ref = O.pipeline(V, F, ratio=ratio, round_seams=rs, stop_after="field")
+    m = ref["mesh"]
+    in_cut, seam0, vptr, vv, ve = _seam_inputs(m)
+    src = np.flatnonzero(ref["singular"] != 0)
+    cut, seam = M.seam_paths(gpu_ctx, m.nV, m.nE, vptr, vv, ve, src, in_cut, seam0)
+    want = O.compute_seam(m, ref["singular"])
+    assert np.array_equal(seam, want)
+    assert cut[src].all() and set(np.flatnonzero(cut)) >= set(np.unique(m.edge2vert[want]).tolist())
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_seam_paths_many_sources(gpu_ctx, seed):
+    """60 seeded random sources on a level-4 sphere: many searches, most ending on earlier paths."""
+    V, F, _, _ = meshgen.workload("ico4_noise")
+    m = O.Hmesh(V, F)
+    sing = np.zeros(m.nV, np.int64)
+    sing[np.random.default_rng(seed).choice(m.nV, 60, replace=False)] = 1
+    in_cut, seam0, vptr, vv, ve = _seam_inputs(m)
+    _, seam = M.seam_paths(gpu_ctx, m.nV, m.nE, vptr, vv, ve, np.flatnonzero(sing), in_cut, seam0)
+    assert np.array_equal(seam, O.compute_seam(m, sing))
