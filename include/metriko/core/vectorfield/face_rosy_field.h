@@ -278,17 +278,28 @@ namespace metriko {
                 nb[3 * size_t(i) + j] = (seam[e] || m.isBE[e]) ? -1 : (b ? m.edge2face(e, 1) : m.edge2face(e, 0));
                 nm[3 * size_t(i) + j] = (b ? 1 : -1) * fld.matching[e];
             }
-        std::deque<std::pair<int, int>> q;
-        q.emplace_back(0, 0);
-        while (!q.empty()) {
-            auto [i, mm] = q.front();
-            q.pop_front();
-            if (visit[i]) continue;
-            visit[i] = 1;
-            turns[i] = mm;
-            for (int j = 0; j < 3; j++) {
-                const int fn = nb[3 * size_t(i) + j];
-                if (fn >= 0 && !visit[fn]) q.emplace_back(fn, (nm[3 * size_t(i) + j] + mm + 1000 * N) % N);
+        if (gpu::bound_context()) {
+            // inside a device pipeline call: the same turns from the level-by-level search on the
+            // device (mtk_comb_turns; the turns do not depend on the path inside the cut disk)
+            gpu::check(mtk_comb_turns(gpu::bound_context(), m.nF, N, nb.data(), nm.data(), turns.data()), "mtk_comb_turns");
+            METRIKO_PARALLEL_FOR
+            for (int i = 0; i < m.nF; i++) {
+                visit[i] = turns[i] >= 0;
+                if (turns[i] < 0) turns[i] = 0;
+            }
+        } else {
+            std::deque<std::pair<int, int>> q;
+            q.emplace_back(0, 0);
+            while (!q.empty()) {
+                auto [i, mm] = q.front();
+                q.pop_front();
+                if (visit[i]) continue;
+                visit[i] = 1;
+                turns[i] = mm;
+                for (int j = 0; j < 3; j++) {
+                    const int fn = nb[3 * size_t(i) + j];
+                    if (fn >= 0 && !visit[fn]) q.emplace_back(fn, (nm[3 * size_t(i) + j] + mm + 1000 * N) % N);
+                }
             }
         }
         METRIKO_PARALLEL_FOR

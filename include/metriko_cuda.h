@@ -400,6 +400,19 @@ int mtk_seam_paths(mtk_ctx* ctx, int32_t nV, int32_t nE, const int32_t* vptr, co
                    int32_t n_src, const int32_t* src, uint8_t* in_cut, uint8_t* seam);
 
 /*
+ * The combing search of compute_combbed_field on the device
+ * (include/metriko/core/vectorfield/face_rosy_field.h:217-242 of the reference): from face 0
+ * (turn 0), across every face side that is neither a seam nor a boundary, the neighbour's turn is
+ * (the side's signed matching + the face's turn) mod N.  Level by level, one grid barrier per
+ * level; the turns do not depend on the path inside the cut disk (every singular vertex lies on
+ * the seam), so they equal the reference's queue order's.
+ *   nb[3 nF]     the face across side j of face f, -1 across a seam or a boundary edge
+ *   nm[3 nF]     the side's signed matching ((+1 or -1) * matching[e], face_rosy_field.h:237-238)
+ *   turns[nF]    out: each face's turn, -1 for a face the search does not reach
+ */
+int mtk_comb_turns(mtk_ctx* ctx, int32_t nF, int32_t N, const int32_t* nb, const int32_t* nm, int32_t* turns);
+
+/*
  * Assembled sparse systems (the general linear-solver seam).  Replaces, for symmetric / Hermitian
  * positive-definite matrices, the direct solvers behind solveSquare(SprsC&, VecXc&) and
  * solveSmallestEig(SprsC&, SprsC&, int) (include/metriko/core/solver/sparse_linear_solver.h:16-54)

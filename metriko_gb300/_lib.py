@@ -26,7 +26,7 @@ EXPORTS = [
     "mtk_mesh_geometry", "mtk_ctx_set_wait_limit", "mtk_pipeline_position_gradient", "mtk_size_field_position_partials",
     "mtk_field_power_adjoint", "mtk_face_geometry_backward", "mtk_csr_create", "mtk_csr_destroy", "mtk_csr_pcg",
     "mtk_csr_smallest_eig", "mtk_curl_matching", "mtk_mesh_field_inputs", "mtk_field_smoothest_mesh",
-    "mtk_seam_paths",
+    "mtk_seam_paths", "mtk_comb_turns",
 ]
 
 
@@ -131,6 +131,7 @@ def lib():
         L.mtk_curl_matching.argtypes = [C.c_void_p] + [C.c_int32] * 4 + [C.c_void_p] * 13
         L.mtk_mesh_field_inputs.argtypes = [C.c_void_p, C.c_int32, C.c_int32] + [C.c_void_p] * 5
         L.mtk_seam_paths.argtypes = [C.c_void_p, C.c_int32, C.c_int32] + [C.c_void_p] * 3 + [C.c_int32] + [C.c_void_p] * 3
+        L.mtk_comb_turns.argtypes = [C.c_void_p, C.c_int32, C.c_int32] + [C.c_void_p] * 3
         L.mtk_field_smoothest_mesh.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
                                                C.c_void_p, C.c_int32, C.POINTER(SolveOpts), C.c_void_p,
                                                C.POINTER(Stats)]
@@ -496,6 +497,16 @@ def seam_paths(ctx: Context, nV, nE, vptr, vv, ve, sources, in_cut, seam):
     _check(lib().mtk_seam_paths(ctx.handle, nV, nE, _ptr(vptr), _ptr(vv), _ptr(ve), len(src), _ptr(src), _ptr(cut),
                                 _ptr(sm)), "mtk_seam_paths")
     return cut.astype(bool), sm.astype(bool)
+
+
+def comb_turns(ctx: Context, nb, nm, N=4):
+    """mtk_comb_turns: each face's combing turn (-1 where the search does not reach)."""
+    nb = np.ascontiguousarray(nb, np.int32).reshape(-1)
+    nm = np.ascontiguousarray(nm, np.int32).reshape(-1)
+    nF = len(nb) // 3
+    turns = np.zeros(nF, np.int32)
+    _check(lib().mtk_comb_turns(ctx.handle, nF, N, _ptr(nb), _ptr(nm), _ptr(turns)), "mtk_comb_turns")
+    return turns
 
 
 class CsrMatrix:

@@ -365,7 +365,78 @@ __global__ void __launch_bounds__(kBlock, 1) seam_paths(int nV, int ns, const in
     }
 }
 
+// ------------------------------------------------------------------ combing turns
+// compute_combbed_field's search (face_rosy_field.h:217-242): from face 0 (turn 0), across every
+// face side that is neither a seam nor a boundary, the neighbour's turn is (the side's signed
+// matching + the face's turn) mod N.  The reference pops a queue; here the faces are reached level
+// by level (one grid barrier per level), a face taking the value of whichever neighbour of the
+// previous level claims it first.  Every singular vertex lies on the seam, so no loop inside the
+// cut disk carries holonomy: the turns do not depend on the path, and any claim gives the
+// reference's value (the tests compare with the host search on every fixture).
+__global__ void __launch_bounds__(kBlock, 1) comb_turns(int nF, int N, const int* __restrict__ nb,
+                                                       const int* __restrict__ nm, int* turns, int* fr, int* ctl,
+                                                       GridBarrier bar) {
+    // ctl[0..2]: frontier counts per slot (level d reads d % 3, fills (d + 1) % 3, clears (d + 2) % 3)
+    const int stride = gridDim.x * blockDim.x;
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
+    for (int d = 0; d < nF; d++) {
+        const int p = d % 3, q = (d + 1) % 3, r = (d + 2) % 3;
+        const int n = ld_volatile(ctl + p);
+        if (n == 0) break;
+        const int* cur = fr + (size_t)p * nF;
+        int* nxt = fr + (size_t)q * nF;
+        if (lead) ctl[r] = 0;
+        for (int i = t0; i < n; i += stride) {
+            const int f = __ldcg(cur + i);
+            const int tf = __ldcg(turns + f);
+            for (int j = 0; j < 3; j++) {
+                const int g = nb[3 * (size_t)f + j];
+                if (g < 0) continue;
+                const int val = ((nm[3 * (size_t)f + j] + tf) % N + N) % N;
+                if (atomicCAS(turns + g, -1, val) == -1) nxt[atomicAdd(ctl + q, 1)] = g;
+            }
+        }
+        if (!grid_sync(bar)) return;
+    }
+}
+
 }  // namespace
+
+extern "C" int mtk_comb_turns(mtk_ctx* c, int32_t nF, int32_t N, const int32_t* nb, const int32_t* nm, int32_t* turns) {
+    if (!c || nF <= 0 || N < 1 || !nb || !nm || !turns) return MTK_ERR_BAD_INPUT;
+    for (int64_t i = 0; i < 3 * (int64_t)nF; i++)
+        if (nb[i] < -1 || nb[i] >= nF) {
+            mtk_set_last_error("mtk_comb_turns: neighbour out of range", __FILE__, __LINE__);
+            return MTK_ERR_BAD_INPUT;
+        }
+    MTK_CUDA_TRY(cudaSetDevice(c->device));
+    AllocStreamScope alloc_scope(c->stream);
+    cudaStream_t st = c->stream;
+    DBuf<int> dnb, dnm, dturn, dfr, dctl;
+    MTK_TRY(dnb.upload(nb, 3 * (size_t)nF, st));
+    MTK_TRY(dnm.upload(nm, 3 * (size_t)nF, st));
+    MTK_TRY(dturn.alloc(nF));
+    MTK_TRY(dfr.alloc(3 * (size_t)nF));
+    MTK_CUDA_TRY(cudaMemsetAsync(dturn.p, 0xff, sizeof(int) * nF, st));   // -1: not reached
+    const int zero = 0;
+    MTK_CUDA_TRY(cudaMemcpyAsync(dturn.p, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
+    MTK_CUDA_TRY(cudaMemcpyAsync(dfr.p, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
+    const int h_ctl[3] = {1, 0, 0};
+    MTK_TRY(dctl.upload(h_ctl, 3, st));
+    int grid = 0;
+    MTK_TRY(launch_persistent(c, comb_turns, &grid, (int)nF, (int)N, (const int*)dnb.p, (const int*)dnm.p, dturn.p, dfr.p,
+                              dctl.p, barrier_of(c)));
+    MTK_CUDA_TRY(cudaGetLastError());
+    MTK_CUDA_TRY(cudaMemcpyAsync(turns, dturn.p, sizeof(int) * nF, cudaMemcpyDeviceToHost, st));
+    MTK_CUDA_TRY(cudaMemcpyAsync(c->h_int, c->dev_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    MTK_CUDA_TRY(cudaStreamSynchronize(st));
+    if (c->h_int[0]) {
+        mtk_set_last_error("mtk_comb_turns: a grid barrier wait ran out", __FILE__, __LINE__);
+        return MTK_ERR_TIMEOUT;
+    }
+    return MTK_OK;
+}
 
 extern "C" int mtk_seam_paths(mtk_ctx* c, int32_t nV, int32_t nE, const int32_t* vptr, const int32_t* vv,
                               const int32_t* ve, int32_t n_src, const int32_t* src, uint8_t* in_cut, uint8_t* seam) {

@@ -176,3 +176,50 @@ def test_seam_paths_many_sources(gpu_ctx, seed):
     in_cut, seam0, vptr, vv, ve = _seam_inputs(m)
     _, seam = M.seam_paths(gpu_ctx, m.nV, m.nE, vptr, vv, ve, np.flatnonzero(sing), in_cut, seam0)
     assert np.array_equal(seam, O.compute_seam(m, sing))
+
+
+def _queue_turns(m, matching, seam, N=4):
+    """compute_combbed_field's queue search (face_rosy_field.h:217-242): the turn of each face when
+    it is first popped, -1 for faces never reached."""
+    from collections import deque
+    turns = np.full(m.nF, -1, np.int64)
+    q = deque([(0, 0)])
+    while q:
+        i, mm = q.popleft()
+        if turns[i] >= 0:
+            continue
+        turns[i] = mm
+        for j in range(3):
+            e = m.edge[m.FH[i, j]]
+            if m.isBE[e] or seam[e]:
+                continue
+            b = m.edge2face[e, 0] == i
+            fn = m.edge2face[e, 1] if b else m.edge2face[e, 0]
+            if turns[fn] < 0:
+                q.append((fn, ((1 if b else -1) * matching[e] + mm) % N))
+    return turns
+
+
+@pytest.mark.parametrize("name", ["ico3_noise", "torus_32x16", "genus2_s3", "cap4_sh8", "cyl_32x12", "ico5_sh8"])
+def test_comb_turns_match_queue_search(gpu_ctx, name):
+    """The combing turns from the device's level-by-level search equal the reference's queue
+    order on every face (the turns do not depend on the path inside the cut disk)."""
+    V, F, ratio, rs = meshgen.workload(name)
+    ref = O.pipeline(V, F, ratio=ratio, round_seams=rs, stop_after="setup")
+    m, seam, matching = ref["mesh"], ref["seam"], ref["matching"]
+    nb = np.full((m.nF, 3), -1, np.int64)
+    nm = np.zeros((m.nF, 3), np.int64)
+    for j in range(3):
+        e = m.edge[m.FH[:, j]]
+        b = m.edge2face[e, 0] == np.arange(m.nF)
+        other = np.where(b, m.edge2face[e, 1], m.edge2face[e, 0])
+        nb[:, j] = np.where(seam[e] | m.isBE[e], -1, other)
+        nm[:, j] = np.where(b, 1, -1) * matching[e]
+    got = M.comb_turns(gpu_ctx, nb, nm)
+    want = _queue_turns(m, matching, seam)
+    assert np.array_equal(got, want)
+    # and the combed field built from them is the oracle's
+    _, cm = O.combed_field(m, ref["field"], matching, seam, 4)
+    f0, f1 = O._interior_faces(m)
+    t = np.maximum(got, 0)
+    assert np.array_equal(np.where(m.isBE, -1, (t[f0] - t[f1] + matching + 4000) % 4), cm)
