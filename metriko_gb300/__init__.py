@@ -8,5 +8,5 @@ from ._lib import (Context, MetrikoError, PREC_FP64, PREC_MIXED, field_smoothest
                    field_inputs, field_solve, injective_barrier, local_injectivity, map_deviation, mesh_geometry, pipeline, seeded_init,
                    size_field_gradient, solve_opts, spmv_bench, topology_from_field, position_gradient,
                    face_geometry_backward, CsrMatrix, csr_smallest_eig, curl_matching, mesh_field_inputs,
-                   field_smoothest_mesh)
+                   field_smoothest_mesh, seam_paths, comb_turns, num_edges)
 from . import meshgen  # noqa: F401

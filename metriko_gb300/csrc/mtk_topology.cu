@@ -295,7 +295,10 @@ __global__ void __launch_bounds__(kBlock, 1) seam_paths(int nV, int ns, const in
         const int s = src[si];
         const unsigned int iter = (unsigned int)si + 1u;
         if (ld_volatile(ctl) == 0) {
-            // no cut vertex anywhere: the search would exhaust the mesh, the path is the source alone
+            // no cut vertex anywhere: the search would exhaust the mesh, the path is the source
+            // alone.  Every CTA reads ctl[0] before the lead changes it (first barrier), so all
+            // CTAs take this branch together.
+            if (!grid_sync(bar)) return;
             if (lead) { in_cut[s] = 1; ctl[0] = 1; }
             if (!grid_sync(bar)) return;
             continue;
@@ -477,7 +480,8 @@ extern "C" int mtk_seam_paths(mtk_ctx* c, int32_t nV, int32_t nE, const int32_t*
     MTK_TRY(dpred.alloc(nV));
     int h_ctl[8] = {ncut, 0, 0, 0, kNone, kNone, kNone, 0};
     MTK_TRY(dctl.upload(h_ctl, 8, st));
-    MTK_CUDA_TRY(cudaMemsetAsync(dsd.p, 0, sizeof(unsigned long long) * nV, st));
+    MTK_CUDA_TRY(cudaMemsetAsync(dsd.p, 0, sizeof(unsigned long long) * nV, st));      // no search yet
+    MTK_CUDA_TRY(cudaMemsetAsync(dpred.p, 0xff, sizeof(unsigned long long) * nV, st));  // above every key
     int grid = 0;
     MTK_TRY(launch_persistent(c, seam_paths, &grid, (int)nV, (int)n_src, (const int*)dptr.p, (const int*)dvv.p,
                               (const int*)dve.p, (const int*)dsrc.p, dcut.p, dsd.p, dpred.p, dfr.p, dctl.p, dseam.p,
