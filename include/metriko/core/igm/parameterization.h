@@ -30,6 +30,7 @@
 
 #include "metriko/core/hmesh/hmesh.h"
 #include "metriko/core/igm/iterative_rounding/iter_rounding.h"
+#include "metriko/core/igm/iterative_rounding/local_injectivity.h"
 #include "metriko/core/solver/matrix_ops.h"
 
 namespace metriko {
@@ -159,6 +160,12 @@ namespace metriko {
 
         void setup();
         void build_system(IntegSystem& sys);   // host part of integ()
+        // The reduced system of the localInjectivity path (li::System: G = G2 fullx2Nfunc UFull,
+        // F2, length, the index sets), from build_system's products; host only.
+        void li_system(const IntegSystem& sys, li::System& s) const;
+        // x (full variables) -> the reduced coordinates [y ; z] of UFull (z by least squares on the
+        // constrained block: USmall has full column rank)
+        std::vector<double> to_reduced(const IntegSystem& sys, const li::System& s, const VecXd& x) const;
         void build_target(IntegSystem& sys) const;   // F2, length, cutV of build_system
         // Size-field gradient of the naive integration (mtk_size_field_gradient); no counterpart
         // in the reference.  s: log-size per raw vertex; T: per-face loss target (8 per face) or
@@ -481,7 +488,73 @@ namespace metriko {
         d.nSingular = singularIdcs.size(); d.singularIdcs = singularIdcs.data();
         d.nInteger = integerIdcs.size(); d.integerIdcs = integerIdcs.data();
         d.seamless = seamless; d.roundSeams = roundSeams;
-        if (localInjectivity) throw std::invalid_argument("localInjectivity has no GPU solver (its barrier pieces are mtk_injective_barrier / mtk_local_injectivity)");
+    }
+
+    inline void RosyParameterization::li_system(const IntegSystem& sys, li::System& s) const {
+        s.N = N;
+        s.n = n;
+        s.nF = cut.nF;
+        s.nCut = cut.nV;
+        s.nfull = n * nR;
+        s.nZ = int(sys.USmall.cols());
+        s.nY = 0;
+        for (int v : sys.full2y) s.nY = std::max(s.nY, v + 1);
+        s.nred = s.nY + s.nZ;
+        s.length = sys.length;
+        s.F2 = sys.F2;
+        s.full2y = sys.full2y;
+        s.jslot.assign(s.nfull, -1);
+        for (size_t k = 0; k < sys.uniqueJ.size(); k++) s.jslot[sys.uniqueJ[k]] = int(k);
+        s.USmall = sys.USmall;
+        s.fullx2N = &sys.fullx2Nfunc;
+        s.cutF = cut.idx;
+        s.fixedIdcs.assign(fixedIdcs.begin(), fixedIdcs.end());
+        s.fixedVals.assign(fixedVals.begin(), fixedVals.end());
+        s.singularIdcs.assign(singularIdcs.begin(), singularIdcs.end());
+        s.integerIdcs.assign(integerIdcs.begin(), integerIdcs.end());
+        s.roundSeams = roundSeams;
+        li::build_gradients(s, cut.pos, raw.faceNormal, raw.faceBasisX, raw.faceBasisY, raw.faceArea);
+    }
+
+    inline std::vector<double> RosyParameterization::to_reduced(const IntegSystem& sys, const li::System& s,
+                                                                const VecXd& x) const {
+        std::vector<double> xs(s.nred, 0.0);
+        for (int i = 0; i < s.nfull; i++) if (s.full2y[i] >= 0) xs[s.full2y[i]] = x[i];
+        const int nJ = int(sys.uniqueJ.size()), nZ = s.nZ;
+        if (nZ == 0) return xs;
+        // normal equations of USmall z = x_J (nZ x nZ, Cholesky)
+        MatXd A(nZ, nZ, 0.0);
+        std::vector<double> b(nZ, 0.0);
+        for (int r = 0; r < nJ; r++) {
+            const double xj = x[sys.uniqueJ[r]];
+            for (int a = 0; a < nZ; a++) {
+                b[a] += sys.USmall(r, a) * xj;
+                for (int c = 0; c < nZ; c++) A(a, c) += sys.USmall(r, a) * sys.USmall(r, c);
+            }
+        }
+        for (int j = 0; j < nZ; j++) {
+            double d = A(j, j);
+            for (int k = 0; k < j; k++) d -= A(j, k) * A(j, k);
+            d = std::sqrt(d);
+            A(j, j) = d;
+            for (int i = j + 1; i < nZ; i++) {
+                double v = A(i, j);
+                for (int k = 0; k < j; k++) v -= A(i, k) * A(j, k);
+                A(i, j) = v / d;
+            }
+        }
+        for (int i = 0; i < nZ; i++) {
+            double v = b[i];
+            for (int k = 0; k < i; k++) v -= A(i, k) * b[k];
+            b[i] = v / A(i, i);
+        }
+        for (int i = nZ - 1; i >= 0; i--) {
+            double v = b[i];
+            for (int k = i + 1; k < nZ; k++) v -= A(k, i) * b[k];
+            b[i] = v / A(i, i);
+        }
+        for (int z = 0; z < nZ; z++) xs[s.nY + z] = b[z];
+        return xs;
     }
 
     inline void RosyParameterization::build_target(IntegSystem& sys) const {
@@ -565,7 +638,51 @@ namespace metriko {
             fprintf(stderr, "[host] %-22s %8.1f ms\n", "integ build_system",
                     std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
         const SprsD& fullx2Nfunc = sys.fullx2Nfunc;
-        bool success = iterative_rounding(sys.desc, fullx, naivex, fixOrder, fixVals);
+        bool success = true;
+        if (!localInjectivity) {
+            success = iterative_rounding(sys.desc, fullx, naivex, fixOrder, fixVals);
+        } else {
+            // the naive integration on the device, then the damped LM path (li::iterative_rounding)
+            // with its linear solves on the device (mtk_csr_pcg, FP64) and the orientation check
+            // of the map by mtk_local_injectivity
+            mtk_igm_desc nd = sys.desc;
+            nd.seamless = 0;
+            std::vector<int> fo, fv;
+            VecXd nx;
+            iterative_rounding(nd, naivex, nx, fo, fv);
+            li::System ls;
+            li_system(sys, ls);
+            const std::vector<double> xs0 = to_reduced(sys, ls, naivex);
+            li::Solve solve = [](const SprsD& S, const std::vector<double>& b, std::vector<double>& x) {
+                mtk_csr* A = nullptr;
+                if (mtk_csr_create(gpu::context(), S.nr, S.ptr.data(), S.idx.data(), S.val.data(), 0, &A) != MTK_OK) return false;
+                x.assign(S.nr, 0.0);
+                mtk_solve_opts o = gpu::options().solve;
+                o.precision = MTK_PREC_FP64;
+                o.tol = 1e-13;
+                o.max_iter = std::max(o.max_iter, 20 * S.nr + 1000);
+                const int st = mtk_csr_pcg(gpu::context(), A, 1, b.data(), x.data(), &o, nullptr);
+                mtk_csr_destroy(A);
+                return st == MTK_OK;
+            };
+            auto injective = [this, &ls, &fullx2Nfunc](const std::vector<double>& xs) {
+                const std::vector<double> X = ls.ufull_times(xs);
+                const std::vector<double> NF = fullx2Nfunc * X;
+                std::vector<double> cfn_(12 * size_t(cut.nF));
+                for (int f = 0; f < cut.nF; f++)
+                    for (int j = 0; j < 3; j++)
+                        for (int k = 0; k < N; k++) cfn_[3 * size_t(N) * f + N * j + k] = NF[N * size_t(cut.idx(f, j)) + k];
+                int flipped = 0;
+                gpu::check(mtk_local_injectivity(gpu::context(), cut.nF, N, cfn_.data(), &flipped, nullptr),
+                           "mtk_local_injectivity");
+                return flipped == 0;
+            };
+            li::Result r = li::iterative_rounding(ls, xs0, seamless, solve, injective);
+            success = r.success;
+            fullx = VecXd(r.fullx);
+            fixOrder = r.fixOrder;
+            fixVals = r.fixVals;
+        }
 
         // ---- nfn (cut vertex x N) and cfn (face x 3N)  (integ.ipp:88-98)
         std::vector<double> NF = fullx2Nfunc * fullx.d;

@@ -203,6 +203,8 @@ typedef struct {
     int32_t seamless;           /* RosyParameterization::seamless                         */
     int32_t stop_after;         /* 0 = full path, 1 = after field+matching, 2 = after setup */
     int32_t field_type;         /* 0 = FieldType::Smoothest, 1 = FieldType::CurvatureAligned */
+    int32_t local_injectivity;  /* RosyParameterization::localInjectivity (damped LM with the
+                                   injective barrier; its linear solves on the device)      */
 } mtk_pipeline_opts;
 
 int mtk_pipeline_run(mtk_ctx* ctx, int32_t nV, int32_t nF, const double* V, const int32_t* F,

@@ -61,7 +61,7 @@ class Stats(C.Structure):
 class PipelineOpts(C.Structure):
     _fields_ = [("seed", C.c_int32), ("n_iter", C.c_int32), ("ratio", C.c_double),
                 ("round_seams", C.c_int32), ("seamless", C.c_int32), ("stop_after", C.c_int32),
-                ("field_type", C.c_int32)]
+                ("field_type", C.c_int32), ("local_injectivity", C.c_int32)]
 
 
 _lib = None
@@ -220,7 +220,7 @@ def field_smoothest(ctx: Context, nbr, theta, area, x0, n_rosy=4, n_iter=50, opt
 
 
 def pipeline(ctx: Context, V, F, ratio=0.02, seed=0, round_seams=False, seamless=True, n_iter=50,
-             opts=None, stop_after=0, check=True, field_type="smoothest"):
+             opts=None, stop_after=0, check=True, field_type="smoothest", local_injectivity=False):
     """mtk_pipeline_run: Hmesh -> smoothest field -> Curl matching -> seams -> cut mesh ->
     combing -> RosyParameterization setup()/integ() (example_igm.cpp:13-31)."""
     V = np.ascontiguousarray(V, np.float64)
@@ -242,7 +242,7 @@ def pipeline(ctx: Context, V, F, ratio=0.02, seed=0, round_seams=False, seamless
     n_full = C.c_int32(0)
     n_fixed = C.c_int32(0)
     p = PipelineOpts(seed, n_iter, ratio, int(round_seams), int(seamless), stop_after,
-                     {"smoothest": 0, "curvature_aligned": 1}[field_type])
+                     {"smoothest": 0, "curvature_aligned": 1}[field_type], int(local_injectivity))
     o = opts or solve_opts()
     st = Stats()
     status = lib().mtk_pipeline_run(ctx.handle, nV, nF, _ptr(V), _ptr(F), C.byref(p), C.byref(o),
@@ -384,7 +384,7 @@ def size_field_gradient(ctx: Context, V, F, s, T=None, mu=0.0, ratio=0.02, seed=
     grad = np.zeros(nV)
     loss = C.c_double(0)
     n_full = C.c_int32(0)
-    p = PipelineOpts(seed, n_iter, ratio, int(round_seams), 0, 0, 0)
+    p = PipelineOpts(seed, n_iter, ratio, int(round_seams), 0, 0, 0, 0)
     o = opts or solve_opts()
     st = Stats()
     _check(lib().mtk_pipeline_size_field_gradient(ctx.handle, nV, nF, _ptr(V), _ptr(F), C.byref(p), C.byref(o), _ptr(s),
@@ -409,7 +409,7 @@ def position_gradient(ctx: Context, V, F, s, mu=0.0, ratio=0.02, seed=0, round_s
     grad_V = np.zeros((nV, 3))
     loss = C.c_double(0)
     n_full = C.c_int32(0)
-    p = PipelineOpts(seed, n_iter, ratio, int(round_seams), 0, 0, 0)
+    p = PipelineOpts(seed, n_iter, ratio, int(round_seams), 0, 0, 0, 0)
     o = opts or solve_opts()
     st = Stats()
     _check(lib().mtk_pipeline_position_gradient(ctx.handle, nV, nF, _ptr(V), _ptr(F), C.byref(p), C.byref(o), _ptr(s),

@@ -134,7 +134,7 @@ extern "C" int mtk_pipeline_run(mtk_ctx* ctx, int32_t nV, int32_t nF, const doub
         stamp("cut mesh+combing+extr", ts2);
         RosyParameterization rp(*mesh, *cutm, extf, cmbf->singular, cmbf->matching, seam, 4, popts->ratio);
         rp.seamless = popts->seamless != 0;
-        rp.localInjectivity = false;
+        rp.localInjectivity = popts->local_injectivity != 0;
         rp.roundSeams = popts->round_seams != 0;
         rp.verbose = false;
         stamp("transitions", ts2);

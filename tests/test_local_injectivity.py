@@ -1,0 +1,88 @@
+"""The localInjectivity rounding path of the header-only host API (li::iterative_rounding:
+NaiveIntegration's damped LM with the injective barrier and its stop at the first locally
+injective map, then the greedy rounding with one damped LM per rounded variable) against the
+oracle's restatement of the reference (pipeline(..., local_injectivity=True)), on the CPU: the
+linear solves by host Jacobi-preconditioned CG (tests/cpp/li_harness.cpp), the same method the
+product runs on the device (mtk_csr_pcg).  Integer decisions identical, uv within 1e-6 of the
+uv bounding-box diagonal (1e-3 where the rounding fails its integrality check)."""
+import shutil
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import metriko_gb300 as M
+from metriko_gb300 import meshgen
+from oracle import metriko_oracle as O
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+@pytest.fixture(scope="module")
+def harness(tmp_path_factory):
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not found")
+    M.lib()
+    lib = ROOT / "metriko_gb300" / "libmetriko_cuda.so"
+    exe = tmp_path_factory.mktemp("cpp") / "li_harness"
+    cuda_inc = Path(shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc").resolve().parent.parent / "include"
+    cmd = ["g++", "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-I", str(ROOT / "include"),
+           "-I", str(cuda_inc), str(ROOT / "tests" / "cpp" / "li_harness.cpp"), "-o", str(exe), str(lib),
+           "-Wl,-rpath," + str(lib.parent)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    return exe
+
+
+def run_harness(exe, tmp, V, F, ratio, rs, compressed, x0):
+    blob, outp = tmp / "in.bin", tmp / "out.bin"
+    with open(blob, "wb") as fh:
+        fh.write(np.array([len(V), len(F)], np.int32).tobytes())
+        fh.write(np.array([ratio], np.float64).tobytes())
+        fh.write(np.array([int(rs)], np.int32).tobytes())
+        fh.write(np.ascontiguousarray(V, np.float64).tobytes())
+        fh.write(np.ascontiguousarray(F, np.int32).tobytes())
+        fh.write(np.stack([compressed.real, compressed.imag], 1).astype(np.float64).tobytes())
+        fh.write(np.array([len(x0)], np.int32).tobytes())
+        fh.write(np.ascontiguousarray(x0, np.float64).tobytes())
+    r = subprocess.run([str(exe), str(blob), str(outp)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, (r.returncode, r.stderr[-2000:])
+    b = outp.read_bytes()
+    ok, nfix = np.frombuffer(b[:8], np.int32)
+    o = 8
+    fo = np.frombuffer(b[o:o + 4 * nfix], np.int32); o += 4 * nfix
+    fv = np.frombuffer(b[o:o + 4 * nfix], np.int32); o += 4 * nfix
+    nf = int(np.frombuffer(b[o:o + 4], np.int32)[0]); o += 4
+    fullx = np.frombuffer(b[o:o + 8 * nf], np.float64); o += 8 * nf
+    x_ni = np.frombuffer(b[o:o + 8 * nf], np.float64); o += 8 * nf
+    ni_it, resolves = np.frombuffer(b[o:o + 8], np.int32)
+    return dict(success=bool(ok), fix_order=fo, fix_vals=fv, fullx=fullx, x_ni=x_ni, ni_iterations=int(ni_it),
+                resolves=int(resolves))
+
+
+# the workloads' own grid ratios (the barrier inactive: the same result as the plain path) and
+# coarse grids where the barrier and the damping decide the result (different fixing orders
+# from the plain path, and the reference's rounding fails its integrality check on several)
+CASES = [("ico2_noise", None), ("ico3_noise", None), ("ico3_noise", 0.15), ("cap3_noise", None),
+         ("ico2_noise", 0.3), ("ico2_noise", 0.6), ("ico3_noise", 0.3), ("cap3_noise", 0.6), ("torus_32x16", 0.3)]
+
+
+@pytest.mark.parametrize("name,ratio", CASES)
+def test_host_local_injectivity_path_matches_oracle(harness, tmp_path, name, ratio):
+    V, F, r0, rs = meshgen.workload(name)
+    ratio = r0 if ratio is None else ratio
+    ref = O.pipeline(V, F, ratio=ratio, round_seams=rs, local_injectivity=True)
+    res = run_harness(harness, tmp_path, V, F, ratio, rs, np.asarray(ref["compressed"], complex), ref["info"]["x0"])
+    assert res["success"] == bool(ref["success"])
+    assert list(res["fix_order"]) == list(ref["info"]["fix_order"])
+    assert list(res["fix_vals"]) == list(ref["info"]["fix_vals"])
+    assert res["resolves"] == int(ref["info"]["resolves"])
+    diag = max(np.ptp(ref["fullx"]), 1.0) * np.sqrt(2.0)
+    assert np.abs(res["x_ni"] - ref["info"]["x_ni_lm"]).max() <= 1e-6 * diag
+    # A rounding that fails its integrality check returns the last iterate of a damped LM that
+    # did not reach the lattice (100 iterations, damping still moving); there the iterative and
+    # the direct solves part by 1e-4 of the diagonal (ico2_noise at 0.6, torus_32x16 at 0.3),
+    # while the integer decisions above stay identical.
+    tol = 1e-6 if ref["success"] else 1e-3
+    assert np.abs(res["fullx"] - ref["fullx"]).max() <= tol * diag
