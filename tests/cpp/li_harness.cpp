@@ -4,7 +4,8 @@
 // linear solves by Jacobi-preconditioned CG on the host (the same method as the device
 // mtk_csr_pcg the product calls) and the orientation check on the host.
 // Input (binary): nV, nF (int32), ratio (double), round_seams (int32), V, F, compressed (nF complex),
-// x0 (nFull doubles, preceded by nFull as int32).  Output (binary, argv[2]): success, n_fix,
+// x0 (nFull doubles, preceded by nFull as int32).  Like the product's solves, the CG stops on its
+// recurrence (relative residual 1e-13) and fails at its iteration cap or on a breakdown.  Output (binary, argv[2]): success, n_fix,
 // fix_order[n_fix], fix_vals[n_fix] (int32), nFull (int32), fullx (doubles), x_ni (doubles),
 // ni_iterations, resolves (int32).
 #include <cmath>
@@ -27,7 +28,8 @@ static bool pcg(const SprsD& A, const std::vector<double>& b, std::vector<double
     double bb = 0, rz = 0;
     for (int i = 0; i < n; i++) { bb += b[i] * b[i]; z[i] = dinv[i] * r[i]; p[i] = z[i]; rz += r[i] * z[i]; }
     if (bb == 0) return true;
-    for (int it = 0; it < 200000; it++) {
+    const int max_iter = 20 * n + 1000;   // the product's cap
+    for (int it = 0; it < max_iter; it++) {
         double pq = 0;
         for (int i = 0; i < n; i++) {
             double s = 0;
