@@ -187,7 +187,10 @@ int mtk_iterative_rounding(mtk_ctx* ctx, const mtk_igm_desc* desc, const mtk_sol
 
 /*
  * Whole path of example_igm.cpp with host buffers: V (nV*3), F (nF*3), N = 4, Smoothest
- * field, Curl matching, seamless = 1, localInjectivity = 0.  Outputs (caller-allocated,
+ * field, Curl matching, seamless = 1, localInjectivity = 0 unless popts->local_injectivity
+ * (then the reference's damped LM with the injective barrier on the host, each of its linear
+ * solves by mtk_csr_pcg and each orientation check by mtk_local_injectivity; MTK_ERR_ROUNDING
+ * where its rounding fails the integrality check).  Outputs (caller-allocated,
  * may be NULL unless noted):
  *   singular[nV], matching[nE] (combed), seam[nE] (0/1), compressed[2*nF]
  *   cfn[nF*3*N]       corner parameterisation (row f: corner j, function k at N*j + k)
