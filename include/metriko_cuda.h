@@ -245,10 +245,10 @@ int mtk_topology_from_field(int32_t nV, int32_t nF, const double* V, const int32
  *   Working memory is a 64 MiB static device array inside the library (held by every GPU that
  *   loads the library until exit), which limits nF to 409600; larger nF -> MTK_ERR_BAD_INPUT.
  *   The first call on a device looks the array up (cudaGetSymbolAddress) and keeps its address
- *   for the life of the process: make that first call before any stream capture, and make no
- *   call on a device after cudaDeviceReset().  All calls share the array: calls that overlap on
- *   the GPU race.  *iterations (may be NULL) receives the total PCG iterations.  The call reads
- *   its status back and waits for `stream` before it returns.
+ *   for the life of the process; make no call on a device after cudaDeviceReset().  All calls
+ *   share the array: calls that overlap on the GPU race.  *iterations (may be NULL) receives the
+ *   total PCG iterations.  The call reads its status back and waits for `stream` before it
+ *   returns, so no call can be captured into a CUDA graph (call it outside any capture).
  */
 int mtk_field_smoothest_noalloc(int32_t nF, int32_t nRosy, const int32_t* nbr, const double* theta,
                                 const double* area, const double* x0, int32_t n_iter, double tol,

@@ -9,8 +9,8 @@
 // The array (kScratchBytes = 64 MiB) is part of the library image: every GPU that loads the
 // library holds it until the process exits.  It bounds the problem size to kMaxFaces faces.
 // The first call on a device looks the array's device address up with cudaGetSymbolAddress
-// (host code cannot use the symbol itself: in host code it names a host-side stand-in), so
-// that first call should come before any stream capture.  The address is kept for the life of
+// (host code cannot use the symbol itself: in host code it names a host-side stand-in).  No
+// call can be captured into a CUDA graph: each one synchronizes its stream.  The address is kept for the life of
 // the process; a cudaDeviceReset() unloads the module, and the entry point must not be called
 // on that device after one.  Every call shares the array, which keeps the last call's
 // contents: the barrier words, the error flag and the status word are cleared at the start of
