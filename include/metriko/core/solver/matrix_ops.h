@@ -1,4 +1,9 @@
 //
+// Restates parts of metriko (https://github.com/komietty/metriko),
+// Copyright (C) 2025 Saki Komikado <komietty@gmail.com>, and the published algorithm of Eigen's
+// FullPivLU::kernel().  This Source Code Form is subject to the terms of the Mozilla Public
+// License v.2.0 (https://mozilla.org/MPL/2.0/).
+//
 // metriko-gb300: small dense helpers of the constraint reduction.
 //
 // reduce_to_linearly_independent replaces metriko include/metriko/core/solver/matrix_ops.h:12-28.
