@@ -117,9 +117,11 @@ extern "C" int mtk_ctx_set_wait_limit(mtk_ctx* c, int64_t polls) {
 
 // splitmix64 over (seed, 2f) and (seed, 2f+1), mapped to [-1, 1).  Replaces the
 // std::rand-based VecXc::Random start of solveSmallestEig (sparse_linear_solver.h:32) with a
-// reproducible vector that the CPU oracle regenerates bit-for-bit.
+// reproducible vector that the CPU oracle regenerates bit-for-bit.  Every entry depends only on
+// its index, so the host threads split the range.
 extern "C" void mtk_seeded_init(int32_t n, int32_t seed, double* out) {
     const uint64_t G = 0x9E3779B97F4A7C15ULL;
+#pragma omp parallel for schedule(static) if (n > 65536)
     for (int64_t i = 0; i < 2 * (int64_t)n; i++) {
         uint64_t z = (uint64_t)(uint32_t)seed * G + (uint64_t)(i + 1) * G;
         z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
