@@ -136,6 +136,9 @@ namespace metriko {
         MatXd nfn;
         MatXd cfn;
         double deviation = 0;   // map_deviation of the result (computed by integ())
+        // When set (nF x 3N doubles, row-major), integ() writes the corner values there instead
+        // of into cfn, which then stays empty: a caller's output buffer, filled without a copy
+        double* cfn_target = nullptr;
         std::vector<int> fixOrder, fixVals;   // greedy rounding order (diagnostics)
         bool verbose = false;
         bool seamless = false;
@@ -397,7 +400,7 @@ namespace metriko {
     // faces and functions of |normalized(ext_k) - normalized(grad_k)|.  cfn: nF x 3N, the value
     // of function k at corner j in column N j + k.  Per-face sums in parallel, their total in
     // face order.
-    inline double map_deviation(const MatXd& cutV, const MatXi& cutF, const MatXd& cfn, const MatXd& ext, int N) {
+    inline double map_deviation(const MatXd& cutV, const MatXi& cutF, const double* cfn, const MatXd& ext, int N) {
         const int nF = cutF.rows();
         if (nF == 0 || N <= 0) return 0;
         std::vector<double> part(nF);
@@ -411,9 +414,10 @@ namespace metriko {
             for (int j = 0; j < 3; j++) g[j] = nu.cross(p[(j + 2) % 3] - p[(j + 1) % 3]) / a2;
             double s = 0;
             for (int k = 0; k < N; k++) {
-                Row3d grad = g[0] * cfn(f, k);
-                grad = grad + g[1] * cfn(f, N + k);
-                grad = grad + g[2] * cfn(f, 2 * N + k);
+                const double* c = cfn + 3 * size_t(N) * f;
+                Row3d grad = g[0] * c[k];
+                grad = grad + g[1] * c[N + k];
+                grad = grad + g[2] * c[2 * N + k];
                 const Row3d e{ext(f, 3 * k), ext(f, 3 * k + 1), ext(f, 3 * k + 2)};
                 s += (e.normalized() - grad.normalized()).norm();
             }
@@ -422,6 +426,9 @@ namespace metriko {
         double sum = 0;
         for (double v : part) sum += v;
         return sum / (double(nF) * N);
+    }
+    inline double map_deviation(const MatXd& cutV, const MatXi& cutF, const MatXd& cfn, const MatXd& ext, int N) {
+        return map_deviation(cutV, cutF, cfn.data(), ext, N);
     }
 
     inline void RosyParameterization::build_system(IntegSystem& sys) {
@@ -706,13 +713,14 @@ namespace metriko {
         nfn = MatXd(cut.nV, N);
         METRIKO_PARALLEL_FOR
         for (int i = 0; i < cut.nV; i++) for (int k = 0; k < N; k++) nfn(i, k) = NF[N * size_t(i) + k];
-        cfn = MatXd(raw.nF, 3 * N);
+        if (!cfn_target) cfn = MatXd(raw.nF, 3 * N);
+        double* cf = cfn_target ? cfn_target : cfn.data();
         METRIKO_PARALLEL_FOR
         for (int f = 0; f < raw.nF; f++)
             for (int j = 0; j < 3; j++)
-                for (int k = 0; k < N; k++) cfn(f, N * j + k) = nfn(cut.idx(f, j), k);
+                for (int k = 0; k < N; k++) cf[3 * size_t(N) * f + N * j + k] = NF[N * size_t(cut.idx(f, j)) + k];
         // ---- how close the map's gradients are to the field (integ.ipp:100-117)
-        deviation = map_deviation(cut.pos, cut.idx, cfn, ext, N);
+        deviation = map_deviation(cut.pos, cut.idx, cf, ext, N);
         if (verbose || (getenv("MTK_DEBUG") && getenv("MTK_DEBUG")[0] == '1'))
             fprintf(stderr, "Deviation of the recovered tf from the original : %.9g\n", deviation);
         return success;

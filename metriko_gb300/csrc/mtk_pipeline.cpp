@@ -152,6 +152,7 @@ extern "C" int mtk_pipeline_run(mtk_ctx* ctx, int32_t nV, int32_t nF, const doub
             if (stats) { *stats = gpu::stats(); stats->ms_host = host_ms; stats->ms_total = std::chrono::duration<double, std::milli>(clk::now() - t0).count(); }
             return MTK_OK;
         }
+        rp.cfn_target = cfn_out;   // the corner values straight into the caller's buffer
         bool ok = rp.integ();
         stamp("integ (host+gpu)", ts2);
         const int nFull = rp.fullx.size();
@@ -165,7 +166,7 @@ extern "C" int mtk_pipeline_run(mtk_ctx* ctx, int32_t nV, int32_t nF, const doub
             if (fix_order) fix_order[i] = rp.fixOrder[i];
             if (fix_vals) fix_vals[i] = rp.fixVals[i];
         }
-        if (cfn_out) std::memcpy(cfn_out, rp.cfn.data(), sizeof(double) * size_t(nF) * 12);
+
         if (stats) {
             *stats = gpu::stats();
             stats->ms_total = std::chrono::duration<double, std::milli>(clk::now() - t0).count();
