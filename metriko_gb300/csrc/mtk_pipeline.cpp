@@ -58,10 +58,12 @@ extern "C" int mtk_pipeline_run(mtk_ctx* ctx, int32_t nV, int32_t nF, const doub
     gpu::options().n_iter = popts->n_iter > 0 ? popts->n_iter : 50;
     try {
         auto ts = clk::now();
-        MatXd V(nV, 3);
-        MatXi F(nF, 3);
-        std::memcpy(V.data(), Vb, sizeof(double) * 3 * size_t(nV));
-        std::memcpy(F.data(), Fb, sizeof(int32_t) * 3 * size_t(nF));
+        auto host_mesh_input = [Vb, Fb, nV, nF] {
+            std::pair<MatXd, MatXi> vf{MatXd(nV, 3), MatXi(nF, 3)};
+            std::memcpy(vf.first.data(), Vb, sizeof(double) * 3 * size_t(nV));
+            std::memcpy(vf.second.data(), Fb, sizeof(int32_t) * 3 * size_t(nF));
+            return vf;
+        };
         const bool seams = popts->stop_after != 1;
         std::unique_ptr<Hmesh> mesh;
         std::unique_ptr<FaceRosyField> rawfp;
@@ -71,8 +73,9 @@ extern "C" int mtk_pipeline_run(mtk_ctx* ctx, int32_t nV, int32_t nF, const doub
             // computed on the device from V and F (mtk_field_smoothest_mesh), so a host thread
             // builds the whole halfedge mesh and the field-independent part of the seam search
             // while the GPU solves
-            auto built = std::async(std::launch::async, [&V, &F, seams] {
+            auto built = std::async(std::launch::async, [&host_mesh_input, seams] {
                 side_thread_cores(2);
+                const auto [V, F] = host_mesh_input();   // the host copy of V, F beside the solve
                 auto m = std::make_unique<Hmesh>(V, F, Hmesh::Deferred{});
                 m->finish();
                 SeamBase b = seams ? seam_base(*m) : SeamBase{};
@@ -95,7 +98,10 @@ extern "C" int mtk_pipeline_run(mtk_ctx* ctx, int32_t nV, int32_t nF, const doub
             lap(ts);
             stamp("field (gpu) + hmesh", ts2);
         } else {
-            mesh = std::make_unique<Hmesh>(V, F, Hmesh::Deferred{});
+            {
+                const auto [V, F] = host_mesh_input();
+                mesh = std::make_unique<Hmesh>(V, F, Hmesh::Deferred{});
+            }
             lap(ts);
             stamp("hmesh", ts2);
             // while the GPU solves the field, a host thread completes the mesh (element lists,
