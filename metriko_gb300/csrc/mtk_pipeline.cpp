@@ -85,9 +85,11 @@ extern "C" int mtk_pipeline_run(mtk_ctx* ctx, int32_t nV, int32_t nF, const doub
             mtk_seeded_init(nF, gpu::options().seed, x0.data());
             const int fs = mtk_field_smoothest_mesh(ctx, nV, nF, Vb, Fb, 4, x0.data(), gpu::options().n_iter,
                                                     &gpu::options().solve, cfield.data(), &gpu::stats());
+            stamp("field (gpu)", ts2);
             ts = clk::now();
             auto pr = built.get();   // a wait here (the mesh outlasting the field) is host time
             lap(ts);
+            stamp("hmesh join", ts2);
             gpu::check(fs, "mtk_field_smoothest_mesh");
             mesh = std::move(pr.first);
             base = std::move(pr.second);
@@ -96,7 +98,7 @@ extern "C" int mtk_pipeline_run(mtk_ctx* ctx, int32_t nV, int32_t nF, const doub
             for (int f = 0; f < nF; f++) rawfp->compressed[f] = complex(cfield[2 * f], cfield[2 * f + 1]);
             rawfp->set_field_from_compressed();
             lap(ts);
-            stamp("field (gpu) + hmesh", ts2);
+            stamp("field expansion", ts2);
         } else {
             {
                 const auto [V, F] = host_mesh_input();
