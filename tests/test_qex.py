@@ -20,6 +20,15 @@ from oracle import qex_oracle as Q
 ROOT = Path(__file__).resolve().parents[1]
 
 
+def load_workload(name):
+    """meshgen workloads, and icosphere_obj: the reference's own model (example/models/icosphere.obj)
+    as its golden fixture holds it."""
+    if name == "icosphere_obj":
+        g = np.load(ROOT / "tests" / "golden" / "icosphere_obj.npz")
+        return g["V"], g["F"], float(g["ratio"]), bool(g["round_seams"])
+    return meshgen.workload(name)
+
+
 @pytest.fixture(scope="module")
 def qex_harness(tmp_path_factory):
     if shutil.which("g++") is None:
@@ -93,12 +102,12 @@ def oracle_qex(out, F):
     return uv, q
 
 
-CASES = [("ico2_noise", 0.3), ("ico2_noise", None), ("ico3_noise", 0.15)]
+CASES = [("ico2_noise", 0.3), ("ico2_noise", None), ("ico3_noise", 0.15), ("icosphere_obj", 0.1)]
 
 
 @pytest.mark.parametrize("name,ratio", CASES)
 def test_qex_matches_oracle(qex_harness, tmp_path, name, ratio):
-    V, F, r0, rs = meshgen.workload(name)
+    V, F, r0, rs = load_workload(name)
     ratio = r0 if ratio is None else ratio
     out = O.pipeline(V, F, ratio=ratio, round_seams=False, seamless=True, local_injectivity=True)
     assert out["success"]

@@ -20,6 +20,15 @@ from oracle import tmesh_oracle as T
 ROOT = Path(__file__).resolve().parents[1]
 
 
+def load_workload(name):
+    """meshgen workloads, and icosphere_obj: the reference's own model (example/models/icosphere.obj)
+    as its golden fixture holds it."""
+    if name == "icosphere_obj":
+        g = np.load(ROOT / "tests" / "golden" / "icosphere_obj.npz")
+        return g["V"], g["F"], float(g["ratio"]), bool(g["round_seams"])
+    return meshgen.workload(name)
+
+
 @pytest.fixture(scope="module")
 def harness(tmp_path_factory):
     if shutil.which("g++") is None:
@@ -101,12 +110,12 @@ def oracle_graph(out, F):
 
 
 CASES = [("ico2_noise", False), ("ico3_noise", False), ("genus2_s3", False), ("ico2_noise", True),
-         ("ico3_noise", True)]
+         ("ico3_noise", True), ("icosphere_obj", False)]
 
 
 @pytest.mark.parametrize("name,seamless", CASES)
 def test_motorcycle_graph_and_tmesh_match_oracle(harness, tmp_path, name, seamless):
-    V, F, ratio, rs = meshgen.workload(name)
+    V, F, ratio, rs = load_workload(name)
     out = O.pipeline(V, F, ratio=ratio, round_seams=rs, seamless=seamless, local_injectivity=not seamless)
     uv, ports, curves, tm = oracle_graph(out, F)
     res = run_harness(harness, tmp_path, V, F, uv, out["combed_matching"], out["singular"])
