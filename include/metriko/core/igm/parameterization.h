@@ -665,29 +665,47 @@ namespace metriko {
             li::System ls;
             li_system(sys, ls);
             const std::vector<double> xs0 = to_reduced(sys, ls, naivex);
-            // The damped LM systems carry squared weights from 1e-4 to 1e10: a PCG whose
-            // recurrence reaches 1e-13 leaves a true relative residual of up to ~1e-4 there (the
-            // FP64 floor at that conditioning), which still gives the reference's decisions.  So a
-            // solve counts as done when the PCG stopped on its own test: NOT_CONVERGED from the
-            // final true-residual check only (the stats are written after the PCG's test passed;
-            // an exhausted cap returns before them).  A breakdown (the analogue of a failed
-            // factorization) or an exhausted cap fails it.
+            // The damped LM systems carry squared weights from 1e-4 to 1e10 and, near the barrier,
+            // rows that grow without bound: a PCG whose recurrence reaches 1e-13 can leave a true
+            // relative residual of up to ~1e-4 there, where the reference factorizes.  So each
+            // solve is refined three times in FP64 (the residual b - S x exact on the host, one
+            // more PCG for the correction), which brings it to round-off.  A PCG counts as done when it stopped on its own test: NOT_CONVERGED from the final
+            // true-residual check only (the stats are written after the PCG's test passed; an
+            // exhausted cap returns before them).  A breakdown (the analogue of a failed
+            // factorization) or an exhausted cap fails the first pass and ends the refinement.
             li::Solve solve = [](const SprsD& S, const std::vector<double>& b, std::vector<double>& x) {
                 mtk_csr* A = nullptr;
                 if (mtk_csr_create(gpu::context(), S.nr, S.ptr.data(), S.idx.data(), S.val.data(), 0, &A) != MTK_OK) return false;
-                x.assign(S.nr, 0.0);
                 mtk_solve_opts o = gpu::options().solve;
                 o.precision = MTK_PREC_FP64;
                 o.tol = 1e-13;
                 o.max_iter = std::max(o.max_iter, 20 * S.nr + 1000);
-                mtk_stats st{};
-                const int s = mtk_csr_pcg(gpu::context(), A, 1, b.data(), x.data(), &o, &st);
+                auto pcg = [&](const std::vector<double>& rhs, std::vector<double>& out) {
+                    out.assign(S.nr, 0.0);
+                    mtk_stats st{};
+                    const int s = mtk_csr_pcg(gpu::context(), A, 1, rhs.data(), out.data(), &o, &st);
+                    if (s == MTK_OK) return true;
+                    if (s != MTK_ERR_NOT_CONVERGED || st.solves == 0 || st.pcg_iters >= o.max_iter) return false;
+                    for (double v : out)
+                        if (!std::isfinite(v)) return false;
+                    return true;
+                };
+                bool ok = pcg(b, x);
+                if (ok) {
+                    std::vector<double> r(S.nr), e;
+                    for (int k = 0; k < 3; k++) {
+                        METRIKO_PARALLEL_FOR
+                        for (int i = 0; i < S.nr; i++) {
+                            double t = b[i];
+                            for (int q = S.ptr[i]; q < S.ptr[i + 1]; q++) t -= S.val[q] * x[S.idx[q]];
+                            r[i] = t;
+                        }
+                        if (!pcg(r, e)) break;
+                        for (int i = 0; i < S.nr; i++) x[i] += e[i];
+                    }
+                }
                 mtk_csr_destroy(A);
-                if (s == MTK_OK) return true;
-                if (s != MTK_ERR_NOT_CONVERGED || st.solves == 0 || st.pcg_iters >= o.max_iter) return false;
-                for (double v : x)
-                    if (!std::isfinite(v)) return false;
-                return true;
+                return ok;
             };
             auto injective = [this, &ls, &fullx2Nfunc](const std::vector<double>& xs) {
                 const std::vector<double> X = ls.ufull_times(xs);

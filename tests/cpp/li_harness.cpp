@@ -5,7 +5,8 @@
 // mtk_csr_pcg the product calls) and the orientation check on the host.
 // Input (binary): nV, nF (int32), ratio (double), round_seams (int32), V, F, compressed (nF complex),
 // x0 (nFull doubles, preceded by nFull as int32).  Like the product's solves, the CG stops on its
-// recurrence (relative residual 1e-13) and fails at its iteration cap or on a breakdown.  Output (binary, argv[2]): success, n_fix,
+// recurrence (relative residual 1e-13), fails at its iteration cap or on a breakdown, and each
+// solve is refined three times on the exact residual.  Output (binary, argv[2]): success, n_fix,
 // fix_order[n_fix], fix_vals[n_fix] (int32), nFull (int32), fullx (doubles), x_ni (doubles),
 // ni_iterations, resolves (int32).
 #include <cmath>
@@ -18,7 +19,7 @@
 
 using namespace metriko;
 
-static bool pcg(const SprsD& A, const std::vector<double>& b, std::vector<double>& x) {
+static bool pcg1(const SprsD& A, const std::vector<double>& b, std::vector<double>& x) {
     const int n = A.nr;
     x.assign(n, 0.0);
     std::vector<double> dinv(n, 0.0), r(b), z(n), p(n), q(n);
@@ -53,6 +54,22 @@ static bool pcg(const SprsD& A, const std::vector<double>& b, std::vector<double
         for (int i = 0; i < n; i++) p[i] = z[i] + beta * p[i];
     }
     return false;
+}
+
+// one pass and three FP64 refinements on the exact residual, as the product's solves
+static bool pcg(const SprsD& A, const std::vector<double>& b, std::vector<double>& x) {
+    if (!pcg1(A, b, x)) return false;
+    std::vector<double> r(A.nr), e;
+    for (int k = 0; k < 3; k++) {
+        for (int i = 0; i < A.nr; i++) {
+            double t = b[i];
+            for (int q = A.ptr[i]; q < A.ptr[i + 1]; q++) t -= A.val[q] * x[A.idx[q]];
+            r[i] = t;
+        }
+        if (!pcg1(A, r, e)) break;
+        for (int i = 0; i < A.nr; i++) x[i] += e[i];
+    }
+    return true;
 }
 
 int main(int argc, char** argv) {

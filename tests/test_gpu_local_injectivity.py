@@ -16,6 +16,8 @@ import metriko_gb300 as M
 from metriko_gb300 import meshgen
 from oracle import metriko_oracle as O
 
+from test_qex import load_workload
+
 pytestmark = pytest.mark.gpu
 ROUNDING = 7
 
@@ -23,12 +25,12 @@ ROUNDING = 7
 # active and the rounding still succeeds, and grids where the reference's rounding fails (the
 # level-4 sphere at its own ratio among them: 5,120 faces)
 CASES = [("ico2_noise", None), ("ico3_noise", 0.15), ("cap3_noise", None), ("ico2_noise", 0.3),
-         ("ico3_noise", 0.3), ("torus_32x16", 0.3), ("ico4_noise", None)]
+         ("ico3_noise", 0.3), ("torus_32x16", 0.3), ("ico4_noise", None), ("icosphere_obj", None)]
 
 
 @pytest.mark.parametrize("name,ratio", CASES)
 def test_pipeline_local_injectivity_matches_oracle(gpu_ctx, name, ratio):
-    V, F, r0, rs = meshgen.workload(name)
+    V, F, r0, rs = load_workload(name)
     ratio = r0 if ratio is None else ratio
     ref = O.pipeline(V, F, ratio=ratio, round_seams=rs, local_injectivity=True)
     r = M.pipeline(gpu_ctx, V, F, ratio=ratio, round_seams=rs, opts=M.solve_opts("mixed", tol=1e-10),

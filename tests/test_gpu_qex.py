@@ -6,17 +6,16 @@ import numpy as np
 import pytest
 
 import metriko_gb300 as M
-from metriko_gb300 import meshgen
 from oracle import metriko_oracle as O
 
-from test_qex import corner_uv, oracle_qex, qex_harness, run_qex_harness  # noqa: F401
+from test_qex import corner_uv, load_workload, oracle_qex, qex_harness, run_qex_harness  # noqa: F401
 
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("name,ratio", [("ico2_noise", None), ("ico3_noise", 0.15)])
+@pytest.mark.parametrize("name,ratio", [("ico2_noise", None), ("ico3_noise", 0.15), ("icosphere_obj", None)])
 def test_pipeline_qex_matches_oracle(gpu_ctx, qex_harness, tmp_path, name, ratio):  # noqa: F811
-    V, F, r0, rs = meshgen.workload(name)
+    V, F, r0, rs = load_workload(name)
     ratio = r0 if ratio is None else ratio
     ref = O.pipeline(V, F, ratio=ratio, round_seams=False, seamless=True, local_injectivity=True)
     _, q = oracle_qex(ref, F)

@@ -8,17 +8,16 @@ import numpy as np
 import pytest
 
 import metriko_gb300 as M
-from metriko_gb300 import meshgen
 from oracle import metriko_oracle as O
 
-from test_tmesh import _corner_uv, harness, oracle_graph, run_harness  # noqa: F401
+from test_tmesh import _corner_uv, harness, load_workload, oracle_graph, run_harness  # noqa: F401
 
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("name", ["ico3_noise", "genus2_s3"])
+@pytest.mark.parametrize("name", ["ico3_noise", "genus2_s3", "icosphere_obj"])
 def test_pipeline_motorcycle_graph_matches_oracle(gpu_ctx, harness, tmp_path, name):  # noqa: F811
-    V, F, ratio, rs = meshgen.workload(name)
+    V, F, ratio, rs = load_workload(name)
     ref = O.pipeline(V, F, ratio=ratio, round_seams=rs, seamless=False, local_injectivity=True)
     _, ports, curves, tm = oracle_graph(ref, F)
     r = M.pipeline(gpu_ctx, V, F, ratio=ratio, round_seams=rs, seamless=False, local_injectivity=True,

@@ -16,6 +16,8 @@ import metriko_gb300 as M
 from metriko_gb300 import meshgen
 from oracle import metriko_oracle as O
 
+from test_qex import load_workload
+
 ROOT = Path(__file__).resolve().parents[1]
 
 
@@ -65,12 +67,13 @@ def run_harness(exe, tmp, V, F, ratio, rs, compressed, x0):
 # coarse grids where the barrier and the damping decide the result (different fixing orders
 # from the plain path, and the reference's rounding fails its integrality check on several)
 CASES = [("ico2_noise", None), ("ico3_noise", None), ("ico3_noise", 0.15), ("cap3_noise", None),
-         ("ico2_noise", 0.3), ("ico2_noise", 0.6), ("ico3_noise", 0.3), ("cap3_noise", 0.6), ("torus_32x16", 0.3)]
+         ("ico2_noise", 0.3), ("ico2_noise", 0.6), ("ico3_noise", 0.3), ("cap3_noise", 0.6), ("torus_32x16", 0.3),
+         ("icosphere_obj", None)]
 
 
 @pytest.mark.parametrize("name,ratio", CASES)
 def test_host_local_injectivity_path_matches_oracle(harness, tmp_path, name, ratio):
-    V, F, r0, rs = meshgen.workload(name)
+    V, F, r0, rs = load_workload(name)
     ratio = r0 if ratio is None else ratio
     ref = O.pipeline(V, F, ratio=ratio, round_seams=rs, local_injectivity=True)
     res = run_harness(harness, tmp_path, V, F, ratio, rs, np.asarray(ref["compressed"], complex), ref["info"]["x0"])

@@ -102,7 +102,7 @@ def oracle_qex(out, F):
     return uv, q
 
 
-CASES = [("ico2_noise", 0.3), ("ico2_noise", None), ("ico3_noise", 0.15), ("icosphere_obj", 0.1)]
+CASES = [("ico2_noise", 0.3), ("ico2_noise", None), ("ico3_noise", 0.15), ("icosphere_obj", None)]
 
 
 @pytest.mark.parametrize("name,ratio", CASES)
